@@ -1,0 +1,183 @@
+/*
+ * gpr_gb300.h - C ABI of the GB300-native GPR (Godunov-Peshkov-Romenski)
+ * ADER-WENO time step.
+ *
+ * Every entry point takes plain device pointers (float64 / int32 / uint8
+ * arrays in the reference's cell-major layouts), sizes, a `gpr_par` by
+ * pointer (host memory) and a CUDA stream (`void*`, NULL = legacy default
+ * stream).  Work is enqueued on that stream; functions return 0 on success or
+ * a negative GPR_E_* code.  No entry point allocates device memory unless its
+ * comment says so; scratch buffers are passed in by the caller.
+ *
+ * Layouts (identical to the reference, code/cpp/src/etc/grid.cpp:129-130,
+ * solvers/weno/weno.cpp:83-124, solvers/fv/fv.cpp:7-9):
+ *   u   : [nx][ny][V]                 conserved state, V doubles per cell
+ *   ub  : [nx+2N][ny+2N][V]           state with N ghost cells per side
+ *   wh  : [nx+2][ny+2][N^d][V]        WENO reconstruction (x-node major)
+ *   qh  : [nx+2][ny+2][N][N^d][V]     space-time predictor (time-node major)
+ *   mask: [nx+2][ny+2] uint8          predictor/update mask
+ * with V = 14 + 3*THERMAL + LSET, N = 2 Gauss-Legendre nodes, d = 1 or 2
+ * (ny absent in 1D).  The variable order is
+ *   [rho, rho E, rho v(3), A (3x3 row-major), rho J (3, if THERMAL), phi (LSET)].
+ */
+#ifndef GPR_GB300_H
+#define GPR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+#define GPR_OK 0
+#define GPR_E_ARG (-1)        /* bad size, dimension, flag or pointer        */
+#define GPR_E_CUDA (-2)       /* a CUDA runtime call failed                  */
+#define GPR_E_UNSUPPORTED (-3) /* variant (N, V, flux) not compiled in       */
+#define GPR_E_TOO_LARGE (-4)  /* size beyond a stated fixed maximum          */
+
+/* Flux codes (code/cpp/src/solvers/fv/fluxes.h:7-9). */
+#define GPR_FLUX_RUSANOV 0
+#define GPR_FLUX_ROE 1
+#define GPR_FLUX_OSHER 2
+
+/* Boundary codes (code/cpp/src/etc/grid.cpp:5-10). */
+#define GPR_BC_TRANSMISSIVE 0
+#define GPR_BC_PERIODIC 1
+#define GPR_BC_SLIP 2
+#define GPR_BC_STICK 3
+#define GPR_BC_MOVING 4
+#define GPR_BC_SYMMETRIC 5
+
+/* Material flags. */
+#define GPR_SOLID 1
+#define GPR_POWER_LAW 2
+#define GPR_BINGHAM 4
+
+/* Predictor status codes written per cell (see gpr_predictor). */
+#define GPR_PRED_PICARD 0   /* Picard fixed point met the reference stopping rule */
+#define GPR_PRED_NEWTON 1   /* Picard failed; Newton met the tolerance            */
+#define GPR_PRED_FAILED 2   /* neither converged; best iterate written            */
+
+/* Material parameters: the fields of the reference's Par
+ * (code/cpp/src/system/objects.h:22-98) that the GPR step reads. */
+typedef struct gpr_par {
+  int32_t EOS;   /* 0 stiffened gas, 1 shock MG, 2 JWL, 3 Cochran-Chan, 4 GR */
+  int32_t flags; /* GPR_SOLID | GPR_POWER_LAW | GPR_BINGHAM                  */
+  double rho0, Tref, cv, pINF, Gamma0, c02, s, alpha, beta, gamma;
+  double A, B, R1, R2;
+  double b02, mu, tau0, sigmaY, n;
+  double calpha2, kappa;
+  double dp[3]; /* body force */
+} gpr_par;
+
+/* ------------------------------------------------------------------------ */
+/* Library information.                                                     */
+
+/* Returns the library version as an integer (major*10000+minor*100+patch). */
+int gpr_version(void);
+/* Writes the V values compiled in (up to `cap`) and returns how many. */
+int gpr_supported_nvars(int32_t *out, int cap);
+
+/* ------------------------------------------------------------------------ */
+/* Grid helpers.                                                            */
+
+/* Replaces GPRpy.boundaries (code/cpp/src/etc/grid.h:6, grid.cpp:147-170):
+ * fills ub (with N ghost cells per side) from u under the boundary codes
+ * bcs[2*ndim] (left, right per axis). */
+int gpr_boundaries(const double *u, double *ub, const int32_t *nX, int ndim,
+                   const int32_t *bcs, int nvar, void *stream);
+
+/* Replaces GPRpy.extend_mask (grid.h:10, grid.cpp:176-230). */
+int gpr_extend_mask(const uint8_t *mask, uint8_t *maskb, const int32_t *nX,
+                    int ndim, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Stages of the ADER-WENO step.                                            */
+
+/* Replaces GPRpy.solvers.weno.weno_launcher (solvers/weno/weno.h:6,
+ * weno.cpp:126-157): WENO reconstruction of ub into wh over the nx+2 (x ny+2)
+ * predictor cells. */
+int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX,
+                      int ndim, int nvar, void *stream);
+
+/* Replaces solvers.dg.predictor (solvers/dg/dg.h:7, dg1.cpp:75-131,
+ * dg2.cpp:102-171): local space-time Galerkin predictor of every masked cell.
+ * Picard iteration with the reference's initial guess, update and per-cell
+ * stopping rule; cells where Picard does not converge within its iteration
+ * cap (or produces NaN) are finished by a Newton solve of the same fixed
+ * point.  `status` (optional, one int32 per predictor cell) receives
+ * GPR_PRED_* in the low byte and the Picard iteration count << 8.
+ * stiff=1 skips Picard and goes straight to Newton (the reference's STIFF). */
+int gpr_predictor(double *qh, const double *wh, double dt, const double *dX,
+                  int ndim, const int32_t *nX, int stiff, const gpr_par *par,
+                  const uint8_t *mask, int32_t *status, int nvar,
+                  void *stream);
+
+/* Replaces solvers.fv.fv_launcher (solvers/fv/fv.h:17, fv.cpp:281-297):
+ * u += space-time quadrature of the non-conservative/source terms
+ * (SOURCES, TIME) and the path-conservative interface fluxes. */
+int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
+                    const double *dX, int ndim, int sources, int time_dg,
+                    int flux, const gpr_par *par, const uint8_t *mask,
+                    int nvar, void *stream);
+
+/* Replaces solvers.timestep (solvers/iterator.cpp:148-177) for one material:
+ * dt = CFL / max_cells sum_d max_abs_eigs/dx_d, x0.2 while count <= 5,
+ * clipped to tf - t.  The result is written to dt_out (device double).
+ * `scratch` must hold gpr_timestep_scratch_doubles(ncell) doubles. */
+int gpr_timestep_scratch_doubles(int64_t ncell);
+int gpr_timestep(const double *u, int64_t ncell, const double *dX, int ndim,
+                 double cfl, double t, double tf, int count,
+                 const gpr_par *par, double *dt_out, double *scratch,
+                 int nvar, void *stream);
+
+/* Replaces solvers.renorm_distortion (solvers/utils.cpp:6-23) for one
+ * material: A <- A * cbrt(rho / (rho0 det A)) where rho > 0. */
+int gpr_renorm_distortion(double *u, int64_t ncell, const gpr_par *par,
+                          int nvar, void *stream);
+
+/* Replaces solvers.split.ode_launcher (solvers/split/ode.cpp:5-11): the
+ * analytic stiff-source step (body force, distortion relaxation, thermal
+ * impulse relaxation) of every cell over dt. */
+int gpr_ode_launcher(double *u, int64_t ncell, double dt, const gpr_par *par,
+                     int nvar, void *stream);
+
+/* Replaces solvers.ader_stepper (solvers/steppers.cpp:10-22): one ADER-WENO
+ * step u <- u + (WENO -> predictor -> FV) of one material grid, with ub
+ * already filled by gpr_boundaries.  wh/qh are caller scratch of the sizes
+ * above; dt is a host value.  status as in gpr_predictor (optional). */
+int gpr_ader_stepper(double *u, const double *ub, const int32_t *nX, int ndim,
+                     double dt, const double *dX, int stiff, int flux,
+                     const gpr_par *par, const uint8_t *mask, double *wh,
+                     double *qh, int32_t *status, int nvar, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,
+ * eig.cpp): batched over `count` states Q[count][V].                        */
+
+/* out[count][V] += F_d(Q) (equations.cpp:11-48). */
+int gpr_flux(const double *Q, double *out, int64_t count, int d,
+             const gpr_par *par, int nvar, void *stream);
+/* out[count][V] = S(Q) (equations.cpp:50-67). */
+int gpr_source(const double *Q, double *out, int64_t count,
+               const gpr_par *par, int nvar, void *stream);
+/* out[count][V] = B_d(Q) x (equations.cpp:89-167). */
+int gpr_Bdot(const double *Q, const double *x, double *out, int64_t count,
+             int d, const gpr_par *par, int nvar, void *stream);
+/* out[count] = max |eigenvalue| of the GPR system in direction d
+ * (eig.cpp:66-77). */
+int gpr_max_abs_eigs(const double *Q, double *out, int64_t count, int d,
+                     const gpr_par *par, int nvar, void *stream);
+/* Interface dissipation / jump terms (solvers/fv/fluxes.cpp:9-75):
+ * out[count][V] = D_flux(qL, qR) including F(qL)+F(qR), and
+ * bout[count][V] = Bint(qL, qR). */
+int gpr_interface_terms(const double *qL, const double *qR, double *out,
+                        double *bout, int64_t count, int d, int flux,
+                        const gpr_par *par, int nvar, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPR_GB300_H */

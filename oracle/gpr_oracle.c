@@ -1,0 +1,2648 @@
+/*
+ * gpr_oracle.c - CPU ORACLE (test infrastructure, not product code).
+ *
+ * A plain-C restatement of the reference GPR ADER-WENO time step
+ * (haranjackson/phd, code/cpp/src), used by the tests, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * It follows the reference's algorithms and operation order function by
+ * function (each function cites the reference file:line it restates); it is
+ * never linked into, or called by, the CUDA library.
+ *
+ * Parity of this oracle against the compiled reference is pinned by the
+ * golden fixtures under tests/golden/ (generated from the reference's own
+ * C++ by tests/golden/make_golden.py).
+ *
+ * Runtime configuration: N (Gauss nodes / basis functions), THERMAL and LSET
+ * select V = 14 + 3*THERMAL + LSET as the reference's options.h:4-35 does at
+ * compile time.  VISCOUS is always on and MULTI always off.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/gpr_gb300.h"
+
+#define MAXN 4
+#define MAXV 18
+
+/* WENO and DG constants of options.h:24-31. */
+static const double LAMS = 1.0;
+static const double LAMC = 1e5;
+static const double WENO_EPS = 1e-14;
+static double DG_TOL = 6e-6;
+static int DG_IT = 50;
+
+static int N = 2, V = 17, THERMAL = 1, LSET = 0;
+static int FN2 = 0, CN2 = 1;
+
+static double NODES[MAXN], WGHTS[MAXN];
+static double ENDVALS[2][MAXN];
+static double DERVALS[MAXN][MAXN];
+static double mLinv[MAXN][MAXN], mRinv[MAXN][MAXN], mCLinv[MAXN][MAXN],
+    mCRinv[MAXN][MAXN];
+static double SIG[MAXN][MAXN];
+static double DG_DER[MAXN][MAXN], DG_MAT[MAXN][MAXN], DG_MATinv[MAXN][MAXN];
+
+/* ------------------------------------------------------------------------ */
+/* Polynomials in the monomial basis (restates scipy/poly.cpp:6-66).       */
+
+typedef struct {
+  int n;
+  double c[2 * MAXN + 2];
+} poly;
+
+static double poly_eval(const poly *p, double x) {
+  double r = 0.0;
+  for (int i = p->n - 1; i >= 0; i--)
+    r = r * x + p->c[i];
+  return r;
+}
+
+static poly poly_diff(const poly *p) {
+  poly r;
+  r.n = p->n > 1 ? p->n - 1 : 1;
+  r.c[0] = 0.0;
+  for (int i = 0; i < p->n - 1; i++)
+    r.c[i] = p->c[i + 1] * (i + 1);
+  return r;
+}
+
+static poly poly_int(const poly *p) {
+  poly r;
+  r.n = p->n + 1;
+  r.c[0] = 0.0;
+  for (int i = 1; i < r.n; i++)
+    r.c[i] = p->c[i - 1] / i;
+  return r;
+}
+
+static poly poly_mul(const poly *a, const poly *b) {
+  poly r;
+  r.n = a->n + b->n - 1;
+  for (int i = 0; i < r.n; i++)
+    r.c[i] = 0.0;
+  for (int i = 0; i < a->n; i++)
+    for (int j = 0; j < b->n; j++)
+      r.c[i + j] += a->c[i] * b->c[j];
+  return r;
+}
+
+static poly basis[MAXN];
+
+/* Gauss-Legendre nodes/weights on [0,1] (restates poly/basis.cpp:7-20 and
+ * scipy/legendre.cpp: leggauss): Newton iteration on P_N from the
+ * Chebyshev-like initial guesses, weights 2/((1-x^2) P_N'(x)^2). */
+static void gauss_legendre(int n, double *x, double *w) {
+  for (int i = 0; i < n; i++) {
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+    double pp = 0.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int k = 1; k <= n; k++) {
+        double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p2) / k;
+      }
+      pp = n * (z * p0 - p1) / (z * z - 1.0);
+      double dz = p0 / pp;
+      z -= dz;
+      if (fabs(dz) < 1e-16)
+        break;
+    }
+    /* ascending order on [-1,1] */
+    x[n - 1 - i] = z;
+    w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+  /* symmetrise as the reference does (legendre.cpp: w,x symmetrised) */
+  for (int i = 0; i < n / 2; i++) {
+    double xs = 0.5 * (x[n - 1 - i] - x[i]);
+    x[i] = -xs;
+    x[n - 1 - i] = xs;
+    double ws = 0.5 * (w[i] + w[n - 1 - i]);
+    w[i] = ws;
+    w[n - 1 - i] = ws;
+  }
+  if (n % 2)
+    x[n / 2] = 0.0;
+}
+
+static int invert(int n, double a_[MAXN][MAXN], double out[MAXN][MAXN]) {
+  double a[MAXN][2 * MAXN];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < 2 * n; j++)
+      a[i][j] = j < n ? a_[i][j] : (j - n == i ? 1.0 : 0.0);
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++)
+      if (fabs(a[r][c]) > fabs(a[p][c]))
+        p = r;
+    if (a[p][c] == 0.0)
+      return -1;
+    for (int j = 0; j < 2 * n; j++) {
+      double t = a[c][j];
+      a[c][j] = a[p][j];
+      a[p][j] = t;
+    }
+    double inv = 1.0 / a[c][c];
+    for (int j = 0; j < 2 * n; j++)
+      a[c][j] *= inv;
+    for (int r = 0; r < n; r++)
+      if (r != c) {
+        double f = a[r][c];
+        for (int j = 0; j < 2 * n; j++)
+          a[r][j] -= f * a[c][j];
+      }
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      out[i][j] = a[i][j + n];
+  return 0;
+}
+
+/* Builds every constant of etc/globals.cpp:16-50. */
+int or_configure(int n, int thermal, int lset, double dg_tol, int dg_it) {
+  if (n < 2 || n > MAXN || lset < 0 || lset > 1)
+    return -1;
+  N = n;
+  THERMAL = thermal ? 1 : 0;
+  LSET = lset;
+  V = 14 + 3 * THERMAL + LSET;
+  FN2 = (int)floor((N - 1) / 2.0);
+  CN2 = (int)ceil((N - 1) / 2.0);
+  DG_TOL = dg_tol > 0 ? dg_tol : 6e-6;
+  DG_IT = dg_it > 0 ? dg_it : 50;
+
+  double x[MAXN], w[MAXN];
+  gauss_legendre(N, x, w);
+  for (int i = 0; i < N; i++) {
+    NODES[i] = (x[i] + 1.0) / 2.0;
+    WGHTS[i] = w[i] / 2.0;
+  }
+  /* Lagrange basis on the scaled nodes (poly/basis.cpp:22-53) */
+  for (int i = 0; i < N; i++) {
+    poly p;
+    p.n = 1;
+    p.c[0] = 1.0;
+    for (int j = 0; j < N; j++) {
+      if (j == i)
+        continue;
+      poly f;
+      f.n = 2;
+      f.c[0] = -NODES[j];
+      f.c[1] = 1.0;
+      p = poly_mul(&p, &f);
+      for (int k = 0; k < p.n; k++)
+        p.c[k] /= (NODES[i] - NODES[j]);
+    }
+    basis[i] = p;
+  }
+  for (int j = 0; j < N; j++) {
+    ENDVALS[0][j] = poly_eval(&basis[j], 0.0);
+    ENDVALS[1][j] = poly_eval(&basis[j], 1.0);
+  }
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      poly d = poly_diff(&basis[j]);
+      DERVALS[i][j] = poly_eval(&d, NODES[i]);
+    }
+  /* WENO stencil matrices (weno/weno_matrices.cpp:9-28) */
+  double mL[MAXN][MAXN], mR[MAXN][MAXN], mCL[MAXN][MAXN], mCR[MAXN][MAXN];
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      poly P = poly_int(&basis[j]);
+      mL[i][j] = poly_eval(&P, i - N + 2) - poly_eval(&P, i - N + 1);
+      mR[i][j] = poly_eval(&P, i + 1) - poly_eval(&P, i);
+      mCL[i][j] = poly_eval(&P, i - CN2 + 1) - poly_eval(&P, i - CN2);
+      mCR[i][j] = poly_eval(&P, i - FN2 + 1) - poly_eval(&P, i - FN2);
+    }
+  invert(N, mL, mLinv);
+  invert(N, mR, mRinv);
+  invert(N, mCL, mCLinv);
+  invert(N, mCR, mCRinv);
+  /* oscillation indicator (weno_matrices.cpp:30-42) */
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      double s = 0.0;
+      poly di = basis[i], dj = basis[j];
+      for (int a = 1; a < N; a++) {
+        di = poly_diff(&di);
+        dj = poly_diff(&dj);
+        poly p = poly_mul(&di, &dj);
+        poly P = poly_int(&p);
+        s += poly_eval(&P, 1.0) - poly_eval(&P, 0.0);
+      }
+      SIG[i][j] = s;
+    }
+  /* DG matrices (dg/dg_matrices.cpp:29-53, etc/globals.cpp:42-44) */
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      double e = poly_eval(&basis[i], 1.0) * poly_eval(&basis[j], 1.0);
+      double dd;
+      if (i == j) {
+        double b1 = poly_eval(&basis[i], 1.0), b0 = poly_eval(&basis[i], 0.0);
+        dd = (b1 * b1 - b0 * b0) / 2;
+      } else {
+        poly d = poly_diff(&basis[j]);
+        dd = WGHTS[i] * poly_eval(&d, NODES[i]);
+      }
+      DG_DER[i][j] = dd;
+      (void)e;
+    }
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++)
+      DG_MAT[i][j] = poly_eval(&basis[i], 1.0) * poly_eval(&basis[j], 1.0) -
+                     DG_DER[j][i];
+  invert(N, DG_MAT, DG_MATinv);
+  return V;
+}
+
+int or_nvar(void) { return V; }
+
+/* Exposes the constants for the tests: NODES, WGHTS, ENDVALS, DERVALS,
+ * DG_DER, DG_MAT, SIG, mLinv, mRinv (each padded to MAXN x MAXN). */
+void or_constants(double *out) {
+  int k = 0;
+  for (int i = 0; i < MAXN; i++)
+    out[k++] = i < N ? NODES[i] : 0.0;
+  for (int i = 0; i < MAXN; i++)
+    out[k++] = i < N ? WGHTS[i] : 0.0;
+  for (int e = 0; e < 2; e++)
+    for (int i = 0; i < MAXN; i++)
+      out[k++] = i < N ? ENDVALS[e][i] : 0.0;
+  for (int i = 0; i < MAXN; i++)
+    for (int j = 0; j < MAXN; j++)
+      out[k++] = DERVALS[i][j];
+  for (int i = 0; i < MAXN; i++)
+    for (int j = 0; j < MAXN; j++)
+      out[k++] = DG_DER[i][j];
+  for (int i = 0; i < MAXN; i++)
+    for (int j = 0; j < MAXN; j++)
+      out[k++] = DG_MAT[i][j];
+  for (int i = 0; i < MAXN; i++)
+    for (int j = 0; j < MAXN; j++)
+      out[k++] = SIG[i][j];
+}
+
+/* ------------------------------------------------------------------------ */
+/* EOS (restates system/energy/mg.cpp:6-303).                              */
+
+static double Gamma_MG(double r, const gpr_par *P) {
+  switch (P->EOS) {
+  case 0:
+    return P->gamma - 1;
+  case 1:
+    return P->Gamma0 * P->rho0 / r;
+  case 4:
+    return P->gamma;
+  default:
+    return P->Gamma0;
+  }
+}
+
+static double p_ref(double r, const gpr_par *P) {
+  switch (P->EOS) {
+  case 0:
+    return -P->pINF;
+  case 1: {
+    if (r > P->rho0) {
+      double tmp = 1 / P->rho0 - P->s * (1 / P->rho0 - 1 / r);
+      return P->c02 * (1 / P->rho0 - 1 / r) / (tmp * tmp);
+    }
+    return P->c02 * (r - P->rho0);
+  }
+  case 4: {
+    double tmp = pow(r / P->rho0, P->alpha);
+    return P->c02 * r / P->alpha * (tmp - 1) * tmp;
+  }
+  case 2: {
+    double v_ = P->rho0 / r;
+    return P->A * exp(-P->R1 * v_) + P->B * exp(-P->R2 * v_);
+  }
+  default: {
+    double v_ = P->rho0 / r;
+    return P->A * pow(v_, -P->R1) - P->B * pow(v_, -P->R2);
+  }
+  }
+}
+
+static double e_ref(double r, const gpr_par *P) {
+  switch (P->EOS) {
+  case 0:
+    return P->pINF / r;
+  case 1:
+    if (r > P->rho0)
+      return 0.5 * p_ref(r, P) * (1 / P->rho0 - 1 / r);
+    return 0.0;
+  case 4: {
+    double tmp = pow(r / P->rho0, P->alpha);
+    return P->c02 / (2 * P->alpha * P->alpha) * (tmp - 1) * (tmp - 1);
+  }
+  case 2: {
+    double v_ = P->rho0 / r;
+    return P->A / (P->rho0 * P->R1) * exp(-P->R1 * v_) +
+           P->B / (P->rho0 * P->R2) * exp(-P->R2 * v_);
+  }
+  default: {
+    double v_ = P->rho0 / r;
+    return -P->A / (P->rho0 * (1 - P->R1)) * (pow(v_, 1 - P->R1) - 1) +
+           P->B / (P->rho0 * (1 - P->R2)) * (pow(v_, 1 - P->R2) - 1);
+  }
+  }
+}
+
+static double pressure_mg(double r, double e, const gpr_par *P) {
+  return (e - e_ref(r, P)) * r * Gamma_MG(r, P) + p_ref(r, P);
+}
+
+static double phi_mg(double r, const gpr_par *P) {
+  switch (P->EOS) {
+  case 0:
+    return pow(r / P->rho0, P->gamma - 1);
+  case 1:
+    return exp(P->Gamma0 * (1 - P->rho0 / r));
+  case 4:
+    return pow(r / P->rho0, P->gamma);
+  default:
+    return pow(r / P->rho0, P->Gamma0);
+  }
+}
+
+static double temperature_mg(double r, double p, const gpr_par *P) {
+  return phi_mg(r, P) * P->Tref +
+         (p - p_ref(r, P)) / (r * Gamma_MG(r, P) * P->cv);
+}
+
+static double dGamma_MG(double r, const gpr_par *P) {
+  if (P->EOS == 1)
+    return -P->Gamma0 * P->rho0 / (r * r);
+  return 0.0;
+}
+
+static double dp_ref(double r, const gpr_par *P) {
+  switch (P->EOS) {
+  case 0:
+    return 0.0;
+  case 1: {
+    if (r > P->rho0) {
+      double tmp = P->s * (r - P->rho0) - r;
+      return P->c02 * P->rho0 * P->rho0 * (P->s * (P->rho0 - r) - r) /
+             (tmp * tmp * tmp);
+    }
+    return P->c02;
+  }
+  case 4: {
+    double tmp = pow(r / P->rho0, P->alpha);
+    return P->c02 / P->alpha * tmp * ((1 + P->alpha) * (tmp - 1) + P->alpha * tmp);
+  }
+  case 2: {
+    double v_ = P->rho0 / r;
+    return v_ / r * (P->A * P->R1 * exp(-P->R1 * v_) + P->B * P->R2 * exp(-P->R2 * v_));
+  }
+  default: {
+    double v_ = P->rho0 / r;
+    return P->A * P->R1 / r * pow(v_, -P->R1) - P->B * P->R2 / r * pow(v_, -P->R2);
+  }
+  }
+}
+
+static double de_ref(double r, const gpr_par *P) {
+  if (P->EOS == 1) {
+    if (r > P->rho0) {
+      double tmp = P->s * (r - P->rho0) - r;
+      return -(r - P->rho0) * P->rho0 * P->c02 / (tmp * tmp * tmp);
+    }
+    return 0.0;
+  }
+  return p_ref(r, P) / (r * r);
+}
+
+static double dedrho(double r, double p, const gpr_par *P) {
+  double G = Gamma_MG(r, P), dG = dGamma_MG(r, P), pr = p_ref(r, P),
+         dpr = dp_ref(r, P), der = de_ref(r, P);
+  return der - (dpr * r * G + (G + r * dG) * (p - pr)) / ((r * G) * (r * G));
+}
+
+static double dedp(double r, const gpr_par *P) {
+  return 1 / (r * Gamma_MG(r, P));
+}
+
+static double dTdrho(double r, double p, const gpr_par *P) {
+  double G = Gamma_MG(r, P), dG = dGamma_MG(r, P), pr = p_ref(r, P),
+         dpr = dp_ref(r, P);
+  return -(dpr * r * G + (G + r * dG) * (p - pr)) / ((r * G) * (r * G)) / P->cv;
+}
+
+static double dTdp(double r, const gpr_par *P) { return dedp(r, P) / P->cv; }
+
+/* Shear wave quantities (system/waves/shear.cpp:6-41). */
+static double c_s2(double r, const gpr_par *P) {
+  return P->b02 * pow(r / P->rho0, P->beta);
+}
+static double dc_s2drho(double r, const gpr_par *P) {
+  return P->beta / r * c_s2(r, P);
+}
+static double C_0(double r, const gpr_par *P) {
+  return (1 - P->beta / Gamma_MG(r, P)) * c_s2(r, P);
+}
+static double dC_0drho(double r, const gpr_par *P) {
+  double cs2 = c_s2(r, P), dcs2 = dc_s2drho(r, P), G = Gamma_MG(r, P),
+         dG = dGamma_MG(r, P);
+  return (1 - P->beta / G) * dcs2 + P->beta / (G * G) * dG * cs2;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Matrix functions (system/functions/matrices.cpp:8-27).                  */
+
+/* A is row-major 3x3 at Q+5. */
+static void AdevG(const double *A, double *out) {
+  double G[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  double x = (G[0] + G[4] + G[8]) / 3;
+  G[0] -= x;
+  G[4] -= x;
+  G[8] -= x;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      out[3 * i + j] = A[3 * i] * G[j] + A[3 * i + 1] * G[3 + j] +
+                       A[3 * i + 2] * G[6 + j];
+}
+
+static double devGsq(const double *A) {
+  double G00 = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+  double G11 = A[3] * A[3] + A[4] * A[4] + A[5] * A[5];
+  double G22 = A[6] * A[6] + A[7] * A[7] + A[8] * A[8];
+  double G01 = A[0] * A[3] + A[1] * A[4] + A[2] * A[5];
+  double G02 = A[0] * A[6] + A[1] * A[7] + A[2] * A[8];
+  double G12 = A[3] * A[6] + A[4] * A[7] + A[5] * A[8];
+  double t = (G00 + G11 + G22) / 3;
+  return ((G00 - t) * (G00 - t) + (G11 - t) * (G11 - t) + (G22 - t) * (G22 - t) +
+          2 * (G01 * G01 + G02 * G02 + G12 * G12));
+}
+
+static double det3(const double *A) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+         A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* State variables (system/energy/eos.cpp, variables/state.cpp).           */
+
+static double E_2A(double r, const double *A, const gpr_par *P) {
+  return C_0(r, P) / 4 * devGsq(A);
+}
+
+static double internal_energy(const double *Q, const gpr_par *P) {
+  double r = Q[0];
+  double E = Q[1] / r;
+  double v0 = Q[2] / r, v1 = Q[3] / r, v2 = Q[4] / r;
+  double E1 = E - (v0 * v0 + v1 * v1 + v2 * v2) / 2;
+  E1 -= E_2A(r, Q + 5, P);
+  if (THERMAL) {
+    double J0 = Q[14] / r, J1 = Q[15] / r, J2 = Q[16] / r;
+    E1 -= P->calpha2 * (J0 * J0 + J1 * J1 + J2 * J2) / 2;
+  }
+  return E1;
+}
+
+double or_pressure(const double *Q, const gpr_par *P) {
+  return pressure_mg(Q[0], internal_energy(Q, P), P);
+}
+
+double or_temperature(const double *Q, const gpr_par *P) {
+  return temperature_mg(Q[0], or_pressure(Q, P), P);
+}
+
+/* dEdA_s = cs2 * AdevG(A) (energy/derivatives.cpp:73-79) */
+static void dEdA_s(const double *Q, const gpr_par *P, double *out) {
+  double cs2 = c_s2(Q[0], P);
+  AdevG(Q + 5, out);
+  for (int i = 0; i < 9; i++)
+    out[i] *= cs2;
+}
+
+/* sigma column d: -rho E_A^T A(:,d)   (variables/state.cpp:23-29) */
+static void sigma_d(const double *Q, const gpr_par *P, int d, double *out) {
+  double EA[9];
+  dEdA_s(Q, P, EA);
+  const double *A = Q + 5;
+  double r = Q[0];
+  for (int i = 0; i < 3; i++)
+    out[i] = -r * (EA[i] * A[d] + EA[3 + i] * A[3 + d] + EA[6 + i] * A[6 + d]);
+}
+
+static void sigma_full(const double *Q, const gpr_par *P, double *out) {
+  for (int d = 0; d < 3; d++) {
+    double c[3];
+    sigma_d(Q, P, d, c);
+    for (int i = 0; i < 3; i++)
+      out[3 * i + d] = c[i];
+  }
+}
+
+static void dsigmadrho(const double *Q, const gpr_par *P, int d, double *out) {
+  double r = Q[0];
+  double cs2 = c_s2(r, P), dcs2 = dc_s2drho(r, P);
+  sigma_d(Q, P, d, out);
+  double f = 1 / r + dcs2 / cs2;
+  for (int i = 0; i < 3; i++)
+    out[i] *= f;
+}
+
+/* dsigmadA (variables/state.cpp:43-56): -rho cs2 ret^T */
+static void dsigmadA(const double *Q, const gpr_par *P, int d, double *out) {
+  double r = Q[0];
+  double cs2 = c_s2(r, P);
+  const double *A = Q + 5;
+  double G[9], ret[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  AdevG(A, ret);
+  for (int i = 0; i < 3; i++)
+    ret[3 * i + d] *= 2.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      ret[3 * i + j] += 1.0 / 3.0 * A[3 * i + d] * G[3 * d + j];
+  for (int i = 0; i < 9; i++)
+    ret[i] += G[4 * d] * A[i];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      out[3 * i + j] = -r * cs2 * ret[3 * j + i];
+}
+
+static double sigma_norm(const double *s) {
+  double a = s[0] - s[4], b = s[4] - s[8], c = s[8] - s[0];
+  double t1 = a * a + b * b + c * c;
+  double t2 = s[1] * s[1] + s[5] * s[5] + s[6] * s[6];
+  return sqrt(0.5 * t1 + 3 * t2);
+}
+
+/* theta1inv (variables/sources.cpp:13-81) */
+static double theta1inv(const double *Q, const gpr_par *P) {
+  double r = Q[0];
+  double A53 = pow(det3(Q + 5), 5.0 / 3.0);
+  double cs2 = c_s2(r, P);
+  double n = P->n;
+  int SOLID = P->flags & GPR_SOLID, PL = P->flags & GPR_POWER_LAW,
+      BING = P->flags & GPR_BINGHAM;
+  if (SOLID) {
+    if (PL) {
+      double s[9];
+      sigma_full(Q, P, s);
+      double sn = sigma_norm(s);
+      sn = sn < 1e8 ? sn : 1e8;
+      return 3 * A53 / (cs2 * P->tau0) * pow(sn / P->sigmaY, n);
+    }
+    return 0.0;
+  } else if (BING) {
+    double s[9];
+    sigma_full(Q, P, s);
+    double nn = 0;
+    for (int i = 0; i < 9; i++)
+      nn += s[i] * s[i];
+    double sn = sqrt(nn) / sqrt(2.0);
+    if (sn > P->sigmaY)
+      return A53 * P->rho0 / (2 * P->mu) * (1.0 - P->sigmaY / sn);
+    return 0.0;
+  } else {
+    double c = A53 * P->rho0 / (2 * pow(P->mu, 1 / n));
+    if (PL) {
+      double s[9];
+      sigma_full(Q, P, s);
+      double nn = 0;
+      for (int i = 0; i < 9; i++)
+        nn += s[i] * s[i];
+      double sn = sqrt(nn) / sqrt(2.0);
+      return c * pow(sn, (1 - n) / n);
+    }
+    return c;
+  }
+}
+
+static double theta2inv(const double *Q, const gpr_par *P) {
+  return or_temperature(Q, P) / (P->kappa * Q[0]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* System (system/equations.cpp).                                          */
+
+/* ret += F_d(Q)   (equations.cpp:11-48) */
+void or_flux(const double *Q, int d, const gpr_par *P, double *ret) {
+  double r = Q[0];
+  double rE = Q[1];
+  const double *rv = Q + 2;
+  double p = or_pressure(Q, P);
+  double vd = rv[d] / r;
+  ret[0] += rv[d];
+  ret[1] += vd * (rE + p);
+  for (int i = 0; i < 3; i++)
+    ret[2 + i] += vd * rv[i];
+  ret[2 + d] += p;
+  {
+    const double *A = Q + 5;
+    double sd[3];
+    sigma_d(Q, P, d, sd);
+    ret[1] -= (sd[0] * rv[0] + sd[1] * rv[1] + sd[2] * rv[2]) / r;
+    for (int i = 0; i < 3; i++)
+      ret[2 + i] -= sd[i];
+    double Av[3];
+    for (int i = 0; i < 3; i++)
+      Av[i] = (A[3 * i] * rv[0] + A[3 * i + 1] * rv[1] + A[3 * i + 2] * rv[2]) / r;
+    ret[5 + d] += Av[0];
+    ret[8 + d] += Av[1];
+    ret[11 + d] += Av[2];
+  }
+  if (THERMAL) {
+    const double *rJ = Q + 14;
+    double T = temperature_mg(r, p, P);
+    ret[1] += P->calpha2 * T * rJ[d] / r;
+    for (int i = 0; i < 3; i++)
+      ret[14 + i] += vd * rJ[i];
+    ret[14 + d] += T;
+  }
+}
+
+/* ret = S(Q)   (equations.cpp:50-67) */
+void or_source(const double *Q, const gpr_par *P, double *ret) {
+  for (int i = 0; i < V; i++)
+    ret[i] = 0.0;
+  ret[2] = P->dp[0];
+  ret[3] = P->dp[1];
+  ret[4] = P->dp[2];
+  {
+    double EA[9];
+    dEdA_s(Q, P, EA);
+    double t1 = theta1inv(Q, P);
+    for (int i = 0; i < 9; i++)
+      ret[5 + i] = -EA[i] * t1;
+  }
+  if (THERMAL) {
+    double r = Q[0];
+    double t2 = theta2inv(Q, P);
+    for (int i = 0; i < 3; i++)
+      ret[14 + i] = -r * (P->calpha2 * Q[14 + i] / r) * t2;
+  }
+}
+
+/* ret = B_d(Q) x   (equations.cpp:189-267) */
+void or_Bdot(const double *Q, const double *x, int d, double *ret) {
+  double r = Q[0];
+  double v0 = Q[2] / r, v1 = Q[3] / r, v2 = Q[4] / r;
+  for (int i = 0; i < V; i++)
+    ret[i] = 0.0;
+  if (d == 0) {
+    ret[5] = -v1 * x[6] - v2 * x[7];
+    ret[6] = v0 * x[6];
+    ret[7] = v0 * x[7];
+    ret[8] = -v1 * x[9] - v2 * x[10];
+    ret[9] = v0 * x[9];
+    ret[10] = v0 * x[10];
+    ret[11] = -v1 * x[12] - v2 * x[13];
+    ret[12] = v0 * x[12];
+    ret[13] = v0 * x[13];
+  } else if (d == 1) {
+    ret[5] = v1 * x[5];
+    ret[6] = -v0 * x[5] - v2 * x[7];
+    ret[7] = v1 * x[7];
+    ret[8] = v1 * x[8];
+    ret[9] = -v0 * x[8] - v2 * x[10];
+    ret[10] = v1 * x[10];
+    ret[11] = v1 * x[11];
+    ret[12] = -v0 * x[11] - v2 * x[13];
+    ret[13] = v1 * x[13];
+  } else {
+    ret[5] = v2 * x[5];
+    ret[6] = v2 * x[6];
+    ret[7] = -v0 * x[5] - v1 * x[6];
+    ret[8] = v2 * x[8];
+    ret[9] = v2 * x[9];
+    ret[10] = -v0 * x[8] - v1 * x[9];
+    ret[11] = v2 * x[11];
+    ret[12] = v2 * x[12];
+    ret[13] = -v0 * x[11] - v1 * x[12];
+  }
+  double vd = d == 0 ? v0 : (d == 1 ? v1 : v2);
+  for (int i = 1; i < LSET + 1; i++)
+    ret[V - i] = vd * x[V - i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Real nonsymmetric eigenvalues: Householder reduction to upper Hessenberg */
+/* form, then the Francis double-shift QR iteration (Golub & Van Loan,      */
+/* Matrix Computations, Alg. 7.4.2 / 7.5.1-7.5.2).  Eigen's EigenSolver,    */
+/* which the reference calls (system/eig.cpp:73, fv/fluxes.cpp:30-33), is    */
+/* the same algorithm family.  With want_vec the Schur vectors are          */
+/* accumulated and eigenvectors recovered by back-substitution.             */
+
+#define EMAX 18
+/* Eigenvalues closer than MULT_TOL * ||T|| are one (semisimple) multiple
+ * eigenvalue: their Schur vectors are kept as independent eigenvectors. */
+#define MULT_TOL 1e-12
+
+static void hessenberg(int n, double *H, double *Z) {
+  /* H is n x n row-major (stride EMAX); Z accumulates (if not NULL). */
+  for (int k = 0; k < n - 2; k++) {
+    double alpha = 0.0;
+    for (int i = k + 1; i < n; i++)
+      alpha += H[i * EMAX + k] * H[i * EMAX + k];
+    alpha = sqrt(alpha);
+    if (alpha == 0.0)
+      continue;
+    double x0 = H[(k + 1) * EMAX + k];
+    double beta = x0 > 0 ? -alpha : alpha;
+    double v[EMAX];
+    for (int i = 0; i < n; i++)
+      v[i] = 0.0;
+    v[k + 1] = x0 - beta;
+    for (int i = k + 2; i < n; i++)
+      v[i] = H[i * EMAX + k];
+    double vv = 0.0;
+    for (int i = k + 1; i < n; i++)
+      vv += v[i] * v[i];
+    if (vv == 0.0)
+      continue;
+    double tau = 2.0 / vv;
+    /* H = (I - tau v v^T) H (I - tau v v^T) */
+    for (int j = 0; j < n; j++) {
+      double s = 0.0;
+      for (int i = k + 1; i < n; i++)
+        s += v[i] * H[i * EMAX + j];
+      s *= tau;
+      for (int i = k + 1; i < n; i++)
+        H[i * EMAX + j] -= s * v[i];
+    }
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; j++)
+        s += H[i * EMAX + j] * v[j];
+      s *= tau;
+      for (int j = k + 1; j < n; j++)
+        H[i * EMAX + j] -= s * v[j];
+    }
+    if (Z) {
+      for (int i = 0; i < n; i++) {
+        double s = 0.0;
+        for (int j = k + 1; j < n; j++)
+          s += Z[i * EMAX + j] * v[j];
+        s *= tau;
+        for (int j = k + 1; j < n; j++)
+          Z[i * EMAX + j] -= s * v[j];
+      }
+    }
+    for (int i = k + 2; i < n; i++)
+      H[i * EMAX + k] = 0.0;
+  }
+}
+
+/* Francis double-shift QR on upper Hessenberg H (n x n, stride EMAX).
+ * Eigenvalues to (wr, wi).  If Z != NULL the transformations are applied
+ * to the whole matrix and accumulated into Z (real Schur form).
+ * Returns 0 on success, -1 if it fails to converge. */
+static int hqr(int n, double *H, double *wr, double *wi, double *Z) {
+  const double eps = 2.220446049250313e-16;
+  double norm = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = (i > 0 ? i - 1 : 0); j < n; j++)
+      norm += fabs(H[i * EMAX + j]);
+  int hi = n - 1;
+  int iter = 0, total = 0;
+  double exshift = 0.0;
+  while (hi >= 0) {
+    /* look for a small subdiagonal element */
+    int l = hi;
+    while (l > 0) {
+      double s = fabs(H[(l - 1) * EMAX + l - 1]) + fabs(H[l * EMAX + l]);
+      if (s == 0.0)
+        s = norm;
+      if (fabs(H[l * EMAX + l - 1]) < eps * s)
+        break;
+      l--;
+    }
+    if (l == hi) { /* one root */
+      H[hi * EMAX + hi] += exshift;
+      wr[hi] = H[hi * EMAX + hi];
+      wi[hi] = 0.0;
+      if (hi > 0)
+        H[hi * EMAX + hi - 1] = 0.0;
+      hi--;
+      iter = 0;
+      continue;
+    }
+    double x = H[hi * EMAX + hi];
+    double y = H[(hi - 1) * EMAX + hi - 1];
+    double w = H[hi * EMAX + hi - 1] * H[(hi - 1) * EMAX + hi];
+    if (l == hi - 1) { /* two roots */
+      if (hi >= 2)
+        H[(hi - 1) * EMAX + hi - 2] = 0.0;
+      double p = 0.5 * (y - x);
+      double q = p * p + w;
+      /* A complex pair whose imaginary part is at rounding level is a real
+       * double root (a semisimple multiple eigenvalue split by rounding). */
+      if (q < 0.0 && sqrt(-q) <= MULT_TOL * norm)
+        q = 0.0;
+      double z = sqrt(fabs(q));
+      H[hi * EMAX + hi] = x + exshift;
+      H[(hi - 1) * EMAX + hi - 1] = y + exshift;
+      x = H[hi * EMAX + hi];
+      if (q >= 0.0) { /* real pair */
+        z = p >= 0 ? p + z : p - z;
+        wr[hi - 1] = x + z;
+        wr[hi] = z != 0.0 ? x - w / z : x + z;
+        wi[hi - 1] = wi[hi] = 0.0;
+        if (Z) {
+          /* rotate to upper triangular */
+          double xx = H[hi * EMAX + hi - 1];
+          double s = fabs(xx) + fabs(z);
+          double pp = xx / s, qq = z / s;
+          double rr = sqrt(pp * pp + qq * qq);
+          pp /= rr;
+          qq /= rr;
+          for (int j = hi - 1; j < n; j++) {
+            double a = H[(hi - 1) * EMAX + j];
+            H[(hi - 1) * EMAX + j] = qq * a + pp * H[hi * EMAX + j];
+            H[hi * EMAX + j] = qq * H[hi * EMAX + j] - pp * a;
+          }
+          for (int i = 0; i <= hi; i++) {
+            double a = H[i * EMAX + hi - 1];
+            H[i * EMAX + hi - 1] = qq * a + pp * H[i * EMAX + hi];
+            H[i * EMAX + hi] = qq * H[i * EMAX + hi] - pp * a;
+          }
+          for (int i = 0; i < n; i++) {
+            double a = Z[i * EMAX + hi - 1];
+            Z[i * EMAX + hi - 1] = qq * a + pp * Z[i * EMAX + hi];
+            Z[i * EMAX + hi] = qq * Z[i * EMAX + hi] - pp * a;
+          }
+          H[hi * EMAX + hi - 1] = 0.0;
+        }
+      } else { /* complex pair */
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = z;
+        wi[hi] = -z;
+      }
+      hi -= 2;
+      iter = 0;
+      continue;
+    }
+    /* form shift */
+    if (iter == 10 || iter == 20) { /* exceptional shift */
+      exshift += x;
+      for (int i = 0; i <= hi; i++)
+        H[i * EMAX + i] -= x;
+      double s = fabs(H[hi * EMAX + hi - 1]) + fabs(H[(hi - 1) * EMAX + hi - 2]);
+      x = y = 0.75 * s;
+      w = -0.4375 * s * s;
+    }
+    iter++;
+    total++;
+    if (total > 60 * n)
+      return -1;
+    /* look for two consecutive small subdiagonal elements */
+    int m = hi - 2;
+    double p = 0, q = 0, r = 0, z;
+    while (m >= l) {
+      z = H[m * EMAX + m];
+      r = x - z;
+      double s = y - z;
+      p = (r * s - w) / H[(m + 1) * EMAX + m] + H[m * EMAX + m + 1];
+      q = H[(m + 1) * EMAX + m + 1] - z - r - s;
+      r = H[(m + 2) * EMAX + m + 1];
+      s = fabs(p) + fabs(q) + fabs(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      double u = fabs(H[m * EMAX + m - 1]) * (fabs(q) + fabs(r));
+      double vv = fabs(p) * (fabs(H[(m - 1) * EMAX + m - 1]) + fabs(z) +
+                             fabs(H[(m + 1) * EMAX + m + 1]));
+      if (u < eps * vv)
+        break;
+      m--;
+    }
+    for (int i = m + 2; i <= hi; i++) {
+      H[i * EMAX + i - 2] = 0.0;
+      if (i > m + 2)
+        H[i * EMAX + i - 3] = 0.0;
+    }
+    /* double QR step on rows l..hi, columns m..hi */
+    for (int k = m; k <= hi - 1; k++) {
+      int notlast = (k != hi - 1);
+      if (k != m) {
+        p = H[k * EMAX + k - 1];
+        q = H[(k + 1) * EMAX + k - 1];
+        r = notlast ? H[(k + 2) * EMAX + k - 1] : 0.0;
+        x = fabs(p) + fabs(q) + fabs(r);
+        if (x == 0.0)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      double s = sqrt(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        H[k * EMAX + k - 1] = -s * x;
+      else if (l != m)
+        H[k * EMAX + k - 1] = -H[k * EMAX + k - 1];
+      p += s;
+      x = p / s;
+      y = q / s;
+      z = r / s;
+      q /= p;
+      r /= p;
+      int jlo = Z ? k : k, jhi = Z ? n - 1 : hi;
+      for (int j = jlo; j <= jhi; j++) { /* row modification */
+        double pp = H[k * EMAX + j] + q * H[(k + 1) * EMAX + j];
+        if (notlast) {
+          pp += r * H[(k + 2) * EMAX + j];
+          H[(k + 2) * EMAX + j] -= pp * z;
+        }
+        H[k * EMAX + j] -= pp * x;
+        H[(k + 1) * EMAX + j] -= pp * y;
+      }
+      int ilo = Z ? 0 : l;
+      int ihi = hi < k + 3 ? hi : k + 3;
+      for (int i = ilo; i <= ihi; i++) { /* column modification */
+        double pp = x * H[i * EMAX + k] + y * H[i * EMAX + k + 1];
+        if (notlast) {
+          pp += z * H[i * EMAX + k + 2];
+          H[i * EMAX + k + 2] -= pp * r;
+        }
+        H[i * EMAX + k] -= pp;
+        H[i * EMAX + k + 1] -= pp * q;
+      }
+      if (Z) {
+        for (int i = 0; i < n; i++) {
+          double pp = x * Z[i * EMAX + k] + y * Z[i * EMAX + k + 1];
+          if (notlast) {
+            pp += z * Z[i * EMAX + k + 2];
+            Z[i * EMAX + k + 2] -= pp * r;
+          }
+          Z[i * EMAX + k] -= pp;
+          Z[i * EMAX + k + 1] -= pp * q;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* max |lambda| over the eigenvalues of the n x n row-major matrix M. */
+static double max_abs_eig(int n, const double *M) {
+  double H[EMAX * EMAX], wr[EMAX], wi[EMAX];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      H[i * EMAX + j] = M[i * n + j];
+  hessenberg(n, H, NULL);
+  if (hqr(n, H, wr, wi, NULL))
+    return NAN;
+  double m = 0.0;
+  for (int i = 0; i < n; i++) {
+    double a = hypot(wr[i], wi[i]);
+    if (a > m || a != a)
+      m = a;
+  }
+  return m;
+}
+
+int or_eigenvalues(int n, const double *M, double *wr, double *wi) {
+  double H[EMAX * EMAX];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      H[i * EMAX + j] = M[i * n + j];
+  hessenberg(n, H, NULL);
+  return hqr(n, H, wr, wi, NULL);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Thermo-acoustic tensor and max |eig| (system/eig.cpp:8-77).              */
+
+void or_thermo_acoustic_tensor(const double *Q, int d, const gpr_par *P,
+                               double *out) {
+  int m = THERMAL ? 4 : 3;
+  double r = Q[0];
+  double p = or_pressure(Q, P);
+  double X1[4][5], X2[5][4];
+  memset(X1, 0, sizeof X1);
+  memset(X2, 0, sizeof X2);
+  /* Xi1 (eig.cpp:8-27) */
+  X1[0][1] = 1 / r;
+  double dsr[3], dsA[9];
+  dsigmadrho(Q, P, d, dsr);
+  dsigmadA(Q, P, d, dsA);
+  for (int i = 0; i < 3; i++) {
+    X1[i][0] = -1 / r * dsr[i];
+    for (int j = 0; j < 3; j++)
+      X1[i][2 + j] = -1 / r * dsA[3 * i + j];
+  }
+  if (THERMAL) {
+    X1[3][0] = dTdrho(r, p, P) / r;
+    X1[3][1] = dTdp(r, P) / r;
+  }
+  /* Xi2 (eig.cpp:29-53) */
+  {
+    /* c_0 (waves/speeds.cpp:8-18) */
+    double dEdr = dedrho(r, p, P) + dC_0drho(r, P) / 4 * devGsq(Q + 5);
+    double dEp = dedp(r, P);
+    double c0 = sqrt((p / (r * r) - dEdr) / dEp);
+    X2[0][0] = r;
+    X2[1][d] = r * c0 * c0;
+    double sg[3];
+    sigma_d(Q, P, d, sg);
+    for (int i = 0; i < 3; i++)
+      X2[1][i] += sg[i] - r * dsr[i];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        X2[2 + i][j] = Q[5 + 3 * i + j];
+    if (THERMAL) {
+      double T = temperature_mg(r, p, P);
+      double ch = sqrt(P->calpha2 * T / P->cv) / r;
+      X2[1][3] = r * ch * ch / dTdp(r, P);
+    }
+  }
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < m; j++) {
+      double s = 0.0;
+      for (int k = 0; k < (THERMAL ? 5 : 5); k++)
+        s += X1[i][k] * X2[k][j];
+      out[i * m + j] = s;
+    }
+}
+
+double or_max_abs_eigs(const double *Q, int d, const gpr_par *P) {
+  int m = THERMAL ? 4 : 3;
+  double Xi[16];
+  or_thermo_acoustic_tensor(Q, d, P, Xi);
+  double vd = Q[2 + d] / Q[0];
+  double lam = sqrt(max_abs_eig(m, Xi));
+  if (vd > 0)
+    return vd + lam;
+  return lam - vd;
+}
+
+/* ------------------------------------------------------------------------ */
+/* System Jacobian (system/jacobians.cpp:10-152, equations.cpp:169-187).   */
+
+static double dEdrho_Q(const double *Q, const gpr_par *P) {
+  double r = Q[0];
+  double p = or_pressure(Q, P);
+  return dedrho(r, p, P) + dC_0drho(r, P) / 4 * devGsq(Q + 5);
+}
+
+static void dFdP(const double *Q, int d, const gpr_par *P, double *ret) {
+  int n = V;
+  memset(ret, 0, sizeof(double) * n * n);
+#define R_(i, j) ret[(i) * n + (j)]
+  double r = Q[0];
+  double E = Q[1] / r;
+  double p = or_pressure(Q, P);
+  double v[3] = {Q[2] / r, Q[3] / r, Q[4] / r};
+  const double *A = Q + 5;
+  double Er = dEdrho_Q(Q, P);
+  double Ep = dedp(r, P);
+  double vd = v[d];
+  double rvd = r * vd;
+  double G[9], AG[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  AdevG(A, AG);
+  R_(0, 0) = vd;
+  R_(0, 2 + d) = r;
+  R_(1, 0) = (E + r * Er) * vd;
+  R_(1, 1) = (r * Ep + 1) * vd;
+  for (int i = 0; i < 3; i++)
+    R_(1, 2 + i) = r * vd * v[i];
+  R_(1, 2 + d) += r * E + p;
+  for (int i = 0; i < 3; i++)
+    R_(2 + i, 0) = vd * v[i];
+  for (int i = 2; i < 5; i++)
+    R_(i, i) = rvd;
+  for (int i = 0; i < 3; i++)
+    R_(2 + i, 2 + d) += r * v[i];
+  R_(2 + d, 1) = 1.0;
+  {
+    double sg[3], sr[3], psi[9];
+    sigma_d(Q, P, d, sg);
+    dsigmadrho(Q, P, d, sr);
+    double C0 = C_0(r, P);
+    for (int i = 0; i < 9; i++)
+      psi[i] = C0 * AG[i];
+    double cs2 = c_s2(r, P);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        int ind = i * 3 + j;
+        double tmp = 0.0;
+        for (int k = 0; k < 3; k++) {
+          /* dsigmadA(rho, cs2, A, G, AdevG, d, k, i, j) (state.cpp:58-71) */
+          int ii = d, jj = k, mm = i, nn = j;
+          double t = A[3 * mm + ii] * G[3 * jj + nn] + A[3 * mm + jj] * G[3 * ii + nn] -
+                     2.0 / 3.0 * G[3 * ii + jj] * A[3 * mm + nn];
+          if (ii == nn)
+            t += AG[3 * mm + jj];
+          if (jj == nn)
+            t += AG[3 * mm + ii];
+          double dsA = -r * cs2 * t;
+          R_(2 + k, 5 + ind) = -dsA;
+          tmp -= v[k] * dsA;
+        }
+        R_(1, 5 + ind) = tmp;
+      }
+    R_(1, 0) -= sr[0] * v[0] + sr[1] * v[1] + sr[2] * v[2];
+    for (int i = 0; i < 3; i++)
+      R_(1, 2 + i) -= sg[i];
+    for (int i = 0; i < 9; i++)
+      R_(1, 5 + i) += r * vd * psi[i];
+    for (int i = 0; i < 3; i++)
+      R_(2 + i, 0) -= sr[i];
+    for (int j = 0; j < 3; j++) {
+      R_(5 + d, 2 + j) = A[j];
+      R_(8 + d, 2 + j) = A[3 + j];
+      R_(11 + d, 2 + j) = A[6 + j];
+      R_(5 + d, 5 + j) = v[j];
+      R_(8 + d, 8 + j) = v[j];
+      R_(11 + d, 11 + j) = v[j];
+    }
+  }
+  if (THERMAL) {
+    double ca2 = P->calpha2;
+    double T = temperature_mg(r, p, P);
+    double Tr = dTdrho(r, p, P);
+    double Tp = dTdp(r, P);
+    double J[3] = {Q[14] / r, Q[15] / r, Q[16] / r};
+    double H[3] = {ca2 * Q[14] / r, ca2 * Q[15] / r, ca2 * Q[16] / r};
+    R_(1, 0) += Tr * H[d];
+    R_(1, 1) += Tp * H[d];
+    for (int i = 0; i < 3; i++)
+      R_(1, 14 + i) = rvd * H[i];
+    R_(1, 14 + d) += ca2 * T;
+    for (int i = 0; i < 3; i++)
+      R_(14 + i, 0) = v[d] * J[i];
+    R_(14 + d, 0) += Tr;
+    R_(14 + d, 1) = Tp;
+    for (int i = 0; i < 3; i++)
+      R_(14 + i, 2 + d) = r * J[i];
+    for (int i = 14; i < 17; i++)
+      R_(i, i) = rvd;
+  }
+#undef R_
+}
+
+static void dPdQ(const double *Q, const gpr_par *P, double *ret) {
+  int n = V;
+  memset(ret, 0, sizeof(double) * n * n);
+  for (int i = 0; i < n; i++)
+    ret[i * n + i] = 1.0;
+#define R_(i, j) ret[(i) * n + (j)]
+  double r = Q[0];
+  double E = Q[1] / r;
+  double v[3] = {Q[2] / r, Q[3] / r, Q[4] / r};
+  double Er = dEdrho_Q(Q, P);
+  double Ep = dedp(r, P);
+  double G_ = 1 / (r * Ep);
+  double tmp = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) - (E + r * Er);
+  double J[3] = {0, 0, 0};
+  if (THERMAL) {
+    J[0] = Q[14] / r;
+    J[1] = Q[15] / r;
+    J[2] = Q[16] / r;
+    tmp += P->calpha2 * (J[0] * J[0] + J[1] * J[1] + J[2] * J[2]);
+  }
+  double Ups = G_ * tmp;
+  R_(1, 0) = Ups;
+  R_(1, 1) = G_;
+  for (int i = 0; i < 3; i++) {
+    R_(1, 2 + i) = -G_ * v[i];
+    R_(2 + i, 0) = -v[i] / r;
+  }
+  for (int i = 2; i < 5; i++)
+    R_(i, i) = 1 / r;
+  {
+    double AG[9];
+    AdevG(Q + 5, AG);
+    double C0 = C_0(r, P);
+    for (int i = 0; i < 9; i++)
+      R_(1, 5 + i) = -G_ * r * (C0 * AG[i]);
+  }
+  if (THERMAL) {
+    for (int i = 0; i < 3; i++) {
+      R_(1, 14 + i) = -G_ * (P->calpha2 * Q[14 + i] / r);
+      R_(14 + i, 0) = -J[i] / r;
+    }
+    for (int i = 14; i < 17; i++)
+      R_(i, i) = 1 / r;
+  }
+#undef R_
+}
+
+/* system_matrix = dFdP dPdQ + B   (equations.cpp:269-276) */
+void or_system_matrix(const double *Q, int d, const gpr_par *P, double *M) {
+  int n = V;
+  double *F = malloc(sizeof(double) * n * n * 2);
+  double *D = F + n * n;
+  dFdP(Q, d, P, F);
+  dPdQ(Q, P, D);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double s = 0.0;
+      for (int k = 0; k < n; k++)
+        s += F[i * n + k] * D[k * n + j];
+      M[i * n + j] = s;
+    }
+  free(F);
+  /* block (equations.cpp:169-187) */
+  double r = Q[0];
+  double vd = Q[2 + d] / r;
+  for (int i = 5; i < 14; i++)
+    M[i * n + i] += vd;
+  for (int i = 0; i < 3; i++) {
+    double vi = Q[2 + i] / r;
+    M[(5 + d) * n + 5 + i] -= vi;
+    M[(8 + d) * n + 8 + i] -= vi;
+    M[(11 + d) * n + 11 + i] -= vi;
+  }
+  for (int i = 1; i < LSET + 1; i++)
+    M[(V - i) * n + V - i] += vd;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Interface terms (solvers/fv/fluxes.cpp).                                */
+
+/* Bint (fluxes.cpp:9-20) */
+void or_Bint(const double *qL, const double *qR, int d, double *ret) {
+  double dq[MAXV], q[MAXV], tmp[MAXV];
+  for (int k = 0; k < V; k++) {
+    ret[k] = 0.0;
+    dq[k] = qR[k] - qL[k];
+  }
+  for (int i = 0; i < N; i++) {
+    for (int k = 0; k < V; k++)
+      q[k] = qL[k] + NODES[i] * dq[k];
+    or_Bdot(q, dq, d, tmp);
+    for (int k = 0; k < V; k++)
+      ret[k] += WGHTS[i] * tmp[k];
+  }
+}
+
+/* D_RUS (fluxes.cpp:66-75) */
+void or_D_RUS(const double *qL, const double *qR, int d, const gpr_par *P,
+              double *f) {
+  double m1 = or_max_abs_eigs(qL, d, P);
+  double m2 = or_max_abs_eigs(qR, d, P);
+  double m = m1 > m2 ? m1 : m2;
+  for (int k = 0; k < V; k++)
+    f[k] = m * (qL[k] - qR[k]);
+  or_flux(qL, d, P, f);
+  or_flux(qR, d, P, f);
+}
+
+/* Complex solve of (R) x = b by Gaussian elimination with partial
+ * pivoting; R is n x n complex (re, im) row-major, overwritten. */
+static int csolve(int n, double *Rr, double *Ri, double *br, double *bi) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    double best = hypot(Rr[c * n + c], Ri[c * n + c]);
+    for (int r = c + 1; r < n; r++) {
+      double a = hypot(Rr[r * n + c], Ri[r * n + c]);
+      if (a > best) {
+        best = a;
+        p = r;
+      }
+    }
+    if (best == 0.0)
+      return -1;
+    if (p != c) {
+      for (int j = 0; j < n; j++) {
+        double t = Rr[c * n + j];
+        Rr[c * n + j] = Rr[p * n + j];
+        Rr[p * n + j] = t;
+        t = Ri[c * n + j];
+        Ri[c * n + j] = Ri[p * n + j];
+        Ri[p * n + j] = t;
+      }
+      double t = br[c];
+      br[c] = br[p];
+      br[p] = t;
+      t = bi[c];
+      bi[c] = bi[p];
+      bi[p] = t;
+    }
+    double pr = Rr[c * n + c], pi = Ri[c * n + c];
+    double den = pr * pr + pi * pi;
+    for (int r = c + 1; r < n; r++) {
+      double ar = Rr[r * n + c], ai = Ri[r * n + c];
+      double fr = (ar * pr + ai * pi) / den, fi = (ai * pr - ar * pi) / den;
+      for (int j = c; j < n; j++) {
+        double xr = Rr[c * n + j], xi = Ri[c * n + j];
+        Rr[r * n + j] -= fr * xr - fi * xi;
+        Ri[r * n + j] -= fr * xi + fi * xr;
+      }
+      br[r] -= fr * br[c] - fi * bi[c];
+      bi[r] -= fr * bi[c] + fi * br[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    double sr = br[r], si = bi[r];
+    for (int j = r + 1; j < n; j++) {
+      sr -= Rr[r * n + j] * br[j] - Ri[r * n + j] * bi[j];
+      si -= Rr[r * n + j] * bi[j] + Ri[r * n + j] * br[j];
+    }
+    double pr = Rr[r * n + r], pi = Ri[r * n + r];
+    double den = pr * pr + pi * pi;
+    br[r] = (sr * pr + si * pi) / den;
+    bi[r] = (si * pr - sr * pi) / den;
+  }
+  return 0;
+}
+
+/* Eigenvectors from the real Schur form T (quasi upper triangular) and the
+ * Schur vectors Z: back-substitution per eigenvalue, complex pairs handled
+ * in complex arithmetic.  Produces the complex eigenvector matrix (columns)
+ * in (Rr, Ri), n x n row-major. */
+static void schur_eigvecs(int n, const double *T, const double *Z,
+                          const double *wr, const double *wi, double *Rr,
+                          double *Ri) {
+  double norm = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = i > 0 ? i - 1 : 0; j < n; j++)
+      norm += fabs(T[i * EMAX + j]);
+  for (int k = 0; k < n; k++) {
+    double lr = wr[k], li = wi[k];
+    double yr[EMAX], yi[EMAX];
+    for (int i = 0; i < n; i++)
+      yr[i] = yi[i] = 0.0;
+    /* find the block containing k */
+    int blk2 = (k + 1 < n && T[(k + 1) * EMAX + k] != 0.0) ? 1 : 0;
+    int blk1 = (k > 0 && T[k * EMAX + k - 1] != 0.0) ? 1 : 0;
+    int top; /* last index of the eigenvector's support */
+    if (!blk1 && !blk2) {
+      yr[k] = 1.0;
+      top = k;
+    } else {
+      /* 2x2 block at (b, b+1) */
+      int b = blk2 ? k : k - 1;
+      /* solve (T_bb - lambda I) [y_b; y_b1] = 0 */
+      double a11 = T[b * EMAX + b] - lr, a12 = T[b * EMAX + b + 1];
+      double a21 = T[(b + 1) * EMAX + b];
+      /* choose y_{b+1} = 1, y_b = -a12/(a11 - i li) if possible */
+      if (fabs(a12) >= fabs(a21)) {
+        /* y_b = 1, y_{b+1} = -(a11 - i li)/a12 */
+        yr[b] = 1.0;
+        yi[b] = 0.0;
+        yr[b + 1] = -a11 / a12;
+        yi[b + 1] = li / a12;
+      } else {
+        /* y_{b+1} = 1, y_b = -a22'/a21 where a22' = T_b1b1 - lambda */
+        double a22r = T[(b + 1) * EMAX + b + 1] - lr;
+        yr[b + 1] = 1.0;
+        yi[b + 1] = 0.0;
+        yr[b] = -a22r / a21;
+        yi[b] = li / a21;
+      }
+      top = b + 1;
+    }
+    /* back-substitute rows above the block */
+    int start = (blk1 || blk2) ? (blk2 ? k - 1 : k - 2) : k - 1;
+    for (int i = start; i >= 0; i--) {
+      int is2 = (i > 0 && T[i * EMAX + i - 1] != 0.0);
+      if (!is2) {
+        double sr = 0.0, si = 0.0;
+        for (int j = i + 1; j <= top; j++) {
+          sr += T[i * EMAX + j] * yr[j];
+          si += T[i * EMAX + j] * yi[j];
+        }
+        double dr = T[i * EMAX + i] - lr, di = -li;
+        if (hypot(dr, di) <= MULT_TOL * norm) {
+          yr[i] = yi[i] = 0.0; /* same eigenvalue: independent Schur vector */
+          continue;
+        }
+        double den = dr * dr + di * di;
+        yr[i] = -(sr * dr + si * di) / den;
+        yi[i] = -(si * dr - sr * di) / den;
+      } else {
+        /* 2x2 block rows (i-1, i) */
+        int a = i - 1;
+        double s1r = 0, s1i = 0, s2r = 0, s2i = 0;
+        for (int j = i + 1; j <= top; j++) {
+          s1r += T[a * EMAX + j] * yr[j];
+          s1i += T[a * EMAX + j] * yi[j];
+          s2r += T[i * EMAX + j] * yr[j];
+          s2i += T[i * EMAX + j] * yi[j];
+        }
+        /* [[t11-l, t12],[t21, t22-l]] y = -s */
+        double m11r = T[a * EMAX + a] - lr, m11i = -li;
+        double m12 = T[a * EMAX + i], m21 = T[i * EMAX + a];
+        double m22r = T[i * EMAX + i] - lr, m22i = -li;
+        double detr = m11r * m22r - m11i * m22i - m12 * m21;
+        double deti = m11r * m22i + m11i * m22r;
+        if (hypot(detr, deti) <= MULT_TOL * norm * MULT_TOL * norm) {
+          yr[a] = yi[a] = yr[i] = yi[i] = 0.0;
+          i--;
+          continue;
+        }
+        double den = detr * detr + deti * deti;
+        /* y_a = (-s1*m22 + m12*s2)/det ; y_i = (-m11*s2 + m21*s1)/det */
+        double nar = -(s1r * m22r - s1i * m22i) + m12 * s2r;
+        double nai = -(s1r * m22i + s1i * m22r) + m12 * s2i;
+        double nir = -(m11r * s2r - m11i * s2i) + m21 * s1r;
+        double nii = -(m11r * s2i + m11i * s2r) + m21 * s1i;
+        yr[a] = (nar * detr + nai * deti) / den;
+        yi[a] = (nai * detr - nar * deti) / den;
+        yr[i] = (nir * detr + nii * deti) / den;
+        yi[i] = (nii * detr - nir * deti) / den;
+        i--; /* skip a */
+      }
+    }
+    /* x = Z y */
+    for (int i = 0; i < n; i++) {
+      double sr = 0.0, si = 0.0;
+      for (int j = 0; j <= top; j++) {
+        sr += Z[i * EMAX + j] * yr[j];
+        si += Z[i * EMAX + j] * yi[j];
+      }
+      Rr[i * n + k] = sr;
+      Ri[i * n + k] = si;
+    }
+  }
+}
+
+/* Adds sum_i w_i R_i |Lambda_i| R_i^{-1} dq for J = system_matrix(q) into
+ * (acc) -- the eigen-part of D_OSH (fluxes.cpp:22-44) / D_ROE (:46-64). */
+static int abs_jac_apply(const double *J, const double *dq, double w,
+                         double *acc) {
+  int n = V;
+  double H[EMAX * EMAX], Z[EMAX * EMAX], wr[EMAX], wi[EMAX];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      H[i * EMAX + j] = J[i * n + j];
+      Z[i * EMAX + j] = (i == j) ? 1.0 : 0.0;
+    }
+  hessenberg(n, H, Z);
+  if (hqr(n, H, wr, wi, Z))
+    return -1;
+  double Rr[EMAX * EMAX], Ri[EMAX * EMAX], Cr[EMAX * EMAX], Ci[EMAX * EMAX];
+  schur_eigvecs(n, H, Z, wr, wi, Rr, Ri);
+  memcpy(Cr, Rr, sizeof(double) * n * n);
+  memcpy(Ci, Ri, sizeof(double) * n * n);
+  double br[EMAX], bi[EMAX];
+  for (int k = 0; k < n; k++) {
+    br[k] = dq[k];
+    bi[k] = 0.0;
+  }
+  if (csolve(n, Cr, Ci, br, bi))
+    return -1;
+  for (int k = 0; k < n; k++) {
+    double a = hypot(wr[k], wi[k]);
+    br[k] *= a;
+    bi[k] *= a;
+  }
+  for (int i = 0; i < n; i++) {
+    double s = 0.0;
+    for (int k = 0; k < n; k++)
+      s += Rr[i * n + k] * br[k] - Ri[i * n + k] * bi[k];
+    acc[i] += w * s;
+  }
+  return 0;
+}
+
+/* D_OSH (fluxes.cpp:22-44) */
+void or_D_OSH(const double *qL, const double *qR, int d, const gpr_par *P,
+              double *f) {
+  int n = V;
+  double dq[MAXV], q[MAXV];
+  double *J = malloc(sizeof(double) * n * n);
+  for (int k = 0; k < n; k++) {
+    dq[k] = qL[k] - qR[k];
+    f[k] = 0.0;
+  }
+  for (int i = 0; i < N; i++) {
+    for (int k = 0; k < n; k++)
+      q[k] = qR[k] + NODES[i] * dq[k];
+    or_system_matrix(q, d, P, J);
+    if (abs_jac_apply(J, dq, WGHTS[i], f)) {
+      for (int k = 0; k < n; k++)
+        f[k] = NAN;
+    }
+  }
+  free(J);
+  or_flux(qL, d, P, f);
+  or_flux(qR, d, P, f);
+}
+
+/* D_ROE (fluxes.cpp:46-64) */
+void or_D_ROE(const double *qL, const double *qR, int d, const gpr_par *P,
+              double *f) {
+  int n = V;
+  double dq[MAXV], q[MAXV];
+  double *J = calloc(n * n * 2, sizeof(double));
+  double *Ji = J + n * n;
+  for (int k = 0; k < n; k++) {
+    dq[k] = qL[k] - qR[k];
+    f[k] = 0.0;
+  }
+  for (int i = 0; i < N; i++) {
+    for (int k = 0; k < n; k++)
+      q[k] = qR[k] + NODES[i] * dq[k];
+    or_system_matrix(q, d, P, Ji);
+    for (int k = 0; k < n * n; k++)
+      J[k] += WGHTS[i] * Ji[k];
+  }
+  if (abs_jac_apply(J, dq, 1.0, f))
+    for (int k = 0; k < n; k++)
+      f[k] = NAN;
+  free(J);
+  or_flux(qL, d, P, f);
+  or_flux(qR, d, P, f);
+}
+
+static void interface_D(int FLUX, const double *qL, const double *qR, int d,
+                        const gpr_par *P, double *f) {
+  switch (FLUX) {
+  case GPR_FLUX_OSHER:
+    or_D_OSH(qL, qR, d, P, f);
+    break;
+  case GPR_FLUX_ROE:
+    or_D_ROE(qL, qR, d, P, f);
+    break;
+  default:
+    or_D_RUS(qL, qR, d, P, f);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Boundaries and masks (etc/grid.cpp:12-230).                              */
+
+static void bc_row(double *dst, const double *src, int code, int d, int side,
+                   const double *srcrow0) {
+  (void)side;
+  memcpy(dst, src, sizeof(double) * V);
+  switch (code) {
+  case GPR_BC_SLIP:
+    dst[2 + d] *= -1.0;
+    break;
+  case GPR_BC_STICK:
+    dst[2] *= -1.0;
+    dst[3] *= -1.0;
+    dst[4] *= -1.0;
+    break;
+  case GPR_BC_MOVING:
+    dst[2] *= -1.0;
+    dst[3] *= -1.0;
+    dst[4] *= -1.0;
+    dst[2] += 2.0 * dst[0];
+    dst[1] += (dst[2] * dst[2] - srcrow0[2] * srcrow0[2]) / (2 * dst[0]);
+    break;
+  case GPR_BC_SYMMETRIC: {
+    dst[2 + d] *= -1.0;
+    double *A = dst + 5;
+    for (int k = 0; k < 3; k++)
+      A[3 * d + k] *= -1.0;
+    for (int k = 0; k < 3; k++)
+      A[3 * k + d] *= -1.0;
+  } break;
+  default:
+    break;
+  }
+}
+
+/* boundaries1 (grid.cpp:12-125) over a strided line: u rows at u + i*su,
+ * ub rows at ub + i*sb (strides in doubles). */
+static void boundaries1(const double *u, long su, double *ub, long sb, int nx,
+                        const int *bt, int d) {
+  for (int i = 0; i < N; i++) {
+    const double *src;
+    switch (bt[0]) {
+    case GPR_BC_TRANSMISSIVE:
+      src = u;
+      break;
+    case GPR_BC_PERIODIC:
+      src = u + (long)(nx - N + i) * su;
+      break;
+    default:
+      src = u + (long)(N - 1 - i) * su;
+    }
+    bc_row(ub + (long)i * sb, src, bt[0] == GPR_BC_PERIODIC ? 0 : bt[0], d, 0, src);
+  }
+  for (int i = 0; i < N; i++) {
+    const double *src;
+    switch (bt[1]) {
+    case GPR_BC_TRANSMISSIVE:
+      src = u + (long)(nx - 1) * su;
+      break;
+    case GPR_BC_PERIODIC:
+      src = u + (long)i * su;
+      break;
+    default:
+      src = u + (long)(nx - 1 - i) * su;
+    }
+    bc_row(ub + (long)(i + nx + N) * sb, src, bt[1] == GPR_BC_PERIODIC ? 0 : bt[1],
+           d, 1, src);
+  }
+}
+
+int or_boundaries(const double *u, double *ub, const int *nX, int ndim,
+                  const int *bcs) {
+  int nx = nX[0];
+  if (ndim == 1) {
+    memcpy(ub + N * V, u, sizeof(double) * nx * V);
+    boundaries1(u, V, ub, V, nx, bcs, 0);
+    return 0;
+  }
+  int ny = nX[1];
+  long nyb = ny + 2 * N;
+  for (int i = 0; i < nx; i++)
+    memcpy(ub + ((long)(i + N) * nyb + N) * V, u + (long)i * ny * V,
+           sizeof(double) * ny * V);
+  for (int j = 0; j < ny; j++)
+    boundaries1(u + (long)j * V, (long)ny * V, ub + (long)(j + N) * V, nyb * V, nx,
+                bcs, 0);
+  for (int i = 0; i < nx + 2 * N; i++)
+    boundaries1(ub + ((long)i * nyb + N) * V, V, ub + (long)i * nyb * V, V, ny,
+                bcs + 2, 1);
+  return 0;
+}
+
+int or_extend_mask(const uint8_t *mask, uint8_t *maskb, const int *nX, int ndim) {
+  int nx = nX[0];
+  if (ndim == 1) {
+    for (int i = 0; i < nx; i++)
+      maskb[i + 1] = (mask[i] || (i > 0 && mask[i - 1]) || (i < nx - 1 && mask[i + 1]));
+    maskb[0] = maskb[1];
+    maskb[nx + 1] = maskb[nx];
+    return 0;
+  }
+  int ny = nX[1];
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      int ind = i * ny + j;
+      maskb[(i + 1) * (ny + 2) + (j + 1)] =
+          (mask[ind] || (i > 0 && mask[(i - 1) * ny + j]) ||
+           (i < nx - 1 && mask[(i + 1) * ny + j]) || (j > 0 && mask[ind - 1]) ||
+           (j < ny - 1 && mask[ind + 1]));
+    }
+  for (int i = 0; i < nx; i++) {
+    maskb[(i + 1) * (ny + 2)] = mask[i * ny];
+    maskb[(i + 1) * (ny + 2) + (ny + 1)] = mask[i * ny + (ny - 1)];
+  }
+  for (int j = 0; j < ny; j++) {
+    maskb[j + 1] = mask[j];
+    maskb[(nx + 1) * (ny + 2) + (j + 1)] = mask[(nx - 1) * ny + j];
+  }
+  maskb[0] = 0;
+  maskb[ny + 1] = 0;
+  maskb[(nx + 1) * (ny + 2)] = 0;
+  maskb[(nx + 1) * (ny + 2) + (ny + 1)] = 0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* WENO (solvers/weno/weno.cpp).                                            */
+
+/* weight (weno.cpp:4-15) for one variable */
+static double weno_weight(const double *w, double LAM) {
+  /* (w^T SIG) w, the reference's evaluation order: on near-constant data
+   * w^T SIG is a difference of nearly equal coefficients, and forming it
+   * first keeps the indicator accurate where the expanded quadratic form
+   * would cancel catastrophically. */
+  double t = 0.0;
+  for (int b = 0; b < N; b++) {
+    double tb = 0.0;
+    for (int a = 0; a < N; a++)
+      tb += w[a] * SIG[a][b];
+    t += tb * w[b];
+  }
+  t += WENO_EPS;
+  double t2 = t * t, t4 = t2 * t2, den = t4 * t4;
+  return LAM / den;
+}
+
+/* coeffs (weno.cpp:17-73): data rows at data + r*sd (r = 0..2N-2), result
+ * rows (N nodes) at ret + a*sr. */
+static void weno_coeffs(double *ret, long sr, const double *data, long sd,
+                        int nx, int gap, int ind) {
+  for (int k = 0; k < V; k++) {
+    double wL[MAXN], wR[MAXN], wCL[MAXN], wCR[MAXN];
+    for (int a = 0; a < N; a++) {
+      double sL = 0, sR = 0, sCL = 0, sCR = 0;
+      for (int b = 0; b < N; b++) {
+        sL += mLinv[a][b] * data[(long)b * sd + k];
+        sR += mRinv[a][b] * data[(long)(N - 1 + b) * sd + k];
+        if (N > 2) {
+          sCL += mCLinv[a][b] * data[(long)(FN2 + b) * sd + k];
+          if (N % 2 == 0)
+            sCR += mCRinv[a][b] * data[(long)(CN2 + b) * sd + k];
+        }
+      }
+      wL[a] = sL;
+      wR[a] = sR;
+      wCL[a] = sCL;
+      wCR[a] = sCR;
+    }
+    double oL = weno_weight(wL, LAMS), oR = weno_weight(wR, LAMS);
+    double oCL = 0, oCR = 0;
+    if (N > 2) {
+      oCL = weno_weight(wCL, LAMC);
+      if (N % 2 == 0)
+        oCR = weno_weight(wCR, LAMC);
+    }
+    double num[MAXN] = {0, 0, 0, 0}, den = 0.0;
+    if (ind >= gap) {
+      for (int a = 0; a < N; a++)
+        num[a] += wL[a] * oL;
+      den += oL;
+    }
+    if (ind <= nx - gap - 1) {
+      for (int a = 0; a < N; a++)
+        num[a] += wR[a] * oR;
+      den += oR;
+    }
+    if (N > 2) {
+      if (ind + FN2 >= gap) {
+        for (int a = 0; a < N; a++)
+          num[a] += wCL[a] * oCL;
+        den += oCL;
+      }
+      if ((N % 2 == 0) && (ind - FN2 <= nx - gap - 1)) {
+        for (int a = 0; a < N; a++)
+          num[a] += wCR[a] * oCR;
+        den += oCR;
+      }
+    }
+    for (int a = 0; a < N; a++)
+      ret[(long)a * sr + k] = num[a] / den;
+  }
+}
+
+int or_weno_launcher(double *wh, const double *ub, const int *nX, int ndim) {
+  if (ndim == 1) {
+    int nx = nX[0] + 2;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+      weno_coeffs(wh + (long)i * N * V, V, ub + (long)i * V, V, nx, 0, i);
+    return 0;
+  }
+  int nx = nX[0] + 2, ny = nX[1] + 2;
+  int nyb = ny + 2 * (N - 1);
+  double *ux = malloc(sizeof(double) * (long)nx * nyb * N * V);
+  /* x sweep over every ub column (weno.cpp:93-104) */
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < nyb; j++) {
+    int gap = (j < N || j >= nyb - N) ? N : 0;
+    for (int i = 0; i < nx; i++)
+      weno_coeffs(ux + ((long)i * nyb + j) * N * V, V, ub + ((long)i * nyb + j) * V,
+                  (long)nyb * V, nx, gap, i);
+  }
+  /* y sweep per x node (weno.cpp:106-121) */
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nx; i++)
+    for (int ii = 0; ii < N; ii++) {
+      int gap = (i == 0 || i == nx - 1) ? 1 : 0;
+      for (int j = 0; j < ny; j++)
+        weno_coeffs(wh + (((long)i * ny + j) * N * N + ii * N) * V, V,
+                    ux + (((long)i * nyb + j) * N + ii) * V, (long)N * V, ny, gap, j);
+    }
+  free(ux);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Space-time DG predictor (solvers/dg/dg1.cpp, dg2.cpp).                   */
+
+/* rhs1 / rhs2: q, Ww and ret are [N time][N^d space][V]. */
+static void dg_rhs(int ndim, const double *q, const double *Ww, double dt,
+                   const double *dX, const gpr_par *P, double *ret) {
+  int ns = ndim == 1 ? N : N * N;
+  int nn = N * ns;
+  double *F = malloc(sizeof(double) * nn * V * 4);
+  double *G = F + nn * V, *dqx = G + nn * V, *dqy = dqx + nn * V;
+  memset(F, 0, sizeof(double) * nn * V * 2);
+  double dx = dX[0], dy = ndim == 2 ? dX[1] : 1.0;
+  /* spatial derivatives (dg1.cpp:31-32, evaluations.cpp:3-18) */
+  for (int t = 0; t < N; t++) {
+    if (ndim == 1) {
+      for (int i = 0; i < N; i++)
+        for (int k = 0; k < V; k++) {
+          double s = 0.0;
+          for (int m = 0; m < N; m++)
+            s += DERVALS[i][m] * q[((t * N) + m) * V + k];
+          dqx[(t * N + i) * V + k] = s / dx;
+        }
+    } else {
+      for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+          for (int k = 0; k < V; k++) {
+            double sx = 0.0, sy = 0.0;
+            for (int m = 0; m < N; m++) {
+              sx += DERVALS[i][m] * q[((t * N + m) * N + j) * V + k];
+              sy += DERVALS[j][m] * q[((t * N + i) * N + m) * V + k];
+            }
+            dqx[((t * N + i) * N + j) * V + k] = sx / dx;
+            dqy[((t * N + i) * N + j) * V + k] = sy / dy;
+          }
+    }
+  }
+  double tmp[MAXV], tmpy[MAXV];
+  for (int n = 0; n < nn; n++) {
+    const double *qn = q + n * V;
+    int t = n / ns, i = (n / (ndim == 1 ? 1 : N)) % N, j = n % N;
+    or_source(qn, P, ret + n * V);
+    or_Bdot(qn, dqx + n * V, 0, tmp);
+    if (ndim == 2)
+      or_Bdot(qn, dqy + n * V, 1, tmpy);
+    double w = ndim == 1 ? WGHTS[t] * WGHTS[i] : WGHTS[t] * WGHTS[i] * WGHTS[j];
+    for (int k = 0; k < V; k++) {
+      double r = ret[n * V + k] - (ndim == 2 ? tmp[k] + tmpy[k] : tmp[k]);
+      ret[n * V + k] = r * w;
+    }
+    or_flux(qn, 0, P, F + n * V);
+    if (ndim == 2)
+      or_flux(qn, 1, P, G + n * V);
+  }
+  if (ndim == 1) {
+    for (int t = 0; t < N; t++)
+      for (int i = 0; i < N; i++)
+        for (int k = 0; k < V; k++) {
+          double s = 0.0;
+          for (int m = 0; m < N; m++)
+            s += WGHTS[t] * DG_DER[i][m] * F[(t * N + m) * V + k];
+          ret[(t * N + i) * V + k] -= s / dx;
+        }
+  } else {
+    /* dg2.cpp:42-66 */
+    for (int t = 0; t < N; t++)
+      for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+          for (int k = 0; k < V; k++) {
+            double sx = 0.0, sy = 0.0;
+            for (int m = 0; m < N; m++) {
+              sx += WGHTS[t] * DG_DER[i][m] * (WGHTS[j] * F[((t * N + m) * N + j) * V + k]);
+              sy += DG_DER[j][m] * G[((t * N + i) * N + m) * V + k];
+            }
+            ret[((t * N + i) * N + j) * V + k] -= sx / dx;
+            ret[((t * N + i) * N + j) * V + k] -= WGHTS[t] * WGHTS[i] * sy / dy;
+          }
+  }
+  for (int n = 0; n < nn * V; n++)
+    ret[n] = ret[n] * dt + Ww[n];
+  free(F);
+}
+
+/* q = DG_U^{-1} r with DG_U = kron(DG_MAT, W [, W]) (etc/globals.cpp:46-50) */
+static void dg_solve(int ndim, const double *r, double *q) {
+  int ns = ndim == 1 ? N : N * N;
+  for (int s = 0; s < ns; s++) {
+    double ws = ndim == 1 ? WGHTS[s] : WGHTS[s / N] * WGHTS[s % N];
+    for (int t = 0; t < N; t++)
+      for (int k = 0; k < V; k++) {
+        double acc = 0.0;
+        for (int m = 0; m < N; m++)
+          acc += DG_MATinv[t][m] * r[(m * ns + s) * V + k];
+        q[(t * ns + s) * V + k] = acc / ws;
+      }
+  }
+}
+
+/* obj(q) = rhs(q) - DG_U q   (dg1.cpp:37-49, dg2.cpp:73-90) */
+static void dg_obj(int ndim, const double *q, const double *Ww, double dt,
+                   const double *dX, const gpr_par *P, double *out) {
+  int ns = ndim == 1 ? N : N * N;
+  dg_rhs(ndim, q, Ww, dt, dX, P, out);
+  for (int t = 0; t < N; t++)
+    for (int s = 0; s < ns; s++) {
+      double ws = ndim == 1 ? WGHTS[s] : WGHTS[s / N] * WGHTS[s % N];
+      for (int m = 0; m < N; m++)
+        for (int k = 0; k < V; k++)
+          out[(t * ns + s) * V + k] -= DG_MAT[t][m] * ws * q[(m * ns + s) * V + k];
+    }
+}
+
+/* Dense Newton on obj(q) = 0 with a finite-difference Jacobian: the
+ * oracle's check of the device Newton path for cells where the reference's
+ * Picard iteration does not converge.  Returns iterations or -1. */
+static int dg_newton(int ndim, double *q, const double *Ww, double dt,
+                     const double *dX, const gpr_par *P, double tol, int maxit) {
+  int ns = ndim == 1 ? N : N * N;
+  int n = N * ns * V;
+  double *J = malloc(sizeof(double) * ((long)n * n + 4 * n));
+  double *f = J + (long)n * n, *f2 = f + n, *qp = f2 + n, *dxv = qp + n;
+  int it;
+  for (it = 0; it < maxit; it++) {
+    dg_obj(ndim, q, Ww, dt, dX, P, f);
+    double fn = 0.0;
+    for (int i = 0; i < n; i++)
+      fn = fmax(fn, fabs(f[i]));
+    if (fn != fn)
+      break;
+    for (int c = 0; c < n; c++) {
+      memcpy(qp, q, sizeof(double) * n);
+      double h = 1e-7 * (1.0 + fabs(q[c]));
+      qp[c] += h;
+      dg_obj(ndim, qp, Ww, dt, dX, P, f2);
+      for (int r = 0; r < n; r++)
+        J[(long)r * n + c] = (f2[r] - f[r]) / h;
+    }
+    /* solve J dx = -f (partial pivoting) */
+    for (int r = 0; r < n; r++)
+      dxv[r] = -f[r];
+    int ok = 1;
+    for (int c = 0; c < n && ok; c++) {
+      int p = c;
+      for (int r = c + 1; r < n; r++)
+        if (fabs(J[(long)r * n + c]) > fabs(J[(long)p * n + c]))
+          p = r;
+      if (J[(long)p * n + c] == 0.0) {
+        ok = 0;
+        break;
+      }
+      if (p != c) {
+        for (int j = 0; j < n; j++) {
+          double t = J[(long)c * n + j];
+          J[(long)c * n + j] = J[(long)p * n + j];
+          J[(long)p * n + j] = t;
+        }
+        double t = dxv[c];
+        dxv[c] = dxv[p];
+        dxv[p] = t;
+      }
+      for (int r = c + 1; r < n; r++) {
+        double fct = J[(long)r * n + c] / J[(long)c * n + c];
+        if (fct == 0.0)
+          continue;
+        for (int j = c; j < n; j++)
+          J[(long)r * n + j] -= fct * J[(long)c * n + j];
+        dxv[r] -= fct * dxv[c];
+      }
+    }
+    if (!ok)
+      break;
+    for (int r = n - 1; r >= 0; r--) {
+      double s = dxv[r];
+      for (int j = r + 1; j < n; j++)
+        s -= J[(long)r * n + j] * dxv[j];
+      dxv[r] = s / J[(long)r * n + r];
+    }
+    int conv = 1;
+    for (int i = 0; i < n; i++) {
+      q[i] += dxv[i];
+      if (fabs(dxv[i]) > tol * (1 + fabs(q[i])))
+        conv = 0;
+    }
+    if (conv) {
+      free(J);
+      return it + 1;
+    }
+  }
+  free(J);
+  return -1;
+}
+
+/* predictor1 / predictor2 (dg1.cpp:75-131, dg2.cpp:102-171).  status[cell]
+ * receives: Picard iteration count (>0) when the reference's Picard
+ * converged; -(Newton iterations) - 1000 when Picard failed and the oracle's
+ * Newton solve converged; -1 when neither converged (row left unwritten, as
+ * the reference leaves it); 0 for masked-out cells. */
+int or_predictor(double *qh, const double *wh, double dt, const double *dX,
+                 int ndim, const int *nX, int stiff, const gpr_par *P,
+                 const uint8_t *mask, int *status, int newton_fallback) {
+  int ncell = ndim == 1 ? nX[0] + 2 : (nX[0] + 2) * (nX[1] + 2);
+  int ns = ndim == 1 ? N : N * N;
+  int nn = N * ns;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int c = 0; c < ncell; c++) {
+    if (status)
+      status[c] = 0;
+    if (!mask[c])
+      continue;
+    const double *w = wh + (long)c * ns * V;
+    double *qi = qh + (long)c * nn * V;
+    double Ww[2 * MAXN * MAXN * MAXN * MAXV];
+    double q0[2 * MAXN * MAXN * MAXN * MAXV], q1[2 * MAXN * MAXN * MAXN * MAXV],
+        r[2 * MAXN * MAXN * MAXN * MAXV];
+    /* initial_condition (dg1.cpp:68-73, dg2.cpp:92-100) */
+    for (int t = 0; t < N; t++)
+      for (int s = 0; s < ns; s++) {
+        double ws = ndim == 1 ? WGHTS[s] : WGHTS[s / N] * WGHTS[s % N];
+        for (int k = 0; k < V; k++)
+          Ww[(t * ns + s) * V + k] = ENDVALS[0][t] * ws * w[s * V + k];
+      }
+    /* standard_initial_guess (initial_guess.cpp:4-15) */
+    for (int t = 0; t < N; t++)
+      memcpy(q0 + t * ns * V, w, sizeof(double) * ns * V);
+    int done = 0, nan = 0;
+    if (!stiff) {
+      for (int count = 0; count < DG_IT; count++) {
+        dg_rhs(ndim, q0, Ww, dt, dX, P, r);
+        dg_solve(ndim, r, q1);
+        int big = 0, hasnan = 0;
+        for (int k = 0; k < nn * V; k++) {
+          if (fabs(q1[k] - q0[k]) > DG_TOL * (1 + fabs(q0[k])))
+            big = 1;
+          if (q1[k] != q1[k])
+            hasnan = 1;
+        }
+        if (big) {
+          memcpy(q0, q1, sizeof(double) * nn * V);
+          continue;
+        } else if (hasnan) {
+          nan = 1;
+          break;
+        } else {
+          memcpy(qi, q1, sizeof(double) * nn * V);
+          if (status)
+            status[c] = count + 1;
+          done = 1;
+          break;
+        }
+      }
+    }
+    if (!done && newton_fallback) {
+      for (int t = 0; t < N; t++)
+        memcpy(q0 + t * ns * V, w, sizeof(double) * ns * V);
+      int it = dg_newton(ndim, q0, Ww, dt, dX, P, 1e-12, 30);
+      if (it > 0) {
+        memcpy(qi, q0, sizeof(double) * nn * V);
+        if (status)
+          status[c] = -1000 - it;
+        done = 1;
+      }
+    }
+    if (!done && status)
+      status[c] = nan ? -2 : -1;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Finite-volume update (solvers/fv/fv.cpp).                               */
+
+static void centers_cell(double *ucell, const double *qh_t, int ndim, double dx,
+                         double dy, double wght_t, int SOURCES,
+                         const gpr_par *P) {
+  int ns = ndim == 1 ? N : N * N;
+  double S[MAXV], tmpx[MAXV], tmpy[MAXV], dqx[MAXV], dqy[MAXV];
+  for (int s = 0; s < ns; s++) {
+    const double *qs = qh_t + s * V;
+    int a = ndim == 1 ? s : s / N, b = ndim == 1 ? 0 : s % N;
+    for (int k = 0; k < V; k++) {
+      double sx = 0.0, sy = 0.0;
+      for (int m = 0; m < N; m++) {
+        if (ndim == 1)
+          sx += DERVALS[a][m] * qh_t[m * V + k];
+        else {
+          sx += DERVALS[a][m] * qh_t[(m * N + b) * V + k];
+          sy += DERVALS[b][m] * qh_t[(a * N + m) * V + k];
+        }
+      }
+      dqx[k] = sx;
+      dqy[k] = sy;
+    }
+    if (SOURCES)
+      or_source(qs, P, S);
+    else
+      for (int k = 0; k < V; k++)
+        S[k] = 0.0;
+    or_Bdot(qs, dqx, 0, tmpx);
+    if (ndim == 2)
+      or_Bdot(qs, dqy, 1, tmpy);
+    for (int k = 0; k < V; k++) {
+      S[k] -= tmpx[k] / dx;
+      if (ndim == 2)
+        S[k] -= tmpy[k] / dy;
+    }
+    double w = ndim == 1 ? wght_t * WGHTS[s] : wght_t * WGHTS[a] * WGHTS[b];
+    for (int k = 0; k < V; k++)
+      ucell[k] += w * S[k];
+  }
+}
+
+int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
+                   const double *dX, int ndim, int SOURCES, int TIME, int FLUX,
+                   const gpr_par *P, const uint8_t *mask) {
+  int nt = TIME ? N : 1;
+  int nx = nX[0], ny = ndim == 2 ? nX[1] : 1;
+  int ns = ndim == 1 ? N : N * N;
+  double dx = dX[0], dy = ndim == 2 ? dX[1] : 1.0;
+  long ncellb = ndim == 1 ? nx + 2 : (long)(nx + 2) * (ny + 2);
+  (void)ncellb;
+  /* centers (fv.cpp:11-109) */
+  for (int t = 0; t < nt; t++) {
+    double wt = TIME ? dt * WGHTS[t] : dt;
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < (long)nx * ny; c++) {
+      int i = ndim == 1 ? (int)c : (int)(c / ny), j = ndim == 1 ? 0 : (int)(c % ny);
+      long cb = ndim == 1 ? i + 1 : (long)(i + 1) * (ny + 2) + (j + 1);
+      if (!mask[cb])
+        continue;
+      const double *qt = qh + (cb * nt + t) * ns * V;
+      centers_cell(u + c * V, qt, ndim, dx, dy, wt, SOURCES, P);
+    }
+  }
+  /* interfaces (fv.cpp:111-279): fluxes per face computed in parallel,
+   * then applied in the reference's order. */
+  double ENDL[MAXN], ENDR[MAXN];
+  for (int m = 0; m < N; m++) {
+    ENDL[m] = ENDVALS[1][m];
+    ENDR[m] = ENDVALS[0][m];
+  }
+  if (ndim == 1) {
+    double *fb = malloc(sizeof(double) * (nx + 1) * 2 * V);
+    for (int t = 0; t < nt; t++) {
+      double wt = TIME ? dt * WGHTS[t] : dt;
+      double kk = wt / (2.0 * dx);
+#pragma omp parallel for schedule(static)
+      for (int i = 0; i < nx + 1; i++) {
+        double *f = fb + (long)i * 2 * V, *b = f + V;
+        if (!(mask[i] && mask[i + 1]))
+          continue;
+        const double *qhl = qh + ((long)i * nt + t) * N * V;
+        const double *qhr = qh + ((long)(i + 1) * nt + t) * N * V;
+        double ql[MAXV], qr[MAXV];
+        for (int k = 0; k < V; k++) {
+          double sl = 0, sr = 0;
+          for (int m = 0; m < N; m++) {
+            sl += ENDL[m] * qhl[m * V + k];
+            sr += ENDR[m] * qhr[m * V + k];
+          }
+          ql[k] = sl;
+          qr[k] = sr;
+        }
+        interface_D(FLUX, ql, qr, 0, P, f);
+        or_Bint(ql, qr, 0, b);
+      }
+      for (int i = 0; i < nx + 1; i++) {
+        if (!(mask[i] && mask[i + 1]))
+          continue;
+        const double *f = fb + (long)i * 2 * V, *b = f + V;
+        if (i > 0)
+          for (int k = 0; k < V; k++)
+            u[(long)(i - 1) * V + k] -= kk * (b[k] + f[k]);
+        if (i < nx)
+          for (int k = 0; k < V; k++)
+            u[(long)i * V + k] -= kk * (b[k] - f[k]);
+      }
+    }
+    free(fb);
+    return 0;
+  }
+  /* 2D (fv.cpp:162-268): per face (i,j) of the (nx+1)x(ny+1) grid; the x
+   * face sits between predictor cells (i,j) and (i+1,j), the y face between
+   * (i,j) and (i,j+1). */
+  long nfx = (long)(nx + 1) * (ny + 1);
+  double *fx = malloc(sizeof(double) * nfx * 4 * V);
+  for (int t = 0; t < nt; t++) {
+    double wt = TIME ? dt * WGHTS[t] : dt;
+    double xW[MAXN], yW[MAXN];
+    for (int s = 0; s < N; s++) {
+      xW[s] = wt / (2. * dx) * WGHTS[s];
+      yW[s] = wt / (2. * dy) * WGHTS[s];
+    }
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < nfx; c++) {
+      int i = (int)(c / (ny + 1)), j = (int)(c % (ny + 1));
+      double *ux0 = fx + c * 4 * V, *ux1 = ux0 + V, *uy0 = ux1 + V, *uy1 = uy0 + V;
+      for (int k = 0; k < 4 * V; k++)
+        ux0[k] = 0.0;
+      long cb = (long)i * (ny + 2) + j;
+      if (!mask[cb])
+        continue;
+      const double *qh0 = qh + (cb * nt + t) * N * N * V;
+      double q0[MAXV], q1[MAXV], f[MAXV], b[MAXV];
+      if (mask[cb + (ny + 2)] && j > 0) {
+        const double *qhx = qh + ((cb + (ny + 2)) * nt + t) * N * N * V;
+        for (int s = 0; s < N; s++) {
+          for (int k = 0; k < V; k++) {
+            double s0 = 0, s1 = 0;
+            for (int m = 0; m < N; m++) {
+              s0 += ENDVALS[1][m] * qh0[(m * N + s) * V + k];
+              s1 += ENDVALS[0][m] * qhx[(m * N + s) * V + k];
+            }
+            q0[k] = s0;
+            q1[k] = s1;
+          }
+          interface_D(FLUX, q0, q1, 0, P, f);
+          or_Bint(q0, q1, 0, b);
+          for (int k = 0; k < V; k++) {
+            ux0[k] += xW[s] * (b[k] + f[k]);
+            ux1[k] += xW[s] * (b[k] - f[k]);
+          }
+        }
+      }
+      if (mask[cb + 1] && i > 0) {
+        const double *qhy = qh + ((cb + 1) * nt + t) * N * N * V;
+        for (int s = 0; s < N; s++) {
+          for (int k = 0; k < V; k++) {
+            double s0 = 0, s1 = 0;
+            for (int m = 0; m < N; m++) {
+              s0 += ENDVALS[1][m] * qh0[(s * N + m) * V + k];
+              s1 += ENDVALS[0][m] * qhy[(s * N + m) * V + k];
+            }
+            q0[k] = s0;
+            q1[k] = s1;
+          }
+          interface_D(FLUX, q0, q1, 1, P, f);
+          or_Bint(q0, q1, 1, b);
+          for (int k = 0; k < V; k++) {
+            uy0[k] += yW[s] * (b[k] + f[k]);
+            uy1[k] += yW[s] * (b[k] - f[k]);
+          }
+        }
+      }
+    }
+    for (long c = 0; c < nfx; c++) {
+      int i = (int)(c / (ny + 1)), j = (int)(c % (ny + 1));
+      long cb = (long)i * (ny + 2) + j;
+      if (!mask[cb])
+        continue;
+      const double *ux0 = fx + c * 4 * V, *ux1 = ux0 + V, *uy0 = ux1 + V, *uy1 = uy0 + V;
+      long uind0 = ((long)(i - 1) * ny + (j - 1)) * V;
+      if (mask[cb + (ny + 2)] && j > 0) {
+        long uindx = ((long)i * ny + (j - 1)) * V;
+        if (i > 0)
+          for (int k = 0; k < V; k++)
+            u[uind0 + k] -= ux0[k];
+        if (i < nx)
+          for (int k = 0; k < V; k++)
+            u[uindx + k] -= ux1[k];
+      }
+      if (mask[cb + 1] && i > 0) {
+        long uindy = ((long)(i - 1) * ny + j) * V;
+        if (j > 0)
+          for (int k = 0; k < V; k++)
+            u[uind0 + k] -= uy0[k];
+        if (j < ny)
+          for (int k = 0; k < V; k++)
+            u[uindy + k] -= uy1[k];
+      }
+    }
+  }
+  free(fx);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* CFL time step, distortion housekeeping (solvers/iterator.cpp:148-177,    */
+/* solvers/utils.cpp:6-23).                                                  */
+
+double or_timestep(const double *u, long ncell, const double *dX, int ndim,
+                   double CFL, double t, double tf, int count, const gpr_par *P) {
+  double MAX = 0.0;
+#pragma omp parallel for reduction(max : MAX) schedule(static)
+  for (long c = 0; c < ncell; c++) {
+    double tmp = 0.0;
+    for (int d = 0; d < ndim; d++)
+      tmp += or_max_abs_eigs(u + c * V, d, P) / dX[d];
+    if (tmp > MAX) /* NaN cells are skipped, as std::max(MAX, NaN) does */
+      MAX = tmp;
+  }
+  double dt = CFL / MAX;
+  if (count <= 5)
+    dt *= 0.2;
+  if (t + dt > tf)
+    return tf - t;
+  return dt;
+}
+
+void or_renorm_distortion(double *u, long ncell, const gpr_par *P) {
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < ncell; c++) {
+    double *Q = u + c * V;
+    double r = Q[0];
+    if (r > 0) {
+      double cc = cbrt(r / (P->rho0 * det3(Q + 5)));
+      for (int k = 5; k < 14; k++)
+        Q[k] *= cc;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Split stiff-source ODE step (system/relaxation/analytic.cpp).           */
+
+/* Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations: S = W D W^T
+ * (columns of W are eigenvectors). */
+static void jacobi3(double S[3][3], double Wm[3][3], double d[3]) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      Wm[i][j] = i == j;
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = fabs(S[0][1]) + fabs(S[0][2]) + fabs(S[1][2]);
+    if (off == 0.0)
+      break;
+    for (int p = 0; p < 2; p++)
+      for (int q = p + 1; q < 3; q++) {
+        if (S[p][q] == 0.0)
+          continue;
+        double theta = (S[q][q] - S[p][p]) / (2 * S[p][q]);
+        double t = (theta >= 0 ? 1 : -1) / (fabs(theta) + sqrt(theta * theta + 1));
+        double c = 1 / sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < 3; k++) {
+          double a = S[k][p], b = S[k][q];
+          S[k][p] = c * a - s * b;
+          S[k][q] = s * a + c * b;
+        }
+        for (int k = 0; k < 3; k++) {
+          double a = S[p][k], b = S[q][k];
+          S[p][k] = c * a - s * b;
+          S[q][k] = s * a + c * b;
+        }
+        for (int k = 0; k < 3; k++) {
+          double a = Wm[k][p], b = Wm[k][q];
+          Wm[k][p] = c * a - s * b;
+          Wm[k][q] = s * a + c * b;
+        }
+      }
+  }
+  for (int i = 0; i < 3; i++)
+    d[i] = S[i][i];
+}
+
+/* SVD of a 3x3 (row-major) A = U diag(s) V^T, s descending, via the Jacobi
+ * eigen-decomposition of A^T A; U = A V / s (re-orthogonalised). */
+static void svd3(const double *A, double U[3][3], double s[3], double Vm[3][3]) {
+  double S[3][3], W[3][3], d[3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      S[i][j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  jacobi3(S, W, d);
+  int idx[3] = {0, 1, 2};
+  for (int a = 0; a < 3; a++)
+    for (int b = a + 1; b < 3; b++)
+      if (d[idx[b]] > d[idx[a]]) {
+        int t = idx[a];
+        idx[a] = idx[b];
+        idx[b] = t;
+      }
+  for (int c = 0; c < 3; c++) {
+    s[c] = sqrt(fmax(d[idx[c]], 0.0));
+    for (int r = 0; r < 3; r++)
+      Vm[r][c] = W[r][idx[c]];
+  }
+  /* U columns: A v_c / s_c, Gram-Schmidt for stability */
+  for (int c = 0; c < 3; c++) {
+    double x[3];
+    for (int r = 0; r < 3; r++)
+      x[r] = A[3 * r] * Vm[0][c] + A[3 * r + 1] * Vm[1][c] + A[3 * r + 2] * Vm[2][c];
+    for (int p = 0; p < c; p++) {
+      double dp = x[0] * U[0][p] + x[1] * U[1][p] + x[2] * U[2][p];
+      for (int r = 0; r < 3; r++)
+        x[r] -= dp * U[r][p];
+    }
+    double nrm = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    for (int r = 0; r < 3; r++)
+      U[r][c] = x[r] / nrm;
+  }
+}
+
+static double posd(double x) { return x > 0 ? x : 0.0; }
+
+/* nondimensionalized_time (analytic.cpp:17-69) */
+static double nondim_time(double r, double detA3, double m0, double u0,
+                          double dt, const gpr_par *P) {
+  if (P->flags & GPR_POWER_LAW) {
+    double n = P->n;
+    double cs2 = c_s2(r, P);
+    double a = 9. * m0 - u0 - 9.;
+    double b = 6. * m0 - u0 - 6.;
+    double c, lam, tmp1, tmp2;
+    if (P->flags & GPR_SOLID) {
+      c = (108. * a - 324. * b + 108. * a * a - 396. * a * b + 297. * b * b -
+           24. * (a * a * b - 2. * a * b * b + b * b * b) - 4. * pow(a - b, 4.));
+      if (c <= 0.)
+        return 0.;
+      lam = c / (18. * a - 36. * b + 9. * a * a - 132. / 5. * a * b +
+                 33. / 2. * b * b - 8. / 7. * a * a * b + 2. * a * b * b -
+                 8. / 9. * b * b * b - pow(a, 4.) / 6. + 16. / 27. * a * a * a * b -
+                 4. / 5. * a * a * b * b + 16. / 33. * a * b * b * b - pow(b, 4.) / 9.);
+      tmp1 = n * lam / P->tau0 * pow(detA3, 4. * n + 7.);
+      tmp2 = pow(sqrt(c) * r * cs2 / (6. * P->sigmaY), n);
+      return 2. / (n * lam) * log(tmp1 * tmp2 * dt + 1.);
+    } else {
+      double k = (1 - n) / n;
+      c = (108. * a - 324. * b + 180. * a * a - 612. * a * b + 459. * b * b -
+           24. * (a * a * b - 2. * a * b * b + b * b * b) - 4. * pow(a - b, 4.));
+      if (c <= 0.)
+        return 0.;
+      lam = c / (18. * a - 36. * b + 15. * a * a - 204. / 5. * a * b +
+                 51. / 2. * b * b - 8. / 7. * a * a * b + 2. * a * b * b -
+                 8. / 9. * b * b * b - pow(a, 4.) / 6. + 16. / 27. * a * a * a * b -
+                 4. / 5. * a * a * b * b + 16. / 33. * a * b * b * b - pow(b, 4.) / 9.);
+      double tau1 = 6 * pow(P->mu, 1. / n) / (P->rho0 * P->b02);
+      tmp1 = k * lam / tau1 * pow(detA3, 4. * k + 7.);
+      tmp2 = pow(sqrt(c) * r * cs2 / (6. * sqrt(3.)), k);
+      return 2. / (k * lam) * log(tmp1 * tmp2 * dt + 1.);
+    }
+  }
+  return P->rho0 * P->b02 * pow(detA3, 7.) / (3. * P->mu) * dt;
+}
+
+/* analyticSolver_distortion (analytic.cpp:71-128) */
+static void ode_distortion(double *Q, double dt, const gpr_par *P) {
+  double *A = Q + 5;
+  double U[3][3], s[3], Vm[3][3];
+  svd3(A, U, s, Vm);
+  double detA = s[0] * s[1] * s[2];
+  double r = detA * P->rho0;
+  double detA1_3 = cbrt(detA);
+  double detA2_3 = detA1_3 * detA1_3;
+  double s0 = s[0] * s[0] / detA2_3;
+  double s1 = s[1] * s[1] / detA2_3;
+  double s2 = s[2] * s[2] / detA2_3;
+  double m0 = (s0 + s1 + s2) / 3.;
+  double u0 = ((s0 - s1) * (s0 - s1) + (s1 - s2) * (s1 - s2) + (s2 - s0) * (s2 - s0)) / 3.;
+  if (u0 < 1e-12)
+    return;
+  double tau = nondim_time(r, detA1_3, m0, u0, dt, P);
+  double e6 = exp(-6. * tau), e9 = exp(-9. * tau);
+  double a = 3. * m0 - u0 / 3. - 3.;
+  double b = 2. * m0 - u0 / 3. - 2.;
+  double m = 1. + a * e6 - b * e9;
+  double u = posd(6. * a * e6 - 9. * b * e9);
+  double Dl = -2. * m * m * m + m * u + 2.;
+  double arg1 = posd(6. * u * u * u - 81. * Dl * Dl);
+  double x1;
+  if (fabs(Dl) < 1e-12)
+    x1 = sqrt(6. * u) / 3. * cos(M_PI / 6.) + m;
+  else if (arg1 == 0.) {
+    double tmp = cbrt(54. * Dl);
+    x1 = tmp / 6. + u / tmp + m;
+  } else {
+    double th = atan(sqrt(arg1) / (9. * Dl));
+    x1 = sqrt(6. * u) / 3. * cos(th / 3.) + m;
+  }
+  double tmp2 = 3. * m - x1;
+  double arg2 = posd(x1 * tmp2 * tmp2 - 4.);
+  double x2 = 0.5 * (sqrt(arg2 / x1) + tmp2);
+  double x3 = 1. / (x1 * x2);
+  double x[3] = {x1, x2, x3};
+  for (int i = 0; i < 3; i++)
+    for (int j = i + 1; j < 3; j++)
+      if (x[j] < x[i]) {
+        double t = x[i];
+        x[i] = x[j];
+        x[j] = t;
+      }
+  /* A = U diag(detA^1/3 sqrt(x[2-i])) V^T */
+  double sc[3];
+  for (int i = 0; i < 3; i++)
+    sc[i] = detA1_3 * sqrt(x[2 - i]);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double acc = 0.0;
+      for (int k = 0; k < 3; k++)
+        acc += U[i][k] * sc[k] * Vm[j][k];
+      A[3 * i + j] = acc;
+    }
+}
+
+/* analyticSolver_thermal (analytic.cpp:130-150) */
+static void ode_thermal(double *Q, double dt, const gpr_par *P) {
+  double r = Q[0];
+  double E = Q[1] / r;
+  double v0 = Q[2] / r, v1 = Q[3] / r, v2 = Q[4] / r;
+  double c1 = E - E_2A(r, Q + 5, P) - (v0 * v0 + v1 * v1 + v2 * v2) / 2;
+  double c2 = P->calpha2 / 2.;
+  double k = 2 * P->calpha2 / (P->kappa * r * P->cv);
+  c1 *= k;
+  c2 *= k;
+  double ea = exp(-c1 * dt / 2);
+  double J2 = Q[14] * Q[14] + Q[15] * Q[15] + Q[16] * Q[16];
+  double den = 1 - c2 / c1 * (1 - ea * ea) * J2 / (r * r);
+  double f = ea / sqrt(den);
+  Q[14] *= f;
+  Q[15] *= f;
+  Q[16] *= f;
+}
+
+void or_ode_cell(double *Q, double dt, const gpr_par *P) {
+  Q[2] += P->dp[0] * dt;
+  Q[3] += P->dp[1] * dt;
+  Q[4] += P->dp[2] * dt;
+  ode_distortion(Q, dt, P);
+  if (THERMAL)
+    ode_thermal(Q, dt, P);
+}
+
+void or_ode_launcher(double *u, long ncell, double dt, const gpr_par *P) {
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < ncell; c++)
+    or_ode_cell(u + c * V, dt, P);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Steppers (solvers/steppers.cpp:10-66, split/homogeneous.cpp:5-67).       */
+
+int or_ader_stepper(double *u, const double *ub, const int *nX, int ndim,
+                    double dt, const double *dX, int stiff, int FLUX,
+                    const gpr_par *P, const uint8_t *mask, int *status,
+                    int newton_fallback) {
+  long ncb = ndim == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+  int ns = ndim == 1 ? N : N * N;
+  double *wh = malloc(sizeof(double) * ncb * ns * V);
+  double *qh = malloc(sizeof(double) * ncb * N * ns * V);
+  for (long k = 0; k < ncb * N * ns * V; k++)
+    qh[k] = NAN;
+  or_weno_launcher(wh, ub, nX, ndim);
+  or_predictor(qh, wh, dt, dX, ndim, nX, stiff, P, mask, status, newton_fallback);
+  or_fv_launcher(u, qh, nX, dt, dX, ndim, 1, 1, FLUX, P, mask);
+  free(wh);
+  free(qh);
+  return 0;
+}
+
+/* midstepper (split/homogeneous.cpp:5-67) */
+int or_midstepper(double *wh, double dt, const double *dX, int ndim,
+                  const gpr_par *P, const uint8_t *mask, long ncell) {
+  int ns = ndim == 1 ? N : N * N;
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < ncell; c++) {
+    if (!mask[c])
+      continue;
+    double *w = wh + c * ns * V;
+    double F[MAXN * MAXN * MAXV], G[MAXN * MAXN * MAXV], dwx[MAXN * MAXN * MAXV],
+        dwy[MAXN * MAXN * MAXV], dFx[MAXN * MAXN * MAXV], dGy[MAXN * MAXN * MAXV];
+    memset(F, 0, sizeof F);
+    memset(G, 0, sizeof G);
+    for (int s = 0; s < ns; s++) {
+      or_flux(w + s * V, 0, P, F + s * V);
+      if (ndim == 2)
+        or_flux(w + s * V, 1, P, G + s * V);
+    }
+    for (int s = 0; s < ns; s++) {
+      int a = ndim == 1 ? s : s / N, b = ndim == 1 ? 0 : s % N;
+      for (int k = 0; k < V; k++) {
+        double sx = 0, sf = 0, sy = 0, sg = 0;
+        for (int m = 0; m < N; m++) {
+          int ix = ndim == 1 ? m : m * N + b;
+          sx += DERVALS[a][m] * w[ix * V + k];
+          sf += DERVALS[a][m] * F[ix * V + k];
+          if (ndim == 2) {
+            int iy = a * N + m;
+            sy += DERVALS[b][m] * w[iy * V + k];
+            sg += DERVALS[b][m] * G[iy * V + k];
+          }
+        }
+        dwx[s * V + k] = sx;
+        dFx[s * V + k] = sf;
+        dwy[s * V + k] = sy;
+        dGy[s * V + k] = sg;
+      }
+    }
+    double Bx[MAXV], By[MAXV];
+    for (int s = 0; s < ns; s++) {
+      or_Bdot(w + s * V, dwx + s * V, 0, Bx);
+      if (ndim == 2)
+        or_Bdot(w + s * V, dwy + s * V, 1, By);
+      for (int k = 0; k < V; k++) {
+        double inc = (dFx[s * V + k] + Bx[k]) / dX[0];
+        if (ndim == 2)
+          inc += (dGy[s * V + k] + By[k]) / dX[1];
+        w[s * V + k] -= dt / 2 * inc;
+      }
+    }
+  }
+  return 0;
+}
+
+/* split_stepper (steppers.cpp:50-66); ub is modified (ODE half step). */
+int or_split_stepper(double *u, double *ub, const int *nX, int ndim, double dt,
+                     const double *dX, int HALF_STEP, int FLUX, const gpr_par *P,
+                     const uint8_t *mask) {
+  long nc = ndim == 1 ? nX[0] : (long)nX[0] * nX[1];
+  long ncb = ndim == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+  long nub = ndim == 1 ? nX[0] + 2 * N : (long)(nX[0] + 2 * N) * (nX[1] + 2 * N);
+  int ns = ndim == 1 ? N : N * N;
+  or_ode_launcher(u, nc, dt / 2, P);
+  or_ode_launcher(ub, nub, dt / 2, P);
+  double *wh = malloc(sizeof(double) * ncb * ns * V);
+  or_weno_launcher(wh, ub, nX, ndim);
+  if (HALF_STEP)
+    or_midstepper(wh, dt, dX, ndim, P, mask, ncb);
+  or_fv_launcher(u, wh, nX, dt, dX, ndim, 0, 0, FLUX, P, mask);
+  or_ode_launcher(u, nc, dt / 2, P);
+  free(wh);
+  return 0;
+}
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void or_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0)
+    omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
