@@ -1,0 +1,491 @@
+"""Benchmark of the GB300 GPR ADER-WENO step.
+
+Workload: 2D Taylor-Green vortex, 512 x 512 cells on [0, 2pi]^2, V = 17
+(viscous + heat conduction), FP64, N = 2, Rusanov flux, periodic boundaries,
+cs = 10, mu = 1e-2.  A step is one full time step of the reference's
+iterator for one material: CFL time step -> boundaries -> WENO -> space-time
+predictor -> FV update -> distortion renormalisation, device resident (dt
+never leaves the GPU).  Metric: cell-updates per second (one interior cell
+advanced one time step), whole job.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU oracle (a C restatement of the reference
+solver; the reference's own C++ cannot be built on the GPU host) on the host
+cores, on a 512 x 64 strip of the same problem (same cell size and time
+step), and prints its own JSON line.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 Mcell-updates/s (TGV 512^2 ADER-WENO step)"
+UNIT = "Mcell-updates/s"
+
+# Algorithmic FP64 operation counts per unit of work, counted by
+# oracle/opcount.cpp on the oracle's restatement of the reference
+# (add/sub/mul/div/sqrt = 1 flop, each transcendental call = 1), 2D, V = 17.
+# Filled from profiles/opcount_tgv.txt.
+OPS = {
+    "predictor_per_cell_iter": 12310.4,   # per predictor cell and Picard iteration
+    "face_quadrature_point": 3787.2,      # D_RUS + Bint + extrapolation, per point
+    "cells_per_cell": 4202.0,             # volume term (both time nodes), per cell
+    "weno_per_cell": 3193.5,              # per predictor cell (both sweeps)
+    "cfl_per_cell": 2958.4,               # per cell (two max_abs_eigs)
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--cfl", type=float, default=0.4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="run only this many steps (for ncu captures), no JSON")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline / reference arm
+
+def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0):
+    """Oracle (C restatement of the reference solver) on all host cores, on
+    an n x strip slice of the TGV (same dx, dy, time step)."""
+    from oracle import Oracle
+    from phd_gb300 import problems
+    O = Oracle()
+    threads = O.num_threads()
+    u0, MP, tf, dX, bcs = problems.taylor_green(n=n, cs=10.0, mu=1e-2)
+    u = np.ascontiguousarray(u0[:, :strip, :]).copy()
+    nX = np.array([n, strip], np.int32)
+    ncell = n * strip
+    count = 0
+    for _ in range(warmup):
+        dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
+        ub = O.boundaries(u, nX, [1] * 4)
+        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP)
+        O.renorm_distortion(u.reshape(-1), MP)
+        count += 1
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(steps):
+        dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
+        ub = O.boundaries(u, nX, [1] * 4)
+        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP)
+        O.renorm_distortion(u.reshape(-1), MP)
+        count += 1
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    value = ncell * done / el / 1e6
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "TGV %dx%d strip (same dx, dt as %dx%d), %d steps after %d warm-up, "
+                      "oracle/gpr_oracle.c with %d OpenMP threads" % (n, strip, n, n, done,
+                                                                       warmup, threads),
+            "seconds": el}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(args.steps, args.warmup, n=args.n, cfl=args.cfl, budget_s=120.0)
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "tgv2d_512x512_v17_rusanov_cfl%.2g" % args.cfl,
+                       "grid": [args.n, args.n], "nvar": 17, "order_N": 2,
+                       "parallelism": "cpu"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# FP64 peak microbenchmark (own kernel): independent DFMA chains
+
+FP64_PEAK_SRC = r"""
+#include <cuda_runtime.h>
+__global__ void dfma_peak(double *out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+  double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const double b = 0.999999999, c = 1e-12;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+      a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+  }
+  double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[0] = s;
+}
+extern "C" int dfma_peak_launch(double *out, int iters, int grid, int block, void *stream) {
+  dfma_peak<<<grid, block, 0, (cudaStream_t)stream>>>(out, iters);
+  return (int)cudaGetLastError();
+}
+"""
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s, 2 flops per DFMA),
+    from an own kernel of independent DFMA chains."""
+    from phd_gb300 import _lib
+    bdir = os.path.join(ROOT, "phd_gb300", "_build")
+    so = os.path.join(bdir, "fp64peak.so")
+    src = os.path.join(bdir, "fp64peak.cu")
+    os.makedirs(bdir, exist_ok=True)
+    if not os.path.exists(so):
+        open(src, "w").write(FP64_PEAK_SRC)
+        subprocess.run(["nvcc"] + _lib.ARCH + ["-O3", "-shared", "-Xcompiler", "-fPIC", "-o",
+                                               so, src], check=True)
+    lib = ctypes.CDLL(so)
+    lib.dfma_peak_launch.restype = ctypes.c_int
+    lib.dfma_peak_launch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_void_p]
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    iters = 2048
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    grid, block = sms * 8, 256
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    po = ctypes.c_void_p(out.data_ptr())
+    assert lib.dfma_peak_launch(po, iters, grid, block, stream) == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        lib.dfma_peak_launch(po, iters, grid, block, stream)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        flops = 2.0 * 8 * 16 * iters * grid * block
+        best = max(best, flops / (ms * 1e-3) / 1e12)
+    return best
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+
+def run_gb300(args):
+    import torch
+    import phd_gb300 as G
+    from phd_gb300 import _lib, api
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    lib = _lib.load()
+
+    n = args.n
+    u0, MP, tf, dX, bcs = G.problems.taylor_green(n=n, cs=10.0, mu=1e-2)
+    V = 17
+    nX = np.array([n, n], np.int32)
+    ncell = n * n
+    pn = nX.ctypes.data_as(ctypes.c_void_p)
+    dXa = np.array(dX, dtype=np.float64)
+    pd = dXa.ctypes.data_as(ctypes.c_void_p)
+    bc = np.array([1, 1, 1, 1], np.int32)
+    pb = bc.ctypes.data_as(ctypes.c_void_p)
+    cpar = MP.to_ctypes()
+    pp = ctypes.cast(ctypes.pointer(cpar), ctypes.c_void_p)
+
+    u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device=dev)
+    nscr = lib.gpr_iterate_scratch_doubles(pn, 2, V)
+    scratch = torch.empty(nscr, dtype=torch.float64, device=dev)
+    status = torch.zeros((n + 2) * (n + 2), dtype=torch.int32, device=dev)
+    clock = torch.tensor([0.0, 0.0, 1e9, args.cfl, 0.0], dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step(k=1, uu=None):
+        uu = u if uu is None else uu
+        _lib.check(lib.gpr_iterate(ctypes.c_void_p(uu.data_ptr()), pn, 2, pd, pb, 0, pp, None,
+                                   ctypes.c_void_p(clock.data_ptr()), k,
+                                   ctypes.c_void_p(scratch.data_ptr()),
+                                   ctypes.c_void_p(status.data_ptr()), V, sp), "iterate")
+
+    if args.profile_steps:
+        for _ in range(args.profile_steps):
+            step()
+        torch.cuda.synchronize()
+        return 0
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as cs:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_per_step = ms / args.steps
+    value = ncell * world * args.steps / (ms * 1e-3) / 1e6
+    st = status.cpu().numpy()
+    iters = (st >> 8)
+    picard_ok = (st & 0xff) == 0
+    hist = np.bincount(iters[picard_ok], minlength=1).tolist()
+    mean_iters = float(iters[picard_ok].mean()) if picard_ok.any() else float("nan")
+    failed = int((~picard_ok).sum())
+    clk = clock.cpu().numpy()
+
+    # stage timing (CUDA events on the launching stream) for the roofline
+    stage_ms = stage_times(lib, torch, u, MP, nX, dXa, bc, args.cfl, V, dev, sp, stream)
+
+    # end-to-end through the C ABI with host buffers: H2D of the state,
+    # one step, D2H of the state, every step
+    host = torch.empty(ncell * V, dtype=torch.float64, pin_memory=True)
+    host.copy_(u.cpu())
+    ue = torch.empty_like(u)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    for _ in range(args.steps):
+        ue.copy_(host, non_blocking=True)
+        step(uu=ue)
+        host.copy_(ue, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = f0.elapsed_time(f1)
+    e2e_value = ncell * world * args.steps / (e2e_ms * 1e-3) / 1e6
+
+    peak = None
+    try:
+        peak = fp64_peak_tflops(torch)
+    except Exception as ex:  # report, do not hide
+        peak_err = str(ex)
+    else:
+        peak_err = None
+
+    roof = roofline(stage_ms, ncell, n, mean_iters, peak)
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tgv2d_512x512_v17_rusanov_cfl%.2g" % args.cfl,
+                       "grid": [n, n], "nvar": 17, "order_N": 2, "flux": "rusanov",
+                       "cfl": args.cfl, "material": "sg gamma=1.4 cv=2.5 cs=10 mu=1e-2 "
+                                                    "calpha=1 Pr=2/3",
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "per-step working set (u, ub, wh, qh: ~0.5 GB) exceeds the "
+                             "129 MB L2; no flush needed"},
+            "predictor": {"picard_iteration_histogram": hist,
+                          "mean_picard_iterations": mean_iters, "picard_failed_cells": failed},
+            "sim_time": float(clk[0]), "sim_steps": int(clk[4]),
+            "stage_ms": stage_ms,
+            "roofline": roof,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ncell * V * 8,
+                    "d2h_bytes_per_step": ncell * V * 8},
+            "gpu_launches": 14 * args.steps,
+            "clocks": cs.summary()}
+    if peak_err:
+        line["roofline"]["peak_error"] = peak_err
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(3, 1, n=n, cfl=args.cfl, budget_s=20.0)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def stage_times(lib, torch, u, MP, nX, dXa, bc, cfl, V, dev, sp, stream, reps=3):
+    """Average device time of each stage of a step, CUDA events on the
+    launching stream."""
+    from phd_gb300 import _lib
+    pn = nX.ctypes.data_as(ctypes.c_void_p)
+    pd = dXa.ctypes.data_as(ctypes.c_void_p)
+    pb = bc.ctypes.data_as(ctypes.c_void_p)
+    cpar = MP.to_ctypes()
+    pp = ctypes.cast(ctypes.pointer(cpar), ctypes.c_void_p)
+    n0, n1 = int(nX[0]), int(nX[1])
+    ncell = n0 * n1
+    ncb = (n0 + 2) * (n1 + 2)
+    uu = u.clone()
+    ub = torch.empty((n0 + 4) * (n1 + 4) * V, dtype=torch.float64, device=dev)
+    wh = torch.empty(ncb * 4 * V, dtype=torch.float64, device=dev)
+    qh = torch.empty(ncb * 8 * V, dtype=torch.float64, device=dev)
+    ws = torch.empty(max(lib.gpr_weno_scratch_doubles(pn, 2, V),
+                         lib.gpr_fv_scratch_doubles(pn, 2, V)), dtype=torch.float64, device=dev)
+    dtd = torch.empty(1, dtype=torch.float64, device=dev)
+    tsc = torch.empty(1, dtype=torch.float64, device=dev)
+    st = torch.zeros(ncb, dtype=torch.int32, device=dev)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    names = ["cfl", "boundaries", "weno", "predictor", "fv", "renorm"]
+    acc = {k: 0.0 for k in names}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+    for r in range(reps + 1):
+        ev[0].record(stream)
+        _lib.check(lib.gpr_timestep(P(uu), ncell, pd, 2, cfl, 0.0, 1e9, 10, pp, P(dtd), P(tsc),
+                                    V, sp), "timestep")
+        ev[1].record(stream)
+        dt = float(dtd.item())
+        ev[1].record(stream)
+        _lib.check(lib.gpr_boundaries(P(uu), P(ub), pn, 2, pb, V, sp), "bc")
+        ev[2].record(stream)
+        _lib.check(lib.gpr_weno_launcher(P(wh), P(ub), pn, 2, P(ws), V, sp), "weno")
+        ev[3].record(stream)
+        _lib.check(lib.gpr_predictor(P(qh), P(wh), dt, pd, 2, pn, 0, pp, None, P(st), V, sp),
+                   "pred")
+        ev[4].record(stream)
+        _lib.check(lib.gpr_fv_launcher(P(uu), P(qh), pn, dt, pd, 2, 1, 1, 0, pp, None, P(ws),
+                                       V, sp), "fv")
+        ev[5].record(stream)
+        _lib.check(lib.gpr_renorm_distortion(P(uu), ncell, pp, V, sp), "renorm")
+        ev[6].record(stream)
+        torch.cuda.synchronize()
+        if r == 0:
+            continue
+        for i, k in enumerate(names):
+            if k == "cfl":
+                continue
+            acc[k] += ev[i].elapsed_time(ev[i + 1]) / reps
+    # the CFL stage alone (its events straddle a host read above)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        lib.gpr_timestep(P(uu), ncell, pd, 2, cfl, 0.0, 1e9, 10, pp, P(dtd), P(tsc), V, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    acc["cfl"] = e0.elapsed_time(e1) / reps
+    acc["_mean_picard_iterations_stage_run"] = float((st.cpu().numpy() >> 8).mean())
+    return acc
+
+
+def roofline(stage_ms, ncell, n, mean_iters, peak):
+    """Roofline of the dominant stage against the measured FP64 peak."""
+    stages = {k: v for k, v in stage_ms.items() if not k.startswith("_")}
+    dom = max(stages, key=stages.get)
+    ncb = (n + 2) ** 2
+    nface = 2 * (n + 1) ** 2
+    flops = None
+    if dom == "predictor" and OPS["predictor_per_cell_iter"]:
+        flops = OPS["predictor_per_cell_iter"] * ncb * mean_iters
+    elif dom == "fv":
+        flops = OPS["face_quadrature_point"] * 4 * nface + OPS["cells_per_cell"] * ncell
+    out = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": peak,
+           "peak_source": "measured: DFMA microbenchmark in bench.py on this GPU",
+           "traffic": None}
+    if flops is not None and peak:
+        ach = flops / (stages[dom] * 1e-3) / 1e12
+        out.update(achieved=ach, frac=ach / peak, algorithmic_flops_per_launch=flops)
+    else:
+        out.update(achieved=None, frac=None)
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

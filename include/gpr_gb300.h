@@ -2,10 +2,10 @@
  * gpr_gb300.h - C ABI of the GB300-native GPR (Godunov-Peshkov-Romenski)
  * ADER-WENO time step.
  *
- * Every entry point takes plain device pointers (float64 / int32 / uint8
- * arrays in the reference's cell-major layouts), sizes, a `gpr_par` by
- * pointer (host memory) and a CUDA stream (`void*`, NULL = legacy default
- * stream).  Work is enqueued on that stream; functions return 0 on success or
+ * Every entry point takes plain device pointers for grid data (float64 /
+ * int32 / uint8 arrays in the reference's cell-major layouts), HOST pointers
+ * for the small control arrays (nX, dX, bcs) and for `gpr_par`, and a CUDA
+ * stream (`void*`, NULL = legacy default stream).  Work is enqueued on that stream; functions return 0 on success or
  * a negative GPR_E_* code.  No entry point allocates device memory unless its
  * comment says so; scratch buffers are passed in by the caller.
  *
@@ -97,9 +97,12 @@ int gpr_extend_mask(const uint8_t *mask, uint8_t *maskb, const int32_t *nX,
 
 /* Replaces GPRpy.solvers.weno.weno_launcher (solvers/weno/weno.h:6,
  * weno.cpp:126-157): WENO reconstruction of ub into wh over the nx+2 (x ny+2)
- * predictor cells. */
+ * predictor cells.  2D needs caller scratch of
+ * gpr_weno_scratch_doubles(nX, 2, nvar) doubles (the x-sweep result);
+ * 1D needs none (scratch may be NULL). */
+long gpr_weno_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX,
-                      int ndim, int nvar, void *stream);
+                      int ndim, double *scratch, int nvar, void *stream);
 
 /* Replaces solvers.dg.predictor (solvers/dg/dg.h:7, dg1.cpp:75-131,
  * dg2.cpp:102-171): local space-time Galerkin predictor of every masked cell.
@@ -116,11 +119,14 @@ int gpr_predictor(double *qh, const double *wh, double dt, const double *dX,
 
 /* Replaces solvers.fv.fv_launcher (solvers/fv/fv.h:17, fv.cpp:281-297):
  * u += space-time quadrature of the non-conservative/source terms
- * (SOURCES, TIME) and the path-conservative interface fluxes. */
+ * (SOURCES, TIME) and the path-conservative interface fluxes.  Caller
+ * scratch of gpr_fv_scratch_doubles(nX, ndim, nvar) doubles holds the face
+ * fluxes. */
+long gpr_fv_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     const double *dX, int ndim, int sources, int time_dg,
                     int flux, const gpr_par *par, const uint8_t *mask,
-                    int nvar, void *stream);
+                    double *scratch, int nvar, void *stream);
 
 /* Replaces solvers.timestep (solvers/iterator.cpp:148-177) for one material:
  * dt = CFL / max_cells sum_d max_abs_eigs/dx_d, x0.2 while count <= 5,
@@ -145,12 +151,30 @@ int gpr_ode_launcher(double *u, int64_t ncell, double dt, const gpr_par *par,
 
 /* Replaces solvers.ader_stepper (solvers/steppers.cpp:10-22): one ADER-WENO
  * step u <- u + (WENO -> predictor -> FV) of one material grid, with ub
- * already filled by gpr_boundaries.  wh/qh are caller scratch of the sizes
- * above; dt is a host value.  status as in gpr_predictor (optional). */
+ * already filled by gpr_boundaries.  Caller scratch of
+ * gpr_ader_scratch_doubles(nX, ndim, nvar) doubles holds wh, qh and the
+ * stage temporaries; dt is a host value.  status as in gpr_predictor
+ * (optional). */
+long gpr_ader_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_ader_stepper(double *u, const double *ub, const int32_t *nX, int ndim,
                      double dt, const double *dX, int stiff, int flux,
-                     const gpr_par *par, const uint8_t *mask, double *wh,
-                     double *qh, int32_t *status, int nvar, void *stream);
+                     const gpr_par *par, const uint8_t *mask, double *scratch,
+                     int32_t *status, int nvar, void *stream);
+
+/* Replaces solvers.iterator (solvers/iterator.cpp:179-264) for one
+ * material, device resident: runs `nsteps` steps of
+ *   CFL time step -> boundaries -> WENO -> predictor -> FV -> renorm
+ * with the clock in device memory, clock[5] = {t, dt, tf, cfl, count}
+ * (count stored as a double).  Steps taken once t >= tf change nothing, so
+ * a fixed number of steps can be enqueued or captured in a CUDA graph without
+ * a host synchronisation.  Caller scratch of
+ * gpr_iterate_scratch_doubles(nX, ndim, nvar) doubles; mask may be NULL (all
+ * cells); status as in gpr_predictor (optional, last step's). */
+long gpr_iterate_scratch_doubles(const int32_t *nX, int ndim, int nvar);
+int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX,
+                const int32_t *bcs, int flux, const gpr_par *par,
+                const uint8_t *mask, double *clock, int nsteps, double *scratch,
+                int32_t *status, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,

@@ -1,0 +1,53 @@
+"""phd_gb300 - GB300-native (sm_103a, FP64) GPR ADER-WENO time step.
+
+A drop-in for the hot path of the reference's pybind11 module `GPRpy`
+(haranjackson/phd, code/cpp/bindings/bindings.cpp): the same names and
+argument orders, operating in place on torch CUDA tensors, backed by the
+hand-written CUDA kernels in phd_gb300/csrc through the C ABI declared in
+include/gpr_gb300.h.
+
+    import phd_gb300 as GPRpy
+    GPRpy.boundaries(u, ub, nX, bcs)
+    GPRpy.solvers.ader_stepper(u, ub, nX, dt, dX, False, 0, MP, mask)
+"""
+from types import SimpleNamespace
+
+from . import api
+from ._lib import build, load
+from .params import Par, material_params, Cvec
+from . import problems
+
+__all__ = ["boundaries", "extend_mask", "options", "classes", "solvers", "system",
+           "build", "load", "Par", "material_params", "Cvec", "problems"]
+
+boundaries = api.boundaries
+extend_mask = api.extend_mask
+
+options = SimpleNamespace(N=lambda: 2, NV=lambda: 17, VISCOUS=lambda: True,
+                          THERMAL=lambda: True, MULTI=lambda: False, LSET=lambda: 0)
+
+classes = SimpleNamespace(Par=Par)
+
+system = SimpleNamespace(flux=api.flux, source=api.source, Bdot=api.Bdot,
+                         max_abs_eigs=api.max_abs_eigs)
+
+
+def _iterator(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
+              contorted_tol=1.0, max_steps=None):
+    from .driver import iterate
+    return iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
+                   max_steps=max_steps)
+
+
+solvers = SimpleNamespace(
+    weno=SimpleNamespace(weno_launcher=api.weno_launcher),
+    dg=SimpleNamespace(predictor=api.predictor),
+    fv=SimpleNamespace(fv_launcher=api.fv_launcher, D_RUS=api.D_RUS, Bint=api.Bint),
+    split=SimpleNamespace(ode_launcher=api.ode_launcher),
+    ader_stepper=api.ader_stepper,
+    ader_stepper_para=api.ader_stepper_para,
+    timestep=api.timestep,
+    renorm_distortion=api.renorm_distortion,
+    extended_dimensions=api.extended_dimensions,
+    iterator=_iterator,
+)

@@ -1,0 +1,543 @@
+// gpr_capi.cu - C ABI of the GB300 GPR ADER-WENO step (include/gpr_gb300.h).
+//
+// Host launchers: argument checks, variant dispatch on the number of
+// variables (V = 17: viscous + heat conduction; V = 14: viscous), grid
+// sizing and the stage sequence of one ADER step.  All device work is
+// stream-ordered on the caller's stream; nothing here synchronises.
+#include <mutex>
+#include <stdio.h>
+
+#include "gpr_kernels.cuh"
+#include "gpr_ode.cuh"
+
+using namespace gpr;
+
+namespace {
+
+const Consts &consts() {
+  static Consts c = make_consts();
+  return c;
+}
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+inline int blocks(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+inline int cuda_rc() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpr_gb300: CUDA error %s\n", cudaGetErrorString(e));
+    return GPR_E_CUDA;
+  }
+  return GPR_OK;
+}
+
+// Pointwise kernels (one thread per state) behind gpr_flux / gpr_source /
+// gpr_Bdot / gpr_max_abs_eigs / gpr_interface_terms.
+template <class L>
+__global__ void k_pointwise(int what, const double *__restrict__ Q, const double *__restrict__ X,
+                            double *__restrict__ out, double *__restrict__ out2, long count,
+                            int d, int flux, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= count)
+    return;
+  double q[V], r[V];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = Q[c * V + k];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  switch (what) {
+  case 0:  // flux (adds)
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] = out[c * V + k];
+    flux_add<L::THERMAL, V>(q, s, d, P, r);
+    break;
+  case 1:
+    source<L::THERMAL, V>(q, s, P, r);
+    break;
+  case 2: {
+    double x[V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      x[k] = X[c * V + k];
+    bdot<V, L::LSET>(s.v, x, d, r);
+  } break;
+  case 3:
+    out[c] = max_abs_eigs<L::THERMAL>(q, s, d, P);
+    return;
+  default: {
+    double qr[V], b[V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      qr[k] = X[c * V + k];
+    interface_point<L>(q, qr, d, P, C, r, b);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      out2[c * V + k] = b[k];
+  } break;
+  }
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    out[c * V + k] = r[k];
+}
+
+// extend_mask (etc/grid.cpp:176-230): one thread per predictor cell.
+__global__ void k_extend_mask(const uint8_t *__restrict__ mask, uint8_t *__restrict__ maskb,
+                              int nx, int ny, int nd) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (nd == 1) {
+    if (idx >= nx + 2)
+      return;
+    int i = (int)idx - 1;
+    auto m = [&](int k) { return mask[k] != 0; };
+    int ii = i < 0 ? 0 : (i > nx - 1 ? nx - 1 : i);  // maskb(0)=maskb(1), maskb(nx+1)=maskb(nx)
+    bool v = m(ii) || (ii > 0 && m(ii - 1)) || (ii < nx - 1 && m(ii + 1));
+    maskb[idx] = v;
+    return;
+  }
+  long nb = (long)(nx + 2) * (ny + 2);
+  if (idx >= nb)
+    return;
+  int bi = idx / (ny + 2), bj = idx % (ny + 2);
+  int i = bi - 1, j = bj - 1;
+  bool v;
+  bool ei = i < 0 || i > nx - 1, ej = j < 0 || j > ny - 1;
+  if (ei && ej)
+    v = false;  // corners
+  else if (ei)
+    v = mask[(long)(i < 0 ? 0 : nx - 1) * ny + j] != 0;
+  else if (ej)
+    v = mask[(long)i * ny + (j < 0 ? 0 : ny - 1)] != 0;
+  else {
+    long ind = (long)i * ny + j;
+    v = mask[ind] || (i > 0 && mask[ind - ny]) || (i < nx - 1 && mask[ind + ny]) ||
+        (j > 0 && mask[ind - 1]) || (j < ny - 1 && mask[ind + 1]);
+  }
+  maskb[idx] = v;
+}
+
+template <class L> struct Ops {
+  static constexpr int V = L::V;
+
+  static int boundaries(const double *u, double *ub, const int32_t *nX, int nd,
+                        const int32_t *bcs, cudaStream_t st) {
+    int nx = nX[0], ny = nd == 2 ? nX[1] : 1;
+    long n = (long)nx * ny * V;
+    k_fill_interior<V><<<blocks(n, 256), 256, 0, st>>>(u, ub, nx, ny, nd);
+    long g0 = (long)(nd == 1 ? 1 : ny) * 2 * NN * V;
+    k_ghosts<V><<<blocks(g0, 256), 256, 0, st>>>(ub, nx, ny, nd, 0, bcs[0], bcs[1]);
+    if (nd == 2) {
+      long g1 = (long)(nx + 2 * NN) * 2 * NN * V;
+      k_ghosts<V><<<blocks(g1, 256), 256, 0, st>>>(ub, nx, ny, nd, 1, bcs[2], bcs[3]);
+    }
+    return cuda_rc();
+  }
+
+  static long weno_scratch(const int32_t *nX, int nd) {
+    if (nd == 1)
+      return 0;
+    return (long)(nX[0] + 2) * (nX[1] + 2 * NN) * NN * V;
+  }
+
+  static int weno(double *wh, const double *ub, const int32_t *nX, int nd, double *scratch,
+                  cudaStream_t st) {
+    const Consts &C = consts();
+    if (nd == 1) {
+      int ncb = nX[0] + 2;
+      k_weno1d<V><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, C);
+      return cuda_rc();
+    }
+    int nxp = nX[0] + 2, nyp = nX[1] + 2, nyb = nX[1] + 2 * NN;
+    k_weno2d_x<V><<<blocks((long)nxp * nyb * V, 256), 256, 0, st>>>(scratch, ub, nxp, nyb, C);
+    k_weno2d_y<V><<<blocks((long)nxp * nyp * NN * V, 256), 256, 0, st>>>(wh, scratch, nxp,
+                                                                         nyp, C);
+    return cuda_rc();
+  }
+
+  static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
+                       const double *dX, int nd, const int32_t *nX, int stiff,
+                       const DevPar &P, const uint8_t *mask, int32_t *status,
+                       cudaStream_t st) {
+    const Consts &C = consts();
+    (void)stiff;
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    if (nd == 1) {
+      long nt = ncb * NN * NN;
+      k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
+          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], 1.0, P, C);
+    } else {
+      long nt = ncb * NN * NN * NN;
+      k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
+          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], 1.0 / dX[1], P, C);
+    }
+    return cuda_rc();
+  }
+
+  static long fv_scratch(const int32_t *nX, int nd) {
+    if (nd == 1)
+      return (long)(nX[0] + 1) * 2 * V;
+    return 2L * (nX[0] + 1) * (nX[1] + 1) * 2 * V;
+  }
+
+  static int fv(double *u, const double *qh, const int32_t *nX, double dt,
+                const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
+                const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st) {
+    const Consts &C = consts();
+    int nx = nX[0];
+    if (nd == 1) {
+      long nf = (long)(nx + 1) * NN;
+      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, nx, mask, dt, dt_dev, dX[0],
+                                                     time_dg, P, C);
+      long nc = (long)nx * NN * NN;
+      k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
+                                                      dt_dev, dX[0], 1.0, sources, time_dg, P,
+                                                      C);
+      return cuda_rc();
+    }
+    int ny = nX[1];
+    long nf = (long)(nx + 1) * (ny + 1);
+    double *fbx = scratch, *fby = scratch + nf * 2 * V;
+    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
+                                                             dt_dev, dX[0], dX[1], time_dg, P,
+                                                             C);
+    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fby, qh, nx, ny, 1, mask, dt,
+                                                             dt_dev, dX[0], dX[1], time_dg, P,
+                                                             C);
+    long nc = (long)nx * ny * NN * NN * NN;
+    k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
+                                                    dX[0], dX[1], sources, time_dg, P, C);
+    return cuda_rc();
+  }
+
+  static int timestep(const double *u, long ncell, const double *dX, int nd, double cfl,
+                      double t, double tf, int count, const DevPar &P, double *dt_out,
+                      double *scratch, cudaStream_t st) {
+    unsigned long long *mx = (unsigned long long *)scratch;
+    cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
+    k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+                                                      nd == 2 ? dX[1] : 1.0, mx, P);
+    k_cfl_finalize<<<1, 1, 0, st>>>(mx, cfl, t, tf, count, dt_out);
+    return cuda_rc();
+  }
+
+  static int renorm(double *u, long ncell, const DevPar &P, cudaStream_t st) {
+    k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, nullptr);
+    return cuda_rc();
+  }
+
+  static int pointwise(int what, const double *Q, const double *X, double *out, double *out2,
+                       long count, int d, int flux, const DevPar &P, cudaStream_t st) {
+    k_pointwise<L><<<blocks(count, 64), 64, 0, st>>>(what, Q, X, out, out2, count, d, flux, P,
+                                                     consts());
+    return cuda_rc();
+  }
+
+  // One device-resident iterator step (iterator.cpp:204-240 for one
+  // material): CFL -> boundaries -> WENO -> predictor -> FV -> renorm ->
+  // clock advance, with dt living in clk[1].
+  static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
+                     const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
+                     int nsteps, double *scratch, int32_t *status, cudaStream_t st) {
+    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
+    long ns = nd == 1 ? NN : NN * NN;
+    double *ub = scratch;
+    double *wh = ub + nub * V;
+    double *qh = wh + ncb * ns * V;
+    double *tmp = qh + ncb * NN * ns * V;
+    unsigned long long *mx = (unsigned long long *)(tmp + (weno_scratch(nX, nd) > fv_scratch(nX, nd)
+                                                               ? weno_scratch(nX, nd)
+                                                               : fv_scratch(nX, nd)));
+    double *dt_dev = clk + 1;
+    for (int s = 0; s < nsteps; s++) {
+      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
+      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+                                                        nd == 2 ? dX[1] : 1.0, mx, P);
+      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
+      int rc = boundaries(u, ub, nX, nd, bcs, st);
+      if (rc)
+        return rc;
+      rc = weno(wh, ub, nX, nd, tmp, st);
+      if (rc)
+        return rc;
+      rc = predictor(qh, wh, 0.0, dt_dev, dX, nd, nX, 0, P, mask, status, st);
+      if (rc)
+        return rc;
+      rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st);
+      if (rc)
+        return rc;
+      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
+      k_clock_advance<<<1, 1, 0, st>>>(clk);
+    }
+    return cuda_rc();
+  }
+
+  static long iterate_scratch(const int32_t *nX, int nd) {
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
+    long ns = nd == 1 ? NN : NN * NN;
+    long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
+    return nub * V + ncb * ns * V + ncb * NN * ns * V + (w > f ? w : f) + 1;
+  }
+
+  static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {
+    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt, nullptr, 1.0, P);
+    return cuda_rc();
+  }
+};
+
+using L17 = Layout<true, 0>;
+using L14 = Layout<false, 0>;
+
+bool check_grid(const int32_t *nX, int nd) {
+  if (!nX || (nd != 1 && nd != 2))
+    return false;
+  for (int d = 0; d < nd; d++)
+    if (nX[d] < 1)
+      return false;
+  return true;
+}
+
+#define DISPATCH(nvar, CALL)                                                                 \
+  switch (nvar) {                                                                            \
+  case 17: {                                                                                 \
+    using O = Ops<L17>;                                                                      \
+    return CALL;                                                                             \
+  }                                                                                          \
+  case 14: {                                                                                 \
+    using O = Ops<L14>;                                                                      \
+    return CALL;                                                                             \
+  }                                                                                          \
+  default:                                                                                   \
+    return GPR_E_UNSUPPORTED;                                                                \
+  }
+
+}  // namespace
+
+extern "C" {
+
+int gpr_version(void) { return 100; }
+
+int gpr_supported_nvars(int32_t *out, int cap) {
+  static const int32_t vs[] = {17, 14};
+  int n = 0;
+  for (int i = 0; i < 2 && i < cap; i++)
+    out[n++] = vs[i];
+  return 2;
+}
+
+int gpr_extend_mask(const uint8_t *mask, uint8_t *maskb, const int32_t *nX, int ndim,
+                    void *stream) {
+  if (!mask || !maskb || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  int nx = nX[0], ny = ndim == 2 ? nX[1] : 1;
+  long nb = ndim == 1 ? nx + 2 : (long)(nx + 2) * (ny + 2);
+  k_extend_mask<<<blocks(nb, 256), 256, 0, S(stream)>>>(mask, maskb, nx, ny, ndim);
+  return cuda_rc();
+}
+
+int gpr_flux(const double *Q, double *out, int64_t count, int d, const gpr_par *par, int nvar,
+             void *stream) {
+  if (!Q || !out || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(0, Q, nullptr, out, nullptr, count, d, 0, P, S(stream)))
+}
+
+int gpr_source(const double *Q, double *out, int64_t count, const gpr_par *par, int nvar,
+               void *stream) {
+  if (!Q || !out || count < 0 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(1, Q, nullptr, out, nullptr, count, 0, 0, P, S(stream)))
+}
+
+int gpr_Bdot(const double *Q, const double *x, double *out, int64_t count, int d,
+             const gpr_par *par, int nvar, void *stream) {
+  if (!Q || !x || !out || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(2, Q, x, out, nullptr, count, d, 0, P, S(stream)))
+}
+
+int gpr_max_abs_eigs(const double *Q, double *out, int64_t count, int d, const gpr_par *par,
+                     int nvar, void *stream) {
+  if (!Q || !out || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(3, Q, nullptr, out, nullptr, count, d, 0, P, S(stream)))
+}
+
+int gpr_interface_terms(const double *qL, const double *qR, double *out, double *bout,
+                        int64_t count, int d, int flux, const gpr_par *par, int nvar,
+                        void *stream) {
+  if (!qL || !qR || !out || !bout || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(4, qL, qR, out, bout, count, d, flux, P, S(stream)))
+}
+
+int gpr_boundaries(const double *u, double *ub, const int32_t *nX, int ndim,
+                   const int32_t *bcs, int nvar, void *stream) {
+  if (!u || !ub || !bcs || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  for (int i = 0; i < 2 * ndim; i++)
+    if (bcs[i] < 0 || bcs[i] > 5)
+      return GPR_E_ARG;
+  DISPATCH(nvar, O::boundaries(u, ub, nX, ndim, bcs, S(stream)))
+}
+
+long gpr_weno_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
+  if (!check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DISPATCH(nvar, O::weno_scratch(nX, ndim))
+}
+
+int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX, int ndim,
+                      double *scratch, int nvar, void *stream) {
+  if (!wh || !ub || !check_grid(nX, ndim) || (ndim == 2 && !scratch))
+    return GPR_E_ARG;
+  DISPATCH(nvar, O::weno(wh, ub, nX, ndim, scratch, S(stream)))
+}
+
+int gpr_predictor(double *qh, const double *wh, double dt, const double *dX, int ndim,
+                  const int32_t *nX, int stiff, const gpr_par *par, const uint8_t *mask,
+                  int32_t *status, int nvar, void *stream) {
+  if (!qh || !wh || !dX || !par || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::predictor(qh, wh, dt, nullptr, dX, ndim, nX, stiff, P, mask, status,
+                              S(stream)))
+}
+
+long gpr_fv_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
+  if (!check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DISPATCH(nvar, O::fv_scratch(nX, ndim))
+}
+
+int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
+                    const double *dX, int ndim, int sources, int time_dg, int flux,
+                    const gpr_par *par, const uint8_t *mask, double *scratch, int nvar,
+                    void *stream) {
+  if (!u || !qh || !dX || !par || !scratch || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, sources, time_dg, P, mask, scratch,
+                       S(stream)))
+}
+
+int gpr_timestep_scratch_doubles(int64_t ncell) {
+  (void)ncell;
+  return 1;
+}
+
+int gpr_timestep(const double *u, int64_t ncell, const double *dX, int ndim, double cfl,
+                 double t, double tf, int count, const gpr_par *par, double *dt_out,
+                 double *scratch, int nvar, void *stream) {
+  if (!u || ncell < 1 || !dX || (ndim != 1 && ndim != 2) || !par || !dt_out || !scratch)
+    return GPR_E_ARG;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::timestep(u, ncell, dX, ndim, cfl, t, tf, count, P, dt_out, scratch,
+                             S(stream)))
+}
+
+int gpr_renorm_distortion(double *u, int64_t ncell, const gpr_par *par, int nvar,
+                          void *stream) {
+  if (!u || ncell < 0 || !par)
+    return GPR_E_ARG;
+  if (ncell == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::renorm(u, ncell, P, S(stream)))
+}
+
+int gpr_ode_launcher(double *u, int64_t ncell, double dt, const gpr_par *par, int nvar,
+                     void *stream) {
+  if (!u || ncell < 0 || !par)
+    return GPR_E_ARG;
+  if (ncell == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::ode(u, ncell, dt, P, S(stream)))
+}
+
+long gpr_ader_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
+  if (!check_grid(nX, ndim))
+    return GPR_E_ARG;
+  long ncb = ndim == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+  long ns = ndim == 1 ? NN : NN * NN;
+  long wh = ncb * ns * nvar, qh = ncb * NN * ns * nvar;
+  long w = gpr_weno_scratch_doubles(nX, ndim, nvar);
+  long f = gpr_fv_scratch_doubles(nX, ndim, nvar);
+  if (w < 0 || f < 0)
+    return GPR_E_UNSUPPORTED;
+  return wh + qh + (w > f ? w : f);
+}
+
+int gpr_ader_stepper(double *u, const double *ub, const int32_t *nX, int ndim, double dt,
+                     const double *dX, int stiff, int flux, const gpr_par *par,
+                     const uint8_t *mask, double *scratch, int32_t *status, int nvar,
+                     void *stream) {
+  if (!u || !ub || !dX || !par || !scratch || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  long ncb = ndim == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+  long ns = ndim == 1 ? NN : NN * NN;
+  double *wh = scratch;
+  double *qh = wh + ncb * ns * nvar;
+  double *tmp = qh + ncb * NN * ns * nvar;
+  int rc = gpr_weno_launcher(wh, ub, nX, ndim, tmp, nvar, stream);
+  if (rc)
+    return rc;
+  rc = gpr_predictor(qh, wh, dt, dX, ndim, nX, stiff, par, mask, status, nvar, stream);
+  if (rc)
+    return rc;
+  return gpr_fv_launcher(u, qh, nX, dt, dX, ndim, 1, 1, flux, par, mask, tmp, nvar, stream);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+long gpr_iterate_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
+  if (!check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DISPATCH(nvar, O::iterate_scratch(nX, ndim))
+}
+
+int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const int32_t *bcs,
+                int flux, const gpr_par *par, const uint8_t *mask, double *clock, int nsteps,
+                double *scratch, int32_t *status, int nvar, void *stream) {
+  if (!u || !dX || !bcs || !par || !clock || !scratch || nsteps < 0 || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  for (int i = 0; i < 2 * ndim; i++)
+    if (bcs[i] < 0 || bcs[i] > 5)
+      return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::iterate(u, nX, ndim, dX, bcs, P, mask, clock, nsteps, scratch, status,
+                            S(stream)))
+}
+
+}  // extern "C"

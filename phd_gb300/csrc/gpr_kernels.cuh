@@ -1,0 +1,783 @@
+// gpr_kernels.cuh - the ADER-WENO step kernels (N = 2), templated on the
+// variable layout (THERMAL, LSET).  Host-side launchers live in gpr_capi.cu.
+#pragma once
+
+#include "gpr_consts.cuh"
+#include "gpr_device.cuh"
+
+namespace gpr {
+
+constexpr double LAMS = 1.0;       // WENO side-stencil weight (options.h:24)
+constexpr double WENO_EPS = 1e-14; // options.h:26
+constexpr double DG_TOL = 6e-6;    // options.h:30
+constexpr int DG_IT = 50;          // options.h:29
+
+template <bool TH, int LS> struct Layout {
+  static constexpr bool THERMAL = TH;
+  static constexpr int LSET = LS;
+  static constexpr int V = 14 + (TH ? 3 : 0) + LS;
+};
+
+// ---------------------------------------------------------------------------
+// Boundary ghost cells (etc/grid.cpp:12-170).  One thread per (ghost row, k)
+// of one axis; 2D runs the x pass over interior rows, then the y pass over
+// all rows (corners are filled from x ghosts as in the reference).
+
+GPR_D int bc_src_index(int code, int side, int i, int n) {
+  // index into the interior line of length n for ghost i (0..N-1) of side
+  if (code == GPR_BC_TRANSMISSIVE)
+    return side == 0 ? 0 : n - 1;
+  if (code == GPR_BC_PERIODIC)
+    return side == 0 ? n - NN + i : i;
+  return side == 0 ? NN - 1 - i : n - 1 - i;  // reflecting types
+}
+
+template <int V>
+GPR_D double bc_value(int code, int d, int k, const double *src) {
+  double x = src[k];
+  switch (code) {
+  case GPR_BC_SLIP:
+  case GPR_BC_SYMMETRIC:
+    if (k == 2 + d)
+      x = -x;
+    if (code == GPR_BC_SYMMETRIC && k >= 5 && k < 14) {
+      int r = (k - 5) / 3, c = (k - 5) % 3;
+      if (r == d)
+        x = -x;
+      if (c == d)
+        x = -x;
+    }
+    break;
+  case GPR_BC_STICK:
+    if (k >= 2 && k < 5)
+      x = -x;
+    break;
+  case GPR_BC_MOVING:
+    if (k >= 2 && k < 5)
+      x = -x;
+    if (k == 2)
+      x += 2.0 * src[0];
+    if (k == 1) {
+      double m = -src[2] + 2.0 * src[0];
+      x += (m * m - src[2] * src[2]) / (2.0 * src[0]);
+    }
+    break;
+  default:
+    break;
+  }
+  return x;
+}
+
+// Copies interior u into ub (cell-major), one thread per (cell, var).
+template <int V>
+__global__ void k_fill_interior(const double *__restrict__ u, double *__restrict__ ub,
+                                int nx, int ny, int nd) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  long total = (long)nx * ny * V;
+  if (idx >= total)
+    return;
+  int k = idx % V;
+  long c = idx / V;
+  if (nd == 1) {
+    ub[(c + NN) * V + k] = u[idx];
+  } else {
+    int i = c / ny, j = c % ny;
+    ub[((long)(i + NN) * (ny + 2 * NN) + (j + NN)) * V + k] = u[idx];
+  }
+}
+
+// Ghost rows along one axis.  For axis 0: lines are columns j (interior rows
+// j+N of ub when nd == 2), for axis 1: lines are all ub rows i.
+template <int V>
+__global__ void k_ghosts(double *__restrict__ ub, int nx, int ny, int nd, int axis,
+                         int bcl, int bcr) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int nline = nd == 1 ? 1 : (axis == 0 ? ny : nx + 2 * NN);
+  long total = (long)nline * 2 * NN * V;
+  if (idx >= total)
+    return;
+  int k = idx % V;
+  long rest = idx / V;
+  int g = rest % (2 * NN);  // ghost slot: 0..N-1 left, N..2N-1 right
+  int line = rest / (2 * NN);
+  int side = g >= NN;
+  int i = side ? g - NN : g;
+  int n = axis == 0 ? nx : ny;
+  int code = side ? bcr : bcl;
+  int si = bc_src_index(code, side, i, n);
+  int gi = side ? i + n + NN : i;  // ghost position along the line
+  long nyb = ny + 2 * NN;
+  const double *src;
+  double *dst;
+  if (nd == 1) {
+    src = ub + (long)(si + NN) * V;
+    dst = ub + (long)gi * V;
+  } else if (axis == 0) {
+    long j = line + NN;
+    src = ub + ((long)(si + NN) * nyb + j) * V;
+    dst = ub + ((long)gi * nyb + j) * V;
+  } else {
+    long ii = line;
+    src = ub + (ii * nyb + (si + NN)) * V;
+    dst = ub + (ii * nyb + gi) * V;
+  }
+  if (code == GPR_BC_PERIODIC)
+    code = GPR_BC_TRANSMISSIVE;  // plain copy
+  dst[k] = bc_value<V>(code, axis, k, src);
+}
+
+// ---------------------------------------------------------------------------
+// WENO (solvers/weno/weno.cpp:4-124).  One thread per (cell, variable):
+// data rows d0[0], d0[sd], d0[2 sd] (cells i-1, i, i+1); writes the N = 2
+// node values out[0], out[so].
+GPR_D void weno_point(const double *__restrict__ d0, long sd, double *__restrict__ out,
+                      long so, int ind, int nx, int gap, const Consts &C) {
+  double a = d0[0], b = d0[sd], c = d0[2 * sd];
+  double wL0 = C.mLinv[0][0] * a + C.mLinv[0][1] * b;
+  double wL1 = C.mLinv[1][0] * a + C.mLinv[1][1] * b;
+  double wR0 = C.mRinv[0][0] * b + C.mRinv[0][1] * c;
+  double wR1 = C.mRinv[1][0] * b + C.mRinv[1][1] * c;
+  // (w^T SIG) w, the reference's evaluation order (weno.cpp:9), which stays
+  // accurate on nearly constant data
+  double tL = (wL0 * C.sig[0][0] + wL1 * C.sig[1][0]) * wL0 +
+              (wL0 * C.sig[0][1] + wL1 * C.sig[1][1]) * wL1 + WENO_EPS;
+  double tR = (wR0 * C.sig[0][0] + wR1 * C.sig[1][0]) * wR0 +
+              (wR0 * C.sig[0][1] + wR1 * C.sig[1][1]) * wR1 + WENO_EPS;
+  tL *= tL;
+  tL *= tL;
+  tL *= tL;
+  tR *= tR;
+  tR *= tR;
+  tR *= tR;
+  double oL = LAMS / tL, oR = LAMS / tR;
+  double n0 = 0.0, n1 = 0.0, den = 0.0;
+  if (ind >= gap) {
+    n0 += wL0 * oL;
+    n1 += wL1 * oL;
+    den += oL;
+  }
+  if (ind <= nx - gap - 1) {
+    n0 += wR0 * oR;
+    n1 += wR1 * oR;
+    den += oR;
+  }
+  double iden = 1.0 / den;
+  out[0] = n0 * iden;
+  out[so] = n1 * iden;
+}
+
+// 1D: wh[i][a][k] for i in 0..nx+1 from ub rows i..i+2 (weno.cpp:75-81, 146)
+template <int V>
+__global__ void k_weno1d(double *__restrict__ wh, const double *__restrict__ ub, int ncb,
+                         Consts C) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)ncb * V)
+    return;
+  int k = idx % V;
+  int i = idx / V;
+  weno_point(ub + (long)i * V + k, V, wh + (long)i * NN * V + k, V, i, ncb, 0, C);
+}
+
+// 2D x sweep (weno.cpp:93-104): ux[i][j][a][k], i in 0..nx'-1 (nx' = nx+2),
+// j over every ub column (ny+2N).
+template <int V>
+__global__ void k_weno2d_x(double *__restrict__ ux, const double *__restrict__ ub, int nxp,
+                           int nyb, Consts C) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)nxp * nyb * V)
+    return;
+  int k = idx % V;
+  long rest = idx / V;
+  int j = rest % nyb;
+  int i = rest / nyb;
+  int gap = (j < NN || j >= nyb - NN) ? NN : 0;
+  weno_point(ub + ((long)i * nyb + j) * V + k, (long)nyb * V,
+             ux + ((long)i * nyb + j) * NN * V + k, V, i, nxp, gap, C);
+}
+
+// 2D y sweep (weno.cpp:106-121): wh[i][j][ii][jj][k]
+template <int V>
+__global__ void k_weno2d_y(double *__restrict__ wh, const double *__restrict__ ux, int nxp,
+                           int nyp, Consts C) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)nxp * nyp * NN * V)
+    return;
+  int k = idx % V;
+  long rest = idx / V;
+  int ii = rest % NN;
+  rest /= NN;
+  int j = rest % nyp;
+  int i = rest / nyp;
+  int nyb = nyp + 2 * (NN - 1);
+  int gap = (i == 0 || i == nxp - 1) ? 1 : 0;
+  weno_point(ux + (((long)i * nyb + j) * NN + ii) * V + k, (long)NN * V,
+             wh + (((long)i * nyp + j) * NN * NN + ii * NN) * V + k, V, j, nyp, gap, C);
+}
+
+// ---------------------------------------------------------------------------
+// Space-time DG predictor (solvers/dg/dg1.cpp:8-131, dg2.cpp:8-171).
+//
+// One thread per space-time node: NP = N^(d+1) consecutive lanes hold one
+// cell (lane g = t N^d + s).  Spatial derivatives, the DG_DER flux term and
+// the DG_U^-1 time coupling need the partner nodes' values, exchanged with
+// warp shuffles (partners differ in one index: lane ^ bit).  Each iteration
+// is the reference's Picard update q <- DG_U^-1 (Ww + dt R(q)) with its
+// per-cell stopping rule |q1 - q0| <= DG_TOL (1 + |q0|) (dg1.cpp:108-127).
+
+template <int V>
+GPR_D void shfl_vec(const double *src, double *dst, int lanemask) {
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    dst[k] = __shfl_xor_sync(0xffffffffu, src[k], lanemask);
+}
+
+// rhs at this thread's node; returns R in r (Ww added), q unchanged.
+template <class L, int ND>
+GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int i, int j,
+                       double dt, double idx, double idy, const DevPar &P, const Consts &C) {
+  constexpr int V = L::V;
+  // lane bit layout: 1D g = 2t + i ; 2D g = 4t + 2i + j
+  constexpr int XB = ND == 1 ? 1 : 2;  // flips i
+  constexpr int YB = 1;                // flips j (2D)
+  double tmp[V], other[V];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  source<L::THERMAL, V>(q, s, P, r);
+  // x derivative: DERVALS[i][m] q(t, m, j) / dx
+  shfl_vec<V>(q, other, XB);
+  {
+    double a = C.derv[i][i] * idx, b = C.derv[i][1 - i] * idx;
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      tmp[k] = a * q[k] + b * other[k];
+    double bd[V];
+    bdot<V, L::LSET>(s.v, tmp, 0, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] -= bd[k];
+  }
+  if (ND == 2) {
+    shfl_vec<V>(q, other, YB);
+    double a = C.derv[j][j] * idy, b = C.derv[j][1 - j] * idy;
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      tmp[k] = a * q[k] + b * other[k];
+    double bd[V];
+    bdot<V, L::LSET>(s.v, tmp, 1, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] -= bd[k];
+  }
+  double wn = ND == 1 ? C.w[t] * C.w[i] : C.w[t] * C.w[i] * C.w[j];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    r[k] *= wn;
+  // - W_t [W_j] DG_DER(i, m) F(t, m, j) / dx
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    tmp[k] = 0.0;
+  flux_add<L::THERMAL, V>(q, s, 0, P, tmp);
+  shfl_vec<V>(tmp, other, XB);
+  {
+    double wx = (ND == 1 ? C.w[t] : C.w[t] * C.w[j]) * idx;
+    double a = wx * C.dgder[i][i], b = wx * C.dgder[i][1 - i];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] -= a * tmp[k] + b * other[k];
+  }
+  if (ND == 2) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      tmp[k] = 0.0;
+    flux_add<L::THERMAL, V>(q, s, 1, P, tmp);
+    shfl_vec<V>(tmp, other, YB);
+    double wy = C.w[t] * C.w[i] * idy;
+    double a = wy * C.dgder[j][j], b = wy * C.dgder[j][1 - j];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] -= a * tmp[k] + b * other[k];
+  }
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    r[k] = r[k] * dt + Ww[k];
+}
+
+// q_new(t, s) = sum_m DG_MATinv[t][m] r(m, s) / W_s
+template <int V, int ND>
+GPR_D void dg_solve_node(const double *r, double *qn, int t, int i, int j, const Consts &C) {
+  constexpr int TB = ND == 1 ? 2 : 4;  // flips t
+  double other[V];
+  shfl_vec<V>(r, other, TB);
+  // 1 / W_s: 2 and 4 for the N = 2 weights (exact)
+  double iws = ND == 1 ? 1.0 / C.w[i] : 1.0 / (C.w[i] * C.w[j]);
+  double a = C.dgmatinv[t][t] * iws, b = C.dgmatinv[t][1 - t] * iws;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    qn[k] = a * r[k] + b * other[k];
+}
+
+// Picard predictor.  ncb predictor cells; each warp holds 32/NP cells.
+// status[c] (optional): GPR_PRED_PICARD | iterations << 8 when converged,
+// GPR_PRED_FAILED when Picard did not converge (row left for the Newton pass,
+// with the last Picard iterate written so the row is always defined).
+template <class L, int ND>
+__global__ void __launch_bounds__(128) k_predictor_picard(
+    double *__restrict__ qh, const double *__restrict__ wh, long ncb,
+    const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
+    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
+  constexpr int NP = NN * NS;                 // space-time nodes
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int g = threadIdx.x % NP;
+  long c = gt / NP;
+  bool valid = c < ncb;
+  bool active = valid && (mask == nullptr || mask[c]);
+  int t = g / NS, sidx = g % NS;
+  int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
+  double w[V], Ww[V], q[V], r[V], qn[V];
+  long cc = valid ? c : 0;
+  const double *wc = wh + (cc * NS + sidx) * V;
+  double f = C.endv[0][t] * (ND == 1 ? C.w[i] : C.w[i] * C.w[j]);
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    w[k] = valid ? wc[k] : 1.0;
+    Ww[k] = f * w[k];
+    q[k] = w[k];  // standard initial guess (initial_guess.cpp:4-15)
+  }
+  // groups are aligned to NP lanes; the group shares the convergence decision
+  unsigned lane = threadIdx.x & 31u;
+  unsigned gmask = ((NP == 32) ? 0xffffffffu : ((1u << NP) - 1u)) << (lane & ~(NP - 1u));
+  bool done = !active;
+  int iters = 0;
+  bool nan_seen = false;
+  for (int it = 0; it < DG_IT; it++) {
+    if (__all_sync(0xffffffffu, done))
+      break;
+    dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
+    dg_solve_node<V, ND>(r, qn, t, i, j, C);
+    bool big = false, hasnan = false;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      if (fabs(qn[k] - q[k]) > DG_TOL * (1.0 + fabs(q[k])))
+        big = true;
+      if (qn[k] != qn[k])
+        hasnan = true;
+    }
+    unsigned bigm = __ballot_sync(0xffffffffu, big) & gmask;
+    unsigned nanm = __ballot_sync(0xffffffffu, hasnan) & gmask;
+    if (!done) {
+      iters = it + 1;
+      if (bigm) {
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          q[k] = qn[k];
+      } else if (nanm) {
+        nan_seen = true;
+        done = true;
+      } else {
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          q[k] = qn[k];
+        done = true;
+        if (active) {
+          double *out = qh + (c * NP + g) * V;
+#pragma unroll
+          for (int k = 0; k < V; k++)
+            out[k] = q[k];
+          if (status && g == 0)
+            status[c] = GPR_PRED_PICARD | (iters << 8);
+        }
+      }
+    }
+  }
+  if (active && (!done || nan_seen)) {
+    // Picard failed: leave the initial guess for the Newton pass
+    double *out = qh + (c * NP + g) * V;
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      out[k] = w[k];
+    if (status && g == 0)
+      status[c] = GPR_PRED_FAILED | (iters << 8);
+  }
+  if (valid && !active && status && g == 0)
+    status[c] = GPR_PRED_PICARD;
+}
+
+// ---------------------------------------------------------------------------
+// Finite-volume update (solvers/fv/fv.cpp:11-297).
+//
+// Face pass: one thread per (face, time node t[, transverse node s]).  It
+// extrapolates qL, qR to the face, evaluates the Rusanov dissipation
+// D = max(lambda_L, lambda_R)(qL - qR) + F(qL) + F(qR) (fluxes.cpp:66-75) and
+// the path integral Bint (fluxes.cpp:9-20), weights them, and the NQ lanes
+// of a face reduce with shuffles.  Face results: fb[face][0][k] (to the left
+// cell, subtracted) and fb[face][1][k] (to the right cell).
+
+template <class L>
+GPR_D void interface_point(const double *ql, const double *qr, int d, const DevPar &P,
+                           const Consts &C, double *f, double *b) {
+  constexpr int V = L::V;
+  Prim<L::THERMAL> sl, sr;
+  prim<L::THERMAL>(ql, P, sl);
+  prim<L::THERMAL>(qr, P, sr);
+  double m1 = max_abs_eigs<L::THERMAL>(ql, sl, d, P);
+  double m2 = max_abs_eigs<L::THERMAL>(qr, sr, d, P);
+  double m = m1 > m2 ? m1 : m2;  // std::max(m1, m2)
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    f[k] = m * (ql[k] - qr[k]);
+  flux_add<L::THERMAL, V>(ql, sl, d, P, f);
+  flux_add<L::THERMAL, V>(qr, sr, d, P, f);
+  // Bint: sum_i W_i B(qL + x_i dq) dq, dq = qR - qL; B needs only v
+  double dq[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    dq[k] = qr[k] - ql[k];
+    b[k] = 0.0;
+  }
+#pragma unroll
+  for (int n = 0; n < NN; n++) {
+    double rho = ql[0] + C.nodes[n] * dq[0];
+    double ir = 1.0 / rho;
+    double v[3] = {(ql[2] + C.nodes[n] * dq[2]) * ir, (ql[3] + C.nodes[n] * dq[3]) * ir,
+                   (ql[4] + C.nodes[n] * dq[4]) * ir};
+    double bd[V];
+    bdot<V, L::LSET>(v, dq, d, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      b[k] += C.w[n] * bd[k];
+  }
+}
+
+// 1D faces i = 0..nx between predictor cells i and i+1.  NQ = N lanes per
+// face (time nodes).
+template <class L>
+__global__ void __launch_bounds__(128) k_faces1d(
+    double *__restrict__ fb, const double *__restrict__ qh, int nx,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int time_dg, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NQ = NN;
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int t = threadIdx.x % NQ;
+  long face = gt / NQ;
+  bool valid = face <= nx;
+  long fi = valid ? face : 0;
+  bool active = valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
+  int nt = time_dg ? NN : 1;
+  double ql[V], qr[V], f[V], b[V];
+  const double *ql_ = qh + (fi * nt + (time_dg ? t : 0)) * NN * V;
+  const double *qr_ = qh + ((fi + 1) * nt + (time_dg ? t : 0)) * NN * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    ql[k] = C.endv[1][0] * ql_[k] + C.endv[1][1] * ql_[V + k];
+    qr[k] = C.endv[0][0] * qr_[k] + C.endv[0][1] * qr_[V + k];
+  }
+  double kk = (time_dg ? dt * C.w[t] : dt) / (2.0 * dx);
+  if (active) {
+    interface_point<L>(ql, qr, 0, P, C, f, b);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      f[k] = b[k] = 0.0;
+  }
+  double *out = fb + fi * 2 * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double lft = active ? kk * (b[k] + f[k]) : 0.0;
+    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
+    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
+    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
+    if (valid && t == 0) {
+      out[k] = lft;
+      out[V + k] = rgt;
+    }
+  }
+}
+
+// 2D faces: direction dir, faces (i, j) of the (nx+1) x (ny+1) face grid,
+// between predictor cells (i, j) and (i+1, j) (dir 0) or (i, j+1) (dir 1);
+// NQ = N*N lanes per face (time node t, transverse node s).
+template <class L>
+__global__ void __launch_bounds__(128) k_faces2d(
+    double *__restrict__ fb, const double *__restrict__ qh, int nx, int ny, int dir,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    double dy, int time_dg, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NQ = NN * NN;
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int lq = threadIdx.x % NQ;
+  int t = lq / NN, s = lq % NN;
+  long face = gt / NQ;
+  long nf = (long)(nx + 1) * (ny + 1);
+  bool valid = face < nf;
+  long fi = valid ? face : 0;
+  int i = fi / (ny + 1), j = fi % (ny + 1);
+  long cb = (long)i * (ny + 2) + j;
+  long cn = dir == 0 ? cb + (ny + 2) : cb + 1;
+  bool geo = dir == 0 ? (j > 0) : (i > 0);
+  bool active = valid && geo && (mask == nullptr || (mask[cb] && mask[cn])) &&
+                (time_dg || t == 0);
+  int nt = time_dg ? NN : 1;
+  int tt = time_dg ? t : 0;
+  const double *q0 = qh + (cb * nt + tt) * NN * NN * V;
+  const double *q1 = qh + (cn * nt + tt) * NN * NN * V;
+  double ql[V], qr[V], f[V], b[V];
+  // endpts2d (evaluations.cpp:20-35): dir 0 -> nodes (m, s); dir 1 -> (s, m)
+  long o0 = dir == 0 ? (long)s * V : (long)s * NN * V;
+  long st = dir == 0 ? (long)NN * V : (long)V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    ql[k] = C.endv[1][0] * q0[o0 + k] + C.endv[1][1] * q0[o0 + st + k];
+    qr[k] = C.endv[0][0] * q1[o0 + k] + C.endv[0][1] * q1[o0 + st + k];
+  }
+  double wt = time_dg ? dt * C.w[t] : dt;
+  double kk = wt / (2.0 * (dir == 0 ? dx : dy)) * C.w[s];
+  if (active) {
+    interface_point<L>(ql, qr, dir, P, C, f, b);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      f[k] = b[k] = 0.0;
+  }
+  double *out = fb + fi * 2 * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double lft = active ? kk * (b[k] + f[k]) : 0.0;
+    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
+    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
+    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
+    lft += __shfl_xor_sync(0xffffffffu, lft, 2);
+    rgt += __shfl_xor_sync(0xffffffffu, rgt, 2);
+    if (valid && lq == 0) {
+      out[k] = lft;
+      out[V + k] = rgt;
+    }
+  }
+}
+
+// Cell pass: one thread per (cell, space-time node): the volume term
+// w_t w_s (S - B dq/dx [- B dq/dy]) (fv.cpp:11-109), reduced over the cell's
+// NP lanes, then u += volume - face contributions.
+template <class L, int ND>
+__global__ void __launch_bounds__(128) k_cells(
+    double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
+    const double *__restrict__ fby, int nx, int ny, const uint8_t *__restrict__ mask,
+    double dt, const double *__restrict__ dt_dev, double dx, double dy, int sources,
+    int time_dg, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NS = ND == 1 ? NN : NN * NN;
+  constexpr int NP = NN * NS;
+  constexpr int XB = ND == 1 ? 1 : 2;
+  constexpr int YB = 1;
+  if (dt_dev)
+    dt = *dt_dev;
+  const double idx = 1.0 / dx, idy = 1.0 / dy;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int g = threadIdx.x % NP;
+  long c = gt / NP;  // interior cell (u index)
+  long ncell = ND == 1 ? nx : (long)nx * ny;
+  bool valid = c < ncell;
+  long cc = valid ? c : 0;
+  int ci = ND == 1 ? (int)cc : (int)(cc / ny), cj = ND == 1 ? 0 : (int)(cc % ny);
+  long cb = ND == 1 ? ci + 1 : (long)(ci + 1) * (ny + 2) + (cj + 1);
+  bool active = valid && (mask == nullptr || mask[cb]);
+  int t = g / NS, sidx = g % NS;
+  int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
+  int nt = time_dg ? NN : 1;
+  bool live = active && (time_dg || t == 0);
+  int tt = time_dg ? t : 0;
+  const double *qc = qh + ((cb * nt + tt) * NS + sidx) * V;
+  double q[V], other[V], dq[V], acc[V];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = qc[k];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  if (sources)
+    source<L::THERMAL, V>(q, s, P, acc);
+  else {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      acc[k] = 0.0;
+  }
+  shfl_vec<V>(q, other, XB);
+  {
+    double a = C.derv[i][i], b = C.derv[i][1 - i];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      dq[k] = a * q[k] + b * other[k];
+    double bd[V];
+    bdot<V, L::LSET>(s.v, dq, 0, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      acc[k] -= bd[k] * idx;
+  }
+  if (ND == 2) {
+    shfl_vec<V>(q, other, YB);
+    double a = C.derv[j][j], b = C.derv[j][1 - j];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      dq[k] = a * q[k] + b * other[k];
+    double bd[V];
+    bdot<V, L::LSET>(s.v, dq, 1, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      acc[k] -= bd[k] * idy;
+  }
+  double wt = time_dg ? dt * C.w[t] : dt;
+  double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double x = live ? wn * acc[k] : 0.0;
+#pragma unroll
+    for (int o = 1; o < NP; o <<= 1)
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+    acc[k] = x;
+  }
+  if (!valid || g != 0 || !active)
+    return;
+  double *uc = u + cc * V;
+  if (ND == 1) {
+    // face ci: R part, face ci+1: L part (fv.cpp:143-146)
+    const double *fl = fbx + (long)ci * 2 * V;
+    const double *fr = fbx + (long)(ci + 1) * 2 * V;
+    bool okl = mask == nullptr || (mask[ci] && mask[ci + 1]);
+    bool okr = mask == nullptr || (mask[ci + 1] && mask[ci + 2]);
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      double x = uc[k] + acc[k];
+      if (okr)
+        x -= fr[k];
+      if (okl)
+        x -= fl[V + k];
+      uc[k] = x;
+    }
+  } else {
+    // x faces (fi, fj) with fi = ci+1 (L part) and fi = ci (R part), fj = cj+1;
+    // y faces fi = ci+1 with fj = cj+1 (L part) and fj = cj (R part).
+    long fxl = (long)(ci + 1) * (ny + 1) + (cj + 1);  // L part to this cell
+    long fxr = (long)ci * (ny + 1) + (cj + 1);        // R part to this cell
+    long fyl = (long)(ci + 1) * (ny + 1) + (cj + 1);
+    long fyr = (long)(ci + 1) * (ny + 1) + cj;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      double x = uc[k] + acc[k];
+      x -= fbx[fxl * 2 * V + k];
+      x -= fbx[fxr * 2 * V + V + k];
+      x -= fby[fyl * 2 * V + k];
+      x -= fby[fyr * 2 * V + V + k];
+      uc[k] = x;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CFL time step (solvers/iterator.cpp:148-177): per-cell sum_d mae/dx_d,
+// block max, atomicMax on the bit pattern (non-negative doubles order as
+// unsigned integers); NaN cells are skipped as std::max skips them.
+template <class L>
+__global__ void __launch_bounds__(256) k_cfl_max(const double *__restrict__ u, long ncell,
+                                                 int nd, double dx, double dy,
+                                                 unsigned long long *__restrict__ out,
+                                                 DevPar P) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  double m = 0.0;
+  if (c < ncell) {
+    double q[V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      q[k] = u[c * V + k];
+    Prim<L::THERMAL> s;
+    prim<L::THERMAL>(q, P, s);
+    double tmp = max_abs_eigs<L::THERMAL>(q, s, 0, P) / dx;
+    if (nd == 2)
+      tmp += max_abs_eigs<L::THERMAL>(q, s, 1, P) / dy;
+    if (tmp > m)
+      m = tmp;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double sm[8];
+  if ((threadIdx.x & 31) == 0)
+    sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+      b = fmax(b, sm[w]);
+    atomicMax(out, (unsigned long long)__double_as_longlong(b));
+  }
+}
+
+__global__ void k_cfl_finalize(const unsigned long long *__restrict__ mx, double cfl, double t,
+                               double tf, int count, double *__restrict__ dt_out) {
+  double MAX = __longlong_as_double((long long)*mx);
+  double dt = cfl / MAX;
+  if (count <= 5)
+    dt *= 0.2;
+  if (t + dt > tf)
+    dt = tf - t;
+  *dt_out = dt;
+}
+
+// Device clock of the device-resident time loop: [t, dt, tf, cfl, count].
+// The CFL finalize reads t/count and writes dt (0 once t >= tf); the advance
+// kernel adds dt to t and counts the step.
+__global__ void k_clock_finalize(const unsigned long long *__restrict__ mx,
+                                 double *__restrict__ clk) {
+  double t = clk[0], tf = clk[2], cfl = clk[3];
+  long count = (long)clk[4];
+  double dt = 0.0;
+  if (t < tf) {
+    double MAX = __longlong_as_double((long long)*mx);
+    dt = cfl / MAX;
+    if (count <= 5)
+      dt *= 0.2;
+    if (t + dt > tf)
+      dt = tf - t;
+  }
+  clk[1] = dt;
+}
+
+__global__ void k_clock_advance(double *__restrict__ clk) {
+  if (clk[1] > 0.0) {
+    clk[0] += clk[1];
+    clk[4] += 1.0;
+  }
+}
+
+// renorm_distortion (solvers/utils.cpp:6-23); skipped when the device clock
+// says the step did not run (dt == 0).
+template <int V>
+__global__ void k_renorm(double *__restrict__ u, long ncell, double rho0,
+                         const double *__restrict__ dt_dev) {
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  if (dt_dev && *dt_dev == 0.0)
+    return;
+  double *q = u + c * V;
+  double r = q[0];
+  if (r > 0) {
+    double A[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      A[k] = q[5 + k];
+    double f = cbrt(r / (rho0 * det3(A)));
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      q[5 + k] = A[k] * f;
+  }
+}
+
+}  // namespace gpr

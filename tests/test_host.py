@@ -1,0 +1,93 @@
+"""Host-side checks that need no GPU: the C-ABI library builds, loads and
+exports every entry point include/gpr_gb300.h declares; the parameter
+builder matches the reference's defaults; problem factories have the
+configured shapes."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    txt = open(os.path.join(ROOT, "include", "gpr_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gpr_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from phd_gb300 import _lib
+    path = _lib.build()
+    lib = ctypes.CDLL(path)
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding table covers them
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def test_library_reports_version_without_gpu():
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    assert lib.gpr_version() >= 100
+    buf = (ctypes.c_int32 * 8)()
+    n = lib.gpr_supported_nvars(ctypes.cast(buf, ctypes.c_void_p), 8)
+    assert 17 in list(buf)[:n]
+
+
+def test_scratch_queries_and_argument_errors_without_gpu():
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    nX = (ctypes.c_int32 * 2)(512, 512)
+    p = ctypes.cast(nX, ctypes.c_void_p)
+    assert lib.gpr_ader_scratch_doubles(p, 2, 17) > 514 * 514 * 8 * 17
+    assert lib.gpr_ader_scratch_doubles(p, 2, 16) == -3  # unsupported V
+    assert lib.gpr_ader_scratch_doubles(p, 3, 17) == -1  # bad ndim
+    bad = (ctypes.c_int32 * 1)(0)
+    assert lib.gpr_weno_scratch_doubles(ctypes.cast(bad, ctypes.c_void_p), 1, 17) == -1
+
+
+def test_material_params_defaults():
+    from phd_gb300.params import material_params, Par
+    MP = material_params("sg", 1.0, cv=2.5, gamma=1.4, b0=1.0, calpha=1.0, mu=1e-2, Pr=2 / 3)
+    assert MP.EOS == 0 and MP.n == 1 and not MP.POWER_LAW and not MP.SOLID
+    assert MP.b02 == 1.0 and MP.calpha2 == 1.0 and MP.pINF == 0 and MP.Tref == 0
+    assert abs(MP.kappa - 0.0525) < 1e-15
+    back = Par.from_array(MP.to_array())
+    for k in ("rho0", "cv", "gamma", "b02", "mu", "n", "calpha2", "kappa"):
+        assert getattr(back, k) == getattr(MP, k)
+    elastic = material_params("sg", 1.0, gamma=1.4, b0=1.0)
+    assert elastic.SOLID and not elastic.POWER_LAW
+
+
+def test_problem_shapes():
+    from phd_gb300 import problems
+    u, MP, tf, dX, bcs = problems.shock_tube()
+    assert u.shape == (200, 17) and tf == 0.2 and bcs == "transitive"
+    assert np.all(u[:100, 0] == 1.0) and np.all(u[100:, 0] == 0.125)
+    u, MP, tf, dX, bcs = problems.taylor_green(n=8)
+    assert u.shape == (8, 8, 17) and bcs == "periodic"
+    u, MP, tf, dX, bcs = problems.stokes()
+    assert u.shape == (400, 17)
+    insts = problems.batched_shock_tubes(count=4)
+    assert len(insts) == 4 and all(128 <= i[0].shape[0] <= 2048 for i in insts)
+
+
+def test_cvec_matches_reference_energy():
+    """Cvec reproduces the reference's conserved energy on the golden states."""
+    from conftest import golden
+    from phd_gb300.params import Par
+    from oracle import Oracle
+    g = golden("pointwise_v17.npz")
+    O = Oracle()
+    for m in range(g["Q"].shape[0]):
+        MP = Par.from_array(g["mp_arrays"][m])
+        for Q in g["Q"][m][:6]:
+            p = O.pressure(Q, MP)
+            from phd_gb300.params import Cvec
+            Q2 = Cvec(Q[0], p, Q[2:5] / Q[0], MP, Q[5:14].reshape(3, 3), Q[14:17] / Q[0])
+            assert np.allclose(Q2, Q, rtol=1e-13, atol=1e-13)
