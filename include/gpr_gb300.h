@@ -176,6 +176,24 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX,
                 const uint8_t *mask, double *clock, int nsteps, double *scratch,
                 int32_t *status, int nvar, void *stream);
 
+/* One 1D ADER-WENO step that allocates nothing and takes no scratch.  It has
+ * no counterpart in the reference.  It is for callers that cannot allocate
+ * device memory (an application that owns the device through its own fixed
+ * pool, or a loop where an allocation would synchronise the device): the
+ * WENO, predictor and face-flux scratch comes from a fixed array compiled
+ * into the library, sized for nx <= GPR_NOALLOC_MAX_CELLS cells of at most 17
+ * variables (about 4.5 MB, held by every GPU that loads the library until the
+ * process exits).  Larger grids are rejected with GPR_E_TOO_LARGE.  The
+ * array's device address is looked up on the first call made on each device,
+ * so that first call must come before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by
+ * the caller.  Otherwise as gpr_ader_stepper with ndim = 1. */
+#define GPR_NOALLOC_MAX_CELLS 4096
+int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
+                                double dt, double dx, int stiff, int flux,
+                                const gpr_par *par, const uint8_t *mask,
+                                int32_t *status, int nvar, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,
  * eig.cpp): batched over `count` states Q[count][V].                        */

@@ -541,3 +541,98 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free 1D ADER step.
+//
+// Some callers cannot allocate device memory at all: a host application
+// that owns the whole device through its own fixed pool (and forbids any
+// other cudaMalloc), or a latency-critical loop where an allocation would
+// synchronise the device.  For them this entry point takes its scratch (the
+// WENO reconstruction, the space-time predictor and the face fluxes) from a
+// fixed array compiled into the library instead of from the caller.
+//
+// The array is sized for up to GPR_NOALLOC_MAX_CELLS cells of up to 17
+// variables (about 4.5 MB) and every GPU that loads the library holds it
+// until the process exits.  Its device address is looked up once per device
+// (cudaGetSymbolAddress, with that device current) on the first call made on
+// that device, so that first call must come before any stream capture.
+// Every call shares the array and it keeps the last call's contents; nothing
+// in it has to start at zero (each call overwrites what it reads), but calls
+// that overlap on the GPU (different streams, or different host threads on
+// one device) race on it and must be serialised by the caller.
+namespace {
+
+constexpr long kNoallocDoubles =
+    ((long)(GPR_NOALLOC_MAX_CELLS + 2) * NN * 17)            // wh
+    + ((long)(GPR_NOALLOC_MAX_CELLS + 2) * NN * NN * 17)     // qh
+    + ((long)(GPR_NOALLOC_MAX_CELLS + 1) * 2 * 17);          // face fluxes
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
+
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[256] = {nullptr};
+
+int noalloc_scratch(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
+    return GPR_E_CUDA;
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      fprintf(stderr, "gpr_gb300: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+      return GPR_E_CUDA;
+    }
+    g_noalloc_ptr[dev] = (double *)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GPR_OK;
+}
+
+}  // namespace
+
+extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx, double dt,
+                                           double dx, int stiff, int flux, const gpr_par *par,
+                                           const uint8_t *mask, int32_t *status, int nvar,
+                                           void *stream) {
+  if (!u || !ub || !par || nx < 1)
+    return GPR_E_ARG;
+  if (nx > GPR_NOALLOC_MAX_CELLS || nvar > 17)
+    return GPR_E_TOO_LARGE;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  double *scr = nullptr;
+  int rc = noalloc_scratch(&scr);
+  if (rc)
+    return rc;
+  int32_t nX[1] = {nx};
+  double dX[1] = {dx};
+  long ncb = nx + 2;
+  double *wh = scr;
+  double *qh = wh + ncb * NN * nvar;
+  double *fb = qh + ncb * NN * NN * nvar;
+  DevPar P = make_devpar(*par);
+  cudaStream_t st = S(stream);
+  switch (nvar) {
+  case 17: {
+    using O = Ops<L17>;
+    if ((rc = O::weno(wh, ub, nX, 1, nullptr, st)))
+      return rc;
+    if ((rc = O::predictor(qh, wh, dt, nullptr, dX, 1, nX, stiff, P, mask, status, st)))
+      return rc;
+    return O::fv(u, qh, nX, dt, nullptr, dX, 1, 1, 1, P, mask, fb, st);
+  }
+  case 14: {
+    using O = Ops<L14>;
+    if ((rc = O::weno(wh, ub, nX, 1, nullptr, st)))
+      return rc;
+    if ((rc = O::predictor(qh, wh, dt, nullptr, dX, 1, nX, stiff, P, mask, status, st)))
+      return rc;
+    return O::fv(u, qh, nX, dt, nullptr, dX, 1, 1, 1, P, mask, fb, st);
+  }
+  default:
+    return GPR_E_UNSUPPORTED;
+  }
+}
