@@ -128,6 +128,16 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     int flux, const gpr_par *par, const uint8_t *mask,
                     double *scratch, int nvar, void *stream);
 
+/* The face pass of gpr_fv_launcher alone (interfs1/interfs2, fv.cpp:111-279):
+ * writes, per face and direction, the contribution subtracted from the left
+ * cell (fb[face][0][V]) and from the right cell (fb[face][1][V]) into fb,
+ * which has gpr_fv_scratch_doubles(nX, ndim, nvar) doubles (x faces first,
+ * then y faces in 2D, each (nx+1)(ny+1) faces). */
+int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt,
+                       const double *dX, int ndim, int time_dg, int flux,
+                       const gpr_par *par, const uint8_t *mask, double *fb,
+                       int nvar, void *stream);
+
 /* Replaces solvers.timestep (solvers/iterator.cpp:148-177) for one material:
  * dt = CFL / max_cells sum_d max_abs_eigs/dx_d, x0.2 while count <= 5,
  * clipped to tf - t.  The result is written to dt_out (device double).

@@ -75,6 +75,7 @@ SIGNATURES = {
     "gpr_predictor": (_I, [_P, _P, _D, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
     "gpr_fv_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_fv_launcher": (_I, [_P, _P, _P, _D, _P, _I, _I, _I, _I, _P, _P, _P, _I, _P]),
+    "gpr_fv_face_fluxes": (_I, [_P, _P, _D, _P, _I, _I, _I, _P, _P, _P, _I, _P]),
     "gpr_timestep_scratch_doubles": (_I, [_I64]),
     "gpr_timestep": (_I, [_P, _I64, _P, _I, _D, _D, _D, _I, _P, _P, _P, _I, _P]),
     "gpr_renorm_distortion": (_I, [_P, _I64, _P, _I, _P]),

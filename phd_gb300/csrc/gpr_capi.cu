@@ -212,6 +212,30 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
+  // Face pass of the FV update only: the k_faces kernels writing the face
+  // contributions (to the left and right cells) into fb.
+  static int faces(const double *qh, const int32_t *nX, double dt, const double *dX, int nd,
+                   int time_dg, const DevPar &P, const uint8_t *mask, double *fb,
+                   cudaStream_t st) {
+    const Consts &C = consts();
+    int nx = nX[0];
+    if (nd == 1) {
+      long nf = (long)(nx + 1) * NN;
+      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, nx, mask, dt, nullptr, dX[0],
+                                                     time_dg, P, C);
+      return cuda_rc();
+    }
+    int ny = nX[1];
+    long nf = (long)(nx + 1) * (ny + 1);
+    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb, qh, nx, ny, 0, mask, dt,
+                                                             nullptr, dX[0], dX[1], time_dg,
+                                                             P, C);
+    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb + nf * 2 * V, qh, nx, ny, 1,
+                                                             mask, dt, nullptr, dX[0], dX[1],
+                                                             time_dg, P, C);
+    return cuda_rc();
+  }
+
   static int timestep(const double *u, long ncell, const double *dX, int nd, double cfl,
                       double t, double tf, int count, const DevPar &P, double *dt_out,
                       double *scratch, cudaStream_t st) {
@@ -443,6 +467,17 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, sources, time_dg, P, mask, scratch,
                        S(stream)))
+}
+
+int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt, const double *dX,
+                       int ndim, int time_dg, int flux, const gpr_par *par,
+                       const uint8_t *mask, double *fb, int nvar, void *stream) {
+  if (!qh || !dX || !par || !fb || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV)
+    return GPR_E_UNSUPPORTED;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::faces(qh, nX, dt, dX, ndim, time_dg, P, mask, fb, S(stream)))
 }
 
 int gpr_timestep_scratch_doubles(int64_t ncell) {

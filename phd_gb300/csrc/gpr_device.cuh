@@ -32,6 +32,8 @@ struct DevPar {
   double dp0, dp1, dp2;
   double th1c;   // rho0 / (2 mu^(1/n))          (sources.cpp:71)
   double tau1;   // 6 mu^(1/n) / (rho0 b02)      (analytic.cpp:62)
+  double iG;     // 1/Gamma for the constant-Gamma EOS; 1/(Gamma0 rho0) for shock MG
+  double C0f;    // 1 - beta/Gamma for the constant-Gamma EOS
 };
 
 inline DevPar make_devpar(const gpr_par &p) {
@@ -67,6 +69,9 @@ inline DevPar make_devpar(const gpr_par &p) {
   d.dp2 = p.dp[2];
   d.th1c = p.rho0 / (2.0 * pow(p.mu, 1.0 / p.n));
   d.tau1 = 6.0 * pow(p.mu, 1.0 / p.n) / (p.rho0 * p.b02);
+  double G = p.EOS == 0 ? p.gamma - 1.0 : (p.EOS == 4 ? p.gamma : p.Gamma0);
+  d.iG = p.EOS == 1 ? 1.0 / (p.Gamma0 * p.rho0) : 1.0 / G;
+  d.C0f = 1.0 - p.beta / G;
   return d;
 }
 
@@ -164,6 +169,7 @@ template <bool TH> struct Prim {
   double cs2;            // b02 (rho/rho0)^beta
   double devGsq;         // |dev G|^2
   double p, T;           // pressure, temperature
+  double irG;            // 1 / (rho Gamma)
   EosRho e;
 };
 
@@ -193,7 +199,10 @@ GPR_D void prim(const double *q, const DevPar &P, Prim<TH> &s) {
   }
   s.e = eos_rho(s.r, s.ir, P);
   s.cs2 = P.beta == 0.0 ? P.b02 : P.b02 * pow(s.r * P.ir0, P.beta);
-  double C0 = (1.0 - P.beta / s.e.G) * s.cs2;
+  // C_0 = (1 - beta/Gamma) cs2 (shear.cpp:23-29); rho Gamma = Gamma0 rho0 for shock MG
+  double C0 = P.beta == 0.0 ? s.cs2
+                            : (P.EOS == 1 ? (1.0 - P.beta / s.e.G) : P.C0f) * s.cs2;
+  s.irG = P.EOS == 1 ? P.iG : s.ir * P.iG;
   double E1 = q[1] * s.ir - 0.5 * (s.v[0] * s.v[0] + s.v[1] * s.v[1] + s.v[2] * s.v[2]) -
               0.25 * C0 * s.devGsq;
   if (TH) {
@@ -205,7 +214,7 @@ GPR_D void prim(const double *q, const DevPar &P, Prim<TH> &s) {
   // pressure_mg (mg.cpp:126-131), temperature_mg (mg.cpp:133-139)
   double rG = s.r * s.e.G;
   s.p = (E1 - s.e.er) * rG + s.e.pr;
-  s.T = s.e.phi * P.Tref + (s.p - s.e.pr) / (rG * P.cv);
+  s.T = s.e.phi * P.Tref + (s.p - s.e.pr) * s.irG * P.icv;
 }
 
 // sigma column d: -rho cs2 (A devG)^T A(:,d)   (state.cpp:23-29)
@@ -536,6 +545,90 @@ template <int n> GPR_D double max_abs_eig(double (&H)[n][n]) {
   return best;
 }
 
+// Largest eigenvalue of a small real matrix whose spectrum is dominated by a
+// simple, real, positive eigenvalue (the squared fastest wave speed of the
+// thermo-acoustic tensor): characteristic polynomial by principal minors,
+// Laguerre's iteration (cubically convergent, monotone from an upper bound
+// for real-rooted polynomials) started at the infinity-norm bound, then a
+// certificate: the polynomial deflated by (x - lambda) must have every root
+// strictly inside |z| < (1 - 1e-9) lambda (Jury's criterion on the scaled
+// quotient).  Returns false when the certificate fails (complex roots of
+// larger modulus, a multiple largest root, no convergence); the caller then
+// runs the QR iteration, so the result is max |eig| either way.
+template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &lam) {
+  static_assert(m == 3 || m == 4, "3x3 or 4x4");
+  double c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0;
+#pragma unroll
+  for (int i = 0; i < m; i++)
+    c1 += X[i][i];
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = i + 1; j < m; j++)
+      c2 += X[i][i] * X[j][j] - X[i][j] * X[j][i];
+  auto det3 = [&](int a, int b, int c) {
+    return X[a][a] * (X[b][b] * X[c][c] - X[b][c] * X[c][b]) -
+           X[a][b] * (X[b][a] * X[c][c] - X[b][c] * X[c][a]) +
+           X[a][c] * (X[b][a] * X[c][b] - X[b][b] * X[c][a]);
+  };
+  if (m == 3) {
+    c3 = det3(0, 1, 2);
+  } else {
+    c3 = det3(0, 1, 2) + det3(0, 1, 3) + det3(0, 2, 3) + det3(1, 2, 3);
+    // det of the 4x4 by complementary 2x2 minors of rows (0,1) and (2,3)
+    const int r2 = m == 4 ? 2 : 0, r3 = m == 4 ? 3 : 0;
+    auto s = [&](int a, int b) { return X[0][a] * X[1][b] - X[0][b] * X[1][a]; };
+    auto t = [&](int a, int b) { return X[r2][a] * X[r3][b] - X[r2][b] * X[r3][a]; };
+    c4 = s(0, 1) * t(2, 3) - s(0, 2) * t(1, 3) + s(0, 3) * t(1, 2) + s(1, 2) * t(0, 3) -
+         s(1, 3) * t(0, 2) + s(2, 3) * t(0, 1);
+  }
+  // p(x) = x^m - c1 x^(m-1) + c2 x^(m-2) - c3 x^(m-3) [+ c4]
+  double R = 0.0;
+#pragma unroll
+  for (int i = 0; i < m; i++) {
+    double rs = 0.0;
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      rs += fabs(X[i][j]);
+    R = fmax(R, rs);
+  }
+  double x = R * (1.0 + 1e-12) + 1e-300;
+  for (int it = 0; it < 16; it++) {
+    double p = 1.0, dp = 0.0, d2p = 0.0;
+    const double cf[4] = {-c1, c2, -c3, c4};
+#pragma unroll
+    for (int k = 0; k < m; k++) {
+      d2p = d2p * x + 2.0 * dp;
+      dp = dp * x + p;
+      p = p * x + cf[k];
+    }
+    if (p == 0.0)
+      break;
+    double ip = 1.0 / p;
+    double G = dp * ip;
+    double H = G * G - d2p * ip;
+    double disc = fmax((m - 1) * (m * H - G * G), 0.0);
+    double a = m / (G + copysign(sqrt(disc), G));
+    x -= a;
+    if (!(fabs(a) > 1e-5 * fabs(x)))  // cubic convergence: the error is now ~|a|^3
+      break;
+  }
+  lam = x;
+  if (!(x > 0.0) || !(x <= R * (1.0 + 1e-9)))
+    return false;
+  // deflate and certify: all other roots strictly inside |z| < (1-1e-9) lam
+  double l = x * (1.0 - 1e-9);
+  double q2 = -c1 + x, q1 = c2 + x * q2;
+  if (m == 3) {
+    double a1 = q2 / l, a0 = q1 / (l * l);
+    return fabs(a0) < 1.0 && fabs(a1) < 1.0 + a0;
+  }
+  double q0 = -c3 + x * q1;
+  double a2 = q2 / l, a1 = q1 / (l * l), a0 = q0 / (l * l * l);
+  return (1.0 + a2 + a1 + a0 > 0.0) && (1.0 - a2 + a1 - a0 > 0.0) && fabs(a0) < 1.0 &&
+         fabs(a0 * a0 - 1.0) > fabs(a0 * a2 - a1);
+}
+
 // max |eigenvalue| of the GPR system in direction d (system/eig.cpp:8-77):
 // |v_d| + sqrt(max |eig(Xi1 Xi2)|).  Xi1 (4x5) and Xi2 (5x4) are assembled
 // implicitly: Xi = Xi1 Xi2 is formed directly from its nonzero blocks.
@@ -564,11 +657,15 @@ GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPa
   double dsr[3] = {fr * sg[0], fr * sg[1], fr * sg[2]};
   // c0^2 = (p/rho^2 - dE/drho) / dE/dp   (waves/speeds.cpp:8-18)
   const EosRho &e = s.e;
-  double rG = r * e.G;
-  double dedr = e.der - (e.dpr * rG + (e.G + r * e.dG) * (s.p - e.pr)) / (rG * rG);
+  double rG = r * e.G, irG2 = s.irG * s.irG;
+  double dnum = e.dpr * rG + (e.G + r * e.dG) * (s.p - e.pr);
+  double dedr = e.der - dnum * irG2;
   double cs2 = s.cs2;
-  double dcs2 = P.beta * ir * cs2;
-  double dC0 = (1.0 - P.beta / e.G) * dcs2 + P.beta / (e.G * e.G) * e.dG * cs2;
+  double dC0 = 0.0;
+  if (P.beta != 0.0) {
+    double dcs2 = P.beta * ir * cs2;
+    dC0 = (1.0 - P.beta / e.G) * dcs2 + P.beta / (e.G * e.G) * e.dG * cs2;
+  }
   double dEdr = dedr + 0.25 * dC0 * s.devGsq;
   double c02 = (s.p * ir * ir - dEdr) * rG;  // dE/dp = 1/(rho Gamma)
   // Xi2 row 1: b = sigma - rho dsigma/drho + rho c0^2 e_d ; h = calpha2 T Gamma
@@ -590,8 +687,8 @@ GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPa
     }
   if (TH) {
     double h = P.calpha2 * s.T * e.G;
-    double tp = ir / (rG * P.cv);  // dT/dp / rho
-    double dTr = -(e.dpr * rG + (e.G + r * e.dG) * (s.p - e.pr)) / (rG * rG) * P.icv;
+    double tp = ir * s.irG * P.icv;  // dT/dp / rho
+    double dTr = -dnum * irG2 * P.icv;
     X[0][m - 1] = h * ir;
     X[1][m - 1] = 0.0;
     X[2][m - 1] = 0.0;
@@ -600,7 +697,10 @@ GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPa
     X[m - 1][2] = tp * b[2];
     X[m - 1][m - 1] = tp * h;
   }
-  double lam = sqrt(max_abs_eig<m>(X));
+  double l2;
+  if (!max_eig_laguerre<m>(X, l2))
+    l2 = max_abs_eig<m>(X);  // QR fallback: complex or multiple dominant roots
+  double lam = sqrt(l2);
   double vd = s.v[d];
   return vd > 0 ? vd + lam : lam - vd;
 }
