@@ -336,10 +336,14 @@ def run_gb300(args):
     value = ncell * world * args.steps / (ms * 1e-3) / 1e6
     st = status.cpu().numpy()
     iters = (st >> 8)
-    picard_ok = (st & 0xff) == 0
+    kind = st & 0xff
+    picard_ok = kind == 0
+    newton = kind == 1
     hist = np.bincount(iters[picard_ok], minlength=1).tolist()
-    mean_iters = float(iters[picard_ok].mean()) if picard_ok.any() else float("nan")
-    failed = int((~picard_ok).sum())
+    nhist = np.bincount(iters[newton], minlength=1).tolist() if newton.any() else []
+    mean_iters = float(iters[picard_ok].mean()) if picard_ok.any() else 0.0
+    mean_newton = float(iters[newton].mean()) if newton.any() else 0.0
+    failed = int((kind == 2).sum())
     clk = clock.cpu().numpy()
 
     # stage timing (CUDA events on the launching stream) for the roofline
@@ -385,7 +389,11 @@ def run_gb300(args):
                        "l2": "per-step working set (u, ub, wh, qh: ~0.5 GB) exceeds the "
                              "129 MB L2; no flush needed"},
             "predictor": {"picard_iteration_histogram": hist,
-                          "mean_picard_iterations": mean_iters, "picard_failed_cells": failed},
+                          "mean_picard_iterations": mean_iters,
+                          "newton_cells": int(newton.sum()),
+                          "newton_iteration_histogram": nhist,
+                          "mean_newton_iterations": mean_newton,
+                          "unconverged_cells": failed},
             "sim_time": float(clk[0]), "sim_steps": int(clk[4]),
             "stage_ms": stage_ms,
             "roofline": roof,

@@ -107,11 +107,15 @@ int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX,
 /* Replaces solvers.dg.predictor (solvers/dg/dg.h:7, dg1.cpp:75-131,
  * dg2.cpp:102-171): local space-time Galerkin predictor of every masked cell.
  * Picard iteration with the reference's initial guess, update and per-cell
- * stopping rule; cells where Picard does not converge within its iteration
- * cap (or produces NaN) are finished by a Newton solve of the same fixed
- * point.  `status` (optional, one int32 per predictor cell) receives
- * GPR_PRED_* in the low byte and the Picard iteration count << 8.
- * stiff=1 skips Picard and goes straight to Newton (the reference's STIFF). */
+ * stopping rule (|dq| <= 6e-6 (1 + |q|), at most 50 iterations).  Cells where
+ * Picard does not converge (the reference leaves their rows unwritten) or
+ * produces NaN (the reference switches to Newton-Krylov) are finished by a
+ * stiff-source Newton iteration on the same fixed point, implicit in the
+ * relaxation sources, to |dq| <= 1e-11 (1 + |q|).  `status` (optional, one
+ * int32 per predictor cell) receives GPR_PRED_* in the low byte and the
+ * iteration count of the pass that finished the cell << 8.  stiff=1 skips
+ * Picard and goes straight to the Newton iteration (the reference's STIFF).
+ * The output rows of every masked cell are always written. */
 int gpr_predictor(double *qh, const double *wh, double dt, const double *dX,
                   int ndim, const int32_t *nX, int stiff, const gpr_par *par,
                   const uint8_t *mask, int32_t *status, int nvar,

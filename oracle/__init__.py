@@ -45,6 +45,7 @@ def _load():
             "or_configure": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, ctypes.c_int]),
             "or_nvar": (ctypes.c_int, []),
+            "or_set_stiff": (None, [ctypes.c_double, ctypes.c_int]),
             "or_constants": (None, [_dp]),
             "or_pressure": (ctypes.c_double, [_dp, P]),
             "or_temperature": (ctypes.c_double, [_dp, P]),

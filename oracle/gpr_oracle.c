@@ -35,6 +35,9 @@ static const double LAMC = 1e5;
 static const double WENO_EPS = 1e-14;
 static double DG_TOL = 6e-6;
 static int DG_IT = 50;
+/* stiff-source Newton iteration: tolerance on the update and iteration cap */
+static double STIFF_TOL = 1e-11;
+static int STIFF_IT = 60;
 
 static int N = 2, V = 17, THERMAL = 1, LSET = 0;
 static int FN2 = 0, CN2 = 1;
@@ -261,6 +264,11 @@ int or_configure(int n, int thermal, int lset, double dg_tol, int dg_it) {
 }
 
 int or_nvar(void) { return V; }
+
+void or_set_stiff(double tol, int maxit) {
+  STIFF_TOL = tol;
+  STIFF_IT = maxit;
+}
 
 /* Exposes the constants for the tests: NODES, WGHTS, ENDVALS, DERVALS,
  * DG_DER, DG_MAT, SIG, mLinv, mRinv (each padded to MAXN x MAXN). */
@@ -2003,6 +2011,216 @@ static int dg_newton(int ndim, double *q, const double *Ww, double dt,
   return -1;
 }
 
+/* Stiff-source Jacobian blocks at one state: the distortion block
+ * JA[9][9] = dS_A/dA and the heat-flux block JJ[3][3] = dS_J/d(rho J).
+ * S_A = -cs2 theta1(det A) A devG(A) (equations.cpp:156-159), with
+ *   d(A devG)/dA : X -> X devG + A X^T A + A A^T X - 2/3 (A:X) A,
+ *   d theta1/dA : X -> 5/3 theta1 tr(A^-1 X) (theta1 ~ det(A)^(5/3));
+ * S_J = -calpha2 J T / kappa with J = rho J / rho and
+ *   dT/d(rho J_k) = -calpha2 J_k / (rho cv Gamma rho) * rho Gamma = -calpha2 J_k / (rho cv).
+ * Only the Newtonian relaxation rate is differentiated; other rates use
+ * the same expression with their theta1 (a quasi-Newton Jacobian). */
+static void stiff_jacobian(const double *Q, const gpr_par *P, double JA[9][9],
+                           double JJ[3][3]) {
+  double r = Q[0];
+  const double *A = Q + 5;
+  double cs2 = c_s2(r, P);
+  double th = theta1inv(Q, P);
+  double G[9], dG[9], H[9], AG[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+      H[3 * i + j] = A[3 * i] * A[3 * j] + A[3 * i + 1] * A[3 * j + 1] + A[3 * i + 2] * A[3 * j + 2];
+    }
+  double t3 = (G[0] + G[4] + G[8]) / 3;
+  for (int k = 0; k < 9; k++)
+    dG[k] = G[k];
+  dG[0] -= t3;
+  dG[4] -= t3;
+  dG[8] -= t3;
+  AdevG(A, AG);
+  /* A^-1 (for the det term) */
+  double d = det3(A);
+  double Ai[9];
+  Ai[0] = (A[4] * A[8] - A[5] * A[7]) / d;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) / d;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) / d;
+  Ai[3] = (A[5] * A[6] - A[3] * A[8]) / d;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) / d;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) / d;
+  Ai[6] = (A[3] * A[7] - A[4] * A[6]) / d;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) / d;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) / d;
+  int newtonian = !(P->flags & (GPR_SOLID | GPR_POWER_LAW | GPR_BINGHAM));
+  for (int m = 0; m < 3; m++)
+    for (int n = 0; n < 3; n++) {
+      int c = 3 * m + n;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double v = (i == m ? dG[3 * n + j] : 0.0) + A[3 * i + n] * A[3 * m + j] +
+                     (n == j ? H[3 * i + m] : 0.0) - 2.0 / 3.0 * A[3 * i + j] * A[3 * m + n];
+          double dth = newtonian ? 5.0 / 3.0 * th * Ai[3 * n + m] : 0.0;
+          JA[3 * i + j][c] = -cs2 * (th * v + AG[3 * i + j] * dth);
+        }
+    }
+  for (int l = 0; l < 3; l++)
+    for (int k = 0; k < 3; k++)
+      JJ[l][k] = 0.0;
+  if (THERMAL) {
+    double T = or_temperature(Q, P);
+    double J[3] = {Q[14] / r, Q[15] / r, Q[16] / r};
+    double f = -P->calpha2 / P->kappa;
+    for (int l = 0; l < 3; l++)
+      for (int k = 0; k < 3; k++) {
+        double dT = -P->calpha2 * J[k] / (r * P->cv);
+        JJ[l][k] = f * ((l == k ? T / r : 0.0) + J[l] * dT);
+      }
+  }
+}
+
+/* Dense solve with partial pivoting, n <= 24, A row-major n x n. */
+static int small_solve(int n, double *A, double *b) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++)
+      if (fabs(A[r * n + c]) > fabs(A[p * n + c]))
+        p = r;
+    if (A[p * n + c] == 0.0)
+      return -1;
+    if (p != c) {
+      for (int j = 0; j < n; j++) {
+        double t = A[c * n + j];
+        A[c * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
+      double t = b[c];
+      b[c] = b[p];
+      b[p] = t;
+    }
+    double inv = 1.0 / A[c * n + c];
+    for (int r = c + 1; r < n; r++) {
+      double f = A[r * n + c] * inv;
+      if (f == 0.0)
+        continue;
+      for (int j = c; j < n; j++)
+        A[r * n + j] -= f * A[c * n + j];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    double s = b[r];
+    for (int j = r + 1; j < n; j++)
+      s -= A[r * n + j] * b[j];
+    b[r] = s / A[r * n + r];
+  }
+  return 0;
+}
+
+/* Stiff-source Newton iteration on the predictor fixed point
+ *   Fp(q) = DG_U q - Ww - dt R(q) = 0:
+ *   delta = (DG_U - dt W dS/dq)^-1 (Ww + dt R(q) - DG_U q),  q += delta,
+ * with dS/dq the local source Jacobian (stiff_jacobian) at each space-time
+ * node, so the correction is implicit in the relaxation sources and explicit
+ * in the fluxes.  With dS/dq = 0 this is exactly the Picard update of
+ * dg1.cpp:110.  Per spatial node the system couples the N time nodes through
+ * DG_MAT: an (N*9) system for A, an (N*3) system for rho J and the DG_MAT
+ * solve for the other variables.  Returns iterations, or -1. */
+static int dg_stiff(int ndim, double *q, const double *Ww, double dt, const double *dX,
+                    const gpr_par *P, double tol, int maxit) {
+  int ns = ndim == 1 ? N : N * N;
+  int nn = N * ns;
+  double r[2 * MAXN * MAXN * MAXN * MAXV], g[2 * MAXN * MAXN * MAXN * MAXV];
+  double JA[MAXN * MAXN * MAXN][9][9], JJ[MAXN * MAXN * MAXN][3][3];
+  for (int it = 0; it < maxit; it++) {
+    dg_rhs(ndim, q, Ww, dt, dX, P, r);
+    /* g = r - DG_U q */
+    for (int t = 0; t < N; t++)
+      for (int s = 0; s < ns; s++) {
+        double ws = ndim == 1 ? WGHTS[s] : WGHTS[s / N] * WGHTS[s % N];
+        for (int k = 0; k < V; k++) {
+          double uq = 0.0;
+          for (int m = 0; m < N; m++)
+            uq += DG_MAT[t][m] * q[(m * ns + s) * V + k];
+          g[(t * ns + s) * V + k] = r[(t * ns + s) * V + k] - ws * uq;
+        }
+      }
+    for (int n = 0; n < nn; n++)
+      stiff_jacobian(q + n * V, P, JA[n], JJ[n]);
+    double dmax = 0.0;
+    int bad = 0;
+    for (int s = 0; s < ns; s++) {
+      double ws = ndim == 1 ? WGHTS[s] : WGHTS[s / N] * WGHTS[s % N];
+      /* non-stiff variables: DG_MAT solve (rows of S are zero there) */
+      for (int k = 0; k < V; k++) {
+        if ((k >= 5 && k < 14) || (THERMAL && k >= 14 && k < 17))
+          continue;
+        for (int t = 0; t < N; t++) {
+          double acc = 0.0;
+          for (int m = 0; m < N; m++)
+            acc += DG_MATinv[t][m] * g[(m * ns + s) * V + k];
+          r[(t * ns + s) * V + k] = acc / ws;
+        }
+      }
+      /* distortion block: (DG_MAT x I9 - dt W_t JA_t) dA = gA / W_s */
+      {
+        int n9 = 9 * N;
+        double K[9 * MAXN * 9 * MAXN], b[9 * MAXN];
+        for (int t = 0; t < N; t++)
+          for (int i = 0; i < 9; i++) {
+            int row = t * 9 + i;
+            b[row] = g[(t * ns + s) * V + 5 + i] / ws;
+            for (int t2 = 0; t2 < N; t2++)
+              for (int j = 0; j < 9; j++)
+                K[row * n9 + t2 * 9 + j] =
+                    (i == j ? DG_MAT[t][t2] : 0.0) -
+                    (t == t2 ? dt * WGHTS[t] * JA[t * ns + s][i][j] : 0.0);
+          }
+        if (small_solve(n9, K, b))
+          bad = 1;
+        for (int t = 0; t < N; t++)
+          for (int i = 0; i < 9; i++)
+            r[(t * ns + s) * V + 5 + i] = b[t * 9 + i];
+      }
+      if (THERMAL) {
+        int n3 = 3 * N;
+        double K[3 * MAXN * 3 * MAXN], b[3 * MAXN];
+        for (int t = 0; t < N; t++)
+          for (int i = 0; i < 3; i++) {
+            int row = t * 3 + i;
+            b[row] = g[(t * ns + s) * V + 14 + i] / ws;
+            for (int t2 = 0; t2 < N; t2++)
+              for (int j = 0; j < 3; j++)
+                K[row * n3 + t2 * 3 + j] =
+                    (i == j ? DG_MAT[t][t2] : 0.0) -
+                    (t == t2 ? dt * WGHTS[t] * JJ[t * ns + s][i][j] : 0.0);
+          }
+        if (small_solve(n3, K, b))
+          bad = 1;
+        for (int t = 0; t < N; t++)
+          for (int i = 0; i < 3; i++)
+            r[(t * ns + s) * V + 14 + i] = b[t * 3 + i];
+      }
+    }
+    if (bad)
+      return -1;
+    int conv = 1;
+    for (int k = 0; k < nn * V; k++) {
+      q[k] += r[k];
+      if (fabs(r[k]) > tol * (1 + fabs(q[k])))
+        conv = 0;
+      if (r[k] != r[k])
+        return -1;
+      dmax = fmax(dmax, fabs(r[k]));
+    }
+    (void)dmax;
+    if (conv)
+      return it + 1;
+  }
+  return -1;
+}
+
+int or_stiff_iterations_hist[64];
+
 /* predictor1 / predictor2 (dg1.cpp:75-131, dg2.cpp:102-171).  status[cell]
  * receives: Picard iteration count (>0) when the reference's Picard
  * converged; -(Newton iterations) - 1000 when Picard failed and the oracle's
@@ -2065,7 +2283,8 @@ int or_predictor(double *qh, const double *wh, double dt, const double *dX,
     if (!done && newton_fallback) {
       for (int t = 0; t < N; t++)
         memcpy(q0 + t * ns * V, w, sizeof(double) * ns * V);
-      int it = dg_newton(ndim, q0, Ww, dt, dX, P, 1e-12, 30);
+      int it = newton_fallback == 2 ? dg_newton(ndim, q0, Ww, dt, dX, P, 1e-12, 30)
+                                    : dg_stiff(ndim, q0, Ww, dt, dX, P, STIFF_TOL, STIFF_IT);
       if (it > 0) {
         memcpy(qi, q0, sizeof(double) * nn * V);
         if (status)

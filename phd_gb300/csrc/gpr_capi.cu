@@ -162,17 +162,41 @@ template <class L> struct Ops {
                        const DevPar &P, const uint8_t *mask, int32_t *status,
                        cudaStream_t st) {
     const Consts &C = consts();
-    (void)stiff;
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
     if (nd == 1) {
       long nt = ncb * NN * NN;
       k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], 1.0, P, C);
-    } else {
-      long nt = ncb * NN * NN * NN;
-      k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], 1.0 / dX[1], P, C);
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+      return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
     }
+    long nt = ncb * NN * NN * NN;
+    k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
+        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+    return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
+  }
+
+  // Stiff-source Newton pass over the cells the Picard pass flagged.
+  template <int ND>
+  static int stiff_pass(double *qh, const double *wh, long ncb, const uint8_t *mask,
+                        int32_t *status, double dt, const double *dt_dev, double idx,
+                        double idy, const DevPar &P, const Consts &C, cudaStream_t st) {
+    constexpr int NP = ND == 1 ? NN * NN : NN * NN * NN;
+    constexpr int BS = 64;
+    size_t smem = (size_t)(BS / NP) * StiffSmem<L, ND>::per_cell * sizeof(float);
+    // per device and cheap: set on every call
+    cudaFuncSetAttribute(k_predictor_stiff<L, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    int dev = 0, nsm = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_predictor_stiff<L, ND>, BS, smem);
+    long need = (ncb * NP + BS - 1) / BS;
+    long grid = (long)nsm * (per_sm > 0 ? per_sm : 1);
+    if (grid > need)
+      grid = need;
+    k_predictor_stiff<L, ND><<<(int)grid, BS, smem, st>>>(qh, wh, ncb, mask, status, dt,
+                                                           dt_dev, idx, idy, P, C);
     return cuda_rc();
   }
 

@@ -20,6 +20,7 @@ struct Consts {
   double mLinv[NN][NN], mRinv[NN][NN];  // WENO stencil inverses
   double sig[NN][NN];            // oscillation indicator
   double dgder[NN][NN];          // <psi_i, psi_j'>
+  double dgmat[NN][NN];          // DG_END - DG_DER^T
   double dgmatinv[NN][NN];       // (DG_END - DG_DER^T)^-1
   double wprod2[NN][NN];         // w_i w_j
 };
@@ -81,6 +82,9 @@ inline Consts make_consts() {
     for (int j = 0; j < NN; j++)
       dgmat[i][j] = psi(i, 1.0) * psi(j, 1.0) - c.dgder[j][i];
   inv2(dgmat, c.dgmatinv);
+  for (int i = 0; i < NN; i++)
+    for (int j = 0; j < NN; j++)
+      c.dgmat[i][j] = dgmat[i][j];
   for (int i = 0; i < NN; i++)
     for (int j = 0; j < NN; j++)
       c.wprod2[i][j] = c.w[i] * c.w[j];

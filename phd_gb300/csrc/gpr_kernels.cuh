@@ -324,7 +324,7 @@ template <class L, int ND>
 __global__ void __launch_bounds__(128) k_predictor_picard(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
-    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, Consts C) {
+    const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar P, Consts C) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
   constexpr int NP = NN * NS;                 // space-time nodes
@@ -353,21 +353,39 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   bool done = !active;
   int iters = 0;
   bool nan_seen = false;
-  for (int it = 0; it < DG_IT; it++) {
+  const int maxit = stiff ? 0 : DG_IT;
+  // Divergence detection: a cell whose largest update grows 64x above the
+  // smallest it has reached is diverging (a contracting Picard map shrinks
+  // it geometrically) and goes to the stiff-source Newton pass at once,
+  // instead of spending the remaining iterations of the cap.
+  double dmin = 1e300;
+  for (int it = 0; it < maxit; it++) {
     if (__all_sync(0xffffffffu, done))
       break;
     dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
     dg_solve_node<V, ND>(r, qn, t, i, j, C);
     bool big = false, hasnan = false;
+    double dmax = 0.0;
 #pragma unroll
     for (int k = 0; k < V; k++) {
-      if (fabs(qn[k] - q[k]) > DG_TOL * (1.0 + fabs(q[k])))
+      double dd = fabs(qn[k] - q[k]);
+      if (dd > DG_TOL * (1.0 + fabs(q[k])))
         big = true;
       if (qn[k] != qn[k])
         hasnan = true;
+      dmax = fmax(dmax, dd);
     }
+#pragma unroll
+    for (int o = 1; o < NP; o <<= 1)
+      dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     unsigned bigm = __ballot_sync(0xffffffffu, big) & gmask;
     unsigned nanm = __ballot_sync(0xffffffffu, hasnan) & gmask;
+    if (!done && bigm && it >= 3 && dmax > 64.0 * dmin) {
+      nan_seen = true;  // hand over to the Newton pass
+      done = true;
+      iters = it + 1;
+    }
+    dmin = fmin(dmin, dmax);
     if (!done) {
       iters = it + 1;
       if (bigm) {
@@ -394,16 +412,307 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
     }
   }
   if (active && (!done || nan_seen)) {
-    // Picard failed: leave the initial guess for the Newton pass
+    // Picard failed: write the initial guess and flag the cell for the
+    // stiff-source Newton pass with a NaN in its first entry
     double *out = qh + (c * NP + g) * V;
 #pragma unroll
     for (int k = 0; k < V; k++)
       out[k] = w[k];
+    if (g == 0)
+      out[0] = __longlong_as_double(0x7ff8000000000bad);
     if (status && g == 0)
       status[c] = GPR_PRED_FAILED | (iters << 8);
   }
   if (valid && !active && status && g == 0)
     status[c] = GPR_PRED_PICARD;
+}
+
+// ---------------------------------------------------------------------------
+// Stiff-source Newton pass for the cells whose Picard iteration failed (the
+// reference leaves their rows unwritten, dg1.cpp:108-127, or falls back to a
+// Jacobian-free Newton-Krylov solve on NaN, dg1.cpp:117-121).
+//
+// Iteration on the predictor fixed point Fp(q) = DG_U q - Ww - dt R(q) = 0:
+//   delta = (DG_U - dt W dS/dq)^-1 (Ww + dt R(q) - DG_U q),   q += delta,
+// with dS/dq the exact local Jacobian of the relaxation sources at each
+// space-time node (distortion 9x9, heat flux 3x3): implicit in the stiff
+// sources, explicit in the fluxes; with dS/dq = 0 it is the Picard update.
+// Per spatial node the correction couples the N = 2 time nodes through
+// DG_MAT: an 18x18 system for A and a 6x6 system for rho J, assembled in
+// shared memory by the node's two lanes and solved by one lane each
+// (partial pivoting); the other variables use DG_MAT^-1 directly.
+constexpr double STIFF_TOL = 1e-11;  // on the Newton update, relative
+constexpr int STIFF_IT = 60;
+
+template <bool TH>
+GPR_D void stiff_jacobian_rows(const double *q, const Prim<TH> &s, const DevPar &P, double a,
+                               double mdiag, float *rowsA, int ldA, float *rowsJ, int ldJ) {
+  // rowsA[i*ldA + j] (i = 0..8, j = 0..8): M[t][t] delta_ij - a JA[i][j]
+  const double *A = q + 5;
+  double H[9], dG[9];
+  double G00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  double G11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  double G22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  double G01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  double G02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  double G12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  double t3 = (G00 + G11 + G22) * (1.0 / 3.0);
+  dG[0] = G00 - t3; dG[1] = G01; dG[2] = G02;
+  dG[3] = G01; dG[4] = G11 - t3; dG[5] = G12;
+  dG[6] = G02; dG[7] = G12; dG[8] = G22 - t3;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+      H[3 * i + m] = A[3 * i] * A[3 * m] + A[3 * i + 1] * A[3 * m + 1] + A[3 * i + 2] * A[3 * m + 2];
+  double dA = det3(A);
+  int newtonian = !(P.flags & (GPR_SOLID | GPR_POWER_LAW | GPR_BINGHAM));
+  double th = theta1inv<TH>(q, s, P);
+  double id = 1.0 / dA;
+  double Ai[9];  // A^-1
+  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  Ai[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+  double fth = newtonian ? (5.0 / 3.0) * th : 0.0;
+  double ca = a * s.cs2;  // a (-JA) = ca (th v + AdG dth)
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      int rr = 3 * i + j;
+#pragma unroll
+      for (int m = 0; m < 3; m++)
+#pragma unroll
+        for (int n = 0; n < 3; n++) {
+          double v = (i == m ? dG[3 * n + j] : 0.0) + A[3 * i + n] * A[3 * m + j] +
+                     (n == j ? H[3 * i + m] : 0.0) - (2.0 / 3.0) * A[3 * i + j] * A[3 * m + n];
+          double e = ca * (th * v + s.AdG[rr] * fth * Ai[3 * n + m]);
+          rowsA[rr * ldA + 3 * m + n] = (float)((rr == 3 * m + n ? mdiag : 0.0) + e);
+        }
+    }
+  if (TH) {
+    double f = a * P.calpha2 * P.ikappa;  // -a JJ = f (T/rho I + J dT)
+#pragma unroll
+    for (int l = 0; l < 3; l++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        double dT = -P.calpha2 * s.J[k] * s.ir * P.icv;
+        rowsJ[l * ldJ + k] =
+            (float)((l == k ? mdiag : 0.0) + f * ((l == k ? s.T * s.ir : 0.0) + s.J[l] * dT));
+      }
+  }
+}
+
+// In-place Gaussian elimination with partial pivoting on the n x n system
+// M (leading dimension ld) with right-hand side b; solution left in b.  The
+// stiff pass solves its correction systems in FP32: the residual is FP64, so
+// the converged fixed point is the FP64 one and the single-precision
+// Jacobian only changes the (already linear) contraction rate slightly.
+template <int n, class R>
+GPR_D bool smem_solve(R *M, int ld, R *b) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    R best = fabs(M[c * ld + c]);
+#pragma unroll 4
+    for (int r = c + 1; r < n; r++) {
+      R v = fabs(M[r * ld + c]);
+      if (v > best) {
+        best = v;
+        p = r;
+      }
+    }
+    if (!(best > R(0)))
+      return false;
+    if (p != c) {
+#pragma unroll 4
+      for (int j = c; j < n; j++) {
+        R tmp = M[c * ld + j];
+        M[c * ld + j] = M[p * ld + j];
+        M[p * ld + j] = tmp;
+      }
+      R tmp = b[c];
+      b[c] = b[p];
+      b[p] = tmp;
+    }
+    R inv = R(1) / M[c * ld + c];
+    for (int r = c + 1; r < n; r++) {
+      R f = M[r * ld + c] * inv;
+#pragma unroll 4
+      for (int j = c + 1; j < n; j++)
+        M[r * ld + j] -= f * M[c * ld + j];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    R acc = b[r];
+#pragma unroll 4
+    for (int j = r + 1; j < n; j++)
+      acc -= M[r * ld + j] * b[j];
+    b[r] = acc / M[r * ld + r];
+  }
+  return true;
+}
+
+template <class L, int ND> struct StiffSmem {
+  static constexpr int NS = ND == 1 ? NN : NN * NN;
+  static constexpr int NA = 9 * NN, NJ = 3 * NN;
+  // odd number of floats: the solver lanes of neighbouring spatial nodes
+  // then start on different shared-memory banks
+  static constexpr int raw = NA * NA + NA + (L::THERMAL ? NJ * NJ + NJ : 0);
+  static constexpr int per_node = raw | 1;
+  static constexpr int CPB = 8;  // cells per 64-thread block (2D: 8 lanes each)
+  static constexpr int per_cell = NS * per_node;
+};
+
+template <class L, int ND>
+__global__ void __launch_bounds__(64) k_predictor_stiff(
+    double *__restrict__ qh, const double *__restrict__ wh, long ncb,
+    const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
+    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NS = ND == 1 ? NN : NN * NN;
+  constexpr int NP = NN * NS;
+  constexpr int TB = ND == 1 ? 2 : 4;  // flips t
+  constexpr int NA = 9 * NN, NJ = 3 * NN;
+  using SM = StiffSmem<L, ND>;
+  extern __shared__ float fsmem[];
+  if (dt_dev)
+    dt = *dt_dev;
+  const int g = threadIdx.x % NP;
+  const int t = g / NS, sidx = g % NS;
+  const int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
+  float *cellmem = fsmem + (threadIdx.x / NP) * SM::per_cell;
+  float *Am = cellmem + sidx * SM::per_node;  // 18 x 18
+  float *Ab = Am + NA * NA;                   // 18
+  float *Jm = Ab + NA;                        // 6 x 6
+  float *Jb = Jm + NJ * NJ;                   // 6
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned gmask = ((NP == 32) ? 0xffffffffu : ((1u << NP) - 1u)) << (lane & ~(NP - 1u));
+  const double f = C.endv[0][t] * (ND == 1 ? C.w[i] : C.w[i] * C.w[j]);
+  const double ws = ND == 1 ? C.w[i] : C.w[i] * C.w[j];
+  const double iws = 1.0 / ws;
+  const double a_t = dt * C.w[t];
+  const double M0 = C.dgmat[t][t], M1 = C.dgmat[t][1 - t];
+  const long cells_per_block = blockDim.x / NP;
+  // persistent: blocks stride over the cells; the loop bound is uniform in
+  // the block so every lane takes part in the warp-level exchanges
+  for (long base = blockIdx.x * cells_per_block; base < ncb;
+       base += (long)gridDim.x * cells_per_block) {
+    long c = base + threadIdx.x / NP;
+    bool valid = c < ncb;
+    long cc = valid ? c : 0;
+    bool active = valid && (mask == nullptr || mask[cc]);
+    double flag = active ? qh[cc * NP * V] : 0.0;  // NaN sentinel of the Picard pass
+    active = active && (flag != flag);
+    if (__all_sync(0xffffffffu, !active))
+      continue;
+    double Ww[V], q[V], r[V], other[V];
+    const double *wc = wh + (cc * NS + sidx) * V;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      double w = active ? wc[k] : 1.0;
+      Ww[k] = f * w;
+      q[k] = w;
+    }
+    bool done = !active;
+    bool ok = false;
+    int iters = 0;
+    for (int it = 0; it < STIFF_IT; it++) {
+      if (__all_sync(0xffffffffu, done))
+        break;
+      dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
+      // residual g = r - W_s sum_m DG_MAT[t][m] q(m)
+      shfl_vec<V>(q, other, TB);
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        r[k] -= ws * (M0 * q[k] + M1 * other[k]);
+      if (!done) {
+        Prim<L::THERMAL> st;
+        prim<L::THERMAL>(q, P, st);
+        stiff_jacobian_rows<L::THERMAL>(q, st, P, a_t, M0, Am + t * 9 * NA + t * 9, NA,
+                                        Jm + t * 3 * NJ + t * 3, NJ);
+#pragma unroll
+        for (int a = 0; a < 9; a++)
+#pragma unroll
+          for (int b = 0; b < 9; b++)
+            Am[(t * 9 + a) * NA + (1 - t) * 9 + b] = a == b ? (float)M1 : 0.0f;
+#pragma unroll
+        for (int a = 0; a < 9; a++)
+          Ab[t * 9 + a] = (float)(r[5 + a] * iws);
+        if (L::THERMAL) {
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+              Jm[(t * 3 + a) * NJ + (1 - t) * 3 + b] = a == b ? (float)M1 : 0.0f;
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+            Jb[t * 3 + a] = (float)(r[14 + a] * iws);
+        }
+      }
+      __syncwarp();
+      bool solved = true;
+      if (!done) {
+        if (t == 0)
+          solved = smem_solve<NA>(Am, NA, Ab);
+        else if (L::THERMAL)
+          solved = smem_solve<NJ>(Jm, NJ, Jb);
+      }
+      __syncwarp();
+      // non-stiff variables: DG_MAT^-1 g / W_s (partner time node's residual)
+      shfl_vec<V>(r, other, TB);
+      double delta[V];
+      double ia = C.dgmatinv[t][t] * iws, ib = C.dgmatinv[t][1 - t] * iws;
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        delta[k] = ia * r[k] + ib * other[k];
+#pragma unroll
+      for (int a = 0; a < 9; a++)
+        delta[5 + a] = (double)Ab[t * 9 + a];
+      if (L::THERMAL) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+          delta[14 + a] = (double)Jb[t * 3 + a];
+      }
+      __syncwarp();
+      bool big = false, bad = !solved;
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        double qn = q[k] + delta[k];
+        if (fabs(delta[k]) > STIFF_TOL * (1.0 + fabs(qn)))
+          big = true;
+        if (qn != qn)
+          bad = true;
+        if (!done)
+          q[k] = qn;
+      }
+      unsigned bigm = __ballot_sync(0xffffffffu, big) & gmask;
+      unsigned badm = __ballot_sync(0xffffffffu, bad) & gmask;
+      if (!done) {
+        iters = it + 1;
+        if (badm) {
+          done = true;
+        } else if (!bigm) {
+          done = true;
+          ok = true;
+        }
+      }
+    }
+    if (active) {
+      double *out = qh + (cc * NP + g) * V;
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        out[k] = q[k];
+      if (status && g == 0)
+        status[cc] = (ok ? GPR_PRED_NEWTON : GPR_PRED_FAILED) | (iters << 8);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -214,6 +214,47 @@ def test_periodic_1d_conservation(G):
         assert abs(got[:, k].sum() - u0[:, k].sum()) < 1e-12 * max(1.0, tot), k
 
 
+@pytest.mark.parametrize("case", ["tgv16_cfl08", "tube_stiff", "forced_stiff"])
+def test_stiff_predictor_against_oracle(G, case):
+    """Cells where the reference's Picard iteration diverges (stiff
+    relaxation at the reference driver's CFL 0.8) are finished by the
+    stiff-source Newton iteration; GPU and oracle run the same iteration to
+    1e-11 and agree with an independent dense finite-difference Newton solve
+    of the same fixed point."""
+    O = Oracle()
+    stiff = False
+    if case == "tgv16_cfl08":
+        u0, MP, tf, dX, bcs = G.problems.taylor_green(n=16, cs=10.0, mu=1e-2)
+        nX, bc, cfl = np.array([16, 16], np.int32), [1] * 4, 0.8
+    elif case == "tube_stiff":
+        u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=64, mu=1e-4, cs=5.0)
+        nX, bc, cfl = np.array([64], np.int32), [0, 0], 0.8
+    else:  # STIFF = True on a non-stiff tube: Newton from the start
+        u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=48)
+        nX, bc, cfl, stiff = np.array([48], np.int32), [0, 0], 0.8, True
+    u, _, _ = O.run(u0, MP, 1e9, dX, bc[0], cfl=0.4, max_steps=3)
+    dt = O.timestep(u, dX, cfl, 0.0, 1e9, 10, MP)
+    ub = O.boundaries(u, nX, bc)
+    wh = O.weno_launcher(ub, nX)
+    ref, st_ref = O.predictor(wh, dt, dX, nX, MP, stiff=stiff, newton_fallback=1)
+    fd, st_fd = O.predictor(wh, dt, dX, nX, MP, stiff=stiff, newton_fallback=2)
+    assert (st_ref < -1000).sum() > 0, "case must exercise the stiff path"
+    assert not ((st_ref == -1) | (st_ref == -2)).any()
+    ncb = int(np.prod(nX + 2))
+    qh = torch.full((ref.size,), np.nan, dtype=torch.float64, device=DEV)
+    status = torch.full((ncb,), -1, dtype=torch.int32, device=DEV)
+    G.api.set_grid(nX)
+    mask = torch.ones(ncb, dtype=torch.bool, device=DEV)
+    G.solvers.dg.predictor(qh, T(wh), dt, dX, stiff, False, MP, mask, status=status)
+    got, st = H(qh), H(status)
+    assert np.isfinite(got).all()
+    newton = (st & 0xff) == 1
+    assert (newton == (st_ref < -1000)).all(), "same cells take the stiff path"
+    assert ((st & 0xff) != 2).all(), "no cell may be left unconverged"
+    assert rel_err(got, ref) < 1e-10
+    assert rel_err(got, fd) < 1e-9
+
+
 def test_errors_are_raised(G):
     u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=16)
     u = T(u0).view(-1)
