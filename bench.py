@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--cfl", type=float, default=0.4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
     return ap.parse_args()
@@ -375,6 +376,12 @@ def run_gb300(args):
         peak_err = None
 
     roof = roofline(stage_ms, ncell, n, mean_iters, peak)
+    batched = None
+    if rank == 0 and not args.no_batched:
+        try:
+            batched = batched_bench(torch)
+        except Exception as ex:
+            batched = {"error": str(ex)}
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -399,6 +406,7 @@ def run_gb300(args):
             "roofline": roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ncell * V * 8,
                     "d2h_bytes_per_step": ncell * V * 8},
+            "batched": batched,
             "gpu_launches": 14 * args.steps,
             "clocks": cs.summary()}
     if peak_err:
@@ -411,6 +419,76 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def batched_bench(torch, steps=10, plain_steps=2, count=512):
+    """512 independent 1D shock tubes (cell counts ~U{128..2048}, random
+    states and materials) advanced by the batched form (one launch per stage
+    for all instances, the step captured in a CUDA graph), against looping the
+    plain path (gpr_iterate, one instance at a time) over the same instances.
+    Both count cell-updates actually performed."""
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    from phd_gb300.batch import Batch
+    lib = _lib.load()
+    insts = [(u, MP, dX, bcs) for (u, MP, tf, dX, bcs) in G.problems.batched_shock_tubes(count)]
+    B = Batch(insts, cfl=0.8, tf=0.2)
+    for _ in range(3):  # warm-up
+        B.step(1)
+    g = B.capture(1)
+    torch.cuda.synchronize()
+    u0 = int(B.updates.item())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    upd_b = int(B.updates.item()) - u0
+    st = B.status.cpu().numpy()
+    # plain path: one gpr_iterate call per instance and step
+    V = 17
+    bufs = []
+    for (u, MP, dX, bc) in insts:
+        nx = np.array([u.shape[0]], np.int32)
+        ut = torch.tensor(u.reshape(-1), dtype=torch.float64, device="cuda")
+        scr = torch.empty(lib.gpr_iterate_scratch_doubles(nx.ctypes.data_as(ctypes.c_void_p), 1, V),
+                          dtype=torch.float64, device="cuda")
+        clk = torch.tensor([0.0, 0.0, 0.2, 0.8, 0.0], dtype=torch.float64, device="cuda")
+        dxa = np.array(dX, np.float64)
+        bca = np.array([0, 0], np.int32)
+        cp = MP.to_ctypes()
+        bufs.append((nx, ut, scr, clk, dxa, bca, cp))
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def plain_step():
+        for (nx, ut, scr, clk, dxa, bca, cp) in bufs:
+            lib.gpr_iterate(ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+                            dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
+                            0, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                            ctypes.c_void_p(clk.data_ptr()), 1, ctypes.c_void_p(scr.data_ptr()),
+                            None, V, sp)
+    for _ in range(3):
+        plain_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(plain_steps):
+        plain_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1)
+    cells = int(B.nx.sum())
+    vb = upd_b / (ms_b * 1e-3) / 1e6
+    vp = cells * plain_steps / (ms_p * 1e-3) / 1e6
+    return {"workload": "%d 1D shock tubes, nx ~ U{128..2048} (%d cells), random states and "
+                        "materials (mu ~ logU[1e-4,1e-1], cs ~ U[0.5,5], gamma ~ U[1.2,1.67]), "
+                        "own CFL-0.8 clocks" % (count, cells),
+            "batched_value": vb, "plain_loop_value": vp, "unit": UNIT,
+            "speedup": vb / vp, "batched_ms_per_step": ms_b / steps,
+            "plain_loop_ms_per_step": ms_p / plain_steps,
+            "newton_cells_last_step": int(((st & 0xff) == 1).sum()),
+            "batched_steps": steps, "plain_steps": plain_steps}
 
 
 def stage_times(lib, torch, u, MP, nX, dXa, bc, cfl, V, dev, sp, stream, reps=3):

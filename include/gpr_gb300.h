@@ -209,6 +209,35 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
                                 int32_t *status, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched form: many independent 1D grids (instances) of uneven sizes, each
+ * with its own material, boundary codes and CFL clock, advanced together by
+ * one launch per stage (no counterpart in the reference, which runs one grid
+ * per `iterator` call; each instance follows solvers/iterator.cpp:204-245).
+ *
+ * Instances are packed one after another in u: instance k owns
+ * u[off_k .. off_k + nx[k]) cells, off_k = nx[0] + ... + nx[k-1].  The
+ * device clock array holds {t, dt, tf, cfl, count} per instance (count as a
+ * double); an instance whose t has reached tf gets dt = 0 and its steps
+ * change nothing, so a fixed number of steps can be enqueued or captured in
+ * a CUDA graph without host synchronisation.
+ *
+ * gpr_batch_init writes the instance tables (materials, maps, offsets) into
+ * the caller's scratch (gpr_batch_scratch_doubles doubles) and sets every
+ * clock to t = 0; it synchronises the stream once (the tables are copied from
+ * host memory).  gpr_batch_iterate then runs nsteps steps.  `status`
+ * (optional) receives the predictor status of each packed predictor cell
+ * (nx[k] + 2 per instance); `updates` (optional, device uint64) accumulates
+ * the cell-updates performed (sum of nx[k] over instances that advanced). */
+long gpr_batch_scratch_doubles(int ninst, const int32_t *nx, int nvar);
+int gpr_batch_init(double *clock, int ninst, const int32_t *nx,
+                   const double *dx, const int32_t *bcs, const gpr_par *pars,
+                   double cfl, double tf, double *scratch, int nvar,
+                   void *stream);
+int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx,
+                      int nsteps, double *scratch, int32_t *status,
+                      unsigned long long *updates, int nvar, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,
  * eig.cpp): batched over `count` states Q[count][V].                        */
 

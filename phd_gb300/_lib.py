@@ -86,6 +86,9 @@ SIGNATURES = {
     "gpr_iterate": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _I, _P]),
     "gpr_ader_stepper_1d_noalloc": (_I, [_P, _P, ctypes.c_int32, _D, _D, _I, _I, _P, _P, _P,
                                          _I, _P]),
+    "gpr_batch_scratch_doubles": (_L, [_I, _P, _I]),
+    "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
+    "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
     "gpr_flux": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),

@@ -1,0 +1,101 @@
+"""Batched form: many independent 1D GPR grids advanced together.
+
+Each instance has its own cell count, material, boundary codes and CFL
+clock (the reference runs one grid per `solvers.iterator` call,
+code/cpp/src/solvers/iterator.cpp:179-264).  All instances are packed into
+one device buffer and every stage of the step is one kernel launch for all of
+them; the step loop needs no host synchronisation and can be captured in a
+CUDA graph (`capture`).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import GprParC
+
+BC = {"transitive": 0, "transmissive": 0, "periodic": 1, "slip": 2, "stick": 3,
+      "moving": 4, "symmetric": 5}
+
+
+class Batch:
+    """instances: list of (u0 [nx, V] array, Par, dx, bcs) tuples."""
+
+    def __init__(self, instances, cfl=0.8, tf=0.2, device="cuda"):
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.V = int(instances[0][0].shape[-1])
+        self.ninst = len(instances)
+        self.nx = np.array([inst[0].shape[0] for inst in instances], dtype=np.int32)
+        self.off = np.concatenate([[0], np.cumsum(self.nx)]).astype(np.int64)
+        dx = np.array([float(inst[2][0] if np.ndim(inst[2]) else inst[2]) for inst in instances])
+        bcs = []
+        for inst in instances:
+            b = inst[3]
+            code = BC[b] if isinstance(b, str) else int(b)
+            bcs += [code, code]
+        self.dx = np.ascontiguousarray(dx)
+        self.bcs = np.ascontiguousarray(np.array(bcs, dtype=np.int32))
+        pars = (GprParC * self.ninst)()
+        for k, inst in enumerate(instances):
+            pars[k] = inst[1].to_ctypes()
+        self._pars = pars
+        u = np.concatenate([np.asarray(inst[0], dtype=np.float64).reshape(-1, self.V)
+                            for inst in instances])
+        self.u = torch.tensor(u.reshape(-1), dtype=torch.float64, device=self.device)
+        self.clock = torch.zeros(5 * self.ninst, dtype=torch.float64, device=self.device)
+        nscr = self.lib.gpr_batch_scratch_doubles(self.ninst, self._p(self.nx), self.V)
+        _lib.check(nscr, "batch_scratch_doubles")
+        self.scratch = torch.empty(nscr, dtype=torch.float64, device=self.device)
+        self.status = torch.zeros(int((self.nx + 2).sum()), dtype=torch.int32,
+                                  device=self.device)
+        self.updates = torch.zeros(1, dtype=torch.int64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gpr_batch_init(
+                self._t(self.clock), self.ninst, self._p(self.nx), self._p(self.dx),
+                self._p(self.bcs), ctypes.cast(pars, ctypes.c_void_p), float(cfl), float(tf),
+                self._t(self.scratch), self.V, self._stream()), "batch_init")
+
+    @staticmethod
+    def _p(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    @staticmethod
+    def _t(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    @staticmethod
+    def _stream():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def step(self, nsteps=1):
+        """Enqueue nsteps steps of every instance on the current stream."""
+        _lib.check(self.lib.gpr_batch_iterate(
+            self._t(self.u), self._t(self.clock), self.ninst, self._p(self.nx), int(nsteps),
+            self._t(self.scratch), self._t(self.status), self._t(self.updates), self.V,
+            self._stream()), "batch_iterate")
+
+    def capture(self, nsteps=1):
+        """A CUDA graph of nsteps steps (replay with graph.replay())."""
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.step(nsteps)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        return g
+
+    def state(self, k):
+        """Instance k's state as a [nx, V] tensor view."""
+        a, b = int(self.off[k]), int(self.off[k + 1])
+        return self.u.view(-1, self.V)[a:b]
+
+    def times(self):
+        c = self.clock.view(-1, 5).cpu().numpy()
+        return c[:, 0], c[:, 4].astype(int)
+
+    def done(self):
+        t, _ = self.times()
+        return bool(np.all(t >= self.clock.view(-1, 5)[:, 2].cpu().numpy()))

@@ -119,6 +119,49 @@ __global__ void k_extend_mask(const uint8_t *__restrict__ mask, uint8_t *__restr
   maskb[idx] = v;
 }
 
+// Packed sizes and scratch offsets (in doubles) of the batched form.
+struct BatchLayout {
+  long nu = 0, nub = 0, nb = 0, nf = 0;
+  long o_par, o_iu, o_iub, o_ib, o_if, o_nx, o_ou, o_oub, o_ob, o_of, o_bc, o_idx, o_mx;
+  long o_ub, o_wh, o_qh, o_fb, total;
+};
+
+BatchLayout batch_layout_v(int ninst, const int32_t *nx, int V) {
+  BatchLayout b;
+  for (int k = 0; k < ninst; k++) {
+    b.nu += nx[k];
+    b.nub += nx[k] + 2 * NN;
+    b.nb += nx[k] + 2;
+    b.nf += nx[k] + 1;
+  }
+  auto dbl = [](long bytes) { return (bytes + 7) / 8; };
+  long o = 0;
+  auto take = [&](long ndoubles) {
+    long at = o;
+    o += (ndoubles + 31) & ~31L;  // 256-byte aligned pieces
+    return at;
+  };
+  b.o_par = take(dbl((long)ninst * sizeof(DevPar)));
+  b.o_iu = take(dbl(b.nu * 4));
+  b.o_iub = take(dbl(b.nub * 4));
+  b.o_ib = take(dbl(b.nb * 4));
+  b.o_if = take(dbl(b.nf * 4));
+  b.o_nx = take(dbl(ninst * 4L));
+  b.o_ou = take(dbl(ninst * 4L));
+  b.o_oub = take(dbl(ninst * 4L));
+  b.o_ob = take(dbl(ninst * 4L));
+  b.o_of = take(dbl(ninst * 4L));
+  b.o_bc = take(dbl(ninst * 8L));
+  b.o_idx = take(ninst);
+  b.o_mx = take(ninst);
+  b.o_ub = take(b.nub * V);
+  b.o_wh = take(b.nb * NN * V);
+  b.o_qh = take(b.nb * NN * NN * V);
+  b.o_fb = take(b.nf * 2 * V);
+  b.total = o;
+  return b;
+}
+
 template <class L> struct Ops {
   static constexpr int V = L::V;
 
@@ -167,36 +210,38 @@ template <class L> struct Ops {
     if (nd == 1) {
       long nt = ncb * NN * NN;
       k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
       return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
     }
     long nt = ncb * NN * NN * NN;
     k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
-        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
     return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
   }
 
   // Stiff-source Newton pass over the cells the Picard pass flagged.
-  template <int ND>
+  template <int ND, bool BATCH = false>
   static int stiff_pass(double *qh, const double *wh, long ncb, const uint8_t *mask,
                         int32_t *status, double dt, const double *dt_dev, double idx,
-                        double idy, const DevPar &P, const Consts &C, cudaStream_t st) {
+                        double idy, const DevPar &P, const Consts &C, cudaStream_t st,
+                        const Batch &B = Batch{}) {
     constexpr int NP = ND == 1 ? NN * NN : NN * NN * NN;
     constexpr int BS = 64;
     size_t smem = (size_t)(BS / NP) * StiffSmem<L, ND>::per_cell * sizeof(float);
     // per device and cheap: set on every call
-    cudaFuncSetAttribute(k_predictor_stiff<L, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+    cudaFuncSetAttribute(k_predictor_stiff<L, ND, BATCH>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0, nsm = 152, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_predictor_stiff<L, ND>, BS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_predictor_stiff<L, ND, BATCH>, BS,
+                                                  smem);
     long need = (ncb * NP + BS - 1) / BS;
     long grid = (long)nsm * (per_sm > 0 ? per_sm : 1);
     if (grid > need)
       grid = need;
-    k_predictor_stiff<L, ND><<<(int)grid, BS, smem, st>>>(qh, wh, ncb, mask, status, dt,
-                                                           dt_dev, idx, idy, P, C);
+    k_predictor_stiff<L, ND, BATCH><<<(int)grid, BS, smem, st>>>(qh, wh, ncb, mask, status, dt,
+                                                                  dt_dev, idx, idy, P, C, B);
     return cuda_rc();
   }
 
@@ -213,12 +258,12 @@ template <class L> struct Ops {
     int nx = nX[0];
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
-      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, nx, mask, dt, dt_dev, dX[0],
-                                                     time_dg, P, C);
+      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
+                                                     dt_dev, dX[0], time_dg, P, C, Batch{});
       long nc = (long)nx * NN * NN;
       k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
                                                       dt_dev, dX[0], 1.0, sources, time_dg, P,
-                                                      C);
+                                                      C, Batch{});
       return cuda_rc();
     }
     int ny = nX[1];
@@ -232,7 +277,8 @@ template <class L> struct Ops {
                                                              C);
     long nc = (long)nx * ny * NN * NN * NN;
     k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
-                                                    dX[0], dX[1], sources, time_dg, P, C);
+                                                    dX[0], dX[1], sources, time_dg, P, C,
+                                                    Batch{});
     return cuda_rc();
   }
 
@@ -245,8 +291,8 @@ template <class L> struct Ops {
     int nx = nX[0];
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
-      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, nx, mask, dt, nullptr, dX[0],
-                                                     time_dg, P, C);
+      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
+                                                     dX[0], time_dg, P, C, Batch{});
       return cuda_rc();
     }
     int ny = nX[1];
@@ -330,6 +376,60 @@ template <class L> struct Ops {
     long ns = nd == 1 ? NN : NN * NN;
     long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
     return nub * V + ncb * ns * V + ncb * NN * ns * V + (w > f ? w : f) + 1;
+  }
+
+  // ---- batched form -------------------------------------------------------
+  static BatchLayout batch_layout(int ninst, const int32_t *nx) {
+    return batch_layout_v(ninst, nx, V);
+  }
+
+  static Batch batch_view(double *scr, int ninst, const BatchLayout &b, double *clk) {
+    Batch B;
+    B.P = (const DevPar *)(scr + b.o_par);
+    B.inst_u = (const int32_t *)(scr + b.o_iu);
+    B.inst_ub = (const int32_t *)(scr + b.o_iub);
+    B.inst_b = (const int32_t *)(scr + b.o_ib);
+    B.inst_f = (const int32_t *)(scr + b.o_if);
+    B.nx = (const int32_t *)(scr + b.o_nx);
+    B.off_u = (const int32_t *)(scr + b.o_ou);
+    B.off_ub = (const int32_t *)(scr + b.o_oub);
+    B.off_b = (const int32_t *)(scr + b.o_ob);
+    B.off_f = (const int32_t *)(scr + b.o_of);
+    B.bc = (const int32_t *)(scr + b.o_bc);
+    B.idx = scr + b.o_idx;
+    B.clk = clk;
+    B.ninst = ninst;
+    return B;
+  }
+
+  static int batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,
+                           double *scr, int32_t *status, unsigned long long *updates,
+                           cudaStream_t st) {
+    const Consts &C = consts();
+    BatchLayout b = batch_layout(ninst, nx);
+    Batch B = batch_view(scr, ninst, b, clk);
+    double *ub = scr + b.o_ub, *wh = scr + b.o_wh, *qh = scr + b.o_qh, *fb = scr + b.o_fb;
+    unsigned long long *mx = (unsigned long long *)(scr + b.o_mx);
+    DevPar P0{};
+    for (int s = 0; s < nsteps; s++) {
+      k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B);
+      k_b_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B);
+      k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
+      k_b_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wh, ub, b.nb, C, B);
+      k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, 128), 128, 0, st>>>(
+          qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B);
+      int rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
+                                   C, st, B);
+      if (rc)
+        return rc;
+      k_faces1d<L, true><<<blocks(b.nf * NN, 128), 128, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
+                                                                  nullptr, 1.0, 1, P0, C, B);
+      k_cells<L, 1, true><<<blocks(b.nu * NN * NN, 128), 128, 0, st>>>(
+          u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B);
+      k_b_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, B);
+      k_b_clock_advance<<<blocks(ninst, 128), 128, 0, st>>>(B, updates);
+    }
+    return cuda_rc();
   }
 
   static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {
@@ -695,3 +795,126 @@ extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t 
     return GPR_E_UNSUPPORTED;
   }
 }
+
+// ---------------------------------------------------------------------------
+// Batched form (many independent 1D instances in one launch per stage).
+#include <vector>
+
+extern "C" {
+
+long gpr_batch_scratch_doubles(int ninst, const int32_t *nx, int nvar) {
+  if (ninst < 1 || !nx)
+    return GPR_E_ARG;
+  for (int k = 0; k < ninst; k++)
+    if (nx[k] < 2)
+      return GPR_E_ARG;
+  DISPATCH(nvar, O::batch_layout(ninst, nx).total)
+}
+
+int gpr_batch_init(double *clock, int ninst, const int32_t *nx, const double *dx,
+                   const int32_t *bcs, const gpr_par *pars, double cfl, double tf,
+                   double *scratch, int nvar, void *stream) {
+  if (!clock || ninst < 1 || !nx || !dx || !bcs || !pars || !scratch)
+    return GPR_E_ARG;
+  for (int k = 0; k < ninst; k++)
+    if (nx[k] < 2 || !(dx[k] > 0) || bcs[2 * k] < 0 || bcs[2 * k] > 5 || bcs[2 * k + 1] < 0 ||
+        bcs[2 * k + 1] > 5)
+      return GPR_E_ARG;
+  long total = gpr_batch_scratch_doubles(ninst, nx, nvar);
+  if (total < 0)
+    return (int)total;
+  // host images of the tables
+  std::vector<DevPar> P(ninst);
+  std::vector<int32_t> ou(ninst), oub(ninst), ob(ninst), of(ninst), bc(2 * ninst);
+  std::vector<double> idx(ninst), clk(5 * (size_t)ninst);
+  long nu = 0, nub = 0, nb = 0, nf = 0;
+  for (int k = 0; k < ninst; k++) {
+    P[k] = make_devpar(pars[k]);
+    ou[k] = (int32_t)nu;
+    oub[k] = (int32_t)nub;
+    ob[k] = (int32_t)nb;
+    of[k] = (int32_t)nf;
+    nu += nx[k];
+    nub += nx[k] + 2 * NN;
+    nb += nx[k] + 2;
+    nf += nx[k] + 1;
+    bc[2 * k] = bcs[2 * k];
+    bc[2 * k + 1] = bcs[2 * k + 1];
+    idx[k] = 1.0 / dx[k];
+    double *c = clk.data() + 5 * k;
+    c[0] = 0.0;
+    c[1] = 0.0;
+    c[2] = tf;
+    c[3] = cfl;
+    c[4] = 0.0;
+  }
+  if (nu >= 0x7fffffff / 4)
+    return GPR_E_TOO_LARGE;
+  std::vector<int32_t> iu(nu), iub(nub), ib(nb), iff(nf);
+  for (int k = 0; k < ninst; k++) {
+    for (int c = 0; c < nx[k]; c++)
+      iu[ou[k] + c] = k;
+    for (int c = 0; c < nx[k] + 2 * NN; c++)
+      iub[oub[k] + c] = k;
+    for (int c = 0; c < nx[k] + 2; c++)
+      ib[ob[k] + c] = k;
+    for (int c = 0; c < nx[k] + 1; c++)
+      iff[of[k] + c] = k;
+  }
+  cudaStream_t st = S(stream);
+  auto put = [&](long off, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(scratch + off, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  cudaError_t e = cudaSuccess;
+#define PUT(off, vec) \
+  if (e == cudaSuccess) e = put(off, vec.data(), vec.size() * sizeof(vec[0]))
+  switch (nvar) {
+  case 17:
+  case 14: {
+    BatchLayout lay = batch_layout_v(ninst, nx, nvar);
+    PUT(lay.o_par, P);
+    PUT(lay.o_iu, iu);
+    PUT(lay.o_iub, iub);
+    PUT(lay.o_ib, ib);
+    PUT(lay.o_if, iff);
+    std::vector<int32_t> nxv(nx, nx + ninst);
+    PUT(lay.o_nx, nxv);
+    PUT(lay.o_ou, ou);
+    PUT(lay.o_oub, oub);
+    PUT(lay.o_ob, ob);
+    PUT(lay.o_of, of);
+    PUT(lay.o_bc, bc);
+    PUT(lay.o_idx, idx);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(scratch + lay.o_mx, 0, sizeof(unsigned long long) * ninst, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(clock, clk.data(), clk.size() * sizeof(double),
+                          cudaMemcpyHostToDevice, st);
+    // the host images above must outlive the copies
+    if (e == cudaSuccess)
+      e = cudaStreamSynchronize(st);
+  } break;
+  default:
+    return GPR_E_UNSUPPORTED;
+  }
+#undef PUT
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpr_gb300: batch init: %s\n", cudaGetErrorString(e));
+    return GPR_E_CUDA;
+  }
+  return GPR_OK;
+}
+
+int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx, int nsteps,
+                      double *scratch, int32_t *status, unsigned long long *updates, int nvar,
+                      void *stream) {
+  if (!u || !clock || ninst < 1 || !nx || nsteps < 0 || !scratch)
+    return GPR_E_ARG;
+  for (int k = 0; k < ninst; k++)
+    if (nx[k] < 2)
+      return GPR_E_ARG;
+  DISPATCH(nvar, O::batch_iterate(u, clock, ninst, nx, nsteps, scratch, status, updates,
+                                  S(stream)))
+}
+
+}  // extern "C"

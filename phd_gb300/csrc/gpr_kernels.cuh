@@ -19,6 +19,26 @@ template <bool TH, int LS> struct Layout {
 };
 
 // ---------------------------------------------------------------------------
+// Batched form: many independent 1D grids (instances) of uneven sizes, each
+// with its own material and its own clock, packed one after another.  For
+// instance k with nx_k interior cells the packed index spaces are
+//   u  cells   off_u[k]  .. off_u[k]  + nx_k      (off_u[k+1] = off_u[k] + nx_k)
+//   ub cells   off_ub[k] .. off_ub[k] + nx_k + 2N (= off_u[k] + 2N k)
+//   predictor  off_b[k]  .. off_b[k]  + nx_k + 2  (= off_u[k] + 2 k)
+//   faces      off_f[k]  .. off_f[k]  + nx_k + 1  (= off_u[k] + k)
+// and inst_* map every packed index to its instance.  clk[k] holds
+// {t, dt, tf, cfl, count}; a finished instance has dt = 0 and its steps
+// change nothing.
+struct Batch {
+  const DevPar *P;
+  const int32_t *inst_u, *inst_ub, *inst_b, *inst_f;
+  const int32_t *nx, *off_u, *off_ub, *off_b, *off_f, *bc;
+  const double *idx;  // 1 / dx per instance
+  double *clk;        // [ninst][5]
+  int ninst;
+};
+
+// ---------------------------------------------------------------------------
 // Boundary ghost cells (etc/grid.cpp:12-170).  One thread per (ghost row, k)
 // of one axis; 2D runs the x pass over interior rows, then the y pass over
 // all rows (corners are filled from x ghosts as in the reference).
@@ -320,11 +340,12 @@ GPR_D void dg_solve_node(const double *r, double *qn, int t, int i, int j, const
 // status[c] (optional): GPR_PRED_PICARD | iterations << 8 when converged,
 // GPR_PRED_FAILED when Picard did not converge (row left for the Newton pass,
 // with the last Picard iterate written so the row is always defined).
-template <class L, int ND>
+template <class L, int ND, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_predictor_picard(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
-    const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar P, Consts C) {
+    const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar Pv, Consts C,
+    Batch B) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
   constexpr int NP = NN * NS;                 // space-time nodes
@@ -334,6 +355,12 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   int g = threadIdx.x % NP;
   long c = gt / NP;
   bool valid = c < ncb;
+  const int inst = BATCH ? B.inst_b[valid ? c : 0] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    dt = B.clk[5 * inst + 1];
+    idx = B.idx[inst];
+  }
   bool active = valid && (mask == nullptr || mask[c]);
   int t = g / NS, sidx = g % NS;
   int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
@@ -354,10 +381,12 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   int iters = 0;
   bool nan_seen = false;
   const int maxit = stiff ? 0 : DG_IT;
-  // Divergence detection: a cell whose largest update grows 64x above the
-  // smallest it has reached is diverging (a contracting Picard map shrinks
-  // it geometrically) and goes to the stiff-source Newton pass at once,
-  // instead of spending the remaining iterations of the cap.
+  // Divergence detection: a cell whose largest update has grown 1e8 times
+  // above the smallest it reached is diverging and goes to the stiff-source
+  // Newton pass at once instead of spending the rest of the iteration cap.
+  // Slowly or non-monotonically converging cells (the reference converges
+  // some only after ~40 iterations) never grow that much, so every cell the
+  // reference's Picard iteration converges still converges by Picard.
   double dmin = 1e300;
   for (int it = 0; it < maxit; it++) {
     if (__all_sync(0xffffffffu, done))
@@ -380,7 +409,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
       dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     unsigned bigm = __ballot_sync(0xffffffffu, big) & gmask;
     unsigned nanm = __ballot_sync(0xffffffffu, hasnan) & gmask;
-    if (!done && bigm && it >= 3 && dmax > 64.0 * dmin) {
+    if (!done && bigm && it >= 3 && dmax > 1e8 * dmin) {
       nan_seen = true;  // hand over to the Newton pass
       done = true;
       iters = it + 1;
@@ -570,11 +599,12 @@ template <class L, int ND> struct StiffSmem {
   static constexpr int per_cell = NS * per_node;
 };
 
-template <class L, int ND>
+template <class L, int ND, bool BATCH = false>
 __global__ void __launch_bounds__(64) k_predictor_stiff(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
-    const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
-    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, Consts C) {
+    const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt_in,
+    const double *__restrict__ dt_dev, double idx_in, double idy, DevPar Pv, Consts C,
+    Batch B) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;
   constexpr int NP = NN * NS;
@@ -583,7 +613,7 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
   using SM = StiffSmem<L, ND>;
   extern __shared__ float fsmem[];
   if (dt_dev)
-    dt = *dt_dev;
+    dt_in = *dt_dev;
   const int g = threadIdx.x % NP;
   const int t = g / NS, sidx = g % NS;
   const int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
@@ -597,7 +627,6 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
   const double f = C.endv[0][t] * (ND == 1 ? C.w[i] : C.w[i] * C.w[j]);
   const double ws = ND == 1 ? C.w[i] : C.w[i] * C.w[j];
   const double iws = 1.0 / ws;
-  const double a_t = dt * C.w[t];
   const double M0 = C.dgmat[t][t], M1 = C.dgmat[t][1 - t];
   const long cells_per_block = blockDim.x / NP;
   // persistent: blocks stride over the cells; the loop bound is uniform in
@@ -612,6 +641,11 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
     active = active && (flag != flag);
     if (__all_sync(0xffffffffu, !active))
       continue;
+    const int inst = BATCH ? B.inst_b[cc] : 0;
+    const DevPar &P = BATCH ? B.P[inst] : Pv;
+    const double dt = BATCH ? B.clk[5 * inst + 1] : dt_in;
+    const double idx = BATCH ? B.idx[inst] : idx_in;
+    const double a_t = dt * C.w[t];
     double Ww[V], q[V], r[V], other[V];
     const double *wc = wh + (cc * NS + sidx) * V;
 #pragma unroll
@@ -763,11 +797,11 @@ GPR_D void interface_point(const double *ql, const double *qr, int d, const DevP
 
 // 1D faces i = 0..nx between predictor cells i and i+1.  NQ = N lanes per
 // face (time nodes).
-template <class L>
+template <class L, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_faces1d(
-    double *__restrict__ fb, const double *__restrict__ qh, int nx,
+    double *__restrict__ fb, const double *__restrict__ qh, long nface,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    int time_dg, DevPar P, Consts C) {
+    int time_dg, DevPar Pv, Consts C, Batch B) {
   constexpr int V = L::V;
   constexpr int NQ = NN;
   if (dt_dev)
@@ -775,8 +809,17 @@ __global__ void __launch_bounds__(128) k_faces1d(
   long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   int t = threadIdx.x % NQ;
   long face = gt / NQ;
-  bool valid = face <= nx;
-  long fi = valid ? face : 0;
+  bool valid = face < nface;
+  long fo = valid ? face : 0;
+  // predictor cell on the left of the face (packed index in the batched form)
+  long fi = fo;
+  const int inst = BATCH ? B.inst_f[fo] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    fi = B.off_b[inst] + (fo - B.off_f[inst]);
+    dt = B.clk[5 * inst + 1];
+    dx = 1.0 / B.idx[inst];
+  }
   bool active = valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
   int nt = time_dg ? NN : 1;
   double ql[V], qr[V], f[V], b[V];
@@ -795,7 +838,7 @@ __global__ void __launch_bounds__(128) k_faces1d(
     for (int k = 0; k < V; k++)
       f[k] = b[k] = 0.0;
   }
-  double *out = fb + fi * 2 * V;
+  double *out = fb + fo * 2 * V;
 #pragma unroll
   for (int k = 0; k < V; k++) {
     double lft = active ? kk * (b[k] + f[k]) : 0.0;
@@ -875,12 +918,12 @@ __global__ void __launch_bounds__(128) k_faces2d(
 // Cell pass: one thread per (cell, space-time node): the volume term
 // w_t w_s (S - B dq/dx [- B dq/dy]) (fv.cpp:11-109), reduced over the cell's
 // NP lanes, then u += volume - face contributions.
-template <class L, int ND>
+template <class L, int ND, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_cells(
     double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
-    const double *__restrict__ fby, int nx, int ny, const uint8_t *__restrict__ mask,
+    const double *__restrict__ fby, long nx, int ny, const uint8_t *__restrict__ mask,
     double dt, const double *__restrict__ dt_dev, double dx, double dy, int sources,
-    int time_dg, DevPar P, Consts C) {
+    int time_dg, DevPar Pv, Consts C, Batch B) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;
   constexpr int NP = NN * NS;
@@ -888,15 +931,27 @@ __global__ void __launch_bounds__(128) k_cells(
   constexpr int YB = 1;
   if (dt_dev)
     dt = *dt_dev;
-  const double idx = 1.0 / dx, idy = 1.0 / dy;
   long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   int g = threadIdx.x % NP;
   long c = gt / NP;  // interior cell (u index)
   long ncell = ND == 1 ? nx : (long)nx * ny;
   bool valid = c < ncell;
   long cc = valid ? c : 0;
-  int ci = ND == 1 ? (int)cc : (int)(cc / ny), cj = ND == 1 ? 0 : (int)(cc % ny);
+  const int inst = BATCH ? B.inst_u[cc] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  double idx = 1.0 / dx;
+  const double idy = 1.0 / dy;
+  long ci = ND == 1 ? cc : (cc / ny);
+  int cj = ND == 1 ? 0 : (int)(cc % ny);
   long cb = ND == 1 ? ci + 1 : (long)(ci + 1) * (ny + 2) + (cj + 1);
+  long fo = ci;  // face on the left of the cell (1D)
+  if (BATCH) {
+    long li = cc - B.off_u[inst];
+    cb = B.off_b[inst] + li + 1;
+    fo = B.off_f[inst] + li;
+    dt = B.clk[5 * inst + 1];
+    idx = B.idx[inst];
+  }
   bool active = valid && (mask == nullptr || mask[cb]);
   int t = g / NS, sidx = g % NS;
   int i = ND == 1 ? sidx : sidx / NN, j = ND == 1 ? 0 : sidx % NN;
@@ -956,10 +1011,10 @@ __global__ void __launch_bounds__(128) k_cells(
   double *uc = u + cc * V;
   if (ND == 1) {
     // face ci: R part, face ci+1: L part (fv.cpp:143-146)
-    const double *fl = fbx + (long)ci * 2 * V;
-    const double *fr = fbx + (long)(ci + 1) * 2 * V;
-    bool okl = mask == nullptr || (mask[ci] && mask[ci + 1]);
-    bool okr = mask == nullptr || (mask[ci + 1] && mask[ci + 2]);
+    const double *fl = fbx + fo * 2 * V;
+    const double *fr = fbx + (fo + 1) * 2 * V;
+    bool okl = mask == nullptr || (mask[cb - 1] && mask[cb]);
+    bool okr = mask == nullptr || (mask[cb] && mask[cb + 1]);
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double x = uc[k] + acc[k];
@@ -1086,6 +1141,129 @@ __global__ void k_renorm(double *__restrict__ u, long ncell, double rho0,
 #pragma unroll
     for (int k = 0; k < 9; k++)
       q[5 + k] = A[k] * f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched helper kernels (1D).
+
+// ub of every instance: interior copy and ghost cells (grid.cpp:12-125,
+// 147-160), one thread per (packed ub cell, variable).
+template <int V>
+__global__ void k_b_boundaries(const double *__restrict__ u, double *__restrict__ ub,
+                               long nub, Batch B) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= nub * V)
+    return;
+  int k = idx % V;
+  long cb = idx / V;
+  int inst = B.inst_ub[cb];
+  int nx = B.nx[inst];
+  long li = cb - B.off_ub[inst];
+  const double *ui = u + (long)B.off_u[inst] * V;
+  if (li >= NN && li < nx + NN) {
+    ub[cb * V + k] = ui[(li - NN) * V + k];
+    return;
+  }
+  int side = li >= nx + NN;
+  int gi = side ? (int)(li - nx - NN) : (int)li;
+  int code = B.bc[2 * inst + side];
+  int si = bc_src_index(code, side, gi, nx);
+  if (code == GPR_BC_PERIODIC)
+    code = GPR_BC_TRANSMISSIVE;
+  ub[cb * V + k] = bc_value<V>(code, 0, k, ui + (long)si * V);
+}
+
+// WENO per (packed predictor cell, variable)
+template <int V>
+__global__ void k_b_weno(double *__restrict__ wh, const double *__restrict__ ub, long ncb,
+                         Consts C, Batch B) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= ncb * V)
+    return;
+  int k = idx % V;
+  long c = idx / V;
+  int inst = B.inst_b[c];
+  long li = c - B.off_b[inst];
+  const double *d0 = ub + ((long)B.off_ub[inst] + li) * V + k;
+  weno_point(d0, V, wh + c * NN * V + k, V, (int)li, B.nx[inst] + 2, 0, C);
+}
+
+// per-instance CFL maximum: atomicMax of the bit pattern per instance
+template <class L>
+__global__ void __launch_bounds__(256) k_b_cfl_max(const double *__restrict__ u, long ncell,
+                                                   unsigned long long *__restrict__ mx,
+                                                   Batch B) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  int inst = B.inst_u[c];
+  const DevPar &P = B.P[inst];
+  double q[V];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = u[c * V + k];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  double m = max_abs_eigs<L::THERMAL>(q, s, 0, P) * B.idx[inst];
+  if (m > 0.0)  // NaN and zero are skipped
+    atomicMax(mx + inst, (unsigned long long)__double_as_longlong(m));
+}
+
+// per-instance dt (iterator.cpp:148-177 per instance) and the step counter
+__global__ void k_b_clock_finalize(unsigned long long *__restrict__ mx, Batch B) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= B.ninst)
+    return;
+  double *c = B.clk + 5 * k;
+  double t = c[0], tf = c[2], cfl = c[3];
+  long count = (long)c[4];
+  double dt = 0.0;
+  if (t < tf) {
+    double MAX = __longlong_as_double((long long)mx[k]);
+    dt = cfl / MAX;
+    if (count <= 5)
+      dt *= 0.2;
+    if (t + dt > tf)
+      dt = tf - t;
+  }
+  c[1] = dt;
+  mx[k] = 0ull;  // ready for the next step's maximum
+}
+
+template <int V>
+__global__ void k_b_renorm(double *__restrict__ u, long ncell, Batch B) {
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  int inst = B.inst_u[c];
+  if (B.clk[5 * inst + 1] == 0.0)
+    return;
+  double *q = u + c * V;
+  double r = q[0];
+  if (r > 0) {
+    double A[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      A[k] = q[5 + k];
+    double f = cbrt(r / (B.P[inst].rho0 * det3(A)));
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      q[5 + k] = A[k] * f;
+  }
+}
+
+__global__ void k_b_clock_advance(Batch B, unsigned long long *__restrict__ updates) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= B.ninst)
+    return;
+  double *c = B.clk + 5 * k;
+  if (c[1] > 0.0) {
+    c[0] += c[1];
+    c[4] += 1.0;
+    if (updates)
+      atomicAdd(updates, (unsigned long long)B.nx[k]);
   }
 }
 
