@@ -238,6 +238,48 @@ int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx,
                       unsigned long long *updates, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint of the batched 1D step (no counterpart in the reference, which
+ * has no derivatives): reverse-mode cotangents of a misfit with respect to
+ * the initial states and six material fields of every instance.
+ *
+ * Differentiable model: stiffened-gas EOS, Newtonian viscosity (flags 0),
+ * beta = 0, Tref = 0, Rusanov flux, boundary codes other than "moving".
+ * The six fields are the DevPar members {gamma, 1/Gamma, b02, rho0 /
+ * (2 mu^(1/n)), calpha2, 1/kappa}; the caller maps them to its parameters.
+ *
+ * gpr_adj_forward_step runs one step of the batched form (gpr_batch_init
+ * tables in `scratch`) with the predictor tolerances dg_tol / dg_it (tight,
+ * e.g. 1e-13, so the predictor is its fixed point); with a non-NULL `tape`
+ * (gpr_adj_tape_doubles doubles) it records what the backward step needs.
+ * dt_mode 0 takes the CFL step and writes it to dt_io[ninst] if given;
+ * dt_mode 1 takes dt_io as the step (a schedule held fixed).
+ *
+ * gpr_adj_backward_step maps the cotangent ubar of the state after a
+ * recorded step to the cotangent before it (in place), adds the step's
+ * material-field cotangents to thbar[ninst][6], and carries tbar[ninst] (the
+ * cotangent of the clock t; start it at 0).  frozen_dt = 1 treats each dt as
+ * a constant (the adjoint of the fixed-schedule forward); frozen_dt = 0
+ * differentiates dt through the CFL rule (at ties of the CFL maximum the
+ * smallest cell index is taken).  ascratch: gpr_adj_scratch_doubles
+ * doubles.  info[nb] (int32 per packed predictor cell, zero it first) gets
+ * bit 0 set where the transposed predictor iteration did not converge. */
+int gpr_adj_num_fields(void);
+int gpr_adj_supported(int ninst, const gpr_par *pars, const int32_t *bcs, int nvar);
+long gpr_adj_tape_doubles(int ninst, const int32_t *nx, int nvar);
+long gpr_adj_scratch_doubles(int ninst, const int32_t *nx, int nvar);
+int gpr_adj_forward_step(double *u, double *clock, int ninst, const int32_t *nx,
+                         double *scratch, double *tape, double *dt_io, int dt_mode,
+                         double dg_tol, int dg_it, int32_t *status, int nvar, void *stream);
+int gpr_adj_backward_step(double *ubar, double *thbar, double *tbar, int frozen_dt, int ninst,
+                          const int32_t *nx, const double *scratch, const double *tape,
+                          double *ascratch, int32_t *info, int nvar, void *stream);
+/* Jacobians of F_x, S and lambda_x at count states (test hook):
+ * JF, JS [count][K][V] (column k = d/d(state k) for k < V, d/d(field k-V)
+ * after), dlam [count][K]; K = V + 6. */
+int gpr_adj_point_jacobians(const double *Q, int64_t count, const gpr_par *par, double *JF,
+                            double *JS, double *dlam, int nvar, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,
  * eig.cpp): batched over `count` states Q[count][V].                        */
 

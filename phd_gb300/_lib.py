@@ -13,8 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgpr_gb300.so")
-SOURCES = ["gpr_capi.cu"]
-HEADERS = ["gpr_device.cuh", "gpr_kernels.cuh", "gpr_consts.cuh", "gpr_ode.cuh"]
+SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu"]
+HEADERS = ["gpr_device.cuh", "gpr_kernels.cuh", "gpr_consts.cuh", "gpr_ode.cuh", "gpr_host.cuh",
+           "gpr_adjoint.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 _lock = threading.Lock()
@@ -89,6 +90,13 @@ SIGNATURES = {
     "gpr_batch_scratch_doubles": (_L, [_I, _P, _I]),
     "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
     "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
+    "gpr_adj_num_fields": (_I, []),
+    "gpr_adj_supported": (_I, [_I, _P, _P, _I]),
+    "gpr_adj_tape_doubles": (_L, [_I, _P, _I]),
+    "gpr_adj_scratch_doubles": (_L, [_I, _P, _I]),
+    "gpr_adj_forward_step": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _D, _I, _P, _I, _P]),
+    "gpr_adj_backward_step": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P]),
+    "gpr_adj_point_jacobians": (_I, [_P, _I64, _P, _P, _P, _P, _I, _P]),
     "gpr_flux": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),

@@ -1,0 +1,1364 @@
+// gpr_adjoint.cuh - hand-written adjoint (reverse mode) of the 1D ADER-WENO
+// step of gpr_kernels.cuh, for the batched packing of many instances.
+//
+// Forward step n (per instance, solvers/iterator.cpp:204-245 with
+// solvers/steppers.cpp:10-48):
+//   dt   = CFL dx / max_c lambda(u_c)        (x 0.2 for the first steps,
+//                                             clipped to tf - t)
+//   ub   = boundaries(u)                     (etc/grid.cpp:12-125)
+//   wh   = WENO(ub)                          (weno/weno.cpp:4-157)
+//   qh   = fixed point of q = DG_U^-1 (W w + dt R(q))   (dg/dg1.cpp:8-131)
+//   u'   = u + FV(qh, dt)                    (fv/fv.cpp:11-160)
+//   u+   = renorm(u')                        (solvers/utils.cpp:6-23)
+// Backward step n: given the cotangent of u+, produce the cotangent of u, add
+// the material-parameter cotangents, and carry the cotangent of the clock t
+// (the last step's dt = tf - t depends on every earlier dt).
+//
+// The predictor is differentiated at its converged fixed point by one
+// transposed linear solve per cell, (DG_U - dt dR/dq)^T mu = qbar, iterated
+// as the transposed Picard map mu <- DG_U^-T (qbar + dt dR/dq^T mu), which
+// contracts exactly when the forward Picard iteration does.  The WENO
+// weights, the Rusanov flux with its max-wave-speed switch, the path integral
+// of B, the renormalisation and the CFL time step are differentiated exactly.
+//
+// Per-node Jacobians of F, S and lambda with respect to the state and six
+// material fields come from forward-mode dual numbers: one thread per
+// (evaluation point, tangent), over a restatement of the device physics for
+// the differentiable model (stiffened-gas EOS, Newtonian viscosity, beta = 0,
+// Tref = 0, direction x).  The eigenvalue derivative of the acoustic tensor
+// uses d lambda = tr(adj(lambda I - X) dX) / tr(adj(lambda I - X)) for the
+// simple dominant eigenvalue.
+#pragma once
+
+#include "gpr_kernels.cuh"
+
+namespace gpr {
+
+// Differentiable material fields (DevPar members).  The host maps user
+// parameters (mu, cs, calpha, gamma, ...) onto them by the chain rule.
+constexpr int NPD = 6;
+enum { PD_GAMMA = 0, PD_IG = 1, PD_B02 = 2, PD_TH1C = 3, PD_CALPHA2 = 4, PD_IKAPPA = 5 };
+
+// ---------------------------------------------------------------------------
+// Dual numbers with one tangent.
+struct Dual {
+  double v, d;
+};
+GPR_D Dual operator+(Dual a, Dual b) { return Dual{a.v + b.v, a.d + b.d}; }
+GPR_D Dual operator-(Dual a, Dual b) { return Dual{a.v - b.v, a.d - b.d}; }
+GPR_D Dual operator-(Dual a) { return Dual{-a.v, -a.d}; }
+GPR_D Dual operator*(Dual a, Dual b) { return Dual{a.v * b.v, a.d * b.v + a.v * b.d}; }
+GPR_D Dual operator+(Dual a, double b) { return Dual{a.v + b, a.d}; }
+GPR_D Dual operator+(double b, Dual a) { return Dual{a.v + b, a.d}; }
+GPR_D Dual operator-(Dual a, double b) { return Dual{a.v - b, a.d}; }
+GPR_D Dual operator-(double b, Dual a) { return Dual{b - a.v, -a.d}; }
+GPR_D Dual operator*(Dual a, double b) { return Dual{a.v * b, a.d * b}; }
+GPR_D Dual operator*(double b, Dual a) { return Dual{a.v * b, a.d * b}; }
+GPR_D Dual operator/(Dual a, Dual b) {
+  double iv = 1.0 / b.v, r = a.v * iv;
+  return Dual{r, (a.d - r * b.d) * iv};
+}
+GPR_D Dual operator/(double a, Dual b) {
+  double iv = 1.0 / b.v, r = a * iv;
+  return Dual{r, -r * b.d * iv};
+}
+GPR_D Dual dsqrt(Dual a) {
+  double s = sqrt(a.v);
+  return Dual{s, 0.5 * a.d / s};
+}
+GPR_D Dual dcbrt(Dual a) {
+  double c = cbrt(a.v);
+  return Dual{c, a.d / (3.0 * c * c)};
+}
+
+struct DPar {
+  Dual gamma, iG, b02, th1c, calpha2, ikappa;
+  double pINF, icv, dp0, dp1, dp2;
+};
+
+// p: index of the seeded material field, or < 0 for none
+GPR_D DPar dpar_seed(const DevPar &P, int p) {
+  DPar D;
+  D.gamma = Dual{P.gamma, p == PD_GAMMA ? 1.0 : 0.0};
+  D.iG = Dual{P.iG, p == PD_IG ? 1.0 : 0.0};
+  D.b02 = Dual{P.b02, p == PD_B02 ? 1.0 : 0.0};
+  D.th1c = Dual{P.th1c, p == PD_TH1C ? 1.0 : 0.0};
+  D.calpha2 = Dual{P.calpha2, p == PD_CALPHA2 ? 1.0 : 0.0};
+  D.ikappa = Dual{P.ikappa, p == PD_IKAPPA ? 1.0 : 0.0};
+  D.pINF = P.pINF;
+  D.icv = P.icv;
+  D.dp0 = P.dp0;
+  D.dp1 = P.dp1;
+  D.dp2 = P.dp2;
+  return D;
+}
+
+template <bool TH> struct DPrim {
+  Dual r, ir, v[3], J[3], AdG[9], devGsq, G, irG, p, T;
+};
+
+// prim() of gpr_device.cuh for EOS 0 with beta = 0 and Tref = 0
+// (state.cpp, eos.cpp, mg.cpp:126-139)
+template <bool TH>
+GPR_D void dprim(const Dual *q, const DPar &P, DPrim<TH> &s) {
+  s.r = q[0];
+  s.ir = 1.0 / s.r;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    s.v[i] = q[2 + i] * s.ir;
+  const Dual *A = q + 5;
+  Dual G00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  Dual G11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  Dual G22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  Dual G01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  Dual G02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  Dual G12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  Dual t = (G00 + G11 + G22) * (1.0 / 3.0);
+  Dual D00 = G00 - t, D11 = G11 - t, D22 = G22 - t;
+  s.devGsq = D00 * D00 + D11 * D11 + D22 * D22 + 2.0 * (G01 * G01 + G02 * G02 + G12 * G12);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Dual a0 = A[3 * i], a1 = A[3 * i + 1], a2 = A[3 * i + 2];
+    s.AdG[3 * i + 0] = a0 * D00 + a1 * G01 + a2 * G02;
+    s.AdG[3 * i + 1] = a0 * G01 + a1 * D11 + a2 * G12;
+    s.AdG[3 * i + 2] = a0 * G02 + a1 * G12 + a2 * D22;
+  }
+  s.G = P.gamma - 1.0;
+  s.irG = s.ir * P.iG;
+  Dual E1 = q[1] * s.ir - 0.5 * (s.v[0] * s.v[0] + s.v[1] * s.v[1] + s.v[2] * s.v[2]) -
+            0.25 * (P.b02 * s.devGsq);
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      s.J[i] = q[14 + i] * s.ir;
+    E1 = E1 - 0.5 * (P.calpha2 * (s.J[0] * s.J[0] + s.J[1] * s.J[1] + s.J[2] * s.J[2]));
+  }
+  Dual er = P.pINF * s.ir;
+  s.p = (E1 - er) * (s.r * s.G) - P.pINF;
+  s.T = (s.p + P.pINF) * s.irG * P.icv;
+}
+
+// sigma column 0: -rho cs2 (A devG)^T A(:,0)   (state.cpp:23-29)
+template <bool TH>
+GPR_D void dsigma0(const Dual *q, const DPrim<TH> &s, const DPar &P, Dual *sg) {
+  const Dual *A = q + 5;
+  Dual f = -(s.r * P.b02);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    sg[i] = f * (s.AdG[i] * A[0] + s.AdG[3 + i] * A[3] + s.AdG[6 + i] * A[6]);
+}
+
+// F_x(Q)   (equations.cpp:11-48)
+template <bool TH, int V>
+GPR_D void dflux0(const Dual *q, const DPrim<TH> &s, const DPar &P, Dual *F) {
+  const Dual *A = q + 5;
+  Dual sg[3];
+  dsigma0<TH>(q, s, P, sg);
+  Dual v0 = s.v[0];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    F[k] = Dual{0.0, 0.0};
+  F[0] = q[2];
+  F[1] = v0 * (q[1] + s.p) - (sg[0] * s.v[0] + sg[1] * s.v[1] + sg[2] * s.v[2]);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    F[2 + i] = v0 * q[2 + i] - sg[i];
+  F[2] = F[2] + s.p;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    F[5 + 3 * i] = A[3 * i] * s.v[0] + A[3 * i + 1] * s.v[1] + A[3 * i + 2] * s.v[2];
+  if (TH) {
+    F[1] = F[1] + P.calpha2 * s.T * s.J[0];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      F[14 + i] = v0 * q[14 + i];
+    F[14] = F[14] + s.T;
+  }
+}
+
+GPR_D Dual ddet3(const Dual *A) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+         A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+
+// S(Q) for Newtonian viscosity (equations.cpp:50-67, sources.cpp:13-93)
+template <bool TH, int V>
+GPR_D void dsource(const Dual *q, const DPrim<TH> &s, const DPar &P, Dual *S) {
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    S[k] = Dual{0.0, 0.0};
+  S[2] = Dual{P.dp0, 0.0};
+  S[3] = Dual{P.dp1, 0.0};
+  S[4] = Dual{P.dp2, 0.0};
+  Dual dA = ddet3(q + 5);
+  Dual cb = dcbrt(dA);
+  Dual th = dA * cb * cb * P.th1c;  // det(A)^(5/3) rho0 / (2 mu)
+  Dual f = -(P.b02 * th);
+#pragma unroll
+  for (int i = 0; i < 9; i++)
+    S[5 + i] = s.AdG[i] * f;
+  if (TH) {
+    Dual g = -(P.calpha2 * s.T * P.ikappa);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      S[14 + i] = g * s.J[i];
+  }
+}
+
+// adjugate of a small matrix (adj[j][i] = cofactor (i, j))
+GPR_D double det3m(double a, double b, double c, double d, double e, double f, double g,
+                   double h, double i) {
+  return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+template <int m> GPR_D void adjugate(const double (&M)[m][m], double (&adj)[m][m]);
+
+template <> GPR_D void adjugate<3>(const double (&M)[3][3], double (&adj)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      int r0 = i == 0 ? 1 : 0, r1 = i == 2 ? 1 : 2;
+      int c0 = j == 0 ? 1 : 0, c1 = j == 2 ? 1 : 2;
+      double minor = M[r0][c0] * M[r1][c1] - M[r0][c1] * M[r1][c0];
+      adj[j][i] = ((i + j) & 1) ? -minor : minor;
+    }
+}
+
+template <> GPR_D void adjugate<4>(const double (&M)[4][4], double (&adj)[4][4]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int r[3], c[3];
+      int nr = 0, nc = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (k != i)
+          r[nr++] = k;
+        if (k != j)
+          c[nc++] = k;
+      }
+      double minor = det3m(M[r[0]][c[0]], M[r[0]][c[1]], M[r[0]][c[2]], M[r[1]][c[0]],
+                           M[r[1]][c[1]], M[r[1]][c[2]], M[r[2]][c[0]], M[r[2]][c[1]],
+                           M[r[2]][c[2]]);
+      adj[j][i] = ((i + j) & 1) ? -minor : minor;
+    }
+}
+
+// lambda_x(Q) = |v_x| + sqrt(max eig(Xi1 Xi2)) (system/eig.cpp:8-77), the
+// restatement of max_abs_eigs for EOS 0 and beta = 0.  The value of the
+// dominant eigenvalue comes from the same solver as the forward step.
+template <bool TH>
+GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
+  const Dual *A = q + 5;
+  Dual Gd[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+    Gd[j] = A[0] * A[j] + A[3] * A[3 + j] + A[6] * A[6 + j];
+  Dual ret[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      ret[3 * i + j] = (j == 0 ? 2.0 : 1.0) * s.AdG[3 * i + j] +
+                       (1.0 / 3.0) * (A[3 * i] * Gd[j]) + Gd[0] * A[3 * i + j];
+  Dual sg[3];
+  dsigma0<TH>(q, s, P, sg);
+  Dual dsr[3] = {s.ir * sg[0], s.ir * sg[1], s.ir * sg[2]};
+  // EOS 0: dp_ref/drho = 0, dGamma/drho = 0, de_ref/drho = -pINF / rho^2
+  Dual irG2 = s.irG * s.irG;
+  Dual dnum = s.G * (s.p + P.pINF);
+  Dual dedr = -(P.pINF * (s.ir * s.ir)) - dnum * irG2;
+  Dual rG = s.r * s.G;
+  Dual c02 = (s.p * (s.ir * s.ir) - dedr) * rG;
+  Dual b[3] = {sg[0] - s.r * dsr[0], sg[1] - s.r * dsr[1], sg[2] - s.r * dsr[2]};
+  b[0] = b[0] + s.r * c02;
+  constexpr int m = TH ? 4 : 3;
+  Dual X[m][m];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      Dual acc = P.b02 * (ret[i] * A[c] + ret[3 + i] * A[3 + c] + ret[6 + i] * A[6 + c]);
+      if (c == 0)
+        acc = acc - dsr[i];
+      if (i == 0)
+        acc = acc + b[c] * s.ir;
+      X[i][c] = acc;
+    }
+  if (TH) {
+    Dual h = P.calpha2 * s.T * s.G;
+    Dual tp = s.ir * s.irG * P.icv;
+    Dual dTr = -(dnum * irG2 * P.icv);
+    X[0][m - 1] = h * s.ir;
+    X[1][m - 1] = Dual{0.0, 0.0};
+    X[2][m - 1] = Dual{0.0, 0.0};
+    X[m - 1][0] = dTr + tp * b[0];
+    X[m - 1][1] = tp * b[1];
+    X[m - 1][2] = tp * b[2];
+    X[m - 1][m - 1] = tp * h;
+  }
+  double Xv[m][m];
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      Xv[i][j] = X[i][j].v;
+  double l2;
+  if (!max_eig_laguerre<m>(Xv, l2))
+    l2 = max_abs_eig<m>(Xv);
+  double M[m][m], adj[m][m];
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      M[i][j] = (i == j ? l2 : 0.0) - X[i][j].v;
+  adjugate<m>(M, adj);
+  double num = 0.0, den = 0.0;
+#pragma unroll
+  for (int i = 0; i < m; i++) {
+    den += adj[i][i];
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      num += adj[j][i] * X[i][j].d;
+  }
+  Dual lam = dsqrt(Dual{l2, num / den});
+  Dual v0 = s.v[0];
+  return v0.v > 0 ? v0 + lam : lam - v0;
+}
+
+// One tangent of the point functions at state qp: k < V seeds state
+// variable k, k >= V seeds material field k - V.
+template <class L>
+GPR_D void point_tangent(const double *qp, int k, const DevPar &P, Dual *F, Dual *S,
+                         Dual *lam) {
+  constexpr int V = L::V;
+  Dual q[V];
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    q[j] = Dual{qp[j], j == k ? 1.0 : 0.0};
+  DPar D = dpar_seed(P, k - V);
+  DPrim<L::THERMAL> s;
+  dprim<L::THERMAL>(q, D, s);
+  if (F)
+    dflux0<L::THERMAL, V>(q, s, D, F);
+  if (S)
+    dsource<L::THERMAL, V>(q, s, D, S);
+  if (lam)
+    *lam = dlambda0<L::THERMAL>(q, s, D);
+}
+
+// ---------------------------------------------------------------------------
+// B_x(v) x (bdot, d = 0, no level sets): transposes.
+template <int V>
+GPR_D void bdot0_xT(const double *v, const double *yb, double *xb) {  // xb += B^T yb
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    xb[6 + 3 * r] += -v[1] * yb[5 + 3 * r] + v[0] * yb[6 + 3 * r];
+    xb[7 + 3 * r] += -v[2] * yb[5 + 3 * r] + v[0] * yb[7 + 3 * r];
+  }
+}
+
+GPR_D void bdot0_vT(const double *x, const double *yb, double *vb) {  // vb = d(B(v)x)/dv^T yb
+  double a = 0.0, b = 0.0, c = 0.0;
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    a += x[6 + 3 * r] * yb[6 + 3 * r] + x[7 + 3 * r] * yb[7 + 3 * r];
+    b -= x[6 + 3 * r] * yb[5 + 3 * r];
+    c -= x[7 + 3 * r] * yb[5 + 3 * r];
+  }
+  vb[0] = a;
+  vb[1] = b;
+  vb[2] = c;
+}
+
+// qb += (dv/dq)^T vb for v = q[2..4] / q[0]
+GPR_D void vel_T(const double *q, const double *vb, double *qb, double scale) {
+  double ir = 1.0 / q[0];
+  double v0 = q[2] * ir, v1 = q[3] * ir, v2 = q[4] * ir;
+  qb[0] -= scale * (vb[0] * v0 + vb[1] * v1 + vb[2] * v2) * ir;
+  qb[2] += scale * vb[0] * ir;
+  qb[3] += scale * vb[1] * ir;
+  qb[4] += scale * vb[2] * ir;
+}
+
+// Sign of a ghost value relative to its source for the linear boundary codes
+// (bc_value: slip / symmetric flip the normal momentum and, for symmetric,
+// the A entries of row or column 0; stick flips the momentum).
+GPR_D double bc_sign(int code, int k) {
+  switch (code) {
+  case GPR_BC_SLIP:
+    return k == 2 ? -1.0 : 1.0;
+  case GPR_BC_SYMMETRIC: {
+    double s = k == 2 ? -1.0 : 1.0;
+    if (k >= 5 && k < 14) {
+      int r = (k - 5) / 3, c = (k - 5) % 3;
+      if (r == 0)
+        s = -s;
+      if (c == 0)
+        s = -s;
+    }
+    return s;
+  }
+  case GPR_BC_STICK:
+    return (k >= 2 && k < 5) ? -1.0 : 1.0;
+  default:
+    return 1.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forward-step recording.
+
+// argmax cell of the CFL maximum (smallest packed index among the cells that
+// attain it), after k_b_cfl_max has written the per-instance maximum
+template <class L>
+__global__ void __launch_bounds__(256) k_adj_argmax(const double *__restrict__ u, long ncell,
+                                                    const unsigned long long *__restrict__ mx,
+                                                    unsigned int *__restrict__ amax, Batch B) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  int inst = B.inst_u[c];
+  const DevPar &P = B.P[inst];
+  double q[V];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = u[c * V + k];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  double m = max_abs_eigs<L::THERMAL>(q, s, 0, P) * B.idx[inst];
+  if (m > 0.0 && (unsigned long long)__double_as_longlong(m) == mx[inst])
+    atomicMin(amax + inst, (unsigned int)c);
+}
+
+// k_b_clock_finalize with recording: dt_mode 0 takes the CFL step (and
+// writes it to dt_io if given), dt_mode 1 takes dt from dt_io (a step
+// schedule held fixed).  tclk receives {t, dt, tf, cfl, count} of the step,
+// aux {clipped, argmax cell}.
+static __global__ void k_adj_clock_finalize(unsigned long long *__restrict__ mx, Batch B,
+                                     double *__restrict__ dt_io, int dt_mode,
+                                     double *__restrict__ tclk, double *__restrict__ aux,
+                                     const unsigned int *__restrict__ amax) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= B.ninst)
+    return;
+  double *c = B.clk + 5 * k;
+  double t = c[0], tf = c[2], cfl = c[3];
+  long count = (long)c[4];
+  double dt = 0.0;
+  bool clipped = false;
+  if (t < tf) {
+    if (dt_mode == 1) {
+      dt = dt_io[k];
+    } else {
+      double MAX = __longlong_as_double((long long)mx[k]);
+      dt = cfl / MAX;
+      if (count <= 5)
+        dt *= 0.2;
+      if (t + dt > tf) {
+        dt = tf - t;
+        clipped = true;
+      }
+    }
+  }
+  c[1] = dt;
+  mx[k] = 0ull;
+  if (dt_mode == 0 && dt_io)
+    dt_io[k] = dt;
+  if (tclk) {
+#pragma unroll
+    for (int j = 0; j < 5; j++)
+      tclk[5 * k + j] = c[j];
+    aux[2 * k] = clipped ? 1.0 : 0.0;
+    aux[2 * k + 1] = (amax && amax[k] != 0xffffffffu) ? (double)amax[k] : -1.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Backward-step kernels.  B.clk points at the recorded clock of the step.
+
+// renormalisation: A+ = c A', c = cbrt(rho / (rho0 det A'))  (utils.cpp:6-23)
+template <int V>
+__global__ void k_adj_renorm(double *__restrict__ ub, const double *__restrict__ up, long ncell,
+                             Batch B) {
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  int inst = B.inst_u[c];
+  if (B.clk[5 * inst + 1] == 0.0)
+    return;
+  const double *q = up + c * V;
+  double r = q[0];
+  if (!(r > 0))
+    return;
+  double A[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    A[k] = q[5 + k];
+  double dA = det3(A);
+  double f = cbrt(r / (B.P[inst].rho0 * dA));
+  double *g = ub + c * V;
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    s += g[5 + k] * A[k];
+  // df/dA = -f/3 A^-T, df/drho = f / (3 rho)
+  double cof[9];
+  cof[0] = A[4] * A[8] - A[5] * A[7];
+  cof[1] = A[5] * A[6] - A[3] * A[8];
+  cof[2] = A[3] * A[7] - A[4] * A[6];
+  cof[3] = A[2] * A[7] - A[1] * A[8];
+  cof[4] = A[0] * A[8] - A[2] * A[6];
+  cof[5] = A[1] * A[6] - A[0] * A[7];
+  cof[6] = A[1] * A[5] - A[2] * A[4];
+  cof[7] = A[2] * A[3] - A[0] * A[5];
+  cof[8] = A[0] * A[4] - A[1] * A[3];
+  double h = s * f / (3.0 * dA);
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    g[5 + k] = f * g[5 + k] - h * cof[k];
+  g[0] += s * f / (3.0 * r);
+}
+
+// Jacobian columns at the 8 evaluation points of every predictor cell:
+// e = 0..3 the space-time nodes (t = e/2, s = e%2): F and S;
+// e = 4..7 the cell ends (t = (e-4)/2, side = (e-4)%2, side 0 = x = 0): F
+// and lambda (with the lambda value for the Rusanov switch in EV).
+// JN[((c*4 + e)*K + k)*2V + o], JE[((c*4 + e-4)*K + k)*(V+1) + o].
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_jac(const double *__restrict__ qh, long nb,
+                                                 double *__restrict__ JN, double *__restrict__ JE,
+                                                 double *__restrict__ EV, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= nb * 8 * K)
+    return;
+  int k = gid % K;
+  long rest = gid / K;
+  int e = rest % 8;
+  long c = rest / 8;
+  int inst = B.inst_b[c];
+  if (B.clk[5 * inst + 1] == 0.0)
+    return;
+  const DevPar &P = B.P[inst];
+  double qp[V];
+  if (e < 4) {
+    const double *src = qh + (c * 4 + e) * V;
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      qp[j] = src[j];
+  } else {
+    int t = (e - 4) / 2, side = (e - 4) % 2;
+    const double *q0 = qh + (c * 4 + 2 * t) * V;
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      qp[j] = C.endv[side][0] * q0[j] + C.endv[side][1] * q0[V + j];
+  }
+  Dual F[V];
+  if (e < 4) {
+    Dual S[V];
+    point_tangent<L>(qp, k, P, F, S, nullptr);
+    double *o = JN + ((c * 4 + e) * K + k) * 2 * V;
+#pragma unroll
+    for (int j = 0; j < V; j++) {
+      o[j] = F[j].d;
+      o[V + j] = S[j].d;
+    }
+  } else {
+    Dual lam;
+    point_tangent<L>(qp, k, P, F, nullptr, &lam);
+    double *o = JE + ((c * 4 + e - 4) * K + k) * (V + 1);
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      o[j] = F[j].d;
+    o[V] = lam.d;
+    if (k == 0) {
+      Prim<L::THERMAL> sp;
+      prim<L::THERMAL>(qp, P, sp);
+      EV[c * 4 + e - 4] = max_abs_eigs<L::THERMAL>(qp, sp, 0, P);
+    }
+  }
+}
+
+// One face's contribution to the cotangent of the state on one side.
+// Face flux f = max(lamL, lamR)(qL - qR) + F(qL) + F(qR) (fluxes.cpp:66-75),
+// path integral b = sum_n w_n B(qL + x_n dq) dq (fluxes.cpp:9-20); the left
+// cell receives -kk (b + f), the right -kk (b - f) (fv.cpp:143-146).
+template <int V, int K>
+GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR,
+                    const double *ubL, const double *ubR, double kk, bool mineL,
+                    const double *Jm, const Consts &C, double *qb, double *thb) {
+  double Fb[V], Bb[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double a = ubL ? ubL[k] : 0.0, b = ubR ? ubR[k] : 0.0;
+    Fb[k] = -kk * (a - b);
+    Bb[k] = -kk * (a + b);
+  }
+  bool Lmax = lamL > lamR;  // std::max(m1, m2) picks m2 on ties
+  double sm = Lmax ? lamL : lamR;
+  double sbar = 0.0;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    sbar += Fb[k] * (ql[k] - qr[k]);
+  bool mine_max = mineL ? Lmax : !Lmax;
+  for (int j = 0; j < K; j++) {
+    const double *col = Jm + j * (V + 1);
+    double acc = 0.0;
+#pragma unroll
+    for (int o = 0; o < V; o++)
+      acc += col[o] * Fb[o];
+    if (mine_max)
+      acc += sbar * col[V];
+    if (j < V)
+      qb[j] += acc;
+    else
+      thb[j - V] += acc;
+  }
+  double sgn = mineL ? sm : -sm;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    qb[k] += sgn * Fb[k];
+  double dq[V], dqb[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    dq[k] = qr[k] - ql[k];
+    dqb[k] = 0.0;
+  }
+#pragma unroll
+  for (int n = 0; n < NN; n++) {
+    double xn = C.nodes[n];
+    double rho = ql[0] + xn * dq[0];
+    double ir = 1.0 / rho;
+    double v[3] = {(ql[2] + xn * dq[2]) * ir, (ql[3] + xn * dq[3]) * ir,
+                   (ql[4] + xn * dq[4]) * ir};
+    double yb[V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      yb[k] = C.w[n] * Bb[k];
+    bdot0_xT<V>(v, yb, dqb);
+    double vb[3];
+    bdot0_vT(dq, yb, vb);
+    double f = mineL ? 1.0 - xn : xn;
+    qb[0] -= f * (vb[0] * v[0] + vb[1] * v[1] + vb[2] * v[2]) * ir;
+    qb[2] += f * vb[0] * ir;
+    qb[3] += f * vb[1] * ir;
+    qb[4] += f * vb[2] * ir;
+  }
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    qb[k] += mineL ? -dqb[k] : dqb[k];
+}
+
+// FV adjoint: cotangent of qh from the cotangent ubar of u' (faces and the
+// volume term), one thread per (predictor cell, time node).  Also the
+// material-field cotangents (thf) and <ubar, u' - u> / dt (dtf) since the FV
+// increment is linear in dt.
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_fv(
+    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ JN,
+    const double *__restrict__ JE, const double *__restrict__ EV, const double *__restrict__ un,
+    const double *__restrict__ up, long nb, double *__restrict__ qbar, double *__restrict__ thf,
+    double *__restrict__ dtf, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= nb * 2)
+    return;
+  long c = gid / 2;
+  int t = gid % 2;
+  int inst = B.inst_b[c];
+  double dt = B.clk[5 * inst + 1];
+  double *qb = qbar + (c * 4 + 2 * t) * V;
+  double th[NPD];
+#pragma unroll
+  for (int p = 0; p < NPD; p++)
+    th[p] = 0.0;
+  if (dt == 0.0) {
+    for (int k = 0; k < 2 * V; k++)
+      qb[k] = 0.0;
+#pragma unroll
+    for (int p = 0; p < NPD; p++)
+      thf[(c * 2 + t) * NPD + p] = 0.0;
+    if (t == 0)
+      dtf[c] = 0.0;
+    return;
+  }
+  const int li = (int)(c - B.off_b[inst]), nx = B.nx[inst];
+  const double idx = B.idx[inst];
+  const double dx = 1.0 / idx;
+  const double kk = (dt * C.w[t]) / (2.0 * dx);
+  const double *ubi = ubar + (long)B.off_u[inst] * V;
+  const double *qc = qh + (c * 4 + 2 * t) * V;
+  double acc[2][V], qLb[V], qRb[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    qLb[k] = 0.0;
+    qRb[k] = 0.0;
+  }
+  if (li <= nx) {  // face li: this cell on the left
+    int f = li;
+    const double *qn = qh + ((c + 1) * 4 + 2 * t) * V;
+    double ql[V], qr[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      ql[k] = C.endv[1][0] * qc[k] + C.endv[1][1] * qc[V + k];
+      qr[k] = C.endv[0][0] * qn[k] + C.endv[0][1] * qn[V + k];
+    }
+    face_adj<V, K>(ql, qr, EV[c * 4 + 2 * t + 1], EV[(c + 1) * 4 + 2 * t],
+                   f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
+                   kk, true, JE + (c * 4 + 2 * t + 1) * K * (V + 1), C, qLb, th);
+  }
+  if (li >= 1) {  // face li - 1: this cell on the right
+    int f = li - 1;
+    const double *qp = qh + ((c - 1) * 4 + 2 * t) * V;
+    double ql[V], qr[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      ql[k] = C.endv[1][0] * qp[k] + C.endv[1][1] * qp[V + k];
+      qr[k] = C.endv[0][0] * qc[k] + C.endv[0][1] * qc[V + k];
+    }
+    face_adj<V, K>(ql, qr, EV[(c - 1) * 4 + 2 * t + 1], EV[c * 4 + 2 * t],
+                   f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
+                   kk, false, JE + (c * 4 + 2 * t) * K * (V + 1), C, qRb, th);
+  }
+#pragma unroll
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      acc[m][k] = C.endv[1][m] * qLb[k] + C.endv[0][m] * qRb[k];
+  if (li >= 1 && li <= nx) {
+    // volume term: u += (dt w_t) w_s (S - idx B(v) dq)   (fv.cpp:11-109)
+    const double *ubc = ubi + (long)(li - 1) * V;
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      double a = (dt * C.w[t]) * C.w[s];
+      const double *qs = qc + s * V, *qo = qc + (1 - s) * V;
+      const double *J = JN + (c * 4 + 2 * t + s) * K * 2 * V;
+      for (int j = 0; j < K; j++) {
+        const double *col = J + j * 2 * V + V;
+        double x = 0.0;
+#pragma unroll
+        for (int o = 0; o < V; o++)
+          x += col[o] * ubc[o];
+        if (j < V)
+          acc[s][j] += a * x;
+        else
+          th[j - V] += a * x;
+      }
+      double yb[V], dq[V], xb[V];
+      double ir = 1.0 / qs[0];
+      double v[3] = {qs[2] * ir, qs[3] * ir, qs[4] * ir};
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        yb[k] = -a * idx * ubc[k];
+        dq[k] = C.derv[s][s] * qs[k] + C.derv[s][1 - s] * qo[k];
+        xb[k] = 0.0;
+      }
+      double vb[3];
+      bdot0_vT(dq, yb, vb);
+      vel_T(qs, vb, acc[s], 1.0);
+      bdot0_xT<V>(v, yb, xb);
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        acc[s][k] += C.derv[s][s] * xb[k];
+        acc[1 - s][k] += C.derv[s][1 - s] * xb[k];
+      }
+    }
+    if (t == 0) {
+      long j = (long)B.off_u[inst] + li - 1;
+      double x = 0.0;
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        x += ubc[k] * (up[j * V + k] - un[j * V + k]);
+      dtf[c] = x / dt;
+    }
+  } else if (t == 0) {
+    dtf[c] = 0.0;
+  }
+#pragma unroll
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      qb[m * V + k] = acc[m][k];
+#pragma unroll
+  for (int p = 0; p < NPD; p++)
+    thf[(c * 2 + t) * NPD + p] = th[p];
+}
+
+// Predictor adjoint at the converged fixed point.  With
+//   R(q)_{t,i} = w_t w_i (S(q_ti) - B(q_ti) x_ti) - w_t idx sum_m DG_DER[i][m] F(q_tm),
+//   x_ti = idx sum_m DERVALS[i][m] q_tm                      (dg1.cpp:8-66)
+// the fixed point q = DG_U^-1 (W w + dt R(q)) gives, for the cotangent qbar
+// of q, mu = (DG_U - dt dR/dq)^-T qbar, and then
+//   wbar = (d(W w)/dw)^T mu,  dtbar = mu . R(q),  thbar = dt mu . dR/dth.
+// Stage 1 (k_adj_pred_iter, 4 lanes per cell as in k_predictor_picard)
+// iterates mu <- DG_U^-T (qbar + dt (dR/dq)^T mu), which contracts exactly
+// where the forward Picard iteration does; cells it leaves unconverged
+// (those the forward hands to its Newton pass) get the exact dense solve of
+// stage 2 (k_adj_pred_dense, one block per cell); stage 3 (k_adj_pred_post)
+// forms the cotangents from mu.
+constexpr int ADJ_PRED_IT = 100;
+constexpr double ADJ_PRED_TOL = 1e-13;
+
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_pred_iter(
+    const double *__restrict__ qh, const double *__restrict__ qbar, const double *__restrict__ JN,
+    long nb, double *__restrict__ mu_buf, int32_t *__restrict__ need, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int g = threadIdx.x % 4;
+  const long c = gt / 4;
+  const bool valid = c < nb;
+  const long cc = valid ? c : 0;
+  const int t = g / 2, i = g % 2;
+  const int inst = B.inst_b[cc];
+  const double dt = B.clk[5 * inst + 1];
+  const double idx = B.idx[inst];
+  const bool active = valid && dt != 0.0;
+  double q[V], qb[V], mu[V], other[V], x[V];
+  const double *qs = qh + (cc * 4 + g) * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    q[k] = qs[k];
+    qb[k] = active ? qbar[(cc * 4 + g) * V + k] : 0.0;
+    mu[k] = 0.0;
+  }
+  shfl_vec<V>(q, other, 1);
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    x[k] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * other[k]);
+  double ir = 1.0 / q[0];
+  double v[3] = {q[2] * ir, q[3] * ir, q[4] * ir};
+  const double *J = JN + (cc * 4 + g) * K * 2 * V;
+  const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx;
+  const double iws = 1.0 / C.w[i];
+  bool done = !active;
+  bool conv = !active;
+  for (int it = 0; it < ADJ_PRED_IT; it++) {
+    if (__all_sync(0xffffffffu, done))
+      break;
+    double xb[V], r[V], z[V], y[V], mun[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      xb[k] = 0.0;
+      z[k] = -wn * mu[k];
+    }
+    bdot0_xT<V>(v, z, xb);  // xb = -wn B^T mu
+    double vb[3];
+    bdot0_vT(x, z, vb);  // through v(q): -wn (d(B x)/dv)^T mu
+    shfl_vec<V>(mu, other, 1);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      y[k] = C.dgder[i][i] * mu[k] + C.dgder[1 - i][i] * other[k];
+    for (int j = 0; j < V; j++) {
+      const double *col = J + j * 2 * V;
+      double sF = 0.0, sS = 0.0;
+#pragma unroll
+      for (int o = 0; o < V; o++) {
+        sF += col[o] * y[o];
+        sS += col[V + o] * mu[o];
+      }
+      r[j] = wn * sS - wti * sF;
+    }
+    vel_T(q, vb, r, 1.0);
+    shfl_vec<V>(xb, other, 1);
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      r[k] += idx * (C.derv[i][i] * xb[k] + C.derv[1 - i][i] * other[k]);
+      z[k] = qb[k] + dt * r[k];
+    }
+    shfl_vec<V>(z, other, 2);
+    double dd = 0.0, sc = 0.0;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      mun[k] = (C.dgmatinv[t][t] * z[k] + C.dgmatinv[1 - t][t] * other[k]) * iws;
+      dd = fmax(dd, fabs(mun[k] - mu[k]));
+      sc = fmax(sc, fabs(mun[k]));
+    }
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) {
+      dd = fmax(dd, __shfl_xor_sync(0xffffffffu, dd, o));
+      sc = fmax(sc, __shfl_xor_sync(0xffffffffu, sc, o));
+    }
+    if (!done) {
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        mu[k] = mun[k];
+      if (dd <= ADJ_PRED_TOL * sc || !(sc == sc)) {
+        done = true;
+        conv = sc == sc;
+      }
+    }
+  }
+  if (!valid)
+    return;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    mu_buf[(c * 4 + g) * V + k] = mu[k];
+  if (g == 0)
+    need[c] = conv ? 0 : 1;
+}
+
+// d(B_x(v(q)) x)_r / dq_c and B_x(v)[r][c] (bdot, d = 0)
+GPR_D double dBx_dq(int r, int c, const double *x, const double *v, double iq0) {
+  double dv[3] = {0.0, 0.0, 0.0};
+  if (r >= 5 && r < 14) {
+    int rr = (r - 5) / 3, cc = (r - 5) % 3;
+    if (cc == 0) {
+      dv[1] = -x[6 + 3 * rr];
+      dv[2] = -x[7 + 3 * rr];
+    } else {
+      dv[0] = x[5 + 3 * rr + cc];
+    }
+  }
+  if (c == 0)
+    return -(dv[0] * v[0] + dv[1] * v[1] + dv[2] * v[2]) * iq0;
+  if (c >= 2 && c < 5)
+    return dv[c - 2] * iq0;
+  return 0.0;
+}
+
+GPR_D double Bx_mat(int r, int c, const double *v) {
+  if (r < 5 || r >= 14)
+    return 0.0;
+  int rr = (r - 5) / 3, cc = (r - 5) % 3;
+  if (cc == 0) {
+    if (c == 6 + 3 * rr)
+      return -v[1];
+    if (c == 7 + 3 * rr)
+      return -v[2];
+    return 0.0;
+  }
+  return c == r ? v[0] : 0.0;
+}
+
+// Exact transposed solve (DG_U - dt dR/dq)^T mu = qbar for the cells the
+// iteration left unconverged: the 4V x 4V system assembled from the node
+// Jacobians in shared memory, Gaussian elimination with partial pivoting.
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_pred_dense(
+    const double *__restrict__ qh, const double *__restrict__ qbar, const double *__restrict__ JN,
+    long nb, const int32_t *__restrict__ need, double *__restrict__ mu_buf,
+    int32_t *__restrict__ info, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD, NQ = 4 * V, LD = NQ + 1;
+  __shared__ double A[NQ * LD];
+  __shared__ double b[NQ], lcol[NQ];
+  __shared__ double xs[4][V], vs[4][3], iq0[4];
+  __shared__ int piv;
+  __shared__ int bad;
+  const long c = blockIdx.x;
+  if (c >= nb || !need[c])
+    return;
+  const int inst = B.inst_b[c];
+  const double dt = B.clk[5 * inst + 1];
+  const double idx = B.idx[inst];
+  const double *qc = qh + c * 4 * V;
+  if (threadIdx.x < 4) {
+    int g = threadIdx.x, i = g % 2;
+    const double *q = qc + g * V, *qo = qc + (g ^ 1) * V;
+    for (int k = 0; k < V; k++)
+      xs[g][k] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * qo[k]);
+    double ir = 1.0 / q[0];
+    iq0[g] = ir;
+    vs[g][0] = q[2] * ir;
+    vs[g][1] = q[3] * ir;
+    vs[g][2] = q[4] * ir;
+  }
+  if (threadIdx.x == 0)
+    bad = 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < NQ * NQ; e += blockDim.x) {
+    int row = e / NQ, col = e % NQ;  // entry M[row][col]
+    int gr = row / V, vr = row % V, gc = col / V, vc = col % V;
+    int t = gr / 2, i = gr % 2, tc = gc / 2, m = gc % 2;
+    double val = (i == m && vr == vc) ? C.dgmat[t][tc] * C.w[i] : 0.0;
+    if (t == tc) {
+      const double *Jn = JN + (c * 4 + gc) * K * 2 * V;
+      double wn = C.w[t] * C.w[i];
+      double r = -C.w[t] * idx * C.dgder[i][m] * Jn[vc * 2 * V + vr];
+      if (i == m)
+        r += wn * (Jn[vc * 2 * V + V + vr] - dBx_dq(vr, vc, xs[gr], vs[gr], iq0[gr]));
+      r -= wn * Bx_mat(vr, vc, vs[gr]) * idx * C.derv[i][m];
+      val -= dt * r;
+    }
+    A[col * LD + row] = val;  // transposed
+  }
+  for (int r = threadIdx.x; r < NQ; r += blockDim.x)
+    b[r] = qbar[c * 4 * V + r];
+  __syncthreads();
+  for (int k = 0; k < NQ; k++) {
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int r = k + threadIdx.x; r < NQ; r += 32) {
+        double a = fabs(A[r * LD + k]);
+        if (a > best) {
+          best = a;
+          bi = r;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_down_sync(0xffffffffu, best, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        piv = bi;
+        if (!(best > 0.0))
+          bad = 1;
+      }
+    }
+    __syncthreads();
+    if (bad)
+      break;
+    const int p = piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < NQ; j += blockDim.x) {
+        double tmp = A[k * LD + j];
+        A[k * LD + j] = A[p * LD + j];
+        A[p * LD + j] = tmp;
+      }
+      if (threadIdx.x == 0) {
+        double tmp = b[k];
+        b[k] = b[p];
+        b[p] = tmp;
+      }
+    }
+    __syncthreads();
+    const double ia = 1.0 / A[k * LD + k];
+    for (int r = k + 1 + threadIdx.x; r < NQ; r += blockDim.x)
+      lcol[r] = A[r * LD + k] * ia;
+    __syncthreads();
+    const int w = NQ - k - 1;
+    for (int e = threadIdx.x; e < w * (w + 1); e += blockDim.x) {
+      int r = k + 1 + e / (w + 1), j = k + 1 + e % (w + 1);
+      if (j < NQ)
+        A[r * LD + j] -= lcol[r] * A[k * LD + j];
+      else
+        b[r] -= lcol[r] * b[k];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (threadIdx.x == 0)
+      info[c] |= 1;
+    return;
+  }
+  // back substitution by warp 0
+  if (threadIdx.x < 32) {
+    for (int k = NQ - 1; k >= 0; k--) {
+      double s = 0.0;
+      for (int j = k + 1 + threadIdx.x; j < NQ; j += 32)
+        s += A[k * LD + j] * b[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0)
+        b[k] = (b[k] - s) / A[k * LD + k];
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < NQ; r += blockDim.x)
+    mu_buf[c * 4 * V + r] = b[r];
+}
+
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_pred_post(
+    const double *__restrict__ qh, const double *__restrict__ mu_buf,
+    const double *__restrict__ JN, long nb, double *__restrict__ wbar, double *__restrict__ thp,
+    double *__restrict__ dtp, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int g = threadIdx.x % 4;
+  const long c = gt / 4;
+  const bool valid = c < nb;
+  const long cc = valid ? c : 0;
+  const int t = g / 2, i = g % 2;
+  const int inst = B.inst_b[cc];
+  const double dt = B.clk[5 * inst + 1];
+  const DevPar &P = B.P[inst];
+  const double idx = B.idx[inst];
+  const bool active = valid && dt != 0.0;
+  double q[V], mu[V], other[V], y[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    q[k] = qh[(cc * 4 + g) * V + k];
+    mu[k] = active ? mu_buf[(cc * 4 + g) * V + k] : 0.0;
+  }
+  const double *J = JN + (cc * 4 + g) * K * 2 * V;
+  const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx;
+  shfl_vec<V>(mu, other, 1);
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    y[k] = C.dgder[i][i] * mu[k] + C.dgder[1 - i][i] * other[k];
+  // R(q) at this node: dg_rhs_node with dt = 1 and W w = 0
+  double R[V], zero[V];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    zero[k] = 0.0;
+  dg_rhs_node<L, 1>(q, zero, R, t, i, 0, 1.0, idx, 1.0, P, C);
+  double dtb = 0.0;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    dtb += mu[k] * R[k];
+  double th[NPD];
+#pragma unroll
+  for (int p = 0; p < NPD; p++) {
+    double sF = 0.0, sS = 0.0;
+    if (active) {
+      const double *col = J + (V + p) * 2 * V;
+#pragma unroll
+      for (int o = 0; o < V; o++) {
+        sF += col[o] * y[o];
+        sS += col[V + o] * mu[o];
+      }
+    }
+    th[p] = dt * (wn * sS - wti * sF);
+  }
+  // W w: Ww(t, s) = ENDVALS[0][t] w_s wh(s)  (dg1.cpp:68-73)
+  double wb[V];
+  const double f = C.endv[0][t] * C.w[i];
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    wb[k] = f * mu[k];
+  shfl_vec<V>(wb, other, 2);
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    dtb += __shfl_xor_sync(0xffffffffu, dtb, o);
+#pragma unroll
+    for (int p = 0; p < NPD; p++)
+      th[p] += __shfl_xor_sync(0xffffffffu, th[p], o);
+  }
+  if (!valid)
+    return;
+  if (t == 0) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      wbar[(c * 2 + i) * V + k] = active ? wb[k] + other[k] : 0.0;
+  }
+  if (g == 0) {
+    dtp[c] = active ? dtb : 0.0;
+#pragma unroll
+    for (int p = 0; p < NPD; p++)
+      thp[c * NPD + p] = active ? th[p] : 0.0;
+  }
+}
+
+// WENO adjoint: per (predictor cell, variable), the cotangents of the three
+// stencil values (weno.cpp:4-73 with the gap-free 1D stencils).
+template <int V>
+__global__ void k_adj_weno(const double *__restrict__ wbar, const double *__restrict__ un,
+                           long nb, double *__restrict__ gst, Consts C, Batch B) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= nb * V)
+    return;
+  int k = idx % V;
+  long c = idx / V;
+  int inst = B.inst_b[c];
+  double *out = gst + (c * V + k) * 3;
+  if (B.clk[5 * inst + 1] == 0.0) {
+    out[0] = out[1] = out[2] = 0.0;
+    return;
+  }
+  int li = (int)(c - B.off_b[inst]), nx = B.nx[inst];
+  const double *ui = un + (long)B.off_u[inst] * V;
+  double d[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    int b = li + m;
+    if (b >= NN && b < nx + NN) {
+      d[m] = ui[(long)(b - NN) * V + k];
+    } else {
+      int side = b >= nx + NN;
+      int gi = side ? b - nx - NN : b;
+      int code = B.bc[2 * inst + side];
+      int si = bc_src_index(code, side, gi, nx);
+      if (code == GPR_BC_PERIODIC)
+        code = GPR_BC_TRANSMISSIVE;
+      d[m] = bc_value<V>(code, 0, k, ui + (long)si * V);
+    }
+  }
+  double a = d[0], b = d[1], cc = d[2];
+  double wL0 = C.mLinv[0][0] * a + C.mLinv[0][1] * b;
+  double wL1 = C.mLinv[1][0] * a + C.mLinv[1][1] * b;
+  double wR0 = C.mRinv[0][0] * b + C.mRinv[0][1] * cc;
+  double wR1 = C.mRinv[1][0] * b + C.mRinv[1][1] * cc;
+  double tL = (wL0 * C.sig[0][0] + wL1 * C.sig[1][0]) * wL0 +
+              (wL0 * C.sig[0][1] + wL1 * C.sig[1][1]) * wL1 + WENO_EPS;
+  double tR = (wR0 * C.sig[0][0] + wR1 * C.sig[1][0]) * wR0 +
+              (wR0 * C.sig[0][1] + wR1 * C.sig[1][1]) * wR1 + WENO_EPS;
+  double pL = tL * tL, pR = tR * tR;
+  pL *= pL;
+  pL *= pL;
+  pR *= pR;
+  pR *= pR;
+  double oL = LAMS / pL, oR = LAMS / pR;
+  double iden = 1.0 / (oL + oR);
+  double o0 = (wL0 * oL + wR0 * oR) * iden, o1 = (wL1 * oL + wR1 * oR) * iden;
+  double g0 = wbar[(c * 2 + 0) * V + k], g1 = wbar[(c * 2 + 1) * V + k];
+  double oLb = (g0 * (wL0 - o0) + g1 * (wL1 - o1)) * iden;
+  double oRb = (g0 * (wR0 - o0) + g1 * (wR1 - o1)) * iden;
+  double tLb = -8.0 * oL / tL * oLb, tRb = -8.0 * oR / tR * oRb;
+  double sx = C.sig[0][1] + C.sig[1][0];
+  double wL0b = g0 * oL * iden + tLb * (2.0 * C.sig[0][0] * wL0 + sx * wL1);
+  double wL1b = g1 * oL * iden + tLb * (sx * wL0 + 2.0 * C.sig[1][1] * wL1);
+  double wR0b = g0 * oR * iden + tRb * (2.0 * C.sig[0][0] * wR0 + sx * wR1);
+  double wR1b = g1 * oR * iden + tRb * (sx * wR0 + 2.0 * C.sig[1][1] * wR1);
+  out[0] = C.mLinv[0][0] * wL0b + C.mLinv[1][0] * wL1b;
+  out[1] = C.mLinv[0][1] * wL0b + C.mLinv[1][1] * wL1b + C.mRinv[0][0] * wR0b +
+           C.mRinv[1][0] * wR1b;
+  out[2] = C.mRinv[0][1] * wR0b + C.mRinv[1][1] * wR1b;
+}
+
+// ubar(u) += sum of the stencil cotangents of every ub cell that copies u
+// (interior cell j+N, and the ghost cells whose source is j).
+template <int V>
+__global__ void k_adj_gather(double *__restrict__ ubar, const double *__restrict__ gst,
+                             long nu, Batch B) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= nu * V)
+    return;
+  int k = idx % V;
+  long j = idx / V;
+  int inst = B.inst_u[j];
+  if (B.clk[5 * inst + 1] == 0.0)
+    return;
+  int lj = (int)(j - B.off_u[inst]), nx = B.nx[inst];
+  const double *gi = gst + (long)B.off_b[inst] * V * 3;
+  auto G = [&](int b) {
+    double s = 0.0;
+    for (int c = b - 2; c <= b; c++)
+      if (c >= 0 && c <= nx + 1)
+        s += gi[((long)c * V + k) * 3 + (b - c)];
+    return s;
+  };
+  double add = G(lj + NN);
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    int code = B.bc[2 * inst + side];
+#pragma unroll
+    for (int g = 0; g < NN; g++) {
+      if (bc_src_index(code, side, g, nx) == lj) {
+        int b = side ? nx + NN + g : g;
+        add += bc_sign(code == GPR_BC_PERIODIC ? GPR_BC_TRANSMISSIVE : code, k) * G(b);
+      }
+    }
+  }
+  ubar[j * V + k] += add;
+}
+
+// Per instance (one block each): sum the material-field and dt cotangents
+// of the step, and propagate dt through the CFL rule.  tbar carries the
+// cotangent of the clock: the clipped last step dt = tf - t passes -dtbar
+// to every earlier step's dt.
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_reduce(
+    double *__restrict__ ubar, double *__restrict__ thbar, double *__restrict__ tbar,
+    const double *__restrict__ thf, const double *__restrict__ thp, const double *__restrict__ dtf,
+    const double *__restrict__ dtp, const double *__restrict__ un, const double *__restrict__ aux,
+    int frozen, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  const int inst = blockIdx.x;
+  const double dt = B.clk[5 * inst + 1];
+  if (dt == 0.0)
+    return;
+  __shared__ double red[128][NPD + 1];
+  __shared__ double cf;
+  const long ob = B.off_b[inst];
+  const int nbi = B.nx[inst] + 2;
+  double acc[NPD + 1];
+#pragma unroll
+  for (int p = 0; p <= NPD; p++)
+    acc[p] = 0.0;
+  for (int c = threadIdx.x; c < nbi; c += blockDim.x) {
+    long cb = ob + c;
+#pragma unroll
+    for (int p = 0; p < NPD; p++)
+      acc[p] += thf[(cb * 2) * NPD + p] + thf[(cb * 2 + 1) * NPD + p] + thp[cb * NPD + p];
+    acc[NPD] += dtf[cb] + dtp[cb];
+  }
+#pragma unroll
+  for (int p = 0; p <= NPD; p++)
+    red[threadIdx.x][p] = acc[p];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int p = 0; p <= NPD; p++)
+        red[threadIdx.x][p] += red[threadIdx.x + s][p];
+    __syncthreads();
+  }
+  const bool clipped = aux[2 * inst] != 0.0;
+  const long cstar = (long)aux[2 * inst + 1];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int p = 0; p < NPD; p++)
+      thbar[inst * NPD + p] += red[0][p];
+    double dtb = red[0][NPD];
+    cf = 0.0;
+    if (!frozen) {
+      if (clipped) {
+        tbar[inst] = -dtb;
+      } else if (cstar >= 0) {
+        double dtot = dtb + tbar[inst];
+        const DevPar &P = B.P[inst];
+        double q[V];
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          q[k] = un[cstar * V + k];
+        Prim<L::THERMAL> s;
+        prim<L::THERMAL>(q, P, s);
+        double lam = max_abs_eigs<L::THERMAL>(q, s, 0, P);
+        cf = -dtot * dt / lam;  // dt = cfl dx / lam  =>  d dt / d lam = -dt / lam
+      }
+    }
+  }
+  __syncthreads();
+  if (cf != 0.0 && threadIdx.x < K) {
+    const int k = threadIdx.x;
+    double q[V];
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      q[j] = un[cstar * V + j];
+    Dual lam;
+    point_tangent<L>(q, k, B.P[inst], nullptr, nullptr, &lam);
+    if (k < V)
+      ubar[cstar * V + k] += cf * lam.d;
+    else
+      thbar[inst * NPD + (k - V)] += cf * lam.d;
+  }
+}
+
+// Pointwise Jacobians (test hook): JF, JS [count][K][V], dlam [count][K].
+template <class L>
+__global__ void k_adj_point(const double *__restrict__ Q, long count, double *__restrict__ JF,
+                            double *__restrict__ JS, double *__restrict__ dlam, DevPar P) {
+  constexpr int V = L::V, K = V + NPD;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= count * K)
+    return;
+  int k = gid % K;
+  long c = gid / K;
+  double q[V];
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    q[j] = Q[c * V + j];
+  Dual F[V], S[V], lam;
+  point_tangent<L>(q, k, P, F, S, &lam);
+#pragma unroll
+  for (int j = 0; j < V; j++) {
+    JF[(c * K + k) * V + j] = F[j].d;
+    JS[(c * K + k) * V + j] = S[j].d;
+  }
+  dlam[c * K + k] = lam.d;
+}
+
+}  // namespace gpr

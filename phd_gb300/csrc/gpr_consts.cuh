@@ -23,6 +23,12 @@ struct Consts {
   double dgmat[NN][NN];          // DG_END - DG_DER^T
   double dgmatinv[NN][NN];       // (DG_END - DG_DER^T)^-1
   double wprod2[NN][NN];         // w_i w_j
+  // predictor stopping rules: Picard |dq| <= dg_tol (1 + |q|) within dg_it
+  // iterations (options.h:29-30), stiff-source Newton |delta| <= stiff_tol
+  // (1 + |q|) within stiff_it; the differentiable step tightens them so the
+  // predictor result is its fixed point to rounding
+  double dg_tol, stiff_tol;
+  int dg_it, stiff_it;
 };
 
 // Lagrange basis on the two nodes: psi_0(x) = (x - x1)/(x0 - x1), ...
@@ -88,6 +94,10 @@ inline Consts make_consts() {
   for (int i = 0; i < NN; i++)
     for (int j = 0; j < NN; j++)
       c.wprod2[i][j] = c.w[i] * c.w[j];
+  c.dg_tol = 6e-6;
+  c.dg_it = 50;
+  c.stiff_tol = 1e-11;
+  c.stiff_it = 60;
   return c;
 }
 

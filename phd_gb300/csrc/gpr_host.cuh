@@ -1,0 +1,125 @@
+// gpr_host.cuh - host-side helpers shared by the C ABI translation units:
+// constants, launch sizing, the packed layout of the batched form and the
+// persistent launch of the stiff-source Newton pass.
+#pragma once
+
+#include <stdio.h>
+
+#include "gpr_kernels.cuh"
+
+namespace gpr {
+namespace host {
+
+inline const Consts &consts() {
+  static Consts c = make_consts();
+  return c;
+}
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+inline int blocks(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+inline int cuda_rc() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpr_gb300: CUDA error %s\n", cudaGetErrorString(e));
+    return GPR_E_CUDA;
+  }
+  return GPR_OK;
+}
+
+// 256-byte aligned pieces of a scratch buffer (offsets in doubles)
+struct Carve {
+  long o = 0;
+  long take(long ndoubles) {
+    long at = o;
+    o += (ndoubles + 31) & ~31L;
+    return at;
+  }
+};
+
+// Packed sizes and scratch offsets (in doubles) of the batched form.
+struct BatchLayout {
+  long nu = 0, nub = 0, nb = 0, nf = 0;
+  long o_par, o_iu, o_iub, o_ib, o_if, o_nx, o_ou, o_oub, o_ob, o_of, o_bc, o_idx, o_mx;
+  long o_ub, o_wh, o_qh, o_fb, total;
+};
+
+inline BatchLayout batch_layout_v(int ninst, const int32_t *nx, int V) {
+  BatchLayout b;
+  for (int k = 0; k < ninst; k++) {
+    b.nu += nx[k];
+    b.nub += nx[k] + 2 * NN;
+    b.nb += nx[k] + 2;
+    b.nf += nx[k] + 1;
+  }
+  auto dbl = [](long bytes) { return (bytes + 7) / 8; };
+  Carve cv;
+  b.o_par = cv.take(dbl((long)ninst * sizeof(DevPar)));
+  b.o_iu = cv.take(dbl(b.nu * 4));
+  b.o_iub = cv.take(dbl(b.nub * 4));
+  b.o_ib = cv.take(dbl(b.nb * 4));
+  b.o_if = cv.take(dbl(b.nf * 4));
+  b.o_nx = cv.take(dbl(ninst * 4L));
+  b.o_ou = cv.take(dbl(ninst * 4L));
+  b.o_oub = cv.take(dbl(ninst * 4L));
+  b.o_ob = cv.take(dbl(ninst * 4L));
+  b.o_of = cv.take(dbl(ninst * 4L));
+  b.o_bc = cv.take(dbl(ninst * 8L));
+  b.o_idx = cv.take(ninst);
+  b.o_mx = cv.take(ninst);
+  b.o_ub = cv.take(b.nub * V);
+  b.o_wh = cv.take(b.nb * NN * V);
+  b.o_qh = cv.take(b.nb * NN * NN * V);
+  b.o_fb = cv.take(b.nf * 2 * V);
+  b.total = cv.o;
+  return b;
+}
+
+inline Batch batch_view_of(double *scr, int ninst, const BatchLayout &b, double *clk) {
+  Batch B;
+  B.P = (const DevPar *)(scr + b.o_par);
+  B.inst_u = (const int32_t *)(scr + b.o_iu);
+  B.inst_ub = (const int32_t *)(scr + b.o_iub);
+  B.inst_b = (const int32_t *)(scr + b.o_ib);
+  B.inst_f = (const int32_t *)(scr + b.o_if);
+  B.nx = (const int32_t *)(scr + b.o_nx);
+  B.off_u = (const int32_t *)(scr + b.o_ou);
+  B.off_ub = (const int32_t *)(scr + b.o_oub);
+  B.off_b = (const int32_t *)(scr + b.o_ob);
+  B.off_f = (const int32_t *)(scr + b.o_of);
+  B.bc = (const int32_t *)(scr + b.o_bc);
+  B.idx = scr + b.o_idx;
+  B.clk = clk;
+  B.ninst = ninst;
+  return B;
+}
+
+// Stiff-source Newton pass over the cells the Picard pass flagged: a
+// persistent grid sized by occupancy (the kernel strides over the cells).
+template <class L, int ND, bool BATCH>
+int launch_stiff(double *qh, const double *wh, long ncb, const uint8_t *mask, int32_t *status,
+                 double dt, const double *dt_dev, double idx, double idy, const DevPar &P,
+                 const Consts &C, cudaStream_t st, const Batch &B) {
+  constexpr int NP = ND == 1 ? NN * NN : NN * NN * NN;
+  constexpr int BS = 64;
+  size_t smem = (size_t)(BS / NP) * StiffSmem<L, ND>::per_cell * sizeof(float);
+  // per device and cheap: set on every call
+  cudaFuncSetAttribute(k_predictor_stiff<L, ND, BATCH>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0, nsm = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_predictor_stiff<L, ND, BATCH>, BS,
+                                                smem);
+  long need = (ncb * NP + BS - 1) / BS;
+  long grid = (long)nsm * (per_sm > 0 ? per_sm : 1);
+  if (grid > need)
+    grid = need;
+  k_predictor_stiff<L, ND, BATCH><<<(int)grid, BS, smem, st>>>(qh, wh, ncb, mask, status, dt,
+                                                                dt_dev, idx, idy, P, C, B);
+  return cuda_rc();
+}
+
+}  // namespace host
+}  // namespace gpr

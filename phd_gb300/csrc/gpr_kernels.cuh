@@ -9,8 +9,6 @@ namespace gpr {
 
 constexpr double LAMS = 1.0;       // WENO side-stencil weight (options.h:24)
 constexpr double WENO_EPS = 1e-14; // options.h:26
-constexpr double DG_TOL = 6e-6;    // options.h:30
-constexpr int DG_IT = 50;          // options.h:29
 
 template <bool TH, int LS> struct Layout {
   static constexpr bool THERMAL = TH;
@@ -242,7 +240,7 @@ __global__ void k_weno2d_y(double *__restrict__ wh, const double *__restrict__ u
 // the DG_U^-1 time coupling need the partner nodes' values, exchanged with
 // warp shuffles (partners differ in one index: lane ^ bit).  Each iteration
 // is the reference's Picard update q <- DG_U^-1 (Ww + dt R(q)) with its
-// per-cell stopping rule |q1 - q0| <= DG_TOL (1 + |q0|) (dg1.cpp:108-127).
+// per-cell stopping rule |q1 - q0| <= dg_tol (1 + |q0|) (dg1.cpp:108-127).
 
 template <int V>
 GPR_D void shfl_vec(const double *src, double *dst, int lanemask) {
@@ -380,7 +378,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   bool done = !active;
   int iters = 0;
   bool nan_seen = false;
-  const int maxit = stiff ? 0 : DG_IT;
+  const int maxit = stiff ? 0 : C.dg_it;
   // Divergence detection: a cell whose largest update has grown 1e8 times
   // above the smallest it reached is diverging and goes to the stiff-source
   // Newton pass at once instead of spending the rest of the iteration cap.
@@ -398,7 +396,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double dd = fabs(qn[k] - q[k]);
-      if (dd > DG_TOL * (1.0 + fabs(q[k])))
+      if (dd > C.dg_tol * (1.0 + fabs(q[k])))
         big = true;
       if (qn[k] != qn[k])
         hasnan = true;
@@ -470,8 +468,6 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
 // DG_MAT: an 18x18 system for A and a 6x6 system for rho J, assembled in
 // shared memory by the node's two lanes and solved by one lane each
 // (partial pivoting); the other variables use DG_MAT^-1 directly.
-constexpr double STIFF_TOL = 1e-11;  // on the Newton update, relative
-constexpr int STIFF_IT = 60;
 
 template <bool TH>
 GPR_D void stiff_jacobian_rows(const double *q, const Prim<TH> &s, const DevPar &P, double a,
@@ -657,7 +653,7 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
     bool done = !active;
     bool ok = false;
     int iters = 0;
-    for (int it = 0; it < STIFF_IT; it++) {
+    for (int it = 0; it < C.stiff_it; it++) {
       if (__all_sync(0xffffffffu, done))
         break;
       dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
@@ -719,7 +715,7 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
 #pragma unroll
       for (int k = 0; k < V; k++) {
         double qn = q[k] + delta[k];
-        if (fabs(delta[k]) > STIFF_TOL * (1.0 + fabs(qn)))
+        if (fabs(delta[k]) > C.stiff_tol * (1.0 + fabs(qn)))
           big = true;
         if (qn != qn)
           bad = true;
@@ -1083,7 +1079,7 @@ __global__ void __launch_bounds__(256) k_cfl_max(const double *__restrict__ u, l
   }
 }
 
-__global__ void k_cfl_finalize(const unsigned long long *__restrict__ mx, double cfl, double t,
+static __global__ void k_cfl_finalize(const unsigned long long *__restrict__ mx, double cfl, double t,
                                double tf, int count, double *__restrict__ dt_out) {
   double MAX = __longlong_as_double((long long)*mx);
   double dt = cfl / MAX;
@@ -1097,7 +1093,7 @@ __global__ void k_cfl_finalize(const unsigned long long *__restrict__ mx, double
 // Device clock of the device-resident time loop: [t, dt, tf, cfl, count].
 // The CFL finalize reads t/count and writes dt (0 once t >= tf); the advance
 // kernel adds dt to t and counts the step.
-__global__ void k_clock_finalize(const unsigned long long *__restrict__ mx,
+static __global__ void k_clock_finalize(const unsigned long long *__restrict__ mx,
                                  double *__restrict__ clk) {
   double t = clk[0], tf = clk[2], cfl = clk[3];
   long count = (long)clk[4];
@@ -1113,7 +1109,7 @@ __global__ void k_clock_finalize(const unsigned long long *__restrict__ mx,
   clk[1] = dt;
 }
 
-__global__ void k_clock_advance(double *__restrict__ clk) {
+static __global__ void k_clock_advance(double *__restrict__ clk) {
   if (clk[1] > 0.0) {
     clk[0] += clk[1];
     clk[4] += 1.0;
@@ -1212,7 +1208,7 @@ __global__ void __launch_bounds__(256) k_b_cfl_max(const double *__restrict__ u,
 }
 
 // per-instance dt (iterator.cpp:148-177 per instance) and the step counter
-__global__ void k_b_clock_finalize(unsigned long long *__restrict__ mx, Batch B) {
+static __global__ void k_b_clock_finalize(unsigned long long *__restrict__ mx, Batch B) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= B.ninst)
     return;
@@ -1254,7 +1250,7 @@ __global__ void k_b_renorm(double *__restrict__ u, long ncell, Batch B) {
   }
 }
 
-__global__ void k_b_clock_advance(Batch B, unsigned long long *__restrict__ updates) {
+static __global__ void k_b_clock_advance(Batch B, unsigned long long *__restrict__ updates) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= B.ninst)
     return;
