@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--cfl", type=float, default=0.4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
     return ap.parse_args()
@@ -382,6 +383,12 @@ def run_gb300(args):
             batched = batched_bench(torch)
         except Exception as ex:
             batched = {"error": str(ex)}
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        try:
+            adjoint = adjoint_bench(torch)
+        except Exception as ex:  # reported, not fatal to the main line
+            adjoint = {"error": str(ex)}
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -407,6 +414,7 @@ def run_gb300(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ncell * V * 8,
                     "d2h_bytes_per_step": ncell * V * 8},
             "batched": batched,
+            "adjoint": adjoint,
             "gpu_launches": 14 * args.steps,
             "clocks": cs.summary()}
     if peak_err:
@@ -419,6 +427,96 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def adjoint_bench(torch, fd_check=True):
+    """Differentiation form on the first Stokes problem (400 cells on
+    [-1, 1], t_end = 1.0, CFL 0.8, checkpoints every 32 steps): misfit of
+    v_y against the run at the true parameters (mu, cs, calpha) =
+    (1e-2, 1, 1), gradient at (1.2e-2, 0.9, 1.1) with respect to the
+    parameters and the 400 x 17 initial state.  Times the forward pass and
+    the backward pass (segment recompute + backward steps) with CUDA events,
+    reports their ratio per step, and the largest relative error of the
+    parameter gradient against central differences (h = 1e-6) of the same
+    forward.  The same for 64 instances with parameters perturbed by up to
+    10%, in one batched loop."""
+    import phd_gb300 as G
+    from phd_gb300.adjoint import Problem, solve
+    from phd_gb300.params import material_params
+
+    def make_par(th):
+        return material_params("sg", 1.0, cv=1.0, gamma=1.4, b0=th[1], calpha=th[2], mu=th[0],
+                               Pr=0.75)
+
+    nx, tf = 400, 1.0
+    u0, _, _, dX, _ = G.problems.stokes(nx=nx, mu=1e-2, cs=1.0, calpha=1.0, tf=tf)
+    dx = dX[0]
+    theta = np.array([1.2e-2, 0.9, 1.1])
+    out = {}
+    for ninst in (1, 64):
+        rng = np.random.default_rng(20261203)
+        th = theta[None, :] * (1.0 + (0.1 * rng.uniform(-1, 1, (ninst, 3)) if ninst > 1 else 0.0))
+        u0p = np.tile(u0, (ninst, 1))
+        Pt = Problem([nx] * ninst, [dx] * ninst, "transitive", make_par, cfl=0.8, tf=tf)
+        uT = Pt.forward(torch.tensor(u0p, device="cuda"),
+                        [make_par(np.array([1e-2, 1.0, 1.0]))] * ninst)
+        target = (uT[:, 3] / uT[:, 0]).clone()
+
+        def loss(uN):
+            return 0.5 * torch.sum((uN[:, 3] / uN[:, 0] - target) ** 2)
+
+        prob = Problem([nx] * ninst, [dx] * ninst, "transitive", make_par, cfl=0.8, tf=tf)
+        pars = [make_par(th[k]) for k in range(ninst)]
+        # warm-up (builds, allocates the tapes)
+        uN = prob.forward(torch.tensor(u0p, device="cuda"), pars).clone().requires_grad_(True)
+        loss(uN).backward()
+        prob.backward(uN.grad)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record()
+        uN = prob.forward(torch.tensor(u0p, device="cuda"), pars)
+        e[1].record()
+        uN = uN.clone().requires_grad_(True)
+        loss(uN).backward()
+        ub0, fb = prob.backward(uN.grad)
+        e[2].record()
+        torch.cuda.synchronize()
+        fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        nsteps = prob.nsteps
+        # the plain forward (reference stopping rule 6e-6) for comparison
+        plain = Problem([nx] * ninst, [dx] * ninst, "transitive", make_par, cfl=0.8, tf=tf,
+                        dg_tol=6e-6, dg_it=50)
+        plain.forward(torch.tensor(u0p, device="cuda"), pars)
+        torch.cuda.synchronize()
+        e[0].record()
+        plain.forward(torch.tensor(u0p, device="cuda"), pars)
+        e[1].record()
+        torch.cuda.synchronize()
+        fwd_plain = e[0].elapsed_time(e[1])
+        r = {"instances": ninst, "cells": nx * ninst, "steps": nsteps,
+             "forward_ms_per_step": fwd / nsteps, "backward_ms_per_step": bwd / nsteps,
+             "adjoint_over_forward": bwd / fwd,
+             "plain_forward_ms_per_step": fwd_plain / plain.nsteps,
+             "adjoint_over_plain_forward": (bwd / nsteps) / (fwd_plain / plain.nsteps),
+             "cell_updates_per_s_forward": nx * ninst * nsteps / (fwd * 1e-3)}
+        if fd_check and ninst == 1:
+            g = prob.theta_grad(fb, th)[0]
+            errs = []
+            for j in range(3):
+                h = 1e-6 * theta[j]
+                Ls = []
+                for s in (1, -1):
+                    t2 = theta.copy()
+                    t2[j] += s * h
+                    P2 = Problem([nx], [dx], "transitive", make_par, cfl=0.8, tf=tf)
+                    Ls.append(float(loss(P2.forward(torch.tensor(u0p, device="cuda"),
+                                                    [make_par(t2)]))))
+                fd = (Ls[0] - Ls[1]) / (2 * h)
+                errs.append(abs(g[j] - fd) / abs(fd))
+            r["grad_wrt_mu_cs_calpha"] = [float(x) for x in g]
+            r["grad_rel_err_vs_fd_h1e-6"] = max(errs)
+        out["stokes_%d" % ninst] = r
+    return out
 
 
 def batched_bench(torch, steps=10, plain_steps=2, count=512):

@@ -16,7 +16,7 @@ namespace {
 // the state before renormalisation, the step's clock {t, dt, tf, cfl, count}
 // per instance, {clipped, argmax cell} per instance, and the argmax scratch.
 struct TapeLayout {
-  long o_un, o_qh, o_up, o_clk, o_aux, o_amax, total;
+  long o_un, o_qh, o_up, o_clk, o_aux, o_amax, o_mcell, total;
 };
 
 TapeLayout tape_layout_v(int ninst, const int32_t *nx, int V) {
@@ -29,6 +29,7 @@ TapeLayout tape_layout_v(int ninst, const int32_t *nx, int V) {
   t.o_clk = cv.take(5L * ninst);
   t.o_aux = cv.take(2L * ninst);
   t.o_amax = cv.take((ninst + 1) / 2);
+  t.o_mcell = cv.take(b.nu);
   t.total = cv.o;
   return t;
 }
@@ -37,7 +38,7 @@ TapeLayout tape_layout_v(int ninst, const int32_t *nx, int V) {
 // (F, lambda), lambda at the ends, cotangents of qh and wh, stencil
 // cotangents, per-cell material-field and dt partial sums.
 struct AdjLayout {
-  long o_jn, o_je, o_ev, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
+  long o_jn, o_je, o_ev, o_eig, o_dots, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
 };
 
 AdjLayout adj_layout_v(int ninst, const int32_t *nx, int V) {
@@ -47,7 +48,10 @@ AdjLayout adj_layout_v(int ninst, const int32_t *nx, int V) {
   AdjLayout a;
   a.o_jn = cv.take(b.nb * 4 * K * 2 * V);
   a.o_je = cv.take(b.nb * 4 * K * (V + 1));
-  a.o_ev = cv.take(b.nb * 4);
+  // lambda and eigen data at the cell ends, then at the CFL argmax states
+  a.o_ev = cv.take(b.nb * 4 + ninst);
+  a.o_eig = cv.take((b.nb * 4 + ninst) * 17);
+  a.o_dots = cv.take(b.nb * 2 * 4 * K);
   a.o_qb = cv.take(b.nb * 4 * V);
   a.o_wb = cv.take(b.nb * 2 * V);
   a.o_g = cv.take(b.nb * V * 3);
@@ -91,9 +95,10 @@ template <class L> struct Adj {
         return GPR_E_CUDA;
     }
     DevPar P0{};
-    k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B);
+    double *mcell = tape ? tape + tl.o_mcell : nullptr;
+    k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B, mcell);
     if (tape)
-      k_adj_argmax<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, amax, B);
+      k_adj_argmax<<<blocks(b.nu, 256), 256, 0, st>>>(mcell, b.nu, mx, amax, B);
     k_adj_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B, dt_io, dt_mode, tclk, aux,
                                                              amax);
     k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
@@ -128,23 +133,30 @@ template <class L> struct Adj {
     const double *un = tape + tl.o_un, *qh = tape + tl.o_qh, *up = tape + tl.o_up,
                  *aux = tape + tl.o_aux;
     double *JN = ascr + al.o_jn, *JE = ascr + al.o_je, *EV = ascr + al.o_ev,
+           *EIG = ascr + al.o_eig, *EVs = EV + b.nb * 4,
+           *EIGs = EIG + b.nb * 4 * Xi<L::THERMAL>::ND, *DOT = ascr + al.o_dots,
            *qb = ascr + al.o_qb, *wb = ascr + al.o_wb, *g = ascr + al.o_g,
            *thf = ascr + al.o_thf, *thp = ascr + al.o_thp, *dtf = ascr + al.o_dtf,
            *dtp = ascr + al.o_dtp, *mu = ascr + al.o_mu;
     int32_t *need = (int32_t *)(ascr + al.o_need);
     k_adj_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(ubar, up, b.nu, B);
-    k_adj_jac<L><<<blocks(b.nb * 8 * K, 128), 128, 0, st>>>(qh, b.nb, JN, JE, EV, C, B);
-    k_adj_fv<L><<<blocks(b.nb * 2, 128), 128, 0, st>>>(ubar, qh, JN, JE, EV, un, up, b.nb, qb,
-                                                        thf, dtf, C, B);
-    k_adj_pred_iter<L><<<blocks(b.nb * 4, 128), 128, 0, st>>>(qh, qb, JN, b.nb, mu, need, C,
-                                                               B);
+    k_adj_eig<L><<<blocks(b.nb * 4 + ninst, 128), 128, 0, st>>>(qh, b.nb, un, aux, EV, EIG, C,
+                                                                  B);
+    k_adj_jac_nodes<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, JN, B);
+    k_adj_jac_ends<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, JE, EIG, C, B);
+    k_adj_fv_dots<L><<<blocks(b.nb * 2 * K, 128), 128, 0, st>>>(ubar, qh, JN, JE, EV, b.nb, DOT,
+                                                                 C, B);
+    k_adj_fv<L><<<blocks(b.nb * 2, 128), 128, 0, st>>>(ubar, qh, DOT, EV, un, up, b.nb, qb, thf,
+                                                        dtf, C, B);
+    k_adj_pred_iter<L><<<blocks(b.nb, ADJ_CPB), 32 * ADJ_CPB, 0, st>>>(qh, qb, JN, b.nb, mu,
+                                                                      need, C, B);
     k_adj_pred_dense<L><<<(unsigned)b.nb, 128, 0, st>>>(qh, qb, JN, b.nb, need, mu, info, C, B);
     k_adj_pred_post<L><<<blocks(b.nb * 4, 128), 128, 0, st>>>(qh, mu, JN, b.nb, wb, thp, dtp, C,
                                                                B);
     k_adj_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wb, un, b.nb, g, C, B);
     k_adj_gather<V><<<blocks(b.nu * V, 256), 256, 0, st>>>(ubar, g, b.nu, B);
-    k_adj_reduce<L><<<ninst, 128, 0, st>>>(ubar, thbar, tbar, thf, thp, dtf, dtp, un, aux,
-                                           frozen, B);
+    k_adj_reduce<L><<<ninst, 128, 0, st>>>(ubar, thbar, tbar, thf, thp, dtf, dtp, un, aux, EVs,
+                                           EIGs, frozen, B);
     return cuda_rc();
   }
 

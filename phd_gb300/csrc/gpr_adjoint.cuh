@@ -249,8 +249,14 @@ template <> GPR_D void adjugate<4>(const double (&M)[4][4], double (&adj)[4][4])
 // lambda_x(Q) = |v_x| + sqrt(max eig(Xi1 Xi2)) (system/eig.cpp:8-77), the
 // restatement of max_abs_eigs for EOS 0 and beta = 0.  The value of the
 // dominant eigenvalue comes from the same solver as the forward step.
+template <bool TH> struct Xi {
+  static constexpr int m = TH ? 4 : 3;
+  static constexpr int ND = m * m + 1;  // eigen data: l2, then Y (m x m)
+};
+
 template <bool TH>
-GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
+GPR_D void dxi0(const Dual *q, const DPrim<TH> &s, const DPar &P, Dual (&X)[Xi<TH>::m][Xi<TH>::m]) {
+  constexpr int m = Xi<TH>::m;
   const Dual *A = q + 5;
   Dual Gd[3];
 #pragma unroll
@@ -274,8 +280,6 @@ GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
   Dual c02 = (s.p * (s.ir * s.ir) - dedr) * rG;
   Dual b[3] = {sg[0] - s.r * dsr[0], sg[1] - s.r * dsr[1], sg[2] - s.r * dsr[2]};
   b[0] = b[0] + s.r * c02;
-  constexpr int m = TH ? 4 : 3;
-  Dual X[m][m];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -287,7 +291,7 @@ GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
         acc = acc + b[c] * s.ir;
       X[i][c] = acc;
     }
-  if (TH) {
+  if constexpr (TH) {
     Dual h = P.calpha2 * s.T * s.G;
     Dual tp = s.ir * s.irG * P.icv;
     Dual dTr = -(dnum * irG2 * P.icv);
@@ -299,31 +303,66 @@ GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
     X[m - 1][2] = tp * b[2];
     X[m - 1][m - 1] = tp * h;
   }
-  double Xv[m][m];
+}
+
+// Eigen data of the dominant eigenvalue l2 of X: eig[0] = l2,
+// eig[1 + i m + j] = Y[i][j] with d l2 = sum_ij Y[i][j] dX[i][j],
+// Y = adj(l2 I - X)^T / tr(adj(l2 I - X)).
+template <int m> GPR_D void xi_eigdata(const double (&Xv)[m][m], double *eig) {
+  double Xc[m][m];
 #pragma unroll
   for (int i = 0; i < m; i++)
 #pragma unroll
     for (int j = 0; j < m; j++)
-      Xv[i][j] = X[i][j].v;
+      Xc[i][j] = Xv[i][j];
   double l2;
-  if (!max_eig_laguerre<m>(Xv, l2))
-    l2 = max_abs_eig<m>(Xv);
+  if (!max_eig_laguerre<m>(Xc, l2))
+    l2 = max_abs_eig<m>(Xc);
   double M[m][m], adj[m][m];
 #pragma unroll
   for (int i = 0; i < m; i++)
 #pragma unroll
     for (int j = 0; j < m; j++)
-      M[i][j] = (i == j ? l2 : 0.0) - X[i][j].v;
+      M[i][j] = (i == j ? l2 : 0.0) - Xv[i][j];
   adjugate<m>(M, adj);
-  double num = 0.0, den = 0.0;
+  double den = 0.0;
 #pragma unroll
-  for (int i = 0; i < m; i++) {
+  for (int i = 0; i < m; i++)
     den += adj[i][i];
+  double iden = 1.0 / den;
+  eig[0] = l2;
+#pragma unroll
+  for (int i = 0; i < m; i++)
 #pragma unroll
     for (int j = 0; j < m; j++)
-      num += adj[j][i] * X[i][j].d;
+      eig[1 + i * m + j] = adj[j][i] * iden;
+}
+
+// lambda with its tangent; eig: eigen data of X (computed here when null)
+template <bool TH>
+GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P,
+                    const double *eig = nullptr) {
+  constexpr int m = Xi<TH>::m;
+  Dual X[m][m];
+  dxi0<TH>(q, s, P, X);
+  double loc[Xi<TH>::ND];
+  if (!eig) {
+    double Xv[m][m];
+#pragma unroll
+    for (int i = 0; i < m; i++)
+#pragma unroll
+      for (int j = 0; j < m; j++)
+        Xv[i][j] = X[i][j].v;
+    xi_eigdata<m>(Xv, loc);
+    eig = loc;
   }
-  Dual lam = dsqrt(Dual{l2, num / den});
+  double dl2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      dl2 += eig[1 + i * m + j] * X[i][j].d;
+  Dual lam = dsqrt(Dual{eig[0], dl2});
   Dual v0 = s.v[0];
   return v0.v > 0 ? v0 + lam : lam - v0;
 }
@@ -332,7 +371,7 @@ GPR_D Dual dlambda0(const Dual *q, const DPrim<TH> &s, const DPar &P) {
 // variable k, k >= V seeds material field k - V.
 template <class L>
 GPR_D void point_tangent(const double *qp, int k, const DevPar &P, Dual *F, Dual *S,
-                         Dual *lam) {
+                         Dual *lam, const double *eig = nullptr) {
   constexpr int V = L::V;
   Dual q[V];
 #pragma unroll
@@ -346,7 +385,7 @@ GPR_D void point_tangent(const double *qp, int k, const DevPar &P, Dual *F, Dual
   if (S)
     dsource<L::THERMAL, V>(q, s, D, S);
   if (lam)
-    *lam = dlambda0<L::THERMAL>(q, s, D);
+    *lam = dlambda0<L::THERMAL>(q, s, D, eig);
 }
 
 // ---------------------------------------------------------------------------
@@ -412,24 +451,15 @@ GPR_D double bc_sign(int code, int k) {
 // Forward-step recording.
 
 // argmax cell of the CFL maximum (smallest packed index among the cells that
-// attain it), after k_b_cfl_max has written the per-instance maximum
-template <class L>
-__global__ void __launch_bounds__(256) k_adj_argmax(const double *__restrict__ u, long ncell,
+// attain it), from the per-cell values k_b_cfl_max stored
+static __global__ void __launch_bounds__(256) k_adj_argmax(const double *__restrict__ mcell, long ncell,
                                                     const unsigned long long *__restrict__ mx,
                                                     unsigned int *__restrict__ amax, Batch B) {
-  constexpr int V = L::V;
   long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= ncell)
     return;
   int inst = B.inst_u[c];
-  const DevPar &P = B.P[inst];
-  double q[V];
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    q[k] = u[c * V + k];
-  Prim<L::THERMAL> s;
-  prim<L::THERMAL>(q, P, s);
-  double m = max_abs_eigs<L::THERMAL>(q, s, 0, P) * B.idx[inst];
+  double m = mcell[c];
   if (m > 0.0 && (unsigned long long)__double_as_longlong(m) == mx[inst])
     atomicMin(amax + inst, (unsigned int)c);
 }
@@ -523,100 +553,162 @@ __global__ void k_adj_renorm(double *__restrict__ ub, const double *__restrict__
   g[0] += s * f / (3.0 * r);
 }
 
-// Jacobian columns at the 8 evaluation points of every predictor cell:
-// e = 0..3 the space-time nodes (t = e/2, s = e%2): F and S;
-// e = 4..7 the cell ends (t = (e-4)/2, side = (e-4)%2, side 0 = x = 0): F
-// and lambda (with the lambda value for the Rusanov switch in EV).
-// JN[((c*4 + e)*K + k)*2V + o], JE[((c*4 + e-4)*K + k)*(V+1) + o].
+// Cell-end states qL / qR of predictor cell c at time node t (side 0:
+// x = 0, side 1: x = 1), the same expressions as k_faces1d.
+template <int V>
+GPR_D void end_state(const double *qh, long c, int t, int side, const Consts &C, double *qp) {
+  const double *q0 = qh + (c * 4 + 2 * t) * V;
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    qp[j] = C.endv[side][0] * q0[j] + C.endv[side][1] * q0[V + j];
+}
+
+// Per cell end (4 per predictor cell, e = 2t + side): lambda (EV, the value
+// the forward's Rusanov switch compared) and the eigen data of the acoustic
+// tensor (EIG), shared by the end's tangent threads.
+// Points nb*4 .. nb*4 + ninst - 1: the state entering the step at each
+// instance's CFL argmax cell (for the derivative of dt).
 template <class L>
-__global__ void __launch_bounds__(128) k_adj_jac(const double *__restrict__ qh, long nb,
-                                                 double *__restrict__ JN, double *__restrict__ JE,
-                                                 double *__restrict__ EV, Consts C, Batch B) {
+__global__ void __launch_bounds__(128) k_adj_eig(const double *__restrict__ qh, long nb,
+                                                 const double *__restrict__ un,
+                                                 const double *__restrict__ aux,
+                                                 double *__restrict__ EV,
+                                                 double *__restrict__ EIG, Consts C, Batch B) {
+  constexpr int V = L::V, m = Xi<L::THERMAL>::m, ND = Xi<L::THERMAL>::ND;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= nb * 4 + B.ninst)
+    return;
+  double qp[V];
+  int inst;
+  if (gid < nb * 4) {
+    long c = gid / 4;
+    int e = gid % 4;
+    inst = B.inst_b[c];
+    if (B.clk[5 * inst + 1] == 0.0)
+      return;
+    end_state<V>(qh, c, e / 2, e % 2, C, qp);
+  } else {
+    inst = (int)(gid - nb * 4);
+    long cs = (long)aux[2 * inst + 1];
+    if (B.clk[5 * inst + 1] == 0.0 || cs < 0)
+      return;
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      qp[j] = un[cs * V + j];
+  }
+  const DevPar &P = B.P[inst];
+  Prim<L::THERMAL> sp;
+  prim<L::THERMAL>(qp, P, sp);
+  EV[gid] = max_abs_eigs<L::THERMAL>(qp, sp, 0, P);
+  Dual q[V];
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    q[j] = Dual{qp[j], 0.0};
+  DPar D = dpar_seed(P, -1);
+  DPrim<L::THERMAL> s;
+  dprim<L::THERMAL>(q, D, s);
+  Dual X[m][m];
+  dxi0<L::THERMAL>(q, s, D, X);
+  double Xv[m][m];
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      Xv[i][j] = X[i][j].v;
+  xi_eigdata<m>(Xv, EIG + gid * ND);
+}
+
+// Jacobian columns at the 4 space-time nodes of every predictor cell
+// (e = 2t + s): F and S, JN[((c*4 + e)*K + k)*2V + o].
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_jac_nodes(const double *__restrict__ qh, long nb,
+                                                       double *__restrict__ JN, Batch B) {
   constexpr int V = L::V, K = V + NPD;
   long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (gid >= nb * 8 * K)
+  if (gid >= nb * 4 * K)
     return;
   int k = gid % K;
-  long rest = gid / K;
-  int e = rest % 8;
-  long c = rest / 8;
+  long pt = gid / K;  // c*4 + e
+  long c = pt / 4;
   int inst = B.inst_b[c];
   if (B.clk[5 * inst + 1] == 0.0)
     return;
-  const DevPar &P = B.P[inst];
   double qp[V];
-  if (e < 4) {
-    const double *src = qh + (c * 4 + e) * V;
+  const double *src = qh + pt * V;
 #pragma unroll
-    for (int j = 0; j < V; j++)
-      qp[j] = src[j];
-  } else {
-    int t = (e - 4) / 2, side = (e - 4) % 2;
-    const double *q0 = qh + (c * 4 + 2 * t) * V;
+  for (int j = 0; j < V; j++)
+    qp[j] = src[j];
+  Dual F[V], S[V];
+  point_tangent<L>(qp, k, B.P[inst], F, S, nullptr);
+  double *o = JN + (pt * K + k) * 2 * V;
 #pragma unroll
-    for (int j = 0; j < V; j++)
-      qp[j] = C.endv[side][0] * q0[j] + C.endv[side][1] * q0[V + j];
+  for (int j = 0; j < V; j++) {
+    o[j] = F[j].d;
+    o[V + j] = S[j].d;
   }
-  Dual F[V];
-  if (e < 4) {
-    Dual S[V];
-    point_tangent<L>(qp, k, P, F, S, nullptr);
-    double *o = JN + ((c * 4 + e) * K + k) * 2 * V;
+}
+
+// Jacobian columns at the 4 cell ends (e = 2t + side): F and lambda,
+// JE[((c*4 + e)*K + k)*(V+1) + o].
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_jac_ends(const double *__restrict__ qh, long nb,
+                                                      double *__restrict__ JE,
+                                                      const double *__restrict__ EIG, Consts C,
+                                                      Batch B) {
+  constexpr int V = L::V, K = V + NPD, ND = Xi<L::THERMAL>::ND;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= nb * 4 * K)
+    return;
+  int k = gid % K;
+  long pt = gid / K;
+  long c = pt / 4;
+  int e = (int)(pt % 4);
+  int inst = B.inst_b[c];
+  if (B.clk[5 * inst + 1] == 0.0)
+    return;
+  double qp[V];
+  end_state<V>(qh, c, e / 2, e % 2, C, qp);
+  Dual F[V], lam;
+  point_tangent<L>(qp, k, B.P[inst], F, nullptr, &lam, EIG + pt * ND);
+  double *o = JE + (pt * K + k) * (V + 1);
 #pragma unroll
-    for (int j = 0; j < V; j++) {
-      o[j] = F[j].d;
-      o[V + j] = S[j].d;
-    }
-  } else {
-    Dual lam;
-    point_tangent<L>(qp, k, P, F, nullptr, &lam);
-    double *o = JE + ((c * 4 + e - 4) * K + k) * (V + 1);
-#pragma unroll
-    for (int j = 0; j < V; j++)
-      o[j] = F[j].d;
-    o[V] = lam.d;
-    if (k == 0) {
-      Prim<L::THERMAL> sp;
-      prim<L::THERMAL>(qp, P, sp);
-      EV[c * 4 + e - 4] = max_abs_eigs<L::THERMAL>(qp, sp, 0, P);
-    }
-  }
+  for (int j = 0; j < V; j++)
+    o[j] = F[j].d;
+  o[V] = lam.d;
 }
 
 // One face's contribution to the cotangent of the state on one side.
 // Face flux f = max(lamL, lamR)(qL - qR) + F(qL) + F(qR) (fluxes.cpp:66-75),
 // path integral b = sum_n w_n B(qL + x_n dq) dq (fluxes.cpp:9-20); the left
 // cell receives -kk (b + f), the right -kk (b - f) (fv.cpp:143-146).
-template <int V, int K>
-GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR,
-                    const double *ubL, const double *ubR, double kk, bool mineL,
-                    const double *Jm, const Consts &C, double *qb, double *thb) {
-  double Fb[V], Bb[V];
+// Face cotangents (fb, bb) of the flux and path-integral terms from the
+// cotangents of the two cells the face updates.
+template <int V>
+GPR_D void face_cot(const double *ubL, const double *ubR, double kk, double *Fb, double *Bb) {
 #pragma unroll
   for (int k = 0; k < V; k++) {
     double a = ubL ? ubL[k] : 0.0, b = ubR ? ubR[k] : 0.0;
     Fb[k] = -kk * (a - b);
     Bb[k] = -kk * (a + b);
   }
+}
+
+// dJ[j] = sum_o dF_o/dq_j Fb_o (+ sbar dlambda/dq_j on the max side): the
+// Jacobian part, from k_adj_fv_dots.
+template <int V, int K>
+GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR,
+                    const double *ubL, const double *ubR, double kk, bool mineL,
+                    const double *dJ, const Consts &C, double *qb, double *thb) {
+  double Fb[V], Bb[V];
+  face_cot<V>(ubL, ubR, kk, Fb, Bb);
   bool Lmax = lamL > lamR;  // std::max(m1, m2) picks m2 on ties
   double sm = Lmax ? lamL : lamR;
-  double sbar = 0.0;
 #pragma unroll
-  for (int k = 0; k < V; k++)
-    sbar += Fb[k] * (ql[k] - qr[k]);
-  bool mine_max = mineL ? Lmax : !Lmax;
   for (int j = 0; j < K; j++) {
-    const double *col = Jm + j * (V + 1);
-    double acc = 0.0;
-#pragma unroll
-    for (int o = 0; o < V; o++)
-      acc += col[o] * Fb[o];
-    if (mine_max)
-      acc += sbar * col[V];
     if (j < V)
-      qb[j] += acc;
+      qb[j] += dJ[j];
     else
-      thb[j - V] += acc;
+      thb[j - V] += dJ[j];
   }
   double sgn = mineL ? sm : -sm;
 #pragma unroll
@@ -657,10 +749,83 @@ GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR
 // volume term), one thread per (predictor cell, time node).  Also the
 // material-field cotangents (thf) and <ubar, u' - u> / dt (dtf) since the FV
 // increment is linear in dt.
+//
+// k_adj_fv_dots first forms the Jacobian dot products, one thread per
+// (predictor cell, time node, Jacobian column j): D[(c*2 + t)*4 + r][j] for
+// r = 0 the face on the right of the cell (cell on its left), r = 1 the face
+// on its left, r = 2, 3 the volume term's S at spatial nodes 0, 1.
+template <class L>
+__global__ void __launch_bounds__(128) k_adj_fv_dots(
+    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ JN,
+    const double *__restrict__ JE, const double *__restrict__ EV, long nb,
+    double *__restrict__ D, Consts C, Batch B) {
+  constexpr int V = L::V, K = V + NPD;
+  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (gid >= nb * 2 * K)
+    return;
+  const int j = gid % K;
+  const long ct = gid / K;
+  const long c = ct / 2;
+  const int t = (int)(ct % 2);
+  const int inst = B.inst_b[c];
+  const double dt = B.clk[5 * inst + 1];
+  double d[4] = {0.0, 0.0, 0.0, 0.0};
+  if (dt != 0.0) {
+    const int li = (int)(c - B.off_b[inst]), nx = B.nx[inst];
+    const double kk = (dt * C.w[t]) / (2.0 * (1.0 / B.idx[inst]));
+    const double *ubi = ubar + (long)B.off_u[inst] * V;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      // r = 0: face li (this cell on the left); r = 1: face li - 1
+      if (r == 0 ? li > nx : li < 1)
+        continue;
+      const int f = r == 0 ? li : li - 1;
+      const long cl = r == 0 ? c : c - 1;
+      const double *qa = qh + (cl * 4 + 2 * t) * V, *qb2 = qh + ((cl + 1) * 4 + 2 * t) * V;
+      double Fb[V], Bb[V];
+      face_cot<V>(f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
+                  kk, Fb, Bb);
+      double sbar = 0.0;
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        double ql = C.endv[1][0] * qa[k] + C.endv[1][1] * qa[V + k];
+        double qr = C.endv[0][0] * qb2[k] + C.endv[0][1] * qb2[V + k];
+        sbar += Fb[k] * (ql - qr);
+      }
+      const double lamL = EV[cl * 4 + 2 * t + 1], lamR = EV[(cl + 1) * 4 + 2 * t];
+      const bool Lmax = lamL > lamR;  // std::max(m1, m2) picks m2 on ties
+      const bool mine_max = r == 0 ? Lmax : !Lmax;
+      const double *col = JE + ((c * 4 + 2 * t + (r == 0 ? 1 : 0)) * K + j) * (V + 1);
+      double acc = 0.0;
+#pragma unroll
+      for (int o = 0; o < V; o++)
+        acc += col[o] * Fb[o];
+      if (mine_max)
+        acc += sbar * col[V];
+      d[r] = acc;
+    }
+    if (li >= 1 && li <= nx) {
+      const double *ubc = ubi + (long)(li - 1) * V;
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const double *col = JN + ((c * 4 + 2 * t + s) * K + j) * 2 * V + V;
+        double acc = 0.0;
+#pragma unroll
+        for (int o = 0; o < V; o++)
+          acc += col[o] * ubc[o];
+        d[2 + s] = acc;
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+    D[(ct * 4 + r) * K + j] = d[r];
+}
+
 template <class L>
 __global__ void __launch_bounds__(128) k_adj_fv(
-    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ JN,
-    const double *__restrict__ JE, const double *__restrict__ EV, const double *__restrict__ un,
+    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ D,
+    const double *__restrict__ EV, const double *__restrict__ un,
     const double *__restrict__ up, long nb, double *__restrict__ qbar, double *__restrict__ thf,
     double *__restrict__ dtf, Consts C, Batch B) {
   constexpr int V = L::V, K = V + NPD;
@@ -709,7 +874,7 @@ __global__ void __launch_bounds__(128) k_adj_fv(
     }
     face_adj<V, K>(ql, qr, EV[c * 4 + 2 * t + 1], EV[(c + 1) * 4 + 2 * t],
                    f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
-                   kk, true, JE + (c * 4 + 2 * t + 1) * K * (V + 1), C, qLb, th);
+                   kk, true, D + ((c * 2 + t) * 4 + 0) * K, C, qLb, th);
   }
   if (li >= 1) {  // face li - 1: this cell on the right
     int f = li - 1;
@@ -722,7 +887,7 @@ __global__ void __launch_bounds__(128) k_adj_fv(
     }
     face_adj<V, K>(ql, qr, EV[(c - 1) * 4 + 2 * t + 1], EV[c * 4 + 2 * t],
                    f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
-                   kk, false, JE + (c * 4 + 2 * t) * K * (V + 1), C, qRb, th);
+                   kk, false, D + ((c * 2 + t) * 4 + 1) * K, C, qRb, th);
   }
 #pragma unroll
   for (int m = 0; m < 2; m++)
@@ -736,17 +901,13 @@ __global__ void __launch_bounds__(128) k_adj_fv(
     for (int s = 0; s < 2; s++) {
       double a = (dt * C.w[t]) * C.w[s];
       const double *qs = qc + s * V, *qo = qc + (1 - s) * V;
-      const double *J = JN + (c * 4 + 2 * t + s) * K * 2 * V;
-      for (int j = 0; j < K; j++) {
-        const double *col = J + j * 2 * V + V;
-        double x = 0.0;
+      const double *dS = D + ((c * 2 + t) * 4 + 2 + s) * K;
 #pragma unroll
-        for (int o = 0; o < V; o++)
-          x += col[o] * ubc[o];
+      for (int j = 0; j < K; j++) {
         if (j < V)
-          acc[s][j] += a * x;
+          acc[s][j] += a * dS[j];
         else
-          th[j - V] += a * x;
+          th[j - V] += a * dS[j];
       }
       double yb[V], dq[V], xb[V];
       double ir = 1.0 / qs[0];
@@ -801,104 +962,142 @@ __global__ void __launch_bounds__(128) k_adj_fv(
 // stage 2 (k_adj_pred_dense, one block per cell); stage 3 (k_adj_pred_post)
 // forms the cotangents from mu.
 constexpr int ADJ_PRED_IT = 100;
-constexpr double ADJ_PRED_TOL = 1e-13;
+constexpr double ADJ_PRED_TOL = 1e-11;
+
+// One warp per cell: lane = 8 g + p serves node g (= 2t + i) and the entries
+// k = p, p + 8, p + 16 of its vectors; the node Jacobians (state columns)
+// are staged once in shared memory.
+constexpr int ADJ_CPB = 2;  // cells (warps) per block
 
 template <class L>
-__global__ void __launch_bounds__(128) k_adj_pred_iter(
+__global__ void __launch_bounds__(32 * ADJ_CPB) k_adj_pred_iter(
     const double *__restrict__ qh, const double *__restrict__ qbar, const double *__restrict__ JN,
     long nb, double *__restrict__ mu_buf, int32_t *__restrict__ need, Consts C, Batch B) {
   constexpr int V = L::V, K = V + NPD;
-  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int g = threadIdx.x % 4;
-  const long c = gt / 4;
+  __shared__ double Js[ADJ_CPB][4][2][V][V + 1];  // [cell][node][F, S][j][o] = d(F_o)/dq_j
+  __shared__ double sm_mu[ADJ_CPB][4][V], sm_y[ADJ_CPB][4][V], sm_xb[ADJ_CPB][4][V],
+      sm_z[ADJ_CPB][4][V], sm_x[ADJ_CPB][4][V], sm_v[ADJ_CPB][4][3];
+  const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const long c = (long)blockIdx.x * ADJ_CPB + w;
   const bool valid = c < nb;
   const long cc = valid ? c : 0;
-  const int t = g / 2, i = g % 2;
   const int inst = B.inst_b[cc];
   const double dt = B.clk[5 * inst + 1];
   const double idx = B.idx[inst];
   const bool active = valid && dt != 0.0;
-  double q[V], qb[V], mu[V], other[V], x[V];
-  const double *qs = qh + (cc * 4 + g) * V;
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    q[k] = qs[k];
-    qb[k] = active ? qbar[(cc * 4 + g) * V + k] : 0.0;
-    mu[k] = 0.0;
-  }
-  shfl_vec<V>(q, other, 1);
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    x[k] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * other[k]);
-  double ir = 1.0 / q[0];
-  double v[3] = {q[2] * ir, q[3] * ir, q[4] * ir};
-  const double *J = JN + (cc * 4 + g) * K * 2 * V;
-  const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx;
-  const double iws = 1.0 / C.w[i];
-  bool done = !active;
-  bool conv = !active;
-  for (int it = 0; it < ADJ_PRED_IT; it++) {
-    if (__all_sync(0xffffffffu, done))
-      break;
-    double xb[V], r[V], z[V], y[V], mun[V];
-#pragma unroll
-    for (int k = 0; k < V; k++) {
-      xb[k] = 0.0;
-      z[k] = -wn * mu[k];
+  const int g = lane / 8, p = lane % 8, t = g / 2, i = g % 2;
+  if (active) {
+    for (int e = lane; e < 4 * V * 2 * V; e += 32) {
+      int gg = e / (2 * V * V), rem = e % (2 * V * V);
+      int j = rem / (2 * V), o = rem % (2 * V);
+      Js[w][gg][o / V][j][o % V] = JN[((cc * 4 + gg) * K + j) * 2 * V + o];
     }
-    bdot0_xT<V>(v, z, xb);  // xb = -wn B^T mu
-    double vb[3];
-    bdot0_vT(x, z, vb);  // through v(q): -wn (d(B x)/dv)^T mu
-    shfl_vec<V>(mu, other, 1);
+  }
+  // node data: x_ti = idx sum_m DERVALS[i][m] q_tm, v = q[2..4] / q[0]
+  const double *qn = qh + (cc * 4 + g) * V, *qo = qh + (cc * 4 + (g ^ 1)) * V;
+  for (int k = p; k < V; k += 8) {
+    sm_x[w][g][k] = idx * (C.derv[i][i] * qn[k] + C.derv[i][1 - i] * qo[k]);
+    sm_mu[w][g][k] = 0.0;
+  }
+  if (p == 0) {
+    double ir = 1.0 / qn[0];
+    sm_v[w][g][0] = qn[2] * ir;
+    sm_v[w][g][1] = qn[3] * ir;
+    sm_v[w][g][2] = qn[4] * ir;
+  }
+  double qb[3];
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      y[k] = C.dgder[i][i] * mu[k] + C.dgder[1 - i][i] * other[k];
-    for (int j = 0; j < V; j++) {
-      const double *col = J + j * 2 * V;
+  for (int m = 0; m < 3; m++) {
+    int k = p + 8 * m;
+    qb[m] = (active && k < V) ? qbar[(cc * 4 + g) * V + k] : 0.0;
+  }
+  const double q0 = qn[0], iq0 = 1.0 / q0;
+  const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx, iws = 1.0 / C.w[i];
+  __syncwarp();
+  const double *v = sm_v[w][g];
+  bool conv = !active;
+  for (int it = 0; it < ADJ_PRED_IT && active; it++) {
+    // y = sum_i DG_DER[i][m] mu_i ; xb = -wn B^T mu
+    const double *mu = sm_mu[w][g], *mo = sm_mu[w][g ^ 1];
+    for (int k = p; k < V; k += 8) {
+      sm_y[w][g][k] = C.dgder[i][i] * mu[k] + C.dgder[1 - i][i] * mo[k];
+      double xb = 0.0;
+      if (k >= 5 && k < 14) {
+        int rr = (k - 5) / 3, cc3 = (k - 5) % 3;
+        if (cc3 == 1)
+          xb = -v[1] * mu[5 + 3 * rr] + v[0] * mu[6 + 3 * rr];
+        else if (cc3 == 2)
+          xb = -v[2] * mu[5 + 3 * rr] + v[0] * mu[7 + 3 * rr];
+      }
+      sm_xb[w][g][k] = -wn * xb;
+    }
+    __syncwarp();
+    // through v(q): vb = -wn (d(B x)/dv)^T mu
+    const double *x = sm_x[w][g];
+    double vb0 = 0.0, vb1 = 0.0, vb2 = 0.0;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      vb0 += x[6 + 3 * r] * mu[6 + 3 * r] + x[7 + 3 * r] * mu[7 + 3 * r];
+      vb1 -= x[6 + 3 * r] * mu[5 + 3 * r];
+      vb2 -= x[7 + 3 * r] * mu[5 + 3 * r];
+    }
+    vb0 *= -wn;
+    vb1 *= -wn;
+    vb2 *= -wn;
+    const double *y = sm_y[w][g], *xs = sm_xb[w][g], *xso = sm_xb[w][g ^ 1];
+    for (int j = p; j < V; j += 8) {
+      const double *JF = Js[w][g][0][j], *JS = Js[w][g][1][j];
       double sF = 0.0, sS = 0.0;
 #pragma unroll
       for (int o = 0; o < V; o++) {
-        sF += col[o] * y[o];
-        sS += col[V + o] * mu[o];
+        sF += JF[o] * y[o];
+        sS += JS[o] * mu[o];
       }
-      r[j] = wn * sS - wti * sF;
+      double r = wn * sS - wti * sF;
+      if (j == 0)
+        r -= (vb0 * v[0] + vb1 * v[1] + vb2 * v[2]) * iq0;
+      else if (j >= 2 && j < 5)
+        r += (j == 2 ? vb0 : (j == 3 ? vb1 : vb2)) * iq0;
+      r += idx * (C.derv[i][i] * xs[j] + C.derv[1 - i][i] * xso[j]);
+      sm_z[w][g][j] = qb[j / 8] + dt * r;
     }
-    vel_T(q, vb, r, 1.0);
-    shfl_vec<V>(xb, other, 1);
+    __syncwarp();
+    const double *z = sm_z[w][g], *zo = sm_z[w][g ^ 2];
+    double mun[3], dd = 0.0, sc = 0.0;
 #pragma unroll
-    for (int k = 0; k < V; k++) {
-      r[k] += idx * (C.derv[i][i] * xb[k] + C.derv[1 - i][i] * other[k]);
-      z[k] = qb[k] + dt * r[k];
-    }
-    shfl_vec<V>(z, other, 2);
-    double dd = 0.0, sc = 0.0;
-#pragma unroll
-    for (int k = 0; k < V; k++) {
-      mun[k] = (C.dgmatinv[t][t] * z[k] + C.dgmatinv[1 - t][t] * other[k]) * iws;
-      dd = fmax(dd, fabs(mun[k] - mu[k]));
-      sc = fmax(sc, fabs(mun[k]));
+    for (int m = 0; m < 3; m++) {
+      int k = p + 8 * m;
+      if (k < V) {
+        mun[m] = (C.dgmatinv[t][t] * z[k] + C.dgmatinv[1 - t][t] * zo[k]) * iws;
+        dd = fmax(dd, fabs(mun[m] - mu[k]));
+        sc = fmax(sc, fabs(mun[m]));
+      }
     }
 #pragma unroll
-    for (int o = 1; o < 4; o <<= 1) {
+    for (int o = 16; o > 0; o >>= 1) {
       dd = fmax(dd, __shfl_xor_sync(0xffffffffu, dd, o));
       sc = fmax(sc, __shfl_xor_sync(0xffffffffu, sc, o));
     }
-    if (!done) {
+    __syncwarp();
 #pragma unroll
-      for (int k = 0; k < V; k++)
-        mu[k] = mun[k];
-      if (dd <= ADJ_PRED_TOL * sc || !(sc == sc)) {
-        done = true;
-        conv = sc == sc;
-      }
+    for (int m = 0; m < 3; m++) {
+      int k = p + 8 * m;
+      if (k < V)
+        sm_mu[w][g][k] = mun[m];
+    }
+    __syncwarp();
+    if (!(sc == sc))
+      break;
+    if (dd <= ADJ_PRED_TOL * sc) {
+      conv = true;
+      break;
     }
   }
   if (!valid)
     return;
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    mu_buf[(c * 4 + g) * V + k] = mu[k];
-  if (g == 0)
+  for (int k = p; k < V; k += 8)
+    mu_buf[(c * 4 + g) * V + k] = sm_mu[w][g][k];
+  if (lane == 0)
     need[c] = conv ? 0 : 1;
 }
 
@@ -1264,8 +1463,8 @@ __global__ void __launch_bounds__(128) k_adj_reduce(
     double *__restrict__ ubar, double *__restrict__ thbar, double *__restrict__ tbar,
     const double *__restrict__ thf, const double *__restrict__ thp, const double *__restrict__ dtf,
     const double *__restrict__ dtp, const double *__restrict__ un, const double *__restrict__ aux,
-    int frozen, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
+    const double *__restrict__ EVs, const double *__restrict__ EIGs, int frozen, Batch B) {
+  constexpr int V = L::V, K = V + NPD, ND = Xi<L::THERMAL>::ND;
   const int inst = blockIdx.x;
   const double dt = B.clk[5 * inst + 1];
   if (dt == 0.0)
@@ -1309,14 +1508,7 @@ __global__ void __launch_bounds__(128) k_adj_reduce(
         tbar[inst] = -dtb;
       } else if (cstar >= 0) {
         double dtot = dtb + tbar[inst];
-        const DevPar &P = B.P[inst];
-        double q[V];
-#pragma unroll
-        for (int k = 0; k < V; k++)
-          q[k] = un[cstar * V + k];
-        Prim<L::THERMAL> s;
-        prim<L::THERMAL>(q, P, s);
-        double lam = max_abs_eigs<L::THERMAL>(q, s, 0, P);
+        double lam = EVs[inst];
         cf = -dtot * dt / lam;  // dt = cfl dx / lam  =>  d dt / d lam = -dt / lam
       }
     }
@@ -1329,7 +1521,7 @@ __global__ void __launch_bounds__(128) k_adj_reduce(
     for (int j = 0; j < V; j++)
       q[j] = un[cstar * V + j];
     Dual lam;
-    point_tangent<L>(q, k, B.P[inst], nullptr, nullptr, &lam);
+    point_tangent<L>(q, k, B.P[inst], nullptr, nullptr, &lam, EIGs + (long)inst * ND);
     if (k < V)
       ubar[cstar * V + k] += cf * lam.d;
     else

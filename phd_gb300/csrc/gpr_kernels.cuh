@@ -1189,7 +1189,7 @@ __global__ void k_b_weno(double *__restrict__ wh, const double *__restrict__ ub,
 template <class L>
 __global__ void __launch_bounds__(256) k_b_cfl_max(const double *__restrict__ u, long ncell,
                                                    unsigned long long *__restrict__ mx,
-                                                   Batch B) {
+                                                   Batch B, double *__restrict__ mcell = nullptr) {
   constexpr int V = L::V;
   long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= ncell)
@@ -1203,6 +1203,8 @@ __global__ void __launch_bounds__(256) k_b_cfl_max(const double *__restrict__ u,
   Prim<L::THERMAL> s;
   prim<L::THERMAL>(q, P, s);
   double m = max_abs_eigs<L::THERMAL>(q, s, 0, P) * B.idx[inst];
+  if (mcell)
+    mcell[c] = m;
   if (m > 0.0)  // NaN and zero are skipped
     atomicMax(mx + inst, (unsigned long long)__double_as_longlong(m));
 }
