@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
+    ap.add_argument("--profile-adjoint", type=int, default=0, metavar="NINST",
+                    help="with --profile-steps K: K steps of the Stokes differentiation "
+                         "problem for NINST instances, forward then backward (for ncu "
+                         "captures), no JSON")
     return ap.parse_args()
 
 
@@ -694,10 +698,35 @@ def roofline(stage_ms, ncell, n, mean_iters, peak):
     return out
 
 
+def profile_adjoint(ninst, steps):
+    """Forward and backward of `steps` steps of the Stokes problem (400 cells
+    per instance), twice (the second run is the one to capture)."""
+    import torch
+    import phd_gb300 as G
+    from phd_gb300.adjoint import Problem
+    from phd_gb300.params import material_params
+
+    def make_par(th):
+        return material_params("sg", 1.0, cv=1.0, gamma=1.4, b0=th[1], calpha=th[2], mu=th[0],
+                               Pr=0.75)
+
+    u0, _, _, dX, _ = G.problems.stokes(nx=400, tf=1.0)
+    u0p = np.tile(u0, (ninst, 1))
+    prob = Problem([400] * ninst, [dX[0]] * ninst, "transitive", make_par, cfl=0.8, tf=1.0)
+    pars = [make_par(np.array([1.2e-2, 0.9, 1.1]))] * ninst
+    for _ in range(2):
+        uN = prob.forward(torch.tensor(u0p, device="cuda"), pars, max_steps=steps)
+        prob.backward(torch.ones_like(uN))
+    torch.cuda.synchronize()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_adjoint:
+        return profile_adjoint(args.profile_adjoint, args.profile_steps or 32)
     return run_gb300(args)
 
 
