@@ -29,7 +29,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "FP64 Mcell-updates/s (TGV 512^2 ADER-WENO step)"
+# BASELINE.json's metric; "value" is its first part (plain path, TGV 512^2
+# step), the batched form and adjoint / forward ratio are the "batched" and
+# "adjoint" objects of the same line.
+METRIC = "FP64 Mcell-updates/s plain vs batched; adjoint\u00f7forward time at 1e-6 grad err"
 UNIT = "Mcell-updates/s"
 
 # Algorithmic FP64 operation counts per unit of work of the algorithm the
@@ -387,6 +390,12 @@ def run_gb300(args):
             batched = batched_bench(torch)
         except Exception as ex:
             batched = {"error": str(ex)}
+    shock = None
+    if rank == 0 and not args.no_batched:
+        try:
+            shock = shock_tube_bench(torch)
+        except Exception as ex:  # reported, not fatal to the main line
+            shock = {"error": str(ex)}
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         try:
@@ -418,6 +427,7 @@ def run_gb300(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ncell * V * 8,
                     "d2h_bytes_per_step": ncell * V * 8},
             "batched": batched,
+            "shock_tube": shock,
             "adjoint": adjoint,
             "gpu_launches": 14 * args.steps,
             "clocks": cs.summary()}
@@ -431,6 +441,58 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def shock_tube_bench(torch):
+    """The reference's CPU-runnable case: 1D shock tube, 200 cells, CFL 0.8,
+    t_end = 0.2 (248 steps), Rusanov (FLUX 0) and Osher (FLUX 2).  The whole
+    run is one gpr_iterate call (dt on the device, no host synchronisation),
+    timed with CUDA events; the oracle (C restatement of the reference) runs
+    the same problem on the host cores."""
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    from oracle import Oracle
+    lib = _lib.load()
+    u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=200)
+    nx = np.array([200], np.int32)
+    dxa = np.array(dX, np.float64)
+    bca = np.array([0, 0], np.int32)
+    cp = MP.to_ctypes()
+    V = 17
+    scr = torch.empty(lib.gpr_iterate_scratch_doubles(nx.ctypes.data_as(ctypes.c_void_p), 1, V),
+                      dtype=torch.float64, device="cuda")
+    O = Oracle()
+    out = {"workload": "shock tube 200 cells, V=17, CFL 0.8, t_end 0.2"}
+    for flux, name in ((0, "rusanov"), (2, "osher")):
+        def run():
+            ut = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+            clk = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
+            _lib.check(lib.gpr_iterate(
+                ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+                dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
+                ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), None, V,
+                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "iterate")
+            return ut, clk
+        run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ut, clk = run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        steps = int(clk[4].item())
+        t0 = time.perf_counter()
+        ref, n, _ = O.run(u0, MP, tf, dX, 0, cfl=0.8, flux=flux)
+        cpu_s = time.perf_counter() - t0
+        got = ut.cpu().numpy().reshape(ref.shape)
+        out[name] = {"steps": steps, "gpu_ms": ms,
+                     "gpu_value": 200 * steps / (ms * 1e-3) / 1e6,
+                     "cpu_value": 200 * n / cpu_s / 1e6, "cpu_cores": O.num_threads(),
+                     "unit": UNIT, "max_rel_diff_vs_oracle":
+                         float(np.max(np.abs(got - ref) / (1.0 + np.abs(ref))))}
+    return out
 
 
 def adjoint_bench(torch, fd_check=True):

@@ -42,7 +42,8 @@ def _iterator(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, 
 solvers = SimpleNamespace(
     weno=SimpleNamespace(weno_launcher=api.weno_launcher),
     dg=SimpleNamespace(predictor=api.predictor),
-    fv=SimpleNamespace(fv_launcher=api.fv_launcher, D_RUS=api.D_RUS, Bint=api.Bint),
+    fv=SimpleNamespace(fv_launcher=api.fv_launcher, D_RUS=api.D_RUS, D_ROE=api.D_ROE,
+                       D_OSH=api.D_OSH, Bint=api.Bint),
     split=SimpleNamespace(ode_launcher=api.ode_launcher),
     ader_stepper=api.ader_stepper,
     ader_stepper_para=api.ader_stepper_para,

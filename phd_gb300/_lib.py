@@ -15,6 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgpr_gb300.so")
 SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu"]
 HEADERS = ["gpr_device.cuh", "gpr_kernels.cuh", "gpr_consts.cuh", "gpr_ode.cuh", "gpr_host.cuh",
+           "gpr_osher.cuh",
            "gpr_adjoint.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -315,5 +315,15 @@ def D_RUS(qL, qR, d, MP):
     return interface_terms(qL, qR, d, 0, MP)[0]
 
 
+def D_ROE(qL, qR, d, MP):
+    """Roe dissipation plus F(qL) + F(qR) (fluxes.cpp:46-64); d = 0."""
+    return interface_terms(qL, qR, d, 1, MP)[0]
+
+
+def D_OSH(qL, qR, d, MP):
+    """Osher-Solomon dissipation plus F(qL) + F(qR) (fluxes.cpp:22-44); d = 0."""
+    return interface_terms(qL, qR, d, 2, MP)[0]
+
+
 def Bint(qL, qR, d, MP):
     return interface_terms(qL, qR, d, 0, MP)[1]

@@ -9,6 +9,7 @@
 
 #include "gpr_host.cuh"
 #include "gpr_ode.cuh"
+#include "gpr_osher.cuh"
 
 using namespace gpr;
 using namespace gpr::host;
@@ -56,7 +57,10 @@ __global__ void k_pointwise(int what, const double *__restrict__ Q, const double
 #pragma unroll
     for (int k = 0; k < V; k++)
       qr[k] = X[c * V + k];
-    interface_point<L>(q, qr, d, P, C, r, b);
+    if (flux == GPR_FLUX_RUSANOV)
+      interface_point<L>(q, qr, d, P, C, r, b);
+    else
+      interface_point_eig<L>(q, qr, flux, P, C, r, b);
 #pragma unroll
     for (int k = 0; k < V; k++)
       out2[c * V + k] = b[k];
@@ -177,13 +181,19 @@ template <class L> struct Ops {
 
   static int fv(double *u, const double *qh, const int32_t *nX, double dt,
                 const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
-                const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st) {
+                const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st,
+                int flux = GPR_FLUX_RUSANOV) {
     const Consts &C = consts();
     int nx = nX[0];
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
-      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
-                                                     dt_dev, dX[0], time_dg, P, C, Batch{});
+      if (flux == GPR_FLUX_RUSANOV)
+        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
+                                                       dt_dev, dX[0], time_dg, P, C, Batch{});
+      else
+        k_faces1d_eig<L><<<blocks(nf, 64), 64, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
+                                                         dt_dev, dX[0], time_dg, flux, P, C,
+                                                         Batch{});
       long nc = (long)nx * NN * NN;
       k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
                                                       dt_dev, dX[0], 1.0, sources, time_dg, P,
@@ -210,13 +220,18 @@ template <class L> struct Ops {
   // contributions (to the left and right cells) into fb.
   static int faces(const double *qh, const int32_t *nX, double dt, const double *dX, int nd,
                    int time_dg, const DevPar &P, const uint8_t *mask, double *fb,
-                   cudaStream_t st) {
+                   cudaStream_t st, int flux = GPR_FLUX_RUSANOV) {
     const Consts &C = consts();
     int nx = nX[0];
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
-      k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
-                                                     dX[0], time_dg, P, C, Batch{});
+      if (flux == GPR_FLUX_RUSANOV)
+        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
+                                                       dX[0], time_dg, P, C, Batch{});
+      else
+        k_faces1d_eig<L><<<blocks(nf, 64), 64, 0, st>>>(fb, qh, (long)nx + 1, mask, dt,
+                                                         nullptr, dX[0], time_dg, flux, P, C,
+                                                         Batch{});
       return cuda_rc();
     }
     int ny = nX[1];
@@ -258,7 +273,8 @@ template <class L> struct Ops {
   // clock advance, with dt living in clk[1].
   static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
                      const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
-                     int nsteps, double *scratch, int32_t *status, cudaStream_t st) {
+                     int nsteps, double *scratch, int32_t *status, cudaStream_t st,
+                     int flux = GPR_FLUX_RUSANOV) {
     long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
@@ -285,7 +301,7 @@ template <class L> struct Ops {
       rc = predictor(qh, wh, 0.0, dt_dev, dX, nd, nX, 0, P, mask, status, st);
       if (rc)
         return rc;
-      rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st);
+      rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st, flux);
       if (rc)
         return rc;
       k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
@@ -357,6 +373,16 @@ bool check_grid(const int32_t *nX, int nd) {
     if (nX[d] < 1)
       return false;
   return true;
+}
+
+// Rusanov everywhere; Osher and Roe (17x17 eigen-decompositions per face
+// point) on 1D grids.
+int check_flux(int flux, int nd) {
+  if (flux < GPR_FLUX_RUSANOV || flux > GPR_FLUX_OSHER)
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV && nd != 1)
+    return GPR_E_UNSUPPORTED;
+  return GPR_OK;
 }
 
 #define DISPATCH(nvar, CALL)                                                                 \
@@ -442,7 +468,9 @@ int gpr_interface_terms(const double *qL, const double *qR, double *out, double 
                         void *stream) {
   if (!qL || !qR || !out || !bout || count < 0 || d < 0 || d > 2 || !par)
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
+  if (flux < GPR_FLUX_RUSANOV || flux > GPR_FLUX_OSHER)
+    return GPR_E_ARG;
+  if (flux != GPR_FLUX_RUSANOV && d != 0)
     return GPR_E_UNSUPPORTED;
   if (count == 0)
     return GPR_OK;
@@ -495,11 +523,11 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     void *stream) {
   if (!u || !qh || !dX || !par || !scratch || !check_grid(nX, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return GPR_E_UNSUPPORTED;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, sources, time_dg, P, mask, scratch,
-                       S(stream)))
+                       S(stream), flux))
 }
 
 int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt, const double *dX,
@@ -507,10 +535,10 @@ int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt, const dou
                        const uint8_t *mask, double *fb, int nvar, void *stream) {
   if (!qh || !dX || !par || !fb || !check_grid(nX, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return GPR_E_UNSUPPORTED;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
   DevPar P = make_devpar(*par);
-  DISPATCH(nvar, O::faces(qh, nX, dt, dX, ndim, time_dg, P, mask, fb, S(stream)))
+  DISPATCH(nvar, O::faces(qh, nX, dt, dX, ndim, time_dg, P, mask, fb, S(stream), flux))
 }
 
 int gpr_timestep_scratch_doubles(int64_t ncell) {
@@ -567,8 +595,8 @@ int gpr_ader_stepper(double *u, const double *ub, const int32_t *nX, int ndim, d
                      void *stream) {
   if (!u || !ub || !dX || !par || !scratch || !check_grid(nX, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return GPR_E_UNSUPPORTED;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
   long ncb = ndim == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
   long ns = ndim == 1 ? NN : NN * NN;
   double *wh = scratch;
@@ -601,11 +629,11 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const 
   for (int i = 0; i < 2 * ndim; i++)
     if (bcs[i] < 0 || bcs[i] > 5)
       return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return GPR_E_UNSUPPORTED;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::iterate(u, nX, ndim, dX, bcs, P, mask, clock, nsteps, scratch, status,
-                            S(stream)))
+                            S(stream), flux))
 }
 
 }  // extern "C"

@@ -1,0 +1,817 @@
+// gpr_osher.cuh - Osher-Solomon and Roe dissipation on the device
+// (solvers/fv/fluxes.cpp:22-64): D = sum_i w_i |M(q_i)| (qL - qR) over the
+// Gauss nodes of the straight path q_i = qR + x_i (qL - qR) (Osher), or
+// |sum_i w_i M(q_i)| (qL - qR) (Roe), with M = dF/dQ + B the system matrix
+// (system/equations.cpp:269-276) and |M| = R |Lambda| R^-1 from its real
+// nonsymmetric eigen-decomposition.
+//
+// The eigen-decomposition (Householder Hessenberg reduction, Francis
+// double-shift QR with accumulated Schur vectors, eigenvectors by
+// back-substitution on the quasi-triangular Schur form; Golub & Van Loan,
+// Matrix Computations, Alg. 7.4.2, 7.5.1-7.5.2) runs per thread with its
+// matrices in local memory: one thread per (face, time node).  Eigenvalues
+// closer than MULT_TOL ||T|| are treated as one semisimple eigenvalue (their
+// Schur vectors stay independent eigenvectors), which is how the reference's
+// Eigen solver behaves on the GPR system's 9-fold advection eigenvalue.
+#pragma once
+
+#include "gpr_kernels.cuh"
+
+namespace gpr {
+
+constexpr double OSH_MULT_TOL = 1e-12;
+
+// System matrix M = dF_x/dP dP/dQ + B_x (equations.cpp:68-187, 269-276):
+// row-major V x V into M (ld = V).
+template <bool TH, int V>
+GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, double *M) {
+  constexpr int d = 0;
+  double F[V * V], D[V * V];
+#pragma unroll 1
+  for (int i = 0; i < V * V; i++) {
+    F[i] = 0.0;
+    D[i] = 0.0;
+  }
+#define RF(i, j) F[(i) * V + (j)]
+#define RD(i, j) D[(i) * V + (j)]
+  const double r = s.r, ir = s.ir;
+  const double E = Q[1] * ir;
+  const double p = s.p;
+  const double *v = s.v;
+  const double *A = Q + 5;
+  const EosRho &e = s.e;
+  // dE/drho at fixed p and dE/dp (mg.cpp:141-170, eos.cpp)
+  const double rG = r * e.G, irG2 = s.irG * s.irG;
+  const double dnum = e.dpr * rG + (e.G + r * e.dG) * (p - e.pr);
+  const double dedr = e.der - dnum * irG2;
+  const double Ep = s.irG;
+  double dC0 = 0.0;
+  if (P.beta != 0.0) {
+    double dcs2 = P.beta * ir * s.cs2;
+    dC0 = (1.0 - P.beta / e.G) * dcs2 + P.beta / (e.G * e.G) * e.dG * s.cs2;
+  }
+  const double Er = dedr + 0.25 * dC0 * s.devGsq;
+  const double vd = v[d], rvd = r * vd;
+  double G[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  const double *AG = s.AdG;
+  RF(0, 0) = vd;
+  RF(0, 2 + d) = r;
+  RF(1, 0) = (E + r * Er) * vd;
+  RF(1, 1) = (r * Ep + 1.0) * vd;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    RF(1, 2 + i) = r * vd * v[i];
+  RF(1, 2 + d) += r * E + p;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    RF(2 + i, 0) = vd * v[i];
+#pragma unroll
+  for (int i = 2; i < 5; i++)
+    RF(i, i) = rvd;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    RF(2 + i, 2 + d) += r * v[i];
+  RF(2 + d, 1) = 1.0;
+  {
+    double sg[3];
+    sigma_col<TH>(Q, s, d, sg);
+    const double fr = (1.0 + P.beta) * ir;  // 1/rho + dcs2/drho / cs2
+    const double sr[3] = {fr * sg[0], fr * sg[1], fr * sg[2]};
+    const double C0 = P.beta == 0.0 ? s.cs2
+                                    : (P.EOS == 1 ? (1.0 - P.beta / e.G) : P.C0f) * s.cs2;
+    const double cs2 = s.cs2;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int ind = i * 3 + j;
+        double tmp = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          // dsigma_k / dA_ij (state.cpp:58-71) with ii = d, jj = k
+          double t = A[3 * i + d] * G[3 * k + j] + A[3 * i + k] * G[3 * d + j] -
+                     2.0 / 3.0 * G[3 * d + k] * A[3 * i + j];
+          if (d == j)
+            t += AG[3 * i + k];
+          if (k == j)
+            t += AG[3 * i + d];
+          const double dsA = -r * cs2 * t;
+          RF(2 + k, 5 + ind) = -dsA;
+          tmp -= v[k] * dsA;
+        }
+        RF(1, 5 + ind) = tmp;
+      }
+    RF(1, 0) -= sr[0] * v[0] + sr[1] * v[1] + sr[2] * v[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      RF(1, 2 + i) -= sg[i];
+#pragma unroll
+    for (int i = 0; i < 9; i++)
+      RF(1, 5 + i) += rvd * (C0 * AG[i]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      RF(2 + i, 0) -= sr[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      RF(5 + d, 2 + j) = A[j];
+      RF(8 + d, 2 + j) = A[3 + j];
+      RF(11 + d, 2 + j) = A[6 + j];
+      RF(5 + d, 5 + j) = v[j];
+      RF(8 + d, 8 + j) = v[j];
+      RF(11 + d, 11 + j) = v[j];
+    }
+    // dP/dQ (equations.cpp:130-167)
+#pragma unroll
+    for (int i = 0; i < V; i++)
+      RD(i, i) = 1.0;
+    const double G_ = 1.0 / (r * Ep);
+    double tmpu = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) - (E + r * Er);
+    if (TH)
+      tmpu += P.calpha2 * (s.J[0] * s.J[0] + s.J[1] * s.J[1] + s.J[2] * s.J[2]);
+    RD(1, 0) = G_ * tmpu;
+    RD(1, 1) = G_;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      RD(1, 2 + i) = -G_ * v[i];
+      RD(2 + i, 0) = -v[i] * ir;
+    }
+#pragma unroll
+    for (int i = 2; i < 5; i++)
+      RD(i, i) = ir;
+#pragma unroll
+    for (int i = 0; i < 9; i++)
+      RD(1, 5 + i) = -G_ * r * (C0 * AG[i]);
+  }
+  if (TH) {
+    const double ca2 = P.calpha2;
+    const double T = s.T;
+    const double Tr = -dnum * irG2 * P.icv;
+    const double Tp = Ep * P.icv;
+    const double *J = s.J;
+    const double H[3] = {ca2 * Q[14] * ir, ca2 * Q[15] * ir, ca2 * Q[16] * ir};
+    RF(1, 0) += Tr * H[d];
+    RF(1, 1) += Tp * H[d];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      RF(1, 14 + i) = rvd * H[i];
+    RF(1, 14 + d) += ca2 * T;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      RF(14 + i, 0) = v[d] * J[i];
+    RF(14 + d, 0) += Tr;
+    RF(14 + d, 1) = Tp;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      RF(14 + i, 2 + d) = r * J[i];
+#pragma unroll
+    for (int i = 14; i < 17; i++)
+      RF(i, i) = rvd;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      RD(1, 14 + i) = -(1.0 / (r * Ep)) * (ca2 * Q[14 + i] * ir);
+      RD(14 + i, 0) = -J[i] * ir;
+    }
+#pragma unroll
+    for (int i = 14; i < 17; i++)
+      RD(i, i) = ir;
+  }
+#undef RF
+#undef RD
+#pragma unroll 1
+  for (int i = 0; i < V; i++)
+#pragma unroll 1
+    for (int j = 0; j < V; j++) {
+      double acc = 0.0;
+#pragma unroll 1
+      for (int k = 0; k < V; k++)
+        acc += F[i * V + k] * D[k * V + j];
+      M[i * V + j] = acc;
+    }
+  // block (equations.cpp:169-187): the non-conservative product B_x
+#pragma unroll
+  for (int i = 5; i < 14; i++)
+    M[i * V + i] += vd;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    M[(5 + d) * V + 5 + i] -= v[i];
+    M[(8 + d) * V + 8 + i] -= v[i];
+    M[(11 + d) * V + 11 + i] -= v[i];
+  }
+}
+
+// Householder reduction of H (n x n, ld n) to upper Hessenberg form,
+// accumulating the transformations into Z.
+template <int n> GPR_D void hess_reduce(double *H, double *Z) {
+#pragma unroll 1
+  for (int k = 0; k < n - 2; k++) {
+    double alpha = 0.0;
+#pragma unroll 1
+    for (int i = k + 1; i < n; i++)
+      alpha += H[i * n + k] * H[i * n + k];
+    alpha = sqrt(alpha);
+    if (alpha == 0.0)
+      continue;
+    const double x0 = H[(k + 1) * n + k];
+    const double beta = x0 > 0 ? -alpha : alpha;
+    double vv = (x0 - beta) * (x0 - beta);
+#pragma unroll 1
+    for (int i = k + 2; i < n; i++)
+      vv += H[i * n + k] * H[i * n + k];
+    if (vv == 0.0)
+      continue;
+    double v[n];
+#pragma unroll 1
+    for (int i = 0; i <= k; i++)
+      v[i] = 0.0;
+    v[k + 1] = x0 - beta;
+#pragma unroll 1
+    for (int i = k + 2; i < n; i++)
+      v[i] = H[i * n + k];
+    const double tau = 2.0 / vv;
+#pragma unroll 1
+    for (int j = 0; j < n; j++) {
+      double s = 0.0;
+#pragma unroll 1
+      for (int i = k + 1; i < n; i++)
+        s += v[i] * H[i * n + j];
+      s *= tau;
+#pragma unroll 1
+      for (int i = k + 1; i < n; i++)
+        H[i * n + j] -= s * v[i];
+    }
+#pragma unroll 1
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+#pragma unroll 1
+      for (int j = k + 1; j < n; j++)
+        s += H[i * n + j] * v[j];
+      s *= tau;
+#pragma unroll 1
+      for (int j = k + 1; j < n; j++)
+        H[i * n + j] -= s * v[j];
+    }
+#pragma unroll 1
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+#pragma unroll 1
+      for (int j = k + 1; j < n; j++)
+        s += Z[i * n + j] * v[j];
+      s *= tau;
+#pragma unroll 1
+      for (int j = k + 1; j < n; j++)
+        Z[i * n + j] -= s * v[j];
+    }
+#pragma unroll 1
+    for (int i = k + 2; i < n; i++)
+      H[i * n + k] = 0.0;
+  }
+}
+
+// Francis double-shift QR on the upper Hessenberg H to real Schur form,
+// transformations accumulated into Z; eigenvalues to (wr, wi).  Returns
+// false if it does not converge within 60 n iterations.
+template <int n> GPR_D bool hqr_schur(double *H, double *Z, double *wr, double *wi) {
+  const double eps = 2.220446049250313e-16;
+  double norm = 0.0;
+#pragma unroll 1
+  for (int i = 0; i < n; i++)
+#pragma unroll 1
+    for (int j = (i > 0 ? i - 1 : 0); j < n; j++)
+      norm += fabs(H[i * n + j]);
+  int hi = n - 1, iter = 0, total = 0;
+  double exshift = 0.0;
+  while (hi >= 0) {
+    int l = hi;
+    while (l > 0) {
+      double s = fabs(H[(l - 1) * n + l - 1]) + fabs(H[l * n + l]);
+      if (s == 0.0)
+        s = norm;
+      if (fabs(H[l * n + l - 1]) < eps * s)
+        break;
+      l--;
+    }
+    if (l == hi) {  // one root
+      H[hi * n + hi] += exshift;
+      wr[hi] = H[hi * n + hi];
+      wi[hi] = 0.0;
+      if (hi > 0)
+        H[hi * n + hi - 1] = 0.0;
+      hi--;
+      iter = 0;
+      continue;
+    }
+    double x = H[hi * n + hi];
+    double y = H[(hi - 1) * n + hi - 1];
+    double w = H[hi * n + hi - 1] * H[(hi - 1) * n + hi];
+    if (l == hi - 1) {  // two roots
+      if (hi >= 2)
+        H[(hi - 1) * n + hi - 2] = 0.0;
+      double p = 0.5 * (y - x);
+      double q = p * p + w;
+      // a complex pair with a rounding-level imaginary part is a real
+      // double root (a semisimple eigenvalue split by rounding)
+      if (q < 0.0 && sqrt(-q) <= OSH_MULT_TOL * norm)
+        q = 0.0;
+      double z = sqrt(fabs(q));
+      H[hi * n + hi] = x + exshift;
+      H[(hi - 1) * n + hi - 1] = y + exshift;
+      x = H[hi * n + hi];
+      if (q >= 0.0) {
+        z = p >= 0 ? p + z : p - z;
+        wr[hi - 1] = x + z;
+        wr[hi] = z != 0.0 ? x - w / z : x + z;
+        wi[hi - 1] = wi[hi] = 0.0;
+        const double xx = H[hi * n + hi - 1];
+        const double s = fabs(xx) + fabs(z);
+        double pp = xx / s, qq = z / s;
+        const double rr = sqrt(pp * pp + qq * qq);
+        pp /= rr;
+        qq /= rr;
+#pragma unroll 1
+        for (int j = hi - 1; j < n; j++) {
+          const double a = H[(hi - 1) * n + j];
+          H[(hi - 1) * n + j] = qq * a + pp * H[hi * n + j];
+          H[hi * n + j] = qq * H[hi * n + j] - pp * a;
+        }
+#pragma unroll 1
+        for (int i = 0; i <= hi; i++) {
+          const double a = H[i * n + hi - 1];
+          H[i * n + hi - 1] = qq * a + pp * H[i * n + hi];
+          H[i * n + hi] = qq * H[i * n + hi] - pp * a;
+        }
+#pragma unroll 1
+        for (int i = 0; i < n; i++) {
+          const double a = Z[i * n + hi - 1];
+          Z[i * n + hi - 1] = qq * a + pp * Z[i * n + hi];
+          Z[i * n + hi] = qq * Z[i * n + hi] - pp * a;
+        }
+        H[hi * n + hi - 1] = 0.0;
+      } else {
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = z;
+        wi[hi] = -z;
+      }
+      hi -= 2;
+      iter = 0;
+      continue;
+    }
+    if (iter == 10 || iter == 20) {  // exceptional shift
+      exshift += x;
+#pragma unroll 1
+      for (int i = 0; i <= hi; i++)
+        H[i * n + i] -= x;
+      const double s = fabs(H[hi * n + hi - 1]) + fabs(H[(hi - 1) * n + hi - 2]);
+      x = y = 0.75 * s;
+      w = -0.4375 * s * s;
+    }
+    iter++;
+    total++;
+    if (total > 60 * n)
+      return false;
+    int m = hi - 2;
+    double p = 0, q = 0, r = 0, z;
+    while (m >= l) {
+      z = H[m * n + m];
+      r = x - z;
+      double s = y - z;
+      p = (r * s - w) / H[(m + 1) * n + m] + H[m * n + m + 1];
+      q = H[(m + 1) * n + m + 1] - z - r - s;
+      r = H[(m + 2) * n + m + 1];
+      s = fabs(p) + fabs(q) + fabs(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      const double u = fabs(H[m * n + m - 1]) * (fabs(q) + fabs(r));
+      const double vv =
+          fabs(p) * (fabs(H[(m - 1) * n + m - 1]) + fabs(z) + fabs(H[(m + 1) * n + m + 1]));
+      if (u < eps * vv)
+        break;
+      m--;
+    }
+#pragma unroll 1
+    for (int i = m + 2; i <= hi; i++) {
+      H[i * n + i - 2] = 0.0;
+      if (i > m + 2)
+        H[i * n + i - 3] = 0.0;
+    }
+#pragma unroll 1
+    for (int k = m; k <= hi - 1; k++) {
+      const bool notlast = (k != hi - 1);
+      if (k != m) {
+        p = H[k * n + k - 1];
+        q = H[(k + 1) * n + k - 1];
+        r = notlast ? H[(k + 2) * n + k - 1] : 0.0;
+        x = fabs(p) + fabs(q) + fabs(r);
+        if (x == 0.0)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      double s = sqrt(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        H[k * n + k - 1] = -s * x;
+      else if (l != m)
+        H[k * n + k - 1] = -H[k * n + k - 1];
+      p += s;
+      x = p / s;
+      y = q / s;
+      z = r / s;
+      q /= p;
+      r /= p;
+#pragma unroll 1
+      for (int j = k; j < n; j++) {  // rows
+        double pp = H[k * n + j] + q * H[(k + 1) * n + j];
+        if (notlast) {
+          pp += r * H[(k + 2) * n + j];
+          H[(k + 2) * n + j] -= pp * z;
+        }
+        H[k * n + j] -= pp * x;
+        H[(k + 1) * n + j] -= pp * y;
+      }
+      const int ihi = hi < k + 3 ? hi : k + 3;
+#pragma unroll 1
+      for (int i = 0; i <= ihi; i++) {  // columns
+        double pp = x * H[i * n + k] + y * H[i * n + k + 1];
+        if (notlast) {
+          pp += z * H[i * n + k + 2];
+          H[i * n + k + 2] -= pp * r;
+        }
+        H[i * n + k] -= pp;
+        H[i * n + k + 1] -= pp * q;
+      }
+#pragma unroll 1
+      for (int i = 0; i < n; i++) {
+        double pp = x * Z[i * n + k] + y * Z[i * n + k + 1];
+        if (notlast) {
+          pp += z * Z[i * n + k + 2];
+          Z[i * n + k + 2] -= pp * r;
+        }
+        Z[i * n + k] -= pp;
+        Z[i * n + k + 1] -= pp * q;
+      }
+    }
+  }
+  return true;
+}
+
+// Eigenvectors (columns of Rr + i Ri, n x n row-major) from the real Schur
+// form T and Schur vectors Z, by back-substitution per eigenvalue.
+template <int n>
+GPR_D void schur_vectors(const double *T, const double *Z, const double *wr, const double *wi,
+                         double *Rr, double *Ri) {
+  double norm = 0.0;
+#pragma unroll 1
+  for (int i = 0; i < n; i++)
+#pragma unroll 1
+    for (int j = i > 0 ? i - 1 : 0; j < n; j++)
+      norm += fabs(T[i * n + j]);
+#pragma unroll 1
+  for (int k = 0; k < n; k++) {
+    const double lr = wr[k], li = wi[k];
+    double yr[n], yi[n];
+#pragma unroll 1
+    for (int i = 0; i < n; i++)
+      yr[i] = yi[i] = 0.0;
+    const bool blk2 = (k + 1 < n && T[(k + 1) * n + k] != 0.0);
+    const bool blk1 = (k > 0 && T[k * n + k - 1] != 0.0);
+    int top;
+    if (!blk1 && !blk2) {
+      yr[k] = 1.0;
+      top = k;
+    } else {
+      const int b = blk2 ? k : k - 1;
+      const double a11 = T[b * n + b] - lr, a12 = T[b * n + b + 1];
+      const double a21 = T[(b + 1) * n + b];
+      if (fabs(a12) >= fabs(a21)) {
+        yr[b] = 1.0;
+        yi[b] = 0.0;
+        yr[b + 1] = -a11 / a12;
+        yi[b + 1] = li / a12;
+      } else {
+        const double a22r = T[(b + 1) * n + b + 1] - lr;
+        yr[b + 1] = 1.0;
+        yi[b + 1] = 0.0;
+        yr[b] = -a22r / a21;
+        yi[b] = li / a21;
+      }
+      top = b + 1;
+    }
+    const int start = (blk1 || blk2) ? (blk2 ? k - 1 : k - 2) : k - 1;
+#pragma unroll 1
+    for (int i = start; i >= 0; i--) {
+      const bool is2 = (i > 0 && T[i * n + i - 1] != 0.0);
+      if (!is2) {
+        double sr = 0.0, si = 0.0;
+#pragma unroll 1
+        for (int j = i + 1; j <= top; j++) {
+          sr += T[i * n + j] * yr[j];
+          si += T[i * n + j] * yi[j];
+        }
+        const double dr = T[i * n + i] - lr, di = -li;
+        if (hypot(dr, di) <= OSH_MULT_TOL * norm) {
+          yr[i] = yi[i] = 0.0;  // the same eigenvalue: independent Schur vector
+          continue;
+        }
+        const double den = dr * dr + di * di;
+        yr[i] = -(sr * dr + si * di) / den;
+        yi[i] = -(si * dr - sr * di) / den;
+      } else {
+        const int a = i - 1;
+        double s1r = 0, s1i = 0, s2r = 0, s2i = 0;
+#pragma unroll 1
+        for (int j = i + 1; j <= top; j++) {
+          s1r += T[a * n + j] * yr[j];
+          s1i += T[a * n + j] * yi[j];
+          s2r += T[i * n + j] * yr[j];
+          s2i += T[i * n + j] * yi[j];
+        }
+        const double m11r = T[a * n + a] - lr, m11i = -li;
+        const double m12 = T[a * n + i], m21 = T[i * n + a];
+        const double m22r = T[i * n + i] - lr, m22i = -li;
+        const double detr = m11r * m22r - m11i * m22i - m12 * m21;
+        const double deti = m11r * m22i + m11i * m22r;
+        if (hypot(detr, deti) <= OSH_MULT_TOL * norm * OSH_MULT_TOL * norm) {
+          yr[a] = yi[a] = yr[i] = yi[i] = 0.0;
+          i--;
+          continue;
+        }
+        const double den = detr * detr + deti * deti;
+        const double nar = -(s1r * m22r - s1i * m22i) + m12 * s2r;
+        const double nai = -(s1r * m22i + s1i * m22r) + m12 * s2i;
+        const double nir = -(m11r * s2r - m11i * s2i) + m21 * s1r;
+        const double nii = -(m11r * s2i + m11i * s2r) + m21 * s1i;
+        yr[a] = (nar * detr + nai * deti) / den;
+        yi[a] = (nai * detr - nar * deti) / den;
+        yr[i] = (nir * detr + nii * deti) / den;
+        yi[i] = (nii * detr - nir * deti) / den;
+        i--;
+      }
+    }
+#pragma unroll 1
+    for (int i = 0; i < n; i++) {
+      double sr = 0.0, si = 0.0;
+#pragma unroll 1
+      for (int j = 0; j <= top; j++) {
+        sr += Z[i * n + j] * yr[j];
+        si += Z[i * n + j] * yi[j];
+      }
+      Rr[i * n + k] = sr;
+      Ri[i * n + k] = si;
+    }
+  }
+}
+
+// Complex Gaussian elimination with partial pivoting: (Cr + i Ci) x = b,
+// b = (br + i bi) overwritten by x.  Returns false if singular.
+template <int n> GPR_D bool csolve_n(double *Cr, double *Ci, double *br, double *bi) {
+#pragma unroll 1
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    double best = hypot(Cr[c * n + c], Ci[c * n + c]);
+#pragma unroll 1
+    for (int r = c + 1; r < n; r++) {
+      const double a = hypot(Cr[r * n + c], Ci[r * n + c]);
+      if (a > best) {
+        best = a;
+        p = r;
+      }
+    }
+    if (best == 0.0)
+      return false;
+    if (p != c) {
+#pragma unroll 1
+      for (int j = 0; j < n; j++) {
+        double t = Cr[c * n + j];
+        Cr[c * n + j] = Cr[p * n + j];
+        Cr[p * n + j] = t;
+        t = Ci[c * n + j];
+        Ci[c * n + j] = Ci[p * n + j];
+        Ci[p * n + j] = t;
+      }
+      double t = br[c];
+      br[c] = br[p];
+      br[p] = t;
+      t = bi[c];
+      bi[c] = bi[p];
+      bi[p] = t;
+    }
+    const double pr = Cr[c * n + c], pi = Ci[c * n + c];
+    const double den = pr * pr + pi * pi;
+#pragma unroll 1
+    for (int r = c + 1; r < n; r++) {
+      const double ar = Cr[r * n + c], ai = Ci[r * n + c];
+      const double fr = (ar * pr + ai * pi) / den, fi = (ai * pr - ar * pi) / den;
+#pragma unroll 1
+      for (int j = c; j < n; j++) {
+        const double xr = Cr[c * n + j], xi = Ci[c * n + j];
+        Cr[r * n + j] -= fr * xr - fi * xi;
+        Ci[r * n + j] -= fr * xi + fi * xr;
+      }
+      br[r] -= fr * br[c] - fi * bi[c];
+      bi[r] -= fr * bi[c] + fi * br[c];
+    }
+  }
+#pragma unroll 1
+  for (int r = n - 1; r >= 0; r--) {
+    double sr = br[r], si = bi[r];
+#pragma unroll 1
+    for (int j = r + 1; j < n; j++) {
+      sr -= Cr[r * n + j] * br[j] - Ci[r * n + j] * bi[j];
+      si -= Cr[r * n + j] * bi[j] + Ci[r * n + j] * br[j];
+    }
+    const double pr = Cr[r * n + r], pi = Ci[r * n + r];
+    const double den = pr * pr + pi * pi;
+    br[r] = (sr * pr + si * pi) / den;
+    bi[r] = (si * pr - sr * pi) / den;
+  }
+  return true;
+}
+
+// acc += w R |Lambda| R^-1 dq for M (n x n row-major, destroyed).
+template <int n> GPR_D bool abs_apply(double *M, const double *dq, double w, double *acc) {
+  double Z[n * n], wr[n], wi[n], Rr[n * n], Ri[n * n], Cr[n * n], Ci[n * n];
+#pragma unroll 1
+  for (int i = 0; i < n * n; i++)
+    Z[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
+  hess_reduce<n>(M, Z);
+  if (!hqr_schur<n>(M, Z, wr, wi))
+    return false;
+  schur_vectors<n>(M, Z, wr, wi, Rr, Ri);
+#pragma unroll 1
+  for (int i = 0; i < n * n; i++) {
+    Cr[i] = Rr[i];
+    Ci[i] = Ri[i];
+  }
+  double br[n], bi[n];
+#pragma unroll 1
+  for (int k = 0; k < n; k++) {
+    br[k] = dq[k];
+    bi[k] = 0.0;
+  }
+  if (!csolve_n<n>(Cr, Ci, br, bi))
+    return false;
+#pragma unroll 1
+  for (int k = 0; k < n; k++) {
+    const double a = hypot(wr[k], wi[k]);
+    br[k] *= a;
+    bi[k] *= a;
+  }
+#pragma unroll 1
+  for (int i = 0; i < n; i++) {
+    double s = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < n; k++)
+      s += Rr[i * n + k] * br[k] - Ri[i * n + k] * bi[k];
+    acc[i] += w * s;
+  }
+  return true;
+}
+
+// Eigen part of D_OSH (flux 2) / D_ROE (flux 1) at one interface into f
+// (overwritten); NaN if the eigen-decomposition fails (fluxes.cpp:22-64).
+template <class L>
+GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const DevPar &P,
+                           const Consts &C, double *f) {
+  constexpr int V = L::V;
+  double dq[V], q[V], M[V * V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    dq[k] = ql[k] - qr[k];
+    f[k] = 0.0;
+  }
+  bool ok = true;
+  if (flux == GPR_FLUX_OSHER) {
+#pragma unroll 1
+    for (int i = 0; i < NN; i++) {
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        q[k] = qr[k] + C.nodes[i] * dq[k];
+      Prim<L::THERMAL> s;
+      prim<L::THERMAL>(q, P, s);
+      system_matrix<L::THERMAL, V>(q, s, P, M);
+      ok = ok && abs_apply<V>(M, dq, C.w[i], f);
+    }
+  } else {
+    double Mi[V * V];
+#pragma unroll 1
+    for (int i = 0; i < V * V; i++)
+      M[i] = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < NN; i++) {
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        q[k] = qr[k] + C.nodes[i] * dq[k];
+      Prim<L::THERMAL> s;
+      prim<L::THERMAL>(q, P, s);
+      system_matrix<L::THERMAL, V>(q, s, P, Mi);
+#pragma unroll 1
+      for (int k = 0; k < V * V; k++)
+        M[k] += C.w[i] * Mi[k];
+    }
+    ok = abs_apply<V>(M, dq, 1.0, f);
+  }
+  if (!ok) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      f[k] = __longlong_as_double(0x7ff8000000000000ll);
+  }
+}
+
+// Interface terms for flux 1 / 2: f = D + F(qL) + F(qR) and the path integral.
+template <class L>
+GPR_D void interface_point_eig(const double *ql, const double *qr, int flux, const DevPar &P,
+                               const Consts &C, double *f, double *b) {
+  constexpr int V = L::V;
+  eig_dissipation<L>(ql, qr, flux, P, C, f);
+  Prim<L::THERMAL> sl, sr;
+  prim<L::THERMAL>(ql, P, sl);
+  prim<L::THERMAL>(qr, P, sr);
+  flux_add<L::THERMAL, V>(ql, sl, 0, P, f);
+  flux_add<L::THERMAL, V>(qr, sr, 0, P, f);
+  double dq[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    dq[k] = qr[k] - ql[k];
+    b[k] = 0.0;
+  }
+#pragma unroll
+  for (int n = 0; n < NN; n++) {
+    const double rho = ql[0] + C.nodes[n] * dq[0];
+    const double ir = 1.0 / rho;
+    const double v[3] = {(ql[2] + C.nodes[n] * dq[2]) * ir, (ql[3] + C.nodes[n] * dq[3]) * ir,
+                         (ql[4] + C.nodes[n] * dq[4]) * ir};
+    double bd[V];
+    bdot<V, L::LSET>(v, dq, 0, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      b[k] += C.w[n] * bd[k];
+  }
+}
+
+// 1D faces with the Osher or Roe dissipation: one thread per (face, time
+// node); output as k_faces1d (fb[face][0] to the left cell, [1] to the right).
+template <class L, bool BATCH = false>
+__global__ void __launch_bounds__(64) k_faces1d_eig(
+    double *__restrict__ fb, const double *__restrict__ qh, long nface,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int time_dg, int flux, DevPar Pv, Consts C, Batch B) {
+  constexpr int V = L::V;
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int t = threadIdx.x % NN;
+  const long face = gt / NN;
+  const bool valid = face < nface;
+  const long fo = valid ? face : 0;
+  long fi = fo;
+  const int inst = BATCH ? B.inst_f[fo] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    fi = B.off_b[inst] + (fo - B.off_f[inst]);
+    dt = B.clk[5 * inst + 1];
+    dx = 1.0 / B.idx[inst];
+  }
+  const bool active =
+      valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
+  const int nt = time_dg ? NN : 1;
+  double ql[V], qr[V], f[V], b[V];
+  const double *ql_ = qh + (fi * nt + (time_dg ? t : 0)) * NN * V;
+  const double *qr_ = qh + ((fi + 1) * nt + (time_dg ? t : 0)) * NN * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    ql[k] = C.endv[1][0] * ql_[k] + C.endv[1][1] * ql_[V + k];
+    qr[k] = C.endv[0][0] * qr_[k] + C.endv[0][1] * qr_[V + k];
+  }
+  const double kk = (time_dg ? dt * C.w[t] : dt) / (2.0 * dx);
+  if (active) {
+    interface_point_eig<L>(ql, qr, flux, P, C, f, b);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      f[k] = b[k] = 0.0;
+  }
+  double *out = fb + fo * 2 * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double lft = active ? kk * (b[k] + f[k]) : 0.0;
+    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
+    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
+    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
+    if (valid && t == 0) {
+      out[k] = lft;
+      out[V + k] = rgt;
+    }
+  }
+}
+
+}  // namespace gpr

@@ -263,7 +263,13 @@ def test_errors_are_raised(G):
         G.boundaries(u, ub, [16], [0, 9])  # unknown boundary code
     with pytest.raises(TypeError):
         G.boundaries(u.float(), ub, [16], [0, 0])
-    with pytest.raises(RuntimeError):  # Roe is not in this build's flux set
+    with pytest.raises(RuntimeError):  # unknown flux code
         G.solvers.fv.fv_launcher(u, torch.zeros(18 * 4 * 17, dtype=torch.float64, device=DEV),
-                                 [16], 1e-3, dX, True, True, 1, MP,
+                                 [16], 1e-3, dX, True, True, 7, MP,
                                  torch.ones(18, dtype=torch.bool, device=DEV))
+    u2 = torch.zeros(4 * 4 * 17, dtype=torch.float64, device=DEV)
+    with pytest.raises(RuntimeError):  # Roe / Osher are 1D only
+        G.solvers.fv.fv_launcher(u2, torch.zeros(6 * 6 * 8 * 17, dtype=torch.float64,
+                                                 device=DEV),
+                                 [4, 4], 1e-3, [0.1, 0.1], True, True, 1, MP,
+                                 torch.ones(36, dtype=torch.bool, device=DEV))
