@@ -36,7 +36,9 @@ extern "C" {
 #define GPR_E_UNSUPPORTED (-3) /* variant (N, V, flux) not compiled in       */
 #define GPR_E_TOO_LARGE (-4)  /* size beyond a stated fixed maximum          */
 
-/* Flux codes (code/cpp/src/solvers/fv/fluxes.h:7-9). */
+/* Flux codes (code/cpp/src/solvers/fv/fluxes.h:7-9).  Rusanov in 1D and 2D;
+ * Roe and Osher (a 17x17 eigen-decomposition of the system matrix per face
+ * point) on 1D grids, GPR_E_UNSUPPORTED in 2D. */
 #define GPR_FLUX_RUSANOV 0
 #define GPR_FLUX_ROE 1
 #define GPR_FLUX_OSHER 2
@@ -207,6 +209,28 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
                                 double dt, double dx, int stiff, int flux,
                                 const gpr_par *par, const uint8_t *mask,
                                 int32_t *status, int nvar, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Split scheme (the reference driver's default, SPLIT = true):
+ * gpr_midstepper      GPRpy.solvers.split.midstepper (split/homogeneous.h:7):
+ *                     wh -= dt/2 (dF/dx + B dw/dx)/dx [+ y] at the WENO nodes.
+ * gpr_split_stepper   GPRpy.solvers.split_stepper (steppers.h:13-17,
+ *                     steppers.cpp:50-66): ODE half step on u and ub (ub is
+ *                     modified), WENO, midstepper if half_step, FV update on
+ *                     the node values without sources or time integration,
+ *                     ODE half step on u.  scratch: gpr_split_scratch_doubles.
+ * gpr_iterate_split   gpr_iterate with the split scheme in place of the ADER
+ *                     step (iterator.cpp:204-245); scratch: gpr_iterate_scratch_doubles. */
+int gpr_midstepper(double *wh, double dt, const double *dX, int ndim, const int32_t *nX,
+                   const gpr_par *par, const uint8_t *mask, int nvar, void *stream);
+long gpr_split_scratch_doubles(const int32_t *nX, int ndim, int nvar);
+int gpr_split_stepper(double *u, double *ub, const int32_t *nX, int ndim, double dt,
+                      const double *dX, int half_step, int flux, const gpr_par *par,
+                      const uint8_t *mask, double *scratch, int nvar, void *stream);
+int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
+                      const int32_t *bcs, int flux, int half_step, const gpr_par *par,
+                      const uint8_t *mask, double *clock, int nsteps, double *scratch, int nvar,
+                      void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batched form: many independent 1D grids (instances) of uneven sizes, each

@@ -333,6 +333,19 @@ class Oracle:
                             _i(status), int(newton_fallback))
         return u, status
 
+    def midstepper(self, wh, dt, dX, nX, MP, mask=None):
+        """split/homogeneous.cpp:5-67 on a copy of wh (returned)."""
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        ncb = int(np.prod(nX + 2))
+        if mask is None:
+            mask = np.ones(ncb, dtype=np.uint8)
+        w = np.ascontiguousarray(wh, dtype=np.float64).ravel().copy()
+        c, p = self._par(MP)
+        lib.or_midstepper(_d(w), dt, _d(np.asarray(dX, dtype=np.float64)), len(nX), p,
+                          _u8(np.ascontiguousarray(mask, dtype=np.uint8)), ncb)
+        return w
+
     def split_stepper(self, u, ub, nX, dt, dX, MP, mask=None, flux=0,
                       half_step=True):
         lib = self._cfg()

@@ -44,9 +44,11 @@ solvers = SimpleNamespace(
     dg=SimpleNamespace(predictor=api.predictor),
     fv=SimpleNamespace(fv_launcher=api.fv_launcher, D_RUS=api.D_RUS, D_ROE=api.D_ROE,
                        D_OSH=api.D_OSH, Bint=api.Bint),
-    split=SimpleNamespace(ode_launcher=api.ode_launcher),
+    split=SimpleNamespace(ode_launcher=api.ode_launcher, midstepper=api.midstepper),
     ader_stepper=api.ader_stepper,
     ader_stepper_para=api.ader_stepper_para,
+    split_stepper=api.split_stepper,
+    split_stepper_para=api.split_stepper_para,
     timestep=api.timestep,
     renorm_distortion=api.renorm_distortion,
     extended_dimensions=api.extended_dimensions,

@@ -88,6 +88,10 @@ SIGNATURES = {
     "gpr_iterate": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _I, _P]),
     "gpr_ader_stepper_1d_noalloc": (_I, [_P, _P, ctypes.c_int32, _D, _D, _I, _I, _P, _P, _P,
                                          _I, _P]),
+    "gpr_midstepper": (_I, [_P, _D, _P, _I, _P, _P, _P, _I, _P]),
+    "gpr_split_scratch_doubles": (_L, [_P, _I, _I]),
+    "gpr_split_stepper": (_I, [_P, _P, _P, _I, _D, _P, _I, _I, _P, _P, _P, _I, _P]),
+    "gpr_iterate_split": (_I, [_P, _P, _I, _P, _P, _I, _I, _P, _P, _P, _I, _P, _I, _P]),
     "gpr_batch_scratch_doubles": (_L, [_I, _P, _I]),
     "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
     "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),

@@ -192,6 +192,43 @@ def ader_stepper(u, ub, nX, dt, dX, STIFF, FLUX, MP, mask, status=None):
 ader_stepper_para = ader_stepper
 
 
+def midstepper(wh, dt, dX, MP, mask, nX=None):
+    """GPRpy.solvers.split.midstepper (split/homogeneous.h:7): half step of
+    the homogeneous system at the WENO nodes, in place."""
+    lib = _lib.load()
+    dXa, pd = _f64(dX)
+    nd = dXa.size
+    nXa = np.asarray(_grid_from_mask(mask, nd) if nX is None else nX, dtype=np.int32)
+    nXa, pn = _i32(nXa)
+    V = _nvar(wh, int(np.prod(nXa + 2)) * 2 ** nd)
+    pm, _ = _mask_ptr(mask, int(np.prod(nXa + 2)))
+    c, pp = _par(MP)
+    _lib.check(lib.gpr_midstepper(_dev(wh, "wh"), float(dt), pd, nd, pn, pp, pm, V, _stream()),
+               "midstepper")
+    return wh
+
+
+def split_stepper(u, ub, nX, dt, dX, HALF_STEP, FLUX, MP, mask):
+    """GPRpy.solvers.split_stepper (solvers/steppers.cpp:50-66); ub is
+    modified (ODE half step)."""
+    lib = _lib.load()
+    nXa, pn = _i32(nX)
+    set_grid(nXa)
+    dXa, pd = _f64(dX)
+    nd = nXa.size
+    V = _nvar(u, int(np.prod(nXa)))
+    pm, _ = _mask_ptr(mask, int(np.prod(nXa + 2)))
+    c, pp = _par(MP)
+    scr = _scratch(lib.gpr_split_scratch_doubles(pn, nd, V), u)
+    _lib.check(lib.gpr_split_stepper(_dev(u, "u"), _dev(ub, "ub"), pn, nd, float(dt), pd,
+                                     int(bool(HALF_STEP)), int(FLUX), pp, pm, _dev(scr, "s"),
+                                     V, _stream()), "split_stepper")
+    return u
+
+
+split_stepper_para = split_stepper
+
+
 def timestep_device(u, dX, CFL, t, tf, count, MP, out=None):
     """Device form of solvers.timestep: returns a 1-element CUDA tensor."""
     lib = _lib.load()

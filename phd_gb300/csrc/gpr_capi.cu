@@ -310,6 +310,83 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
+  // ---- split scheme (steppers.cpp:50-66, split/homogeneous.cpp) -------------
+  static int midstep(double *wh, double dt, const double *dt_dev, const double *dX, int nd,
+                     const int32_t *nX, const DevPar &P, const uint8_t *mask, cudaStream_t st) {
+    const Consts &C = consts();
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
+    if (nd == 1)
+      k_midstep<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev, idx,
+                                                              idy, P, C);
+    else
+      k_midstep<L, 2><<<blocks(ncb * NN * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev,
+                                                                   idx, idy, P, C);
+    return cuda_rc();
+  }
+
+  // ODE half step on u and ub, WENO, [midstepper], FV without sources and
+  // time integration on the node values, ODE half step on u; ub is modified.
+  // scratch: wh then the WENO / FV temporary.
+  static int split_stepper(double *u, double *ub, const int32_t *nX, int nd, double dt,
+                           const double *dt_dev, const double *dX, int half_step, int flux,
+                           const DevPar &P, const uint8_t *mask, double *scratch,
+                           cudaStream_t st) {
+    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
+    long ns = nd == 1 ? NN : NN * NN;
+    double *wh = scratch, *tmp = wh + ncb * ns * V;
+    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
+    k_ode<L><<<blocks(nub, 128), 128, 0, st>>>(ub, nub, dt / 2, dt_dev, 0.5, P);
+    int rc = weno(wh, ub, nX, nd, tmp, st);
+    if (rc)
+      return rc;
+    if (half_step && (rc = midstep(wh, dt, dt_dev, dX, nd, nX, P, mask, st)))
+      return rc;
+    rc = fv(u, wh, nX, dt, dt_dev, dX, nd, 0, 0, P, mask, tmp, st, flux);
+    if (rc)
+      return rc;
+    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
+    return cuda_rc();
+  }
+
+  static long split_scratch(const int32_t *nX, int nd) {
+    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
+    long ns = nd == 1 ? NN : NN * NN;
+    long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
+    return ncb * ns * V + (w > f ? w : f);
+  }
+
+  // Device-resident iterator with the split scheme (iterator.cpp:204-245,
+  // SPLIT = true); scratch as iterate().
+  static int iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
+                           const int32_t *bcs, const DevPar &P, const uint8_t *mask,
+                           double *clk, int nsteps, double *scratch, int half_step, int flux,
+                           cudaStream_t st) {
+    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
+    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
+    double *ub = scratch;
+    double *rest = ub + nub * V;
+    unsigned long long *mx = (unsigned long long *)(scratch + iterate_scratch(nX, nd) - 1);
+    double *dt_dev = clk + 1;
+    for (int s = 0; s < nsteps; s++) {
+      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
+      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+                                                        nd == 2 ? dX[1] : 1.0, mx, P);
+      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
+      int rc = boundaries(u, ub, nX, nd, bcs, st);
+      if (rc)
+        return rc;
+      rc = split_stepper(u, ub, nX, nd, 0.0, dt_dev, dX, half_step, flux, P, mask, rest, st);
+      if (rc)
+        return rc;
+      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
+      k_clock_advance<<<1, 1, 0, st>>>(clk);
+    }
+    return cuda_rc();
+  }
+
   static long iterate_scratch(const int32_t *nX, int nd) {
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
@@ -619,6 +696,48 @@ long gpr_iterate_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
   if (!check_grid(nX, ndim))
     return GPR_E_ARG;
   DISPATCH(nvar, O::iterate_scratch(nX, ndim))
+}
+
+int gpr_midstepper(double *wh, double dt, const double *dX, int ndim, const int32_t *nX,
+                   const gpr_par *par, const uint8_t *mask, int nvar, void *stream) {
+  if (!wh || !dX || !par || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::midstep(wh, dt, nullptr, dX, ndim, nX, P, mask, S(stream)))
+}
+
+long gpr_split_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
+  if (!check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DISPATCH(nvar, O::split_scratch(nX, ndim))
+}
+
+int gpr_split_stepper(double *u, double *ub, const int32_t *nX, int ndim, double dt,
+                      const double *dX, int half_step, int flux, const gpr_par *par,
+                      const uint8_t *mask, double *scratch, int nvar, void *stream) {
+  if (!u || !ub || !dX || !par || !scratch || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::split_stepper(u, ub, nX, ndim, dt, nullptr, dX, half_step, flux, P, mask,
+                                  scratch, S(stream)))
+}
+
+int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
+                      const int32_t *bcs, int flux, int half_step, const gpr_par *par,
+                      const uint8_t *mask, double *clock, int nsteps, double *scratch, int nvar,
+                      void *stream) {
+  if (!u || !dX || !bcs || !par || !clock || !scratch || nsteps < 0 || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  for (int i = 0; i < 2 * ndim; i++)
+    if (bcs[i] < 0 || bcs[i] > 5)
+      return GPR_E_ARG;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::iterate_split(u, nX, ndim, dX, bcs, P, mask, clock, nsteps, scratch,
+                                  half_step, flux, S(stream)))
 }
 
 int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const int32_t *bcs,

@@ -455,6 +455,79 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
 }
 
 // ---------------------------------------------------------------------------
+// midstepper (split/homogeneous.cpp:5-67): the half step of the homogeneous
+// system at the WENO nodes before the split scheme's FV update,
+//   w_s -= dt/2 ((dF/dx + B_x dw/dx) / dx [+ (dG/dy + B_y dw/dy) / dy]),
+// derivatives by DERVALS within the cell.  One thread per spatial node, the
+// cell's NS = N^d lanes adjacent (x partner lane ^ (ND == 1 ? 1 : 2), y
+// partner lane ^ 1).
+template <class L, int ND>
+__global__ void __launch_bounds__(128) k_midstep(double *__restrict__ wh, long ncb,
+                                                 const uint8_t *__restrict__ mask, double dt,
+                                                 const double *__restrict__ dt_dev, double idx,
+                                                 double idy, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  constexpr int NS = ND == 1 ? NN : NN * NN;
+  constexpr int XB = ND == 1 ? 1 : 2, YB = 1;
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int g = threadIdx.x % NS;
+  const long c = gt / NS;
+  const bool valid = c < ncb;
+  const long cc = valid ? c : 0;
+  const bool active = valid && (mask == nullptr || mask[cc]);
+  const int a = ND == 1 ? g : g / NN, b = ND == 1 ? 0 : g % NN;
+  double w[V], F[V], other[V], dw[V], inc[V];
+  double *wc = wh + (cc * NS + g) * V;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    w[k] = wc[k];
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(w, P, s);
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    F[k] = 0.0;
+  flux_add<L::THERMAL, V>(w, s, 0, P, F);
+  // x: d/dx of w and F over the x partner
+  {
+    const double ca = C.derv[a][a], cb = C.derv[a][1 - a];
+    shfl_vec<V>(w, other, XB);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      dw[k] = ca * w[k] + cb * other[k];
+    shfl_vec<V>(F, other, XB);
+    double bd[V];
+    bdot<V, L::LSET>(s.v, dw, 0, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      inc[k] = ((ca * F[k] + cb * other[k]) + bd[k]) * idx;
+  }
+  if (ND == 2) {
+    const double ca = C.derv[b][b], cb = C.derv[b][1 - b];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      F[k] = 0.0;
+    flux_add<L::THERMAL, V>(w, s, 1, P, F);
+    shfl_vec<V>(w, other, YB);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      dw[k] = ca * w[k] + cb * other[k];
+    shfl_vec<V>(F, other, YB);
+    double bd[V];
+    bdot<V, L::LSET>(s.v, dw, 1, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      inc[k] += ((ca * F[k] + cb * other[k]) + bd[k]) * idy;
+  }
+  if (active) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      wc[k] = w[k] - dt / 2 * inc[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Stiff-source Newton pass for the cells whose Picard iteration failed (the
 // reference leaves their rows unwritten, dg1.cpp:108-127, or falls back to a
 // Jacobian-free Newton-Krylov solve on NaN, dg1.cpp:117-121).

@@ -1,7 +1,8 @@
 """Time loop of the reference's `solvers.iterator` (code/cpp/src/solvers/
 iterator.cpp:179-264) for one material, on the GPU: CFL time step ->
-boundaries -> ADER step -> distortion renormalisation, with the reference's
-100-snapshot return convention and NaN early exit."""
+boundaries -> ADER step (or the split scheme, SPLIT = True) -> distortion
+renormalisation, with the reference's 100-snapshot return convention and NaN
+early exit."""
 import numpy as np
 import torch
 
@@ -26,10 +27,13 @@ class Stepper:
         self.status = torch.zeros(ncb, dtype=torch.int32, device=device)
         self.dt = torch.empty(1, dtype=torch.float64, device=device)
 
-    def step(self, u, dt, dX, bcs, MP, flux=0, stiff=False):
+    def step(self, u, dt, dX, bcs, MP, flux=0, stiff=False, split=False, half_step=True):
         api.boundaries(u, self.ub, self.nX, bcs)
-        api.ader_stepper(u, self.ub, self.nX, dt, dX, stiff, flux, MP, self.mask,
-                         status=self.status)
+        if split:
+            api.split_stepper(u, self.ub, self.nX, dt, dX, half_step, flux, MP, self.mask)
+        else:
+            api.ader_stepper(u, self.ub, self.nX, dt, dX, stiff, flux, MP, self.mask,
+                             status=self.status)
         api.renorm_distortion(u, [MP])
         return u
 
@@ -47,9 +51,8 @@ def iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT=False, HALF_STEP=True, STIF
     while t < tf:
         uprev = uf.clone()
         dt = float(api.timestep_device(uf, dX, CFL, t, tf, count, MP, out=st.dt).item())
-        if SPLIT:
-            raise NotImplementedError("split stepper not available on the GPU path yet")
-        st.step(uf, dt, dX, boundaryTypes, MP, flux=FLUX, stiff=STIFF)
+        st.step(uf, dt, dX, boundaryTypes, MP, flux=FLUX, stiff=STIFF, split=SPLIT,
+                half_step=HALF_STEP)
         t += dt
         count += 1
         if t >= (push + 1) / 100.0 * tf:
