@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
+    ap.add_argument("--profile-shock-tube", type=int, default=-1, metavar="FLUX",
+                    help="with --profile-steps K: K steps of the 200-cell shock tube with "
+                         "flux FLUX (0 Rusanov, 1 Roe, 2 Osher) through gpr_iterate, no JSON")
     ap.add_argument("--profile-adjoint", type=int, default=0, metavar="NINST",
                     help="with --profile-steps K: K steps of the Stokes differentiation "
                          "problem for NINST instances, forward then backward (for ncu "
@@ -783,12 +786,40 @@ def profile_adjoint(ninst, steps):
     return 0
 
 
+def profile_shock_tube(flux, steps):
+    """`steps` steps of the 200-cell shock tube through gpr_iterate (for ncu
+    captures)."""
+    import torch
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=200)
+    nx = np.array([200], np.int32)
+    dxa = np.array(dX, np.float64)
+    bca = np.array([0, 0], np.int32)
+    cp = MP.to_ctypes()
+    scr = torch.empty(lib.gpr_iterate_scratch_doubles(nx.ctypes.data_as(ctypes.c_void_p), 1, 17),
+                      dtype=torch.float64, device="cuda")
+    ut = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+    clk = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
+    _lib.check(lib.gpr_iterate(
+        ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+        dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
+        ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None, ctypes.c_void_p(clk.data_ptr()),
+        steps, ctypes.c_void_p(scr.data_ptr()), None, 17,
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "iterate")
+    torch.cuda.synchronize()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_adjoint:
         return profile_adjoint(args.profile_adjoint, args.profile_steps or 32)
+    if args.profile_shock_tube >= 0:
+        return profile_shock_tube(args.profile_shock_tube, args.profile_steps or 10)
     return run_gb300(args)
 
 

@@ -191,9 +191,8 @@ template <class L> struct Ops {
         k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
                                                        dt_dev, dX[0], time_dg, P, C, Batch{});
       else
-        k_faces1d_eig<L><<<blocks(nf, 64), 64, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
-                                                         dt_dev, dX[0], time_dg, flux, P, C,
-                                                         Batch{});
+        k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
+            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
       long nc = (long)nx * NN * NN;
       k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
                                                       dt_dev, dX[0], 1.0, sources, time_dg, P,
@@ -229,9 +228,8 @@ template <class L> struct Ops {
         k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
                                                        dX[0], time_dg, P, C, Batch{});
       else
-        k_faces1d_eig<L><<<blocks(nf, 64), 64, 0, st>>>(fb, qh, (long)nx + 1, mask, dt,
-                                                         nullptr, dX[0], time_dg, flux, P, C,
-                                                         Batch{});
+        k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
+            fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, flux, P, C, Batch{});
       return cuda_rc();
     }
     int ny = nX[1];

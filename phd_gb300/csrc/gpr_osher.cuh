@@ -23,15 +23,10 @@ constexpr double OSH_MULT_TOL = 1e-12;
 
 // System matrix M = dF_x/dP dP/dQ + B_x (equations.cpp:68-187, 269-276):
 // row-major V x V into M (ld = V).
+// dF_x/dP into F and dP/dQ into D (V x V row-major, zeroed by the caller).
 template <bool TH, int V>
-GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, double *M) {
+GPR_D void system_fd(const double *Q, const Prim<TH> &s, const DevPar &P, double *F, double *D) {
   constexpr int d = 0;
-  double F[V * V], D[V * V];
-#pragma unroll 1
-  for (int i = 0; i < V * V; i++) {
-    F[i] = 0.0;
-    D[i] = 0.0;
-  }
 #define RF(i, j) F[(i) * V + (j)]
 #define RD(i, j) D[(i) * V + (j)]
   const double r = s.r, ir = s.ir;
@@ -182,6 +177,31 @@ GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, do
   }
 #undef RF
 #undef RD
+}
+
+// M += the non-conservative block B_x (equations.cpp:169-187)
+template <int V> GPR_D void system_block(const double *v, double *M) {
+  constexpr int d = 0;
+#pragma unroll
+  for (int i = 5; i < 14; i++)
+    M[i * V + i] += v[d];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    M[(5 + d) * V + 5 + i] -= v[i];
+    M[(8 + d) * V + 8 + i] -= v[i];
+    M[(11 + d) * V + 11 + i] -= v[i];
+  }
+}
+
+template <bool TH, int V>
+GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, double *M) {
+  double F[V * V], D[V * V];
+#pragma unroll 1
+  for (int i = 0; i < V * V; i++) {
+    F[i] = 0.0;
+    D[i] = 0.0;
+  }
+  system_fd<TH, V>(Q, s, P, F, D);
 #pragma unroll 1
   for (int i = 0; i < V; i++)
 #pragma unroll 1
@@ -192,16 +212,7 @@ GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, do
         acc += F[i * V + k] * D[k * V + j];
       M[i * V + j] = acc;
     }
-  // block (equations.cpp:169-187): the non-conservative product B_x
-#pragma unroll
-  for (int i = 5; i < 14; i++)
-    M[i * V + i] += vd;
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    M[(5 + d) * V + 5 + i] -= v[i];
-    M[(8 + d) * V + 8 + i] -= v[i];
-    M[(11 + d) * V + 11 + i] -= v[i];
-  }
+  system_block<V>(s.v, M);
 }
 
 // Householder reduction of H (n x n, ld n) to upper Hessenberg form,
@@ -810,6 +821,711 @@ __global__ void __launch_bounds__(64) k_faces1d_eig(
     if (valid && t == 0) {
       out[k] = lft;
       out[V + k] = rgt;
+    }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative form: one warp per eigenproblem, matrices in shared
+// memory.  The QR iteration's control flow (deflation tests, shifts) is
+// evaluated identically by every lane from shared memory; the row, column
+// and Schur-vector updates of each step are spread over the lanes; the
+// eigenvectors are one lane each; the complex solve eliminates one row per
+// lane.  The arithmetic of every element update is the serial one.
+
+// Per-warp workspace.  After the eigenvectors are formed, H and Z (the
+// Schur form and vectors) are no longer needed and hold the copy of the
+// eigenvector matrix that the complex solve factorises; before the
+// eigen-decomposition Rr and Ri hold dF/dP and dP/dQ.
+template <int n> struct EigWS {
+  double H[n * n], Z[n * n], Rr[n * n], Ri[n * n];
+  double wr[n], wi[n], v[n], br[n], bi[n];
+  double q[n], ql[n], qr[n], dq[n], f[n];
+};
+
+GPR_D double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+template <int n> GPR_D void w_hess(double *H, double *Z, double *v, int lane) {
+#pragma unroll 1
+  for (int k = 0; k < n - 2; k++) {
+    double a2 = 0.0;
+    for (int i = k + 1 + lane; i < n; i += 32)
+      a2 += H[i * n + k] * H[i * n + k];
+    const double alpha = sqrt(warp_sum(a2));
+    if (alpha == 0.0)
+      continue;
+    const double x0 = H[(k + 1) * n + k];
+    const double beta = x0 > 0 ? -alpha : alpha;
+    double t2 = 0.0;
+    for (int i = k + 2 + lane; i < n; i += 32)
+      t2 += H[i * n + k] * H[i * n + k];
+    const double vv = (x0 - beta) * (x0 - beta) + warp_sum(t2);
+    if (vv == 0.0)
+      continue;
+    for (int i = lane; i < n; i += 32)
+      v[i] = i <= k ? 0.0 : (i == k + 1 ? x0 - beta : H[i * n + k]);
+    __syncwarp();
+    const double tau = 2.0 / vv;
+    for (int j = lane; j < n; j += 32) {  // (I - tau v v^T) H, column j
+      double s = 0.0;
+      for (int i = k + 1; i < n; i++)
+        s += v[i] * H[i * n + j];
+      s *= tau;
+      for (int i = k + 1; i < n; i++)
+        H[i * n + j] -= s * v[i];
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {  // H (I - tau v v^T), row i; Z the same
+      double s = 0.0;
+      for (int j = k + 1; j < n; j++)
+        s += H[i * n + j] * v[j];
+      s *= tau;
+      for (int j = k + 1; j < n; j++)
+        H[i * n + j] -= s * v[j];
+      double sz = 0.0;
+      for (int j = k + 1; j < n; j++)
+        sz += Z[i * n + j] * v[j];
+      sz *= tau;
+      for (int j = k + 1; j < n; j++)
+        Z[i * n + j] -= sz * v[j];
+    }
+    __syncwarp();
+    for (int i = k + 2 + lane; i < n; i += 32)
+      H[i * n + k] = 0.0;
+    __syncwarp();
+  }
+}
+
+template <int n> GPR_D bool w_hqr(double *H, double *Z, double *wr, double *wi, int lane) {
+  const double eps = 2.220446049250313e-16;
+  double nrm = 0.0;
+  for (int e = lane; e < n * n; e += 32) {
+    int i = e / n, j = e % n;
+    if (j >= i - 1)
+      nrm += fabs(H[e]);
+  }
+  const double norm = warp_sum(nrm);
+  int hi = n - 1, iter = 0, total = 0;
+  double exshift = 0.0;
+  while (hi >= 0) {
+    int l = hi;
+    while (l > 0) {
+      double s = fabs(H[(l - 1) * n + l - 1]) + fabs(H[l * n + l]);
+      if (s == 0.0)
+        s = norm;
+      if (fabs(H[l * n + l - 1]) < eps * s)
+        break;
+      l--;
+    }
+    if (l == hi) {
+      __syncwarp();
+      if (lane == 0) {
+        H[hi * n + hi] += exshift;
+        wr[hi] = H[hi * n + hi];
+        wi[hi] = 0.0;
+        if (hi > 0)
+          H[hi * n + hi - 1] = 0.0;
+      }
+      __syncwarp();
+      hi--;
+      iter = 0;
+      continue;
+    }
+    double x = H[hi * n + hi];
+    double y = H[(hi - 1) * n + hi - 1];
+    double w = H[hi * n + hi - 1] * H[(hi - 1) * n + hi];
+    if (l == hi - 1) {
+      double p = 0.5 * (y - x);
+      double q = p * p + w;
+      if (q < 0.0 && sqrt(-q) <= OSH_MULT_TOL * norm)
+        q = 0.0;
+      double z = sqrt(fabs(q));
+      __syncwarp();
+      if (lane == 0) {
+        if (hi >= 2)
+          H[(hi - 1) * n + hi - 2] = 0.0;
+        H[hi * n + hi] = x + exshift;
+        H[(hi - 1) * n + hi - 1] = y + exshift;
+      }
+      __syncwarp();
+      x = H[hi * n + hi];
+      if (q >= 0.0) {
+        z = p >= 0 ? p + z : p - z;
+        const double xx = H[hi * n + hi - 1];
+        const double s = fabs(xx) + fabs(z);
+        double pp = xx / s, qq = z / s;
+        const double rr = sqrt(pp * pp + qq * qq);
+        pp /= rr;
+        qq /= rr;
+        __syncwarp();
+        if (lane == 0) {
+          wr[hi - 1] = x + z;
+          wr[hi] = z != 0.0 ? x - w / z : x + z;
+          wi[hi - 1] = wi[hi] = 0.0;
+        }
+        for (int j = hi - 1 + lane; j < n; j += 32) {
+          const double a = H[(hi - 1) * n + j];
+          H[(hi - 1) * n + j] = qq * a + pp * H[hi * n + j];
+          H[hi * n + j] = qq * H[hi * n + j] - pp * a;
+        }
+        __syncwarp();
+        for (int i = lane; i <= hi; i += 32) {
+          const double a = H[i * n + hi - 1];
+          H[i * n + hi - 1] = qq * a + pp * H[i * n + hi];
+          H[i * n + hi] = qq * H[i * n + hi] - pp * a;
+        }
+        for (int i = lane; i < n; i += 32) {
+          const double a = Z[i * n + hi - 1];
+          Z[i * n + hi - 1] = qq * a + pp * Z[i * n + hi];
+          Z[i * n + hi] = qq * Z[i * n + hi] - pp * a;
+        }
+        __syncwarp();
+        if (lane == 0)
+          H[hi * n + hi - 1] = 0.0;
+      } else if (lane == 0) {
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = z;
+        wi[hi] = -z;
+      }
+      __syncwarp();
+      hi -= 2;
+      iter = 0;
+      continue;
+    }
+    if (iter == 10 || iter == 20) {
+      exshift += x;
+      __syncwarp();
+      for (int i = lane; i <= hi; i += 32)
+        H[i * n + i] -= x;
+      __syncwarp();
+      const double s = fabs(H[hi * n + hi - 1]) + fabs(H[(hi - 1) * n + hi - 2]);
+      x = y = 0.75 * s;
+      w = -0.4375 * s * s;
+    }
+    iter++;
+    total++;
+    if (total > 60 * n)
+      return false;
+    // the scalar search runs on lane 0 and is broadcast (the other lanes
+    // would only repeat it)
+    int m = hi - 2;
+    double p = 0, q = 0, r = 0, z;
+    if (lane == 0) {
+      while (m >= l) {
+        z = H[m * n + m];
+        r = x - z;
+        double s = y - z;
+        p = (r * s - w) / H[(m + 1) * n + m] + H[m * n + m + 1];
+        q = H[(m + 1) * n + m + 1] - z - r - s;
+        r = H[(m + 2) * n + m + 1];
+        s = fabs(p) + fabs(q) + fabs(r);
+        p /= s;
+        q /= s;
+        r /= s;
+        if (m == l)
+          break;
+        const double u = fabs(H[m * n + m - 1]) * (fabs(q) + fabs(r));
+        const double vv =
+            fabs(p) * (fabs(H[(m - 1) * n + m - 1]) + fabs(z) + fabs(H[(m + 1) * n + m + 1]));
+        if (u < eps * vv)
+          break;
+        m--;
+      }
+    }
+    m = __shfl_sync(0xffffffffu, m, 0);
+    p = __shfl_sync(0xffffffffu, p, 0);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    __syncwarp();
+    for (int i = m + 2 + lane; i <= hi; i += 32) {
+      H[i * n + i - 2] = 0.0;
+      if (i > m + 2)
+        H[i * n + i - 3] = 0.0;
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int k = m; k <= hi - 1; k++) {
+      const bool notlast = (k != hi - 1);
+      int skip = 0;
+      __syncwarp();
+      if (lane == 0) {
+        if (k != m) {
+          p = H[k * n + k - 1];
+          q = H[(k + 1) * n + k - 1];
+          r = notlast ? H[(k + 2) * n + k - 1] : 0.0;
+          x = fabs(p) + fabs(q) + fabs(r);
+          if (x == 0.0) {
+            skip = 1;
+          } else {
+            p /= x;
+            q /= x;
+            r /= x;
+          }
+        }
+        if (!skip) {
+          double s = sqrt(p * p + q * q + r * r);
+          if (p < 0)
+            s = -s;
+          if (k != m)
+            H[k * n + k - 1] = -s * x;
+          else if (l != m)
+            H[k * n + k - 1] = -H[k * n + k - 1];
+          p += s;
+          x = p / s;
+          y = q / s;
+          z = r / s;
+          q /= p;
+          r /= p;
+        }
+      }
+      skip = __shfl_sync(0xffffffffu, skip, 0);
+      if (skip)
+        continue;
+      p = __shfl_sync(0xffffffffu, p, 0);
+      q = __shfl_sync(0xffffffffu, q, 0);
+      r = __shfl_sync(0xffffffffu, r, 0);
+      x = __shfl_sync(0xffffffffu, x, 0);
+      y = __shfl_sync(0xffffffffu, y, 0);
+      z = __shfl_sync(0xffffffffu, z, 0);
+      for (int j = k + lane; j < n; j += 32) {  // rows
+        double pp = H[k * n + j] + q * H[(k + 1) * n + j];
+        if (notlast) {
+          pp += r * H[(k + 2) * n + j];
+          H[(k + 2) * n + j] -= pp * z;
+        }
+        H[k * n + j] -= pp * x;
+        H[(k + 1) * n + j] -= pp * y;
+      }
+      __syncwarp();
+      const int ihi = hi < k + 3 ? hi : k + 3;
+      for (int i = lane; i <= ihi; i += 32) {  // columns
+        double pp = x * H[i * n + k] + y * H[i * n + k + 1];
+        if (notlast) {
+          pp += z * H[i * n + k + 2];
+          H[i * n + k + 2] -= pp * r;
+        }
+        H[i * n + k] -= pp;
+        H[i * n + k + 1] -= pp * q;
+      }
+      for (int i = lane; i < n; i += 32) {
+        double pp = x * Z[i * n + k] + y * Z[i * n + k + 1];
+        if (notlast) {
+          pp += z * Z[i * n + k + 2];
+          Z[i * n + k + 2] -= pp * r;
+        }
+        Z[i * n + k] -= pp;
+        Z[i * n + k + 1] -= pp * q;
+      }
+      __syncwarp();
+    }
+  }
+  return true;
+}
+
+// eigenvector k on lane k (k < n); T quasi-triangular Schur form, Z vectors
+template <int n>
+GPR_D void w_schur_vectors(const double *T, const double *Z, const double *wr,
+                           const double *wi, double *Rr, double *Ri, int lane) {
+  double nrm = 0.0;
+  for (int e = lane; e < n * n; e += 32) {
+    int i = e / n, j = e % n;
+    if (j >= i - 1)
+      nrm += fabs(T[e]);
+  }
+  const double norm = warp_sum(nrm);
+  const int k = lane;
+  if (k < n) {
+    const double lr = wr[k], li = wi[k];
+    double yr[n], yi[n];
+#pragma unroll 1
+    for (int i = 0; i < n; i++)
+      yr[i] = yi[i] = 0.0;
+    const bool blk2 = (k + 1 < n && T[(k + 1) * n + k] != 0.0);
+    const bool blk1 = (k > 0 && T[k * n + k - 1] != 0.0);
+    int top;
+    if (!blk1 && !blk2) {
+      yr[k] = 1.0;
+      top = k;
+    } else {
+      const int b = blk2 ? k : k - 1;
+      const double a11 = T[b * n + b] - lr, a12 = T[b * n + b + 1];
+      const double a21 = T[(b + 1) * n + b];
+      if (fabs(a12) >= fabs(a21)) {
+        yr[b] = 1.0;
+        yi[b] = 0.0;
+        yr[b + 1] = -a11 / a12;
+        yi[b + 1] = li / a12;
+      } else {
+        const double a22r = T[(b + 1) * n + b + 1] - lr;
+        yr[b + 1] = 1.0;
+        yi[b + 1] = 0.0;
+        yr[b] = -a22r / a21;
+        yi[b] = li / a21;
+      }
+      top = b + 1;
+    }
+    const int start = (blk1 || blk2) ? (blk2 ? k - 1 : k - 2) : k - 1;
+#pragma unroll 1
+    for (int i = start; i >= 0; i--) {
+      const bool is2 = (i > 0 && T[i * n + i - 1] != 0.0);
+      if (!is2) {
+        double sr = 0.0, si = 0.0;
+#pragma unroll 1
+        for (int j = i + 1; j <= top; j++) {
+          sr += T[i * n + j] * yr[j];
+          si += T[i * n + j] * yi[j];
+        }
+        const double dr = T[i * n + i] - lr, di = -li;
+        if (hypot(dr, di) <= OSH_MULT_TOL * norm) {
+          yr[i] = yi[i] = 0.0;
+          continue;
+        }
+        const double den = dr * dr + di * di;
+        yr[i] = -(sr * dr + si * di) / den;
+        yi[i] = -(si * dr - sr * di) / den;
+      } else {
+        const int a = i - 1;
+        double s1r = 0, s1i = 0, s2r = 0, s2i = 0;
+#pragma unroll 1
+        for (int j = i + 1; j <= top; j++) {
+          s1r += T[a * n + j] * yr[j];
+          s1i += T[a * n + j] * yi[j];
+          s2r += T[i * n + j] * yr[j];
+          s2i += T[i * n + j] * yi[j];
+        }
+        const double m11r = T[a * n + a] - lr, m11i = -li;
+        const double m12 = T[a * n + i], m21 = T[i * n + a];
+        const double m22r = T[i * n + i] - lr, m22i = -li;
+        const double detr = m11r * m22r - m11i * m22i - m12 * m21;
+        const double deti = m11r * m22i + m11i * m22r;
+        if (hypot(detr, deti) <= OSH_MULT_TOL * norm * OSH_MULT_TOL * norm) {
+          yr[a] = yi[a] = yr[i] = yi[i] = 0.0;
+          i--;
+          continue;
+        }
+        const double den = detr * detr + deti * deti;
+        const double nar = -(s1r * m22r - s1i * m22i) + m12 * s2r;
+        const double nai = -(s1r * m22i + s1i * m22r) + m12 * s2i;
+        const double nir = -(m11r * s2r - m11i * s2i) + m21 * s1r;
+        const double nii = -(m11r * s2i + m11i * s2r) + m21 * s1i;
+        yr[a] = (nar * detr + nai * deti) / den;
+        yi[a] = (nai * detr - nar * deti) / den;
+        yr[i] = (nir * detr + nii * deti) / den;
+        yi[i] = (nii * detr - nir * deti) / den;
+        i--;
+      }
+    }
+#pragma unroll 1
+    for (int i = 0; i < n; i++) {
+      double sr = 0.0, si = 0.0;
+#pragma unroll 1
+      for (int j = 0; j <= top; j++) {
+        sr += Z[i * n + j] * yr[j];
+        si += Z[i * n + j] * yi[j];
+      }
+      Rr[i * n + k] = sr;
+      Ri[i * n + k] = si;
+    }
+  }
+  __syncwarp();
+}
+
+template <int n>
+GPR_D bool w_csolve(double *Cr, double *Ci, double *br, double *bi, int lane) {
+#pragma unroll 1
+  for (int c = 0; c < n; c++) {
+    double best = -1.0;
+    int p = c;
+    for (int r = c + lane; r < n; r += 32) {
+      const double a = hypot(Cr[r * n + c], Ci[r * n + c]);
+      if (a > best) {
+        best = a;
+        p = r;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int op = __shfl_xor_sync(0xffffffffu, p, o);
+      if (ob > best || (ob == best && op < p)) {
+        best = ob;
+        p = op;
+      }
+    }
+    if (best == 0.0)
+      return false;
+    __syncwarp();
+    if (p != c) {
+      for (int j = lane; j < n; j += 32) {
+        double t = Cr[c * n + j];
+        Cr[c * n + j] = Cr[p * n + j];
+        Cr[p * n + j] = t;
+        t = Ci[c * n + j];
+        Ci[c * n + j] = Ci[p * n + j];
+        Ci[p * n + j] = t;
+      }
+      if (lane == 0) {
+        double t = br[c];
+        br[c] = br[p];
+        br[p] = t;
+        t = bi[c];
+        bi[c] = bi[p];
+        bi[p] = t;
+      }
+    }
+    __syncwarp();
+    const double pr = Cr[c * n + c], pi = Ci[c * n + c];
+    const double den = pr * pr + pi * pi;
+    for (int r = c + 1 + lane; r < n; r += 32) {
+      const double ar = Cr[r * n + c], ai = Ci[r * n + c];
+      const double fr = (ar * pr + ai * pi) / den, fi = (ai * pr - ar * pi) / den;
+      for (int j = c; j < n; j++) {
+        const double xr = Cr[c * n + j], xi = Ci[c * n + j];
+        Cr[r * n + j] -= fr * xr - fi * xi;
+        Ci[r * n + j] -= fr * xi + fi * xr;
+      }
+      br[r] -= fr * br[c] - fi * bi[c];
+      bi[r] -= fr * bi[c] + fi * br[c];
+    }
+    __syncwarp();
+  }
+#pragma unroll 1
+  for (int r = n - 1; r >= 0; r--) {
+    double sr = 0.0, si = 0.0;
+    for (int j = r + 1 + lane; j < n; j += 32) {
+      sr += Cr[r * n + j] * br[j] - Ci[r * n + j] * bi[j];
+      si += Cr[r * n + j] * bi[j] + Ci[r * n + j] * br[j];
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) {
+      const double xr = br[r] - sr, xi = bi[r] - si;
+      const double pr = Cr[r * n + r], pi = Ci[r * n + r];
+      const double den = pr * pr + pi * pi;
+      br[r] = (xr * pr + xi * pi) / den;
+      bi[r] = (xi * pr - xr * pi) / den;
+    }
+    __syncwarp();
+  }
+  return true;
+}
+
+// ws.f += w R |Lambda| R^-1 ws.dq for the matrix in ws.H (destroyed)
+template <int n> GPR_D bool w_abs_apply(EigWS<n> &ws, double w, int lane) {
+  for (int e = lane; e < n * n; e += 32)
+    ws.Z[e] = (e % (n + 1) == 0) ? 1.0 : 0.0;
+  __syncwarp();
+  w_hess<n>(ws.H, ws.Z, ws.v, lane);
+  if (!w_hqr<n>(ws.H, ws.Z, ws.wr, ws.wi, lane))
+    return false;
+  __syncwarp();
+  w_schur_vectors<n>(ws.H, ws.Z, ws.wr, ws.wi, ws.Rr, ws.Ri, lane);
+  double *Cr = ws.H, *Ci = ws.Z;
+  for (int e = lane; e < n * n; e += 32) {
+    Cr[e] = ws.Rr[e];
+    Ci[e] = ws.Ri[e];
+  }
+  for (int k = lane; k < n; k += 32) {
+    ws.br[k] = ws.dq[k];
+    ws.bi[k] = 0.0;
+  }
+  __syncwarp();
+  if (!w_csolve<n>(Cr, Ci, ws.br, ws.bi, lane))
+    return false;
+  for (int k = lane; k < n; k += 32) {
+    const double a = hypot(ws.wr[k], ws.wi[k]);
+    ws.br[k] *= a;
+    ws.bi[k] *= a;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) {
+    double s = 0.0;
+    for (int k = 0; k < n; k++)
+      s += ws.Rr[i * n + k] * ws.br[k] - ws.Ri[i * n + k] * ws.bi[k];
+    ws.f[i] += w * s;
+  }
+  __syncwarp();
+  return true;
+}
+
+// ws.H = M(ws.q) (system matrix); F and D are built in ws.Rr / ws.Ri by lane
+// 0, their product formed by all lanes.
+template <class L> GPR_D void w_system_matrix(EigWS<L::V> &ws, const DevPar &P, int lane) {
+  constexpr int V = L::V;
+  for (int e = lane; e < V * V; e += 32) {
+    ws.Rr[e] = 0.0;
+    ws.Ri[e] = 0.0;
+  }
+  __syncwarp();
+  double vloc[3];
+  if (lane == 0) {
+    double q[V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      q[k] = ws.q[k];
+    Prim<L::THERMAL> s;
+    prim<L::THERMAL>(q, P, s);
+    system_fd<L::THERMAL, V>(q, s, P, ws.Rr, ws.Ri);
+    ws.v[0] = s.v[0];
+    ws.v[1] = s.v[1];
+    ws.v[2] = s.v[2];
+  }
+  __syncwarp();
+  for (int e = lane; e < V * V; e += 32) {
+    const int i = e / V, j = e % V;
+    double acc = 0.0;
+    for (int k = 0; k < V; k++)
+      acc += ws.Rr[i * V + k] * ws.Ri[k * V + j];
+    ws.H[e] = acc;
+  }
+  vloc[0] = ws.v[0];
+  vloc[1] = ws.v[1];
+  vloc[2] = ws.v[2];
+  __syncwarp();
+  if (lane == 0)
+    system_block<V>(vloc, ws.H);
+  __syncwarp();
+}
+
+// 1D faces with the Osher or Roe dissipation: one block per face, one warp
+// per eigen-decomposition: warp w = t * NPATH + i handles time node t and,
+// for Osher, path node i (NPATH = 2; Roe averages the path's matrices in one
+// warp, NPATH = 1).  The contributions are summed in the serial order (path
+// nodes, then time nodes); output as k_faces1d.
+constexpr int EIG_WARPS = 4;
+
+template <class L, bool BATCH = false>
+__global__ void __launch_bounds__(32 * EIG_WARPS) k_faces1d_eigw(
+    double *__restrict__ fb, const double *__restrict__ qh, long nface,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int time_dg, int flux, DevPar Pv, Consts C, Batch B) {
+  constexpr int V = L::V;
+  __shared__ EigWS<V> wsa[EIG_WARPS];
+  __shared__ double part[NN][2][V];
+  if (dt_dev)
+    dt = *dt_dev;
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const long face = blockIdx.x;
+  if (face >= nface)
+    return;  // block-uniform
+  long fi = face;
+  const int inst = BATCH ? B.inst_f[face] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    fi = B.off_b[inst] + (face - B.off_f[inst]);
+    dt = B.clk[5 * inst + 1];
+    dx = 1.0 / B.idx[inst];
+  }
+  const bool active = mask == nullptr || (mask[fi] && mask[fi + 1]);
+  const int nt = time_dg ? NN : 1;
+  const int npath = flux == GPR_FLUX_OSHER ? NN : 1;
+  const int t = wid / npath, ip = wid % npath;
+  const bool mine = active && t < nt;  // warp-uniform
+  EigWS<V> &ws = wsa[wid];
+  if (mine) {
+    const double *ql_ = qh + (fi * nt + t) * NN * V;
+    const double *qr_ = qh + ((fi + 1) * nt + t) * NN * V;
+    for (int k = lane; k < V; k += 32) {
+      ws.ql[k] = C.endv[1][0] * ql_[k] + C.endv[1][1] * ql_[V + k];
+      ws.qr[k] = C.endv[0][0] * qr_[k] + C.endv[0][1] * qr_[V + k];
+      ws.dq[k] = ws.ql[k] - ws.qr[k];
+      ws.f[k] = 0.0;
+    }
+    __syncwarp();
+    bool ok;
+    if (flux == GPR_FLUX_OSHER) {
+      for (int k = lane; k < V; k += 32)
+        ws.q[k] = ws.qr[k] + C.nodes[ip] * ws.dq[k];
+      __syncwarp();
+      w_system_matrix<L>(ws, P, lane);
+      ok = w_abs_apply<V>(ws, C.w[ip], lane);
+    } else {
+      // Roe: the path-averaged matrix, accumulated in Z
+      for (int e = lane; e < V * V; e += 32)
+        ws.Z[e] = 0.0;
+#pragma unroll 1
+      for (int i = 0; i < NN; i++) {
+        for (int k = lane; k < V; k += 32)
+          ws.q[k] = ws.qr[k] + C.nodes[i] * ws.dq[k];
+        __syncwarp();
+        w_system_matrix<L>(ws, P, lane);
+        for (int e = lane; e < V * V; e += 32)
+          ws.Z[e] += C.w[i] * ws.H[e];
+        __syncwarp();
+      }
+      for (int e = lane; e < V * V; e += 32)
+        ws.H[e] = ws.Z[e];
+      __syncwarp();
+      ok = w_abs_apply<V>(ws, 1.0, lane);
+    }
+    if (!ok) {
+      for (int k = lane; k < V; k += 32)
+        ws.f[k] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+  }
+  __syncthreads();
+  // warp t (path node 0) finishes time node t: D + F(qL) + F(qR) and Bint
+  if (mine && ip == 0 && lane == 0) {
+    double ql[V], qr[V], f[V], b[V], dq[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      ql[k] = ws.ql[k];
+      qr[k] = ws.qr[k];
+      double acc = 0.0;
+      for (int i = 0; i < npath; i++)
+        acc += wsa[t * npath + i].f[k];
+      f[k] = acc;
+    }
+    Prim<L::THERMAL> sl, sr;
+    prim<L::THERMAL>(ql, P, sl);
+    prim<L::THERMAL>(qr, P, sr);
+    flux_add<L::THERMAL, V>(ql, sl, 0, P, f);
+    flux_add<L::THERMAL, V>(qr, sr, 0, P, f);
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      dq[k] = qr[k] - ql[k];
+      b[k] = 0.0;
+    }
+#pragma unroll
+    for (int nn = 0; nn < NN; nn++) {
+      const double rho = ql[0] + C.nodes[nn] * dq[0];
+      const double ir = 1.0 / rho;
+      const double v[3] = {(ql[2] + C.nodes[nn] * dq[2]) * ir, (ql[3] + C.nodes[nn] * dq[3]) * ir,
+                           (ql[4] + C.nodes[nn] * dq[4]) * ir};
+      double bd[V];
+      bdot<V, L::LSET>(v, dq, 0, bd);
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        b[k] += C.w[nn] * bd[k];
+    }
+    const double kk = (time_dg ? dt * C.w[t] : dt) / (2.0 * dx);
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      part[t][0][k] = kk * (b[k] + f[k]);
+      part[t][1][k] = kk * (b[k] - f[k]);
+    }
+  }
+  __syncthreads();
+  if (wid == 0) {
+    double *out = fb + face * 2 * V;
+    for (int k = lane; k < V; k += 32) {
+      double l = 0.0, r = 0.0;
+      if (active) {
+        l = part[0][0][k];
+        r = part[0][1][k];
+        if (nt == 2) {
+          l += part[1][0][k];
+          r += part[1][1][k];
+        }
+      }
+      out[k] = l;
+      out[V + k] = r;
     }
   }
 }
