@@ -448,7 +448,8 @@ def run_gb300(args):
 
 def shock_tube_bench(torch):
     """The reference's CPU-runnable case: 1D shock tube, 200 cells, CFL 0.8,
-    t_end = 0.2 (248 steps), Rusanov (FLUX 0) and Osher (FLUX 2).  The whole
+    t_end = 0.2 (248 steps), Rusanov (FLUX 0) and Osher (FLUX 2) ADER steps,
+    and the reference driver's default split scheme (SPLIT, HALF_STEP).  The whole
     run is one gpr_iterate call (dt on the device, no host synchronisation),
     timed with CUDA events; the oracle (C restatement of the reference) runs
     the same problem on the host cores."""
@@ -466,16 +467,25 @@ def shock_tube_bench(torch):
                       dtype=torch.float64, device="cuda")
     O = Oracle()
     out = {"workload": "shock tube 200 cells, V=17, CFL 0.8, t_end 0.2"}
-    for flux, name in ((0, "rusanov"), (2, "osher")):
+    for flux, split, name in ((0, 0, "rusanov"), (2, 0, "osher"), (0, 1, "split_rusanov")):
         def run():
             ut = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
             clk = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
-            _lib.check(lib.gpr_iterate(
-                ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
-                dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
-                ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
-                ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), None, V,
-                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "iterate")
+            sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+            if split:  # the reference driver's default (SPLIT, HALF_STEP)
+                rc = lib.gpr_iterate_split(
+                    ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+                    dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
+                    flux, 1, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                    ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), V, sp)
+            else:
+                rc = lib.gpr_iterate(
+                    ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+                    dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
+                    flux, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                    ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), None,
+                    V, sp)
+            _lib.check(rc, "iterate")
             return ut, clk
         run()
         torch.cuda.synchronize()
@@ -487,7 +497,8 @@ def shock_tube_bench(torch):
         ms = e0.elapsed_time(e1)
         steps = int(clk[4].item())
         t0 = time.perf_counter()
-        ref, n, _ = O.run(u0, MP, tf, dX, 0, cfl=0.8, flux=flux)
+        ref, n, _ = O.run(u0, MP, tf, dX, 0, cfl=0.8, flux=flux, split=bool(split),
+                          half_step=True)
         cpu_s = time.perf_counter() - t0
         got = ut.cpu().numpy().reshape(ref.shape)
         out[name] = {"steps": steps, "gpu_ms": ms,

@@ -8,8 +8,9 @@
 // The eigen-decomposition (Householder Hessenberg reduction, Francis
 // double-shift QR with accumulated Schur vectors, eigenvectors by
 // back-substitution on the quasi-triangular Schur form; Golub & Van Loan,
-// Matrix Computations, Alg. 7.4.2, 7.5.1-7.5.2) runs per thread with its
-// matrices in local memory: one thread per (face, time node).  Eigenvalues
+// Matrix Computations, Alg. 7.4.2, 7.5.1-7.5.2) exists in two forms: per
+// thread with the matrices in local memory (the pointwise entry points), and
+// per warp with the matrices in shared memory (the face kernel).  Eigenvalues
 // closer than MULT_TOL ||T|| are treated as one semisimple eigenvalue (their
 // Schur vectors stay independent eigenvectors), which is how the reference's
 // Eigen solver behaves on the GPR system's 9-fold advection eigenvalue.
@@ -768,63 +769,6 @@ GPR_D void interface_point_eig(const double *ql, const double *qr, int flux, con
       b[k] += C.w[n] * bd[k];
   }
 }
-
-// 1D faces with the Osher or Roe dissipation: one thread per (face, time
-// node); output as k_faces1d (fb[face][0] to the left cell, [1] to the right).
-template <class L, bool BATCH = false>
-__global__ void __launch_bounds__(64) k_faces1d_eig(
-    double *__restrict__ fb, const double *__restrict__ qh, long nface,
-    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    int time_dg, int flux, DevPar Pv, Consts C, Batch B) {
-  constexpr int V = L::V;
-  if (dt_dev)
-    dt = *dt_dev;
-  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int t = threadIdx.x % NN;
-  const long face = gt / NN;
-  const bool valid = face < nface;
-  const long fo = valid ? face : 0;
-  long fi = fo;
-  const int inst = BATCH ? B.inst_f[fo] : 0;
-  const DevPar &P = BATCH ? B.P[inst] : Pv;
-  if (BATCH) {
-    fi = B.off_b[inst] + (fo - B.off_f[inst]);
-    dt = B.clk[5 * inst + 1];
-    dx = 1.0 / B.idx[inst];
-  }
-  const bool active =
-      valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
-  const int nt = time_dg ? NN : 1;
-  double ql[V], qr[V], f[V], b[V];
-  const double *ql_ = qh + (fi * nt + (time_dg ? t : 0)) * NN * V;
-  const double *qr_ = qh + ((fi + 1) * nt + (time_dg ? t : 0)) * NN * V;
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    ql[k] = C.endv[1][0] * ql_[k] + C.endv[1][1] * ql_[V + k];
-    qr[k] = C.endv[0][0] * qr_[k] + C.endv[0][1] * qr_[V + k];
-  }
-  const double kk = (time_dg ? dt * C.w[t] : dt) / (2.0 * dx);
-  if (active) {
-    interface_point_eig<L>(ql, qr, flux, P, C, f, b);
-  } else {
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      f[k] = b[k] = 0.0;
-  }
-  double *out = fb + fo * 2 * V;
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    double lft = active ? kk * (b[k] + f[k]) : 0.0;
-    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
-    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
-    if (valid && t == 0) {
-      out[k] = lft;
-      out[V + k] = rgt;
-    }
-  }
-}
-
 
 // ---------------------------------------------------------------------------
 // Warp-cooperative form: one warp per eigenproblem, matrices in shared
