@@ -25,7 +25,8 @@ def build(force=False):
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
         return LIB
-    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", LIB, SRC, "-lm"]
+    cmd = ["gcc", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", LIB,
+           SRC, "-lm"]
     subprocess.run(cmd, check=True)
     return LIB
 
@@ -84,6 +85,19 @@ def _load():
             "or_split_stepper": (ctypes.c_int, [_dp, _dp, _ip, ctypes.c_int,
                                                 ctypes.c_double, _dp, ctypes.c_int,
                                                 ctypes.c_int, P, _u8p]),
+            "or_distance": (ctypes.c_int, [_dp, _dp, _ip, ctypes.c_int, _dp]),
+            "or_finite_difference": (None, [_dp, _dp, _ip, ctypes.c_int, _dp]),
+            "or_find_interface_cells": (None, [_dp, _ip, ctypes.c_int, _ip]),
+            "or_left_star_state": (ctypes.c_int, [_dp, _dp, P, P, ctypes.c_double, _dp,
+                                                  ctypes.c_int, _dp]),
+            "or_fill_ghost_cells": (ctypes.c_int, [_dp, _u8p, _dp, _ip, ctypes.c_int, _dp,
+                                                   ctypes.c_double, P, ctypes.c_int, _ip]),
+            "or_make_u": (None, [_dp, _dp, _u8p, ctypes.c_long, P, ctypes.c_int]),
+            "or_timestep_multi": (ctypes.c_double, [_dp, _u8p, ctypes.c_long, _dp,
+                                                    ctypes.c_int, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_double,
+                                                    ctypes.c_int, P, ctypes.c_int]),
+            "or_renorm_multi": (None, [_dp, ctypes.c_long, P]),
             "or_num_threads": (ctypes.c_int, []),
             "or_set_num_threads": (None, [ctypes.c_int]),
         }
@@ -359,6 +373,128 @@ class Oracle:
                              int(flux), p,
                              _u8(np.ascontiguousarray(mask, dtype=np.uint8)))
         return u
+
+    # -- level-set ghost fluid (LSET = 1, non-thermal) ----------------------
+    @staticmethod
+    def _pars(MPs):
+        from phd_gb300.params import GprParC
+        arr = (GprParC * len(MPs))(*[MP.to_ctypes() for MP in MPs])
+        return arr, ctypes.cast(arr, ctypes.c_void_p)
+
+    def distance(self, phi, dX, nX):
+        """multi/pfmm.cpp:4-26 (first-order fast marching)."""
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        phi = np.ascontiguousarray(phi, dtype=np.float64).ravel()
+        out = np.zeros_like(phi)
+        lib.or_distance(_d(phi), _d(np.asarray(dX, dtype=np.float64)), _i(nX), len(nX),
+                        _d(out))
+        return out
+
+    def finite_difference(self, phi, dX, nX):
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        phi = np.ascontiguousarray(phi, dtype=np.float64).ravel()
+        out = np.zeros((phi.size, len(nX)))
+        lib.or_finite_difference(_d(phi), _d(np.asarray(dX, dtype=np.float64)), _i(nX),
+                                 len(nX), _d(out))
+        return out
+
+    def find_interface_cells(self, phi, nX):
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        phi = np.ascontiguousarray(phi, dtype=np.float64).ravel()
+        out = np.zeros(phi.size, dtype=np.int32)
+        lib.or_find_interface_cells(_d(phi), _i(nX), len(nX), _i(out))
+        return out
+
+    def left_star_state(self, QL, QR, MPL, MPR, dt, n):
+        lib = self._cfg()
+        out = np.zeros(self.V)
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        cl, pl = self._par(MPL)
+        cr, pr = self._par(MPR)
+        lib.or_left_star_state(_d(np.ascontiguousarray(QL, dtype=np.float64)),
+                               _d(np.ascontiguousarray(QR, dtype=np.float64)), pl, pr, dt,
+                               _d(n), n.size, _d(out))
+        return out
+
+    def fill_ghost_cells(self, u, nX, dX, dt, MPs):
+        """multi/fill.cpp:330-370 on a copy of u.  Returns (u with its level
+        set re-distanced, grids [nmat, ncell, V], masks [nmat, ncell] bool,
+        intMask [nmat, ncell], cells whose fill would read off the grid)."""
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        u = np.ascontiguousarray(u, dtype=np.float64).ravel().copy()
+        ncell = u.size // self.V
+        nmat = len(MPs)
+        grids = np.zeros((nmat, ncell, self.V))
+        masks = np.zeros((nmat, ncell), dtype=np.uint8)
+        im = np.zeros((nmat, ncell), dtype=np.int32)
+        arr, p = self._pars(MPs)
+        bad = lib.or_fill_ghost_cells(_d(grids), _u8(masks), _d(u), _i(nX), len(nX),
+                                      _d(np.asarray(dX, dtype=np.float64)), dt, p, nmat,
+                                      _i(im))
+        if bad < 0:
+            raise RuntimeError("oracle fill_ghost_cells: unsupported variant")
+        return u, grids, masks.astype(bool), im, bad
+
+    def make_u(self, u, grids, masks, MPs):
+        lib = self._cfg()
+        arr, p = self._pars(MPs)
+        g = np.ascontiguousarray(grids, dtype=np.float64)
+        m = np.ascontiguousarray(masks, dtype=np.uint8)
+        lib.or_make_u(_d(u), _d(g), _u8(m), u.size // self.V, p, len(MPs))
+        return u
+
+    def timestep_multi(self, grids, masks, dX, cfl, t, tf, count, MPs):
+        lib = self._cfg()
+        arr, p = self._pars(MPs)
+        g = np.ascontiguousarray(grids, dtype=np.float64)
+        m = np.ascontiguousarray(masks, dtype=np.uint8)
+        return lib.or_timestep_multi(_d(g), _u8(m), m.shape[1],
+                                     _d(np.asarray(dX, dtype=np.float64)), len(dX), cfl, t,
+                                     tf, count, p, len(MPs))
+
+    def renorm_multi(self, u, MPs):
+        lib = self._cfg()
+        arr, p = self._pars(MPs)
+        lib.or_renorm_multi(_d(u), u.size // self.V, p)
+        return u
+
+    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None):
+        """Time loop of solvers/iterator.cpp:85-151 with the ghost-fluid fill
+        (LSET = 1): fill -> timestep -> per material boundaries + ADER step
+        on its masked cells -> make_u -> renorm.  Returns (u, steps, t)."""
+        shape = u0.shape
+        nX = np.array(shape[:-1], dtype=np.int32)
+        nd = len(nX)
+        u = np.ascontiguousarray(u0, dtype=np.float64).ravel().copy()
+        ncell = u.size // self.V
+        nmat = len(MPs)
+        grids = np.stack([u.reshape(ncell, self.V)] * nmat)
+        masks = np.ones((nmat, ncell), dtype=bool)
+        bc = (np.array([bcs] * 2 * nd, dtype=np.int32) if np.isscalar(bcs)
+              else np.asarray(bcs, np.int32))
+        t, count, dt = 0.0, 0, 0.0
+        while t < tf:
+            u, grids, masks, _, _ = self.fill_ghost_cells(u, nX, dX, dt, MPs)
+            dt = self.timestep_multi(grids, masks, dX, cfl, t, tf, count, MPs)
+            for mat in range(nmat):
+                if MPs[mat].EOS <= -1:
+                    continue
+                g = np.ascontiguousarray(grids[mat]).ravel()
+                ub = self.boundaries(g, nX, bc)
+                maskb = self.extend_mask(masks[mat].astype(np.uint8), nX)
+                self.ader_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb)
+                grids[mat] = g.reshape(ncell, self.V)
+            self.make_u(u, grids, masks, MPs)
+            t += dt
+            count += 1
+            self.renorm_multi(u, MPs)
+            if max_steps is not None and count >= max_steps:
+                break
+        return u.reshape(shape), count, t
 
     def num_threads(self):
         return self.lib.or_num_threads()

@@ -2865,3 +2865,1042 @@ void or_set_num_threads(int n) {
   (void)n;
 #endif
 }
+
+/* ======================================================================== */
+/* Level-set ghost-fluid fill (LSET = 1, two materials, VISCOUS, no heat     */
+/* conduction): multi/pfmm.cpp, multi/functions.cpp, multi/fill.cpp,        */
+/* system/multi/{riemann,conditions,eigenvecs,rotations}.cpp and            */
+/* solvers/iterator.cpp:12-42 (make_u).                                     */
+/* ======================================================================== */
+
+#include <float.h>
+
+/* ---- first-order fast marching (the vendored scikit-fmm's
+ * distance_marcher.cpp:5-28,72-151 and base_marcher.cpp:43-198 with
+ * ORDER 1, no narrow band, not periodic; called by multi/pfmm.cpp:4-26). */
+
+enum { FMM_FAR = 0, FMM_NARROW = 1, FMM_FROZEN = 2 };
+
+typedef struct {
+  int ndim, size, shape[2], shift[2];
+  double dx[2], idx2[2];
+  const double *phi;
+  double *dist;
+  unsigned char *flag;
+  /* binary min-heap of grid addresses keyed by |distance| */
+  int *heap, *pos, n;
+  double *key;
+} fmm_t;
+
+static int fmm_nb(const fmm_t *m, int i, int dim, int dir) {
+  int c = m->ndim == 1 ? i : (dim == 0 ? i / m->shape[1] : i % m->shape[1]);
+  int nc = c + dir;
+  if (nc < 0 || nc >= m->shape[dim])
+    return -1;
+  return i + dir * m->shift[dim];
+}
+
+static void fmm_swap(fmm_t *m, int a, int b) {
+  int t = m->heap[a];
+  m->heap[a] = m->heap[b];
+  m->heap[b] = t;
+  m->pos[m->heap[a]] = a;
+  m->pos[m->heap[b]] = b;
+}
+
+static void fmm_up(fmm_t *m, int k) {
+  while (k > 0) {
+    int p = (k - 1) / 2;
+    if (m->key[m->heap[p]] <= m->key[m->heap[k]])
+      break;
+    fmm_swap(m, p, k);
+    k = p;
+  }
+}
+
+static void fmm_down(fmm_t *m, int k) {
+  for (;;) {
+    int l = 2 * k + 1, r = l + 1, s = k;
+    if (l < m->n && m->key[m->heap[l]] < m->key[m->heap[s]])
+      s = l;
+    if (r < m->n && m->key[m->heap[r]] < m->key[m->heap[s]])
+      s = r;
+    if (s == k)
+      break;
+    fmm_swap(m, s, k);
+    k = s;
+  }
+}
+
+static void fmm_push(fmm_t *m, int addr, double key) {
+  m->key[addr] = key;
+  m->heap[m->n] = addr;
+  m->pos[addr] = m->n;
+  m->n++;
+  fmm_up(m, m->n - 1);
+}
+
+static void fmm_set(fmm_t *m, int addr, double key) {
+  double old = m->key[addr];
+  m->key[addr] = key;
+  if (key < old)
+    fmm_up(m, m->pos[addr]);
+  else
+    fmm_down(m, m->pos[addr]);
+}
+
+static int fmm_pop(fmm_t *m) {
+  int top = m->heap[0];
+  m->n--;
+  if (m->n > 0) {
+    m->heap[0] = m->heap[m->n];
+    m->pos[m->heap[0]] = 0;
+    fmm_down(m, 0);
+  }
+  m->pos[top] = -1;
+  return top;
+}
+
+/* updatePointOrderOne + solveQuadratic (distance_marcher.cpp:5-28,72-88):
+ * per axis the frozen neighbour of least |distance|, then the upwind
+ * quadratic; the root is chosen by the sign of phi; 0 when it has no real
+ * root. */
+static double fmm_point(const fmm_t *m, int i) {
+  double a = 0, b = 0, c = 0;
+  for (int dim = 0; dim < m->ndim; dim++) {
+    double value = DBL_MAX;
+    for (int j = -1; j < 2; j += 2) {
+      int n = fmm_nb(m, i, dim, j);
+      if (n != -1 && m->flag[n] == FMM_FROZEN && fabs(m->dist[n]) < fabs(value))
+        value = m->dist[n];
+    }
+    if (value < DBL_MAX) {
+      a += m->idx2[dim];
+      b -= m->idx2[dim] * 2 * value;
+      c += m->idx2[dim] * (value * value);
+    }
+  }
+  c -= 1;
+  double det = b * b - 4 * a * c;
+  if (!(det > 0))
+    return 0;
+  double r0 = (-b + sqrt(det)) / 2.0 / a;
+  double r1 = (-b - sqrt(det)) / 2.0 / a;
+  return m->phi[i] > DBL_EPSILON ? r0 : r1;
+}
+
+/* distance (multi/pfmm.cpp:4-26): signed first-order distance to the zero
+ * level of phi on an nx (x ny) grid of spacings dX.  Returns 0, or 2 when
+ * phi has no zero crossing (dist is then all zeros, as in the reference). */
+int or_distance(const double *phi, const double *dX, const int *nX, int ndim,
+                double *dist) {
+  fmm_t m;
+  memset(&m, 0, sizeof m);
+  m.ndim = ndim;
+  m.size = 1;
+  for (int d = 0; d < ndim; d++) {
+    m.shape[d] = nX[d];
+    m.size *= nX[d];
+    m.dx[d] = dX[d];
+    m.idx2[d] = 1 / dX[d] / dX[d];
+  }
+  m.shift[0] = ndim == 2 ? nX[1] : 1;
+  m.shift[1] = 1;
+  m.phi = phi;
+  m.dist = dist;
+  int size = m.size;
+  m.flag = calloc(size, 1);
+  m.heap = malloc(sizeof(int) * size);
+  m.pos = malloc(sizeof(int) * size);
+  m.key = malloc(sizeof(double) * size);
+  for (int i = 0; i < size; i++)
+    dist[i] = 0.0;
+
+  /* initalizeFrozen (distance_marcher.cpp:90-151, with the reference's
+   * edit: the least per-axis crossing distance, not their harmonic sum) */
+  for (int i = 0; i < size; i++)
+    if (phi[i] == 0.0) {
+      m.flag[i] = FMM_FROZEN;
+      dist[i] = 0.0;
+    }
+  for (int i = 0; i < size; i++) {
+    if (m.flag[i] != FMM_FAR)
+      continue;
+    double ld[2] = {0, 0};
+    int borders = 0;
+    for (int dim = 0; dim < ndim; dim++)
+      for (int j = -1; j < 2; j += 2) {
+        int n = fmm_nb(&m, i, dim, j);
+        if (n != -1 && phi[i] * phi[n] < 0) {
+          borders = 1;
+          double d = m.dx[dim] * phi[i] / (phi[i] - phi[n]);
+          if (ld[dim] == 0 || ld[dim] > d)
+            ld[dim] = d;
+        }
+      }
+    if (borders) {
+      double minDist = DBL_MAX;
+      for (int dim = 0; dim < ndim; dim++) {
+        double t = fabs(ld[dim]);
+        if (t > 0.)
+          minDist = t < minDist ? t : minDist;
+      }
+      dist[i] = phi[i] < 0 ? -minDist : minDist;
+      m.flag[i] = FMM_FROZEN;
+    }
+  }
+
+  /* initalizeNarrow (base_marcher.cpp:62-87) */
+  int nfrozen = 0;
+  for (int i = 0; i < size; i++)
+    nfrozen += m.flag[i] == FMM_FROZEN;
+  for (int i = 0; i < size; i++) {
+    if (m.flag[i] != FMM_FAR)
+      continue;
+    int touch = 0;
+    for (int dim = 0; dim < ndim && !touch; dim++)
+      for (int j = -1; j < 2; j += 2) {
+        int n = fmm_nb(&m, i, dim, j);
+        if (n != -1 && m.flag[n] == FMM_FROZEN)
+          touch = 1;
+      }
+    if (touch) {
+      m.flag[i] = FMM_NARROW;
+      double d = fmm_point(&m, i);
+      dist[i] = d;
+      fmm_push(&m, i, fabs(d));
+    }
+  }
+  int rc = 0;
+  if (!nfrozen) {
+    rc = 2; /* base_marcher.cpp:103-106: nothing to march from */
+  } else {
+    /* main loop (base_marcher.cpp:98-188): freeze the least |distance| and
+     * every equal key with it, then update their unfrozen neighbours */
+    int *batch = malloc(sizeof(int) * size);
+    while (m.n > 0) {
+      int nb = 0;
+      int addr = fmm_pop(&m);
+      double value = m.key[addr];
+      m.flag[addr] = FMM_FROZEN;
+      batch[nb++] = addr;
+      while (m.n > 0 && m.key[m.heap[0]] == value) {
+        int a2 = fmm_pop(&m);
+        m.flag[a2] = FMM_FROZEN;
+        batch[nb++] = a2;
+      }
+      for (int k = 0; k < nb; k++) {
+        int a = batch[k];
+        for (int dim = 0; dim < ndim; dim++)
+          for (int j = -1; j < 2; j += 2) {
+            int n = fmm_nb(&m, a, dim, j);
+            if (n == -1 || m.flag[n] == FMM_FROZEN)
+              continue;
+            double d = fmm_point(&m, n);
+            if (!d)
+              continue;
+            dist[n] = d;
+            if (m.flag[n] == FMM_NARROW) {
+              fmm_set(&m, n, fabs(d));
+            } else {
+              m.flag[n] = FMM_NARROW;
+              fmm_push(&m, n, fabs(d));
+            }
+          }
+      }
+    }
+    free(batch);
+    for (int i = 0; i < size; i++)
+      if (m.flag[i] != FMM_FROZEN)
+        dist[i] = DBL_MAX;
+  }
+  free(m.flag);
+  free(m.heap);
+  free(m.pos);
+  free(m.key);
+  return rc;
+}
+
+/* ---- multi/functions.cpp ---- */
+
+static int ls_sign(double x) { return x <= 0 ? -1 : 1; } /* functions.cpp:7-12 */
+
+/* finite_difference (functions.cpp:16-54): central differences, edge rows
+ * copied from their neighbours; dphi is [ncell][ndim]. */
+void or_finite_difference(const double *phi, const double *dX, const int *nX,
+                          int ndim, double *dphi) {
+  if (ndim == 1) {
+    int n = nX[0];
+    for (int i = 1; i < n - 1; i++)
+      dphi[i] = (phi[i + 1] - phi[i - 1]) / (2 * dX[0]);
+    dphi[0] = dphi[1];
+    dphi[n - 1] = dphi[n - 2];
+    return;
+  }
+  int nx = nX[0], ny = nX[1];
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      int ii = i == 0 ? 1 : (i == nx - 1 ? nx - 2 : i);
+      int jj = j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j);
+      dphi[2 * (i * ny + j)] =
+          (phi[(ii + 1) * ny + j] - phi[(ii - 1) * ny + j]) / (2 * dX[0]);
+      dphi[2 * (i * ny + j) + 1] =
+          (phi[i * ny + jj + 1] - phi[i * ny + jj - 1]) / (2 * dX[1]);
+    }
+}
+
+/* find_interface_cells (fill.cpp:11-74): intMask = sign(phi) on both sides
+ * of every crossing next to a non-isolated phi <= 0 cell; -2 marks an
+ * isolated phi <= 0 cell (2D). */
+void or_find_interface_cells(const double *phi, const int *nX, int ndim,
+                             int32_t *mask) {
+  int nx = nX[0];
+  if (ndim == 1) {
+    for (int i = 0; i < nx; i++)
+      mask[i] = 0;
+    for (int i = 0; i < nx - 1; i++)
+      if (phi[i] * phi[i + 1] <= 0.) {
+        mask[i] = ls_sign(phi[i]);
+        mask[i + 1] = ls_sign(phi[i + 1]);
+      }
+    return;
+  }
+  int ny = nX[1];
+  for (int k = 0; k < nx * ny; k++)
+    mask[k] = 0;
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      int k0 = i * ny + j;
+      if (!(phi[k0] <= 0.))
+        continue;
+      int cl = i > 0 && phi[k0 - ny] <= 0., cr = i < nx - 1 && phi[k0 + ny] <= 0.;
+      int cd = j > 0 && phi[k0 - 1] <= 0., cu = j < ny - 1 && phi[k0 + 1] <= 0.;
+      if (cl || cr || cd || cu) {
+        int nbr[4] = {i > 0 ? k0 - ny : -1, i < nx - 1 ? k0 + ny : -1,
+                      j > 0 ? k0 - 1 : -1, j < ny - 1 ? k0 + 1 : -1};
+        for (int q = 0; q < 4; q++)
+          if (nbr[q] >= 0 && phi[k0] * phi[nbr[q]] <= 0.) {
+            mask[k0] = ls_sign(phi[k0]);
+            mask[nbr[q]] = ls_sign(phi[nbr[q]]);
+          }
+      } else {
+        mask[k0] = -2;
+      }
+    }
+}
+
+/* ---- system/multi: the interface Riemann problem (non-thermal, slip) ---- */
+
+/* rotation_matrix (rotations.cpp:5-35): rows e1 = n, e2, e3. */
+static void ls_rotation(const double *n, int ndim, double R[3][3]) {
+  double e1[3] = {0, 0, 0}, e2[3], e3[3], den;
+  for (int i = 0; i < ndim; i++)
+    e1[i] = n[i];
+  double Sq = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+  if (fabs(e1[1] + e1[2]) <= fabs(e1[1] - e1[2])) {
+    den = sqrt(2 * (1 - e1[0] * e1[1] - e1[1] * e1[2] - e1[2] * e1[0]));
+    e2[0] = e1[1] - e1[2];
+    e2[1] = e1[2] - e1[0];
+    e2[2] = e1[0] - e1[1];
+    double Sum = e1[0] + e1[1] + e1[2];
+    for (int i = 0; i < 3; i++)
+      e3[i] = e1[i] * Sum - Sq;
+  } else {
+    den = sqrt(2 * (1 + e1[0] * e1[1] + e1[1] * e1[2] - e1[2] * e1[0]));
+    e2[0] = e1[1] + e1[2];
+    e2[1] = e1[2] - e1[0];
+    e2[2] = -e1[0] - e1[1];
+    double Sum = e1[0] - e1[1] + e1[2];
+    e3[0] = e1[0] * Sum - Sq;
+    e3[1] = e1[1] * Sum + Sq;
+    e3[2] = e1[2] * Sum - Sq;
+  }
+  for (int i = 0; i < 3; i++) {
+    R[0][i] = e1[i];
+    R[1][i] = e2[i] / den;
+    R[2][i] = e3[i] / den;
+  }
+}
+
+/* rotate_tensors (rotations.cpp:37-47): v <- R v, A <- R A R^T. */
+static void ls_rotate(double *Q, double R[3][3]) {
+  double v[3], A[9], T[9];
+  for (int i = 0; i < 3; i++)
+    v[i] = R[i][0] * Q[2] + R[i][1] * Q[3] + R[i][2] * Q[4];
+  for (int i = 0; i < 3; i++)
+    Q[2 + i] = v[i];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      T[3 * i + j] = R[i][0] * Q[5 + j] + R[i][1] * Q[8 + j] + R[i][2] * Q[11 + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      A[3 * i + j] = T[3 * i] * R[j][0] + T[3 * i + 1] * R[j][1] + T[3 * i + 2] * R[j][2];
+  for (int k = 0; k < 9; k++)
+    Q[5 + k] = A[k];
+  if (THERMAL) {
+    for (int i = 0; i < 3; i++)
+      v[i] = R[i][0] * Q[14] + R[i][1] * Q[15] + R[i][2] * Q[16];
+    for (int i = 0; i < 3; i++)
+      Q[14 + i] = v[i];
+  }
+}
+
+/* Total stress column 0: Sigma = p e0 - sigma(:,0) (variables/state.cpp:39-46) */
+static void ls_Sigma0(const double *Q, const gpr_par *P, double *S) {
+  sigma_d(Q, P, 0, S);
+  for (int i = 0; i < 3; i++)
+    S[i] = -S[i];
+  S[0] += or_pressure(Q, P);
+}
+
+/* c_0 (waves/speeds.cpp:8-18) */
+static double ls_c0(const double *Q, double p, const gpr_par *P) {
+  double r = Q[0];
+  double dEdr = dedrho(r, p, P) + dC_0drho(r, P) / 4 * devGsq(Q + 5);
+  return sqrt((p / (r * r) - dEdr) / dedp(r, P));
+}
+
+/* Gaussian elimination with partial pivoting: solves A X = B in place
+ * (A n x n, B n x m, both row-major). */
+static int ls_solve(int n, int m, double *A, double *B) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++)
+      if (fabs(A[r * n + c]) > fabs(A[p * n + c]))
+        p = r;
+    if (A[p * n + c] == 0.0)
+      return -1;
+    if (p != c) {
+      for (int j = 0; j < n; j++) {
+        double t = A[c * n + j];
+        A[c * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
+      for (int j = 0; j < m; j++) {
+        double t = B[c * m + j];
+        B[c * m + j] = B[p * m + j];
+        B[p * m + j] = t;
+      }
+    }
+    for (int r = c + 1; r < n; r++) {
+      double f = A[r * n + c] / A[c * n + c];
+      for (int j = c; j < n; j++)
+        A[r * n + j] -= f * A[c * n + j];
+      for (int j = 0; j < m; j++)
+        B[r * m + j] -= f * B[c * m + j];
+    }
+  }
+  for (int c = n - 1; c >= 0; c--)
+    for (int j = 0; j < m; j++) {
+      double s = B[c * m + j];
+      for (int k = c + 1; k < n; k++)
+        s -= A[c * n + k] * B[k * m + j];
+      B[c * m + j] = s / A[c * n + c];
+    }
+  return 0;
+}
+
+static int ls_inverse(int n, const double *M, double *out) {
+  double A[25];
+  memcpy(A, M, sizeof(double) * n * n);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      out[i * n + j] = i == j;
+  return ls_solve(n, n, A, out);
+}
+
+/* Inverse principal square root of a matrix with positive real eigenvalues
+ * by the Denman-Beavers iteration (Y -> M^(1/2), Z -> M^(-1/2)).  The
+ * reference forms the same matrix function from an eigen-decomposition,
+ * Q diag(lambda^(-1/2)) Q^(-1) (riemann.cpp:141-146). */
+static int ls_inv_sqrt(int n, const double *M, double *Zout) {
+  double Y[16], Z[16], Yi[16], Zi[16];
+  memcpy(Y, M, sizeof(double) * n * n);
+  for (int i = 0; i < n * n; i++)
+    Z[i] = (i % (n + 1)) == 0;
+  int extra = 0;
+  for (int it = 0; it < 100; it++) {
+    if (ls_inverse(n, Y, Yi) || ls_inverse(n, Z, Zi))
+      return -1;
+    double dmax = 0, ymax = 0;
+    for (int k = 0; k < n * n; k++) {
+      double y = 0.5 * (Y[k] + Zi[k]);
+      double z = 0.5 * (Z[k] + Yi[k]);
+      double dy = fabs(y - Y[k]);
+      dmax = dy > dmax ? dy : dmax;
+      ymax = fabs(y) > ymax ? fabs(y) : ymax;
+      Y[k] = y;
+      Z[k] = z;
+    }
+    if (dmax <= 1e-13 * ymax && ++extra == 2)
+      break;
+  }
+  memcpy(Zout, Z, sizeof(double) * n * n);
+  return 0;
+}
+
+/* The first n1 = 3 columns of riemann_constraints (riemann.cpp:79-154) for
+ * the non-thermal system: rows 0-4 are X (the primitive-variable response
+ * to a change in the normal traction), rows 11-13 are -sgn Y0 Xi1 X; every
+ * other entry of those columns is zero.  The remaining columns of the
+ * reference's matrix multiply zero coefficients in star_stepper and are
+ * not formed.  R is [V][3]. */
+static int ls_constraints(const double *Q, double sgn, const gpr_par *P, double *R) {
+  double r = Q[0];
+  double p = or_pressure(Q, P);
+  const double *A = Q + 5;
+  double sr[3], Pi1[9], Pi1i[9], Ai[9], sg[3];
+  dsigmadrho(Q, P, 0, sr);
+  dsigmadA(Q, P, 0, Pi1);
+  sigma_d(Q, P, 0, sg);
+  if (ls_inverse(3, A, Ai) || ls_inverse(3, Pi1, Pi1i))
+    return -1;
+  double tmp[25];
+  memset(tmp, 0, sizeof tmp);
+  for (int i = 0; i < 3; i++) {
+    tmp[5 * i] = -sr[i];
+    for (int j = 0; j < 3; j++)
+      tmp[5 * i + 2 + j] = -Pi1[3 * i + j];
+  }
+  tmp[1] = 1.;
+  double c0 = ls_c0(Q, p, P);
+  double B[6] = {r, 0, 0, 0, 0, 0};
+  for (int j = 0; j < 3; j++)
+    B[3 + j] = sg[j] - r * sr[j];
+  B[3] += r * c0 * c0;
+  double C[6]; /* Pi1^-1 [-sr, e0] (3x2) */
+  for (int i = 0; i < 3; i++) {
+    C[2 * i] = -(Pi1i[3 * i] * sr[0] + Pi1i[3 * i + 1] * sr[1] + Pi1i[3 * i + 2] * sr[2]);
+    C[2 * i + 1] = Pi1i[3 * i];
+  }
+  double BA[6]; /* B A^-1 (2x3) */
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 3; j++)
+      BA[3 * i + j] = B[3 * i] * Ai[j] + B[3 * i + 1] * Ai[3 + j] + B[3 * i + 2] * Ai[6 + j];
+  double Z[4];
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      Z[2 * i + j] = (i == j) - (BA[3 * i] * C[j] + BA[3 * i + 1] * C[2 + j] +
+                                 BA[3 * i + 2] * C[4 + j]);
+  double dz = Z[0] * Z[3] - Z[1] * Z[2];
+  if (dz == 0.0)
+    return -1;
+  double Zi[4] = {Z[3] / dz, -Z[1] / dz, -Z[2] / dz, Z[0] / dz};
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 5; j++) {
+      double w0 = j == 0 ? 1 : (j == 1 ? 0 : -BA[j - 2]);
+      double w1 = j == 0 ? 0 : (j == 1 ? 1 : -BA[3 + j - 2]);
+      tmp[5 * (3 + i) + j] = Zi[2 * i] * w0 + Zi[2 * i + 1] * w1;
+    }
+  double X[15]; /* tmp^-1 [:, 0:3] */
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 3; j++)
+      X[3 * i + j] = i == j;
+  if (ls_solve(5, 3, tmp, X))
+    return -1;
+  /* Xi1 (3x5), Xi2 (5x3) of eig.cpp:8-53 at d = 0 */
+  double X1[15], X2[15], Xi[9], Y0[9];
+  memset(X1, 0, sizeof X1);
+  memset(X2, 0, sizeof X2);
+  X1[1] = 1 / r;
+  for (int i = 0; i < 3; i++) {
+    X1[5 * i] = -1 / r * sr[i];
+    for (int j = 0; j < 3; j++)
+      X1[5 * i + 2 + j] = -1 / r * Pi1[3 * i + j];
+  }
+  X2[0] = r;
+  X2[3] = r * c0 * c0;
+  for (int j = 0; j < 3; j++)
+    X2[3 + j] += sg[j] - r * sr[j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      X2[3 * (2 + i) + j] = A[3 * i + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0;
+      for (int k = 0; k < 5; k++)
+        s += X1[5 * i + k] * X2[3 * k + j];
+      Xi[3 * i + j] = s;
+    }
+  /* The reference's Q diag(Re(lambda)^(-1/2)) Q^(-1) with Q = Re(eigenvectors)
+   * (riemann.cpp:136-141) is NaN when an eigenvalue has a non-positive real
+   * part, and singular for a complex pair (the real parts of conjugate
+   * eigenvectors coincide); left_star_state then returns its input.  A pair
+   * counts as complex when its imaginary part exceeds 1e-8 of the spectral
+   * radius (below that the reference's choice is decided by rounding). */
+  {
+    double wr[3], wi[3];
+    if (or_eigenvalues(3, Xi, wr, wi))
+      return -1;
+    double rad = 0;
+    for (int i = 0; i < 3; i++)
+      rad = fmax(rad, hypot(wr[i], wi[i]));
+    for (int i = 0; i < 3; i++)
+      if (!(wr[i] > 0) || fabs(wi[i]) > 1e-8 * rad)
+        return -1;
+  }
+  if (ls_inv_sqrt(3, Xi, Y0))
+    return -1;
+  double X1X[9], YX[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0;
+      for (int k = 0; k < 5; k++)
+        s += X1[5 * i + k] * X[3 * k + j];
+      X1X[3 * i + j] = s;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      YX[3 * i + j] = Y0[3 * i] * X1X[j] + Y0[3 * i + 1] * X1X[3 + j] +
+                      Y0[3 * i + 2] * X1X[6 + j];
+  memset(R, 0, sizeof(double) * V * 3);
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 3; j++)
+      R[3 * i + j] = X[3 * i + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      R[3 * (11 + i) + j] = -sgn * YX[3 * i + j];
+  return 0;
+}
+
+/* Cvec_to_Pvec / Pvec_to_Cvec (functions/vectors.cpp:85-154), non-thermal:
+ * P = [rho, p, A(:,0), A(:,1), A(:,2), v, phi]. */
+static void ls_c2p(const double *Q, const gpr_par *P, double *out) {
+  double r = Q[0];
+  memcpy(out, Q, sizeof(double) * V);
+  out[1] = or_pressure(Q, P);
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      out[2 + 3 * j + i] = Q[5 + 3 * i + j];
+  for (int i = 0; i < 3; i++)
+    out[11 + i] = Q[2 + i] / r;
+}
+
+static void ls_p2c(const double *Pv, const gpr_par *P, double *Q) {
+  double r = Pv[0], p = Pv[1], A[9], v[3];
+  memcpy(Q, Pv, sizeof(double) * V);
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      A[3 * i + j] = Pv[2 + 3 * j + i];
+  for (int i = 0; i < 3; i++)
+    v[i] = Pv[11 + i];
+  for (int i = 0; i < 3; i++)
+    Q[2 + i] = r * v[i];
+  for (int k = 0; k < 9; k++)
+    Q[5 + k] = A[k];
+  /* total_energy (energy/eos.cpp:43-47) with E_1 (eos.cpp:10-19) */
+  double G = Gamma_MG(r, P);
+  double E = e_ref(r, P) + (p - p_ref(r, P)) / (r * G);
+  E += (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / 2;
+  E += E_2A(r, A, P);
+  Q[1] = r * E;
+}
+
+static const double STAR_TOL = 1e-8; /* options.h:22 */
+
+/* check_star_convergence (riemann.cpp:26-77), slip conditions. */
+static int ls_converged(const double *QL, const double *QR, const gpr_par *PL,
+                        const gpr_par *PR) {
+  double SL[3];
+  ls_Sigma0(QL, PL, SL);
+  if (PR->EOS > -1) {
+    double r0 = PL->rho0 < PR->rho0 ? PL->rho0 : PR->rho0;
+    double b02 = PL->b02 < PR->b02 ? PL->b02 : PR->b02;
+    double SR[3];
+    ls_Sigma0(QR, PR, SR);
+    double vL = QL[2] / QL[0], vR = QR[2] / QR[0];
+    return fabs(SL[0] - SR[0]) / (b02 * r0) < STAR_TOL &&
+           fabs(vL - vR) / sqrt(b02) < STAR_TOL;
+  }
+  double mx = fabs(SL[0]);
+  for (int i = 1; i < 3; i++)
+    mx = fabs(SL[i]) > mx ? fabs(SL[i]) : mx;
+  return mx / (PL->b02 * PL->rho0) < STAR_TOL;
+}
+
+/* star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:57-90). */
+static int ls_star_step(double *QL, double *QR, const gpr_par *PL, const gpr_par *PR) {
+  double RL[MAXV * 3], RR[MAXV * 3], xL[3], xR[3], cL[3], cR[3], Pv[MAXV];
+  if (ls_constraints(QL, 1, PL, RL))
+    return -1;
+  ls_Sigma0(QL, PL, xL);
+  if (PR->EOS > -1) {
+    if (ls_constraints(QR, -1, PR, RR))
+      return -1;
+    ls_Sigma0(QR, PR, xR);
+    double yL = QL[2] / QL[0], yR = QR[2] / QR[0];
+    double dL = RL[33] * xL[0] + RL[34] * xL[1] + RL[35] * xL[2];
+    double dR = RR[33] * xR[0] + RR[34] * xR[1] + RR[35] * xR[2];
+    double x0 = (yR - yL + dL - dR) / (RL[33] - RR[33]);
+    double x_[3] = {x0, 0., 0.};
+    for (int i = 0; i < 3; i++) {
+      cL[i] = x_[i] - xL[i];
+      cR[i] = x_[i] - xR[i];
+    }
+    ls_c2p(QR, PR, Pv);
+    for (int k = 0; k < V; k++)
+      Pv[k] += RR[3 * k] * cR[0] + RR[3 * k + 1] * cR[1] + RR[3 * k + 2] * cR[2];
+    ls_p2c(Pv, PR, QR);
+  } else {
+    for (int i = 0; i < 3; i++)
+      cL[i] = -xL[i];
+    for (int k = 0; k < V; k++)
+      QR[k] = 0.0;
+  }
+  ls_c2p(QL, PL, Pv);
+  for (int k = 0; k < V; k++)
+    Pv[k] += RL[3 * k] * cL[0] + RL[3 * k + 1] * cL[1] + RL[3 * k + 2] * cL[2];
+  ls_p2c(Pv, PL, QL);
+  return 0;
+}
+
+/* left_star_state (riemann.cpp:203-233): the left star state of the
+ * interface Riemann problem between QL (material PL) and QR (material PR)
+ * along the normal n, by at most 10 linearised steps with a half-step of
+ * the stiff relaxation before each.  Returns QL unchanged when the
+ * iteration produced a NaN.  THERMAL must be off. */
+int or_left_star_state(const double *QL0, const double *QR0, const gpr_par *PL,
+                       const gpr_par *PR, double dt, const double *n, int ndim,
+                       double *out) {
+  if (THERMAL)
+    return -3;
+  double QL[MAXV], QR[MAXV], R[3][3];
+  memcpy(QL, QL0, sizeof(double) * V);
+  memcpy(QR, QR0, sizeof(double) * V);
+  ls_rotation(n, ndim, R);
+  ls_rotate(QL, R);
+  ls_rotate(QR, R);
+  int count = 0;
+  while (!ls_converged(QL, QR, PL, PR) && count < 10) {
+    or_ode_cell(QL, dt / 2, PL);
+    if (PR->EOS > -1)
+      or_ode_cell(QR, dt / 2, PR);
+    if (ls_star_step(QL, QR, PL, PR)) {
+      QL[0] = NAN;
+      break;
+    }
+    count++;
+  }
+  for (int k = 0; k < V; k++)
+    if (isnan(QL[k])) {
+      memcpy(out, QL0, sizeof(double) * V);
+      return count;
+    }
+  double RT[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      RT[i][j] = R[j][i];
+  ls_rotate(QL, RT);
+  memcpy(out, QL, sizeof(double) * V);
+  return count;
+}
+
+/* ---- multi/fill.cpp ---- */
+
+static int ls_mat(const double *Q) { return Q[V - 1] >= 0. ? 1 : 0; } /* vectors.cpp:24-31 */
+
+/* boundary_inds (fill.cpp:96-132): cell indices (not offsets) of the cell
+ * itself, of the interface point and of the probes one cell either side. */
+static void ls_bound_inds(const int *inds, double phii, const double *n, const double *dX,
+                          const int *nX, int ndim, int *ind, int *interf, int *L, int *Rr) {
+  int vi[2], vl[2], vr[2];
+  for (int d = 0; d < ndim; d++) {
+    double xp = (inds[d] + 0.5) * dX[d];
+    double xi = xp - phii * n[d];
+    double xl = xi - 1. * dX[d] * n[d];
+    double xr = xi + 1. * dX[d] * n[d];
+    vi[d] = (int)(xi / dX[d]);
+    vl[d] = (int)(xl / dX[d]);
+    vr[d] = (int)(xr / dX[d]);
+  }
+  if (ndim == 1) {
+    *ind = inds[0];
+    *interf = vi[0];
+    *L = vl[0];
+    *Rr = vr[0];
+  } else {
+    int ny = nX[1];
+    *ind = inds[0] * ny + inds[1];
+    *interf = vi[0] * ny + vi[1];
+    *L = vl[0] * ny + vl[1];
+    *Rr = vr[0] * ny + vr[1];
+  }
+}
+
+static int ls_neighbor_index(const int32_t *mask, int i, int j, int nx, int ny, int N0) {
+  int indn = -1;
+  if (i > 0 && mask[(i - 1) * ny + j] == N0)
+    indn = (i - 1) * ny + j;
+  if (i < nx - 1 && mask[(i + 1) * ny + j] == N0)
+    indn = (i + 1) * ny + j;
+  if (j > 0 && mask[i * ny + j - 1] == N0)
+    indn = i * ny + j - 1;
+  if (j < ny - 1 && mask[i * ny + j + 1] == N0)
+    indn = i * ny + j + 1;
+  return indn;
+}
+
+/* fill_boundary_inner (fill.cpp:134-198).  Returns -1 when the reference
+ * would read outside the grid. */
+static int ls_fill_boundary_inner(double *grid, const int *inds, const double *dX,
+                                  const int *nX, int ndim, double phii, int mat,
+                                  const gpr_par *MPs, double dt, double *n, int indn) {
+  long ncell = ndim == 1 ? nX[0] : (long)nX[0] * nX[1];
+  int ind, interf, L, Rr;
+  ls_bound_inds(inds, phii, n, dX, nX, ndim, &ind, &interf, &L, &Rr);
+  if (interf < 0 || interf >= ncell || L < 0 || L >= ncell || Rr < 0 || Rr >= ncell)
+    return -1;
+  double QL[MAXV], QR[MAXV], out[MAXV];
+  memcpy(QR, grid + (long)Rr * V, sizeof(double) * V);
+  int miR = ls_mat(QR);
+  if (ls_mat(grid + (long)interf * V) == mat) {
+    memcpy(QL, grid + (long)interf * V, sizeof(double) * V);
+  } else if (ls_mat(grid + (long)L * V) == mat) {
+    memcpy(QL, grid + (long)L * V, sizeof(double) * V);
+  } else {
+    if (ndim == 1)
+      return -1;
+    int Li[2] = {inds[0], inds[1]}, Lind;
+    int n0 = (n[0] > 0) - (n[0] < 0), n1 = (n[1] > 0) - (n[1] < 0);
+    int ny = nX[1];
+    if (fabs(n[0]) > fabs(n[1])) {
+      Li[0] -= n0;
+      Lind = Li[0] * ny + Li[1];
+      if (Lind >= 0 && Lind < ncell && ls_mat(grid + (long)Lind * V) == mat) {
+        n[0] = n0;
+        n[1] = 0.;
+      } else {
+        Li[0] += n0;
+        Li[1] -= n1;
+        Lind = Li[0] * ny + Li[1];
+        n[0] = 0.;
+        n[1] = n1;
+      }
+    } else {
+      Li[1] -= n1;
+      Lind = Li[0] * ny + Li[1];
+      if (Lind >= 0 && Lind < ncell && ls_mat(grid + (long)Lind * V) == mat) {
+        n[0] = 0.;
+        n[1] = n1;
+      } else {
+        Li[0] -= n0;
+        Li[1] += n1;
+        Lind = Li[0] * ny + Li[1];
+        n[0] = n0;
+        n[1] = 0.;
+      }
+    }
+    if (Lind < 0 || Lind >= ncell)
+      return -1;
+    if (ls_mat(grid + (long)Lind * V) == mat)
+      memcpy(QL, grid + (long)Lind * V, sizeof(double) * V);
+    else if (indn >= 0)
+      memcpy(QL, grid + (long)indn * V, sizeof(double) * V);
+    else
+      return -1;
+  }
+  or_left_star_state(QL, QR, MPs + mat, MPs + miR, dt, n, ndim, out);
+  memcpy(grid + (long)ind * V, out, sizeof(double) * (V - LSET));
+  if (ls_mat(grid + (long)interf * V) != mat)
+    memcpy(grid + (long)interf * V, out, sizeof(double) * (V - LSET));
+  return 0;
+}
+
+static void ls_normal(const double *g, int ndim, double *n) {
+  double s = 0;
+  for (int d = 0; d < ndim; d++)
+    s += g[d] * g[d];
+  s = sqrt(s);
+  for (int d = 0; d < ndim; d++)
+    n[d] = g[d] / s;
+}
+
+/* fill_boundary_cells (fill.cpp:200-235), in the reference's sequential
+ * (i, j) order. */
+int or_fill_boundary_cells(double *grid, const int32_t *mask, int mat, const double *phi,
+                           const double *dphi, const double *dX, const gpr_par *MPs,
+                           double dt, const int *nX, int ndim) {
+  int nx = nX[0], ny = ndim == 2 ? nX[1] : 1, bad = 0;
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      int ind = i * ny + j;
+      if (mask[ind] != 1)
+        continue;
+      int indn = ndim == 2 ? ls_neighbor_index(mask, i, j, nx, ny, -1) : -1;
+      double n[2];
+      ls_normal(dphi + (long)ind * ndim, ndim, n);
+      int inds[2] = {i, j};
+      if (ls_fill_boundary_inner(grid, inds, dX, nX, ndim, phi[ind], mat, MPs, dt, n, indn))
+        bad++;
+    }
+  return bad;
+}
+
+/* fill_neighbor_inner / fill_neighbor_cells (fill.cpp:237-328): layers
+ * N0 = 1 .. 10N-1 grow outwards from the boundary cells; each new cell
+ * copies the cell one step towards the interface along the normal if that
+ * one is already filled, else the layer neighbour it was reached from. */
+static void ls_fill_neighbor_inner(double *grid, const double *g, const int *inds,
+                                   const double *dX, const int *nX, int ndim,
+                                   const int32_t *mask, int indn) {
+  double n[2];
+  ls_normal(g, ndim, n);
+  int ni[2];
+  for (int d = 0; d < ndim; d++) {
+    double x = (inds[d] + 0.5) * dX[d];
+    double xn = x - dX[d] * n[d];
+    ni[d] = (int)(xn / dX[d]);
+  }
+  int ind = ndim == 1 ? inds[0] : inds[0] * nX[1] + inds[1];
+  int nind = ndim == 1 ? ni[0] : ni[0] * nX[1] + ni[1];
+  if (mask[nind] < 1)
+    nind = indn;
+  memcpy(grid + (long)ind * V, grid + (long)nind * V, sizeof(double) * (V - LSET));
+}
+
+void or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
+                            const double *dX, const int *nX, int ndim) {
+  int nx = nX[0];
+  int *isolates = ndim == 2 ? malloc(sizeof(int) * (long)nx * nX[1]) : NULL;
+  for (int N0 = 1; N0 < 10 * N; N0++) {
+    if (ndim == 1) {
+      for (int i = 0; i < nx; i++) {
+        if (mask[i] != 0)
+          continue;
+        int indn = -1;
+        if (i > 0 && mask[i - 1] == N0)
+          indn = i - 1;
+        if (i < nx - 1 && mask[i + 1] == N0)
+          indn = i + 1;
+        if (indn > -1) {
+          mask[i] = N0 + 1;
+          int inds[1] = {i};
+          ls_fill_neighbor_inner(grid, dphi + i, inds, dX, nX, 1, mask, indn);
+        }
+      }
+    } else {
+      int ny = nX[1], niso = 0;
+      for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++) {
+          int ind = i * ny + j;
+          if (mask[ind] != 0 && mask[ind] != -2)
+            continue;
+          int indn = ls_neighbor_index(mask, i, j, nx, ny, N0);
+          if (indn > -1) {
+            if (mask[ind] == -2)
+              isolates[niso++] = ind;
+            mask[ind] = N0 + 1;
+            int inds[2] = {i, j};
+            ls_fill_neighbor_inner(grid, dphi + 2 * (long)ind, inds, dX, nX, 2, mask, indn);
+          }
+        }
+      for (int k = 0; k < niso; k++)
+        mask[isolates[k]] = -2;
+    }
+  }
+  free(isolates);
+}
+
+/* fill_ghost_cells (fill.cpp:330-370) for LSET = 1 and nmat <= 2:
+ * re-distances the level set of u in place, then builds each material's
+ * grid (nmat x ncell x V) and update mask (nmat x ncell).  Returns the
+ * number of boundary cells whose fill would read outside the grid in the
+ * reference (they are left unfilled here), or -3 for an unsupported
+ * variant. */
+int or_fill_ghost_cells(double *grids, uint8_t *masks, double *u, const int *nX,
+                        int ndim, const double *dX, double dt, const gpr_par *MPs,
+                        int nmat, int32_t *intmask_out) {
+  if (LSET != 1 || THERMAL || nmat < 1 || nmat > 2)
+    return -3;
+  long ncell = ndim == 1 ? nX[0] : (long)nX[0] * nX[1];
+  double *col = malloc(sizeof(double) * ncell), *phi = malloc(sizeof(double) * ncell);
+  double *dphi = malloc(sizeof(double) * ncell * ndim);
+  int32_t *mask = malloc(sizeof(int32_t) * ncell);
+  for (long c = 0; c < ncell; c++)
+    col[c] = u[c * V + V - 1];
+  or_distance(col, dX, nX, ndim, phi);
+  for (long c = 0; c < ncell; c++)
+    u[c * V + V - 1] = phi[c];
+  int bad = 0;
+  for (int mat = 0; mat < nmat; mat++) {
+    double *grid = grids + (long)mat * ncell * V;
+    uint8_t *mk = masks + (long)mat * ncell;
+    if (MPs[mat].EOS <= -1) {
+      memset(mk, 0, ncell);
+      continue;
+    }
+    memcpy(grid, u, sizeof(double) * ncell * V);
+    for (long c = 0; c < ncell; c++)
+      phi[c] = mat == 0 ? u[c * V + V - 1] : -u[c * V + V - 1];
+    or_finite_difference(phi, dX, nX, ndim, dphi);
+    or_find_interface_cells(phi, nX, ndim, mask);
+    bad += or_fill_boundary_cells(grid, mask, mat, phi, dphi, dX, MPs, dt, nX, ndim);
+    or_fill_neighbor_cells(grid, mask, dphi, dX, nX, ndim);
+    for (long c = 0; c < ncell; c++)
+      mk[c] = (phi[c] <= 0. && mask[c] != -2) || mask[c] == 1;
+    if (intmask_out)
+      memcpy(intmask_out + (long)mat * ncell, mask, sizeof(int32_t) * ncell);
+  }
+  free(col);
+  free(phi);
+  free(dphi);
+  free(mask);
+  return bad;
+}
+
+/* make_u (solvers/iterator.cpp:12-42) for LSET = 1. */
+void or_make_u(double *u, const double *grids, const uint8_t *masks, long ncell,
+               const gpr_par *MPs, int nmat) {
+  for (long c = 0; c < ncell; c++) {
+    double s = 0, cnt = 0;
+    for (int mat = 0; mat < nmat; mat++)
+      if (masks[(long)mat * ncell + c]) {
+        s += grids[((long)mat * ncell + c) * V + V - 1];
+        cnt += 1.;
+      }
+    if (cnt > 0.)
+      u[c * V + V - 1] = s / cnt;
+    int mi = ls_mat(u + c * V);
+    if (MPs[mi].EOS > -1)
+      memcpy(u + c * V, grids + ((long)mi * ncell + c) * V, sizeof(double) * (V - 1));
+    else
+      memset(u + c * V, 0, sizeof(double) * (V - 1));
+  }
+}
+
+/* timestep (iterator.cpp:54-83) over the masked cells of every material. */
+double or_timestep_multi(const double *grids, const uint8_t *masks, long ncell,
+                         const double *dX, int ndim, double cfl, double t, double tf,
+                         int count, const gpr_par *MPs, int nmat) {
+  double MAX = 0.;
+  for (int mat = 0; mat < nmat; mat++) {
+    if (MPs[mat].EOS <= -1)
+      continue;
+    for (long c = 0; c < ncell; c++) {
+      if (!masks[(long)mat * ncell + c])
+        continue;
+      double tmp = 0.;
+      for (int d = 0; d < ndim; d++)
+        tmp += or_max_abs_eigs(grids + ((long)mat * ncell + c) * V, d, MPs + mat) / dX[d];
+      MAX = tmp > MAX ? tmp : MAX;
+    }
+  }
+  double dt = cfl / MAX;
+  if (count <= 5)
+    dt *= 0.2;
+  return t + dt > tf ? tf - t : dt;
+}
+
+/* renorm_distortion (solvers/utils.cpp:6-24) with the material of each cell
+ * taken from its level set. */
+void or_renorm_multi(double *u, long ncell, const gpr_par *MPs) {
+  for (long c = 0; c < ncell; c++) {
+    double *Q = u + c * V;
+    const gpr_par *P = MPs + ls_mat(Q);
+    if (P->EOS > -1 && Q[0] > 0) {
+      double k = cbrt(Q[0] / (P->rho0 * det3(Q + 5)));
+      for (int i = 0; i < 9; i++)
+        Q[5 + i] *= k;
+    }
+  }
+}

@@ -10,7 +10,9 @@
 //     (solvers/dg/dg.h:7) but does not bind (bindings.cpp:79);
 //   * multi-material containers are replaced by single-material wrappers
 //     (timestep_single, renorm_single) so plain numpy arrays can be passed;
-//   * small-matrix results are returned as numpy arrays.
+//   * small-matrix results are returned as numpy arrays;
+//   * the ghost-fluid routines (multi/) take and return plain arrays and
+//     lists of arrays.
 #include "etc/types.h"
 #include "options.h"
 
@@ -20,6 +22,9 @@
 
 #include "etc/globals.h"
 #include "etc/grid.h"
+#include "multi/fill.h"
+#include "multi/functions.h"
+#include "multi/pfmm.h"
 #include "solvers/dg/dg.h"
 #include "solvers/fv/fluxes.h"
 #include "solvers/fv/fv.h"
@@ -30,6 +35,7 @@
 #include "solvers/utils.h"
 #include "solvers/weno/weno.h"
 #include "system/eig.h"
+#include "system/multi/riemann.h"
 #include "system/equations.h"
 #include "system/jacobians.h"
 #include "system/relaxation/analytic.h"
@@ -141,6 +147,76 @@ static Vec vode_cell(Vecr Q, double dt, Par &MP) {
   return q;
 }
 
+// ---- level-set ghost fluid (LSET > 0 variants) ----
+static Vec vdistance(Vecr phi, Vecr dX, iVecr nX) {
+  aVec d = dX.array();
+  return distance(phi, d, nX);
+}
+
+static Mat vfinite_difference(Vecr phi, Vecr dX, iVecr nX) {
+  Mat D(phi.size(), nX.size());
+  aVec d = dX.array();
+  iVec n = nX;
+  finite_difference(D, phi, d, n);
+  return D;
+}
+
+static iVec vfind_interface_cells(Vecr phi, iVecr nX) {
+  iVec m(phi.size());
+  find_interface_cells(m, phi, nX);
+  return m;
+}
+
+static Vec vleft_star_state(Vecr QL, Vecr QR, Par &MPL, Par &MPR, double dt,
+                            Vecr n) {
+  VecV l = QL, r = QR;
+  Vec nn = n;
+  return left_star_state(l, r, MPL, MPR, dt, nn);
+}
+
+// fill_ghost_cells on u (re-distanced in place); returns (grids, masks).
+static py::tuple vfill_ghost_cells(Vecr u, iVecr nX, Vecr dX, double dt,
+                                   std::vector<Par> MPs) {
+  int nmat = MPs.size();
+  int ncell = u.size() / V;
+  std::vector<Vec> grids(nmat);
+  std::vector<bVec> masks(nmat);
+  for (int i = 0; i < nmat; i++) {
+    grids[i] = u;
+    masks[i] = bVec::Ones(ncell);
+  }
+  aVec dXa = dX.array();
+  fill_ghost_cells(grids, masks, u, nX, dXa, dt, MPs);
+  py::list g, mk;
+  for (int i = 0; i < nmat; i++) {
+    g.append(grids[i]);
+    Vec mm = masks[i].cast<double>();
+    mk.append(mm);
+  }
+  return py::make_tuple(g, mk);
+}
+
+static void vmake_u(Vecr u, std::vector<Vec> grids, std::vector<Vec> masks,
+                    std::vector<Par> MPs) {
+  std::vector<bVec> bm(masks.size());
+  for (size_t i = 0; i < masks.size(); i++)
+    bm[i] = masks[i].array() != 0.;
+  make_u(u, grids, bm, MPs);
+}
+
+static py::list iterator_multi(Vecr u, double tf, iVecr nX, Vecr dX, double CFL,
+                               iVecr bcs, bool SPLIT, bool HALF_STEP, bool STIFF,
+                               int FLUX, std::vector<Par> MPs,
+                               double contorted_tol) {
+  aVec dXa = dX.array();
+  std::vector<Vec> ret = iterator(u, tf, nX, dXa, CFL, bcs, SPLIT, HALF_STEP,
+                                  STIFF, FLUX, MPs, contorted_tol);
+  py::list out;
+  for (auto &r : ret)
+    out.append(r);
+  return out;
+}
+
 PYBIND11_MODULE(MODNAME, m) {
   m.doc() = "test-only bindings over the reference GPR solver";
 
@@ -213,4 +289,12 @@ PYBIND11_MODULE(MODNAME, m) {
   m.def("D", &vD);
   m.def("Bint", &vBint);
   m.def("ode_cell", &vode_cell);
+
+  m.def("distance", &vdistance);
+  m.def("finite_difference", &vfinite_difference);
+  m.def("find_interface_cells", &vfind_interface_cells);
+  m.def("left_star_state", &vleft_star_state);
+  m.def("fill_ghost_cells", &vfill_ghost_cells);
+  m.def("make_u", &vmake_u);
+  m.def("iterator_multi", &iterator_multi);
 }

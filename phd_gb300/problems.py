@@ -13,6 +13,12 @@ layout.
                     (code/python/tests/fluid/newtonian1.py:45-72, 400 cells).
 * batched_shock_tubes - many independent shock tubes with seeded random
                     sizes, states and materials.
+* shock_bubble    - 2D two-material ghost-fluid shock-bubble interaction
+                    (V = 15: viscous, one level set; the material layout of
+                    helium_bubble, code/python/tests/multi/material.py:43-96).
+* helium_bubble_1d - 1D two-material ghost-fluid problem with the layout of
+                    helium_bubble (code/python/tests/multi/material.py:43-96):
+                    shocked air, air, a helium slab, air; level set +-1.
 """
 import numpy as np
 
@@ -98,3 +104,81 @@ def batched_shock_tubes(count=512, nmin=128, nmax=2048, seed=20261203, tf=0.2):
                               pL=pL, rhoR=rhoR, pR=pR, vL=(vL, 0, 0),
                               vR=(vR, 0, 0), tf=tf))
     return out
+
+
+def _shear(s):
+    return np.array([[1.0, s, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+
+
+def shock_bubble(nx=800, ny=400, mu=1e-4, cs=1.0, mach=1.22, x_shock=0.2,
+                 radius=0.2, centre=(0.6, 0.5), rho_b=0.138, gamma_b=1.67, tf=0.8,
+                 shear=0.0):
+    """A Mach `mach` planar shock in an ideal gas (gamma 1.4, rho 1, p 1)
+    travelling right into a circular bubble of a second gas (gamma_b, rho_b,
+    p 1) on [0, 2] x [0, 1].  Both materials are viscous GPR fluids with shear
+    sound speed cs and viscosity mu, without heat conduction, so V = 15:
+    [rho, rho E, rho v, A, phi] with the level set phi = radius - |x - centre|
+    (positive inside the bubble: material 1, as in the reference's
+    helium_bubble where the second material carries phi = +1).  `shear`
+    multiplies every distortion by [[1, shear, 0], [0, 1, 0], [0, 0, 1]]
+    (det unchanged, energy adjusted): a parity variant whose interface
+    Riemann problems are well conditioned (at an isotropic distortion the
+    shear eigenvalues of the acoustic tensor coincide).  Returns
+    (u[nx, ny, 15], [MP_gas, MP_bubble], tf, dX, bcs)."""
+    g = 1.4
+    gas = material_params("sg", 1.0, cv=2.5, gamma=g, b0=cs, mu=mu)
+    bub = material_params("sg", rho_b, cv=2.5, gamma=gamma_b, b0=cs, mu=mu)
+    # Rankine-Hugoniot post-shock state for a shock of Mach `mach` into (1, 1)
+    M2 = mach * mach
+    p2 = 1.0 + 2 * g / (g + 1) * (M2 - 1)
+    r2 = (g + 1) * M2 / ((g - 1) * M2 + 2)
+    s = mach * np.sqrt(g)
+    v2 = s * (1 - 1 / r2)
+    dX = [2.0 / nx, 1.0 / ny]
+    x = (np.arange(nx) + 0.5) * dX[0]
+    y = (np.arange(ny) + 0.5) * dX[1]
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    phi = radius - np.sqrt((X - centre[0]) ** 2 + (Y - centre[1]) ** 2)
+
+    def Q(rho, p, v, MP):
+        A = (rho / MP.rho0) ** (1 / 3) * _shear(shear)
+        return np.concatenate([Cvec(rho, p, np.array([v, 0.0, 0.0]), MP, A), [0.0]])
+
+    Qpost, Qpre, Qbub = Q(r2, p2, v2, gas), Q(1.0, 1.0, 0.0, gas), Q(rho_b, 1.0, 0.0, bub)
+    u = np.where((X < x_shock)[..., None], Qpost, Qpre)
+    u = np.where((phi >= 0)[..., None], Qbub, u)
+    u[..., -1] = phi
+    return np.ascontiguousarray(u), [gas, bub], tf, dX, "transitive"
+
+
+def helium_bubble_1d(nx=200, mu=1e-2, cs=1.0, mach=1.22, rho_b=0.138, gamma_b=1.67,
+                     tf=0.3, shear=0.0):
+    """1D counterpart of shock_bubble with the layout of the reference's
+    helium_bubble: a Mach `mach` shock in air (gamma 1.4, rho 1, p 1) at
+    x < 0.05 moving right, air up to 0.4, a slab of the second gas on
+    [0.4, 0.6), air beyond; level set -1 in air, +1 in the slab (it is
+    re-distanced every step).  V = 15.  Returns (u[nx, 15], MPs, tf, dX,
+    bcs)."""
+    g = 1.4
+    gas = material_params("sg", 1.0, cv=2.5, gamma=g, b0=cs, mu=mu)
+    bub = material_params("sg", rho_b, cv=2.5, gamma=gamma_b, b0=cs, mu=mu)
+    M2 = mach * mach
+    p2 = 1.0 + 2 * g / (g + 1) * (M2 - 1)
+    r2 = (g + 1) * M2 / ((g - 1) * M2 + 2)
+    v2 = mach * np.sqrt(g) * (1 - 1 / r2)
+    dx = 1.0 / nx
+
+    def Q(rho, p, v, MP, phi):
+        A = (rho / MP.rho0) ** (1 / 3) * _shear(shear)
+        return np.concatenate([Cvec(rho, p, np.array([v, 0.0, 0.0]), MP, A), [phi]])
+
+    u = np.zeros((nx, 15))
+    for i in range(nx):
+        x = i * dx
+        if x < 0.05:
+            u[i] = Q(r2, p2, v2, gas, -1.0)
+        elif 0.4 <= x < 0.6:
+            u[i] = Q(rho_b, 1.0, 0.0, bub, 1.0)
+        else:
+            u[i] = Q(1.0, 1.0, 0.0, gas, -1.0)
+    return u, [gas, bub], tf, [dx], "transitive"

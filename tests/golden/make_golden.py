@@ -1,6 +1,6 @@
 """Generate the golden fixtures under tests/golden/ from the compiled
 reference solver (oracle/_ref, built by `python oracle/build_ref.py v17
-v17n3 v14`).
+v17n3 v15`).
 
 Every array in the fixtures is an output of the reference's own C++ code
 (haranjackson/phd, code/cpp/src) on seeded inputs; inputs are stored beside
@@ -128,7 +128,89 @@ def sheared(u0, MP, shear=0.3):
     return u
 
 
+def multi(R, name):
+    """Level-set ghost fluid (V = 15: viscous, one level set), two sg gases.
+
+    * distance / finite_difference / find_interface_cells on a perturbed
+      circular level set (80 x 40);
+    * left_star_state on random moving, sheared state pairs;
+    * fill_ghost_cells on a 48 x 24 sheared shock-bubble state after a few
+      reference steps;
+    * full reference time loops (solvers/iterator.cpp:85-170 with the ghost
+      fill): 40 x 20 and 1D helium-bubble runs.
+    Distortions are sheared: at an isotropic distortion the two shear
+    eigenvalues of the acoustic tensor coincide and the reference's
+    eigenvector matrix in riemann_constraints (riemann.cpp:136-141) is only
+    conditioned by rounding."""
+    out = {}
+    rng = np.random.default_rng(SEED)
+    bc2 = np.zeros(4, np.int32)
+    u, MPs, tf, dX, bcs = problems.shock_bubble(nx=80, ny=40, mu=1e-2, shear=0.3)
+    nX = np.array(u.shape[:2], np.int32)
+    phi = u[..., -1].ravel() * (1 + 0.3 * np.sin(3 * np.arange(u[..., -1].size)))
+    d = np.asarray(R.distance(phi, np.array(dX), nX))
+    out.update(ls_phi=phi, ls_nX=nX, ls_dX=np.array(dX), ls_dist=d,
+               ls_fd=np.asarray(R.finite_difference(d, np.array(dX), nX)),
+               ls_intmask=np.asarray(R.find_interface_cells(d, nX)))
+    RM = [rd.to_ref_par(R, m) for m in MPs]
+    cnt = 24
+    QL = np.zeros((cnt, 15))
+    QR = np.zeros((cnt, 15))
+    nn = np.zeros((cnt, 2))
+    dts = np.zeros(cnt)
+    star = np.zeros((cnt, 15))
+    sens = np.zeros(cnt)
+    for k in range(cnt):
+        QL[k] = rd.random_state(rng, MPs[0], V=14, vscale=0.2, lset=1)
+        QR[k] = rd.random_state(rng, MPs[1], V=14, vscale=0.2, lset=1)
+        QL[k, -1], QR[k, -1] = -0.5, 0.5
+        a = rng.uniform(0, 2 * np.pi)
+        nn[k] = np.cos(a), np.sin(a)
+        dts[k] = (0.0, 1e-3, 1e-2)[k % 3]
+        star[k] = R.left_star_state(QL[k], QR[k], RM[0], RM[1], dts[k], nn[k])
+        # the reference's own movement under 1e-15 relative input noise
+        for j in range(3):
+            ql = QL[k] * (1 + 1e-15 * rng.standard_normal(15))
+            qr = QR[k] * (1 + 1e-15 * rng.standard_normal(15))
+            sp = R.left_star_state(ql, qr, RM[0], RM[1], dts[k], nn[k])
+            sens[k] = max(sens[k], np.max(np.abs(sp - star[k]) / (1 + np.abs(star[k]))))
+    out.update(star_QL=QL, star_QR=QR, star_n=nn, star_dt=dts, star_out=star,
+               star_sens=sens)
+
+    u, MPs, tf, dX, bcs = problems.shock_bubble(nx=48, ny=24, mu=1e-2, shear=0.3)
+    nX = np.array(u.shape[:2], np.int32)
+    RM = [rd.to_ref_par(R, m) for m in MPs]
+    ret = R.iterator_multi(u.ravel().copy(), 0.01, nX, np.array(dX), 0.8, bc2, False,
+                           False, False, 0, RM, 1e9)
+    uf = np.asarray(ret[99]).copy()
+    ur = uf.copy()
+    g, m = R.fill_ghost_cells(ur, nX, np.array(dX), 2e-3, RM)
+    out.update(fill_u=uf, fill_nX=nX, fill_dX=np.array(dX), fill_dt=np.array(2e-3),
+               fill_u_out=ur, fill_grids=np.stack([np.asarray(x) for x in g]),
+               fill_masks=np.stack([np.asarray(x) != 0 for x in m]))
+
+    u, MPs, tf, dX, bcs = problems.shock_bubble(nx=40, ny=20, mu=1e-2, shear=0.3)
+    nX = np.array(u.shape[:2], np.int32)
+    RM = [rd.to_ref_par(R, m) for m in MPs]
+    ret = R.iterator_multi(u.ravel().copy(), 0.004, nX, np.array(dX), 0.8, bc2, False,
+                           False, False, 0, RM, 1e9)
+    out.update(run2d_u0=u, run2d_tf=np.array(0.004), run2d_dX=np.array(dX),
+               run2d_u_end=np.asarray(ret[99]).reshape(u.shape))
+    u, MPs, tf, dX, bcs = problems.helium_bubble_1d(nx=200, shear=0.3)
+    ret = R.iterator_multi(u.ravel().copy(), 0.05, np.array([200], np.int32),
+                           np.array(dX), 0.8, np.zeros(2, np.int32), False, False,
+                           False, 0, RM, 1e9)
+    out.update(run1d_u0=u, run1d_tf=np.array(0.05), run1d_dX=np.array(dX),
+               run1d_u_end=np.asarray(ret[99]).reshape(u.shape))
+    out["mp_arrays"] = np.stack([MP.to_array() for MP in MPs])
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print("wrote", name)
+
+
 def main():
+    R15 = rd.load("v15")
+    if R15 is not None:
+        multi(R15, "multi_v15.npz")
     R = rd.load("v17")
     if R is None:
         print("oracle/_ref/GPRref_v17 not built; run oracle/build_ref.py v17")

@@ -1,0 +1,112 @@
+"""The CPU oracle's level-set ghost fluid (V = 15: viscous, one level set)
+against golden vectors from the reference's own C++ (tests/golden/
+make_golden.py, multi_v15.npz): re-distancing (multi/pfmm.cpp, first-order
+fast marching), normals (multi/functions.cpp:16-54), interface cells
+(multi/fill.cpp:20-74), the interface Riemann problem
+(system/multi/riemann.cpp:203-233), the whole fill (multi/fill.cpp:330-370)
+and full two-material time loops (solvers/iterator.cpp:85-170)."""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+from oracle import Oracle
+from phd_gb300.params import Par
+
+
+@pytest.fixture(scope="module")
+def O():
+    return Oracle(N=2, thermal=False, lset=1)
+
+
+@pytest.fixture(scope="module")
+def g():
+    return golden("multi_v15.npz")
+
+
+@pytest.fixture(scope="module")
+def MPs(g):
+    return [Par.from_array(a) for a in g["mp_arrays"]]
+
+
+def test_distance_normals_interface(O, g):
+    nX, dX = g["ls_nX"], list(g["ls_dX"])
+    d = O.distance(g["ls_phi"], dX, nX)
+    # the marcher's quadratic updates in a different association order
+    assert np.max(np.abs(d - g["ls_dist"])) < 1e-13
+    fd = O.finite_difference(g["ls_dist"], dX, nX)
+    assert np.array_equal(fd, g["ls_fd"])
+    im = O.find_interface_cells(g["ls_dist"], nX)
+    assert np.array_equal(im, g["ls_intmask"])
+    assert set(np.unique(im)) <= {-2, -1, 0, 1}
+    assert (im == 1).sum() > 20 and (im == -1).sum() > 20
+
+
+def test_distance_no_crossing_is_zero(O):
+    """base_marcher.cpp:103-106: nothing to march from -> zeros."""
+    d = O.distance(np.ones(12), [0.1, 0.1], np.array([3, 4], np.int32))
+    assert np.array_equal(d, np.zeros(12))
+
+
+def test_left_star_state(O, g, MPs):
+    """1e-10, or ten times the reference's own movement under 1e-15 input
+    noise where that is larger (states near a loss of hyperbolicity).  The
+    fixture includes a state whose acoustic tensor has a negative eigenvalue:
+    the reference returns its input there."""
+    fallback = 0
+    for k in range(g["star_QL"].shape[0]):
+        out = O.left_star_state(g["star_QL"][k], g["star_QR"][k], MPs[0], MPs[1],
+                                float(g["star_dt"][k]), g["star_n"][k])
+        tol = max(1e-10, 10 * float(g["star_sens"][k]))
+        assert rel_err(out, g["star_out"][k]) < tol, k
+        fallback += np.array_equal(g["star_out"][k], g["star_QL"][k])
+    assert fallback >= 1
+
+
+def test_fill_ghost_cells(O, g, MPs):
+    nX, dX = g["fill_nX"], list(g["fill_dX"])
+    u, grids, masks, im, bad = O.fill_ghost_cells(g["fill_u"], nX, dX,
+                                                  float(g["fill_dt"]), MPs)
+    assert bad == 0
+    assert np.max(np.abs(u - g["fill_u_out"])) < 1e-13
+    assert np.array_equal(masks, g["fill_masks"])
+    ref = g["fill_grids"].reshape(grids.shape)
+    # Cells the fill leaves alone are copies of u.  Filled cells carry an
+    # interface Riemann solution; where its ten linearised steps stop short
+    # of STAR_TOL the reference itself moves by up to 1.4e-7 under 1e-15
+    # input noise, so those cells are held to 1e-6 and most to 1e-10.
+    filled = (im == 1) | (im > 1)
+    assert rel_err(grids[~filled], ref[~filled]) < 1e-13
+    per_cell = np.max(np.abs(grids - ref) / (1 + np.abs(ref)), axis=2)[filled]
+    assert per_cell.max() < 1e-6
+    assert np.mean(per_cell < 1e-10) > 0.9
+
+
+def test_two_material_loop_2d(O, g, MPs):
+    u, steps, t = O.run_multi(g["run2d_u0"], MPs, float(g["run2d_tf"]),
+                              list(g["run2d_dX"]), 0)
+    assert steps == 4
+    assert rel_err(u, g["run2d_u_end"]) < 1e-10
+
+
+def test_two_material_loop_1d(O, g, MPs):
+    u, steps, t = O.run_multi(g["run1d_u0"], MPs, float(g["run1d_tf"]),
+                              list(g["run1d_dX"]), 0)
+    assert steps == 51
+    assert rel_err(u, g["run1d_u_end"]) < 1e-9
+
+
+def test_make_u_takes_each_cell_from_its_material(O, MPs):
+    """solvers/iterator.cpp:12-42: level set averaged over the grids that
+    updated the cell, the rest of the state from the cell's material."""
+    rng = np.random.default_rng(3)
+    ncell = 10
+    grids = rng.standard_normal((2, ncell, 15))
+    masks = np.ones((2, ncell), bool)
+    masks[0, :3] = False
+    u = rng.standard_normal((ncell, 15))
+    out = O.make_u(u.copy().ravel(), grids, masks, MPs).reshape(ncell, 15)
+    phi = np.where(masks.all(0), grids[:, :, -1].mean(0), grids[1, :, -1])
+    assert np.allclose(out[:, -1], phi, rtol=0, atol=1e-15)
+    for c in range(ncell):
+        mat = 1 if out[c, -1] >= 0 else 0
+        assert np.array_equal(out[c, :14], grids[mat, c, :14])
