@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-shock-bubble", action="store_true")
+    ap.add_argument("--profile-shock-bubble", type=int, default=0, metavar="NX",
+                    help="run --profile-steps steps of the NX x NX/2 shock bubble only "
+                         "(for ncu captures)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
     ap.add_argument("--profile-shock-tube", type=int, default=-1, metavar="FLUX",
@@ -399,6 +403,12 @@ def run_gb300(args):
             shock = shock_tube_bench(torch)
         except Exception as ex:  # reported, not fatal to the main line
             shock = {"error": str(ex)}
+    bubble = None
+    if rank == 0 and not args.no_shock_bubble:
+        try:
+            bubble = shock_bubble_bench(torch, cpu_steps=0 if args.no_cpu_baseline else 2)
+        except Exception as ex:  # reported, not fatal to the main line
+            bubble = {"error": str(ex)}
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         try:
@@ -431,6 +441,7 @@ def run_gb300(args):
                     "d2h_bytes_per_step": ncell * V * 8},
             "batched": batched,
             "shock_tube": shock,
+            "shock_bubble": bubble,
             "adjoint": adjoint,
             "gpu_launches": 14 * args.steps,
             "clocks": cs.summary()}
@@ -507,6 +518,100 @@ def shock_tube_bench(torch):
                      "unit": UNIT, "max_rel_diff_vs_oracle":
                          float(np.max(np.abs(got - ref) / (1.0 + np.abs(ref))))}
     return out
+
+
+def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
+    """2D two-material ghost-fluid shock-bubble: 800 x 400 cells on [0, 2] x
+    [0, 1], V = 15 (viscous, one level set), ideal gas gamma 1.4 (rho 1, p
+    1) around a circular bubble of radius 0.2 at (0.6, 0.5) of gamma 1.67,
+    rho 0.138, p 1; a Mach 1.22 shock from the left; cs = 1, mu = 1e-4;
+    Rusanov flux, CFL 0.8, transmissive boundaries.  A step is one step of the
+    reference's two-material iterator: ghost fill (re-distancing, interface
+    Riemann states, extrapolation layers, for both materials) -> CFL over
+    both masked grids -> masked ADER step of each material -> make_u ->
+    renorm, device resident (gpr_iterate_multi).  The ghost fill is also
+    timed alone; the oracle runs `cpu_steps` steps of the same grid on the
+    host cores."""
+    from phd_gb300 import ghost, problems
+    from oracle import Oracle
+    ny = nx // 2
+    u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=nx, ny=ny)
+    nX = np.array([nx, ny], np.int32)
+    ncell = nx * ny
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device=dev)
+    it = ghost.MultiIterator(nX, dX, 0, MPs, 0.8, tf, device=dev)
+    it.run(u, warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    it.run(u, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = it.clock.cpu().numpy()
+    status = it.status.cpu().numpy().tolist()
+    # the ghost fill alone, on the current state
+    grids = torch.empty(2, ncell * 15, dtype=torch.float64, device=dev)
+    masks = torch.empty(2, ncell, dtype=torch.bool, device=dev)
+    uf = u.clone()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ghost.fill_ghost_cells(grids, masks, uf, nX, dX, float(clk[1]), MPs)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    for _ in range(3):
+        ghost.fill_ghost_cells(grids, masks, uf, nX, dX, float(clk[1]), MPs)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fill_ms = f0.elapsed_time(f1) / 3
+    # end to end with host buffers: H2D of the state, one step, D2H, per step
+    host = torch.empty(ncell * 15, dtype=torch.float64, pin_memory=True)
+    host.copy_(u.cpu())
+    ue = torch.empty_like(u)
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(steps):
+        ue.copy_(host, non_blocking=True)
+        it.run(ue, 1)
+        host.copy_(ue, non_blocking=True)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = g0.elapsed_time(g1)
+    out = {"workload": "shock bubble %dx%d, V=15, two materials, mu=1e-4, CFL 0.8, Rusanov"
+                       % (nx, ny),
+           "steps": steps, "ms_per_step": ms / steps,
+           "value": ncell * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
+           "fill_ms": fill_ms, "fill_share": fill_ms / (ms / steps),
+           "e2e": {"value": ncell * steps / (e2e_ms * 1e-3) / 1e6, "unit": UNIT,
+                   "h2d_bytes_per_step": ncell * 15 * 8, "d2h_bytes_per_step": ncell * 15 * 8},
+           "sim_time": float(clk[0]), "sim_steps": int(clk[4]), "fill_status": status}
+    if cpu_steps:
+        O = Oracle(N=2, thermal=False, lset=1)
+        uc = u0.copy()
+        t0 = time.perf_counter()
+        dt, t = 0.0, 0.0
+        for s in range(cpu_steps):
+            dt = O.step_multi(uc, dt, t, tf, s, MPs, dX, 0)
+            t += dt
+        cpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": ncell * cpu_steps / cpu_s / 1e6, "unit": UNIT,
+                               "cores": O.num_threads(), "kind": "port",
+                               "sample": "first %d steps of the %dx%d grid" % (cpu_steps, nx, ny)}
+    return out
+
+
+def profile_shock_bubble(nx, steps):
+    """`steps` steps of the nx x nx/2 shock bubble (for ncu captures)."""
+    import torch
+    from phd_gb300 import ghost, problems
+    u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=nx, ny=nx // 2)
+    u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+    it = ghost.MultiIterator(np.array([nx, nx // 2], np.int32), dX, 0, MPs, 0.8, tf)
+    it.run(u, steps)
+    torch.cuda.synchronize()
+    ghost.check_status(it.status)
+    return 0
 
 
 def adjoint_bench(torch, fd_check=True):
@@ -831,6 +936,8 @@ def main():
         return profile_adjoint(args.profile_adjoint, args.profile_steps or 32)
     if args.profile_shock_tube >= 0:
         return profile_shock_tube(args.profile_shock_tube, args.profile_steps or 10)
+    if args.profile_shock_bubble:
+        return profile_shock_bubble(args.profile_shock_bubble, args.profile_steps or 4)
     return run_gb300(args)
 
 

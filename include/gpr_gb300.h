@@ -304,6 +304,82 @@ int gpr_adj_point_jacobians(const double *Q, int64_t count, const gpr_par *par, 
                             double *JS, double *dlam, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Level-set ghost fluid (GPRpy.multi.*, code/cpp/src/multi/*.cpp, and
+ * system/multi/riemann.cpp) for the V = 15 layout (viscous, one level set,
+ * no heat conduction) and exactly two materials: material 0 occupies
+ * phi < 0, material 1 phi >= 0 (functions/vectors.cpp:24-31); pars[2].
+ * nX[d] >= 3.  Every fill call accumulates error counts in the caller's
+ * device status[4] (zero it first): [0] the re-distancing did not converge
+ * within its round budget, [1] boundary cells whose fill would read outside
+ * the grid in the reference (left unfilled), [2] extrapolation cells whose
+ * copy source would lie outside the grid (they copy their layer neighbour),
+ * [3] reserved.
+ *
+ * gpr_distance             GPRpy.system.multi.distance (multi/pfmm.cpp:4-26):
+ *                          first-order signed distance to the zero level of
+ *                          phi[ncell]; zeros if phi has no zero crossing.
+ *                          scratch: gpr_distance_scratch_doubles.
+ * gpr_finite_difference    GPRpy.multi.finite_difference
+ *                          (multi/functions.cpp:16-54): dphi[ncell][ndim].
+ * gpr_find_interface_cells GPRpy.multi.find_interface_cells (multi/fill.cpp:20-74):
+ *                          intMask[ncell] in {-2, -1, 0, 1}.
+ * gpr_left_star_state      GPRpy.system.multi.left_star_state
+ *                          (riemann.cpp:203-233), batched: out[k] = left star
+ *                          state of QL[k] | QR[k] along n[k][ndim].
+ * gpr_fill_boundary_cells  GPRpy.multi.fill_boundary_cells (multi/fill.cpp:200-235):
+ *                          grid of material mat, its level set phi, normals
+ *                          dphi and intMask; scratch: gpr_fill_scratch_doubles.
+ * gpr_fill_neighbor_cells  GPRpy.multi.fill_neighbor_cells (multi/fill.cpp:255-328):
+ *                          intMask updated in place; scratch: gpr_fill_scratch_doubles.
+ * gpr_fill_ghost_cells     GPRpy.multi.fill_ghost_cells (multi/fill.cpp:330-370):
+ *                          re-distances u's level set in place and writes
+ *                          grids[2][ncell][V] and masks[2][ncell].
+ * gpr_make_u               GPRpy.solvers.make_u (solvers/iterator.cpp:12-42).
+ * gpr_renorm_multi         GPRpy.solvers.renorm_distortion (solvers/utils.cpp:6-23)
+ *                          with each cell's material from its level set.
+ * gpr_timestep_multi       solvers/iterator.cpp:54-83 over the masked cells of
+ *                          both grids; dt_out is a device double; scratch: 1 double.
+ * gpr_iterate_multi        GPRpy.solvers.iterator (solvers/iterator.cpp:85-170)
+ *                          with the ghost fill, ADER scheme, Rusanov flux,
+ *                          device resident as gpr_iterate; clock[5] as there
+ *                          (set dt = 0 before the first step); scratch:
+ *                          gpr_iterate_multi_scratch_doubles. */
+long gpr_distance_scratch_doubles(const int32_t *nX, int ndim);
+int gpr_distance(const double *phi, double *dist, const int32_t *nX, int ndim,
+                 const double *dX, double *scratch, int32_t *status, void *stream);
+int gpr_finite_difference(const double *phi, double *dphi, const int32_t *nX, int ndim,
+                          const double *dX, void *stream);
+int gpr_find_interface_cells(const double *phi, int32_t *intMask, const int32_t *nX, int ndim,
+                             void *stream);
+int gpr_left_star_state(const double *QL, const double *QR, const double *n, double *out,
+                        int64_t count, int ndim, double dt, const gpr_par *parL,
+                        const gpr_par *parR, int nvar, void *stream);
+long gpr_fill_scratch_doubles(const int32_t *nX, int ndim, int nvar);
+int gpr_fill_boundary_cells(double *grid, const int32_t *intMask, int mat, const double *phi,
+                            const double *dphi, const double *dX, const gpr_par *pars,
+                            int nmat, double dt, const int32_t *nX, int ndim, double *scratch,
+                            int32_t *status, int nvar, void *stream);
+int gpr_fill_neighbor_cells(double *grid, int32_t *intMask, const double *dphi,
+                            const double *dX, const int32_t *nX, int ndim, double *scratch,
+                            int32_t *status, int nvar, void *stream);
+int gpr_fill_ghost_cells(double *grids, uint8_t *masks, double *u, const int32_t *nX, int ndim,
+                         const double *dX, double dt, const gpr_par *pars, int nmat,
+                         double *scratch, int32_t *status, int nvar, void *stream);
+int gpr_make_u(double *u, const double *grids, const uint8_t *masks, int64_t ncell,
+               const gpr_par *pars, int nmat, int nvar, void *stream);
+int gpr_renorm_multi(double *u, int64_t ncell, const gpr_par *pars, int nmat, int nvar,
+                     void *stream);
+int gpr_timestep_multi(const double *grids, const uint8_t *masks, int64_t ncell,
+                       const double *dX, int ndim, double cfl, double t, double tf, int count,
+                       const gpr_par *pars, int nmat, double *dt_out, double *scratch,
+                       int nvar, void *stream);
+long gpr_iterate_multi_scratch_doubles(const int32_t *nX, int ndim, int nvar);
+int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
+                      const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
+                      double *clock, int nsteps, double *scratch, int32_t *status, int nvar,
+                      void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,
  * eig.cpp): batched over `count` states Q[count][V].                        */
 

@@ -93,6 +93,9 @@ def _load():
             "or_fill_ghost_cells": (ctypes.c_int, [_dp, _u8p, _dp, _ip, ctypes.c_int, _dp,
                                                    ctypes.c_double, P, ctypes.c_int, _ip]),
             "or_make_u": (None, [_dp, _dp, _u8p, ctypes.c_long, P, ctypes.c_int]),
+            "or_fill_boundary_cells": (ctypes.c_int, [_dp, _ip, ctypes.c_int, _dp, _dp, _dp,
+                                                      P, ctypes.c_double, _ip, ctypes.c_int]),
+            "or_fill_neighbor_cells": (ctypes.c_int, [_dp, _ip, _dp, _dp, _ip, ctypes.c_int]),
             "or_timestep_multi": (ctypes.c_double, [_dp, _u8p, ctypes.c_long, _dp,
                                                     ctypes.c_int, ctypes.c_double,
                                                     ctypes.c_double, ctypes.c_double,
@@ -439,6 +442,27 @@ class Oracle:
             raise RuntimeError("oracle fill_ghost_cells: unsupported variant")
         return u, grids, masks.astype(bool), im, bad
 
+    def fill_boundary_cells(self, grid, mask, mat, phi, dphi, dX, MPs, dt, nX):
+        """multi/fill.cpp:200-235 in the reference's (i, j) order, in place on
+        grid; returns the number of cells whose fill would read off the grid."""
+        lib = self._cfg()
+        arr, p = self._pars(MPs)
+        nX = np.asarray(nX, dtype=np.int32)
+        return lib.or_fill_boundary_cells(
+            _d(grid), _i(np.ascontiguousarray(mask, dtype=np.int32)), int(mat),
+            _d(np.ascontiguousarray(phi, dtype=np.float64)),
+            _d(np.ascontiguousarray(dphi, dtype=np.float64)),
+            _d(np.asarray(dX, dtype=np.float64)), p, float(dt), _i(nX), len(nX))
+
+    def fill_neighbor_cells(self, grid, mask, dphi, dX, nX):
+        """multi/fill.cpp:255-328, in place on grid and mask (int32)."""
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        return lib.or_fill_neighbor_cells(_d(grid), _i(mask),
+                                          _d(np.ascontiguousarray(dphi, dtype=np.float64)),
+                                          _d(np.asarray(dX, dtype=np.float64)), _i(nX),
+                                          len(nX))
+
     def make_u(self, u, grids, masks, MPs):
         lib = self._cfg()
         arr, p = self._pars(MPs)
@@ -462,39 +486,48 @@ class Oracle:
         lib.or_renorm_multi(_d(u), u.size // self.V, p)
         return u
 
-    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None):
-        """Time loop of solvers/iterator.cpp:85-151 with the ghost-fluid fill
-        (LSET = 1): fill -> timestep -> per material boundaries + ADER step
-        on its masked cells -> make_u -> renorm.  Returns (u, steps, t)."""
-        shape = u0.shape
-        nX = np.array(shape[:-1], dtype=np.int32)
-        nd = len(nX)
-        u = np.ascontiguousarray(u0, dtype=np.float64).ravel().copy()
+    def step_multi(self, u, dt_prev, t, tf, count, MPs, dX, bcs, cfl=0.8, dt=None):
+        """One step of the time loop of solvers/iterator.cpp:85-151 with the
+        ghost-fluid fill (LSET = 1): fill (with the previous step's dt) ->
+        timestep -> per material boundaries + ADER step on its masked cells
+        -> make_u -> renorm.  u (flat or shaped, cell-major) is updated in
+        place; `dt` overrides the CFL step.  Returns dt."""
+        nd = len(dX)
         ncell = u.size // self.V
+        nX = np.asarray(u.shape[:-1] if u.ndim > 1 else [ncell], dtype=np.int32)
+        if nX.size != nd:
+            raise ValueError("pass u shaped (nx[, ny], V)")
+        uf = u.reshape(-1)
         nmat = len(MPs)
-        grids = np.stack([u.reshape(ncell, self.V)] * nmat)
-        masks = np.ones((nmat, ncell), dtype=bool)
         bc = (np.array([bcs] * 2 * nd, dtype=np.int32) if np.isscalar(bcs)
               else np.asarray(bcs, np.int32))
+        uf[:], grids, masks, _, _ = self.fill_ghost_cells(uf, nX, dX, dt_prev, MPs)
+        if dt is None:
+            dt = self.timestep_multi(grids, masks, dX, cfl, t, tf, count, MPs)
+        for mat in range(nmat):
+            if MPs[mat].EOS <= -1:
+                continue
+            g = np.ascontiguousarray(grids[mat]).ravel()
+            ub = self.boundaries(g, nX, bc)
+            maskb = self.extend_mask(masks[mat].astype(np.uint8), nX)
+            self.ader_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb)
+            grids[mat] = g.reshape(ncell, self.V)
+        self.make_u(uf, grids, masks, MPs)
+        self.renorm_multi(uf, MPs)
+        return dt
+
+    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None):
+        """The two-material time loop (step_multi until tf).  Returns
+        (u, steps, t)."""
+        u = np.ascontiguousarray(u0, dtype=np.float64).copy()
         t, count, dt = 0.0, 0, 0.0
         while t < tf:
-            u, grids, masks, _, _ = self.fill_ghost_cells(u, nX, dX, dt, MPs)
-            dt = self.timestep_multi(grids, masks, dX, cfl, t, tf, count, MPs)
-            for mat in range(nmat):
-                if MPs[mat].EOS <= -1:
-                    continue
-                g = np.ascontiguousarray(grids[mat]).ravel()
-                ub = self.boundaries(g, nX, bc)
-                maskb = self.extend_mask(masks[mat].astype(np.uint8), nX)
-                self.ader_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb)
-                grids[mat] = g.reshape(ncell, self.V)
-            self.make_u(u, grids, masks, MPs)
+            dt = self.step_multi(u, dt, t, tf, count, MPs, dX, bcs, cfl)
             t += dt
             count += 1
-            self.renorm_multi(u, MPs)
             if max_steps is not None and count >= max_steps:
                 break
-        return u.reshape(shape), count, t
+        return u, count, t
 
     def num_threads(self):
         return self.lib.or_num_threads()

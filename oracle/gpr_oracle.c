@@ -3426,8 +3426,10 @@ static int ls_constraints(const double *Q, double sgn, const gpr_par *P, double 
    * (riemann.cpp:136-141) is NaN when an eigenvalue has a non-positive real
    * part, and singular for a complex pair (the real parts of conjugate
    * eigenvectors coincide); left_star_state then returns its input.  A pair
-   * counts as complex when its imaginary part exceeds 1e-8 of the spectral
-   * radius (below that the reference's choice is decided by rounding). */
+   * counts as complex when its imaginary part exceeds 1e-6 of the spectral
+   * radius: a double eigenvalue (an isotropic distortion) splits by about
+   * sqrt(eps) under rounding, and there the reference's choice is decided
+   * by rounding alone. */
   {
     double wr[3], wi[3];
     if (or_eigenvalues(3, Xi, wr, wi))
@@ -3436,7 +3438,7 @@ static int ls_constraints(const double *Q, double sgn, const gpr_par *P, double 
     for (int i = 0; i < 3; i++)
       rad = fmax(rad, hypot(wr[i], wi[i]));
     for (int i = 0; i < 3; i++)
-      if (!(wr[i] > 0) || fabs(wi[i]) > 1e-8 * rad)
+      if (!(wr[i] > 0) || fabs(wi[i]) > 1e-6 * rad)
         return -1;
   }
   if (ls_inv_sqrt(3, Xi, Y0))
@@ -3706,13 +3708,19 @@ static int ls_fill_boundary_inner(double *grid, const int *inds, const double *d
   return 0;
 }
 
-static void ls_normal(const double *g, int ndim, double *n) {
+/* normal (multi/functions.cpp:14); returns 0 when it is not finite (a zero
+ * gradient), where the reference would truncate NaN positions to indices. */
+static int ls_normal(const double *g, int ndim, double *n) {
   double s = 0;
   for (int d = 0; d < ndim; d++)
     s += g[d] * g[d];
   s = sqrt(s);
-  for (int d = 0; d < ndim; d++)
+  int ok = 1;
+  for (int d = 0; d < ndim; d++) {
     n[d] = g[d] / s;
+    ok = ok && isfinite(n[d]);
+  }
+  return ok;
 }
 
 /* fill_boundary_cells (fill.cpp:200-235), in the reference's sequential
@@ -3728,9 +3736,9 @@ int or_fill_boundary_cells(double *grid, const int32_t *mask, int mat, const dou
         continue;
       int indn = ndim == 2 ? ls_neighbor_index(mask, i, j, nx, ny, -1) : -1;
       double n[2];
-      ls_normal(dphi + (long)ind * ndim, ndim, n);
       int inds[2] = {i, j};
-      if (ls_fill_boundary_inner(grid, inds, dX, nX, ndim, phi[ind], mat, MPs, dt, n, indn))
+      if (!ls_normal(dphi + (long)ind * ndim, ndim, n) ||
+          ls_fill_boundary_inner(grid, inds, dX, nX, ndim, phi[ind], mat, MPs, dt, n, indn))
         bad++;
     }
   return bad;
@@ -3740,27 +3748,31 @@ int or_fill_boundary_cells(double *grid, const int32_t *mask, int mat, const dou
  * N0 = 1 .. 10N-1 grow outwards from the boundary cells; each new cell
  * copies the cell one step towards the interface along the normal if that
  * one is already filled, else the layer neighbour it was reached from. */
-static void ls_fill_neighbor_inner(double *grid, const double *g, const int *inds,
-                                   const double *dX, const int *nX, int ndim,
-                                   const int32_t *mask, int indn) {
+static int ls_fill_neighbor_inner(double *grid, const double *g, const int *inds,
+                                  const double *dX, const int *nX, int ndim,
+                                  const int32_t *mask, int indn) {
   double n[2];
-  ls_normal(g, ndim, n);
-  int ni[2];
-  for (int d = 0; d < ndim; d++) {
+  int finite = ls_normal(g, ndim, n);
+  int ni[2] = {0, 0};
+  for (int d = 0; d < ndim && finite; d++) {
     double x = (inds[d] + 0.5) * dX[d];
     double xn = x - dX[d] * n[d];
     ni[d] = (int)(xn / dX[d]);
   }
   int ind = ndim == 1 ? inds[0] : inds[0] * nX[1] + inds[1];
   int nind = ndim == 1 ? ni[0] : ni[0] * nX[1] + ni[1];
-  if (mask[nind] < 1)
+  long ncell = ndim == 1 ? nX[0] : (long)nX[0] * nX[1];
+  /* one cell past the last row: the reference reads outside its mask */
+  int off = !finite || nind < 0 || nind >= ncell;
+  if (off || mask[nind] < 1)
     nind = indn;
   memcpy(grid + (long)ind * V, grid + (long)nind * V, sizeof(double) * (V - LSET));
+  return off ? -1 : 0;
 }
 
-void or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
-                            const double *dX, const int *nX, int ndim) {
-  int nx = nX[0];
+int or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
+                           const double *dX, const int *nX, int ndim) {
+  int nx = nX[0], bad = 0;
   int *isolates = ndim == 2 ? malloc(sizeof(int) * (long)nx * nX[1]) : NULL;
   for (int N0 = 1; N0 < 10 * N; N0++) {
     if (ndim == 1) {
@@ -3775,7 +3787,7 @@ void or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
         if (indn > -1) {
           mask[i] = N0 + 1;
           int inds[1] = {i};
-          ls_fill_neighbor_inner(grid, dphi + i, inds, dX, nX, 1, mask, indn);
+          bad += ls_fill_neighbor_inner(grid, dphi + i, inds, dX, nX, 1, mask, indn) != 0;
         }
       }
     } else {
@@ -3791,7 +3803,8 @@ void or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
               isolates[niso++] = ind;
             mask[ind] = N0 + 1;
             int inds[2] = {i, j};
-            ls_fill_neighbor_inner(grid, dphi + 2 * (long)ind, inds, dX, nX, 2, mask, indn);
+            bad += ls_fill_neighbor_inner(grid, dphi + 2 * (long)ind, inds, dX, nX, 2, mask,
+                                          indn) != 0;
           }
         }
       for (int k = 0; k < niso; k++)
@@ -3799,14 +3812,15 @@ void or_fill_neighbor_cells(double *grid, int32_t *mask, const double *dphi,
     }
   }
   free(isolates);
+  return bad;
 }
 
 /* fill_ghost_cells (fill.cpp:330-370) for LSET = 1 and nmat <= 2:
  * re-distances the level set of u in place, then builds each material's
  * grid (nmat x ncell x V) and update mask (nmat x ncell).  Returns the
  * number of boundary cells whose fill would read outside the grid in the
- * reference (they are left unfilled here), or -3 for an unsupported
- * variant. */
+ * reference (they are left unfilled here) or whose layered fill would
+ * read past the last cell, or -3 for an unsupported variant. */
 int or_fill_ghost_cells(double *grids, uint8_t *masks, double *u, const int *nX,
                         int ndim, const double *dX, double dt, const gpr_par *MPs,
                         int nmat, int32_t *intmask_out) {
@@ -3835,7 +3849,7 @@ int or_fill_ghost_cells(double *grids, uint8_t *masks, double *u, const int *nX,
     or_finite_difference(phi, dX, nX, ndim, dphi);
     or_find_interface_cells(phi, nX, ndim, mask);
     bad += or_fill_boundary_cells(grid, mask, mat, phi, dphi, dX, MPs, dt, nX, ndim);
-    or_fill_neighbor_cells(grid, mask, dphi, dX, nX, ndim);
+    bad += or_fill_neighbor_cells(grid, mask, dphi, dX, nX, ndim);
     for (long c = 0; c < ncell; c++)
       mk[c] = (phi[c] <= 0. && mask[c] != -2) || mask[c] == 1;
     if (intmask_out)

@@ -13,11 +13,12 @@ include/gpr_gb300.h.
 from types import SimpleNamespace
 
 from . import api
+from . import ghost as _multi
 from ._lib import build, load
 from .params import Par, material_params, Cvec
 from . import problems
 
-__all__ = ["boundaries", "extend_mask", "options", "classes", "solvers", "system",
+__all__ = ["boundaries", "extend_mask", "options", "classes", "solvers", "system", "multi",
            "build", "load", "Par", "material_params", "Cvec", "problems"]
 
 boundaries = api.boundaries
@@ -29,14 +30,41 @@ options = SimpleNamespace(N=lambda: 2, NV=lambda: 17, VISCOUS=lambda: True,
 classes = SimpleNamespace(Par=Par)
 
 system = SimpleNamespace(flux=api.flux, source=api.source, Bdot=api.Bdot,
-                         max_abs_eigs=api.max_abs_eigs)
+                         max_abs_eigs=api.max_abs_eigs,
+                         multi=SimpleNamespace(left_star_state=_multi.left_star_state,
+                                               distance=_multi.distance))
+
+multi = SimpleNamespace(renormalize_levelsets=_multi.renormalize_levelsets,
+                        finite_difference=_multi.finite_difference,
+                        find_interface_cells=_multi.find_interface_cells,
+                        fill_boundary_cells=_multi.fill_boundary_cells,
+                        fill_neighbor_cells=_multi.fill_neighbor_cells,
+                        fill_ghost_cells=_multi.fill_ghost_cells,
+                        material_indicator=_multi.material_indicator)
+
+
+def _two_materials(u, MPs):
+    return isinstance(MPs, (list, tuple)) and len(MPs) == 2 and (
+        u.shape[-1] == _multi.V if u.dim() > 1 else api._NVAR.get("V") == _multi.V)
 
 
 def _iterator(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
               contorted_tol=1.0, max_steps=None):
+    """solvers.iterator: the two-material ghost-fluid loop for V = 15 and two
+    materials (ADER, Rusanov), else the one-material loop."""
+    if _two_materials(u, MPs):
+        if SPLIT or FLUX != 0 or STIFF:
+            raise RuntimeError("the ghost-fluid loop runs the ADER scheme with Rusanov flux")
+        return _multi.iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=max_steps)
     from .driver import iterate
     return iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
                    max_steps=max_steps)
+
+
+def _renorm_distortion(u, MPs):
+    if _two_materials(u, MPs):
+        return _multi.renorm_distortion(u, MPs)
+    return api.renorm_distortion(u, MPs)
 
 
 solvers = SimpleNamespace(
@@ -50,7 +78,8 @@ solvers = SimpleNamespace(
     split_stepper=api.split_stepper,
     split_stepper_para=api.split_stepper_para,
     timestep=api.timestep,
-    renorm_distortion=api.renorm_distortion,
+    renorm_distortion=_renorm_distortion,
+    make_u=_multi.make_u,
     extended_dimensions=api.extended_dimensions,
     iterator=_iterator,
 )

@@ -13,9 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgpr_gb300.so")
-SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu"]
+SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu", "gpr_multi.cu"]
 HEADERS = ["gpr_device.cuh", "gpr_kernels.cuh", "gpr_consts.cuh", "gpr_ode.cuh", "gpr_host.cuh",
-           "gpr_osher.cuh",
+           "gpr_osher.cuh", "gpr_ops.cuh", "gpr_ops15.h", "gpr_multi.cuh",
            "gpr_adjoint.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -102,6 +102,21 @@ SIGNATURES = {
     "gpr_adj_forward_step": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _D, _I, _P, _I, _P]),
     "gpr_adj_backward_step": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P]),
     "gpr_adj_point_jacobians": (_I, [_P, _I64, _P, _P, _P, _P, _I, _P]),
+    "gpr_distance_scratch_doubles": (_L, [_P, _I]),
+    "gpr_distance": (_I, [_P, _P, _P, _I, _P, _P, _P, _P]),
+    "gpr_finite_difference": (_I, [_P, _P, _P, _I, _P, _P]),
+    "gpr_find_interface_cells": (_I, [_P, _P, _P, _I, _P]),
+    "gpr_left_star_state": (_I, [_P, _P, _P, _P, _I64, _I, _D, _P, _P, _I, _P]),
+    "gpr_fill_scratch_doubles": (_L, [_P, _I, _I]),
+    "gpr_fill_boundary_cells": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _D, _P, _I, _P, _P, _I,
+                                     _P]),
+    "gpr_fill_neighbor_cells": (_I, [_P, _P, _P, _P, _P, _I, _P, _P, _I, _P]),
+    "gpr_fill_ghost_cells": (_I, [_P, _P, _P, _P, _I, _P, _D, _P, _I, _P, _P, _I, _P]),
+    "gpr_make_u": (_I, [_P, _P, _P, _I64, _P, _I, _I, _P]),
+    "gpr_renorm_multi": (_I, [_P, _I64, _P, _I, _I, _P]),
+    "gpr_timestep_multi": (_I, [_P, _P, _I64, _P, _I, _D, _D, _D, _I, _P, _I, _P, _P, _I, _P]),
+    "gpr_iterate_multi_scratch_doubles": (_L, [_P, _I, _I]),
+    "gpr_iterate_multi": (_I, [_P, _P, _I, _P, _P, _I, _P, _I, _P, _I, _P, _P, _I, _P]),
     "gpr_flux": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),

@@ -1,75 +1,20 @@
 // gpr_capi.cu - C ABI of the GB300 GPR ADER-WENO step (include/gpr_gb300.h).
 //
 // Host launchers: argument checks, variant dispatch on the number of
-// variables (V = 17: viscous + heat conduction; V = 14: viscous), grid
+// variables (V = 17: viscous + heat conduction; V = 14: viscous; V = 15:
+// viscous with one level set, whose launchers live in gpr_multi.cu), grid
 // sizing and the stage sequence of one ADER step.  All device work is
 // stream-ordered on the caller's stream; nothing here synchronises.
 #include <mutex>
 #include <stdio.h>
 
-#include "gpr_host.cuh"
-#include "gpr_ode.cuh"
-#include "gpr_osher.cuh"
+#include "gpr_ops.cuh"
+#include "gpr_ops15.h"
 
 using namespace gpr;
 using namespace gpr::host;
 
 namespace {
-
-// Pointwise kernels (one thread per state) behind gpr_flux / gpr_source /
-// gpr_Bdot / gpr_max_abs_eigs / gpr_interface_terms.
-template <class L>
-__global__ void k_pointwise(int what, const double *__restrict__ Q, const double *__restrict__ X,
-                            double *__restrict__ out, double *__restrict__ out2, long count,
-                            int d, int flux, DevPar P, Consts C) {
-  constexpr int V = L::V;
-  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (c >= count)
-    return;
-  double q[V], r[V];
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    q[k] = Q[c * V + k];
-  Prim<L::THERMAL> s;
-  prim<L::THERMAL>(q, P, s);
-  switch (what) {
-  case 0:  // flux (adds)
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      r[k] = out[c * V + k];
-    flux_add<L::THERMAL, V>(q, s, d, P, r);
-    break;
-  case 1:
-    source<L::THERMAL, V>(q, s, P, r);
-    break;
-  case 2: {
-    double x[V];
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      x[k] = X[c * V + k];
-    bdot<V, L::LSET>(s.v, x, d, r);
-  } break;
-  case 3:
-    out[c] = max_abs_eigs<L::THERMAL>(q, s, d, P);
-    return;
-  default: {
-    double qr[V], b[V];
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      qr[k] = X[c * V + k];
-    if (flux == GPR_FLUX_RUSANOV)
-      interface_point<L>(q, qr, d, P, C, r, b);
-    else
-      interface_point_eig<L>(q, qr, flux, P, C, r, b);
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      out2[c * V + k] = b[k];
-  } break;
-  }
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    out[c * V + k] = r[k];
-}
 
 // extend_mask (etc/grid.cpp:176-230): one thread per predictor cell.
 __global__ void k_extend_mask(const uint8_t *__restrict__ mask, uint8_t *__restrict__ maskb,
@@ -106,340 +51,6 @@ __global__ void k_extend_mask(const uint8_t *__restrict__ mask, uint8_t *__restr
   maskb[idx] = v;
 }
 
-template <class L> struct Ops {
-  static constexpr int V = L::V;
-
-  static int boundaries(const double *u, double *ub, const int32_t *nX, int nd,
-                        const int32_t *bcs, cudaStream_t st) {
-    int nx = nX[0], ny = nd == 2 ? nX[1] : 1;
-    long n = (long)nx * ny * V;
-    k_fill_interior<V><<<blocks(n, 256), 256, 0, st>>>(u, ub, nx, ny, nd);
-    long g0 = (long)(nd == 1 ? 1 : ny) * 2 * NN * V;
-    k_ghosts<V><<<blocks(g0, 256), 256, 0, st>>>(ub, nx, ny, nd, 0, bcs[0], bcs[1]);
-    if (nd == 2) {
-      long g1 = (long)(nx + 2 * NN) * 2 * NN * V;
-      k_ghosts<V><<<blocks(g1, 256), 256, 0, st>>>(ub, nx, ny, nd, 1, bcs[2], bcs[3]);
-    }
-    return cuda_rc();
-  }
-
-  static long weno_scratch(const int32_t *nX, int nd) {
-    if (nd == 1)
-      return 0;
-    return (long)(nX[0] + 2) * (nX[1] + 2 * NN) * NN * V;
-  }
-
-  static int weno(double *wh, const double *ub, const int32_t *nX, int nd, double *scratch,
-                  cudaStream_t st) {
-    const Consts &C = consts();
-    if (nd == 1) {
-      int ncb = nX[0] + 2;
-      k_weno1d<V><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, C);
-      return cuda_rc();
-    }
-    int nxp = nX[0] + 2, nyp = nX[1] + 2, nyb = nX[1] + 2 * NN;
-    k_weno2d_x<V><<<blocks((long)nxp * nyb * V, 256), 256, 0, st>>>(scratch, ub, nxp, nyb, C);
-    k_weno2d_y<V><<<blocks((long)nxp * nyp * NN * V, 256), 256, 0, st>>>(wh, scratch, nxp,
-                                                                         nyp, C);
-    return cuda_rc();
-  }
-
-  static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
-                       const double *dX, int nd, const int32_t *nX, int stiff,
-                       const DevPar &P, const uint8_t *mask, int32_t *status,
-                       cudaStream_t st) {
-    const Consts &C = consts();
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
-    if (nd == 1) {
-      long nt = ncb * NN * NN;
-      k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
-      return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
-    }
-    long nt = ncb * NN * NN * NN;
-    k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
-        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
-    return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
-  }
-
-  // Stiff-source Newton pass over the cells the Picard pass flagged.
-  template <int ND, bool BATCH = false>
-  static int stiff_pass(double *qh, const double *wh, long ncb, const uint8_t *mask,
-                        int32_t *status, double dt, const double *dt_dev, double idx,
-                        double idy, const DevPar &P, const Consts &C, cudaStream_t st,
-                        const Batch &B = Batch{}) {
-    return launch_stiff<L, ND, BATCH>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C,
-                                      st, B);
-  }
-
-  static long fv_scratch(const int32_t *nX, int nd) {
-    if (nd == 1)
-      return (long)(nX[0] + 1) * 2 * V;
-    return 2L * (nX[0] + 1) * (nX[1] + 1) * 2 * V;
-  }
-
-  static int fv(double *u, const double *qh, const int32_t *nX, double dt,
-                const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
-                const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st,
-                int flux = GPR_FLUX_RUSANOV) {
-    const Consts &C = consts();
-    int nx = nX[0];
-    if (nd == 1) {
-      long nf = (long)(nx + 1) * NN;
-      if (flux == GPR_FLUX_RUSANOV)
-        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
-                                                       dt_dev, dX[0], time_dg, P, C, Batch{});
-      else
-        k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
-            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
-      long nc = (long)nx * NN * NN;
-      k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
-                                                      dt_dev, dX[0], 1.0, sources, time_dg, P,
-                                                      C, Batch{});
-      return cuda_rc();
-    }
-    int ny = nX[1];
-    long nf = (long)(nx + 1) * (ny + 1);
-    double *fbx = scratch, *fby = scratch + nf * 2 * V;
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
-                                                             dt_dev, dX[0], dX[1], time_dg, P,
-                                                             C);
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fby, qh, nx, ny, 1, mask, dt,
-                                                             dt_dev, dX[0], dX[1], time_dg, P,
-                                                             C);
-    long nc = (long)nx * ny * NN * NN * NN;
-    k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
-                                                    dX[0], dX[1], sources, time_dg, P, C,
-                                                    Batch{});
-    return cuda_rc();
-  }
-
-  // Face pass of the FV update only: the k_faces kernels writing the face
-  // contributions (to the left and right cells) into fb.
-  static int faces(const double *qh, const int32_t *nX, double dt, const double *dX, int nd,
-                   int time_dg, const DevPar &P, const uint8_t *mask, double *fb,
-                   cudaStream_t st, int flux = GPR_FLUX_RUSANOV) {
-    const Consts &C = consts();
-    int nx = nX[0];
-    if (nd == 1) {
-      long nf = (long)(nx + 1) * NN;
-      if (flux == GPR_FLUX_RUSANOV)
-        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
-                                                       dX[0], time_dg, P, C, Batch{});
-      else
-        k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
-            fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, flux, P, C, Batch{});
-      return cuda_rc();
-    }
-    int ny = nX[1];
-    long nf = (long)(nx + 1) * (ny + 1);
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb, qh, nx, ny, 0, mask, dt,
-                                                             nullptr, dX[0], dX[1], time_dg,
-                                                             P, C);
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb + nf * 2 * V, qh, nx, ny, 1,
-                                                             mask, dt, nullptr, dX[0], dX[1],
-                                                             time_dg, P, C);
-    return cuda_rc();
-  }
-
-  static int timestep(const double *u, long ncell, const double *dX, int nd, double cfl,
-                      double t, double tf, int count, const DevPar &P, double *dt_out,
-                      double *scratch, cudaStream_t st) {
-    unsigned long long *mx = (unsigned long long *)scratch;
-    cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-    k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
-                                                      nd == 2 ? dX[1] : 1.0, mx, P);
-    k_cfl_finalize<<<1, 1, 0, st>>>(mx, cfl, t, tf, count, dt_out);
-    return cuda_rc();
-  }
-
-  static int renorm(double *u, long ncell, const DevPar &P, cudaStream_t st) {
-    k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, nullptr);
-    return cuda_rc();
-  }
-
-  static int pointwise(int what, const double *Q, const double *X, double *out, double *out2,
-                       long count, int d, int flux, const DevPar &P, cudaStream_t st) {
-    k_pointwise<L><<<blocks(count, 64), 64, 0, st>>>(what, Q, X, out, out2, count, d, flux, P,
-                                                     consts());
-    return cuda_rc();
-  }
-
-  // One device-resident iterator step (iterator.cpp:204-240 for one
-  // material): CFL -> boundaries -> WENO -> predictor -> FV -> renorm ->
-  // clock advance, with dt living in clk[1].
-  static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
-                     const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
-                     int nsteps, double *scratch, int32_t *status, cudaStream_t st,
-                     int flux = GPR_FLUX_RUSANOV) {
-    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
-    long ns = nd == 1 ? NN : NN * NN;
-    double *ub = scratch;
-    double *wh = ub + nub * V;
-    double *qh = wh + ncb * ns * V;
-    double *tmp = qh + ncb * NN * ns * V;
-    unsigned long long *mx = (unsigned long long *)(tmp + (weno_scratch(nX, nd) > fv_scratch(nX, nd)
-                                                               ? weno_scratch(nX, nd)
-                                                               : fv_scratch(nX, nd)));
-    double *dt_dev = clk + 1;
-    for (int s = 0; s < nsteps; s++) {
-      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
-                                                        nd == 2 ? dX[1] : 1.0, mx, P);
-      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
-      int rc = boundaries(u, ub, nX, nd, bcs, st);
-      if (rc)
-        return rc;
-      rc = weno(wh, ub, nX, nd, tmp, st);
-      if (rc)
-        return rc;
-      rc = predictor(qh, wh, 0.0, dt_dev, dX, nd, nX, 0, P, mask, status, st);
-      if (rc)
-        return rc;
-      rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st, flux);
-      if (rc)
-        return rc;
-      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
-      k_clock_advance<<<1, 1, 0, st>>>(clk);
-    }
-    return cuda_rc();
-  }
-
-  // ---- split scheme (steppers.cpp:50-66, split/homogeneous.cpp) -------------
-  static int midstep(double *wh, double dt, const double *dt_dev, const double *dX, int nd,
-                     const int32_t *nX, const DevPar &P, const uint8_t *mask, cudaStream_t st) {
-    const Consts &C = consts();
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
-    if (nd == 1)
-      k_midstep<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev, idx,
-                                                              idy, P, C);
-    else
-      k_midstep<L, 2><<<blocks(ncb * NN * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev,
-                                                                   idx, idy, P, C);
-    return cuda_rc();
-  }
-
-  // ODE half step on u and ub, WENO, [midstepper], FV without sources and
-  // time integration on the node values, ODE half step on u; ub is modified.
-  // scratch: wh then the WENO / FV temporary.
-  static int split_stepper(double *u, double *ub, const int32_t *nX, int nd, double dt,
-                           const double *dt_dev, const double *dX, int half_step, int flux,
-                           const DevPar &P, const uint8_t *mask, double *scratch,
-                           cudaStream_t st) {
-    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
-    long ns = nd == 1 ? NN : NN * NN;
-    double *wh = scratch, *tmp = wh + ncb * ns * V;
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
-    k_ode<L><<<blocks(nub, 128), 128, 0, st>>>(ub, nub, dt / 2, dt_dev, 0.5, P);
-    int rc = weno(wh, ub, nX, nd, tmp, st);
-    if (rc)
-      return rc;
-    if (half_step && (rc = midstep(wh, dt, dt_dev, dX, nd, nX, P, mask, st)))
-      return rc;
-    rc = fv(u, wh, nX, dt, dt_dev, dX, nd, 0, 0, P, mask, tmp, st, flux);
-    if (rc)
-      return rc;
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
-    return cuda_rc();
-  }
-
-  static long split_scratch(const int32_t *nX, int nd) {
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    long ns = nd == 1 ? NN : NN * NN;
-    long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
-    return ncb * ns * V + (w > f ? w : f);
-  }
-
-  // Device-resident iterator with the split scheme (iterator.cpp:204-245,
-  // SPLIT = true); scratch as iterate().
-  static int iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
-                           const int32_t *bcs, const DevPar &P, const uint8_t *mask,
-                           double *clk, int nsteps, double *scratch, int half_step, int flux,
-                           cudaStream_t st) {
-    long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
-    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
-    double *ub = scratch;
-    double *rest = ub + nub * V;
-    unsigned long long *mx = (unsigned long long *)(scratch + iterate_scratch(nX, nd) - 1);
-    double *dt_dev = clk + 1;
-    for (int s = 0; s < nsteps; s++) {
-      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
-                                                        nd == 2 ? dX[1] : 1.0, mx, P);
-      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
-      int rc = boundaries(u, ub, nX, nd, bcs, st);
-      if (rc)
-        return rc;
-      rc = split_stepper(u, ub, nX, nd, 0.0, dt_dev, dX, half_step, flux, P, mask, rest, st);
-      if (rc)
-        return rc;
-      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
-      k_clock_advance<<<1, 1, 0, st>>>(clk);
-    }
-    return cuda_rc();
-  }
-
-  static long iterate_scratch(const int32_t *nX, int nd) {
-    long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
-    long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
-    long ns = nd == 1 ? NN : NN * NN;
-    long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
-    return nub * V + ncb * ns * V + ncb * NN * ns * V + (w > f ? w : f) + 1;
-  }
-
-  // ---- batched form -------------------------------------------------------
-  static BatchLayout batch_layout(int ninst, const int32_t *nx) {
-    return batch_layout_v(ninst, nx, V);
-  }
-
-  static Batch batch_view(double *scr, int ninst, const BatchLayout &b, double *clk) {
-    return batch_view_of(scr, ninst, b, clk);
-  }
-
-  static int batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,
-                           double *scr, int32_t *status, unsigned long long *updates,
-                           cudaStream_t st) {
-    const Consts &C = consts();
-    BatchLayout b = batch_layout(ninst, nx);
-    Batch B = batch_view(scr, ninst, b, clk);
-    double *ub = scr + b.o_ub, *wh = scr + b.o_wh, *qh = scr + b.o_qh, *fb = scr + b.o_fb;
-    unsigned long long *mx = (unsigned long long *)(scr + b.o_mx);
-    DevPar P0{};
-    for (int s = 0; s < nsteps; s++) {
-      k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B);
-      k_b_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B);
-      k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
-      k_b_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wh, ub, b.nb, C, B);
-      k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, 128), 128, 0, st>>>(
-          qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B);
-      int rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
-                                   C, st, B);
-      if (rc)
-        return rc;
-      k_faces1d<L, true><<<blocks(b.nf * NN, 128), 128, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
-                                                                  nullptr, 1.0, 1, P0, C, B);
-      k_cells<L, 1, true><<<blocks(b.nu * NN * NN, 128), 128, 0, st>>>(
-          u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B);
-      k_b_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, B);
-      k_b_clock_advance<<<blocks(ninst, 128), 128, 0, st>>>(B, updates);
-    }
-    return cuda_rc();
-  }
-
-  static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt, nullptr, 1.0, P);
-    return cuda_rc();
-  }
-};
-
-using L17 = Layout<true, 0>;
-using L14 = Layout<false, 0>;
 
 bool check_grid(const int32_t *nX, int nd) {
   if (!nX || (nd != 1 && nd != 2))
@@ -470,6 +81,10 @@ int check_flux(int flux, int nd) {
     using O = Ops<L14>;                                                                      \
     return CALL;                                                                             \
   }                                                                                          \
+  case 15: {                                                                                 \
+    using O = Ops15;                                                                         \
+    return CALL;                                                                             \
+  }                                                                                          \
   default:                                                                                   \
     return GPR_E_UNSUPPORTED;                                                                \
   }
@@ -481,11 +96,11 @@ extern "C" {
 int gpr_version(void) { return 100; }
 
 int gpr_supported_nvars(int32_t *out, int cap) {
-  static const int32_t vs[] = {17, 14};
+  static const int32_t vs[] = {17, 14, 15};
   int n = 0;
-  for (int i = 0; i < 2 && i < cap; i++)
+  for (int i = 0; i < 3 && i < cap; i++)
     out[n++] = vs[i];
-  return 2;
+  return 3;
 }
 
 int gpr_extend_mask(const uint8_t *mask, uint8_t *maskb, const int32_t *nX, int ndim,
@@ -924,7 +539,8 @@ int gpr_batch_init(double *clock, int ninst, const int32_t *nx, const double *dx
   if (e == cudaSuccess) e = put(off, vec.data(), vec.size() * sizeof(vec[0]))
   switch (nvar) {
   case 17:
-  case 14: {
+  case 14:
+  case 15: {
     BatchLayout lay = batch_layout_v(ninst, nx, nvar);
     PUT(lay.o_par, P);
     PUT(lay.o_iu, iu);

@@ -1,0 +1,1488 @@
+// gpr_multi.cuh - level-set ghost fluid on the device (one level set, at most
+// two materials, no heat conduction: the V = 15 layout).
+//
+// Restates the reference's multi/ module and the interface Riemann problem
+// it calls:
+//   re-distancing        multi/pfmm.cpp:4-26 (first-order fast marching of
+//                        the vendored scikit-fmm, distance_marcher.cpp,
+//                        base_marcher.cpp)
+//   normals              multi/functions.cpp:16-54 (finite_difference)
+//   interface cells      multi/fill.cpp:20-74 (find_interface_cells)
+//   boundary fill        multi/fill.cpp:96-235 (fill_boundary_cells)
+//   layered fill         multi/fill.cpp:237-328 (fill_neighbor_cells)
+//   star state           system/multi/riemann.cpp:26-233, conditions.cpp,
+//                        rotations.cpp, functions/vectors.cpp:85-154
+//   merge, CFL, renorm   solvers/iterator.cpp:12-83, solvers/utils.cpp:6-23
+//
+// The reference runs every piece as a sequential sweep over the grid.  Here
+// each is a data-parallel kernel whose result equals the sequential sweep:
+//   * the fast marching order is replaced by tiled Jacobi iterations of the
+//     same causal upwind update, whose fixed point is what the marcher
+//     computes (band neighbours always enter a point's quadratic, the others
+//     only while their distance is below the point's estimate, as the
+//     marcher's heap order makes it), evaluated with the marcher's
+//     arithmetic, within ~1e-13 of the marcher (the rounding noise of its
+//     own quadratic formula; most fields come out bit for bit);
+//   * a boundary cell reads the right-hand state of the interface from a
+//     cell that an earlier cell of the (i, j) sweep may have filled; those
+//     reads are resolved to the last earlier writer and solved level by
+//     level (almost every cell is on level 0);
+//   * within one layer of the extrapolation, a cell copies from a cell of the
+//     same layer only if the sweep reached that one first; that chain is
+//     followed explicitly.
+#pragma once
+
+#include <float.h>
+
+#include "gpr_kernels.cuh"
+#include "gpr_ode.cuh"
+
+namespace gpr {
+namespace multi {
+
+// Grid of nd = 1 (ny = 1) or 2 dimensions; cell (i, j) is flat index
+// i * ny + j, the reference's cell order.
+struct Grid {
+  int nd, nx, ny;
+  long ncell;
+  double dx, dy;
+};
+
+// Non-contracted FP64 arithmetic where the result feeds a discontinuous
+// decision (index truncation, marcher ordering): the same roundings as the
+// reference's separate multiplies and adds.
+GPR_D double mul(double a, double b) { return __dmul_rn(a, b); }
+GPR_D double add(double a, double b) { return __dadd_rn(a, b); }
+GPR_D double sub(double a, double b) { return __dsub_rn(a, b); }
+GPR_D double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+// ===========================================================================
+// Re-distancing (first-order fast marching, no narrow band, not periodic).
+
+// Frozen band (initalizeFrozen, distance_marcher.cpp:90-151, with the
+// reference's edit: the least per-axis crossing distance): cells where phi
+// is zero or changes sign across a face.  Others start unknown (+inf).
+// phi[c * ps] is the level set of cell c.
+__global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__restrict__ d,
+                           uint8_t *__restrict__ fz, Grid g, int *__restrict__ anyfrozen,
+                           const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell)
+    return;
+  int i = g.nd == 1 ? (int)c : (int)(c / g.ny), j = g.nd == 1 ? 0 : (int)(c % g.ny);
+  double p = phi[c * ps];
+  if (p == 0.0) {
+    d[c] = 0.0;
+    fz[c] = 1;
+    atomicOr(anyfrozen, 1);
+    return;
+  }
+  double ld[2] = {0.0, 0.0};
+  bool borders = false;
+  for (int dim = 0; dim < g.nd; dim++) {
+    double h = dim == 0 ? g.dx : g.dy;
+    for (int dir = -1; dir < 2; dir += 2) {
+      int ii = dim == 0 ? i + dir : i, jj = dim == 1 ? j + dir : j;
+      if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny)
+        continue;
+      double pn = phi[((long)ii * g.ny + jj) * ps];
+      if (mul(p, pn) < 0.0) {
+        borders = true;
+        double dd = dvd(mul(h, p), sub(p, pn));
+        if (ld[dim] == 0.0 || ld[dim] > dd)
+          ld[dim] = dd;
+      }
+    }
+  }
+  if (borders) {
+    double m = DBL_MAX;
+    for (int dim = 0; dim < g.nd; dim++) {
+      double t = fabs(ld[dim]);
+      if (t > 0.0)
+        m = t < m ? t : m;
+    }
+    d[c] = p < 0.0 ? -m : m;
+    fz[c] = 1;
+    atomicOr(anyfrozen, 1);
+  } else {
+    d[c] = INFINITY;
+    fz[c] = 0;
+  }
+}
+
+// The marcher's point update (updatePointOrderOne + solveQuadratic,
+// distance_marcher.cpp:5-28,72-88) for the axes in `use`: the root of
+// sum_k (x - v_k)^2 / h_k^2 = 1 chosen by the sign of phi, 0 without a real
+// root.  idx2 = 1 / h^2.
+GPR_D double fmm_quad(const double v[2], const bool use[2], const double idx2[2], int nd,
+                      double phi) {
+  double a = 0.0, b = 0.0, c = 0.0;
+  for (int dim = 0; dim < nd; dim++)
+    if (use[dim]) {
+      a = add(a, idx2[dim]);
+      b = sub(b, mul(mul(idx2[dim], 2.0), v[dim]));
+      c = add(c, mul(idx2[dim], mul(v[dim], v[dim])));
+    }
+  c = sub(c, 1.0);
+  double det = sub(mul(b, b), mul(mul(4.0, a), c));
+  if (!(det > 0.0))
+    return 0.0;
+  double sq = __dsqrt_rn(det);
+  // (x / 2.0) is exact, as is (x * 0.5)
+  return dvd(mul(phi > DBL_EPSILON ? add(-b, sq) : sub(-b, sq), 0.5), a);
+}
+
+// Update of one unfrozen point from its neighbours' current values
+// (signed; +inf unknown), reproducing what the marcher's heap order makes
+// of it.  Band neighbours (frozen at initialisation) always enter.  The
+// other neighbours enter in increasing |d| (equal keys together, as the
+// marcher freezes them in one batch) while their |d| is below the point's
+// current estimate: exactly those frozen before the point.  Per axis the
+// entered neighbour of least |d| is used (the lower one on ties, as the
+// marcher scans -1 then +1), so per axis only the non-band neighbour of
+// least |d| can matter.  A neighbour that enters lies strictly upwind (the
+// root exceeds its |d| in exact arithmetic); where rounding says otherwise
+// (a noise-level tie) it is left out, so that no two points feed each other
+// and the iteration cannot cycle.  Returns `old` when nothing is known.
+GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], double phi,
+                        const double idx2[2], int nd, double old) {
+  double v[2] = {0.0, 0.0}, cv[2] = {0.0, 0.0}, ck[2] = {INFINITY, INFINITY};
+  bool use[2] = {false, false};
+  for (int dim = 0; dim < nd; dim++)
+    for (int s = 0; s < 2; s++) {
+      double x = nb[dim][s];
+      if (band[dim][s]) {
+        if (!use[dim] || fabs(x) < fabs(v[dim])) {
+          v[dim] = x;
+          use[dim] = true;
+        }
+      } else if (fabs(x) < ck[dim]) {
+        ck[dim] = fabs(x);
+        cv[dim] = x;
+      }
+    }
+  double t = INFINITY;
+  if (use[0] || use[1])
+    t = fmm_quad(v, use, idx2, nd, phi);
+  bool done[2] = {!(ck[0] < INFINITY), nd < 2 || !(ck[1] < INFINITY)};
+  while (!done[0] || !done[1]) {
+    int a = done[0] ? 1 : (done[1] ? 0 : (ck[1] < ck[0] ? 1 : 0));
+    double key = ck[a];
+    if (!(key < fabs(t)))
+      break;
+    bool both = !done[1 - a] && ck[1 - a] == key;
+    double sv0 = v[0], sv1 = v[1];
+    bool su0 = use[0], su1 = use[1];
+    for (int q = 0; q < 2; q++) {
+      int dim = q == 0 ? a : 1 - a;
+      if (q == 1 && !both)
+        break;
+      if (!use[dim] || fabs(cv[dim]) < fabs(v[dim])) {
+        v[dim] = cv[dim];
+        use[dim] = true;
+      }
+      done[dim] = true;
+    }
+    double t2 = fmm_quad(v, use, idx2, nd, phi);
+    if (t2 == 0.0 || !(fabs(t2) > key)) {
+      v[0] = sv0;
+      v[1] = sv1;
+      use[0] = su0;
+      use[1] = su1;
+      break;
+    }
+    t = t2;
+  }
+  return fabs(t) < INFINITY ? t : old;
+}
+
+// One round of tiled Jacobi sweeps.  Each block loads its tile and a
+// one-cell halo into shared memory and runs up to K sweeps of the causal
+// update against that halo, then writes back.  Sweeps are numbered globally
+// (round * K + local sweep); lastg[c] holds the sweep of cell c's last
+// change.  Only a point next to a point that changed in the previous sweep
+// can change (or, in a round's first sweep, next to a halo point that
+// changed at all in the previous round), and each sweep gathers those into
+// a list first, so that whole warps run the FP64 updates (a warp costs the
+// FP64 pipe the same with one lane as with 32).  A tile runs only if it or
+// a neighbouring tile changed in the previous round (tflag[round][tile]);
+// flags[round] records whether anything changed, and a round after a round
+// without change returns at once.  2D tiles are 32 x 32 cells, 1D tiles
+// 1024; FMM_THREADS threads own
+// 1024 / FMM_THREADS cells each.
+constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
+// sweeps per round: four tile diameters
+template <int ND> struct FmmK {
+  static constexpr int K = ND == 2 ? 4 * 2 * FMM_T2 : 4 * FMM_T1;
+};
+
+template <int ND>
+__global__ void __launch_bounds__(FMM_THREADS, 4)
+    k_fmm_round(double *__restrict__ d, const double *__restrict__ phi, long ps,
+                const uint8_t *__restrict__ fz, int *__restrict__ lastg, Grid g, double idx2x,
+                double idx2y, int *__restrict__ flags, int *__restrict__ tflag, int round,
+                int mono, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  if (round > 0 && flags[round - 1] == 0)
+    return;
+  constexpr int TX = ND == 2 ? FMM_T2 : FMM_T1, TY = ND == 2 ? FMM_T2 : 1;
+  constexpr int SX = TX + 2, SY = ND == 2 ? TY + 2 : 1;
+  constexpr int NT = TX * TY, PER = NT / FMM_THREADS, NW = FMM_THREADS / 32;
+  constexpr int FMM_K = FmmK<ND>::K;
+  const int ntx0 = (g.nx + TX - 1) / TX, nty0 = ND == 2 ? (g.ny + TY - 1) / TY : 1;
+  const int ntiles = ntx0 * nty0;
+  const int t = blockIdx.x;
+  if (round > 0) {
+    const int *prev = tflag + (long)(round - 1) * ntiles;
+    int ti = ND == 2 ? t % ntx0 : t, tj = ND == 2 ? t / ntx0 : 0;
+    bool run = prev[t] || (ti > 0 && prev[t - 1]) || (ti < ntx0 - 1 && prev[t + 1]) ||
+               (ND == 2 && ((tj > 0 && prev[t - ntx0]) || (tj < nty0 - 1 && prev[t + ntx0])));
+    if (!run)
+      return;
+  }
+  __shared__ double sd[SX * SY];
+  __shared__ double nvs[NT];
+  __shared__ uint8_t sf[SX * SY];
+  __shared__ int last[SX * SY];  // global sweep of the last change
+  __shared__ int16_t list[NT];
+  __shared__ int wcnt[NW], any[2], total;
+  const int bi = ND == 2 ? t % ntx0 : t, bj = ND == 2 ? t / ntx0 : 0;
+  const int i0 = bi * TX, j0 = bj * TY;
+  for (int e = threadIdx.x; e < SX * SY; e += FMM_THREADS) {
+    int a = ND == 2 ? e / SY : e, b = ND == 2 ? e % SY : 0;
+    int ii = i0 + a - 1, jj = ND == 2 ? j0 + b - 1 : 0;
+    double x = INFINITY;
+    uint8_t f = 0;
+    int lg = -2;
+    if (ii >= 0 && ii < g.nx && jj >= 0 && jj < g.ny) {
+      long c = (long)ii * g.ny + jj;
+      x = d[c];
+      f = fz[c];
+      lg = lastg[c];
+    }
+    sd[e] = x;
+    sf[e] = f;
+    last[e] = lg;
+  }
+  if (threadIdx.x < 2)
+    any[threadIdx.x] = 0;
+  auto smem_of = [&](int l) {
+    return ND == 2 ? (l / TY + 1) * SY + (l % TY + 1) : l + 1;
+  };
+  auto inside_of = [&](int l) {
+    int i = i0 + (ND == 2 ? l / TY : l), j = ND == 2 ? j0 + l % TY : 0;
+    return i < g.nx && j < g.ny;
+  };
+  auto cell_of = [&](int l) {
+    int i = i0 + (ND == 2 ? l / TY : l), j = ND == 2 ? j0 + l % TY : 0;
+    return (long)i * g.ny + j;
+  };
+  auto is_halo = [&](int m) {
+    int a = ND == 2 ? m / SY : m, b = ND == 2 ? m % SY : 1;
+    return a == 0 || a == SX - 1 || (ND == 2 && (b == 0 || b == SY - 1));
+  };
+  bool act[PER];
+  for (int k = 0; k < PER; k++) {
+    int l = threadIdx.x + k * FMM_THREADS;
+    act[k] = inside_of(l) && !fz[cell_of(l)];
+  }
+  const double idx2[2] = {idx2x, idx2y};
+  const int o0 = ND == 2 ? SY : 1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gs0 = round * FMM_K;
+  bool wrote = false;
+  __syncthreads();
+  for (int it = 0; it < FMM_K; it++) {
+    const int gs = gs0 + it;
+    // 1. gather the points that can move this sweep
+    int mine = 0;
+    bool dirty[PER];
+    for (int k = 0; k < PER; k++) {
+      int m = smem_of(threadIdx.x + k * FMM_THREADS);
+      bool dd = act[k] && gs == 0;
+      if (act[k] && gs > 0) {
+        int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
+        for (int q = 0; q < (ND == 2 ? 4 : 2); q++) {
+          int lq = last[nbm[q]];
+          // a halo point is stale for the whole round: any change of it in
+          // the previous round counts in the first sweep
+          dd = dd || lq == gs - 1 || (it == 0 && is_halo(nbm[q]) && lq >= gs0 - FMM_K);
+        }
+      }
+      dirty[k] = dd;
+      mine += dd;
+    }
+    int incl = mine;  // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o)
+        incl += y;
+    }
+    if (lane == 31)
+      wcnt[wid] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < wid; w++)
+      base += wcnt[w];
+    int pos = base + incl - mine;
+    for (int k = 0; k < PER; k++)
+      if (dirty[k])
+        list[pos++] = (int16_t)(threadIdx.x + k * FMM_THREADS);
+    if (threadIdx.x == FMM_THREADS - 1)
+      total = pos;
+    if (threadIdx.x == 0)
+      any[(it + 1) & 1] = 0;
+    __syncthreads();
+    // 2. update them (Jacobi: read the neighbours, write after a barrier)
+    const int n = total;
+    for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
+      int l = list[q], m = smem_of(l);
+      double nb[2][2];
+      bool bd[2][2];
+      nb[0][0] = sd[m - o0];
+      nb[0][1] = sd[m + o0];
+      bd[0][0] = sf[m - o0];
+      bd[0][1] = sf[m + o0];
+      if (ND == 2) {
+        nb[1][0] = sd[m - 1];
+        nb[1][1] = sd[m + 1];
+        bd[1][0] = sf[m - 1];
+        bd[1][1] = sf[m + 1];
+      } else {
+        nb[1][0] = nb[1][1] = INFINITY;
+        bd[1][0] = bd[1][1] = false;
+      }
+      nvs[q] = fmm_update(nb, bd, phi[cell_of(l) * ps], idx2, ND, sd[m]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
+      int m = smem_of(list[q]);
+      double old = sd[m], nv = nvs[q];
+      // from the second half of the round budget on, only a smaller |d| is
+      // taken, which guarantees termination (the marcher's quadratic loses
+      // ~1e-13 to cancellation)
+      if (mono ? fabs(nv) < fabs(old) : nv != old) {
+        sd[m] = nv;
+        last[m] = gs;
+        any[it & 1] = 1;
+      }
+    }
+    __syncthreads();
+    if (!any[it & 1])
+      break;
+  }
+  for (int k = 0; k < PER; k++) {
+    int l = threadIdx.x + k * FMM_THREADS;
+    int m = smem_of(l);
+    if (act[k] && last[m] >= gs0) {
+      long c = cell_of(l);
+      d[c] = sd[m];
+      lastg[c] = last[m];
+      wrote = true;
+    }
+  }
+  bool any_wrote = __syncthreads_or(wrote);
+  if (threadIdx.x == 0) {
+    tflag[(long)round * ntiles + t] = any_wrote ? 1 : 0;
+    if (any_wrote)
+      atomicOr(&flags[round], 1);
+  }
+}
+
+// Final values (base_marcher.cpp:103-106, 190-196): zeros when nothing
+// froze, DBL_MAX where the march never arrived; the distance also replaces
+// the level set in u (renormalize_levelsets, multi/functions.cpp:56-64).
+template <int V>
+__global__ void k_fmm_finish(double *__restrict__ d, double *__restrict__ u, long ncell,
+                             const int *__restrict__ anyfrozen, const int *__restrict__ flags,
+                             int last, int *__restrict__ err, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c == 0 && flags[last] != 0)
+    atomicOr(err, 1);  // not converged within the round budget
+  if (c >= ncell)
+    return;
+  double x = d[c];
+  if (!*anyfrozen)
+    x = 0.0;
+  else if (isinf(x))
+    x = DBL_MAX;
+  d[c] = x;
+  if (u)
+    u[c * V + V - 1] = x;
+}
+
+// ===========================================================================
+// Normals and interface cells of one material from its level set phi
+// (material_indicator, multi/functions.cpp:66-81: phi = +-u's level set for
+// two materials; the material occupies phi <= 0).
+
+__global__ void k_mat_phi(const double *__restrict__ d, int sgn, double *__restrict__ phim,
+                          long ncell, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c < ncell)
+    phim[c] = sgn > 0 ? d[c] : -d[c];
+}
+
+// finite_difference (multi/functions.cpp:16-54): central differences, the
+// first and last rows (columns) copied from their neighbours.  dphi is
+// [ncell][nd].
+__global__ void k_finite_difference(const double *__restrict__ phi, double *__restrict__ dphi,
+                                    Grid g, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell)
+    return;
+  if (g.nd == 1) {
+    int i = (int)c, ii = i == 0 ? 1 : (i == g.nx - 1 ? g.nx - 2 : i);
+    dphi[c] = dvd(sub(phi[ii + 1], phi[ii - 1]), mul(2.0, g.dx));
+    return;
+  }
+  int i = (int)(c / g.ny), j = (int)(c % g.ny);
+  int ii = i == 0 ? 1 : (i == g.nx - 1 ? g.nx - 2 : i);
+  int jj = j == 0 ? 1 : (j == g.ny - 1 ? g.ny - 2 : j);
+  dphi[2 * c] = dvd(sub(phi[(long)(ii + 1) * g.ny + j], phi[(long)(ii - 1) * g.ny + j]),
+                    mul(2.0, g.dx));
+  dphi[2 * c + 1] = dvd(sub(phi[(long)i * g.ny + jj + 1], phi[(long)i * g.ny + jj - 1]),
+                        mul(2.0, g.dy));
+}
+
+// find_interface_cells (multi/fill.cpp:20-74), gathered per cell: the
+// reference's scatter only ever writes sign(phi) of the written cell, or -2
+// for an isolated phi <= 0 cell, so each cell's final value follows from its
+// own neighbourhood.
+GPR_D bool nonisolated(const double *phi, int i, int j, const Grid &g) {
+  long c = (long)i * g.ny + j;
+  return (i > 0 && phi[c - g.ny] <= 0.0) || (i < g.nx - 1 && phi[c + g.ny] <= 0.0) ||
+         (j > 0 && phi[c - 1] <= 0.0) || (j < g.ny - 1 && phi[c + 1] <= 0.0);
+}
+
+__global__ void k_interface_cells(const double *__restrict__ phi, int32_t *__restrict__ im,
+                                  Grid g, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell)
+    return;
+  double p = phi[c];
+  int sg = p <= 0.0 ? -1 : 1;
+  if (g.nd == 1) {
+    int i = (int)c;
+    bool hit = (i > 0 && mul(phi[c - 1], p) <= 0.0) ||
+               (i < g.nx - 1 && mul(p, phi[c + 1]) <= 0.0);
+    im[c] = hit ? sg : 0;
+    return;
+  }
+  int i = (int)(c / g.ny), j = (int)(c % g.ny);
+  long nbr[4] = {i > 0 ? c - g.ny : -1, i < g.nx - 1 ? c + g.ny : -1, j > 0 ? c - 1 : -1,
+                 j < g.ny - 1 ? c + 1 : -1};
+  int ni[4] = {i - 1, i + 1, i, i}, nj[4] = {j, j, j - 1, j + 1};
+  int out = 0;
+  if (p <= 0.0) {
+    if (!nonisolated(phi, i, j, g)) {
+      im[c] = -2;
+      return;
+    }
+    for (int q = 0; q < 4; q++)
+      if (nbr[q] >= 0 && mul(p, phi[nbr[q]]) <= 0.0)
+        out = -1;
+  }
+  // written by a non-isolated phi <= 0 neighbour whose product with us is <= 0
+  for (int q = 0; q < 4 && out == 0; q++) {
+    if (nbr[q] < 0)
+      continue;
+    double pn = phi[nbr[q]];
+    if (pn <= 0.0 && mul(pn, p) <= 0.0 && nonisolated(phi, ni[q], nj[q], g))
+      out = sg;
+  }
+  im[c] = out;
+}
+
+// ===========================================================================
+// Interface Riemann problem (slip conditions, no heat conduction).
+
+// rotation_matrix (rotations.cpp:5-35): rows e1 = n, e2, e3.
+GPR_D void rotation(const double n[2], int nd, double R[3][3]) {
+  double e1[3] = {n[0], nd == 2 ? n[1] : 0.0, 0.0}, e2[3], e3[3], den;
+  double Sq = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+  if (fabs(e1[1] + e1[2]) <= fabs(e1[1] - e1[2])) {
+    den = sqrt(2.0 * (1.0 - e1[0] * e1[1] - e1[1] * e1[2] - e1[2] * e1[0]));
+    e2[0] = e1[1] - e1[2];
+    e2[1] = e1[2] - e1[0];
+    e2[2] = e1[0] - e1[1];
+    double Sum = e1[0] + e1[1] + e1[2];
+    for (int i = 0; i < 3; i++)
+      e3[i] = e1[i] * Sum - Sq;
+  } else {
+    den = sqrt(2.0 * (1.0 + e1[0] * e1[1] + e1[1] * e1[2] - e1[2] * e1[0]));
+    e2[0] = e1[1] + e1[2];
+    e2[1] = e1[2] - e1[0];
+    e2[2] = -e1[0] - e1[1];
+    double Sum = e1[0] - e1[1] + e1[2];
+    e3[0] = e1[0] * Sum - Sq;
+    e3[1] = e1[1] * Sum + Sq;
+    e3[2] = e1[2] * Sum - Sq;
+  }
+  for (int i = 0; i < 3; i++) {
+    R[0][i] = e1[i];
+    R[1][i] = e2[i] / den;
+    R[2][i] = e3[i] / den;
+  }
+}
+
+// rotate_tensors (rotations.cpp:37-47): v <- R v, A <- R A R^T.
+GPR_D void rotate(double *Q, const double R[3][3]) {
+  double v[3], T[9];
+  for (int i = 0; i < 3; i++)
+    v[i] = R[i][0] * Q[2] + R[i][1] * Q[3] + R[i][2] * Q[4];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      T[3 * i + j] = R[i][0] * Q[5 + j] + R[i][1] * Q[8 + j] + R[i][2] * Q[11 + j];
+  for (int i = 0; i < 3; i++) {
+    Q[2 + i] = v[i];
+    for (int j = 0; j < 3; j++)
+      Q[5 + 3 * i + j] = T[3 * i] * R[j][0] + T[3 * i + 1] * R[j][1] + T[3 * i + 2] * R[j][2];
+  }
+}
+
+// Gaussian elimination with partial pivoting: A X = B in place (A n x n,
+// B n x m, row-major).  Returns false on a zero pivot.
+template <int n, int m> GPR_D bool gauss(double *A, double *B) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++)
+      if (fabs(A[r * n + c]) > fabs(A[p * n + c]))
+        p = r;
+    if (A[p * n + c] == 0.0)
+      return false;
+    if (p != c) {
+      for (int j = 0; j < n; j++) {
+        double t = A[c * n + j];
+        A[c * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
+      for (int j = 0; j < m; j++) {
+        double t = B[c * m + j];
+        B[c * m + j] = B[p * m + j];
+        B[p * m + j] = t;
+      }
+    }
+    for (int r = c + 1; r < n; r++) {
+      double f = A[r * n + c] / A[c * n + c];
+      for (int j = c; j < n; j++)
+        A[r * n + j] -= f * A[c * n + j];
+      for (int j = 0; j < m; j++)
+        B[r * m + j] -= f * B[c * m + j];
+    }
+  }
+  for (int c = n - 1; c >= 0; c--)
+    for (int j = 0; j < m; j++) {
+      double s = B[c * m + j];
+      for (int k = c + 1; k < n; k++)
+        s -= A[c * n + k] * B[k * m + j];
+      B[c * m + j] = s / A[c * n + c];
+    }
+  return true;
+}
+
+GPR_D bool inv3(const double *M, double *out) {
+  double A[9];
+  for (int k = 0; k < 9; k++) {
+    A[k] = M[k];
+    out[k] = (k % 4) == 0 ? 1.0 : 0.0;
+  }
+  return gauss<3, 3>(A, out);
+}
+
+// Eigenvalues of a real 3 x 3 matrix from its characteristic polynomial
+// (depressed cubic: trigonometric form for three real roots, Cardano for a
+// complex pair).  ok = false when an eigenvalue has a non-positive real part
+// or the pair's imaginary part exceeds 1e-6 of the spectral radius: the
+// reference's Q diag(Re(lambda)^(-1/2)) Q^(-1) with Q = Re(eigenvectors)
+// (riemann.cpp:136-141) is NaN or singular there and its star state falls
+// back to the input state.
+GPR_D bool eig3_real_positive(const double *M) {
+  double p1 = M[0] + M[4] + M[8];
+  double p2 = M[0] * M[4] - M[1] * M[3] + M[0] * M[8] - M[2] * M[6] + M[4] * M[8] -
+              M[5] * M[7];
+  double p3 = M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) +
+              M[2] * (M[3] * M[7] - M[4] * M[6]);
+  double s = p1 / 3.0;
+  double a = p2 - p1 * p1 / 3.0;
+  double b = -2.0 * p1 * p1 * p1 / 27.0 + p1 * p2 / 3.0 - p3;
+  double disc = b * b / 4.0 + a * a * a / 27.0;  // > 0: complex pair
+  if (disc > 0.0) {
+    double sq = sqrt(disc);
+    double u = cbrt(-b / 2.0 + sq), v = cbrt(-b / 2.0 - sq);
+    double lr = s + u + v;                  // real root
+    double cr = s - (u + v) / 2.0;          // real part of the pair
+    double ci = 0.86602540378443864676 * fabs(u - v);
+    double rad = fmax(fabs(lr), hypot(cr, ci));
+    return lr > 0.0 && cr > 0.0 && !(ci > 1e-6 * rad);
+  }
+  // three real roots: s + 2 sqrt(-a/3) cos(theta/3 - 2 pi k / 3)
+  double r = sqrt(fmax(-a / 3.0, 0.0));
+  double lo;
+  if (r == 0.0) {
+    lo = s;
+  } else {
+    double ct = -b / (2.0 * r * r * r);
+    ct = fmin(1.0, fmax(-1.0, ct));
+    double th = acos(ct);
+    // the smallest of the three is k = 1 (theta / 3 + 2 pi / 3 in [2pi/3, pi])
+    lo = s + 2.0 * r * cos(th / 3.0 + 2.0943951023931954923);
+  }
+  return lo > 0.0;
+}
+
+// Inverse principal square root by the Denman-Beavers iteration
+// (Y -> M^(1/2), Z -> M^(-1/2)); the reference forms the same matrix
+// function from an eigen-decomposition (riemann.cpp:136-141).
+GPR_D bool inv_sqrt3(const double *M, double *Zout) {
+  double Y[9], Z[9], Yi[9], Zi[9];
+  for (int k = 0; k < 9; k++) {
+    Y[k] = M[k];
+    Z[k] = (k % 4) == 0 ? 1.0 : 0.0;
+  }
+  int extra = 0;
+  for (int it = 0; it < 100; it++) {
+    if (!inv3(Y, Yi) || !inv3(Z, Zi))
+      return false;
+    double dmax = 0.0, ymax = 0.0;
+    for (int k = 0; k < 9; k++) {
+      double y = 0.5 * (Y[k] + Zi[k]);
+      double z = 0.5 * (Z[k] + Yi[k]);
+      dmax = fmax(dmax, fabs(y - Y[k]));
+      ymax = fmax(ymax, fabs(y));
+      Y[k] = y;
+      Z[k] = z;
+    }
+    if (dmax <= 1e-13 * ymax && ++extra == 2)
+      break;
+  }
+  for (int k = 0; k < 9; k++)
+    Zout[k] = Z[k];
+  return true;
+}
+
+// Total stress column 0: Sigma = p e0 - sigma(:, 0)  (variables/state.cpp:39-46).
+GPR_D void Sigma0(const double *Q, const Prim<false> &s, double *S) {
+  sigma_col<false>(Q, s, 0, S);
+  S[0] = s.p - S[0];
+  S[1] = -S[1];
+  S[2] = -S[2];
+}
+
+// d sigma(:, 0) / d rho and d sigma(:, 0) / dA (variables/state.cpp:43-56,
+// energy/derivatives.cpp).
+GPR_D void dsigma0(const double *Q, const Prim<false> &s, const DevPar &P, double *sr,
+                   double *Pi1) {
+  double r = s.r;
+  double dcs2 = P.beta / r * s.cs2;
+  sigma_col<false>(Q, s, 0, sr);
+  double f = 1.0 / r + dcs2 / s.cs2;
+  for (int i = 0; i < 3; i++)
+    sr[i] *= f;
+  const double *A = Q + 5;
+  double G[9], ret[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      G[3 * i + j] = A[i] * A[j] + A[3 + i] * A[3 + j] + A[6 + i] * A[6 + j];
+  for (int k = 0; k < 9; k++)
+    ret[k] = s.AdG[k];
+  for (int i = 0; i < 3; i++)
+    ret[3 * i] *= 2.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      ret[3 * i + j] += 1.0 / 3.0 * A[3 * i] * G[j];
+  for (int k = 0; k < 9; k++)
+    ret[k] += G[0] * A[k];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      Pi1[3 * i + j] = -r * s.cs2 * ret[3 * j + i];
+}
+
+// c_0 (waves/speeds.cpp:8-18).
+GPR_D double c0_of(const Prim<false> &s, const DevPar &P) {
+  double r = s.r, G = s.e.G, dG = s.e.dG;
+  double dedrho = s.e.der - (s.e.dpr * r * G + (G + r * dG) * (s.p - s.e.pr)) /
+                                ((r * G) * (r * G));
+  double dcs2 = P.beta / r * s.cs2;
+  double dC0 = (1.0 - P.beta / G) * dcs2 + P.beta / (G * G) * dG * s.cs2;
+  double dEdr = dedrho + dC0 / 4.0 * s.devGsq;
+  double dedp = 1.0 / (r * G);
+  return sqrt((s.p / (r * r) - dEdr) / dedp);
+}
+
+// The first three columns of riemann_constraints (riemann.cpp:79-154) for
+// the non-thermal system; rows 0-4 are X, rows 11-13 -sgn Y0 Xi1 X, the rest
+// zero (the other columns multiply zero coefficients in star_stepper).
+// Rx is [5][3], Ry is [3][3].
+GPR_D bool constraints(const double *Q, double sgn, const DevPar &P, double *Rx, double *Ry) {
+  Prim<false> s;
+  prim<false>(Q, P, s);
+  double r = s.r;
+  const double *A = Q + 5;
+  double sr[3], Pi1[9], Pi1i[9], Ai[9], sg[3];
+  dsigma0(Q, s, P, sr, Pi1);
+  sigma_col<false>(Q, s, 0, sg);
+  if (!inv3(A, Ai) || !inv3(Pi1, Pi1i))
+    return false;
+  double tmp[25];
+  for (int k = 0; k < 25; k++)
+    tmp[k] = 0.0;
+  for (int i = 0; i < 3; i++) {
+    tmp[5 * i] = -sr[i];
+    for (int j = 0; j < 3; j++)
+      tmp[5 * i + 2 + j] = -Pi1[3 * i + j];
+  }
+  tmp[1] = 1.0;
+  double c0 = c0_of(s, P);
+  double B[6] = {r, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int j = 0; j < 3; j++)
+    B[3 + j] = sg[j] - r * sr[j];
+  B[3] += r * c0 * c0;
+  double C[6];
+  for (int i = 0; i < 3; i++) {
+    C[2 * i] = -(Pi1i[3 * i] * sr[0] + Pi1i[3 * i + 1] * sr[1] + Pi1i[3 * i + 2] * sr[2]);
+    C[2 * i + 1] = Pi1i[3 * i];
+  }
+  double BA[6];
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 3; j++)
+      BA[3 * i + j] = B[3 * i] * Ai[j] + B[3 * i + 1] * Ai[3 + j] + B[3 * i + 2] * Ai[6 + j];
+  double Z[4];
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      Z[2 * i + j] = (i == j ? 1.0 : 0.0) -
+                     (BA[3 * i] * C[j] + BA[3 * i + 1] * C[2 + j] + BA[3 * i + 2] * C[4 + j]);
+  double dz = Z[0] * Z[3] - Z[1] * Z[2];
+  if (dz == 0.0)
+    return false;
+  double Zi[4] = {Z[3] / dz, -Z[1] / dz, -Z[2] / dz, Z[0] / dz};
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 5; j++) {
+      double w0 = j == 0 ? 1.0 : (j == 1 ? 0.0 : -BA[j - 2]);
+      double w1 = j == 0 ? 0.0 : (j == 1 ? 1.0 : -BA[3 + j - 2]);
+      tmp[5 * (3 + i) + j] = Zi[2 * i] * w0 + Zi[2 * i + 1] * w1;
+    }
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 3; j++)
+      Rx[3 * i + j] = i == j ? 1.0 : 0.0;
+  if (!gauss<5, 3>(tmp, Rx))
+    return false;
+  // Xi1 (3 x 5) and Xi2 (5 x 3) of system/eig.cpp:8-53 along x
+  double X1[15], X2[15], Xi[9], Y0[9];
+  for (int k = 0; k < 15; k++)
+    X1[k] = X2[k] = 0.0;
+  X1[1] = 1.0 / r;
+  for (int i = 0; i < 3; i++) {
+    X1[5 * i] = -1.0 / r * sr[i];
+    for (int j = 0; j < 3; j++)
+      X1[5 * i + 2 + j] = -1.0 / r * Pi1[3 * i + j];
+  }
+  X2[0] = r;
+  X2[3] = r * c0 * c0;
+  for (int j = 0; j < 3; j++)
+    X2[3 + j] += sg[j] - r * sr[j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      X2[3 * (2 + i) + j] = A[3 * i + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double t = 0.0;
+      for (int k = 0; k < 5; k++)
+        t += X1[5 * i + k] * X2[3 * k + j];
+      Xi[3 * i + j] = t;
+    }
+  if (!eig3_real_positive(Xi) || !inv_sqrt3(Xi, Y0))
+    return false;
+  double X1X[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double t = 0.0;
+      for (int k = 0; k < 5; k++)
+        t += X1[5 * i + k] * Rx[3 * k + j];
+      X1X[3 * i + j] = t;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      Ry[3 * i + j] = -sgn * (Y0[3 * i] * X1X[j] + Y0[3 * i + 1] * X1X[3 + j] +
+                              Y0[3 * i + 2] * X1X[6 + j]);
+  return true;
+}
+
+// Cvec_to_Pvec + P += R c + Pvec_to_Cvec (functions/vectors.cpp:85-154,
+// riemann.cpp:191-200) for the non-thermal layout
+// P = [rho, p, A(:,0), A(:,1), A(:,2), v, phi].
+GPR_D void apply_correction(double *Q, const double *Rx, const double *Ry, const double *cc,
+                            const DevPar &P) {
+  Prim<false> s;
+  prim<false>(Q, P, s);
+  double Pv[14];
+  Pv[0] = Q[0];
+  Pv[1] = s.p;
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      Pv[2 + 3 * j + i] = Q[5 + 3 * i + j];
+  for (int i = 0; i < 3; i++)
+    Pv[11 + i] = Q[2 + i] * s.ir;
+  for (int k = 0; k < 5; k++)
+    Pv[k] += Rx[3 * k] * cc[0] + Rx[3 * k + 1] * cc[1] + Rx[3 * k + 2] * cc[2];
+  for (int k = 0; k < 3; k++)
+    Pv[11 + k] += Ry[3 * k] * cc[0] + Ry[3 * k + 1] * cc[1] + Ry[3 * k + 2] * cc[2];
+  double r = Pv[0], p = Pv[1];
+  Q[0] = r;
+  double A[9];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      A[3 * i + j] = Pv[2 + 3 * j + i];
+  for (int k = 0; k < 9; k++)
+    Q[5 + k] = A[k];
+  double v0 = Pv[11], v1 = Pv[12], v2 = Pv[13];
+  Q[2] = r * v0;
+  Q[3] = r * v1;
+  Q[4] = r * v2;
+  // total_energy (energy/eos.cpp:43-47)
+  double ir = 1.0 / r;
+  EosRho e = eos_rho(r, ir, P);
+  double cs2 = P.beta == 0.0 ? P.b02 : P.b02 * pow(r * P.ir0, P.beta);
+  double C0 = (1.0 - P.beta / e.G) * cs2;
+  double G00 = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+  double G11 = A[3] * A[3] + A[4] * A[4] + A[5] * A[5];
+  double G22 = A[6] * A[6] + A[7] * A[7] + A[8] * A[8];
+  double G01 = A[0] * A[3] + A[1] * A[4] + A[2] * A[5];
+  double G02 = A[0] * A[6] + A[1] * A[7] + A[2] * A[8];
+  double G12 = A[3] * A[6] + A[4] * A[7] + A[5] * A[8];
+  double t = (G00 + G11 + G22) / 3.0;
+  double dg = (G00 - t) * (G00 - t) + (G11 - t) * (G11 - t) + (G22 - t) * (G22 - t) +
+              2.0 * (G01 * G01 + G02 * G02 + G12 * G12);
+  double E = e.er + (p - e.pr) / (r * e.G) + 0.5 * (v0 * v0 + v1 * v1 + v2 * v2) +
+             C0 / 4.0 * dg;
+  Q[1] = r * E;
+}
+
+constexpr double STAR_TOL = 1e-8;  // options.h:22
+
+// check_star_convergence (riemann.cpp:26-77), slip conditions.
+GPR_D bool star_converged(const double *QL, const double *QR, const DevPar &PL,
+                          const DevPar &PR) {
+  Prim<false> sl;
+  prim<false>(QL, PL, sl);
+  double SL[3];
+  Sigma0(QL, sl, SL);
+  if (PR.EOS > -1) {
+    Prim<false> sr;
+    prim<false>(QR, PR, sr);
+    double SR[3];
+    Sigma0(QR, sr, SR);
+    double r0 = fmin(PL.rho0, PR.rho0), b02 = fmin(PL.b02, PR.b02);
+    return fabs(SL[0] - SR[0]) / (b02 * r0) < STAR_TOL &&
+           fabs(QL[2] / QL[0] - QR[2] / QR[0]) / sqrt(b02) < STAR_TOL;
+  }
+  double mx = fmax(fabs(SL[0]), fmax(fabs(SL[1]), fabs(SL[2])));
+  return mx / (PL.b02 * PL.rho0) < STAR_TOL;
+}
+
+// star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:57-90).
+GPR_D bool star_step(double *QL, double *QR, const DevPar &PL, const DevPar &PR) {
+  double RLx[15], RLy[9], cL[3];
+  if (!constraints(QL, 1.0, PL, RLx, RLy))
+    return false;
+  Prim<false> sl;
+  prim<false>(QL, PL, sl);
+  double xL[3];
+  Sigma0(QL, sl, xL);
+  if (PR.EOS > -1) {
+    double RRx[15], RRy[9], xR[3], cR[3];
+    if (!constraints(QR, -1.0, PR, RRx, RRy))
+      return false;
+    Prim<false> sr;
+    prim<false>(QR, PR, sr);
+    Sigma0(QR, sr, xR);
+    double yL = QL[2] / QL[0], yR = QR[2] / QR[0];
+    // row 11 of the constraint matrices (the normal velocity)
+    double dL = RLy[0] * xL[0] + RLy[1] * xL[1] + RLy[2] * xL[2];
+    double dR = RRy[0] * xR[0] + RRy[1] * xR[1] + RRy[2] * xR[2];
+    double x0 = (yR - yL + dL - dR) / (RLy[0] - RRy[0]);
+    double xs[3] = {x0, 0.0, 0.0};
+    for (int i = 0; i < 3; i++) {
+      cL[i] = xs[i] - xL[i];
+      cR[i] = xs[i] - xR[i];
+    }
+    apply_correction(QR, RRx, RRy, cR, PR);
+  } else {
+    for (int i = 0; i < 3; i++)
+      cL[i] = -xL[i];
+    for (int k = 0; k < 14; k++)
+      QR[k] = 0.0;
+  }
+  apply_correction(QL, RLx, RLy, cL, PL);
+  return true;
+}
+
+// left_star_state (riemann.cpp:203-233): the left star state of the
+// interface Riemann problem between QL (material PL) and QR (material PR)
+// along the unit normal n: at most ten linearised steps, each after a half
+// step dt/2 of the stiff relaxation; the input is returned if a NaN appears.
+// The level set entry (index 14) is carried through unchanged.
+GPR_D void left_star_state(const double *QL0, const double *QR0, const DevPar &PL,
+                           const DevPar &PR, double dt, const double n[2], int nd,
+                           double *out) {
+  double QL[15], QR[15], R[3][3];
+  for (int k = 0; k < 15; k++) {
+    QL[k] = QL0[k];
+    QR[k] = QR0[k];
+  }
+  rotation(n, nd, R);
+  rotate(QL, R);
+  rotate(QR, R);
+  bool nan = false;
+  for (int count = 0; count < 10 && !star_converged(QL, QR, PL, PR); count++) {
+    // ode_stepper_analytic (relaxation/analytic.cpp:152-161), no heat flux
+    QL[2] += PL.dp0 * dt / 2;
+    QL[3] += PL.dp1 * dt / 2;
+    QL[4] += PL.dp2 * dt / 2;
+    ode_distortion(QL, dt / 2, PL);
+    if (PR.EOS > -1) {
+      QR[2] += PR.dp0 * dt / 2;
+      QR[3] += PR.dp1 * dt / 2;
+      QR[4] += PR.dp2 * dt / 2;
+      ode_distortion(QR, dt / 2, PR);
+    }
+    if (!star_step(QL, QR, PL, PR)) {
+      nan = true;
+      break;
+    }
+  }
+  for (int k = 0; k < 15; k++)
+    nan = nan || isnan(QL[k]);
+  if (nan) {
+    for (int k = 0; k < 15; k++)
+      out[k] = QL0[k];
+    return;
+  }
+  double RT[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      RT[i][j] = R[j][i];
+  rotate(QL, RT);
+  for (int k = 0; k < 15; k++)
+    out[k] = QL[k];
+}
+
+// ===========================================================================
+// Boundary fill (multi/fill.cpp:96-235).
+
+// One boundary cell (intMask == 1: the first ghost cell outside material
+// mat) and where its fill reads and writes.
+struct BPlan {
+  int c;       // the cell
+  int R;       // probe on the far side of the interface (QR)
+  int ql;      // cell QL is read from
+  int wi;      // interface cell also written (-1: none)
+  int miR;     // material of QR
+  int pad;
+  double n[2]; // normal (axis-aligned by the fallback branch)
+};
+
+// get_material_index (functions/vectors.cpp:24-31) from the level set entry.
+template <int V> GPR_D int mat_of(const double *grid, long c) {
+  return grid[c * V + V - 1] >= 0.0 ? 1 : 0;
+}
+
+// Unit normal of dphi row c (normal, multi/functions.cpp:14); false when it
+// is not finite.
+GPR_D bool unit_normal(const double *dphi, long c, int nd, double n[2]) {
+  if (nd == 1) {
+    double g = dphi[c];
+    double s = __dsqrt_rn(mul(g, g));
+    n[0] = dvd(g, s);
+    n[1] = 0.0;
+    return isfinite(n[0]);
+  }
+  double g0 = dphi[2 * c], g1 = dphi[2 * c + 1];
+  double s = __dsqrt_rn(add(mul(g0, g0), mul(g1, g1)));
+  n[0] = dvd(g0, s);
+  n[1] = dvd(g1, s);
+  return isfinite(n[0]) && isfinite(n[1]);
+}
+
+// Plans every boundary cell: boundary_inds (fill.cpp:96-132) and the choice
+// of QL in fill_boundary_inner (fill.cpp:134-198).  Cells whose fill would
+// read outside the grid in the reference are counted in err[1] and left
+// unfilled.  lastw[x] collects the largest boundary cell writing x.
+template <int V>
+__global__ void k_plan(const double *__restrict__ phi, const double *__restrict__ dphi,
+                       const int32_t *__restrict__ im, const double *__restrict__ grid,
+                       int mat, Grid g,
+                       BPlan *__restrict__ plan, int *__restrict__ nplan,
+                       int32_t *__restrict__ pidx, int32_t *__restrict__ lastw,
+                       int *__restrict__ err, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell || im[c] != 1)
+    return;
+  int i = g.nd == 1 ? (int)c : (int)(c / g.ny), j = g.nd == 1 ? 0 : (int)(c % g.ny);
+  double n[2];
+  if (!unit_normal(dphi, c, g.nd, n)) {
+    atomicAdd(&err[1], 1);
+    return;
+  }
+  double phii = phi[c];
+  int vi[2], vl[2], vr[2];
+  int ind2[2] = {i, j};
+  for (int k = 0; k < g.nd; k++) {
+    double h = k == 0 ? g.dx : g.dy;
+    double xp = mul(add((double)ind2[k], 0.5), h);
+    double xi = sub(xp, mul(phii, n[k]));
+    double hn = mul(mul(1.0, h), n[k]);
+    vi[k] = (int)dvd(xi, h);
+    vl[k] = (int)dvd(sub(xi, hn), h);
+    vr[k] = (int)dvd(add(xi, hn), h);
+  }
+  long interf = g.nd == 1 ? vi[0] : (long)vi[0] * g.ny + vi[1];
+  long L = g.nd == 1 ? vl[0] : (long)vl[0] * g.ny + vl[1];
+  long R = g.nd == 1 ? vr[0] : (long)vr[0] * g.ny + vr[1];
+  if (interf < 0 || interf >= g.ncell || L < 0 || L >= g.ncell || R < 0 || R >= g.ncell) {
+    atomicAdd(&err[1], 1);
+    return;
+  }
+  long ql;
+  if (mat_of<V>(grid, interf) == mat) {
+    ql = interf;
+  } else if (mat_of<V>(grid, L) == mat) {
+    ql = L;
+  } else {
+    if (g.nd == 1) {
+      atomicAdd(&err[1], 1);
+      return;
+    }
+    int Li[2] = {i, j};
+    long Lind;
+    int n0 = (n[0] > 0) - (n[0] < 0), n1 = (n[1] > 0) - (n[1] < 0);
+    if (fabs(n[0]) > fabs(n[1])) {
+      Li[0] -= n0;
+      Lind = (long)Li[0] * g.ny + Li[1];
+      if (Lind >= 0 && Lind < g.ncell && mat_of<V>(grid, Lind) == mat) {
+        n[0] = n0;
+        n[1] = 0.0;
+      } else {
+        Li[0] += n0;
+        Li[1] -= n1;
+        Lind = (long)Li[0] * g.ny + Li[1];
+        n[0] = 0.0;
+        n[1] = n1;
+      }
+    } else {
+      Li[1] -= n1;
+      Lind = (long)Li[0] * g.ny + Li[1];
+      if (Lind >= 0 && Lind < g.ncell && mat_of<V>(grid, Lind) == mat) {
+        n[0] = 0.0;
+        n[1] = n1;
+      } else {
+        Li[0] -= n0;
+        Li[1] += n1;
+        Lind = (long)Li[0] * g.ny + Li[1];
+        n[0] = n0;
+        n[1] = 0.0;
+      }
+    }
+    if (Lind < 0 || Lind >= g.ncell) {
+      atomicAdd(&err[1], 1);
+      return;
+    }
+    if (mat_of<V>(grid, Lind) == mat) {
+      ql = Lind;
+    } else {
+      // neighbor_index(intMask, i, j, nx, ny, -1) (fill.cpp:76-94): the
+      // last of left, right, down, up with intMask -1
+      long indn = -1;
+      if (i > 0 && im[c - g.ny] == -1)
+        indn = c - g.ny;
+      if (i < g.nx - 1 && im[c + g.ny] == -1)
+        indn = c + g.ny;
+      if (j > 0 && im[c - 1] == -1)
+        indn = c - 1;
+      if (j < g.ny - 1 && im[c + 1] == -1)
+        indn = c + 1;
+      if (indn < 0) {
+        atomicAdd(&err[1], 1);
+        return;
+      }
+      ql = indn;
+    }
+  }
+  int k = atomicAdd(nplan, 1);
+  BPlan b;
+  b.c = (int)c;
+  b.R = (int)R;
+  b.ql = (int)ql;
+  b.wi = mat_of<V>(grid, interf) != mat ? (int)interf : -1;
+  b.miR = mat_of<V>(grid, R);
+  b.pad = 0;
+  b.n[0] = n[0];
+  b.n[1] = n[1];
+  plan[k] = b;
+  pidx[c] = k;
+  atomicMax(&lastw[c], (int)c);
+  if (b.wi >= 0)
+    atomicMax(&lastw[b.wi], (int)c);
+}
+
+// For each plan entry, the entry whose fill last wrote its QR cell earlier
+// in the reference's (i, j) sweep (-1: QR is the original state), and its
+// level in that dependency chain.
+__global__ void k_plan_deps(const BPlan *__restrict__ plan, const int *__restrict__ nplan,
+                            const int32_t *__restrict__ pidx,
+                            const int32_t *__restrict__ lastw, int32_t *__restrict__ dep,
+                            const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  int B = *nplan;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B; k += gridDim.x * blockDim.x) {
+    int c = plan[k].c, R = plan[k].R;
+    int w = lastw[R];
+    int dk = -1;
+    if (w >= 0 && w < c) {
+      dk = pidx[w];
+    } else if (w >= c) {
+      // a later (or this) cell writes R too: scan for the last earlier one
+      int best = -1;
+      for (int q = 0; q < B; q++) {
+        int cq = plan[q].c;
+        if (cq < c && cq > best && (cq == R || plan[q].wi == R))
+          best = cq;
+      }
+      dk = best >= 0 ? pidx[best] : -1;
+    }
+    dep[k] = dk;
+  }
+}
+
+__global__ void k_plan_levels(const int *__restrict__ nplan, const int32_t *__restrict__ dep,
+                              int32_t *__restrict__ level, int *__restrict__ maxlevel,
+                              const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  int B = *nplan;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B; k += gridDim.x * blockDim.x) {
+    int L = 0, q = dep[k];
+    while (q >= 0 && L < B) {
+      L++;
+      q = dep[q];
+    }
+    level[k] = L;
+    if (L > 0)
+      atomicMax(maxlevel, L);
+  }
+}
+
+template <int V>
+GPR_D void solve_plan(int k, const BPlan *plan, const int32_t *dep, const double *grid,
+                      double *star, const DevPar &P0, const DevPar &P1, int mat, double dt,
+                      int nd) {
+  static_assert(V == 15, "the ghost fill is for the viscous one-level-set layout");
+  const BPlan &b = plan[k];
+  double QL[V], QR[V], out[V];
+  for (int v = 0; v < V; v++)
+    QL[v] = grid[(long)b.ql * V + v];
+  int dk = dep[k];
+  for (int v = 0; v < V; v++)
+    QR[v] = dk >= 0 && v < V - 1 ? star[(long)dk * V + v] : grid[(long)b.R * V + v];
+  const DevPar &PL = mat == 0 ? P0 : P1;
+  const DevPar &PR = b.miR == 0 ? P0 : P1;
+  left_star_state(QL, QR, PL, PR, dt, b.n, nd, out);
+  for (int v = 0; v < V; v++)
+    star[(long)k * V + v] = out[v];
+}
+
+// Star states of the plan entries on level 0 (all independent).
+template <int V>
+__global__ void __launch_bounds__(64)
+    k_star_level0(const BPlan *__restrict__ plan, const int *__restrict__ nplan,
+                  const int32_t *__restrict__ dep, const int32_t *__restrict__ level,
+                  const double *__restrict__ grid, double *__restrict__ star, DevPar P0,
+                  DevPar P1, int mat, double dt, const double *__restrict__ dt_dev, int nd,
+                  const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  if (dt_dev)
+    dt = *dt_dev;
+  int B = *nplan;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B; k += gridDim.x * blockDim.x)
+    if (level[k] == 0)
+      solve_plan<V>(k, plan, dep, grid, star, P0, P1, mat, dt, nd);
+}
+
+// Deeper levels, in order, in one block (rare: only where a boundary cell's
+// far-side probe was filled earlier in the sweep).
+template <int V>
+__global__ void __launch_bounds__(64)
+    k_star_levels(const BPlan *__restrict__ plan, const int *__restrict__ nplan,
+                  const int32_t *__restrict__ dep, const int32_t *__restrict__ level,
+                  const int *__restrict__ maxlevel, const double *__restrict__ grid,
+                  double *__restrict__ star, DevPar P0, DevPar P1, int mat, double dt,
+                  const double *__restrict__ dt_dev, int nd, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  if (dt_dev)
+    dt = *dt_dev;
+  int B = *nplan, ML = *maxlevel;
+  for (int L = 1; L <= ML; L++) {
+    for (int k = threadIdx.x; k < B; k += blockDim.x)
+      if (level[k] == L)
+        solve_plan<V>(k, plan, dep, grid, star, P0, P1, mat, dt, nd);
+    __syncthreads();
+  }
+}
+
+// Every written cell takes the star state of its last writer in the sweep;
+// the level set entry keeps the grid's value (fill.cpp:194-197).
+template <int V>
+__global__ void k_scatter(const BPlan *__restrict__ plan, const int *__restrict__ nplan,
+                          const int32_t *__restrict__ lastw, const double *__restrict__ star,
+                          double *__restrict__ grid, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  int B = *nplan;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B; k += gridDim.x * blockDim.x) {
+    int c = plan[k].c, wi = plan[k].wi;
+    if (lastw[c] == c)
+      for (int v = 0; v < V - 1; v++)
+        grid[(long)c * V + v] = star[(long)k * V + v];
+    if (wi >= 0 && lastw[wi] == c)
+      for (int v = 0; v < V - 1; v++)
+        grid[(long)wi * V + v] = star[(long)k * V + v];
+  }
+}
+
+// ===========================================================================
+// Layered fill (fill_neighbor_cells, multi/fill.cpp:237-328): layer N0 + 1
+// is every cell with intMask 0 (or -2 in 2D) next to a layer-N0 cell.
+
+struct Layer {
+  const int32_t *m;  // intMask before this layer
+  Grid g;
+  int N0;
+  GPR_D bool open(long x) const {
+    int v = m[x];
+    return v == 0 || (g.nd == 2 && v == -2);
+  }
+  // is x in this layer; indn = the reference's neighbour index (the last
+  // match in the order left, right, down, up)
+  GPR_D bool in(long x, long &indn) const {
+    indn = -1;
+    if (!open(x))
+      return false;
+    if (g.nd == 1) {
+      int i = (int)x;
+      if (i > 0 && m[x - 1] == N0)
+        indn = x - 1;
+      if (i < g.nx - 1 && m[x + 1] == N0)
+        indn = x + 1;
+      return indn >= 0;
+    }
+    int i = (int)(x / g.ny), j = (int)(x % g.ny);
+    if (i > 0 && m[x - g.ny] == N0)
+      indn = x - g.ny;
+    if (i < g.nx - 1 && m[x + g.ny] == N0)
+      indn = x + g.ny;
+    if (j > 0 && m[x - 1] == N0)
+      indn = x - 1;
+    if (j < g.ny - 1 && m[x + 1] == N0)
+      indn = x + 1;
+    return indn >= 0;
+  }
+};
+
+// One layer.  In the reference's sweep a new cell copies the cell one step
+// towards the interface along its normal if that cell's mask is >= 1 at
+// that moment, else the layer-N0 neighbour it was reached from; cells of
+// this layer visited earlier in the sweep already hold their copies, so a
+// copy from one of them is followed to where it copied from.
+template <int V>
+__global__ void k_layer(double *__restrict__ grid, const int32_t *__restrict__ mprev,
+                        int32_t *__restrict__ mnext, const double *__restrict__ dphi, Grid g,
+                        int N0, int *__restrict__ err, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell)
+    return;
+  Layer Ly{mprev, g, N0};
+  long indn;
+  if (!Ly.in(c, indn)) {
+    mnext[c] = mprev[c];
+    return;
+  }
+  mnext[c] = mprev[c] == -2 ? -2 : N0 + 1;  // isolated cells return to -2
+  long x = c, xn = indn, src = -1;
+  for (int hops = 0; hops < 4096; hops++) {
+    double n[2];
+    long nind = -1;
+    if (unit_normal(dphi, x, g.nd, n)) {
+      int i = g.nd == 1 ? (int)x : (int)(x / g.ny), j = g.nd == 1 ? 0 : (int)(x % g.ny);
+      int ind2[2] = {i, j}, ni[2] = {0, 0};
+      for (int k = 0; k < g.nd; k++) {
+        double h = k == 0 ? g.dx : g.dy;
+        double xc = mul(add((double)ind2[k], 0.5), h);
+        ni[k] = (int)dvd(sub(xc, mul(h, n[k])), h);
+      }
+      nind = g.nd == 1 ? ni[0] : (long)ni[0] * g.ny + ni[1];
+    }
+    bool off = nind < 0 || nind >= g.ncell;
+    if (off) {
+      atomicAdd(&err[2], 1);
+      src = xn;
+      break;
+    }
+    if (nind == x) {  // copies itself: keeps its own value
+      src = x;
+      break;
+    }
+    long nn;
+    if (nind < x && Ly.in(nind, nn)) {  // filled earlier in this layer
+      x = nind;
+      xn = nn;
+      continue;
+    }
+    src = mprev[nind] >= 1 ? nind : xn;
+    break;
+  }
+  if (src < 0) {
+    atomicAdd(&err[2], 1);
+    return;
+  }
+  if (src != c)
+    for (int v = 0; v < V - 1; v++)
+      grid[c * V + v] = grid[src * V + v];
+}
+
+// Update mask of material mat (fill.cpp:364-365).
+__global__ void k_mat_mask(const double *__restrict__ phi, const int32_t *__restrict__ im,
+                           uint8_t *__restrict__ mask, long ncell,
+                           const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  int m = im[c];
+  mask[c] = (phi[c] <= 0.0 && m != -2) || m == 1;
+}
+
+// ===========================================================================
+// Merge, CFL and renormalisation over material grids.
+
+// make_u (solvers/iterator.cpp:12-42): the level set averaged over the
+// grids that updated the cell, the rest of the state from the grid of the
+// cell's material (zero for a vacuum).
+template <int V>
+__global__ void k_make_u(double *__restrict__ u, const double *__restrict__ grids,
+                         const uint8_t *__restrict__ masks, long ncell, int nmat, int eos0,
+                         int eos1, const double *__restrict__ dt_dev) {
+  if (dt_dev && *dt_dev == 0.0)
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  double s = 0.0, cnt = 0.0;
+  for (int m = 0; m < nmat; m++)
+    if (masks[(long)m * ncell + c]) {
+      s += grids[((long)m * ncell + c) * V + V - 1];
+      cnt += 1.0;
+    }
+  if (cnt > 0.0)
+    u[c * V + V - 1] = s / cnt;
+  int mi = u[c * V + V - 1] >= 0.0 ? 1 : 0;
+  int eos = mi == 0 ? eos0 : eos1;
+  for (int v = 0; v < V - 1; v++)
+    u[c * V + v] = eos > -1 ? grids[((long)mi * ncell + c) * V + v] : 0.0;
+}
+
+// timestep (solvers/iterator.cpp:54-83): max over the masked cells of one
+// material grid, accumulated over materials in *out.
+template <class L>
+__global__ void __launch_bounds__(256)
+    k_cfl_max_masked(const double *__restrict__ u, const uint8_t *__restrict__ mask, long ncell,
+                     int nd, double dx, double dy, unsigned long long *__restrict__ out,
+                     DevPar P, const double *__restrict__ clk) {
+  constexpr int V = L::V;
+  if (clk && clk[0] >= clk[2])
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  double m = 0.0;
+  if (c < ncell && mask[c]) {
+    double q[V];
+    for (int k = 0; k < V; k++)
+      q[k] = u[c * V + k];
+    Prim<L::THERMAL> s;
+    prim<L::THERMAL>(q, P, s);
+    double tmp = max_abs_eigs<L::THERMAL>(q, s, 0, P) / dx;
+    if (nd == 2)
+      tmp += max_abs_eigs<L::THERMAL>(q, s, 1, P) / dy;
+    if (tmp > m)
+      m = tmp;
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double sm[8];
+  if ((threadIdx.x & 31) == 0)
+    sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+      b = fmax(b, sm[w]);
+    atomicMax(out, (unsigned long long)__double_as_longlong(b));
+  }
+}
+
+// renorm_distortion (solvers/utils.cpp:6-23) with each cell's material
+// from its level set.
+template <int V>
+__global__ void k_renorm_multi(double *__restrict__ u, long ncell, double r00, double r01,
+                               int eos0, int eos1, const double *__restrict__ dt_dev) {
+  if (dt_dev && *dt_dev == 0.0)
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  double *q = u + c * V;
+  int mi = q[V - 1] >= 0.0 ? 1 : 0;
+  if ((mi == 0 ? eos0 : eos1) <= -1)
+    return;
+  double r = q[0];
+  if (r > 0) {
+    double A[9];
+    for (int k = 0; k < 9; k++)
+      A[k] = q[5 + k];
+    double f = cbrt(r / ((mi == 0 ? r00 : r01) * det3(A)));
+    for (int k = 0; k < 9; k++)
+      q[5 + k] = A[k] * f;
+  }
+}
+
+// Pointwise left_star_state for tests and the system.multi binding.
+template <int V>
+__global__ void k_star_pointwise(const double *__restrict__ QL, const double *__restrict__ QR,
+                                 const double *__restrict__ nrm, double *__restrict__ out,
+                                 long count, int nd, double dt, DevPar PL, DevPar PR) {
+  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= count)
+    return;
+  double n[2] = {nrm[k * nd], nd == 2 ? nrm[k * nd + 1] : 0.0};
+  left_star_state(QL + k * V, QR + k * V, PL, PR, dt, n, nd, out + k * V);
+}
+
+}  // namespace multi
+}  // namespace gpr
