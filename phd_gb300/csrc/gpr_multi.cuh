@@ -20,9 +20,10 @@
 //     same causal upwind update, whose fixed point is what the marcher
 //     computes (band neighbours always enter a point's quadratic, the others
 //     only while their distance is below the point's estimate, as the
-//     marcher's heap order makes it), evaluated with the marcher's
-//     arithmetic, within ~1e-13 of the marcher (the rounding noise of its
-//     own quadratic formula; most fields come out bit for bit);
+//     marcher's heap order makes it); the band is computed in FP64 with the
+//     marcher's roundings, the rest in double-float arithmetic with the
+//     quadratic's root written without cancellation (the marcher's own
+//     formula carries ~3e-13 relative noise per update);
 //   * a boundary cell reads the right-hand state of the interface from a
 //     cell that an earlier cell of the (i, j) sweep may have filled; those
 //     reads are resolved to the last earlier writer and solved level by
@@ -61,11 +62,18 @@ GPR_D double dvd(double a, double b) { return __ddiv_rn(a, b); }
 
 // Frozen band (initalizeFrozen, distance_marcher.cpp:90-151, with the
 // reference's edit: the least per-axis crossing distance): cells where phi
-// is zero or changes sign across a face.  Others start unknown (+inf).
-// phi[c * ps] is the level set of cell c.
+// is zero or changes sign across a face, in FP64 with the marcher's
+// roundings.  Others start unknown (+inf).  phi[c * ps] is the level set of
+// cell c.  fz: bit 0 frozen (band), bit 1 the marcher would take the
+// positive root for this cell (phi > DBL_EPSILON).  dff is the double-float
+// working copy of d.
+struct Ff {
+  float h, l;  // value h + l, |l| <= ulp(h) / 2
+};
+
 __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__restrict__ d,
-                           uint8_t *__restrict__ fz, Grid g, int *__restrict__ anyfrozen,
-                           const double *__restrict__ clk) {
+                           Ff *__restrict__ dff, uint8_t *__restrict__ fz, Grid g,
+                           int *__restrict__ anyfrozen, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
   long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -73,65 +81,132 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
     return;
   int i = g.nd == 1 ? (int)c : (int)(c / g.ny), j = g.nd == 1 ? 0 : (int)(c % g.ny);
   double p = phi[c * ps];
+  uint8_t pos = p > DBL_EPSILON ? 2 : 0;
+  double x = INFINITY;
+  bool frozen = false;
   if (p == 0.0) {
-    d[c] = 0.0;
-    fz[c] = 1;
-    atomicOr(anyfrozen, 1);
-    return;
-  }
-  double ld[2] = {0.0, 0.0};
-  bool borders = false;
-  for (int dim = 0; dim < g.nd; dim++) {
-    double h = dim == 0 ? g.dx : g.dy;
-    for (int dir = -1; dir < 2; dir += 2) {
-      int ii = dim == 0 ? i + dir : i, jj = dim == 1 ? j + dir : j;
-      if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny)
-        continue;
-      double pn = phi[((long)ii * g.ny + jj) * ps];
-      if (mul(p, pn) < 0.0) {
-        borders = true;
-        double dd = dvd(mul(h, p), sub(p, pn));
-        if (ld[dim] == 0.0 || ld[dim] > dd)
-          ld[dim] = dd;
+    x = 0.0;
+    frozen = true;
+  } else {
+    double ld[2] = {0.0, 0.0};
+    bool borders = false;
+    for (int dim = 0; dim < g.nd; dim++) {
+      double h = dim == 0 ? g.dx : g.dy;
+      for (int dir = -1; dir < 2; dir += 2) {
+        int ii = dim == 0 ? i + dir : i, jj = dim == 1 ? j + dir : j;
+        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny)
+          continue;
+        double pn = phi[((long)ii * g.ny + jj) * ps];
+        if (mul(p, pn) < 0.0) {
+          borders = true;
+          double dd = dvd(mul(h, p), sub(p, pn));
+          if (ld[dim] == 0.0 || ld[dim] > dd)
+            ld[dim] = dd;
+        }
       }
     }
-  }
-  if (borders) {
-    double m = DBL_MAX;
-    for (int dim = 0; dim < g.nd; dim++) {
-      double t = fabs(ld[dim]);
-      if (t > 0.0)
-        m = t < m ? t : m;
+    if (borders) {
+      double m = DBL_MAX;
+      for (int dim = 0; dim < g.nd; dim++) {
+        double t = fabs(ld[dim]);
+        if (t > 0.0)
+          m = t < m ? t : m;
+      }
+      x = p < 0.0 ? -m : m;
+      frozen = true;
     }
-    d[c] = p < 0.0 ? -m : m;
-    fz[c] = 1;
-    atomicOr(anyfrozen, 1);
-  } else {
-    d[c] = INFINITY;
-    fz[c] = 0;
   }
+  d[c] = x;
+  float xh = (float)x;
+  dff[c] = Ff{xh, frozen ? (float)(x - (double)xh) : 0.0f};
+  fz[c] = (frozen ? 1 : 0) | pos;
+  if (frozen)
+    atomicOr(anyfrozen, 1);
 }
 
-// The marcher's point update (updatePointOrderOne + solveQuadratic,
-// distance_marcher.cpp:5-28,72-88) for the axes in `use`: the root of
-// sum_k (x - v_k)^2 / h_k^2 = 1 chosen by the sign of phi, 0 without a real
-// root.  idx2 = 1 / h^2.
-GPR_D double fmm_quad(const double v[2], const bool use[2], const double idx2[2], int nd,
-                      double phi) {
-  double a = 0.0, b = 0.0, c = 0.0;
-  for (int dim = 0; dim < nd; dim++)
-    if (use[dim]) {
-      a = add(a, idx2[dim]);
-      b = sub(b, mul(mul(idx2[dim], 2.0), v[dim]));
-      c = add(c, mul(idx2[dim], mul(v[dim], v[dim])));
-    }
-  c = sub(c, 1.0);
-  double det = sub(mul(b, b), mul(mul(4.0, a), c));
-  if (!(det > 0.0))
-    return 0.0;
-  double sq = __dsqrt_rn(det);
-  // (x / 2.0) is exact, as is (x * 0.5)
-  return dvd(mul(phi > DBL_EPSILON ? add(-b, sq) : sub(-b, sq), 0.5), a);
+// ---- double-float arithmetic (Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971; Knuth TAOCP
+// vol. 2, 4.2.2): a value is an unevaluated sum of two floats, about 48
+// significant bits, on the FP32 pipe.  The _rn intrinsics keep the compiler
+// from contracting the error-free transformations.
+GPR_D Ff ff_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return Ff{s, e};
+}
+GPR_D Ff ff_fast_two_sum(float a, float b) {  // |a| >= |b|
+  float s = __fadd_rn(a, b);
+  return Ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+GPR_D Ff ff_add(Ff a, Ff b) {
+  Ff s = ff_two_sum(a.h, b.h), t = ff_two_sum(a.l, b.l);
+  s = ff_fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return ff_fast_two_sum(s.h, __fadd_rn(s.l, t.l));
+}
+GPR_D Ff ff_neg(Ff a) { return Ff{-a.h, -a.l}; }
+GPR_D Ff ff_sub(Ff a, Ff b) { return ff_add(a, ff_neg(b)); }
+GPR_D Ff ff_mul(Ff a, Ff b) {
+  float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return ff_fast_two_sum(p, e);
+}
+GPR_D Ff ff_sqrt(Ff a) {  // a > 0
+  float s = __fsqrt_rn(a.h);
+  float p = __fmul_rn(s, s);
+  float pe = __fmaf_rn(s, s, -p);
+  float r = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(a.h, p), pe), a.l), __fmul_rn(2.0f, s));
+  return ff_fast_two_sum(s, r);
+}
+GPR_D bool ff_lt(Ff a, Ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+GPR_D Ff ff_abs(Ff a) { return (a.h < 0.0f || (a.h == 0.0f && a.l < 0.0f)) ? ff_neg(a) : a; }
+GPR_D bool ff_eq(Ff a, Ff b) { return a.h == b.h && a.l == b.l; }
+GPR_D bool ff_inf(Ff a) { return isinf(a.h); }
+
+inline Ff ff_of(double x) {
+  float h = (float)x;
+  return Ff{h, (float)(x - (double)h)};
+}
+
+// Grid constants of the update: spacings, and for the two-axis root
+// x = al u + be w +- sqrt(ga - ab (u - w)^2) with ix = 1/dx^2, iy = 1/dy^2,
+// al = ix / (ix + iy), be = iy / (ix + iy), ga = 1 / (ix + iy), ab = al be.
+// That is the root of the marcher's quadratic (distance_marcher.cpp:5-28)
+// written without its cancellation (b^2 - 4ac loses ~17 bits there).
+struct FmmConst {
+  Ff h[2], al, be, ga, ab;
+};
+
+inline FmmConst fmm_const(double dx, double dy) {
+  FmmConst K;
+  double ix = 1.0 / dx / dx, iy = 1.0 / dy / dy, S = ix + iy;
+  K.h[0] = ff_of(dx);
+  K.h[1] = ff_of(dy);
+  K.al = ff_of(ix / S);
+  K.be = ff_of(iy / S);
+  K.ga = ff_of(1.0 / S);
+  K.ab = ff_of(ix / S * (iy / S));
+  return K;
+}
+
+// Root of the marcher's quadratic for the entered axes (use), positive
+// root where pos; false without a real root.
+GPR_D bool fmm_root(const Ff v[2], const bool use[2], const FmmConst &K, bool pos, Ff &x) {
+  if (use[0] && use[1]) {
+    Ff df = ff_sub(v[0], v[1]);
+    Ff D = ff_sub(K.ga, ff_mul(K.ab, ff_mul(df, df)));
+    if (!(D.h > 0.0f))
+      return false;
+    Ff sq = ff_sqrt(D);
+    Ff m = ff_add(ff_mul(K.al, v[0]), ff_mul(K.be, v[1]));
+    x = pos ? ff_add(m, sq) : ff_sub(m, sq);
+    return true;
+  }
+  int k = use[0] ? 0 : 1;
+  x = pos ? ff_add(v[k], K.h[k]) : ff_sub(v[k], K.h[k]);
+  return true;
 }
 
 // Update of one unfrozen point from its neighbours' current values
@@ -146,47 +221,51 @@ GPR_D double fmm_quad(const double v[2], const bool use[2], const double idx2[2]
 // root exceeds its |d| in exact arithmetic); where rounding says otherwise
 // (a noise-level tie) it is left out, so that no two points feed each other
 // and the iteration cannot cycle.  Returns `old` when nothing is known.
-GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], double phi,
-                        const double idx2[2], int nd, double old) {
-  double v[2] = {0.0, 0.0}, cv[2] = {0.0, 0.0}, ck[2] = {INFINITY, INFINITY};
+GPR_D Ff fmm_update(const Ff nb[2][2], const bool band[2][2], bool pos, const FmmConst &K,
+                    int nd, Ff old) {
+  const Ff INF = Ff{INFINITY, 0.0f};
+  Ff v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
   bool use[2] = {false, false};
   for (int dim = 0; dim < nd; dim++)
     for (int s = 0; s < 2; s++) {
-      double x = nb[dim][s];
+      Ff x = nb[dim][s], ax = ff_abs(x);
       if (band[dim][s]) {
-        if (!use[dim] || fabs(x) < fabs(v[dim])) {
+        if (!use[dim] || ff_lt(ax, ff_abs(v[dim]))) {
           v[dim] = x;
           use[dim] = true;
         }
-      } else if (fabs(x) < ck[dim]) {
-        ck[dim] = fabs(x);
+      } else if (ff_lt(ax, ck[dim])) {
+        ck[dim] = ax;
         cv[dim] = x;
       }
     }
-  double t = INFINITY;
-  if (use[0] || use[1])
-    t = fmm_quad(v, use, idx2, nd, phi);
-  bool done[2] = {!(ck[0] < INFINITY), nd < 2 || !(ck[1] < INFINITY)};
+  Ff t = INF;
+  if (use[0] || use[1]) {
+    Ff r;
+    if (fmm_root(v, use, K, pos, r))
+      t = r;
+  }
+  bool done[2] = {ff_inf(ck[0]), nd < 2 || ff_inf(ck[1])};
   while (!done[0] || !done[1]) {
-    int a = done[0] ? 1 : (done[1] ? 0 : (ck[1] < ck[0] ? 1 : 0));
-    double key = ck[a];
-    if (!(key < fabs(t)))
+    int a = done[0] ? 1 : (done[1] ? 0 : (ff_lt(ck[1], ck[0]) ? 1 : 0));
+    Ff key = ck[a];
+    if (!ff_lt(key, ff_abs(t)))
       break;
-    bool both = !done[1 - a] && ck[1 - a] == key;
-    double sv0 = v[0], sv1 = v[1];
+    bool both = !done[1 - a] && ff_eq(ck[1 - a], key);
+    Ff sv0 = v[0], sv1 = v[1];
     bool su0 = use[0], su1 = use[1];
     for (int q = 0; q < 2; q++) {
       int dim = q == 0 ? a : 1 - a;
       if (q == 1 && !both)
         break;
-      if (!use[dim] || fabs(cv[dim]) < fabs(v[dim])) {
+      if (!use[dim] || ff_lt(ff_abs(cv[dim]), ff_abs(v[dim]))) {
         v[dim] = cv[dim];
         use[dim] = true;
       }
       done[dim] = true;
     }
-    double t2 = fmm_quad(v, use, idx2, nd, phi);
-    if (t2 == 0.0 || !(fabs(t2) > key)) {
+    Ff t2;
+    if (!fmm_root(v, use, K, pos, t2) || !ff_lt(key, ff_abs(t2))) {
       v[0] = sv0;
       v[1] = sv1;
       use[0] = su0;
@@ -195,7 +274,7 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], double phi
     }
     t = t2;
   }
-  return fabs(t) < INFINITY ? t : old;
+  return ff_inf(t) ? old : t;
 }
 
 // One round of tiled Jacobi sweeps.  Each block loads its tile and a
@@ -205,13 +284,14 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], double phi
 // change.  Only a point next to a point that changed in the previous sweep
 // can change (or, in a round's first sweep, next to a halo point that
 // changed at all in the previous round), and each sweep gathers those into
-// a list first, so that whole warps run the FP64 updates (a warp costs the
-// FP64 pipe the same with one lane as with 32).  A tile runs only if it or
-// a neighbouring tile changed in the previous round (tflag[round][tile]);
-// flags[round] records whether anything changed, and a round after a round
-// without change returns at once.  2D tiles are 32 x 32 cells, 1D tiles
-// 1024; FMM_THREADS threads own
-// 1024 / FMM_THREADS cells each.
+// a list first, so that whole warps run the updates.  A tile runs only if
+// it or a neighbouring tile changed in the previous round
+// (tflag[round][tile]); flags[round] records whether anything changed, and a
+// round after a round without change returns at once.  The sweeps run in
+// double-float arithmetic: GB300's FP64 pipe issues one warp instruction
+// per 64 cycles per SM partition, the FP32 pipe one per cycle, and the
+// sweeps make ~30 updates per cell.  2D tiles are 32 x 32 cells, 1D tiles
+// 1024; FMM_THREADS threads own 1024 / FMM_THREADS cells each.
 constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
 // sweeps per round: four tile diameters
 template <int ND> struct FmmK {
@@ -220,9 +300,8 @@ template <int ND> struct FmmK {
 
 template <int ND>
 __global__ void __launch_bounds__(FMM_THREADS, 4)
-    k_fmm_round(double *__restrict__ d, const double *__restrict__ phi, long ps,
-                const uint8_t *__restrict__ fz, int *__restrict__ lastg, Grid g, double idx2x,
-                double idx2y, int *__restrict__ flags, int *__restrict__ tflag, int round,
+    k_fmm_round(Ff *__restrict__ dff, const uint8_t *__restrict__ fz, int *__restrict__ lastg,
+                Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
                 int mono, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
@@ -243,8 +322,8 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
     if (!run)
       return;
   }
-  __shared__ double sd[SX * SY];
-  __shared__ double nvs[NT];
+  __shared__ Ff sd[SX * SY];
+  __shared__ Ff nvs[NT];
   __shared__ uint8_t sf[SX * SY];
   __shared__ int last[SX * SY];  // global sweep of the last change
   __shared__ int16_t list[NT];
@@ -254,12 +333,12 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
   for (int e = threadIdx.x; e < SX * SY; e += FMM_THREADS) {
     int a = ND == 2 ? e / SY : e, b = ND == 2 ? e % SY : 0;
     int ii = i0 + a - 1, jj = ND == 2 ? j0 + b - 1 : 0;
-    double x = INFINITY;
+    Ff x = Ff{INFINITY, 0.0f};
     uint8_t f = 0;
     int lg = -2;
     if (ii >= 0 && ii < g.nx && jj >= 0 && jj < g.ny) {
       long c = (long)ii * g.ny + jj;
-      x = d[c];
+      x = dff[c];
       f = fz[c];
       lg = lastg[c];
     }
@@ -284,17 +363,15 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
     int a = ND == 2 ? m / SY : m, b = ND == 2 ? m % SY : 1;
     return a == 0 || a == SX - 1 || (ND == 2 && (b == 0 || b == SY - 1));
   };
+  __syncthreads();
   bool act[PER];
   for (int k = 0; k < PER; k++) {
     int l = threadIdx.x + k * FMM_THREADS;
-    act[k] = inside_of(l) && !fz[cell_of(l)];
+    act[k] = inside_of(l) && !(sf[smem_of(l)] & 1);
   }
-  const double idx2[2] = {idx2x, idx2y};
   const int o0 = ND == 2 ? SY : 1;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int gs0 = round * FMM_K;
-  bool wrote = false;
-  __syncthreads();
   for (int it = 0; it < FMM_K; it++) {
     const int gs = gs0 + it;
     // 1. gather the points that can move this sweep
@@ -339,32 +416,31 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
     // 2. update them (Jacobi: read the neighbours, write after a barrier)
     const int n = total;
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
-      int l = list[q], m = smem_of(l);
-      double nb[2][2];
+      int m = smem_of(list[q]);
+      Ff nb[2][2];
       bool bd[2][2];
       nb[0][0] = sd[m - o0];
       nb[0][1] = sd[m + o0];
-      bd[0][0] = sf[m - o0];
-      bd[0][1] = sf[m + o0];
+      bd[0][0] = sf[m - o0] & 1;
+      bd[0][1] = sf[m + o0] & 1;
       if (ND == 2) {
         nb[1][0] = sd[m - 1];
         nb[1][1] = sd[m + 1];
-        bd[1][0] = sf[m - 1];
-        bd[1][1] = sf[m + 1];
+        bd[1][0] = sf[m - 1] & 1;
+        bd[1][1] = sf[m + 1] & 1;
       } else {
-        nb[1][0] = nb[1][1] = INFINITY;
+        nb[1][0] = nb[1][1] = Ff{INFINITY, 0.0f};
         bd[1][0] = bd[1][1] = false;
       }
-      nvs[q] = fmm_update(nb, bd, phi[cell_of(l) * ps], idx2, ND, sd[m]);
+      nvs[q] = fmm_update(nb, bd, (sf[m] & 2) != 0, K, ND, sd[m]);
     }
     __syncthreads();
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
       int m = smem_of(list[q]);
-      double old = sd[m], nv = nvs[q];
+      Ff old = sd[m], nv = nvs[q];
       // from the second half of the round budget on, only a smaller |d| is
-      // taken, which guarantees termination (the marcher's quadratic loses
-      // ~1e-13 to cancellation)
-      if (mono ? fabs(nv) < fabs(old) : nv != old) {
+      // taken, which guarantees termination
+      if (mono ? ff_lt(ff_abs(nv), ff_abs(old)) : !ff_eq(nv, old)) {
         sd[m] = nv;
         last[m] = gs;
         any[it & 1] = 1;
@@ -374,12 +450,13 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
     if (!any[it & 1])
       break;
   }
+  bool wrote = false;
   for (int k = 0; k < PER; k++) {
     int l = threadIdx.x + k * FMM_THREADS;
     int m = smem_of(l);
     if (act[k] && last[m] >= gs0) {
       long c = cell_of(l);
-      d[c] = sd[m];
+      dff[c] = sd[m];
       lastg[c] = last[m];
       wrote = true;
     }
@@ -393,10 +470,12 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
 }
 
 // Final values (base_marcher.cpp:103-106, 190-196): zeros when nothing
-// froze, DBL_MAX where the march never arrived; the distance also replaces
-// the level set in u (renormalize_levelsets, multi/functions.cpp:56-64).
+// froze, DBL_MAX where the march never arrived; band points keep their FP64
+// values; the distance also replaces the level set in u
+// (renormalize_levelsets, multi/functions.cpp:56-64).
 template <int V>
-__global__ void k_fmm_finish(double *__restrict__ d, double *__restrict__ u, long ncell,
+__global__ void k_fmm_finish(double *__restrict__ d, const Ff *__restrict__ dff,
+                             const uint8_t *__restrict__ fz, double *__restrict__ u, long ncell,
                              const int *__restrict__ anyfrozen, const int *__restrict__ flags,
                              int last, int *__restrict__ err, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
@@ -407,10 +486,12 @@ __global__ void k_fmm_finish(double *__restrict__ d, double *__restrict__ u, lon
   if (c >= ncell)
     return;
   double x = d[c];
+  if (!(fz[c] & 1)) {
+    Ff f = dff[c];
+    x = isinf(f.h) ? DBL_MAX : (double)f.h + (double)f.l;
+  }
   if (!*anyfrozen)
     x = 0.0;
-  else if (isinf(x))
-    x = DBL_MAX;
   d[c] = x;
   if (u)
     u[c * V + V - 1] = x;
