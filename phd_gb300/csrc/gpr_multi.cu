@@ -157,13 +157,20 @@ bool grid_ok(const int32_t *nX, int nd) {
   return true;
 }
 
-// Round budget: information crosses at least one tile per round; twice the
-// tile count along the half-perimeter, the second half with monotone
-// updates.
+// Sweeps per re-distancing round (a tile's sweeps between halo exchanges):
+// eight tile widths; 32 was slower (25.7 against 23.4 ms per 800 x 400
+// shock-bubble step), 1024 no faster.
+constexpr int kFmmSweeps = 256;
+
+// Round budget: information crosses at least one tile per round, and the
+// global Jacobi needs about as many sweeps as the longest marching path in
+// cells (678 at 800 x 400); twice the larger of the two, the second half
+// with monotone updates.
 int fmm_rounds(const Grid &g) {
-  if (g.nd == 1)
-    return 2 * ((g.nx + FMM_T1 - 1) / FMM_T1) + 4;
-  return 2 * ((g.nx + FMM_T2 - 1) / FMM_T2 + (g.ny + FMM_T2 - 1) / FMM_T2) + 4;
+  int tiles = g.nd == 1 ? (g.nx + FMM_T1 - 1) / FMM_T1
+                        : (g.nx + FMM_T2 - 1) / FMM_T2 + (g.ny + FMM_T2 - 1) / FMM_T2;
+  int sweeps = (g.nx + (g.nd == 2 ? g.ny : 0) + kFmmSweeps - 1) / kFmmSweeps;
+  return 2 * (tiles > sweeps ? tiles : sweeps) + 8;
 }
 
 // Scratch of one fill (offsets in doubles, 256-byte aligned pieces).
@@ -227,12 +234,12 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)
       k_fmm_round<2><<<nb, FMM_THREADS, 0, st>>>(dff, fz, lastg, g, K, flags, tflag, r,
-                                                 r >= R / 2, clk);
+                                                 kFmmSweeps, r >= R / 2, clk);
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)
       k_fmm_round<1><<<nb, FMM_THREADS, 0, st>>>(dff, fz, lastg, g, K, flags, tflag, r,
-                                                 r >= R / 2, clk);
+                                                 kFmmSweeps, r >= R / 2, clk);
   }
   k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, dff, fz, u, g.ncell, cnt, flags,
                                                           R - 1, err, clk);

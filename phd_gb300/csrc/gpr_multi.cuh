@@ -278,9 +278,9 @@ GPR_D Ff fmm_update(const Ff nb[2][2], const bool band[2][2], bool pos, const Fm
 }
 
 // One round of tiled Jacobi sweeps.  Each block loads its tile and a
-// one-cell halo into shared memory and runs up to K sweeps of the causal
+// one-cell halo into shared memory and runs up to FMM_K sweeps of the causal
 // update against that halo, then writes back.  Sweeps are numbered globally
-// (round * K + local sweep); lastg[c] holds the sweep of cell c's last
+// (round * FMM_K + local sweep); lastg[c] holds the sweep of cell c's last
 // change.  Only a point next to a point that changed in the previous sweep
 // can change (or, in a round's first sweep, next to a halo point that
 // changed at all in the previous round), and each sweep gathers those into
@@ -293,16 +293,12 @@ GPR_D Ff fmm_update(const Ff nb[2][2], const bool band[2][2], bool pos, const Fm
 // sweeps make ~30 updates per cell.  2D tiles are 32 x 32 cells, 1D tiles
 // 1024; FMM_THREADS threads own 1024 / FMM_THREADS cells each.
 constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
-// sweeps per round: four tile diameters
-template <int ND> struct FmmK {
-  static constexpr int K = ND == 2 ? 4 * 2 * FMM_T2 : 4 * FMM_T1;
-};
 
 template <int ND>
 __global__ void __launch_bounds__(FMM_THREADS, 4)
     k_fmm_round(Ff *__restrict__ dff, const uint8_t *__restrict__ fz, int *__restrict__ lastg,
                 Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
-                int mono, const double *__restrict__ clk) {
+                int FMM_K, int mono, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
   if (round > 0 && flags[round - 1] == 0)
@@ -310,7 +306,6 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
   constexpr int TX = ND == 2 ? FMM_T2 : FMM_T1, TY = ND == 2 ? FMM_T2 : 1;
   constexpr int SX = TX + 2, SY = ND == 2 ? TY + 2 : 1;
   constexpr int NT = TX * TY, PER = NT / FMM_THREADS, NW = FMM_THREADS / 32;
-  constexpr int FMM_K = FmmK<ND>::K;
   const int ntx0 = (g.nx + TX - 1) / TX, nty0 = ND == 2 ? (g.ny + TY - 1) / TY : 1;
   const int ntiles = ntx0 * nty0;
   const int t = blockIdx.x;
