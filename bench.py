@@ -41,6 +41,11 @@ UNIT = "Mcell-updates/s"
 # reference's own formulation needs ~2x more (profiles/opcount_tgv512.txt:
 # it recomputes the pressure per call and runs a QR eigen-solve per wave
 # speed); the roofline uses the work this implementation has to do.
+# The reference driver's contortion tolerance (code/python/main.py:21): a
+# step resets every distortion when one cell's normalised distortion exceeds
+# 1 + CONTORTED_TOL.
+CONTORTED_TOL = 1.0
+
 OPS = {
     "predictor_per_cell_iter": 6040.0,    # per predictor cell and Picard iteration
     "face_quadrature_point": 1803.0,      # D_RUS + Bint + extrapolation, per point
@@ -315,7 +320,8 @@ def run_gb300(args):
         _lib.check(lib.gpr_iterate(ctypes.c_void_p(uu.data_ptr()), pn, 2, pd, pb, 0, pp, None,
                                    ctypes.c_void_p(clock.data_ptr()), k,
                                    ctypes.c_void_p(scratch.data_ptr()),
-                                   ctypes.c_void_p(status.data_ptr()), V, sp), "iterate")
+                                   ctypes.c_void_p(status.data_ptr()), CONTORTED_TOL, V, sp),
+                   "iterate")
 
     if args.profile_steps:
         for _ in range(args.profile_steps):
@@ -488,14 +494,15 @@ def shock_tube_bench(torch):
                     ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
                     dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
                     flux, 1, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
-                    ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), V, sp)
+                    ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()),
+                    CONTORTED_TOL, V, sp)
             else:
                 rc = lib.gpr_iterate(
                     ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
                     dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
                     flux, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
                     ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), None,
-                    V, sp)
+                    CONTORTED_TOL, V, sp)
             _lib.check(rc, "iterate")
             return ut, clk
         run()
@@ -751,7 +758,7 @@ def batched_bench(torch, steps=10, plain_steps=2, count=512):
                             dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p),
                             0, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
                             ctypes.c_void_p(clk.data_ptr()), 1, ctypes.c_void_p(scr.data_ptr()),
-                            None, V, sp)
+                            None, float("inf"), V, sp)  # as the batched form: no reset
     for _ in range(3):
         plain_step()
     torch.cuda.synchronize()
@@ -922,7 +929,7 @@ def profile_shock_tube(flux, steps):
         ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
         dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
         ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None, ctypes.c_void_p(clk.data_ptr()),
-        steps, ctypes.c_void_p(scr.data_ptr()), None, 17,
+        steps, ctypes.c_void_p(scr.data_ptr()), None, CONTORTED_TOL, 17,
         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "iterate")
     torch.cuda.synchronize()
     return 0

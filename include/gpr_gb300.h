@@ -190,7 +190,19 @@ long gpr_iterate_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX,
                 const int32_t *bcs, int flux, const gpr_par *par,
                 const uint8_t *mask, double *clock, int nsteps, double *scratch,
-                int32_t *status, int nvar, void *stream);
+                int32_t *status, double contorted_tol, int nvar, void *stream);
+
+/* After each step of gpr_iterate, gpr_iterate_split and gpr_iterate_multi:
+ * contorted + reset_distortion (solvers/utils.cpp:44-85, called by
+ * iterator.cpp:149-150 with the driver's contorted_tol, 1.0 in
+ * code/python/main.py:21): if any cell's normalised distortion has
+ * m0 - 1 > contorted_tol, m0 = |A|_F^2 / (3 |det A|^(2/3)), every cell of a
+ * non-vacuum material gets A = (rho / rho0)^(1/3) I and loses its distortion
+ * energy.  INFINITY disables it.  gpr_reset_contorted does it once on u
+ * (pars[nmat], nmat 1 or 2 with the material from the level set); *flag
+ * (device int32) is set to 1 if it reset. */
+int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gpr_par *pars,
+                        int nmat, int32_t *flag, int nvar, void *stream);
 
 /* One 1D ADER-WENO step that allocates nothing and takes no scratch.  It has
  * no counterpart in the reference.  It is for callers that cannot allocate
@@ -229,8 +241,8 @@ int gpr_split_stepper(double *u, double *ub, const int32_t *nX, int ndim, double
                       const uint8_t *mask, double *scratch, int nvar, void *stream);
 int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
                       const int32_t *bcs, int flux, int half_step, const gpr_par *par,
-                      const uint8_t *mask, double *clock, int nsteps, double *scratch, int nvar,
-                      void *stream);
+                      const uint8_t *mask, double *clock, int nsteps, double *scratch,
+                      double contorted_tol, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batched form: many independent 1D grids (instances) of uneven sizes, each
@@ -376,8 +388,8 @@ int gpr_timestep_multi(const double *grids, const uint8_t *masks, int64_t ncell,
 long gpr_iterate_multi_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
                       const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
-                      double *clock, int nsteps, double *scratch, int32_t *status, int nvar,
-                      void *stream);
+                      double *clock, int nsteps, double *scratch, int32_t *status,
+                      double contorted_tol, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,

@@ -100,6 +100,8 @@ def _load():
                                                     ctypes.c_double, ctypes.c_double,
                                                     ctypes.c_int, P, ctypes.c_int]),
             "or_renorm_multi": (None, [_dp, ctypes.c_long, P]),
+            "or_reset_contorted": (ctypes.c_int, [_dp, ctypes.c_long, ctypes.c_double, P,
+                                                  ctypes.c_int]),
             "or_num_threads": (ctypes.c_int, []),
             "or_set_num_threads": (None, [ctypes.c_int]),
         }
@@ -485,7 +487,8 @@ class Oracle:
         lib.or_renorm_multi(_d(u), u.size // self.V, p)
         return u
 
-    def step_multi(self, u, dt_prev, t, tf, count, MPs, dX, bcs, cfl=0.8, dt=None):
+    def step_multi(self, u, dt_prev, t, tf, count, MPs, dX, bcs, cfl=0.8, dt=None,
+                   contorted_tol=None):
         """One step of the time loop of solvers/iterator.cpp:85-151 with the
         ghost-fluid fill (LSET = 1): fill (with the previous step's dt) ->
         timestep -> per material boundaries + ADER step on its masked cells
@@ -513,20 +516,31 @@ class Oracle:
             grids[mat] = g.reshape(ncell, self.V)
         self.make_u(uf, grids, masks, MPs)
         self.renorm_multi(uf, MPs)
+        if contorted_tol is not None:
+            self.reset_contorted(uf, contorted_tol, MPs)
         return dt
 
-    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None):
+    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None, contorted_tol=None):
         """The two-material time loop (step_multi until tf).  Returns
         (u, steps, t)."""
         u = np.ascontiguousarray(u0, dtype=np.float64).copy()
         t, count, dt = 0.0, 0, 0.0
         while t < tf:
-            dt = self.step_multi(u, dt, t, tf, count, MPs, dX, bcs, cfl)
+            dt = self.step_multi(u, dt, t, tf, count, MPs, dX, bcs, cfl,
+                                 contorted_tol=contorted_tol)
             t += dt
             count += 1
             if max_steps is not None and count >= max_steps:
                 break
         return u, count, t
+
+    def reset_contorted(self, u, tol, MPs):
+        """contorted + reset_distortion (solvers/utils.cpp:44-85) in place;
+        returns True if the distortion was reset."""
+        lib = self._cfg()
+        MPs = MPs if isinstance(MPs, (list, tuple)) else [MPs]
+        arr, p = self._pars(MPs)
+        return bool(lib.or_reset_contorted(_d(u), u.size // self.V, float(tol), p, len(MPs)))
 
     def num_threads(self):
         return self.lib.or_num_threads()
@@ -536,10 +550,11 @@ class Oracle:
 
     # -- a full run ------------------------------------------------------------
     def run(self, u0, MP, tf, dX, bcs, cfl=0.8, flux=0, max_steps=None,
-            split=False, half_step=True):
+            split=False, half_step=True, contorted_tol=None):
         """Time loop of solvers/iterator.cpp:179-264 for one material
-        (boundaries -> timestep -> stepper -> renorm), returning the final
-        state and the number of steps."""
+        (boundaries -> timestep -> stepper -> renorm [-> contortion reset if
+        contorted_tol is given]), returning the final state and the number
+        of steps."""
         shape = u0.shape
         nX = np.array(shape[:-1], dtype=np.int32)
         u = np.ascontiguousarray(u0, dtype=np.float64).ravel().copy()
@@ -554,6 +569,8 @@ class Oracle:
             else:
                 self.ader_stepper(u, ub, nX, dt, dX, MP, flux=flux)
             self.renorm_distortion(u, MP)
+            if contorted_tol is not None:
+                self.reset_contorted(u, contorted_tol, [MP])
             t += dt
             count += 1
             if max_steps is not None and count >= max_steps:

@@ -3918,3 +3918,38 @@ void or_renorm_multi(double *u, long ncell, const gpr_par *MPs) {
     }
   }
 }
+
+/* contorted (solvers/utils.cpp:66-85): a cell is contorted when its
+ * normalised distortion has m0 - 1 > tol, m0 the mean of s_i^2 / det^(2/3)
+ * over the singular values s_i of A, i.e. |A|_F^2 / (3 |det A|^(2/3));
+ * then reset_distortion (:44-64) gives every cell of a non-vacuum material
+ * A = (rho / rho0)^(1/3) I and removes its distortion energy rho E_2A.
+ * Returns 1 if it reset. */
+int or_reset_contorted(double *u, long ncell, double tol, const gpr_par *MPs, int nmat) {
+  int hit = 0;
+  for (long c = 0; c < ncell && !hit; c++) {
+    const double *A = u + c * V + 5;
+    double f2 = 0;
+    for (int k = 0; k < 9; k++)
+      f2 += A[k] * A[k];
+    double d13 = cbrt(fabs(det3(A)));
+    if (f2 / (3 * d13 * d13) - 1 > tol)
+      hit = 1;
+  }
+  if (!hit)
+    return 0;
+  for (long c = 0; c < ncell; c++) {
+    double *Q = u + c * V;
+    int mi = LSET ? ls_mat(Q) : 0;
+    const gpr_par *P = MPs + (mi < nmat ? mi : 0);
+    if (P->EOS <= -1)
+      continue;
+    double r = Q[0];
+    double cc = cbrt(r / P->rho0);
+    Q[1] -= r * E_2A(r, Q + 5, P);
+    for (int k = 0; k < 9; k++)
+      Q[5 + k] = 0.0;
+    Q[5] = Q[9] = Q[13] = cc;
+  }
+  return 1;
+}

@@ -63,6 +63,15 @@ static void renorm_single(Vecr u, Par &MP) {
   renorm_distortion(u, MPs);
 }
 
+static bool vcontorted(Vecr u, double tol) { return contorted(u, tol); }
+
+static void reset_single(Vecr u, Par &MP) {
+  std::vector<Par> MPs(1, MP);
+  reset_distortion(u, MPs);
+}
+
+static void reset_multi(Vecr u, std::vector<Par> MPs) { reset_distortion(u, MPs); }
+
 static py::list iterator_single(Vecr u, double tf, iVecr nX, Vecr dX,
                                 double CFL, iVecr bcs, bool SPLIT,
                                 bool HALF_STEP, bool STIFF, int FLUX, Par &MP,
@@ -276,6 +285,9 @@ PYBIND11_MODULE(MODNAME, m) {
   m.def("ode_launcher", &ode_launcher);
   m.def("timestep_single", &timestep_single);
   m.def("renorm_single", &renorm_single);
+  m.def("contorted", &vcontorted);
+  m.def("reset_single", &reset_single);
+  m.def("reset_multi", &reset_multi);
   m.def("iterator_single", &iterator_single);
 
   m.def("flux", &vflux);

@@ -55,10 +55,11 @@ def _iterator(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, 
     if _two_materials(u, MPs):
         if SPLIT or FLUX != 0 or STIFF:
             raise RuntimeError("the ghost-fluid loop runs the ADER scheme with Rusanov flux")
-        return _multi.iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=max_steps)
+        return _multi.iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=max_steps,
+                              contorted_tol=contorted_tol)
     from .driver import iterate
     return iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
-                   max_steps=max_steps)
+                   max_steps=max_steps, contorted_tol=contorted_tol)
 
 
 def _renorm_distortion(u, MPs):
@@ -79,6 +80,7 @@ solvers = SimpleNamespace(
     split_stepper_para=api.split_stepper_para,
     timestep=api.timestep,
     renorm_distortion=_renorm_distortion,
+    reset_contorted=api.reset_contorted,
     make_u=_multi.make_u,
     extended_dimensions=api.extended_dimensions,
     iterator=_iterator,

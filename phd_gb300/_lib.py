@@ -85,13 +85,14 @@ SIGNATURES = {
     "gpr_ader_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_ader_stepper": (_I, [_P, _P, _P, _I, _D, _P, _I, _I, _P, _P, _P, _P, _I, _P]),
     "gpr_iterate_scratch_doubles": (_L, [_P, _I, _I]),
-    "gpr_iterate": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _I, _P]),
+    "gpr_iterate": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _D, _I, _P]),
+    "gpr_reset_contorted": (_I, [_P, _I64, _D, _P, _I, _P, _I, _P]),
     "gpr_ader_stepper_1d_noalloc": (_I, [_P, _P, ctypes.c_int32, _D, _D, _I, _I, _P, _P, _P,
                                          _I, _P]),
     "gpr_midstepper": (_I, [_P, _D, _P, _I, _P, _P, _P, _I, _P]),
     "gpr_split_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_split_stepper": (_I, [_P, _P, _P, _I, _D, _P, _I, _I, _P, _P, _P, _I, _P]),
-    "gpr_iterate_split": (_I, [_P, _P, _I, _P, _P, _I, _I, _P, _P, _P, _I, _P, _I, _P]),
+    "gpr_iterate_split": (_I, [_P, _P, _I, _P, _P, _I, _I, _P, _P, _P, _I, _P, _D, _I, _P]),
     "gpr_batch_scratch_doubles": (_L, [_I, _P, _I]),
     "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
     "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
@@ -116,7 +117,7 @@ SIGNATURES = {
     "gpr_renorm_multi": (_I, [_P, _I64, _P, _I, _I, _P]),
     "gpr_timestep_multi": (_I, [_P, _P, _I64, _P, _I, _D, _D, _D, _I, _P, _I, _P, _P, _I, _P]),
     "gpr_iterate_multi_scratch_doubles": (_L, [_P, _I, _I]),
-    "gpr_iterate_multi": (_I, [_P, _P, _I, _P, _P, _I, _P, _I, _P, _I, _P, _P, _I, _P]),
+    "gpr_iterate_multi": (_I, [_P, _P, _I, _P, _P, _I, _P, _I, _P, _I, _P, _P, _D, _I, _P]),
     "gpr_flux": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),

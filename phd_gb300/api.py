@@ -280,6 +280,25 @@ def renorm_distortion(u, MPs):
     return u
 
 
+def reset_contorted(u, contorted_tol, MPs, flag=None):
+    """solvers/utils.cpp:44-85: contorted(u, tol) and, if so,
+    reset_distortion(u, MPs), in place (two materials: by level set).
+    Returns the device flag (int32, 1 if it reset); no synchronisation."""
+    lib = _lib.load()
+    MPs = MPs if isinstance(MPs, (list, tuple)) else [MPs]
+    V = _guess_nvar(u) if u.dim() == 1 else u.shape[-1]
+    if flag is None:
+        flag = torch.zeros(1, dtype=torch.int32, device=u.device)
+    import ctypes
+    from .params import GprParC
+    arr = (GprParC * len(MPs))(*[MP.to_ctypes() for MP in MPs])
+    _lib.check(lib.gpr_reset_contorted(_dev(u, "u"), u.numel() // V, float(contorted_tol),
+                                       ctypes.cast(arr, ctypes.c_void_p), len(MPs),
+                                       _dev(flag, "flag", torch.int32), V, _stream()),
+               "reset_contorted")
+    return flag
+
+
 def ode_launcher(u, dt, MP):
     """solvers.split.ode_launcher (solvers/split/ode.cpp:5-11)."""
     lib = _lib.load()

@@ -339,8 +339,8 @@ int gpr_split_stepper(double *u, double *ub, const int32_t *nX, int ndim, double
 
 int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
                       const int32_t *bcs, int flux, int half_step, const gpr_par *par,
-                      const uint8_t *mask, double *clock, int nsteps, double *scratch, int nvar,
-                      void *stream) {
+                      const uint8_t *mask, double *clock, int nsteps, double *scratch,
+                      double contorted_tol, int nvar, void *stream) {
   if (!u || !dX || !bcs || !par || !clock || !scratch || nsteps < 0 || !check_grid(nX, ndim))
     return GPR_E_ARG;
   for (int i = 0; i < 2 * ndim; i++)
@@ -350,12 +350,13 @@ int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
     return rc;
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::iterate_split(u, nX, ndim, dX, bcs, P, mask, clock, nsteps, scratch,
-                                  half_step, flux, S(stream)))
+                                  half_step, flux, S(stream), contorted_tol))
 }
 
 int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const int32_t *bcs,
                 int flux, const gpr_par *par, const uint8_t *mask, double *clock, int nsteps,
-                double *scratch, int32_t *status, int nvar, void *stream) {
+                double *scratch, int32_t *status, double contorted_tol, int nvar,
+                void *stream) {
   if (!u || !dX || !bcs || !par || !clock || !scratch || nsteps < 0 || !check_grid(nX, ndim))
     return GPR_E_ARG;
   for (int i = 0; i < 2 * ndim; i++)
@@ -365,7 +366,17 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const 
     return rc;
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::iterate(u, nX, ndim, dX, bcs, P, mask, clock, nsteps, scratch, status,
-                            S(stream), flux))
+                            S(stream), flux, contorted_tol))
+}
+
+int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gpr_par *pars,
+                        int nmat, int32_t *flag, int nvar, void *stream) {
+  if (!u || !pars || !flag || ncell < 1 || nmat < 1 || nmat > 2)
+    return GPR_E_ARG;
+  DevPar P0 = make_devpar(pars[0]), P1 = nmat > 1 ? make_devpar(pars[1]) : P0;
+  DISPATCH(nvar, (O::contortion(u, ncell, contorted_tol, P0, P1, (int *)flag, nullptr,
+                                S(stream)),
+                  cuda_rc()))
 }
 
 }  // extern "C"

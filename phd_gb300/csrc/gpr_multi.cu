@@ -76,6 +76,11 @@ int Ops15::renorm(double *u, long ncell, const DevPar &P, cudaStream_t st) {
   return Ops<L15>::renorm(u, ncell, P, st);
 }
 
+void Ops15::contortion(double *u, long ncell, double tol, const DevPar &P0, const DevPar &P1,
+                         int *flag, const double *dt_dev, cudaStream_t st) {
+  Ops<L15>::contortion(u, ncell, tol, P0, P1, flag, dt_dev, st);
+}
+
 int Ops15::pointwise(int what, const double *Q, const double *X, double *out, double *out2,
                        long count, int d, int flux, const DevPar &P, cudaStream_t st) {
   return Ops<L15>::pointwise(what, Q, X, out, out2, count, d, flux, P, st);
@@ -84,8 +89,8 @@ int Ops15::pointwise(int what, const double *Q, const double *X, double *out, do
 int Ops15::iterate(double *u, const int32_t *nX, int nd, const double *dX,
                      const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
                      int nsteps, double *scratch, int32_t *status, cudaStream_t st,
-                     int flux) {
-  return Ops<L15>::iterate(u, nX, nd, dX, bcs, P, mask, clk, nsteps, scratch, status, st, flux);
+                     int flux, double contorted_tol) {
+  return Ops<L15>::iterate(u, nX, nd, dX, bcs, P, mask, clk, nsteps, scratch, status, st, flux, contorted_tol);
 }
 
 int Ops15::midstep(double *wh, double dt, const double *dt_dev, const double *dX, int nd,
@@ -107,8 +112,8 @@ long Ops15::split_scratch(const int32_t *nX, int nd) {
 int Ops15::iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
                            const int32_t *bcs, const DevPar &P, const uint8_t *mask,
                            double *clk, int nsteps, double *scratch, int half_step, int flux,
-                           cudaStream_t st) {
-  return Ops<L15>::iterate_split(u, nX, nd, dX, bcs, P, mask, clk, nsteps, scratch, half_step, flux, st);
+                           cudaStream_t st, double contorted_tol) {
+  return Ops<L15>::iterate_split(u, nX, nd, dX, bcs, P, mask, clk, nsteps, scratch, half_step, flux, st, contorted_tol);
 }
 
 long Ops15::iterate_scratch(const int32_t *nX, int nd) {
@@ -320,7 +325,7 @@ int fill(double *grids, uint8_t *masks, double *u, const Grid &g, double dt,
 // Scratch of the two-material time loop.
 struct MultiLayout {
   FillLayout f;
-  long o_fill, o_grids, o_masks, o_maskb, o_ub, o_wh, o_qh, o_tmp, o_mx, o_pst, total;
+  long o_fill, o_grids, o_masks, o_maskb, o_ub, o_wh, o_qh, o_tmp, o_mx, o_flag, o_pst, total;
 };
 
 MultiLayout multi_layout(const int32_t *nX, int nd, const Grid &g) {
@@ -341,6 +346,7 @@ MultiLayout multi_layout(const int32_t *nX, int nd, const Grid &g) {
   M.o_qh = cv.take(ncb * NN * ns * V15);
   M.o_tmp = cv.take(w > f ? w : f);
   M.o_mx = cv.take(1);
+  M.o_flag = cv.take(1);
   M.o_pst = cv.take(dbl(ncb * 4));
   M.total = cv.o;
   return M;
@@ -533,12 +539,13 @@ long gpr_iterate_multi_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
 // The two-material loop of solvers/iterator.cpp:85-170 (LSET > 0, ADER
 // scheme): fill -> CFL over the masked cells of both grids -> per material
 // boundaries, extended mask and the masked ADER step -> make_u -> renorm
-// -> clock.  The clock {t, dt, tf, cfl, count} lives on the device; the
-// fill of a step uses the previous step's dt, as the reference does.
+// -> contortion check and reset (solvers/utils.cpp:44-85) -> clock.  The
+// clock {t, dt, tf, cfl, count} lives on the device; the fill of a step uses
+// the previous step's dt, as the reference does.
 int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
                       const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
-                      double *clock, int nsteps, double *scratch, int32_t *status, int nvar,
-                      void *stream) {
+                      double *clock, int nsteps, double *scratch, int32_t *status,
+                      double contorted_tol, int nvar, void *stream) {
   if (!u || !dX || !bcs || !clock || !scratch || !status || nsteps < 0 || !grid_ok(nX, ndim))
     return GPR_E_ARG;
   for (int i = 0; i < 2 * ndim; i++)
@@ -593,6 +600,8 @@ int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
                                                         P[1].EOS, dt_dev);
     k_renorm_multi<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(
         u, g.ncell, P[0].rho0, P[1].rho0, P[0].EOS, P[1].EOS, dt_dev);
+    Ops<L15>::contortion(u, g.ncell, contorted_tol, P[0], P[1], at<int>(scratch, M.o_flag),
+                         dt_dev, st);
     k_clock_advance<<<1, 1, 0, st>>>(clock);
   }
   return cuda_rc();

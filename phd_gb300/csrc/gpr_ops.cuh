@@ -66,6 +66,69 @@ __global__ void k_pointwise(int what, const double *__restrict__ Q, const double
     out[c * V + k] = r[k];
 }
 
+// contorted (solvers/utils.cpp:66-85): raises *flag if a cell's normalised
+// distortion has m0 - 1 > tol, where m0 = |A|_F^2 / (3 |det A|^(2/3)) (the
+// mean over the singular values s_i of s_i^2 / det^(2/3), without the SVD).
+// Skipped when the device clock says the step did not run (dt == 0).
+template <int V>
+__global__ void k_contorted(const double *__restrict__ u, long ncell, double tol,
+                            int *__restrict__ flag, const double *__restrict__ dt_dev) {
+  if (dt_dev && *dt_dev == 0.0)
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  const double *A = u + c * V + 5;
+  double f2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    f2 += A[k] * A[k];
+  double d13 = cbrt(fabs(det3(A)));
+  if (f2 / (3.0 * d13 * d13) - 1.0 > tol)
+    atomicOr(flag, 1);
+}
+
+// reset_distortion (solvers/utils.cpp:44-64) when *flag is set: every cell
+// of a non-vacuum material loses its distortion energy rho E_2A and gets
+// A = (rho / rho0)^(1/3) I.  The material is 0, or that of the level set
+// (functions/vectors.cpp:24-31) with one.
+template <class L>
+__global__ void k_reset_distortion(double *__restrict__ u, long ncell,
+                                   const int *__restrict__ flag, DevPar P0, DevPar P1,
+                                   const double *__restrict__ dt_dev) {
+  constexpr int V = L::V;
+  if (!*flag || (dt_dev && *dt_dev == 0.0))
+    return;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  double *q = u + c * V;
+  int mi = L::LSET > 0 && q[V - 1] >= 0.0 ? 1 : 0;
+  const DevPar &P = mi ? P1 : P0;
+  if (P.EOS <= -1)
+    return;
+  double r = q[0], ir = 1.0 / r;
+  const double *A = q + 5;
+  // E_2A = C_0 / 4 |dev(A A^T)|^2 (energy/eos.cpp, functions/matrices.cpp:16-26)
+  double G00 = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+  double G11 = A[3] * A[3] + A[4] * A[4] + A[5] * A[5];
+  double G22 = A[6] * A[6] + A[7] * A[7] + A[8] * A[8];
+  double G01 = A[0] * A[3] + A[1] * A[4] + A[2] * A[5];
+  double G02 = A[0] * A[6] + A[1] * A[7] + A[2] * A[8];
+  double G12 = A[3] * A[6] + A[4] * A[7] + A[5] * A[8];
+  double t = (G00 + G11 + G22) / 3.0;
+  double dg = (G00 - t) * (G00 - t) + (G11 - t) * (G11 - t) + (G22 - t) * (G22 - t) +
+              2.0 * (G01 * G01 + G02 * G02 + G12 * G12);
+  double Gm = eos_rho(r, ir, P).G;
+  double cs2 = P.beta == 0.0 ? P.b02 : P.b02 * pow(r * P.ir0, P.beta);
+  double C0 = (1.0 - P.beta / Gm) * cs2;
+  q[1] -= r * (C0 / 4.0 * dg);
+  double cc = cbrt(r * P.ir0);
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    q[5 + k] = (k % 4) == 0 ? cc : 0.0;
+}
+
 template <class L> struct Ops {
   static constexpr int V = L::V;
 
@@ -219,6 +282,15 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
+  // contorted + reset_distortion after a step (iterator.cpp:147-150); flag
+  // is device scratch for one int.
+  static void contortion(double *u, long ncell, double tol, const DevPar &P0, const DevPar &P1,
+                         int *flag, const double *dt_dev, cudaStream_t st) {
+    cudaMemsetAsync(flag, 0, sizeof(int), st);
+    k_contorted<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, tol, flag, dt_dev);
+    k_reset_distortion<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, flag, P0, P1, dt_dev);
+  }
+
   static int pointwise(int what, const double *Q, const double *X, double *out, double *out2,
                        long count, int d, int flux, const DevPar &P, cudaStream_t st) {
     k_pointwise<L><<<blocks(count, 64), 64, 0, st>>>(what, Q, X, out, out2, count, d, flux, P,
@@ -232,7 +304,7 @@ template <class L> struct Ops {
   static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
                      const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
                      int nsteps, double *scratch, int32_t *status, cudaStream_t st,
-                     int flux = GPR_FLUX_RUSANOV) {
+                     int flux = GPR_FLUX_RUSANOV, double contorted_tol = INFINITY) {
     long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
@@ -263,6 +335,7 @@ template <class L> struct Ops {
       if (rc)
         return rc;
       k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
+      contortion(u, ncell, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
       k_clock_advance<<<1, 1, 0, st>>>(clk);
     }
     return cuda_rc();
@@ -321,12 +394,12 @@ template <class L> struct Ops {
   static int iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
                            const int32_t *bcs, const DevPar &P, const uint8_t *mask,
                            double *clk, int nsteps, double *scratch, int half_step, int flux,
-                           cudaStream_t st) {
+                           cudaStream_t st, double contorted_tol = INFINITY) {
     long ncell = nd == 1 ? nX[0] : (long)nX[0] * nX[1];
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
     double *ub = scratch;
     double *rest = ub + nub * V;
-    unsigned long long *mx = (unsigned long long *)(scratch + iterate_scratch(nX, nd) - 1);
+    unsigned long long *mx = (unsigned long long *)(scratch + iterate_scratch(nX, nd) - 2);
     double *dt_dev = clk + 1;
     for (int s = 0; s < nsteps; s++) {
       cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
@@ -340,6 +413,7 @@ template <class L> struct Ops {
       if (rc)
         return rc;
       k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
+      contortion(u, ncell, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
       k_clock_advance<<<1, 1, 0, st>>>(clk);
     }
     return cuda_rc();
@@ -350,7 +424,8 @@ template <class L> struct Ops {
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
     long ns = nd == 1 ? NN : NN * NN;
     long w = weno_scratch(nX, nd), f = fv_scratch(nX, nd);
-    return nub * V + ncb * ns * V + ncb * NN * ns * V + (w > f ? w : f) + 1;
+    // + the CFL maximum and the contortion flag
+    return nub * V + ncb * ns * V + ncb * NN * ns * V + (w > f ? w : f) + 2;
   }
 
   // ---- batched form -------------------------------------------------------

@@ -31,12 +31,14 @@ struct Ops15 {
                       double t, double tf, int count, const DevPar &P, double *dt_out,
                       double *scratch, cudaStream_t st);
   static int renorm(double *u, long ncell, const DevPar &P, cudaStream_t st);
+  static void contortion(double *u, long ncell, double tol, const DevPar &P0, const DevPar &P1,
+                         int *flag, const double *dt_dev, cudaStream_t st);
   static int pointwise(int what, const double *Q, const double *X, double *out, double *out2,
                        long count, int d, int flux, const DevPar &P, cudaStream_t st);
   static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
                      const int32_t *bcs, const DevPar &P, const uint8_t *mask, double *clk,
                      int nsteps, double *scratch, int32_t *status, cudaStream_t st,
-                     int flux = GPR_FLUX_RUSANOV);
+                     int flux = GPR_FLUX_RUSANOV, double contorted_tol = INFINITY);
   static int midstep(double *wh, double dt, const double *dt_dev, const double *dX, int nd,
                      const int32_t *nX, const DevPar &P, const uint8_t *mask, cudaStream_t st);
   static int split_stepper(double *u, double *ub, const int32_t *nX, int nd, double dt,
@@ -47,7 +49,7 @@ struct Ops15 {
   static int iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
                            const int32_t *bcs, const DevPar &P, const uint8_t *mask,
                            double *clk, int nsteps, double *scratch, int half_step, int flux,
-                           cudaStream_t st);
+                           cudaStream_t st, double contorted_tol = INFINITY);
   static long iterate_scratch(const int32_t *nX, int nd);
   static BatchLayout batch_layout(int ninst, const int32_t *nx);
   static int batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,

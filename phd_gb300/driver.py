@@ -1,8 +1,8 @@
 """Time loop of the reference's `solvers.iterator` (code/cpp/src/solvers/
 iterator.cpp:179-264) for one material, on the GPU: CFL time step ->
 boundaries -> ADER step (or the split scheme, SPLIT = True) -> distortion
-renormalisation, with the reference's 100-snapshot return convention and NaN
-early exit."""
+renormalisation -> contortion reset (solvers/utils.cpp:44-85), with the
+reference's 100-snapshot return convention and NaN early exit."""
 import numpy as np
 import torch
 
@@ -26,8 +26,10 @@ class Stepper:
         self.mask = torch.ones(ncb, dtype=torch.uint8, device=device)
         self.status = torch.zeros(ncb, dtype=torch.int32, device=device)
         self.dt = torch.empty(1, dtype=torch.float64, device=device)
+        self.flag = torch.zeros(1, dtype=torch.int32, device=device)
 
-    def step(self, u, dt, dX, bcs, MP, flux=0, stiff=False, split=False, half_step=True):
+    def step(self, u, dt, dX, bcs, MP, flux=0, stiff=False, split=False, half_step=True,
+             contorted_tol=None):
         api.boundaries(u, self.ub, self.nX, bcs)
         if split:
             api.split_stepper(u, self.ub, self.nX, dt, dX, half_step, flux, MP, self.mask)
@@ -35,11 +37,13 @@ class Stepper:
             api.ader_stepper(u, self.ub, self.nX, dt, dX, stiff, flux, MP, self.mask,
                              status=self.status)
         api.renorm_distortion(u, [MP])
+        if contorted_tol is not None:
+            api.reset_contorted(u, contorted_tol, [MP], flag=self.flag)
         return u
 
 
 def iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT=False, HALF_STEP=True, STIFF=False,
-            FLUX=0, MPs=None, max_steps=None):
+            FLUX=0, MPs=None, max_steps=None, contorted_tol=1.0):
     MP = MPs[0] if isinstance(MPs, (list, tuple)) else MPs
     nXa = np.asarray(nX, dtype=np.int32)
     V = u.numel() // int(np.prod(nXa))
@@ -52,7 +56,7 @@ def iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT=False, HALF_STEP=True, STIF
         uprev = uf.clone()
         dt = float(api.timestep_device(uf, dX, CFL, t, tf, count, MP, out=st.dt).item())
         st.step(uf, dt, dX, boundaryTypes, MP, flux=FLUX, stiff=STIFF, split=SPLIT,
-                half_step=HALF_STEP)
+                half_step=HALF_STEP, contorted_tol=contorted_tol)
         t += dt
         count += 1
         if t >= (push + 1) / 100.0 * tf:

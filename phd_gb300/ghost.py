@@ -249,7 +249,7 @@ def timestep_device(grids, masks, dX, CFL, t, tf, count, MPs, out=None):
 class MultiIterator:
     """Device buffers of the two-material time loop (gpr_iterate_multi)."""
 
-    def __init__(self, nX, dX, bcs, MPs, cfl, tf, device="cuda"):
+    def __init__(self, nX, dX, bcs, MPs, cfl, tf, device="cuda", contorted_tol=1.0):
         self.lib = _lib.load()
         self.nX, self.pn = _i32(nX)
         self.dX, self.pd = _f64(dX)
@@ -261,21 +261,24 @@ class MultiIterator:
         self.clock = torch.tensor([0.0, 0.0, float(tf), float(cfl), 0.0], dtype=torch.float64,
                                   device=device)
         self.status = torch.zeros(4, dtype=torch.int32, device=device)
+        self.contorted_tol = float(contorted_tol)
 
     def run(self, u, nsteps):
         """Enqueue nsteps steps on u (in place); no host synchronisation."""
         _lib.check(self.lib.gpr_iterate_multi(
             _dev(u, "u"), self.pn, self.nd, self.pd, self.pb, 0, self.pp, 2,
             _dev(self.clock, "clock"), int(nsteps), _dev(self.scr, "s"),
-            _dev(self.status, "status", torch.int32), V, _stream()), "iterate_multi")
+            _dev(self.status, "status", torch.int32), self.contorted_tol, V, _stream()),
+            "iterate_multi")
         return u
 
 
-def iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=None):
+def iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=None, contorted_tol=1.0):
     """GPRpy.solvers.iterator (solvers/iterator.cpp:85-170) with the ghost
     fill (ADER scheme, Rusanov flux): the reference's 100-snapshot list, with
-    the NaN early exit."""
-    it = MultiIterator(nX, dX, boundaryTypes, MPs, CFL, tf, device=u.device)
+    the NaN early exit and the contortion reset."""
+    it = MultiIterator(nX, dX, boundaryTypes, MPs, CFL, tf, device=u.device,
+                       contorted_tol=contorted_tol)
     uf = u.view(-1)
     ret = [None] * 100
     push, count = 0, 0

@@ -1,6 +1,6 @@
 """Generate the golden fixtures under tests/golden/ from the compiled
 reference solver (oracle/_ref, built by `python oracle/build_ref.py v17
-v17n3 v15`).
+v17n3 v15`), one reference variant per process.
 
 Every array in the fixtures is an output of the reference's own C++ code
 (haranjackson/phd, code/cpp/src) on seeded inputs; inputs are stored beside
@@ -207,14 +207,78 @@ def multi(R, name):
     print("wrote", name)
 
 
+def contortion(R, name):
+    """contorted + reset_distortion (solvers/utils.cpp:44-85): random
+    distorted states, and the reference's own time loop (iterator.cpp:85-170
+    with contorted_tol) on a sheared shock tube whose normalised distortion
+    exceeds the tolerance, so that it resets."""
+    rng = np.random.default_rng(SEED + 7)
+    out = {}
+    u, MP, tf, dX, bcs = problems.shock_tube()
+    P = rd.to_ref_par(R, MP)
+    Q = np.stack([rd.random_state(rng, MP, V=17) for _ in range(40)])
+    m0 = []
+    for q in Q:
+        A = q[5:14].reshape(3, 3)
+        sv = np.linalg.svd(A, compute_uv=False)
+        m0.append(np.mean(sv ** 2) / np.prod(sv) ** (2 / 3))
+    out["m0"] = np.array(m0)
+    out["Q"] = Q
+    out["contorted_tol"] = np.array([0.05, 0.2, 10.0])
+    out["contorted"] = np.array([bool(R.contorted(Q.ravel().copy(), t))
+                                 for t in out["contorted_tol"]])
+    qr = Q.ravel().copy()
+    R.reset_single(qr, P)
+    out["reset"] = qr.reshape(Q.shape)
+    out["mp"] = MP.to_array()
+    u0 = sheared(u, MP)
+    ret = R.iterator_single(u0.ravel().copy(), 0.02, np.array([200], np.int32),
+                            np.array(dX), 0.8, np.zeros(2, np.int32), False, False, False, 0,
+                            P, 0.02)
+    out.update(run_u0=u0, run_tf=np.array(0.02), run_tol=np.array(0.02),
+               run_dX=np.array(dX), run_u_end=np.asarray(ret[99]).reshape(u0.shape))
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print("wrote", name)
+
+
+def contortion_multi(R15, name):
+    """reset_distortion with two materials (the material of each cell from
+    its level set) on random distortions."""
+    rng = np.random.default_rng(SEED + 8)
+    u2, MPs, tf2, dX2, bcs2 = problems.shock_bubble(nx=12, ny=6, mu=1e-2)
+    Q2 = u2.reshape(-1, 15).copy()
+    for k in range(Q2.shape[0]):
+        while True:
+            A = np.eye(3) + 0.3 * rng.standard_normal((3, 3))
+            if np.linalg.det(A) > 0.2:
+                break
+        Q2[k, 5:14] = A.ravel()
+    q2 = Q2.ravel().copy()
+    R15.reset_multi(q2, [rd.to_ref_par(R15, m) for m in MPs])
+    np.savez_compressed(os.path.join(HERE, name), Q=Q2, reset=q2.reshape(Q2.shape),
+                        mp=np.stack([m.to_array() for m in MPs]))
+    print("wrote", name)
+
+
 def main():
-    R15 = rd.load("v15")
-    if R15 is not None:
+    # one reference variant per process: the variants' Par types collide in
+    # pybind11's registry
+    variant = sys.argv[1] if len(sys.argv) > 1 else None
+    if variant is None:
+        import subprocess
+        for v in ("v15", "v17"):
+            subprocess.run([sys.executable, os.path.abspath(__file__), v], check=True)
+        return 0
+    if variant == "v15":
+        R15 = rd.load("v15")
         multi(R15, "multi_v15.npz")
+        contortion_multi(R15, "contortion_v15.npz")
+        return 0
     R = rd.load("v17")
     if R is None:
         print("oracle/_ref/GPRref_v17 not built; run oracle/build_ref.py v17")
         return 1
+    contortion(R, "contortion_v17.npz")
     pointwise(R, "pointwise_v17.npz")
 
     # 1D shock tube (200 cells): stages after 20 steps, Rusanov and Osher

@@ -148,3 +148,25 @@ def test_predictor_newton_fallback_on_stiff_cell(O):
     assert (st < -1000).any(), "expected Picard to fail on this stiff case"
     assert (st != -1).all() and (st != -2).all()
     assert np.isfinite(qh).all()
+
+
+def test_contortion_reset():
+    """contorted + reset_distortion (solvers/utils.cpp:44-85) against the
+    reference, on random states, in the reference's own time loop with a
+    tolerance that triggers a reset, and with two materials."""
+    g = golden("contortion_v17.npz")
+    MP = Par.from_array(g["mp"])
+    O = Oracle(N=2, thermal=True, lset=0)
+    for tol, hit in zip(g["contorted_tol"], g["contorted"]):
+        q = g["Q"].ravel().copy()
+        assert O.reset_contorted(q, float(tol), [MP]) == bool(hit)
+        assert rel_err(q, g["reset"].ravel() if hit else g["Q"].ravel()) < 1e-14
+    u, steps, t = O.run(g["run_u0"], MP, float(g["run_tf"]), list(g["run_dX"]), 0, cfl=0.8,
+                        contorted_tol=float(g["run_tol"]))
+    assert rel_err(u, g["run_u_end"]) < 1e-10
+    g = golden("contortion_v15.npz")
+    O15 = Oracle(N=2, thermal=False, lset=1)
+    MPs = [Par.from_array(a) for a in g["mp"]]
+    q = g["Q"].ravel().copy()
+    assert O15.reset_contorted(q, 0.0, MPs)
+    assert rel_err(q, g["reset"].ravel()) < 1e-14
