@@ -36,9 +36,9 @@ extern "C" {
 #define GPR_E_UNSUPPORTED (-3) /* variant (N, V, flux) not compiled in       */
 #define GPR_E_TOO_LARGE (-4)  /* size beyond a stated fixed maximum          */
 
-/* Flux codes (code/cpp/src/solvers/fv/fluxes.h:7-9).  Rusanov in 1D and 2D;
- * Roe and Osher (a 17x17 eigen-decomposition of the system matrix per face
- * point) on 1D grids, GPR_E_UNSUPPORTED in 2D. */
+/* Flux codes (code/cpp/src/solvers/fv/fluxes.h:7-9).  Rusanov, Roe and
+ * Osher (a V x V eigen-decomposition of the system matrix per face point and
+ * path node) in 1D and 2D. */
 #define GPR_FLUX_RUSANOV 0
 #define GPR_FLUX_ROE 1
 #define GPR_FLUX_OSHER 2

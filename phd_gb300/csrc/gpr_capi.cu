@@ -61,13 +61,11 @@ bool check_grid(const int32_t *nX, int nd) {
   return true;
 }
 
-// Rusanov everywhere; Osher and Roe (17x17 eigen-decompositions per face
-// point) on 1D grids.
+// Rusanov, Roe and Osher in 1D and 2D.
 int check_flux(int flux, int nd) {
+  (void)nd;
   if (flux < GPR_FLUX_RUSANOV || flux > GPR_FLUX_OSHER)
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV && nd != 1)
-    return GPR_E_UNSUPPORTED;
   return GPR_OK;
 }
 
@@ -160,8 +158,6 @@ int gpr_interface_terms(const double *qL, const double *qR, double *out, double 
     return GPR_E_ARG;
   if (flux < GPR_FLUX_RUSANOV || flux > GPR_FLUX_OSHER)
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV && d != 0)
-    return GPR_E_UNSUPPORTED;
   if (count == 0)
     return GPR_OK;
   DevPar P = make_devpar(*par);

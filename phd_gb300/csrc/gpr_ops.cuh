@@ -55,7 +55,7 @@ __global__ void k_pointwise(int what, const double *__restrict__ Q, const double
     if (flux == GPR_FLUX_RUSANOV)
       interface_point<L>(q, qr, d, P, C, r, b);
     else
-      interface_point_eig<L>(q, qr, flux, P, C, r, b);
+      interface_point_eig<L>(q, qr, flux, P, C, r, b, d);
 #pragma unroll
     for (int k = 0; k < V; k++)
       out2[c * V + k] = b[k];
@@ -225,12 +225,17 @@ template <class L> struct Ops {
     int ny = nX[1];
     long nf = (long)(nx + 1) * (ny + 1);
     double *fbx = scratch, *fby = scratch + nf * 2 * V;
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
-                                                             dt_dev, dX[0], dX[1], time_dg, P,
-                                                             C);
-    k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fby, qh, nx, ny, 1, mask, dt,
-                                                             dt_dev, dX[0], dX[1], time_dg, P,
-                                                             C);
+    if (flux == GPR_FLUX_RUSANOV) {
+      k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
+                                                               dt_dev, dX[0], dX[1], time_dg, P,
+                                                               C);
+      k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fby, qh, nx, ny, 1, mask, dt,
+                                                               dt_dev, dX[0], dX[1], time_dg, P,
+                                                               C);
+    } else {
+      faces2d_eig(fbx, qh, nx, ny, 0, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+      faces2d_eig(fby, qh, nx, ny, 1, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+    }
     long nc = (long)nx * ny * NN * NN * NN;
     k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
                                                     dX[0], dX[1], sources, time_dg, P, C,
@@ -257,6 +262,12 @@ template <class L> struct Ops {
     }
     int ny = nX[1];
     long nf = (long)(nx + 1) * (ny + 1);
+    if (flux != GPR_FLUX_RUSANOV) {
+      faces2d_eig(fb, qh, nx, ny, 0, mask, dt, nullptr, dX, time_dg, flux, P, C, st);
+      faces2d_eig(fb + nf * 2 * V, qh, nx, ny, 1, mask, dt, nullptr, dX, time_dg, flux, P, C,
+                  st);
+      return cuda_rc();
+    }
     k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb, qh, nx, ny, 0, mask, dt,
                                                              nullptr, dX[0], dX[1], time_dg,
                                                              P, C);
@@ -264,6 +275,21 @@ template <class L> struct Ops {
                                                              mask, dt, nullptr, dX[0], dX[1],
                                                              time_dg, P, C);
     return cuda_rc();
+  }
+
+  // Osher / Roe faces of one direction on a 2D grid: one block per face,
+  // one warp per eigen-decomposition, the workspaces in dynamic shared memory.
+  static void faces2d_eig(double *fb, const double *qh, int nx, int ny, int dir,
+                          const uint8_t *mask, double dt, const double *dt_dev, const double *dX,
+                          int time_dg, int flux, const DevPar &P, const Consts &C,
+                          cudaStream_t st) {
+    size_t smem = EIG2_WARPS * sizeof(EigWS<V>);
+    // per device and cheap: set on every call
+    cudaFuncSetAttribute(k_faces2d_eigw<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    long nf = (long)(nx + 1) * (ny + 1);
+    k_faces2d_eigw<L><<<(unsigned)nf, 32 * EIG2_WARPS, smem, st>>>(
+        fb, qh, nx, ny, dir, mask, dt, dt_dev, dX[0], dX[1], time_dg, flux, P, C);
   }
 
   static int timestep(const double *u, long ncell, const double *dX, int nd, double cfl,
