@@ -148,7 +148,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm
 
-def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0):
+def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0, flux=0):
     """Oracle (C restatement of the reference solver) on all host cores, on
     an n x strip slice of the TGV (same dx, dy, time step)."""
     from oracle import Oracle
@@ -163,7 +163,7 @@ def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0):
     for _ in range(warmup):
         dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
         ub = O.boundaries(u, nX, [1] * 4)
-        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP)
+        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP, flux=flux)
         O.renorm_distortion(u.reshape(-1), MP)
         count += 1
     t0 = time.perf_counter()
@@ -171,7 +171,7 @@ def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0):
     for _ in range(steps):
         dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
         ub = O.boundaries(u, nX, [1] * 4)
-        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP)
+        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP, flux=flux)
         O.renorm_distortion(u.reshape(-1), MP)
         count += 1
         done += 1
@@ -409,6 +409,12 @@ def run_gb300(args):
             shock = shock_tube_bench(torch)
         except Exception as ex:  # reported, not fatal to the main line
             shock = {"error": str(ex)}
+    flux2d = None
+    if rank == 0 and not args.no_shock_bubble:
+        try:
+            flux2d = flux2d_bench(torch, cpu=not args.no_cpu_baseline)
+        except Exception as ex:  # reported, not fatal to the main line
+            flux2d = {"error": str(ex)}
     bubble = None
     if rank == 0 and not args.no_shock_bubble:
         try:
@@ -447,6 +453,7 @@ def run_gb300(args):
                     "d2h_bytes_per_step": ncell * V * 8},
             "batched": batched,
             "shock_tube": shock,
+            "tgv_roe_osher": flux2d,
             "shock_bubble": bubble,
             "adjoint": adjoint,
             "gpu_launches": 14 * args.steps,
@@ -524,6 +531,55 @@ def shock_tube_bench(torch):
                      "cpu_value": 200 * n / cpu_s / 1e6, "cpu_cores": O.num_threads(),
                      "unit": UNIT, "max_rel_diff_vs_oracle":
                          float(np.max(np.abs(got - ref) / (1.0 + np.abs(ref))))}
+    return out
+
+
+def flux2d_bench(torch, n=512, steps=3, warmup=1, cfl=0.4, cpu=True):
+    """The 512 x 512 Taylor-Green step with the Roe (FLUX = 1, the reference
+    driver's default, code/python/main.py) and Osher (FLUX = 2) dissipation:
+    a V x V eigen-decomposition of the system matrix per face point (and
+    path node), through gpr_iterate; the oracle runs a 512 x 16 strip of the
+    same problem on the host cores."""
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    u0, MP, tf, dX, bcs = G.problems.taylor_green(n=n, cs=10.0, mu=1e-2)
+    V = 17
+    nX = np.array([n, n], np.int32)
+    pn = nX.ctypes.data_as(ctypes.c_void_p)
+    dXa = np.array(dX, np.float64)
+    bc = np.array([1, 1, 1, 1], np.int32)
+    cp = MP.to_ctypes()
+    scr = torch.empty(lib.gpr_iterate_scratch_doubles(pn, 2, V), dtype=torch.float64,
+                      device="cuda")
+    out = {"workload": "tgv2d_%dx%d_v17_cfl%.2g" % (n, n, cfl)}
+    for flux, name in ((1, "roe"), (2, "osher")):
+        u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+        clk = torch.tensor([0.0, 0.0, 1e9, cfl, 0.0], dtype=torch.float64, device="cuda")
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def run(k):
+            _lib.check(lib.gpr_iterate(
+                ctypes.c_void_p(u.data_ptr()), pn, 2, dXa.ctypes.data_as(ctypes.c_void_p),
+                bc.ctypes.data_as(ctypes.c_void_p), flux,
+                ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                ctypes.c_void_p(clk.data_ptr()), k, ctypes.c_void_p(scr.data_ptr()), None,
+                CONTORTED_TOL, V, sp), "iterate")
+        run(warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        r = {"steps": steps, "ms_per_step": ms / steps,
+             "value": n * n * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
+             "finite": bool(torch.isfinite(u).all().item())}
+        if cpu:
+            cb = cpu_baseline(1, 0, n=n, strip=16, cfl=cfl, budget_s=30.0, flux=flux)
+            r["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        out[name] = r
     return out
 
 

@@ -91,3 +91,22 @@ def test_cvec_matches_reference_energy():
             from phd_gb300.params import Cvec
             Q2 = Cvec(Q[0], p, Q[2:5] / Q[0], MP, Q[5:14].reshape(3, 3), Q[14:17] / Q[0])
             assert np.allclose(Q2, Q, rtol=1e-13, atol=1e-13)
+
+
+def test_snapshot_files_in_the_reference_format(tmp_path):
+    """store.py:7-14 / main.py:47-52: leading set snapshots, saved as one
+    array under <problem>_<N>_<cfl>_<SPLIT>_<FLUX>_<time>.npy."""
+    import numpy as np
+    from phd_gb300 import store
+    shape = (5, 3)
+    sol = [np.full(15, float(k)) for k in range(4)] + [None] * 95 + [np.full(15, 9.0)]
+    ul = store.snapshots(sol, shape)
+    assert len(ul) == 4 and ul[3].shape == shape and ul[2][0, 0] == 2.0
+
+    def shock_tube():
+        pass
+    path = store.save_results(ul, shock_tube, 2, 0.8, True, 1, directory=str(tmp_path),
+                              stamp=1700000000)
+    assert os.path.basename(path) == "shock_tube_2_0.8_True_1_1700000000.npy"
+    back = np.load(path)
+    assert back.shape == (4,) + shape and back[1, 0, 0] == 1.0
