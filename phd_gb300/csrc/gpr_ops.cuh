@@ -277,18 +277,14 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
-  // Osher / Roe faces of one direction on a 2D grid: one block per face,
-  // one warp per eigen-decomposition, the workspaces in dynamic shared memory.
+  // Osher / Roe faces of one direction on a 2D grid: one thread per face
+  // quadrature point.
   static void faces2d_eig(double *fb, const double *qh, int nx, int ny, int dir,
                           const uint8_t *mask, double dt, const double *dt_dev, const double *dX,
                           int time_dg, int flux, const DevPar &P, const Consts &C,
                           cudaStream_t st) {
-    size_t smem = EIG2_WARPS * sizeof(EigWS<V>);
-    // per device and cheap: set on every call
-    cudaFuncSetAttribute(k_faces2d_eigw<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
     long nf = (long)(nx + 1) * (ny + 1);
-    k_faces2d_eigw<L><<<(unsigned)nf, 32 * EIG2_WARPS, smem, st>>>(
+    k_faces2d_eigt<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(
         fb, qh, nx, ny, dir, mask, dt, dt_dev, dX[0], dX[1], time_dg, flux, P, C);
   }
 
