@@ -746,7 +746,8 @@ def adjoint_bench(torch, fd_check=True):
              "adjoint_over_forward": bwd / fwd,
              "plain_forward_ms_per_step": fwd_plain / plain.nsteps,
              "adjoint_over_plain_forward": (bwd / nsteps) / (fwd_plain / plain.nsteps),
-             "cell_updates_per_s_forward": nx * ninst * nsteps / (fwd * 1e-3)}
+             "cell_updates_per_s_forward": nx * ninst * nsteps / (fwd * 1e-3),
+             "transposed_iterations_mean": prob.adj_iterations}
         if fd_check and ninst == 1:
             g = prob.theta_grad(fb, th)[0]
             errs = []

@@ -298,7 +298,9 @@ int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx,
  * differentiates dt through the CFL rule (at ties of the CFL maximum the
  * smallest cell index is taken).  ascratch: gpr_adj_scratch_doubles
  * doubles.  info[nb] (int32 per packed predictor cell, zero it first) gets
- * bit 0 set where the transposed predictor iteration did not converge. */
+ * bit 0 set where the transposed predictor iteration did not converge (and
+ * the dense solve that replaces it failed), and bits 8 and up accumulate
+ * the cell's transposed-iteration count over the backward steps. */
 int gpr_adj_num_fields(void);
 int gpr_adj_supported(int ninst, const gpr_par *pars, const int32_t *bcs, int nvar);
 long gpr_adj_tape_doubles(int ninst, const int32_t *nx, int nvar);
@@ -314,6 +316,13 @@ int gpr_adj_backward_step(double *ubar, double *thbar, double *tbar, int frozen_
  * after), dlam [count][K]; K = V + 6. */
 int gpr_adj_point_jacobians(const double *Q, int64_t count, const gpr_par *par, double *JF,
                             double *JS, double *dlam, int nvar, void *stream);
+/* Reverse-mode products at count states (test hook): qb[count][V] =
+ * (dF_x/dq)^T Fb + (dS/dq)^T Sb + lb dlambda_x/dq, thb[count][6] the same
+ * with respect to the six material fields; Fb, Sb [count][V], lb [count].
+ * The backward step uses these products in place of full Jacobians. */
+int gpr_adj_point_vjp(const double *Q, int64_t count, const gpr_par *par, const double *Fb,
+                      const double *Sb, const double *lb, double *qb, double *thb, int nvar,
+                      void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Level-set ghost fluid (GPRpy.multi.*, code/cpp/src/multi/*.cpp, and

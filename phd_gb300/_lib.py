@@ -103,6 +103,7 @@ SIGNATURES = {
     "gpr_adj_forward_step": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _D, _I, _P, _I, _P]),
     "gpr_adj_backward_step": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P]),
     "gpr_adj_point_jacobians": (_I, [_P, _I64, _P, _P, _P, _P, _I, _P]),
+    "gpr_adj_point_vjp": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _I, _P]),
     "gpr_distance_scratch_doubles": (_L, [_P, _I]),
     "gpr_distance": (_I, [_P, _P, _P, _I, _P, _P, _P, _P]),
     "gpr_finite_difference": (_I, [_P, _P, _P, _I, _P, _P]),

@@ -197,9 +197,13 @@ class Problem:
                     self.ninst, self._p(self.nx), self._t(self.scratch), self._t(self.tapes[j]),
                     self._t(self.ascratch), self._t(self.info), self.V, self._stream()),
                     "adj_backward_step")
-        if int(self.info.max().item()) != 0:
+        bad = (self.info & 0xff) != 0
+        if bool(bad.any().item()):
             raise RuntimeError("transposed predictor iteration did not converge in %d cells"
-                               % int((self.info != 0).sum().item()))
+                               % int(bad.sum().item()))
+        # mean transposed-iteration count per predictor cell and step
+        self.adj_iterations = float((self.info >> 8).sum().item()) / max(
+            1, self.nb * self.nsteps)
         return ubar.view(-1, self.V), thbar.view(self.ninst, 6)
 
     def theta_grad(self, fieldbar, theta):

@@ -34,11 +34,12 @@ TapeLayout tape_layout_v(int ninst, const int32_t *nx, int V) {
   return t;
 }
 
-// Backward-step scratch: Jacobian columns at the nodes (F, S) and cell ends
-// (F, lambda), lambda at the ends, cotangents of qh and wh, stencil
-// cotangents, per-cell material-field and dt partial sums.
+// Backward-step scratch: Jacobian columns at the nodes (F, S; written only
+// for the cells of the dense solve), lambda and eigen data at the ends,
+// cotangents of qh and wh, stencil cotangents, per-cell material-field and
+// dt partial sums.
 struct AdjLayout {
-  long o_jn, o_je, o_ev, o_eig, o_dots, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
+  long o_jn, o_ev, o_eig, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
 };
 
 AdjLayout adj_layout_v(int ninst, const int32_t *nx, int V) {
@@ -47,11 +48,9 @@ AdjLayout adj_layout_v(int ninst, const int32_t *nx, int V) {
   Carve cv;
   AdjLayout a;
   a.o_jn = cv.take(b.nb * 4 * K * 2 * V);
-  a.o_je = cv.take(b.nb * 4 * K * (V + 1));
   // lambda and eigen data at the cell ends, then at the CFL argmax states
   a.o_ev = cv.take(b.nb * 4 + ninst);
   a.o_eig = cv.take((b.nb * 4 + ninst) * 17);
-  a.o_dots = cv.take(b.nb * 2 * 4 * K);
   a.o_qb = cv.take(b.nb * 4 * V);
   a.o_wb = cv.take(b.nb * 2 * V);
   a.o_g = cv.take(b.nb * V * 3);
@@ -132,9 +131,8 @@ template <class L> struct Adj {
                             const_cast<double *>(tape + tl.o_clk));
     const double *un = tape + tl.o_un, *qh = tape + tl.o_qh, *up = tape + tl.o_up,
                  *aux = tape + tl.o_aux;
-    double *JN = ascr + al.o_jn, *JE = ascr + al.o_je, *EV = ascr + al.o_ev,
-           *EIG = ascr + al.o_eig, *EVs = EV + b.nb * 4,
-           *EIGs = EIG + b.nb * 4 * Xi<L::THERMAL>::ND, *DOT = ascr + al.o_dots,
+    double *JN = ascr + al.o_jn, *EV = ascr + al.o_ev, *EIG = ascr + al.o_eig,
+           *EVs = EV + b.nb * 4, *EIGs = EIG + b.nb * 4 * Xi<L::THERMAL>::ND,
            *qb = ascr + al.o_qb, *wb = ascr + al.o_wb, *g = ascr + al.o_g,
            *thf = ascr + al.o_thf, *thp = ascr + al.o_thp, *dtf = ascr + al.o_dtf,
            *dtp = ascr + al.o_dtp, *mu = ascr + al.o_mu;
@@ -142,17 +140,13 @@ template <class L> struct Adj {
     k_adj_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(ubar, up, b.nu, B);
     k_adj_eig<L><<<blocks(b.nb * 4 + ninst, 128), 128, 0, st>>>(qh, b.nb, un, aux, EV, EIG, C,
                                                                   B);
-    k_adj_jac_nodes<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, JN, B);
-    k_adj_jac_ends<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, JE, EIG, C, B);
-    k_adj_fv_dots<L><<<blocks(b.nb * 2 * K, 128), 128, 0, st>>>(ubar, qh, JN, JE, EV, b.nb, DOT,
-                                                                 C, B);
-    k_adj_fv<L><<<blocks(b.nb * 2, 128), 128, 0, st>>>(ubar, qh, DOT, EV, un, up, b.nb, qb, thf,
-                                                        dtf, C, B);
-    k_adj_pred_iter<L><<<blocks(b.nb, ADJ_CPB), 32 * ADJ_CPB, 0, st>>>(qh, qb, JN, b.nb, mu,
-                                                                      need, C, B);
+    k_adj_fv<L><<<blocks(b.nb * 2, ADJ_FV_PAIRS), 4 * ADJ_FV_PAIRS, 0, st>>>(
+        ubar, qh, EV, EIG, un, up, b.nb, qb, thf, dtf, C, B);
+    k_adj_pred_iter<L><<<blocks(b.nb * 4, ADJ_IT_T), ADJ_IT_T, 0, st>>>(qh, qb, b.nb, mu, need,
+                                                                         info, C, B);
+    k_adj_jac_nodes<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, need, JN, B);
     k_adj_pred_dense<L><<<(unsigned)b.nb, 128, 0, st>>>(qh, qb, JN, b.nb, need, mu, info, C, B);
-    k_adj_pred_post<L><<<blocks(b.nb * 4, 128), 128, 0, st>>>(qh, mu, JN, b.nb, wb, thp, dtp, C,
-                                                               B);
+    k_adj_pred_post<L><<<blocks(b.nb * 4, 128), 128, 0, st>>>(qh, mu, b.nb, wb, thp, dtp, C, B);
     k_adj_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wb, un, b.nb, g, C, B);
     k_adj_gather<V><<<blocks(b.nu * V, 256), 256, 0, st>>>(ubar, g, b.nu, B);
     k_adj_reduce<L><<<ninst, 128, 0, st>>>(ubar, thbar, tbar, thf, thp, dtf, dtp, un, aux, EVs,
@@ -163,6 +157,13 @@ template <class L> struct Adj {
   static int point(const double *Q, long count, const DevPar &P, double *JF, double *JS,
                    double *dlam, cudaStream_t st) {
     k_adj_point<L><<<blocks(count * K, 128), 128, 0, st>>>(Q, count, JF, JS, dlam, P);
+    return cuda_rc();
+  }
+
+  static int point_vjp(const double *Q, long count, const DevPar &P, const double *Fb,
+                       const double *Sb, const double *lb, double *qb, double *thb,
+                       cudaStream_t st) {
+    k_adj_point_vjp<L><<<blocks(count, 128), 128, 0, st>>>(Q, count, Fb, Sb, lb, qb, thb, P);
     return cuda_rc();
   }
 };
@@ -262,6 +263,20 @@ int gpr_adj_point_jacobians(const double *Q, int64_t count, const gpr_par *par, 
     return GPR_OK;
   DevPar P = make_devpar(*par);
   ADJ_DISPATCH(nvar, A::point(Q, count, P, JF, JS, dlam, S(stream)))
+}
+
+int gpr_adj_point_vjp(const double *Q, int64_t count, const gpr_par *par, const double *Fb,
+                      const double *Sb, const double *lb, double *qb, double *thb, int nvar,
+                      void *stream) {
+  if (!Q || !par || !Fb || !Sb || !lb || !qb || !thb || count < 0)
+    return GPR_E_ARG;
+  const int32_t bc0[2] = {0, 0};
+  if (gpr_adj_supported(1, par, bc0, nvar) != GPR_OK)
+    return GPR_E_UNSUPPORTED;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  ADJ_DISPATCH(nvar, A::point_vjp(Q, count, P, Fb, Sb, lb, qb, thb, S(stream)))
 }
 
 }  // extern "C"

@@ -308,16 +308,7 @@ GPR_D void dxi0(const Dual *q, const DPrim<TH> &s, const DPar &P, Dual (&X)[Xi<T
 // Eigen data of the dominant eigenvalue l2 of X: eig[0] = l2,
 // eig[1 + i m + j] = Y[i][j] with d l2 = sum_ij Y[i][j] dX[i][j],
 // Y = adj(l2 I - X)^T / tr(adj(l2 I - X)).
-template <int m> GPR_D void xi_eigdata(const double (&Xv)[m][m], double *eig) {
-  double Xc[m][m];
-#pragma unroll
-  for (int i = 0; i < m; i++)
-#pragma unroll
-    for (int j = 0; j < m; j++)
-      Xc[i][j] = Xv[i][j];
-  double l2;
-  if (!max_eig_laguerre<m>(Xc, l2))
-    l2 = max_abs_eig<m>(Xc);
+template <int m> GPR_D void xi_eigdata_l2(const double (&Xv)[m][m], double l2, double *eig) {
   double M[m][m], adj[m][m];
 #pragma unroll
   for (int i = 0; i < m; i++)
@@ -336,6 +327,19 @@ template <int m> GPR_D void xi_eigdata(const double (&Xv)[m][m], double *eig) {
 #pragma unroll
     for (int j = 0; j < m; j++)
       eig[1 + i * m + j] = adj[j][i] * iden;
+}
+
+template <int m> GPR_D void xi_eigdata(const double (&Xv)[m][m], double *eig) {
+  double Xc[m][m];
+#pragma unroll
+  for (int i = 0; i < m; i++)
+#pragma unroll
+    for (int j = 0; j < m; j++)
+      Xc[i][j] = Xv[i][j];
+  double l2;
+  if (!max_eig_laguerre<m>(Xc, l2))
+    l2 = max_abs_eig<m>(Xc);
+  xi_eigdata_l2<m>(Xv, l2, eig);
 }
 
 // lambda with its tangent; eig: eigen data of X (computed here when null)
@@ -386,6 +390,403 @@ GPR_D void point_tangent(const double *qp, int k, const DevPar &P, Dual *F, Dual
     dsource<L::THERMAL, V>(q, s, D, S);
   if (lam)
     *lam = dlambda0<L::THERMAL>(q, s, D, eig);
+}
+
+// ---------------------------------------------------------------------------
+// Reverse mode of the point functions: for cotangents Fb (of F_x), Sb (of S)
+// and lb (of lambda_x) at state q,
+//   qb  += (dF/dq)^T Fb + (dS/dq)^T Sb + lb dlambda/dq,
+//   thb += the same with respect to the six material fields,
+// the exact derivative of dprim / dflux0 / dsource / dlambda0 above (same
+// operations, traversed backwards), at ~3 evaluations of the point functions
+// instead of one dual evaluation per column.  HF / HS / HL select the terms;
+// eig: eigen data of the acoustic tensor (xi_eigdata; computed here when
+// null); thb may be null.
+template <class L, bool HF, bool HS, bool HL>
+GPR_D void point_vjp(const double *q, const DevPar &P, const double *Fb, const double *Sb,
+                     double lb, const double *eig, double *qb, double *thb) {
+  constexpr bool TH = L::THERMAL;
+  constexpr int m = Xi<TH>::m;
+  const double *A = q + 5;
+  // ---- primal (dprim)
+  const double r = q[0], ir = 1.0 / r;
+  double v[3], J[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    v[i] = q[2 + i] * ir;
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      J[i] = q[14 + i] * ir;
+  }
+  const double G00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  const double G11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  const double G22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  const double G01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  const double G02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  const double G12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  const double tG = (G00 + G11 + G22) * (1.0 / 3.0);
+  const double Dm[3][3] = {{G00 - tG, G01, G02}, {G01, G11 - tG, G12}, {G02, G12, G22 - tG}};
+  const double devGsq = Dm[0][0] * Dm[0][0] + Dm[1][1] * Dm[1][1] + Dm[2][2] * Dm[2][2] +
+                        2.0 * (G01 * G01 + G02 * G02 + G12 * G12);
+  double AdG[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      AdG[3 * i + j] = A[3 * i] * Dm[0][j] + A[3 * i + 1] * Dm[1][j] + A[3 * i + 2] * Dm[2][j];
+  const double Gm1 = P.gamma - 1.0, irG = ir * P.iG;
+  const double vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const double Jsq = J[0] * J[0] + J[1] * J[1] + J[2] * J[2];
+  double E1 = q[1] * ir - 0.5 * vsq - 0.25 * (P.b02 * devGsq);
+  if (TH)
+    E1 = E1 - 0.5 * (P.calpha2 * Jsq);
+  const double er = P.pINF * ir;
+  const double p = (E1 - er) * (r * Gm1) - P.pINF;
+  const double T = (p + P.pINF) * irG * P.icv;
+  // sigma column 0 (dsigma0)
+  const double sgf = -(r * P.b02);
+  double sgm[3], sg[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    sgm[i] = AdG[i] * A[0] + AdG[3 + i] * A[3] + AdG[6 + i] * A[6];
+    sg[i] = sgf * sgm[i];
+  }
+  // ---- adjoints
+  double rb = 0.0, irb = 0.0, vb[3] = {0.0, 0.0, 0.0}, Jb[3] = {0.0, 0.0, 0.0};
+  double Ab[9], AdGb[9], sgb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    Ab[k] = 0.0;
+    AdGb[k] = 0.0;
+  }
+  double pb = 0.0, Tb = 0.0, Gm1b = 0.0, irGb = 0.0;
+  double b02b = 0.0, ca2b = 0.0, th1cb = 0.0, ikb = 0.0, q1b = 0.0;
+  double q2b[3] = {0.0, 0.0, 0.0}, qJb[3] = {0.0, 0.0, 0.0};
+  if (HL) {
+    // lambda = sqrt(l2) +- v0 (dlambda0), d l2 = sum Y dX
+    double le[1 + m * m];
+    const double *ed = eig;
+    double X0[m][m];
+    if (!ed) {
+      Dual qd[L::V];
+#pragma unroll
+      for (int j = 0; j < L::V; j++)
+        qd[j] = Dual{q[j], 0.0};
+      DPar D = dpar_seed(P, -1);
+      DPrim<TH> s;
+      dprim<TH>(qd, D, s);
+      Dual X[m][m];
+      dxi0<TH>(qd, s, D, X);
+#pragma unroll
+      for (int i = 0; i < m; i++)
+#pragma unroll
+        for (int j = 0; j < m; j++)
+          X0[i][j] = X[i][j].v;
+      xi_eigdata<m>(X0, le);
+      ed = le;
+    }
+    vb[0] += v[0] > 0 ? lb : -lb;
+    const double l2b = 0.5 * lb / sqrt(ed[0]);
+    double Xb[m][m];
+#pragma unroll
+    for (int i = 0; i < m; i++)
+#pragma unroll
+      for (int j = 0; j < m; j++)
+        Xb[i][j] = l2b * ed[1 + i * m + j];
+    // reverse of dxi0
+    double Gd[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      Gd[j] = A[0] * A[j] + A[3] * A[3 + j] + A[6] * A[6 + j];
+    double ret[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        ret[3 * i + j] = (j == 0 ? 2.0 : 1.0) * AdG[3 * i + j] +
+                         (1.0 / 3.0) * (A[3 * i] * Gd[j]) + Gd[0] * A[3 * i + j];
+    const double dsr[3] = {ir * sg[0], ir * sg[1], ir * sg[2]};
+    const double irG2 = irG * irG;
+    const double dnum = Gm1 * (p + P.pINF);
+    const double dedr = -(P.pINF * (ir * ir)) - dnum * irG2;
+    const double rG = r * Gm1;
+    const double c02 = (p * (ir * ir) - dedr) * rG;
+    double bv[3] = {sg[0] - r * dsr[0], sg[1] - r * dsr[1], sg[2] - r * dsr[2]};
+    bv[0] = bv[0] + r * c02;
+    double bb[3] = {0.0, 0.0, 0.0}, dsrb[3] = {0.0, 0.0, 0.0}, retb[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      retb[k] = 0.0;
+    double dnumb = 0.0, irG2b = 0.0;
+    if constexpr (TH) {
+      const double h = P.calpha2 * T * Gm1;
+      const double tp = ir * irG * P.icv;
+      const double hb = Xb[0][m - 1] * ir + Xb[m - 1][m - 1] * tp;
+      irb += Xb[0][m - 1] * h;
+      const double tpb = Xb[m - 1][0] * bv[0] + Xb[m - 1][1] * bv[1] + Xb[m - 1][2] * bv[2] +
+                         Xb[m - 1][m - 1] * h;
+      const double dTrb = Xb[m - 1][0];
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        bb[c] += Xb[m - 1][c] * tp;
+      dnumb -= dTrb * irG2 * P.icv;
+      irG2b -= dTrb * dnum * P.icv;
+      irb += tpb * irG * P.icv;
+      irGb += tpb * ir * P.icv;
+      ca2b += hb * T * Gm1;
+      Tb += hb * P.calpha2 * Gm1;
+      Gm1b += hb * P.calpha2 * T;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double xb = Xb[i][c];
+        const double Mv = ret[i] * A[c] + ret[3 + i] * A[3 + c] + ret[6 + i] * A[6 + c];
+        b02b += xb * Mv;
+        const double f = xb * P.b02;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          retb[3 * k + i] += f * A[3 * k + c];
+          Ab[3 * k + c] += f * ret[3 * k + i];
+        }
+        if (c == 0)
+          dsrb[i] -= xb;
+        if (i == 0) {
+          bb[c] += xb * ir;
+          irb += xb * bv[c];
+        }
+      }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      sgb[c] += bb[c];
+      rb -= bb[c] * dsr[c];
+      dsrb[c] -= bb[c] * r;
+    }
+    rb += bb[0] * c02;
+    const double c02b = bb[0] * r;
+    pb += c02b * (ir * ir) * rG;
+    irb += c02b * p * 2.0 * ir * rG;
+    const double dedrb = -c02b * rG;
+    const double rGb = c02b * (p * (ir * ir) - dedr);
+    rb += rGb * Gm1;
+    Gm1b += rGb * r;
+    irb -= dedrb * 2.0 * P.pINF * ir;
+    dnumb -= dedrb * irG2;
+    irG2b -= dedrb * dnum;
+    Gm1b += dnumb * (p + P.pINF);
+    pb += dnumb * Gm1;
+    irGb += irG2b * 2.0 * irG;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      irb += dsrb[i] * sg[i];
+      sgb[i] += dsrb[i] * ir;
+    }
+    double Gdb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const double g = retb[3 * i + j];
+        AdGb[3 * i + j] += (j == 0 ? 2.0 : 1.0) * g;
+        Ab[3 * i] += g * (1.0 / 3.0) * Gd[j];
+        Gdb[j] += g * (1.0 / 3.0) * A[3 * i];
+        Gdb[0] += g * A[3 * i + j];
+        Ab[3 * i + j] += g * Gd[0];
+      }
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        Ab[3 * k] += Gdb[j] * A[3 * k + j];
+        Ab[3 * k + j] += Gdb[j] * A[3 * k];
+      }
+  }
+  if (HF) {
+    // reverse of dflux0
+    q2b[0] += Fb[0];
+    const double f1 = Fb[1];
+    vb[0] += f1 * (q[1] + p);
+    q1b += f1 * v[0];
+    pb += f1 * v[0];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      sgb[i] -= f1 * v[i];
+      vb[i] -= f1 * sg[i];
+    }
+    if (TH) {
+      ca2b += f1 * T * J[0];
+      Tb += f1 * P.calpha2 * J[0];
+      Jb[0] += f1 * P.calpha2 * T;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double f = Fb[2 + i];
+      vb[0] += f * q[2 + i];
+      q2b[i] += f * v[0];
+      sgb[i] -= f;
+    }
+    pb += Fb[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double f = Fb[5 + 3 * i];
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        Ab[3 * i + j] += f * v[j];
+        vb[j] += f * A[3 * i + j];
+      }
+    }
+    if (TH) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const double f = Fb[14 + i];
+        vb[0] += f * q[14 + i];
+        qJb[i] += f * v[0];
+      }
+      Tb += Fb[14];
+    }
+  }
+  if (HS) {
+    // reverse of dsource
+    const double dA = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                      A[2] * (A[3] * A[7] - A[4] * A[6]);
+    const double cb = cbrt(dA);
+    const double th = dA * cb * cb * P.th1c;
+    const double f = -(P.b02 * th);
+    double fb = 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      AdGb[i] += Sb[5 + i] * f;
+      fb += Sb[5 + i] * AdG[i];
+    }
+    b02b -= fb * th;
+    const double thb_ = -fb * P.b02;
+    th1cb += thb_ * dA * cb * cb;
+    const double dAb = thb_ * P.th1c * (5.0 / 3.0) * cb * cb;
+    Ab[0] += dAb * (A[4] * A[8] - A[5] * A[7]);
+    Ab[1] += dAb * (A[5] * A[6] - A[3] * A[8]);
+    Ab[2] += dAb * (A[3] * A[7] - A[4] * A[6]);
+    Ab[3] += dAb * (A[2] * A[7] - A[1] * A[8]);
+    Ab[4] += dAb * (A[0] * A[8] - A[2] * A[6]);
+    Ab[5] += dAb * (A[1] * A[6] - A[0] * A[7]);
+    Ab[6] += dAb * (A[1] * A[5] - A[2] * A[4]);
+    Ab[7] += dAb * (A[2] * A[3] - A[0] * A[5]);
+    Ab[8] += dAb * (A[0] * A[4] - A[1] * A[3]);
+    if (TH) {
+      const double g = -(P.calpha2 * T * P.ikappa);
+      double gb = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        gb += Sb[14 + i] * J[i];
+        Jb[i] += Sb[14 + i] * g;
+      }
+      ca2b -= gb * T * P.ikappa;
+      Tb -= gb * P.calpha2 * P.ikappa;
+      ikb -= gb * P.calpha2 * T;
+    }
+  }
+  // reverse of dsigma0
+  {
+    const double sgfb = sgb[0] * sgm[0] + sgb[1] * sgm[1] + sgb[2] * sgm[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double f = sgb[i] * sgf;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        AdGb[3 * k + i] += f * A[3 * k];
+        Ab[3 * k] += f * AdG[3 * k + i];
+      }
+    }
+    rb -= sgfb * P.b02;
+    b02b -= sgfb * r;
+  }
+  // reverse of dprim
+  pb += Tb * irG * P.icv;
+  irGb += Tb * (p + P.pINF) * P.icv;
+  const double E1b = pb * (r * Gm1);
+  const double erb = -E1b;
+  rb += pb * (E1 - er) * Gm1;
+  Gm1b += pb * (E1 - er) * r;
+  irb += erb * P.pINF;
+  q1b += E1b * ir;
+  irb += E1b * q[1];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    vb[i] -= E1b * v[i];
+  b02b -= 0.25 * E1b * devGsq;
+  const double devGsqb = -0.25 * E1b * P.b02;
+  if (TH) {
+    ca2b -= 0.5 * E1b * Jsq;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      Jb[i] -= E1b * P.calpha2 * J[i];
+      qJb[i] += Jb[i] * ir;
+      irb += Jb[i] * q[14 + i];
+    }
+  }
+  irb += irGb * P.iG;
+  const double iGb = irGb * ir;
+  // AdG = A Dm
+  double Dmb[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        s += AdGb[3 * i + j] * A[3 * i + k];
+      Dmb[k][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      Ab[3 * i + k] += AdGb[3 * i] * Dm[k][0] + AdGb[3 * i + 1] * Dm[k][1] +
+                       AdGb[3 * i + 2] * Dm[k][2];
+  double D00b = Dmb[0][0] + devGsqb * 2.0 * Dm[0][0];
+  double D11b = Dmb[1][1] + devGsqb * 2.0 * Dm[1][1];
+  double D22b = Dmb[2][2] + devGsqb * 2.0 * Dm[2][2];
+  const double G01b = Dmb[0][1] + Dmb[1][0] + devGsqb * 4.0 * G01;
+  const double G02b = Dmb[0][2] + Dmb[2][0] + devGsqb * 4.0 * G02;
+  const double G12b = Dmb[1][2] + Dmb[2][1] + devGsqb * 4.0 * G12;
+  const double tb = -(D00b + D11b + D22b) * (1.0 / 3.0);
+  const double G00b = D00b + tb, G11b = D11b + tb, G22b = D22b + tb;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double a0 = A[3 * k], a1 = A[3 * k + 1], a2 = A[3 * k + 2];
+    Ab[3 * k] += 2.0 * G00b * a0 + G01b * a1 + G02b * a2;
+    Ab[3 * k + 1] += 2.0 * G11b * a1 + G01b * a0 + G12b * a2;
+    Ab[3 * k + 2] += 2.0 * G22b * a2 + G02b * a0 + G12b * a1;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    q2b[i] += vb[i] * ir;
+    irb += vb[i] * q[2 + i];
+  }
+  rb -= irb * ir * ir;
+  qb[0] += rb;
+  qb[1] += q1b;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    qb[2 + i] += q2b[i];
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    qb[5 + k] += Ab[k];
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      qb[14 + i] += qJb[i];
+  }
+  if (thb) {
+    thb[PD_GAMMA] += Gm1b;
+    thb[PD_IG] += iGb;
+    thb[PD_B02] += b02b;
+    thb[PD_TH1C] += th1cb;
+    thb[PD_CALPHA2] += ca2b;
+    thb[PD_IKAPPA] += ikb;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -565,7 +966,8 @@ GPR_D void end_state(const double *qh, long c, int t, int side, const Consts &C,
 
 // Per cell end (4 per predictor cell, e = 2t + side): lambda (EV, the value
 // the forward's Rusanov switch compared) and the eigen data of the acoustic
-// tensor (EIG), shared by the end's tangent threads.
+// tensor (EIG) for the wave speed's reverse-mode product, from the tensor
+// and dominant eigenvalue of the same max_abs_eigs evaluation.
 // Points nb*4 .. nb*4 + ninst - 1: the state entering the step at each
 // instance's CFL argmax cell (for the derivative of dt).
 template <class L>
@@ -599,29 +1001,16 @@ __global__ void __launch_bounds__(128) k_adj_eig(const double *__restrict__ qh, 
   const DevPar &P = B.P[inst];
   Prim<L::THERMAL> sp;
   prim<L::THERMAL>(qp, P, sp);
-  EV[gid] = max_abs_eigs<L::THERMAL>(qp, sp, 0, P);
-  Dual q[V];
-#pragma unroll
-  for (int j = 0; j < V; j++)
-    q[j] = Dual{qp[j], 0.0};
-  DPar D = dpar_seed(P, -1);
-  DPrim<L::THERMAL> s;
-  dprim<L::THERMAL>(q, D, s);
-  Dual X[m][m];
-  dxi0<L::THERMAL>(q, s, D, X);
-  double Xv[m][m];
-#pragma unroll
-  for (int i = 0; i < m; i++)
-#pragma unroll
-    for (int j = 0; j < m; j++)
-      Xv[i][j] = X[i][j].v;
-  xi_eigdata<m>(Xv, EIG + gid * ND);
+  double Xv[m][m], l2;
+  EV[gid] = max_abs_eigs<L::THERMAL>(qp, sp, 0, P, &Xv[0][0], &l2);
+  xi_eigdata_l2<m>(Xv, l2, EIG + gid * ND);
 }
 
-// Jacobian columns at the 4 space-time nodes of every predictor cell
-// (e = 2t + s): F and S, JN[((c*4 + e)*K + k)*2V + o].
+// Jacobian columns at the 4 space-time nodes of the predictor cells the
+// dense solve takes (need[c]): F and S, JN[((c*4 + e)*K + k)*2V + o].
 template <class L>
 __global__ void __launch_bounds__(128) k_adj_jac_nodes(const double *__restrict__ qh, long nb,
+                                                       const int32_t *__restrict__ need,
                                                        double *__restrict__ JN, Batch B) {
   constexpr int V = L::V, K = V + NPD;
   long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -631,7 +1020,7 @@ __global__ void __launch_bounds__(128) k_adj_jac_nodes(const double *__restrict_
   long pt = gid / K;  // c*4 + e
   long c = pt / 4;
   int inst = B.inst_b[c];
-  if (B.clk[5 * inst + 1] == 0.0)
+  if (B.clk[5 * inst + 1] == 0.0 || !need[c])
     return;
   double qp[V];
   const double *src = qh + pt * V;
@@ -646,35 +1035,6 @@ __global__ void __launch_bounds__(128) k_adj_jac_nodes(const double *__restrict_
     o[j] = F[j].d;
     o[V + j] = S[j].d;
   }
-}
-
-// Jacobian columns at the 4 cell ends (e = 2t + side): F and lambda,
-// JE[((c*4 + e)*K + k)*(V+1) + o].
-template <class L>
-__global__ void __launch_bounds__(128) k_adj_jac_ends(const double *__restrict__ qh, long nb,
-                                                      double *__restrict__ JE,
-                                                      const double *__restrict__ EIG, Consts C,
-                                                      Batch B) {
-  constexpr int V = L::V, K = V + NPD, ND = Xi<L::THERMAL>::ND;
-  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (gid >= nb * 4 * K)
-    return;
-  int k = gid % K;
-  long pt = gid / K;
-  long c = pt / 4;
-  int e = (int)(pt % 4);
-  int inst = B.inst_b[c];
-  if (B.clk[5 * inst + 1] == 0.0)
-    return;
-  double qp[V];
-  end_state<V>(qh, c, e / 2, e % 2, C, qp);
-  Dual F[V], lam;
-  point_tangent<L>(qp, k, B.P[inst], F, nullptr, &lam, EIG + pt * ND);
-  double *o = JE + (pt * K + k) * (V + 1);
-#pragma unroll
-  for (int j = 0; j < V; j++)
-    o[j] = F[j].d;
-  o[V] = lam.d;
 }
 
 // One face's contribution to the cotangent of the state on one side.
@@ -693,23 +1053,27 @@ GPR_D void face_cot(const double *ubL, const double *ubR, double kk, double *Fb,
   }
 }
 
-// dJ[j] = sum_o dF_o/dq_j Fb_o (+ sbar dlambda/dq_j on the max side): the
-// Jacobian part, from k_adj_fv_dots.
-template <int V, int K>
+// One face's adjoint on the side of this cell (mineL: the cell is the face's
+// left neighbour): the flux VJP at this cell's end state (with the Rusanov
+// speed's cotangent where this end attains the maximum), the dissipation
+// and the path integral of B.  eig: eigen data at this cell's end.
+template <class L>
 GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR,
                     const double *ubL, const double *ubR, double kk, bool mineL,
-                    const double *dJ, const Consts &C, double *qb, double *thb) {
+                    const double *eig, const DevPar &P, const Consts &C, double *qb,
+                    double *thb) {
+  constexpr int V = L::V;
   double Fb[V], Bb[V];
   face_cot<V>(ubL, ubR, kk, Fb, Bb);
   bool Lmax = lamL > lamR;  // std::max(m1, m2) picks m2 on ties
   double sm = Lmax ? lamL : lamR;
+  double sbar = 0.0;
 #pragma unroll
-  for (int j = 0; j < K; j++) {
-    if (j < V)
-      qb[j] += dJ[j];
-    else
-      thb[j - V] += dJ[j];
-  }
+  for (int k = 0; k < V; k++)
+    sbar += Fb[k] * (ql[k] - qr[k]);
+  const bool mine_max = mineL ? Lmax : !Lmax;
+  point_vjp<L, true, false, true>(mineL ? ql : qr, P, Fb, nullptr, mine_max ? sbar : 0.0, eig,
+                                  qb, thb);
   double sgn = mineL ? sm : -sm;
 #pragma unroll
   for (int k = 0; k < V; k++)
@@ -746,169 +1110,83 @@ GPR_D void face_adj(const double *ql, const double *qr, double lamL, double lamR
 }
 
 // FV adjoint: cotangent of qh from the cotangent ubar of u' (faces and the
-// volume term), one thread per (predictor cell, time node).  Also the
-// material-field cotangents (thf) and <ubar, u' - u> / dt (dtf) since the FV
-// increment is linear in dt.
-//
-// k_adj_fv_dots first forms the Jacobian dot products, one thread per
-// (predictor cell, time node, Jacobian column j): D[(c*2 + t)*4 + r][j] for
-// r = 0 the face on the right of the cell (cell on its left), r = 1 the face
-// on its left, r = 2, 3 the volume term's S at spatial nodes 0, 1.
+// volume term), one thread per (predictor cell, time node), with the
+// reverse-mode products of F, lambda (cell ends) and S (volume nodes).  Also
+// the material-field cotangents (thf) and <ubar, u' - u> / dt (dtf) since
+// the FV increment is linear in dt.
+// Block = 4 warps over the same 32 (predictor cell, time node) pairs; warp
+// w takes one term (0: the face on the cell's right, 1: the face on its
+// left, 2 / 3: the volume term at spatial node 0 / 1), so that the lanes of
+// a warp run the same reverse sweep; the four partial cotangents are summed
+// in shared memory.
+constexpr int ADJ_FV_PAIRS = 32;
+
 template <class L>
-__global__ void __launch_bounds__(128) k_adj_fv_dots(
-    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ JN,
-    const double *__restrict__ JE, const double *__restrict__ EV, long nb,
-    double *__restrict__ D, Consts C, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
-  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (gid >= nb * 2 * K)
-    return;
-  const int j = gid % K;
-  const long ct = gid / K;
-  const long c = ct / 2;
+__global__ void __launch_bounds__(4 * ADJ_FV_PAIRS) k_adj_fv(
+    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ EV,
+    const double *__restrict__ EIG, const double *__restrict__ un,
+    const double *__restrict__ up, long nb, double *__restrict__ qbar, double *__restrict__ thf,
+    double *__restrict__ dtf, Consts C, Batch B) {
+  constexpr int V = L::V, ND = Xi<L::THERMAL>::ND, NO = 2 * V + NPD;
+  __shared__ double red[4][NO][ADJ_FV_PAIRS];
+  const int role = threadIdx.x / ADJ_FV_PAIRS, lane = threadIdx.x % ADJ_FV_PAIRS;
+  const long ct = (long)blockIdx.x * ADJ_FV_PAIRS + lane;
+  const bool valid = ct < nb * 2;
+  const long c = valid ? ct / 2 : 0;
   const int t = (int)(ct % 2);
   const int inst = B.inst_b[c];
   const double dt = B.clk[5 * inst + 1];
-  double d[4] = {0.0, 0.0, 0.0, 0.0};
-  if (dt != 0.0) {
-    const int li = (int)(c - B.off_b[inst]), nx = B.nx[inst];
-    const double kk = (dt * C.w[t]) / (2.0 * (1.0 / B.idx[inst]));
-    const double *ubi = ubar + (long)B.off_u[inst] * V;
+  const DevPar &P = B.P[inst];
+  double acc[2][V], th[NPD];
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      // r = 0: face li (this cell on the left); r = 1: face li - 1
-      if (r == 0 ? li > nx : li < 1)
-        continue;
-      const int f = r == 0 ? li : li - 1;
-      const long cl = r == 0 ? c : c - 1;
-      const double *qa = qh + (cl * 4 + 2 * t) * V, *qb2 = qh + ((cl + 1) * 4 + 2 * t) * V;
-      double Fb[V], Bb[V];
-      face_cot<V>(f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
-                  kk, Fb, Bb);
-      double sbar = 0.0;
-#pragma unroll
-      for (int k = 0; k < V; k++) {
-        double ql = C.endv[1][0] * qa[k] + C.endv[1][1] * qa[V + k];
-        double qr = C.endv[0][0] * qb2[k] + C.endv[0][1] * qb2[V + k];
-        sbar += Fb[k] * (ql - qr);
-      }
-      const double lamL = EV[cl * 4 + 2 * t + 1], lamR = EV[(cl + 1) * 4 + 2 * t];
-      const bool Lmax = lamL > lamR;  // std::max(m1, m2) picks m2 on ties
-      const bool mine_max = r == 0 ? Lmax : !Lmax;
-      const double *col = JE + ((c * 4 + 2 * t + (r == 0 ? 1 : 0)) * K + j) * (V + 1);
-      double acc = 0.0;
-#pragma unroll
-      for (int o = 0; o < V; o++)
-        acc += col[o] * Fb[o];
-      if (mine_max)
-        acc += sbar * col[V];
-      d[r] = acc;
-    }
-    if (li >= 1 && li <= nx) {
-      const double *ubc = ubi + (long)(li - 1) * V;
-#pragma unroll
-      for (int s = 0; s < 2; s++) {
-        const double *col = JN + ((c * 4 + 2 * t + s) * K + j) * 2 * V + V;
-        double acc = 0.0;
-#pragma unroll
-        for (int o = 0; o < V; o++)
-          acc += col[o] * ubc[o];
-        d[2 + s] = acc;
-      }
-    }
+  for (int k = 0; k < V; k++) {
+    acc[0][k] = 0.0;
+    acc[1][k] = 0.0;
   }
-#pragma unroll
-  for (int r = 0; r < 4; r++)
-    D[(ct * 4 + r) * K + j] = d[r];
-}
-
-template <class L>
-__global__ void __launch_bounds__(128) k_adj_fv(
-    const double *__restrict__ ubar, const double *__restrict__ qh, const double *__restrict__ D,
-    const double *__restrict__ EV, const double *__restrict__ un,
-    const double *__restrict__ up, long nb, double *__restrict__ qbar, double *__restrict__ thf,
-    double *__restrict__ dtf, Consts C, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
-  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (gid >= nb * 2)
-    return;
-  long c = gid / 2;
-  int t = gid % 2;
-  int inst = B.inst_b[c];
-  double dt = B.clk[5 * inst + 1];
-  double *qb = qbar + (c * 4 + 2 * t) * V;
-  double th[NPD];
 #pragma unroll
   for (int p = 0; p < NPD; p++)
     th[p] = 0.0;
-  if (dt == 0.0) {
-    for (int k = 0; k < 2 * V; k++)
-      qb[k] = 0.0;
-#pragma unroll
-    for (int p = 0; p < NPD; p++)
-      thf[(c * 2 + t) * NPD + p] = 0.0;
-    if (t == 0)
-      dtf[c] = 0.0;
-    return;
-  }
   const int li = (int)(c - B.off_b[inst]), nx = B.nx[inst];
-  const double idx = B.idx[inst];
-  const double dx = 1.0 / idx;
-  const double kk = (dt * C.w[t]) / (2.0 * dx);
-  const double *ubi = ubar + (long)B.off_u[inst] * V;
-  const double *qc = qh + (c * 4 + 2 * t) * V;
-  double acc[2][V], qLb[V], qRb[V];
+  if (valid && dt != 0.0) {
+    const double idx = B.idx[inst];
+    const double kk = (dt * C.w[t]) / (2.0 * (1.0 / idx));
+    const double *ubi = ubar + (long)B.off_u[inst] * V;
+    const double *qc = qh + (c * 4 + 2 * t) * V;
+    if (role < 2 && (role == 0 ? li <= nx : li >= 1)) {
+      // role 0: face li (this cell on the left); role 1: face li - 1
+      const int f = role == 0 ? li : li - 1;
+      const double *qa = role == 0 ? qc : qh + ((c - 1) * 4 + 2 * t) * V;
+      const double *qn = role == 0 ? qh + ((c + 1) * 4 + 2 * t) * V : qc;
+      const long cl = role == 0 ? c : c - 1;
+      double ql[V], qr[V], eb[V];
 #pragma unroll
-  for (int k = 0; k < V; k++) {
-    qLb[k] = 0.0;
-    qRb[k] = 0.0;
-  }
-  if (li <= nx) {  // face li: this cell on the left
-    int f = li;
-    const double *qn = qh + ((c + 1) * 4 + 2 * t) * V;
-    double ql[V], qr[V];
-#pragma unroll
-    for (int k = 0; k < V; k++) {
-      ql[k] = C.endv[1][0] * qc[k] + C.endv[1][1] * qc[V + k];
-      qr[k] = C.endv[0][0] * qn[k] + C.endv[0][1] * qn[V + k];
-    }
-    face_adj<V, K>(ql, qr, EV[c * 4 + 2 * t + 1], EV[(c + 1) * 4 + 2 * t],
-                   f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
-                   kk, true, D + ((c * 2 + t) * 4 + 0) * K, C, qLb, th);
-  }
-  if (li >= 1) {  // face li - 1: this cell on the right
-    int f = li - 1;
-    const double *qp = qh + ((c - 1) * 4 + 2 * t) * V;
-    double ql[V], qr[V];
-#pragma unroll
-    for (int k = 0; k < V; k++) {
-      ql[k] = C.endv[1][0] * qp[k] + C.endv[1][1] * qp[V + k];
-      qr[k] = C.endv[0][0] * qc[k] + C.endv[0][1] * qc[V + k];
-    }
-    face_adj<V, K>(ql, qr, EV[(c - 1) * 4 + 2 * t + 1], EV[c * 4 + 2 * t],
-                   f > 0 ? ubi + (long)(f - 1) * V : nullptr, f < nx ? ubi + (long)f * V : nullptr,
-                   kk, false, D + ((c * 2 + t) * 4 + 1) * K, C, qRb, th);
-  }
-#pragma unroll
-  for (int m = 0; m < 2; m++)
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      acc[m][k] = C.endv[1][m] * qLb[k] + C.endv[0][m] * qRb[k];
-  if (li >= 1 && li <= nx) {
-    // volume term: u += (dt w_t) w_s (S - idx B(v) dq)   (fv.cpp:11-109)
-    const double *ubc = ubi + (long)(li - 1) * V;
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      double a = (dt * C.w[t]) * C.w[s];
-      const double *qs = qc + s * V, *qo = qc + (1 - s) * V;
-      const double *dS = D + ((c * 2 + t) * 4 + 2 + s) * K;
-#pragma unroll
-      for (int j = 0; j < K; j++) {
-        if (j < V)
-          acc[s][j] += a * dS[j];
-        else
-          th[j - V] += a * dS[j];
+      for (int k = 0; k < V; k++) {
+        ql[k] = C.endv[1][0] * qa[k] + C.endv[1][1] * qa[V + k];
+        qr[k] = C.endv[0][0] * qn[k] + C.endv[0][1] * qn[V + k];
+        eb[k] = 0.0;
       }
+      face_adj<L>(ql, qr, EV[cl * 4 + 2 * t + 1], EV[(cl + 1) * 4 + 2 * t],
+                  f > 0 ? ubi + (long)(f - 1) * V : nullptr,
+                  f < nx ? ubi + (long)f * V : nullptr, kk, role == 0,
+                  EIG + (c * 4 + 2 * t + (role == 0 ? 1 : 0)) * ND, P, C, eb, th);
+      // this cell's end state: ENDVALS[side] . (node 0, node 1)
+      const int side = role == 0 ? 1 : 0;
+#pragma unroll
+      for (int m = 0; m < 2; m++)
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          acc[m][k] = C.endv[side][m] * eb[k];
+    } else if (role >= 2 && li >= 1 && li <= nx) {
+      // volume term: u += (dt w_t) w_s (S - idx B(v) dq)   (fv.cpp:11-109)
+      const int s = role - 2;
+      const double *ubc = ubi + (long)(li - 1) * V;
+      const double a = (dt * C.w[t]) * C.w[s];
+      const double *qs = qc + s * V, *qo = qc + (1 - s) * V;
+      double Sb[V];
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        Sb[k] = a * ubc[k];
+      point_vjp<L, false, true, false>(qs, P, nullptr, Sb, 0.0, nullptr, acc[s], th);
       double yb[V], dq[V], xb[V];
       double ir = 1.0 / qs[0];
       double v[3] = {qs[2] * ir, qs[3] * ir, qs[4] * ir};
@@ -927,26 +1205,37 @@ __global__ void __launch_bounds__(128) k_adj_fv(
         acc[s][k] += C.derv[s][s] * xb[k];
         acc[1 - s][k] += C.derv[s][1 - s] * xb[k];
       }
-    }
-    if (t == 0) {
-      long j = (long)B.off_u[inst] + li - 1;
-      double x = 0.0;
+      if (s == 1 && t == 0) {
+        long j = (long)B.off_u[inst] + li - 1;
+        double x = 0.0;
 #pragma unroll
-      for (int k = 0; k < V; k++)
-        x += ubc[k] * (up[j * V + k] - un[j * V + k]);
-      dtf[c] = x / dt;
+        for (int k = 0; k < V; k++)
+          x += ubc[k] * (up[j * V + k] - un[j * V + k]);
+        dtf[c] = x / dt;
+      }
     }
-  } else if (t == 0) {
+  }
+  if (valid && role == 3 && t == 0 && !(dt != 0.0 && li >= 1 && li <= nx))
     dtf[c] = 0.0;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    red[role][k][lane] = acc[0][k];
+    red[role][V + k][lane] = acc[1][k];
   }
 #pragma unroll
-  for (int m = 0; m < 2; m++)
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      qb[m * V + k] = acc[m][k];
-#pragma unroll
   for (int p = 0; p < NPD; p++)
-    thf[(c * 2 + t) * NPD + p] = th[p];
+    red[role][2 * V + p][lane] = th[p];
+  __syncthreads();
+  if (!valid)
+    return;
+  double *qb = qbar + (c * 4 + 2 * t) * V;
+  for (int k = role; k < NO; k += 4) {
+    const double x = (red[0][k][lane] + red[1][k][lane]) + (red[2][k][lane] + red[3][k][lane]);
+    if (k < 2 * V)
+      qb[k] = x;
+    else
+      thf[(c * 2 + t) * NPD + (k - 2 * V)] = x;
+  }
 }
 
 // Predictor adjoint at the converged fixed point.  With
@@ -957,148 +1246,420 @@ __global__ void __launch_bounds__(128) k_adj_fv(
 //   wbar = (d(W w)/dw)^T mu,  dtbar = mu . R(q),  thbar = dt mu . dR/dth.
 // Stage 1 (k_adj_pred_iter, 4 lanes per cell as in k_predictor_picard)
 // iterates mu <- DG_U^-T (qbar + dt (dR/dq)^T mu), which contracts exactly
-// where the forward Picard iteration does; cells it leaves unconverged
-// (those the forward hands to its Newton pass) get the exact dense solve of
-// stage 2 (k_adj_pred_dense, one block per cell); stage 3 (k_adj_pred_post)
-// forms the cotangents from mu.
-constexpr int ADJ_PRED_IT = 100;
-constexpr double ADJ_PRED_TOL = 1e-11;
-
-// One warp per cell: lane = 8 g + p serves node g (= 2t + i) and the entries
-// k = p, p + 8, p + 16 of its vectors; the node Jacobians (state columns)
-// are staged once in shared memory.
-constexpr int ADJ_CPB = 2;  // cells (warps) per block
+// where the forward Picard iteration does, each lane applying (dR/dq)^T at
+// its node by one reverse-mode product of F and S; cells it leaves
+// unconverged (those the forward hands to its Newton pass) get the exact
+// dense solve of stage 2 (k_adj_pred_dense, one block per cell, over the
+// node Jacobians k_adj_jac_nodes builds for those cells only); stage 3
+// (k_adj_pred_post) forms the cotangents from mu.
+// Primal values that the reverse sweep of F and S reads at one node, cached
+// once per node for the transposed iteration (structure of arrays with
+// stride ST: entry k of a node at c[k * ST]).  wn (the node's quadrature
+// weight w_t w_i) is folded into the source terms so that the S cotangent
+// is mu itself.
+template <class L> struct PCache {
+  static constexpr int V = L::V;
+  enum {
+    IR, IR2, VV, JJ = VV + 3, CJ = JJ + 3, CA2T = CJ + 3, Q1PP, Q1M, DM, ADG = DM + 6,
+    SG = ADG + 9, SGM = SG + 3, SGF = SGM + 3, FSW, COFK, GSW = COFK + 9, GTW, IRGICV, PPICV,
+    RGM1, E1GM1, Q, N = Q + V
+  };
+};
 
 template <class L>
-__global__ void __launch_bounds__(32 * ADJ_CPB) k_adj_pred_iter(
-    const double *__restrict__ qh, const double *__restrict__ qbar, const double *__restrict__ JN,
-    long nb, double *__restrict__ mu_buf, int32_t *__restrict__ need, Consts C, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
-  __shared__ double Js[ADJ_CPB][4][2][V][V + 1];  // [cell][node][F, S][j][o] = d(F_o)/dq_j
-  __shared__ double sm_mu[ADJ_CPB][4][V], sm_y[ADJ_CPB][4][V], sm_xb[ADJ_CPB][4][V],
-      sm_z[ADJ_CPB][4][V], sm_x[ADJ_CPB][4][V], sm_v[ADJ_CPB][4][3];
-  const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const long c = (long)blockIdx.x * ADJ_CPB + w;
+GPR_D void pcache_init(const double *q, const DevPar &P, double wn, double *c, int ST) {
+  using PC = PCache<L>;
+  constexpr bool TH = L::THERMAL;
+  const double *A = q + 5;
+  const double r = q[0], ir = 1.0 / r;
+  double v[3], J[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    v[i] = q[2 + i] * ir;
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      J[i] = q[14 + i] * ir;
+  }
+  const double G00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  const double G11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  const double G22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  const double G01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  const double G02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  const double G12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  const double tG = (G00 + G11 + G22) * (1.0 / 3.0);
+  const double Dm[3][3] = {{G00 - tG, G01, G02}, {G01, G11 - tG, G12}, {G02, G12, G22 - tG}};
+  const double devGsq = Dm[0][0] * Dm[0][0] + Dm[1][1] * Dm[1][1] + Dm[2][2] * Dm[2][2] +
+                        2.0 * (G01 * G01 + G02 * G02 + G12 * G12);
+  double AdG[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      AdG[3 * i + j] = A[3 * i] * Dm[0][j] + A[3 * i + 1] * Dm[1][j] + A[3 * i + 2] * Dm[2][j];
+  const double Gm1 = P.gamma - 1.0, irG = ir * P.iG;
+  double E1 = q[1] * ir - 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) -
+              0.25 * (P.b02 * devGsq);
+  if (TH)
+    E1 = E1 - 0.5 * (P.calpha2 * (J[0] * J[0] + J[1] * J[1] + J[2] * J[2]));
+  const double er = P.pINF * ir;
+  const double p = (E1 - er) * (r * Gm1) - P.pINF;
+  const double T = (p + P.pINF) * irG * P.icv;
+  const double sgf = -(r * P.b02);
+  const double dA = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                    A[2] * (A[3] * A[7] - A[4] * A[6]);
+  const double cb = cbrt(dA);
+  const double th = dA * cb * cb * P.th1c;
+  const double kc = wn * (-P.b02) * P.th1c * (5.0 / 3.0) * cb * cb;
+  const double cof[9] = {A[4] * A[8] - A[5] * A[7], A[5] * A[6] - A[3] * A[8],
+                         A[3] * A[7] - A[4] * A[6], A[2] * A[7] - A[1] * A[8],
+                         A[0] * A[8] - A[2] * A[6], A[1] * A[6] - A[0] * A[7],
+                         A[1] * A[5] - A[2] * A[4], A[2] * A[3] - A[0] * A[5],
+                         A[0] * A[4] - A[1] * A[3]};
+  c[PC::IR * ST] = ir;
+  c[PC::IR2 * ST] = ir * ir;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    c[(PC::VV + i) * ST] = v[i];
+    c[(PC::JJ + i) * ST] = J[i];
+    c[(PC::CJ + i) * ST] = P.calpha2 * J[i];
+    double sm = AdG[i] * A[0] + AdG[3 + i] * A[3] + AdG[6 + i] * A[6];
+    c[(PC::SGM + i) * ST] = sm;
+    c[(PC::SG + i) * ST] = sgf * sm;
+  }
+  c[PC::CA2T * ST] = P.calpha2 * T;
+  c[PC::Q1PP * ST] = q[1] + p;
+  c[PC::Q1M * ST] = q[1] - P.pINF;
+  c[(PC::DM + 0) * ST] = Dm[0][0];
+  c[(PC::DM + 1) * ST] = Dm[1][1];
+  c[(PC::DM + 2) * ST] = Dm[2][2];
+  c[(PC::DM + 3) * ST] = G01;
+  c[(PC::DM + 4) * ST] = G02;
+  c[(PC::DM + 5) * ST] = G12;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    c[(PC::ADG + k) * ST] = AdG[k];
+    c[(PC::COFK + k) * ST] = kc * cof[k];
+  }
+  c[PC::SGF * ST] = sgf;
+  c[PC::FSW * ST] = wn * (-(P.b02 * th));
+  c[PC::GSW * ST] = wn * (-(P.calpha2 * T * P.ikappa));
+  c[PC::GTW * ST] = wn * (P.calpha2 * P.ikappa);
+  c[PC::IRGICV * ST] = irG * P.icv;
+  c[PC::PPICV * ST] = (p + P.pINF) * P.icv;
+  c[PC::RGM1 * ST] = r * Gm1;
+  c[PC::E1GM1 * ST] = (E1 - er) * Gm1;
+#pragma unroll
+  for (int k = 0; k < L::V; k++)
+    c[(PC::Q + k) * ST] = q[k];
+}
+
+// r += (dF/dq)^T Fb + wn (dS/dq)^T mu from the cached primal values: the
+// reverse sweep of point_vjp (HF, HS, no material fields), term by term.
+template <class L>
+GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb,
+                      const double *mu, double *r) {
+  using PC = PCache<L>;
+  constexpr bool TH = L::THERMAL;
+#define PCV(k) c[(k) * ST]
+  const double *qc = c + PC::Q * ST;
+#define PQ(k) qc[(k) * ST]
+  double A[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    A[k] = PQ(5 + k);
+  const double v[3] = {PCV(PC::VV), PCV(PC::VV + 1), PCV(PC::VV + 2)};
+  double vb[3], sgb[3], Ab[9], AdGb[9], Jb[3] = {0.0, 0.0, 0.0}, qJb[3] = {0.0, 0.0, 0.0};
+  double q2b[3];
+  // flux
+  const double f1 = Fb[1];
+  vb[0] = f1 * PCV(PC::Q1PP);
+  vb[1] = 0.0;
+  vb[2] = 0.0;
+  double q1b = f1 * v[0];
+  double pb = f1 * v[0] + Fb[2];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    sgb[i] = -(f1 * v[i]) - Fb[2 + i];
+    vb[i] -= f1 * PCV(PC::SG + i);
+    vb[0] += Fb[2 + i] * PQ(2 + i);
+    q2b[i] = Fb[2 + i] * v[0];
+  }
+  q2b[0] += Fb[0];
+  double Tb = 0.0;
+  if (TH) {
+    Tb = f1 * PCV(PC::CJ) + Fb[14];
+    Jb[0] = f1 * PCV(PC::CA2T);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      vb[0] += Fb[14 + i] * PQ(14 + i);
+      qJb[i] = Fb[14 + i] * v[0];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const double f = Fb[5 + 3 * i];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Ab[3 * i + j] = f * v[j];
+      vb[j] += f * A[3 * i + j];
+    }
+  }
+  // source (wn folded into FSW, COFK, GSW)
+  double fb = 0.0;
+  const double fsw = PCV(PC::FSW);
+#pragma unroll
+  for (int i = 0; i < 9; i++) {
+    fb += mu[5 + i] * PCV(PC::ADG + i);
+    AdGb[i] = mu[5 + i] * fsw;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    Ab[k] += fb * PCV(PC::COFK + k);
+  if (TH) {
+    const double gsw = PCV(PC::GSW);
+    double gb = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      gb += mu[14 + i] * PCV(PC::JJ + i);
+      Jb[i] += mu[14 + i] * gsw;
+    }
+    Tb -= gb * PCV(PC::GTW);
+  }
+  // sigma column 0
+  const double sgf = PCV(PC::SGF);
+  double sgfb = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    sgfb += sgb[i] * PCV(PC::SGM + i);
+    const double f = sgb[i] * sgf;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      AdGb[3 * k + i] += f * A[3 * k];
+      Ab[3 * k] += f * PCV(PC::ADG + 3 * k + i);
+    }
+  }
+  double rb = -(sgfb * P.b02);
+  // prim
+  pb += Tb * PCV(PC::IRGICV);
+  const double irGb = Tb * PCV(PC::PPICV);
+  const double E1b = pb * PCV(PC::RGM1);
+  rb += pb * PCV(PC::E1GM1);
+  const double ir = PCV(PC::IR);
+  double irb = E1b * PCV(PC::Q1M) + irGb * P.iG;
+  q1b += E1b * ir;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    vb[i] -= E1b * v[i];
+  const double devGsqb = -0.25 * P.b02 * E1b;
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      Jb[i] -= E1b * PCV(PC::CJ + i);
+      qJb[i] += Jb[i] * ir;
+      irb += Jb[i] * PQ(14 + i);
+    }
+  }
+  // AdG = A Dm
+  const double D00 = PCV(PC::DM), D11 = PCV(PC::DM + 1), D22 = PCV(PC::DM + 2);
+  const double G01 = PCV(PC::DM + 3), G02 = PCV(PC::DM + 4), G12 = PCV(PC::DM + 5);
+  const double Dm[3][3] = {{D00, G01, G02}, {G01, D11, G12}, {G02, G12, D22}};
+  double Dmb[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      Dmb[k][j] = AdGb[j] * A[k] + AdGb[3 + j] * A[3 + k] + AdGb[6 + j] * A[6 + k];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      Ab[3 * i + k] += AdGb[3 * i] * Dm[k][0] + AdGb[3 * i + 1] * Dm[k][1] +
+                       AdGb[3 * i + 2] * Dm[k][2];
+  const double D00b = Dmb[0][0] + devGsqb * 2.0 * D00;
+  const double D11b = Dmb[1][1] + devGsqb * 2.0 * D11;
+  const double D22b = Dmb[2][2] + devGsqb * 2.0 * D22;
+  const double G01b = Dmb[0][1] + Dmb[1][0] + devGsqb * 4.0 * G01;
+  const double G02b = Dmb[0][2] + Dmb[2][0] + devGsqb * 4.0 * G02;
+  const double G12b = Dmb[1][2] + Dmb[2][1] + devGsqb * 4.0 * G12;
+  const double tb = -(D00b + D11b + D22b) * (1.0 / 3.0);
+  const double G00b = D00b + tb, G11b = D11b + tb, G22b = D22b + tb;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double a0 = A[3 * k], a1 = A[3 * k + 1], a2 = A[3 * k + 2];
+    Ab[3 * k] += 2.0 * G00b * a0 + G01b * a1 + G02b * a2;
+    Ab[3 * k + 1] += 2.0 * G11b * a1 + G01b * a0 + G12b * a2;
+    Ab[3 * k + 2] += 2.0 * G22b * a2 + G02b * a0 + G12b * a1;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    q2b[i] += vb[i] * ir;
+    irb += vb[i] * PQ(2 + i);
+  }
+  rb -= irb * PCV(PC::IR2);
+  r[0] += rb;
+  r[1] += q1b;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    r[2 + i] += q2b[i];
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    r[5 + k] += Ab[k];
+  if (TH) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      r[14 + i] += qJb[i];
+  }
+#undef PCV
+#undef PQ
+}
+
+constexpr int ADJ_PRED_IT = 100;
+constexpr double ADJ_PRED_TOL = 1e-11;
+constexpr int ADJ_IT_T = 64;  // threads (16 cells) per block of k_adj_pred_iter
+
+// max(a, |d|) on the IEEE bit patterns of non-negative doubles (integer
+// order equals numeric order there; NaN patterns sort above every number)
+GPR_D unsigned long long absmax_bits(unsigned long long a, double d) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(d) & 0x7fffffffffffffffULL;
+  return b > a ? b : a;
+}
+
+template <class L>
+__global__ void __launch_bounds__(ADJ_IT_T) k_adj_pred_iter(
+    const double *__restrict__ qh, const double *__restrict__ qbar, long nb,
+    double *__restrict__ mu_buf, int32_t *__restrict__ need, int32_t *__restrict__ info,
+    Consts C, Batch B) {
+  constexpr int V = L::V, NC = PCache<L>::N, ST = ADJ_IT_T;
+  __shared__ double cache[(NC + 6) * ST];
+  double *pc = cache + threadIdx.x;
+  double *xs = cache + NC * ST + threadIdx.x;  // x at 6, 7, 9, 10, 12, 13
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int g = threadIdx.x % 4;
+  const long c = gt / 4;
   const bool valid = c < nb;
   const long cc = valid ? c : 0;
+  const int t = g / 2, i = g % 2;
   const int inst = B.inst_b[cc];
   const double dt = B.clk[5 * inst + 1];
   const double idx = B.idx[inst];
+  const DevPar &P = B.P[inst];
   const bool active = valid && dt != 0.0;
-  const int g = lane / 8, p = lane % 8, t = g / 2, i = g % 2;
-  if (active) {
-    for (int e = lane; e < 4 * V * 2 * V; e += 32) {
-      int gg = e / (2 * V * V), rem = e % (2 * V * V);
-      int j = rem / (2 * V), o = rem % (2 * V);
-      Js[w][gg][o / V][j][o % V] = JN[((cc * 4 + gg) * K + j) * 2 * V + o];
-    }
-  }
-  // node data: x_ti = idx sum_m DERVALS[i][m] q_tm, v = q[2..4] / q[0]
-  const double *qn = qh + (cc * 4 + g) * V, *qo = qh + (cc * 4 + (g ^ 1)) * V;
-  for (int k = p; k < V; k += 8) {
-    sm_x[w][g][k] = idx * (C.derv[i][i] * qn[k] + C.derv[i][1 - i] * qo[k]);
-    sm_mu[w][g][k] = 0.0;
-  }
-  if (p == 0) {
-    double ir = 1.0 / qn[0];
-    sm_v[w][g][0] = qn[2] * ir;
-    sm_v[w][g][1] = qn[3] * ir;
-    sm_v[w][g][2] = qn[4] * ir;
-  }
-  double qb[3];
+  const double wn = C.w[t] * C.w[i], wno = C.w[t] * C.w[1 - i], wti = C.w[t] * idx;
+  // node data: the primal cache, x_ti = idx sum_m DERVALS[i][m] q_tm
+  double mu[V], qb[V], tmp[V];
+  {
+    double q[V];
 #pragma unroll
-  for (int m = 0; m < 3; m++) {
-    int k = p + 8 * m;
-    qb[m] = (active && k < V) ? qbar[(cc * 4 + g) * V + k] : 0.0;
-  }
-  const double q0 = qn[0], iq0 = 1.0 / q0;
-  const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx, iws = 1.0 / C.w[i];
-  __syncwarp();
-  const double *v = sm_v[w][g];
-  bool conv = !active;
-  for (int it = 0; it < ADJ_PRED_IT && active; it++) {
-    // y = sum_i DG_DER[i][m] mu_i ; xb = -wn B^T mu
-    const double *mu = sm_mu[w][g], *mo = sm_mu[w][g ^ 1];
-    for (int k = p; k < V; k += 8) {
-      sm_y[w][g][k] = C.dgder[i][i] * mu[k] + C.dgder[1 - i][i] * mo[k];
-      double xb = 0.0;
-      if (k >= 5 && k < 14) {
-        int rr = (k - 5) / 3, cc3 = (k - 5) % 3;
-        if (cc3 == 1)
-          xb = -v[1] * mu[5 + 3 * rr] + v[0] * mu[6 + 3 * rr];
-        else if (cc3 == 2)
-          xb = -v[2] * mu[5 + 3 * rr] + v[0] * mu[7 + 3 * rr];
+    for (int k = 0; k < V; k++)
+      q[k] = qh[(cc * 4 + g) * V + k];
+    shfl_vec<V>(q, tmp, 1);
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int m = 0; m < 2; m++) {
+        int k = 6 + 3 * r + m;
+        xs[(2 * r + m) * ST] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * tmp[k]);
       }
-      sm_xb[w][g][k] = -wn * xb;
+    pcache_init<L>(q, P, wn, pc, ST);
+  }
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    qb[k] = active ? qbar[(cc * 4 + g) * V + k] : 0.0;
+    mu[k] = 0.0;
+  }
+  const double fa = -wti * C.dgder[i][i], fo = -wti * C.dgder[1 - i][i];
+  const double xa = -wn * idx * C.derv[i][i], xo = -wno * idx * C.derv[1 - i][i];
+  const double ga = C.dgmatinv[t][t] / C.w[i], go = C.dgmatinv[1 - t][t] / C.w[i];
+  const double iq0 = pc[PCache<L>::IR * ST];
+  const double v[3] = {pc[PCache<L>::VV * ST], pc[(PCache<L>::VV + 1) * ST],
+                       pc[(PCache<L>::VV + 2) * ST]};
+  bool conv = !active, done = !active;
+  int nit = 0;
+  for (int it = 0; it < ADJ_PRED_IT; it++) {
+    if (__all_sync(0xffffffffu, done))
+      break;
+    nit += done ? 0 : 1;
+    // F cotangent -wti sum_i DG_DER[i][m] mu_i; S cotangent wn mu (wn in the cache)
+    double Fb[V], r[V];
+    shfl_vec<V>(mu, tmp, 1);
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      Fb[k] = fa * mu[k] + fo * tmp[k];
+      r[k] = 0.0;
     }
-    __syncwarp();
-    // through v(q): vb = -wn (d(B x)/dv)^T mu
-    const double *x = sm_x[w][g];
+    if (active)
+      pcache_vjp<L>(pc, ST, P, Fb, mu, r);
+    // -wn B(v)^T mu through x (coupling the spatial nodes) and through v(q)
+    double xb[6], xq[6];
+#pragma unroll
+    for (int rr = 0; rr < 3; rr++) {
+      xb[2 * rr] = -v[1] * mu[5 + 3 * rr] + v[0] * mu[6 + 3 * rr];
+      xb[2 * rr + 1] = -v[2] * mu[5 + 3 * rr] + v[0] * mu[7 + 3 * rr];
+    }
     double vb0 = 0.0, vb1 = 0.0, vb2 = 0.0;
 #pragma unroll
-    for (int r = 0; r < 3; r++) {
-      vb0 += x[6 + 3 * r] * mu[6 + 3 * r] + x[7 + 3 * r] * mu[7 + 3 * r];
-      vb1 -= x[6 + 3 * r] * mu[5 + 3 * r];
-      vb2 -= x[7 + 3 * r] * mu[5 + 3 * r];
+    for (int rr = 0; rr < 3; rr++) {
+      const double x6 = xs[(2 * rr) * ST], x7 = xs[(2 * rr + 1) * ST];
+      vb0 += x6 * mu[6 + 3 * rr] + x7 * mu[7 + 3 * rr];
+      vb1 -= x6 * mu[5 + 3 * rr];
+      vb2 -= x7 * mu[5 + 3 * rr];
     }
-    vb0 *= -wn;
-    vb1 *= -wn;
-    vb2 *= -wn;
-    const double *y = sm_y[w][g], *xs = sm_xb[w][g], *xso = sm_xb[w][g ^ 1];
-    for (int j = p; j < V; j += 8) {
-      const double *JF = Js[w][g][0][j], *JS = Js[w][g][1][j];
-      double sF = 0.0, sS = 0.0;
+    const double wq = wn * iq0;
+    r[0] += wq * (vb0 * v[0] + vb1 * v[1] + vb2 * v[2]);
+    r[2] -= wq * vb0;
+    r[3] -= wq * vb1;
+    r[4] -= wq * vb2;
 #pragma unroll
-      for (int o = 0; o < V; o++) {
-        sF += JF[o] * y[o];
-        sS += JS[o] * mu[o];
+    for (int m = 0; m < 6; m++)
+      xq[m] = __shfl_xor_sync(0xffffffffu, xb[m], 1);
+#pragma unroll
+    for (int rr = 0; rr < 3; rr++)
+#pragma unroll
+      for (int m = 0; m < 2; m++)
+        r[6 + 3 * rr + m] += xa * xb[2 * rr + m] + xo * xq[2 * rr + m];
+    // z = qbar + dt r; mu = DG_U^-T z (time coupling)
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] = qb[k] + dt * r[k];
+    shfl_vec<V>(r, tmp, 2);
+    unsigned long long ddb = 0, scb = 0;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      const double mn = ga * r[k] + go * tmp[k];
+      ddb = absmax_bits(ddb, mn - mu[k]);
+      scb = absmax_bits(scb, mn);
+      tmp[k] = mn;
+    }
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) {
+      unsigned long long a = __shfl_xor_sync(0xffffffffu, ddb, o);
+      unsigned long long b = __shfl_xor_sync(0xffffffffu, scb, o);
+      ddb = a > ddb ? a : ddb;
+      scb = b > scb ? b : scb;
+    }
+    if (!done) {
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        mu[k] = tmp[k];
+      if (scb > 0x7ff0000000000000ULL) {  // NaN
+        done = true;
+      } else if (__longlong_as_double((long long)ddb) <=
+                 ADJ_PRED_TOL * __longlong_as_double((long long)scb)) {
+        conv = true;
+        done = true;
       }
-      double r = wn * sS - wti * sF;
-      if (j == 0)
-        r -= (vb0 * v[0] + vb1 * v[1] + vb2 * v[2]) * iq0;
-      else if (j >= 2 && j < 5)
-        r += (j == 2 ? vb0 : (j == 3 ? vb1 : vb2)) * iq0;
-      r += idx * (C.derv[i][i] * xs[j] + C.derv[1 - i][i] * xso[j]);
-      sm_z[w][g][j] = qb[j / 8] + dt * r;
-    }
-    __syncwarp();
-    const double *z = sm_z[w][g], *zo = sm_z[w][g ^ 2];
-    double mun[3], dd = 0.0, sc = 0.0;
-#pragma unroll
-    for (int m = 0; m < 3; m++) {
-      int k = p + 8 * m;
-      if (k < V) {
-        mun[m] = (C.dgmatinv[t][t] * z[k] + C.dgmatinv[1 - t][t] * zo[k]) * iws;
-        dd = fmax(dd, fabs(mun[m] - mu[k]));
-        sc = fmax(sc, fabs(mun[m]));
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      dd = fmax(dd, __shfl_xor_sync(0xffffffffu, dd, o));
-      sc = fmax(sc, __shfl_xor_sync(0xffffffffu, sc, o));
-    }
-    __syncwarp();
-#pragma unroll
-    for (int m = 0; m < 3; m++) {
-      int k = p + 8 * m;
-      if (k < V)
-        sm_mu[w][g][k] = mun[m];
-    }
-    __syncwarp();
-    if (!(sc == sc))
-      break;
-    if (dd <= ADJ_PRED_TOL * sc) {
-      conv = true;
-      break;
     }
   }
   if (!valid)
     return;
-  for (int k = p; k < V; k += 8)
-    mu_buf[(c * 4 + g) * V + k] = sm_mu[w][g][k];
-  if (lane == 0)
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    mu_buf[(c * 4 + g) * V + k] = mu[k];
+  if (g == 0) {
     need[c] = conv ? 0 : 1;
+    info[c] += nit << 8;
+  }
 }
 
 // d(B_x(v(q)) x)_r / dq_c and B_x(v)[r][c] (bdot, d = 0)
@@ -1271,10 +1832,10 @@ __global__ void __launch_bounds__(128) k_adj_pred_dense(
 
 template <class L>
 __global__ void __launch_bounds__(128) k_adj_pred_post(
-    const double *__restrict__ qh, const double *__restrict__ mu_buf,
-    const double *__restrict__ JN, long nb, double *__restrict__ wbar, double *__restrict__ thp,
-    double *__restrict__ dtp, Consts C, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
+    const double *__restrict__ qh, const double *__restrict__ mu_buf, long nb,
+    double *__restrict__ wbar, double *__restrict__ thp, double *__restrict__ dtp, Consts C,
+    Batch B) {
+  constexpr int V = L::V;
   long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int g = threadIdx.x % 4;
   const long c = gt / 4;
@@ -1292,7 +1853,6 @@ __global__ void __launch_bounds__(128) k_adj_pred_post(
     q[k] = qh[(cc * 4 + g) * V + k];
     mu[k] = active ? mu_buf[(cc * 4 + g) * V + k] : 0.0;
   }
-  const double *J = JN + (cc * 4 + g) * K * 2 * V;
   const double wn = C.w[t] * C.w[i], wti = C.w[t] * idx;
   shfl_vec<V>(mu, other, 1);
 #pragma unroll
@@ -1308,19 +1868,20 @@ __global__ void __launch_bounds__(128) k_adj_pred_post(
 #pragma unroll
   for (int k = 0; k < V; k++)
     dtb += mu[k] * R[k];
+  // thbar = dt (wn dS/dth^T mu - wti dF/dth^T y)
   double th[NPD];
 #pragma unroll
-  for (int p = 0; p < NPD; p++) {
-    double sF = 0.0, sS = 0.0;
-    if (active) {
-      const double *col = J + (V + p) * 2 * V;
+  for (int p = 0; p < NPD; p++)
+    th[p] = 0.0;
+  if (active) {
+    double Fb[V], Sb[V], qd[V];
 #pragma unroll
-      for (int o = 0; o < V; o++) {
-        sF += col[o] * y[o];
-        sS += col[V + o] * mu[o];
-      }
+    for (int k = 0; k < V; k++) {
+      Fb[k] = -(dt * wti) * y[k];
+      Sb[k] = (dt * wn) * mu[k];
+      qd[k] = 0.0;
     }
-    th[p] = dt * (wn * sS - wti * sF);
+    point_vjp<L, true, true, false>(q, P, Fb, Sb, 0.0, nullptr, qd, th);
   }
   // W w: Ww(t, s) = ENDVALS[0][t] w_s wh(s)  (dg1.cpp:68-73)
   double wb[V];
@@ -1551,6 +2112,37 @@ __global__ void k_adj_point(const double *__restrict__ Q, long count, double *__
     JS[(c * K + k) * V + j] = S[j].d;
   }
   dlam[c * K + k] = lam.d;
+}
+
+// Pointwise VJPs (test hook): per point c, qb[c] = (dF/dq)^T Fb[c] +
+// (dS/dq)^T Sb[c] + lb[c] dlambda/dq and thb[c] the same for the fields.
+template <class L>
+__global__ void k_adj_point_vjp(const double *__restrict__ Q, long count,
+                                const double *__restrict__ Fb, const double *__restrict__ Sb,
+                                const double *__restrict__ lb, double *__restrict__ qb,
+                                double *__restrict__ thb, DevPar P) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= count)
+    return;
+  double q[V], f[V], s[V], o[V], th[NPD];
+#pragma unroll
+  for (int j = 0; j < V; j++) {
+    q[j] = Q[c * V + j];
+    f[j] = Fb[c * V + j];
+    s[j] = Sb[c * V + j];
+    o[j] = 0.0;
+  }
+#pragma unroll
+  for (int p = 0; p < NPD; p++)
+    th[p] = 0.0;
+  point_vjp<L, true, true, true>(q, P, f, s, lb[c], nullptr, o, th);
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    qb[c * V + j] = o[j];
+#pragma unroll
+  for (int p = 0; p < NPD; p++)
+    thb[c * NPD + p] = th[p];
 }
 
 }  // namespace gpr

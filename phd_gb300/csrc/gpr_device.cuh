@@ -632,8 +632,11 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
 // max |eigenvalue| of the GPR system in direction d (system/eig.cpp:8-77):
 // |v_d| + sqrt(max |eig(Xi1 Xi2)|).  Xi1 (4x5) and Xi2 (5x4) are assembled
 // implicitly: Xi = Xi1 Xi2 is formed directly from its nonzero blocks.
+// Xo (m x m, row-major) and l2o, when given, receive Xi and its dominant
+// eigenvalue (for the adjoint's wave-speed derivative).
 template <bool TH>
-GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPar &P) {
+GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPar &P,
+                          double *Xo = nullptr, double *l2o = nullptr) {
   const double *A = q + 5;
   const double r = s.r, ir = s.ir;
   // G = A^T A (row d only needed) and dsigma/dA (state.cpp:43-56):
@@ -697,9 +700,18 @@ GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPa
     X[m - 1][2] = tp * b[2];
     X[m - 1][m - 1] = tp * h;
   }
+  if (Xo) {
+#pragma unroll
+    for (int i = 0; i < m; i++)
+#pragma unroll
+      for (int c = 0; c < m; c++)
+        Xo[i * m + c] = X[i][c];
+  }
   double l2;
   if (!max_eig_laguerre<m>(X, l2))
     l2 = max_abs_eig<m>(X);  // QR fallback: complex or multiple dominant roots
+  if (l2o)
+    *l2o = l2;
   double lam = sqrt(l2);
   double vd = s.v[d];
   return vd > 0 ? vd + lam : lam - vd;

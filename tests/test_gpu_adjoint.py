@@ -170,6 +170,53 @@ def _noisy_state(nx, rng):
     return u0, dx
 
 
+@pytest.mark.parametrize("nvar", [17, 14])
+def test_point_vjp_matches_dual_jacobians(nvar):
+    """The reverse-mode products the backward step uses equal the dual-number
+    Jacobians contracted with the same cotangents."""
+    _cuda()
+    from phd_gb300 import _lib
+    from phd_gb300.adjoint import FIELDS
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    u, dx, _ = _stokes(nx=64)
+    Q = u[:48, :nvar].copy()
+    Q += 0.1 * rng.standard_normal(Q.shape) * (np.abs(Q) + 0.1)
+    Q[:, 0] = np.abs(Q[:, 0]) + 0.5
+    MP = make_par(THETA)
+    V, K, n = nvar, nvar + len(FIELDS), Q.shape[0]
+    Fb = rng.standard_normal((n, V))
+    Sb = rng.standard_normal((n, V))
+    lb = rng.standard_normal(n)
+    c = MP.to_ctypes()
+    pc = ctypes.cast(ctypes.pointer(c), ctypes.c_void_p)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    Qd = dev(Q)
+    JF = torch.zeros(n * K * V, dtype=torch.float64, device="cuda")
+    JS = torch.zeros_like(JF)
+    dl = torch.zeros(n * K, dtype=torch.float64, device="cuda")
+    assert lib.gpr_adj_point_jacobians(ptr(Qd), n, pc, ptr(JF), ptr(JS), ptr(dl), V, None) == 0
+    Fd, Sd, ld = dev(Fb), dev(Sb), dev(lb)
+    qb = torch.zeros(n * V, dtype=torch.float64, device="cuda")
+    thb = torch.zeros(n * len(FIELDS), dtype=torch.float64, device="cuda")
+    assert lib.gpr_adj_point_vjp(ptr(Qd), n, pc, ptr(Fd), ptr(Sd), ptr(ld), ptr(qb), ptr(thb),
+                                 V, None) == 0
+    torch.cuda.synchronize()
+    JF = JF.cpu().numpy().reshape(n, K, V)
+    JS = JS.cpu().numpy().reshape(n, K, V)
+    dl = dl.cpu().numpy().reshape(n, K)
+    want = (np.einsum("nkj,nj->nk", JF, Fb) + np.einsum("nkj,nj->nk", JS, Sb)
+            + dl * lb[:, None])
+    got = np.concatenate([qb.cpu().numpy().reshape(n, V),
+                          thb.cpu().numpy().reshape(n, len(FIELDS))], axis=1)
+    scale = (np.abs(JF).max(axis=2) * np.abs(Fb).max(axis=1)[:, None]
+             + np.abs(JS).max(axis=2) * np.abs(Sb).max(axis=1)[:, None]
+             + np.abs(dl * lb[:, None]) + 1e-300)
+    err = np.abs(got - want) / scale
+    assert err.max() < 1e-12, (np.unravel_index(err.argmax(), err.shape), err.max())
+
+
 def test_one_step_jacobian_matches_finite_differences():
     """The full Jacobian of one step (6 cells x 17 variables, held dt) from
     the backward step, row by row, against central differences column by
