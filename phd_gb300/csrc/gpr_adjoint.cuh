@@ -1355,29 +1355,30 @@ GPR_D void pcache_init(const double *q, const DevPar &P, double wn, double *c, i
 }
 
 // r += (dF/dq)^T Fb + wn (dS/dq)^T mu from the cached primal values: the
-// reverse sweep of point_vjp (HF, HS, no material fields), term by term.
-template <class L>
-GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb,
-                      const double *mu, double *r) {
+// reverse sweep of point_vjp (HF, HS, no material fields), term by term, in
+// the arithmetic type S of the cache (FP64, or FP32 for the correction
+// solves of k_adj_pred_iter).
+template <class L, class S>
+GPR_D void pcache_vjp(const S *c, int ST, S b02, S iG, const S *Fb, const S *mu, S *r) {
   using PC = PCache<L>;
   constexpr bool TH = L::THERMAL;
 #define PCV(k) c[(k) * ST]
-  const double *qc = c + PC::Q * ST;
+  const S *qc = c + PC::Q * ST;
 #define PQ(k) qc[(k) * ST]
-  double A[9];
+  S A[9];
 #pragma unroll
   for (int k = 0; k < 9; k++)
     A[k] = PQ(5 + k);
-  const double v[3] = {PCV(PC::VV), PCV(PC::VV + 1), PCV(PC::VV + 2)};
-  double vb[3], sgb[3], Ab[9], AdGb[9], Jb[3] = {0.0, 0.0, 0.0}, qJb[3] = {0.0, 0.0, 0.0};
-  double q2b[3];
+  const S v[3] = {PCV(PC::VV), PCV(PC::VV + 1), PCV(PC::VV + 2)};
+  S vb[3], sgb[3], Ab[9], AdGb[9], Jb[3] = {S(0), S(0), S(0)}, qJb[3] = {S(0), S(0), S(0)};
+  S q2b[3];
   // flux
-  const double f1 = Fb[1];
+  const S f1 = Fb[1];
   vb[0] = f1 * PCV(PC::Q1PP);
-  vb[1] = 0.0;
-  vb[2] = 0.0;
-  double q1b = f1 * v[0];
-  double pb = f1 * v[0] + Fb[2];
+  vb[1] = S(0);
+  vb[2] = S(0);
+  S q1b = f1 * v[0];
+  S pb = f1 * v[0] + Fb[2];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     sgb[i] = -(f1 * v[i]) - Fb[2 + i];
@@ -1386,7 +1387,7 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
     q2b[i] = Fb[2 + i] * v[0];
   }
   q2b[0] += Fb[0];
-  double Tb = 0.0;
+  S Tb = S(0);
   if (TH) {
     Tb = f1 * PCV(PC::CJ) + Fb[14];
     Jb[0] = f1 * PCV(PC::CA2T);
@@ -1398,7 +1399,7 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    const double f = Fb[5 + 3 * i];
+    const S f = Fb[5 + 3 * i];
 #pragma unroll
     for (int j = 0; j < 3; j++) {
       Ab[3 * i + j] = f * v[j];
@@ -1406,8 +1407,8 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
     }
   }
   // source (wn folded into FSW, COFK, GSW)
-  double fb = 0.0;
-  const double fsw = PCV(PC::FSW);
+  S fb = S(0);
+  const S fsw = PCV(PC::FSW);
 #pragma unroll
   for (int i = 0; i < 9; i++) {
     fb += mu[5 + i] * PCV(PC::ADG + i);
@@ -1417,8 +1418,8 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
   for (int k = 0; k < 9; k++)
     Ab[k] += fb * PCV(PC::COFK + k);
   if (TH) {
-    const double gsw = PCV(PC::GSW);
-    double gb = 0.0;
+    const S gsw = PCV(PC::GSW);
+    S gb = S(0);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       gb += mu[14 + i] * PCV(PC::JJ + i);
@@ -1427,31 +1428,31 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
     Tb -= gb * PCV(PC::GTW);
   }
   // sigma column 0
-  const double sgf = PCV(PC::SGF);
-  double sgfb = 0.0;
+  const S sgf = PCV(PC::SGF);
+  S sgfb = S(0);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     sgfb += sgb[i] * PCV(PC::SGM + i);
-    const double f = sgb[i] * sgf;
+    const S f = sgb[i] * sgf;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       AdGb[3 * k + i] += f * A[3 * k];
       Ab[3 * k] += f * PCV(PC::ADG + 3 * k + i);
     }
   }
-  double rb = -(sgfb * P.b02);
+  S rb = -(sgfb * b02);
   // prim
   pb += Tb * PCV(PC::IRGICV);
-  const double irGb = Tb * PCV(PC::PPICV);
-  const double E1b = pb * PCV(PC::RGM1);
+  const S irGb = Tb * PCV(PC::PPICV);
+  const S E1b = pb * PCV(PC::RGM1);
   rb += pb * PCV(PC::E1GM1);
-  const double ir = PCV(PC::IR);
-  double irb = E1b * PCV(PC::Q1M) + irGb * P.iG;
+  const S ir = PCV(PC::IR);
+  S irb = E1b * PCV(PC::Q1M) + irGb * iG;
   q1b += E1b * ir;
 #pragma unroll
   for (int i = 0; i < 3; i++)
     vb[i] -= E1b * v[i];
-  const double devGsqb = -0.25 * P.b02 * E1b;
+  const S devGsqb = S(-0.25) * b02 * E1b;
   if (TH) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -1461,10 +1462,10 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
     }
   }
   // AdG = A Dm
-  const double D00 = PCV(PC::DM), D11 = PCV(PC::DM + 1), D22 = PCV(PC::DM + 2);
-  const double G01 = PCV(PC::DM + 3), G02 = PCV(PC::DM + 4), G12 = PCV(PC::DM + 5);
-  const double Dm[3][3] = {{D00, G01, G02}, {G01, D11, G12}, {G02, G12, D22}};
-  double Dmb[3][3];
+  const S D00 = PCV(PC::DM), D11 = PCV(PC::DM + 1), D22 = PCV(PC::DM + 2);
+  const S G01 = PCV(PC::DM + 3), G02 = PCV(PC::DM + 4), G12 = PCV(PC::DM + 5);
+  const S Dm[3][3] = {{D00, G01, G02}, {G01, D11, G12}, {G02, G12, D22}};
+  S Dmb[3][3];
 #pragma unroll
   for (int k = 0; k < 3; k++)
 #pragma unroll
@@ -1476,20 +1477,20 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
     for (int k = 0; k < 3; k++)
       Ab[3 * i + k] += AdGb[3 * i] * Dm[k][0] + AdGb[3 * i + 1] * Dm[k][1] +
                        AdGb[3 * i + 2] * Dm[k][2];
-  const double D00b = Dmb[0][0] + devGsqb * 2.0 * D00;
-  const double D11b = Dmb[1][1] + devGsqb * 2.0 * D11;
-  const double D22b = Dmb[2][2] + devGsqb * 2.0 * D22;
-  const double G01b = Dmb[0][1] + Dmb[1][0] + devGsqb * 4.0 * G01;
-  const double G02b = Dmb[0][2] + Dmb[2][0] + devGsqb * 4.0 * G02;
-  const double G12b = Dmb[1][2] + Dmb[2][1] + devGsqb * 4.0 * G12;
-  const double tb = -(D00b + D11b + D22b) * (1.0 / 3.0);
-  const double G00b = D00b + tb, G11b = D11b + tb, G22b = D22b + tb;
+  const S D00b = Dmb[0][0] + devGsqb * S(2) * D00;
+  const S D11b = Dmb[1][1] + devGsqb * S(2) * D11;
+  const S D22b = Dmb[2][2] + devGsqb * S(2) * D22;
+  const S G01b = Dmb[0][1] + Dmb[1][0] + devGsqb * S(4) * G01;
+  const S G02b = Dmb[0][2] + Dmb[2][0] + devGsqb * S(4) * G02;
+  const S G12b = Dmb[1][2] + Dmb[2][1] + devGsqb * S(4) * G12;
+  const S tb = -(D00b + D11b + D22b) * S(1.0 / 3.0);
+  const S G00b = D00b + tb, G11b = D11b + tb, G22b = D22b + tb;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const double a0 = A[3 * k], a1 = A[3 * k + 1], a2 = A[3 * k + 2];
-    Ab[3 * k] += 2.0 * G00b * a0 + G01b * a1 + G02b * a2;
-    Ab[3 * k + 1] += 2.0 * G11b * a1 + G01b * a0 + G12b * a2;
-    Ab[3 * k + 2] += 2.0 * G22b * a2 + G02b * a0 + G12b * a1;
+    const S a0 = A[3 * k], a1 = A[3 * k + 1], a2 = A[3 * k + 2];
+    Ab[3 * k] += S(2) * G00b * a0 + G01b * a1 + G02b * a2;
+    Ab[3 * k + 1] += S(2) * G11b * a1 + G01b * a0 + G12b * a2;
+    Ab[3 * k + 2] += S(2) * G22b * a2 + G02b * a0 + G12b * a1;
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -1516,7 +1517,8 @@ GPR_D void pcache_vjp(const double *c, int ST, const DevPar &P, const double *Fb
 
 constexpr int ADJ_PRED_IT = 100;
 constexpr double ADJ_PRED_TOL = 1e-11;
-constexpr int ADJ_IT_T = 64;  // threads (16 cells) per block of k_adj_pred_iter
+constexpr int ADJ_INNER = 6;  // FP32 iterations per correction solve
+constexpr int ADJ_IT_T = 32;  // threads (8 cells) per block of k_adj_pred_iter
 
 // max(a, |d|) on the IEEE bit patterns of non-negative doubles (integer
 // order equals numeric order there; NaN patterns sort above every number)
@@ -1525,6 +1527,81 @@ GPR_D unsigned long long absmax_bits(unsigned long long a, double d) {
   return b > a ? b : a;
 }
 
+template <class S, int V> GPR_D void shfl_vec_t(const S *src, S *dst, int lanemask) {
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    dst[k] = __shfl_xor_sync(0xffffffffu, src[k], lanemask);
+}
+
+// Per-lane coefficients of the transposed Picard map at node (t, i).
+template <class S> struct TCoef {
+  S fa, fo, xa, xo, ga, go, dt, wn, iq0, v0, v1, v2, b02, iG;
+};
+
+// y = DG_U^-T (z0 + dt R^T x) at this lane's node, where R^T x = (dR/dq)^T
+// x: the F part with cotangent -wti sum_i DG_DER[i][m] x_i, the S part with
+// cotangent wn x, and -wn B(v)^T x through the node derivative x_ti and
+// through v(q).  z0 = nullptr for the homogeneous map (z0 = 0).  All lanes
+// of the warp take part (shuffles with the node partners g ^ 1, g ^ 2).
+template <class L, class S>
+GPR_D void tmap(const S *x, const double *z0, const S *pc, const S *xs, int ST, bool active,
+                const TCoef<S> &k, S *y) {
+  constexpr int V = L::V;
+  S Fb[V], r[V], tmp[V];
+  shfl_vec_t<S, V>(x, tmp, 1);
+#pragma unroll
+  for (int j = 0; j < V; j++) {
+    Fb[j] = k.fa * x[j] + k.fo * tmp[j];
+    r[j] = S(0);
+  }
+  if (active)
+    pcache_vjp<L, S>(pc, ST, k.b02, k.iG, Fb, x, r);
+  S xb[6], xq[6];
+#pragma unroll
+  for (int rr = 0; rr < 3; rr++) {
+    xb[2 * rr] = -k.v1 * x[5 + 3 * rr] + k.v0 * x[6 + 3 * rr];
+    xb[2 * rr + 1] = -k.v2 * x[5 + 3 * rr] + k.v0 * x[7 + 3 * rr];
+  }
+  S vb0 = S(0), vb1 = S(0), vb2 = S(0);
+#pragma unroll
+  for (int rr = 0; rr < 3; rr++) {
+    const S x6 = xs[(2 * rr) * ST], x7 = xs[(2 * rr + 1) * ST];
+    vb0 += x6 * x[6 + 3 * rr] + x7 * x[7 + 3 * rr];
+    vb1 -= x6 * x[5 + 3 * rr];
+    vb2 -= x7 * x[5 + 3 * rr];
+  }
+  const S wq = k.wn * k.iq0;
+  r[0] += wq * (vb0 * k.v0 + vb1 * k.v1 + vb2 * k.v2);
+  r[2] -= wq * vb0;
+  r[3] -= wq * vb1;
+  r[4] -= wq * vb2;
+#pragma unroll
+  for (int m = 0; m < 6; m++)
+    xq[m] = __shfl_xor_sync(0xffffffffu, xb[m], 1);
+#pragma unroll
+  for (int rr = 0; rr < 3; rr++)
+#pragma unroll
+    for (int m = 0; m < 2; m++)
+      r[6 + 3 * rr + m] += k.xa * xb[2 * rr + m] + k.xo * xq[2 * rr + m];
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    r[j] = z0 ? S(z0[j]) + k.dt * r[j] : k.dt * r[j];
+  shfl_vec_t<S, V>(r, tmp, 2);
+#pragma unroll
+  for (int j = 0; j < V; j++)
+    y[j] = k.ga * r[j] + k.go * tmp[j];
+}
+
+// Mixed-precision iterative refinement of the fixed point mu = T(mu),
+// T(mu) = DG_U^-T (qbar + dt R^T mu) (a published technique: the defect in
+// the working precision, the correction equation in a cheaper one).  Each
+// outer step forms the defect d = T(mu) - mu in FP64 (one FP64 evaluation,
+// the convergence test |d| <= tol |T(mu)| as in the plain iteration), then
+// solves the correction equation e = d + T_0(e) (T_0: T without qbar) by
+// ADJ_INNER FP32 iterations over an FP32 copy of the primal cache, and sets
+// mu += e.  The FP32 solve costs little beside the FP64 evaluation on this
+// GPU's FP64 pipe and brings ~6 digits per outer step; a non-finite FP32
+// correction falls back to the plain step mu = T(mu).
 template <class L>
 __global__ void __launch_bounds__(ADJ_IT_T) k_adj_pred_iter(
     const double *__restrict__ qh, const double *__restrict__ qbar, long nb,
@@ -1532,8 +1609,11 @@ __global__ void __launch_bounds__(ADJ_IT_T) k_adj_pred_iter(
     Consts C, Batch B) {
   constexpr int V = L::V, NC = PCache<L>::N, ST = ADJ_IT_T;
   __shared__ double cache[(NC + 6) * ST];
+  __shared__ float cachef[(NC + 6) * ST];
   double *pc = cache + threadIdx.x;
   double *xs = cache + NC * ST + threadIdx.x;  // x at 6, 7, 9, 10, 12, 13
+  float *pcf = cachef + threadIdx.x;
+  float *xsf = cachef + NC * ST + threadIdx.x;
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int g = threadIdx.x % 4;
   const long c = gt / 4;
@@ -1547,89 +1627,71 @@ __global__ void __launch_bounds__(ADJ_IT_T) k_adj_pred_iter(
   const bool active = valid && dt != 0.0;
   const double wn = C.w[t] * C.w[i], wno = C.w[t] * C.w[1 - i], wti = C.w[t] * idx;
   // node data: the primal cache, x_ti = idx sum_m DERVALS[i][m] q_tm
-  double mu[V], qb[V], tmp[V];
+  double mu[V], qb[V], y[V];
   {
     double q[V];
 #pragma unroll
     for (int k = 0; k < V; k++)
       q[k] = qh[(cc * 4 + g) * V + k];
-    shfl_vec<V>(q, tmp, 1);
+    shfl_vec<V>(q, y, 1);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
       for (int m = 0; m < 2; m++) {
         int k = 6 + 3 * r + m;
-        xs[(2 * r + m) * ST] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * tmp[k]);
+        xs[(2 * r + m) * ST] = idx * (C.derv[i][i] * q[k] + C.derv[i][1 - i] * y[k]);
       }
     pcache_init<L>(q, P, wn, pc, ST);
   }
+  for (int k = 0; k < NC + 6; k++)
+    pcf[k * ST] = (float)pc[k * ST];
 #pragma unroll
   for (int k = 0; k < V; k++) {
     qb[k] = active ? qbar[(cc * 4 + g) * V + k] : 0.0;
     mu[k] = 0.0;
   }
-  const double fa = -wti * C.dgder[i][i], fo = -wti * C.dgder[1 - i][i];
-  const double xa = -wn * idx * C.derv[i][i], xo = -wno * idx * C.derv[1 - i][i];
-  const double ga = C.dgmatinv[t][t] / C.w[i], go = C.dgmatinv[1 - t][t] / C.w[i];
-  const double iq0 = pc[PCache<L>::IR * ST];
-  const double v[3] = {pc[PCache<L>::VV * ST], pc[(PCache<L>::VV + 1) * ST],
-                       pc[(PCache<L>::VV + 2) * ST]};
+  TCoef<double> kd;
+  kd.fa = -wti * C.dgder[i][i];
+  kd.fo = -wti * C.dgder[1 - i][i];
+  kd.xa = -wn * idx * C.derv[i][i];
+  kd.xo = -wno * idx * C.derv[1 - i][i];
+  kd.ga = C.dgmatinv[t][t] / C.w[i];
+  kd.go = C.dgmatinv[1 - t][t] / C.w[i];
+  kd.dt = dt;
+  kd.wn = wn;
+  kd.iq0 = pc[PCache<L>::IR * ST];
+  kd.v0 = pc[PCache<L>::VV * ST];
+  kd.v1 = pc[(PCache<L>::VV + 1) * ST];
+  kd.v2 = pc[(PCache<L>::VV + 2) * ST];
+  kd.b02 = P.b02;
+  kd.iG = P.iG;
+  TCoef<float> kf;
+  kf.fa = (float)kd.fa;
+  kf.fo = (float)kd.fo;
+  kf.xa = (float)kd.xa;
+  kf.xo = (float)kd.xo;
+  kf.ga = (float)kd.ga;
+  kf.go = (float)kd.go;
+  kf.dt = (float)kd.dt;
+  kf.wn = (float)kd.wn;
+  kf.iq0 = (float)kd.iq0;
+  kf.v0 = (float)kd.v0;
+  kf.v1 = (float)kd.v1;
+  kf.v2 = (float)kd.v2;
+  kf.b02 = (float)kd.b02;
+  kf.iG = (float)kd.iG;
   bool conv = !active, done = !active;
   int nit = 0;
   for (int it = 0; it < ADJ_PRED_IT; it++) {
     if (__all_sync(0xffffffffu, done))
       break;
     nit += done ? 0 : 1;
-    // F cotangent -wti sum_i DG_DER[i][m] mu_i; S cotangent wn mu (wn in the cache)
-    double Fb[V], r[V];
-    shfl_vec<V>(mu, tmp, 1);
-#pragma unroll
-    for (int k = 0; k < V; k++) {
-      Fb[k] = fa * mu[k] + fo * tmp[k];
-      r[k] = 0.0;
-    }
-    if (active)
-      pcache_vjp<L>(pc, ST, P, Fb, mu, r);
-    // -wn B(v)^T mu through x (coupling the spatial nodes) and through v(q)
-    double xb[6], xq[6];
-#pragma unroll
-    for (int rr = 0; rr < 3; rr++) {
-      xb[2 * rr] = -v[1] * mu[5 + 3 * rr] + v[0] * mu[6 + 3 * rr];
-      xb[2 * rr + 1] = -v[2] * mu[5 + 3 * rr] + v[0] * mu[7 + 3 * rr];
-    }
-    double vb0 = 0.0, vb1 = 0.0, vb2 = 0.0;
-#pragma unroll
-    for (int rr = 0; rr < 3; rr++) {
-      const double x6 = xs[(2 * rr) * ST], x7 = xs[(2 * rr + 1) * ST];
-      vb0 += x6 * mu[6 + 3 * rr] + x7 * mu[7 + 3 * rr];
-      vb1 -= x6 * mu[5 + 3 * rr];
-      vb2 -= x7 * mu[5 + 3 * rr];
-    }
-    const double wq = wn * iq0;
-    r[0] += wq * (vb0 * v[0] + vb1 * v[1] + vb2 * v[2]);
-    r[2] -= wq * vb0;
-    r[3] -= wq * vb1;
-    r[4] -= wq * vb2;
-#pragma unroll
-    for (int m = 0; m < 6; m++)
-      xq[m] = __shfl_xor_sync(0xffffffffu, xb[m], 1);
-#pragma unroll
-    for (int rr = 0; rr < 3; rr++)
-#pragma unroll
-      for (int m = 0; m < 2; m++)
-        r[6 + 3 * rr + m] += xa * xb[2 * rr + m] + xo * xq[2 * rr + m];
-    // z = qbar + dt r; mu = DG_U^-T z (time coupling)
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      r[k] = qb[k] + dt * r[k];
-    shfl_vec<V>(r, tmp, 2);
+    tmap<L, double>(mu, qb, pc, xs, ST, active, kd, y);
     unsigned long long ddb = 0, scb = 0;
 #pragma unroll
     for (int k = 0; k < V; k++) {
-      const double mn = ga * r[k] + go * tmp[k];
-      ddb = absmax_bits(ddb, mn - mu[k]);
-      scb = absmax_bits(scb, mn);
-      tmp[k] = mn;
+      ddb = absmax_bits(ddb, y[k] - mu[k]);
+      scb = absmax_bits(scb, y[k]);
     }
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) {
@@ -1638,16 +1700,45 @@ __global__ void __launch_bounds__(ADJ_IT_T) k_adj_pred_iter(
       ddb = a > ddb ? a : ddb;
       scb = b > scb ? b : scb;
     }
+    bool upd = false;
     if (!done) {
-#pragma unroll
-      for (int k = 0; k < V; k++)
-        mu[k] = tmp[k];
       if (scb > 0x7ff0000000000000ULL) {  // NaN
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          mu[k] = y[k];
         done = true;
       } else if (__longlong_as_double((long long)ddb) <=
                  ADJ_PRED_TOL * __longlong_as_double((long long)scb)) {
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          mu[k] = y[k];
         conv = true;
         done = true;
+      } else {
+        upd = true;
+      }
+    }
+    if (__any_sync(0xffffffffu, upd)) {
+      float df[V], e[V], te[V];
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        df[k] = (float)(y[k] - mu[k]);
+        e[k] = df[k];
+      }
+      for (int j = 1; j < ADJ_INNER; j++) {
+        tmap<L, float>(e, nullptr, pcf, xsf, ST, active, kf, te);
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          e[k] = df[k] + te[k];
+      }
+      if (upd) {
+        bool fin = true;
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          fin = fin && isfinite(e[k]);
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          mu[k] = fin ? mu[k] + (double)e[k] : y[k];
       }
     }
   }
