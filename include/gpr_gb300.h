@@ -134,6 +134,21 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     int flux, const gpr_par *par, const uint8_t *mask,
                     double *scratch, int nvar, void *stream);
 
+/* The two passes of gpr_fv_launcher as separate calls, in place on u:
+ * gpr_fv_centers replaces solvers.fv.centers1 / centers2 (fv.h:7-10,
+ * fv.cpp:11-109: the space-time volume term of the sources and
+ * non-conservative products; no scratch), gpr_fv_interfs replaces
+ * solvers.fv.interfs1 / interfs2 (fv.h:12-15, fv.cpp:111-279: the interface
+ * fluxes and path integrals; scratch as gpr_fv_launcher).  The reference's
+ * separate nx / ny / dx / dy arguments are nX[ndim] and dX[ndim] here. */
+int gpr_fv_centers(double *u, const double *qh, const int32_t *nX, double dt,
+                   const double *dX, int ndim, int sources, int time_dg,
+                   const gpr_par *par, const uint8_t *mask, int nvar, void *stream);
+int gpr_fv_interfs(double *u, const double *qh, const int32_t *nX, double dt,
+                   const double *dX, int ndim, int time_dg, int flux,
+                   const gpr_par *par, const uint8_t *mask, double *scratch,
+                   int nvar, void *stream);
+
 /* The face pass of gpr_fv_launcher alone (interfs1/interfs2, fv.cpp:111-279):
  * writes, per face and direction, the contribution subtracted from the left
  * cell (fb[face][0][V]) and from the right cell (fb[face][1][V]) into fb,
@@ -417,6 +432,14 @@ int gpr_Bdot(const double *Q, const double *x, double *out, int64_t count,
  * (eig.cpp:66-77). */
 int gpr_max_abs_eigs(const double *Q, double *out, int64_t count, int d,
                      const gpr_par *par, int nvar, void *stream);
+/* out[count][V][V] (row = equation) = the system matrix dF_d/dQ + B_d of
+ * the quasi-linear form along d (system/equations.cpp:169-177). */
+int gpr_system_matrix(const double *Q, double *out, int64_t count, int d,
+                      const gpr_par *par, int nvar, void *stream);
+/* out[count][m][m] = Xi1 Xi2 along d (eig.cpp:55-64), m = 4 with heat
+ * conduction (V = 17), else 3. */
+int gpr_thermo_acoustic_tensor(const double *Q, double *out, int64_t count, int d,
+                               const gpr_par *par, int nvar, void *stream);
 /* Interface dissipation / jump terms (solvers/fv/fluxes.cpp:9-75):
  * out[count][V] = D_flux(qL, qR) including F(qL)+F(qR), and
  * bout[count][V] = Bint(qL, qR). */

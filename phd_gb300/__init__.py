@@ -30,7 +30,8 @@ options = SimpleNamespace(N=lambda: 2, NV=lambda: 17, VISCOUS=lambda: True,
 classes = SimpleNamespace(Par=Par)
 
 system = SimpleNamespace(flux=api.flux, source=api.source, Bdot=api.Bdot,
-                         max_abs_eigs=api.max_abs_eigs,
+                         max_abs_eigs=api.max_abs_eigs, system_matrix=api.system_matrix,
+                         thermo_acoustic_tensor=api.thermo_acoustic_tensor,
                          multi=SimpleNamespace(left_star_state=_multi.left_star_state,
                                                distance=_multi.distance))
 
@@ -71,8 +72,9 @@ def _renorm_distortion(u, MPs):
 solvers = SimpleNamespace(
     weno=SimpleNamespace(weno_launcher=api.weno_launcher),
     dg=SimpleNamespace(predictor=api.predictor),
-    fv=SimpleNamespace(fv_launcher=api.fv_launcher, D_RUS=api.D_RUS, D_ROE=api.D_ROE,
-                       D_OSH=api.D_OSH, Bint=api.Bint),
+    fv=SimpleNamespace(fv_launcher=api.fv_launcher, centers1=api.centers1,
+                       centers2=api.centers2, interfs1=api.interfs1, interfs2=api.interfs2,
+                       D_RUS=api.D_RUS, D_ROE=api.D_ROE, D_OSH=api.D_OSH, Bint=api.Bint),
     split=SimpleNamespace(ode_launcher=api.ode_launcher, midstepper=api.midstepper),
     ader_stepper=api.ader_stepper,
     ader_stepper_para=api.ader_stepper_para,

@@ -78,6 +78,8 @@ SIGNATURES = {
     "gpr_fv_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_fv_launcher": (_I, [_P, _P, _P, _D, _P, _I, _I, _I, _I, _P, _P, _P, _I, _P]),
     "gpr_fv_face_fluxes": (_I, [_P, _P, _D, _P, _I, _I, _I, _P, _P, _P, _I, _P]),
+    "gpr_fv_centers": (_I, [_P, _P, _P, _D, _P, _I, _I, _I, _P, _P, _I, _P]),
+    "gpr_fv_interfs": (_I, [_P, _P, _P, _D, _P, _I, _I, _I, _P, _P, _P, _I, _P]),
     "gpr_timestep_scratch_doubles": (_I, [_I64]),
     "gpr_timestep": (_I, [_P, _I64, _P, _I, _D, _D, _D, _I, _P, _P, _P, _I, _P]),
     "gpr_renorm_distortion": (_I, [_P, _I64, _P, _I, _P]),
@@ -123,6 +125,8 @@ SIGNATURES = {
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),
     "gpr_max_abs_eigs": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
+    "gpr_system_matrix": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
+    "gpr_thermo_acoustic_tensor": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_interface_terms": (_I, [_P, _P, _P, _P, _I64, _I, _I, _P, _I, _P]),
 }
 

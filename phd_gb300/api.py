@@ -171,6 +171,49 @@ def fv_launcher(u, rec, nX, dt, dX, SOURCES, TIME, FLUX, MP, mask):
     return u
 
 
+def _fv_part(u, rec, nX, dt, dX, SOURCES, TIME, FLUX, MP, mask, part):
+    lib = _lib.load()
+    nXa, pn = _i32(nX)
+    set_grid(nXa)
+    dXa, pd = _f64(dX)
+    nd = nXa.size
+    V = _nvar(u, int(np.prod(nXa)))
+    pm, _ = _mask_ptr(mask, int(np.prod(nXa + 2)))
+    c, pp = _par(MP)
+    if part == "centers":
+        _lib.check(lib.gpr_fv_centers(_dev(u, "u"), _dev(rec, "rec"), pn, float(dt), pd, nd,
+                                      int(bool(SOURCES)), int(bool(TIME)), pp, pm, V,
+                                      _stream()), "centers")
+    else:
+        scr = _scratch(lib.gpr_fv_scratch_doubles(pn, nd, V), u)
+        _lib.check(lib.gpr_fv_interfs(_dev(u, "u"), _dev(rec, "rec"), pn, float(dt), pd, nd,
+                                      int(bool(TIME)), int(FLUX), pp, pm, _dev(scr, "s"), V,
+                                      _stream()), "interfs")
+    return u
+
+
+def centers1(u, rec, nx, dt, dx, SOURCES, TIME, MP, mask):
+    """GPRpy.solvers.fv.centers1 (solvers/fv/fv.h:7): the volume term of the
+    FV update (sources and non-conservative products), in place on u."""
+    return _fv_part(u, rec, [nx], dt, [dx], SOURCES, TIME, 0, MP, mask, "centers")
+
+
+def centers2(u, rec, nx, ny, dt, dx, dy, SOURCES, TIME, MP, mask):
+    """GPRpy.solvers.fv.centers2 (solvers/fv/fv.h:9)."""
+    return _fv_part(u, rec, [nx, ny], dt, [dx, dy], SOURCES, TIME, 0, MP, mask, "centers")
+
+
+def interfs1(u, rec, nx, dt, dx, TIME, FLUX, MP, mask):
+    """GPRpy.solvers.fv.interfs1 (solvers/fv/fv.h:12): the interface terms
+    of the FV update (fluxes and path integrals), in place on u."""
+    return _fv_part(u, rec, [nx], dt, [dx], False, TIME, FLUX, MP, mask, "interfs")
+
+
+def interfs2(u, rec, nx, ny, dt, dx, dy, TIME, FLUX, MP, mask):
+    """GPRpy.solvers.fv.interfs2 (solvers/fv/fv.h:14)."""
+    return _fv_part(u, rec, [nx, ny], dt, [dx, dy], False, TIME, FLUX, MP, mask, "interfs")
+
+
 def ader_stepper(u, ub, nX, dt, dX, STIFF, FLUX, MP, mask, status=None):
     """GPRpy.solvers.ader_stepper (solvers/steppers.cpp:10-22)."""
     lib = _lib.load()
@@ -352,6 +395,27 @@ def max_abs_eigs(Q, d, MP):
                       device=Q.device)
     _lib.check(lib.gpr_max_abs_eigs(_dev(Q, "Q"), _dev(out, "out"), count, int(d), pp, V,
                                     _stream()), "max_abs_eigs")
+    return out
+
+
+def system_matrix(Q, d, MP):
+    """GPRpy.system.system_matrix (system/equations.cpp:169-177): dF_d/dQ +
+    B_d, [..., V, V] with rows the equations."""
+    lib, Q, V, count, pp = _pointwise(None, Q, MP)
+    out = torch.empty(Q.shape[:-1] + (V, V), dtype=torch.float64, device=Q.device)
+    _lib.check(lib.gpr_system_matrix(_dev(Q, "Q"), _dev(out, "out"), count, int(d), pp, V,
+                                     _stream()), "system_matrix")
+    return out
+
+
+def thermo_acoustic_tensor(Q, d, MP):
+    """GPRpy.system.thermo_acoustic_tensor (system/eig.cpp:55-64): Xi1 Xi2
+    along d, [..., m, m] with m = 4 for V = 17 (heat conduction), else 3."""
+    lib, Q, V, count, pp = _pointwise(None, Q, MP)
+    m = 4 if V == 17 else 3
+    out = torch.empty(Q.shape[:-1] + (m, m), dtype=torch.float64, device=Q.device)
+    _lib.check(lib.gpr_thermo_acoustic_tensor(_dev(Q, "Q"), _dev(out, "out"), count, int(d),
+                                              pp, V, _stream()), "thermo_acoustic_tensor")
     return out
 
 

@@ -111,7 +111,7 @@ template <class L> struct Adj {
     k_faces1d<L, true><<<blocks(b.nf * NN, 128), 128, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
                                                                 nullptr, 1.0, 1, P0, C, B);
     k_cells<L, 1, true><<<blocks(b.nu * NN * NN, 128), 128, 0, st>>>(
-        u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B);
+        u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B, FV_BOTH);
     if (tape && cudaMemcpyAsync(tape + tl.o_up, u, sizeof(double) * b.nu * V,
                                 cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       return GPR_E_CUDA;

@@ -151,6 +151,26 @@ int gpr_max_abs_eigs(const double *Q, double *out, int64_t count, int d, const g
   DISPATCH(nvar, O::pointwise(3, Q, nullptr, out, nullptr, count, d, 0, P, S(stream)))
 }
 
+int gpr_system_matrix(const double *Q, double *out, int64_t count, int d, const gpr_par *par,
+                      int nvar, void *stream) {
+  if (!Q || !out || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(5, Q, nullptr, out, nullptr, count, d, 0, P, S(stream)))
+}
+
+int gpr_thermo_acoustic_tensor(const double *Q, double *out, int64_t count, int d,
+                               const gpr_par *par, int nvar, void *stream) {
+  if (!Q || !out || count < 0 || d < 0 || d > 2 || !par)
+    return GPR_E_ARG;
+  if (count == 0)
+    return GPR_OK;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::pointwise(6, Q, nullptr, out, nullptr, count, d, 0, P, S(stream)))
+}
+
 int gpr_interface_terms(const double *qL, const double *qR, double *out, double *bout,
                         int64_t count, int d, int flux, const gpr_par *par, int nvar,
                         void *stream) {
@@ -214,6 +234,28 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
   DevPar P = make_devpar(*par);
   DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, sources, time_dg, P, mask, scratch,
                        S(stream), flux))
+}
+
+int gpr_fv_centers(double *u, const double *qh, const int32_t *nX, double dt,
+                   const double *dX, int ndim, int sources, int time_dg, const gpr_par *par,
+                   const uint8_t *mask, int nvar, void *stream) {
+  if (!u || !qh || !dX || !par || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, sources, time_dg, P, mask, nullptr,
+                       S(stream), GPR_FLUX_RUSANOV, 1))
+}
+
+int gpr_fv_interfs(double *u, const double *qh, const int32_t *nX, double dt,
+                   const double *dX, int ndim, int time_dg, int flux, const gpr_par *par,
+                   const uint8_t *mask, double *scratch, int nvar, void *stream) {
+  if (!u || !qh || !dX || !par || !scratch || !check_grid(nX, ndim))
+    return GPR_E_ARG;
+  if (int rc = check_flux(flux, ndim))
+    return rc;
+  DevPar P = make_devpar(*par);
+  DISPATCH(nvar, O::fv(u, qh, nX, dt, nullptr, dX, ndim, 0, time_dg, P, mask, scratch,
+                       S(stream), flux, 2))
 }
 
 int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt, const double *dX,

@@ -984,15 +984,20 @@ __global__ void __launch_bounds__(128) k_faces2d(
   }
 }
 
+// Parts of the FV update k_cells applies: the volume term (centers1 /
+// centers2, fv.cpp:11-109) and the face contributions (interfs1 / interfs2,
+// fv.cpp:111-279); fv_launcher applies both.
+constexpr int FV_CENTERS = 1, FV_INTERFS = 2, FV_BOTH = 3;
+
 // Cell pass: one thread per (cell, space-time node): the volume term
 // w_t w_s (S - B dq/dx [- B dq/dy]) (fv.cpp:11-109), reduced over the cell's
-// NP lanes, then u += volume - face contributions.
+// NP lanes, then u += volume - face contributions (the parts selected).
 template <class L, int ND, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_cells(
     double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
     const double *__restrict__ fby, long nx, int ny, const uint8_t *__restrict__ mask,
     double dt, const double *__restrict__ dt_dev, double dx, double dy, int sources,
-    int time_dg, DevPar Pv, Consts C, Batch B) {
+    int time_dg, DevPar Pv, Consts C, Batch B, int parts) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;
   constexpr int NP = NN * NS;
@@ -1031,52 +1036,58 @@ __global__ void __launch_bounds__(128) k_cells(
   double q[V], other[V], dq[V], acc[V];
 #pragma unroll
   for (int k = 0; k < V; k++)
-    q[k] = qc[k];
-  Prim<L::THERMAL> s;
-  prim<L::THERMAL>(q, P, s);
-  if (sources)
-    source<L::THERMAL, V>(q, s, P, acc);
-  else {
+    acc[k] = 0.0;
+  if (parts & FV_CENTERS) {
 #pragma unroll
     for (int k = 0; k < V; k++)
-      acc[k] = 0.0;
-  }
-  shfl_vec<V>(q, other, XB);
-  {
-    double a = C.derv[i][i], b = C.derv[i][1 - i];
+      q[k] = qc[k];
+    Prim<L::THERMAL> s;
+    prim<L::THERMAL>(q, P, s);
+    if (sources)
+      source<L::THERMAL, V>(q, s, P, acc);
+    else {
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      dq[k] = a * q[k] + b * other[k];
-    double bd[V];
-    bdot<V, L::LSET>(s.v, dq, 0, bd);
+      for (int k = 0; k < V; k++)
+        acc[k] = 0.0;
+    }
+    shfl_vec<V>(q, other, XB);
+    {
+      double a = C.derv[i][i], b = C.derv[i][1 - i];
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      acc[k] -= bd[k] * idx;
-  }
-  if (ND == 2) {
-    shfl_vec<V>(q, other, YB);
-    double a = C.derv[j][j], b = C.derv[j][1 - j];
+      for (int k = 0; k < V; k++)
+        dq[k] = a * q[k] + b * other[k];
+      double bd[V];
+      bdot<V, L::LSET>(s.v, dq, 0, bd);
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      dq[k] = a * q[k] + b * other[k];
-    double bd[V];
-    bdot<V, L::LSET>(s.v, dq, 1, bd);
+      for (int k = 0; k < V; k++)
+        acc[k] -= bd[k] * idx;
+    }
+    if (ND == 2) {
+      shfl_vec<V>(q, other, YB);
+      double a = C.derv[j][j], b = C.derv[j][1 - j];
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      acc[k] -= bd[k] * idy;
-  }
-  double wt = time_dg ? dt * C.w[t] : dt;
-  double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
+      for (int k = 0; k < V; k++)
+        dq[k] = a * q[k] + b * other[k];
+      double bd[V];
+      bdot<V, L::LSET>(s.v, dq, 1, bd);
 #pragma unroll
-  for (int k = 0; k < V; k++) {
-    double x = live ? wn * acc[k] : 0.0;
+      for (int k = 0; k < V; k++)
+        acc[k] -= bd[k] * idy;
+    }
+    double wt = time_dg ? dt * C.w[t] : dt;
+    double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
 #pragma unroll
-    for (int o = 1; o < NP; o <<= 1)
-      x += __shfl_xor_sync(0xffffffffu, x, o);
-    acc[k] = x;
+    for (int k = 0; k < V; k++) {
+      double x = live ? wn * acc[k] : 0.0;
+#pragma unroll
+      for (int o = 1; o < NP; o <<= 1)
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+      acc[k] = x;
+    }
   }
   if (!valid || g != 0 || !active)
     return;
+  const bool faces = parts & FV_INTERFS;
   double *uc = u + cc * V;
   if (ND == 1) {
     // face ci: R part, face ci+1: L part (fv.cpp:143-146)
@@ -1087,9 +1098,9 @@ __global__ void __launch_bounds__(128) k_cells(
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double x = uc[k] + acc[k];
-      if (okr)
+      if (faces && okr)
         x -= fr[k];
-      if (okl)
+      if (faces && okl)
         x -= fl[V + k];
       uc[k] = x;
     }
@@ -1103,10 +1114,12 @@ __global__ void __launch_bounds__(128) k_cells(
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double x = uc[k] + acc[k];
-      x -= fbx[fxl * 2 * V + k];
-      x -= fbx[fxr * 2 * V + V + k];
-      x -= fby[fyl * 2 * V + k];
-      x -= fby[fyr * 2 * V + V + k];
+      if (faces) {
+        x -= fbx[fxl * 2 * V + k];
+        x -= fbx[fxr * 2 * V + V + k];
+        x -= fby[fyl * 2 * V + k];
+        x -= fby[fyr * 2 * V + V + k];
+      }
       uc[k] = x;
     }
   }

@@ -56,8 +56,9 @@ long Ops15::fv_scratch(const int32_t *nX, int nd) {
 int Ops15::fv(double *u, const double *qh, const int32_t *nX, double dt,
                 const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
                 const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st,
-                int flux) {
-  return Ops<L15>::fv(u, qh, nX, dt, dt_dev, dX, nd, sources, time_dg, P, mask, scratch, st, flux);
+                int flux, int parts) {
+  return Ops<L15>::fv(u, qh, nX, dt, dt_dev, dX, nd, sources, time_dg, P, mask, scratch, st, flux,
+                      parts);
 }
 
 int Ops15::faces(const double *qh, const int32_t *nX, double dt, const double *dX, int nd,

@@ -47,6 +47,28 @@ __global__ void k_pointwise(int what, const double *__restrict__ Q, const double
   case 3:
     out[c] = max_abs_eigs<L::THERMAL>(q, s, d, P);
     return;
+  case 5: {  // system_matrix along d through the x form (axis_swap)
+    double pq[V], M[V * V];
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      pq[k] = q[axis_swap<L>(k, d)];
+    Prim<L::THERMAL> ps;
+    prim<L::THERMAL>(pq, P, ps);
+    system_matrix<L::THERMAL, V>(pq, ps, P, M);
+    for (int a = 0; a < V; a++)
+      for (int b = 0; b < V; b++)
+        out[(c * V + a) * V + b] = M[axis_swap<L>(a, d) * V + axis_swap<L>(b, d)];
+    return;
+  }
+  case 6: {  // thermo_acoustic_tensor: Xi1 Xi2 along d
+    constexpr int m = L::THERMAL ? 4 : 3;
+    double X[m * m], l2;
+    max_abs_eigs<L::THERMAL>(q, s, d, P, X, &l2);
+#pragma unroll
+    for (int e = 0; e < m * m; e++)
+      out[c * m * m + e] = X[e];
+    return;
+  }
   default: {
     double qr[V], b[V];
 #pragma unroll
@@ -202,15 +224,20 @@ template <class L> struct Ops {
     return 2L * (nX[0] + 1) * (nX[1] + 1) * 2 * V;
   }
 
+  // parts: FV_BOTH (fv_launcher), FV_CENTERS (centers1/2: the volume term,
+  // no scratch needed) or FV_INTERFS (interfs1/2: the face terms).
   static int fv(double *u, const double *qh, const int32_t *nX, double dt,
                 const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
                 const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st,
-                int flux = GPR_FLUX_RUSANOV) {
+                int flux = GPR_FLUX_RUSANOV, int parts = FV_BOTH) {
     const Consts &C = consts();
     int nx = nX[0];
+    const bool faces = parts & FV_INTERFS;
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
-      if (flux == GPR_FLUX_RUSANOV)
+      if (!faces)
+        ;
+      else if (flux == GPR_FLUX_RUSANOV)
         k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
                                                        dt_dev, dX[0], time_dg, P, C, Batch{});
       else
@@ -219,13 +246,14 @@ template <class L> struct Ops {
       long nc = (long)nx * NN * NN;
       k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
                                                       dt_dev, dX[0], 1.0, sources, time_dg, P,
-                                                      C, Batch{});
+                                                      C, Batch{}, parts);
       return cuda_rc();
     }
     int ny = nX[1];
     long nf = (long)(nx + 1) * (ny + 1);
-    double *fbx = scratch, *fby = scratch + nf * 2 * V;
-    if (flux == GPR_FLUX_RUSANOV) {
+    double *fbx = scratch, *fby = faces ? scratch + nf * 2 * V : nullptr;
+    if (!faces) {
+    } else if (flux == GPR_FLUX_RUSANOV) {
       k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
                                                                dt_dev, dX[0], dX[1], time_dg, P,
                                                                C);
@@ -239,7 +267,7 @@ template <class L> struct Ops {
     long nc = (long)nx * ny * NN * NN * NN;
     k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
                                                     dX[0], dX[1], sources, time_dg, P, C,
-                                                    Batch{});
+                                                    Batch{}, parts);
     return cuda_rc();
   }
 
@@ -482,7 +510,8 @@ template <class L> struct Ops {
       k_faces1d<L, true><<<blocks(b.nf * NN, 128), 128, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
                                                                   nullptr, 1.0, 1, P0, C, B);
       k_cells<L, 1, true><<<blocks(b.nu * NN * NN, 128), 128, 0, st>>>(
-          u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B);
+          u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B,
+          FV_BOTH);
       k_b_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, B);
       k_b_clock_advance<<<blocks(ninst, 128), 128, 0, st>>>(B, updates);
     }

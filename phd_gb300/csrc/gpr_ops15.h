@@ -23,7 +23,7 @@ struct Ops15 {
   static int fv(double *u, const double *qh, const int32_t *nX, double dt,
                 const double *dt_dev, const double *dX, int nd, int sources, int time_dg,
                 const DevPar &P, const uint8_t *mask, double *scratch, cudaStream_t st,
-                int flux = GPR_FLUX_RUSANOV);
+                int flux = GPR_FLUX_RUSANOV, int parts = 3);
   static int faces(const double *qh, const int32_t *nX, double dt, const double *dX, int nd,
                    int time_dg, const DevPar &P, const uint8_t *mask, double *fb,
                    cudaStream_t st, int flux = GPR_FLUX_RUSANOV);

@@ -51,6 +51,9 @@ def pointwise(R, name, thermal=True):
     ode = np.zeros((len(MPs), cnt, 3, V))
     pres = np.zeros((len(MPs), cnt))
     temp = np.zeros((len(MPs), cnt))
+    sysm = np.zeros((len(MPs), cnt, 3, V, V))
+    mt = 4 if thermal else 3
+    thermo = np.zeros((len(MPs), cnt, 3, mt, mt))
     for m, MP in enumerate(MPs):
         P = rd.to_ref_par(R, MP)
         for i in range(cnt):
@@ -68,12 +71,14 @@ def pointwise(R, name, thermal=True):
                 dosh[m, i, d] = R.D(2, q, q2, d, P)
                 droe[m, i, d] = R.D(1, q, q2, d, P)
                 bint[m, i, d] = R.Bint(q, q2, d, P)
+                sysm[m, i, d] = R.system_matrix(q, d, P)
+                thermo[m, i, d] = R.thermo_acoustic_tensor(q, d, P)
             for k, dt in enumerate((1e-4, 1e-2, 1.0)):
                 ode[m, i, k] = R.ode_cell(q, dt, P)
     out.update(Q=Q, Q2=Q2, X=X, flux=flux, Bdot=bdot, max_abs_eigs=mae,
                source=src, D_RUS=drus, D_OSH=dosh, D_ROE=droe, Bint=bint,
                ode=ode, ode_dt=np.array([1e-4, 1e-2, 1.0]), pressure=pres,
-               temperature=temp)
+               temperature=temp, system_matrix=sysm, thermo_acoustic_tensor=thermo)
     out["mp_" + "arrays"] = np.stack([MP.to_array() for MP in MPs])
     np.savez_compressed(os.path.join(HERE, name), **out)
     print("wrote", name)
@@ -101,11 +106,21 @@ def stages(R, u0, MP, dX, bcs, cfl, presteps, flux=0):
     assert not np.isnan(qh).any(), "reference Picard did not converge"
     ufv = uf.copy()
     R.fv_launcher(ufv, qh, nX, dt, dXa, True, True, flux, P, mask)
+    # the two passes of fv_launcher on their own (fv.cpp:11-279)
+    ucen, uint = uf.copy(), uf.copy()
+    if nd == 1:
+        R.centers1(ucen, qh, int(nX[0]), dt, float(dXa[0]), True, True, P, mask)
+        R.interfs1(uint, qh, int(nX[0]), dt, float(dXa[0]), True, flux, P, mask)
+    else:
+        R.centers2(ucen, qh, int(nX[0]), int(nX[1]), dt, float(dXa[0]), float(dXa[1]),
+                   True, True, P, mask)
+        R.interfs2(uint, qh, int(nX[0]), int(nX[1]), dt, float(dXa[0]), float(dXa[1]),
+                   True, flux, P, mask)
     ustep = uf.copy()
     R.ader_stepper(ustep, ub, nX, dt, dXa, False, flux, P, mask)
     R.renorm_single(ustep, P)
     return dict(u=uf, dt=np.array(dt), ub=ub, wh=wh, qh=qh, u_fv=ufv,
-                u_step=ustep, nX=nX, dX=dXa, bcs=np.array(bcs), cfl=np.array(cfl),
+                u_centers=ucen, u_interfs=uint, u_step=ustep, nX=nX, dX=dXa, bcs=np.array(bcs), cfl=np.array(cfl),
                 count=np.array(presteps), flux=np.array(flux),
                 mp=MP.to_array())
 

@@ -70,6 +70,10 @@ def test_stages_osher_2d(G):
     G.solvers.fv.fv_launcher(u, T(g["qh"]), nX, dt, dX, True, True, 2, MP, mask)
     assert rel_err(H(u), g["u_fv"]) < 1e-12
     u = T(g["u"])
+    G.solvers.fv.interfs2(u, T(g["qh"]), int(nX[0]), int(nX[1]), dt, dX[0], dX[1], True, 2,
+                          MP, mask)
+    assert rel_err(H(u), g["u_interfs"]) < 1e-12
+    u = T(g["u"])
     G.solvers.ader_stepper(u, T(g["ub"]), nX, dt, dX, False, 2, MP, mask)
     G.solvers.renorm_distortion(u, [MP])
     assert rel_err(H(u), g["u_step"]) < 1e-12
@@ -116,6 +120,9 @@ def test_stages_osher_1d(G):
     u = T(g["u"])
     G.solvers.fv.fv_launcher(u, T(g["qh"]), nX, dt, dX, True, True, 2, MP, mask)
     assert rel_err(H(u), g["u_fv"]) < 1e-12
+    u = T(g["u"])
+    G.solvers.fv.interfs1(u, T(g["qh"]), int(nX[0]), dt, dX[0], True, 2, MP, mask)
+    assert rel_err(H(u), g["u_interfs"]) < 1e-12
     u = T(g["u"])
     G.solvers.ader_stepper(u, T(g["ub"]), nX, dt, dX, False, 2, MP, mask)
     G.solvers.renorm_distortion(u, [MP])

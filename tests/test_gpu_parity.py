@@ -46,6 +46,10 @@ def test_pointwise_physics(G):
             D, B = G.api.interface_terms(Q, Q2, d, 0, MP)
             assert rel_err(H(D), g["D_RUS"][m, :, d]) < 1e-13
             assert rel_err(H(B), g["Bint"][m, :, d]) < 1e-14
+            assert rel_err(H(G.system.thermo_acoustic_tensor(Q, d, MP)),
+                           g["thermo_acoustic_tensor"][m, :, d]) < 1e-13
+            assert rel_err(H(G.system.system_matrix(Q, d, MP)),
+                           g["system_matrix"][m, :, d]) < 1e-13
 
 
 def test_ode_step(G):
@@ -96,6 +100,21 @@ def test_stages(G, name):
     u = T(g["u"])
     G.solvers.fv.fv_launcher(u, T(g["qh"]), nX, dt, dX, True, True, 0, MP, mask)
     assert rel_err(H(u), g["u_fv"]) < 1e-14
+    # its two passes alone (centers1/2, interfs1/2)
+    u = T(g["u"])
+    if nd == 1:
+        G.solvers.fv.centers1(u, T(g["qh"]), int(nX[0]), dt, dX[0], True, True, MP, mask)
+    else:
+        G.solvers.fv.centers2(u, T(g["qh"]), int(nX[0]), int(nX[1]), dt, dX[0], dX[1], True,
+                              True, MP, mask)
+    assert rel_err(H(u), g["u_centers"]) < 1e-14
+    u = T(g["u"])
+    if nd == 1:
+        G.solvers.fv.interfs1(u, T(g["qh"]), int(nX[0]), dt, dX[0], True, 0, MP, mask)
+    else:
+        G.solvers.fv.interfs2(u, T(g["qh"]), int(nX[0]), int(nX[1]), dt, dX[0], dX[1], True,
+                              0, MP, mask)
+    assert rel_err(H(u), g["u_interfs"]) < 1e-14
     # full ADER step + renorm
     u = T(g["u"])
     G.solvers.ader_stepper(u, T(g["ub"]), nX, dt, dX, False, 0, MP, mask)
@@ -268,8 +287,7 @@ def test_errors_are_raised(G):
                                  [16], 1e-3, dX, True, True, 7, MP,
                                  torch.ones(18, dtype=torch.bool, device=DEV))
     u2 = torch.zeros(4 * 4 * 17, dtype=torch.float64, device=DEV)
-    with pytest.raises(RuntimeError):  # Roe / Osher are 1D only
-        G.solvers.fv.fv_launcher(u2, torch.zeros(6 * 6 * 8 * 17, dtype=torch.float64,
-                                                 device=DEV),
-                                 [4, 4], 1e-3, [0.1, 0.1], True, True, 1, MP,
-                                 torch.ones(36, dtype=torch.bool, device=DEV))
+    with pytest.raises(RuntimeError):  # unknown flux code, 2D face pass alone
+        G.solvers.fv.interfs2(u2, torch.zeros(6 * 6 * 8 * 17, dtype=torch.float64, device=DEV),
+                              4, 4, 1e-3, 0.1, 0.1, True, -1, MP,
+                              torch.ones(36, dtype=torch.bool, device=DEV))

@@ -46,6 +46,9 @@ def test_pointwise_physics(O):
                 checks["Dosh%d" % d] = (O.D(2, q, q2, d, MP), g["D_OSH"][m, i, d])
                 checks["Droe%d" % d] = (O.D(1, q, q2, d, MP), g["D_ROE"][m, i, d])
                 checks["Bint%d" % d] = (O.Bint(q, q2, d), g["Bint"][m, i, d])
+                checks["thmt%d" % d] = (O.thermo_acoustic_tensor(q, d, MP),
+                                        g["thermo_acoustic_tensor"][m, i, d])
+                checks["sysm%d" % d] = (O.system_matrix(q, d, MP), g["system_matrix"][m, i, d])
             for k, dt in enumerate(g["ode_dt"]):
                 qq = q.copy()
                 O.ode_launcher(qq, dt, MP)
