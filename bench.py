@@ -36,8 +36,9 @@ METRIC = "FP64 Mcell-updates/s plain vs batched; adjoint\u00f7forward time at 1e
 UNIT = "Mcell-updates/s"
 
 # Algorithmic FP64 operation counts per unit of work of the algorithm the
-# kernels implement (add/sub/mul/div/sqrt = 1 flop, transcendental call = 1),
-# from oracle/opcount_device.cpp (profiles/opcount_device_tgv512.txt).  The
+# kernels implement (add/sub/mul/div/sqrt = 1 flop, transcendental call = 1;
+# the FP32 start of the wave-speed root iteration is not counted), from
+# oracle/opcount_device.cpp (profiles/opcount_device_tgv512.txt).  The
 # reference's own formulation needs ~2x more (profiles/opcount_tgv512.txt:
 # it recomputes the pressure per call and runs a QR eigen-solve per wave
 # speed); the roofline uses the work this implementation has to do.
@@ -48,10 +49,10 @@ CONTORTED_TOL = 1.0
 
 OPS = {
     "predictor_per_cell_iter": 6040.0,    # per predictor cell and Picard iteration
-    "face_quadrature_point": 1803.0,      # D_RUS + Bint + extrapolation, per point
+    "face_quadrature_point": 1655.0,      # D_RUS + Bint + extrapolation, per point
     "cells_per_cell": 3557.0,             # volume term (both time nodes), per cell
     "weno_point": 49.0,                   # per (cell, variable, sweep)
-    "cfl_per_cell": 1128.0,               # per cell (two max_abs_eigs)
+    "cfl_per_cell": 980.0,                # per cell (two max_abs_eigs)
 }
 
 

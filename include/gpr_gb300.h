@@ -216,6 +216,10 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX,
  * energy.  INFINITY disables it.  gpr_reset_contorted does it once on u
  * (pars[nmat], nmat 1 or 2 with the material from the level set); *flag
  * (device int32) is set to 1 if it reset. */
+/* The check alone (GPRpy.solvers.contorted, utils.cpp:65-85): *flag
+ * (device int32) = 1 if any cell has m0 - 1 > contorted_tol, else 0. */
+int gpr_contorted(const double *u, int64_t ncell, double contorted_tol, int32_t *flag,
+                  int nvar, void *stream);
 int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gpr_par *pars,
                         int nmat, int32_t *flag, int nvar, void *stream);
 

@@ -36,6 +36,7 @@ struct cdouble {
   cdouble &operator*=(cdouble o) { T.mul++; v *= o.v; return *this; }
   cdouble &operator/=(cdouble o) { T.div++; v /= o.v; return *this; }
   cdouble operator-() const { return cdouble(-v); }
+  explicit operator float() const { return (float)v; }  // FP32 work is not counted
 };
 static inline cdouble operator+(cdouble a, cdouble b) { T.add++; return cdouble(a.v + b.v); }
 static inline cdouble operator-(cdouble a, cdouble b) { T.add++; return cdouble(a.v - b.v); }

@@ -82,6 +82,7 @@ solvers = SimpleNamespace(
     split_stepper_para=api.split_stepper_para,
     timestep=api.timestep,
     renorm_distortion=_renorm_distortion,
+    contorted=api.contorted,
     reset_contorted=api.reset_contorted,
     make_u=_multi.make_u,
     extended_dimensions=api.extended_dimensions,

@@ -89,6 +89,7 @@ SIGNATURES = {
     "gpr_iterate_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_iterate": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _D, _I, _P]),
     "gpr_reset_contorted": (_I, [_P, _I64, _D, _P, _I, _P, _I, _P]),
+    "gpr_contorted": (_I, [_P, _I64, _D, _P, _I, _P]),
     "gpr_ader_stepper_1d_noalloc": (_I, [_P, _P, ctypes.c_int32, _D, _D, _I, _I, _P, _P, _P,
                                          _I, _P]),
     "gpr_midstepper": (_I, [_P, _D, _P, _I, _P, _P, _P, _I, _P]),

@@ -323,6 +323,19 @@ def renorm_distortion(u, MPs):
     return u
 
 
+def contorted(u, contorted_tol):
+    """GPRpy.solvers.contorted (solvers/utils.cpp:65-85): True if any cell's
+    normalised distortion m0 = |A|_F^2 / (3 |det A|^(2/3)) has m0 - 1 >
+    contorted_tol.  Returns a Python bool (synchronises, as the reference's
+    bool return does)."""
+    lib = _lib.load()
+    V = _guess_nvar(u) if u.dim() == 1 else u.shape[-1]
+    flag = torch.zeros(1, dtype=torch.int32, device=u.device)
+    _lib.check(lib.gpr_contorted(_dev(u, "u"), u.numel() // V, float(contorted_tol),
+                                 _dev(flag, "flag", torch.int32), V, _stream()), "contorted")
+    return bool(flag.item())
+
+
 def reset_contorted(u, contorted_tol, MPs, flag=None):
     """solvers/utils.cpp:44-85: contorted(u, tol) and, if so,
     reset_distortion(u, MPs), in place (two materials: by level set).

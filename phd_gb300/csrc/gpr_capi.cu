@@ -407,6 +407,32 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX, const 
                             S(stream), flux, contorted_tol))
 }
 
+int gpr_contorted(const double *u, int64_t ncell, double contorted_tol, int32_t *flag, int nvar,
+                  void *stream) {
+  if (!u || !flag || ncell < 1)
+    return GPR_E_ARG;
+  cudaStream_t st = S(stream);
+  if (cudaMemsetAsync(flag, 0, sizeof(int32_t), st) != cudaSuccess)
+    return GPR_E_CUDA;
+  switch (nvar) {
+  case 17:
+    k_contorted<17><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, contorted_tol, (int *)flag,
+                                                         nullptr);
+    break;
+  case 14:
+    k_contorted<14><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, contorted_tol, (int *)flag,
+                                                         nullptr);
+    break;
+  case 15:
+    k_contorted<15><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, contorted_tol, (int *)flag,
+                                                         nullptr);
+    break;
+  default:
+    return GPR_E_UNSUPPORTED;
+  }
+  return cuda_rc();
+}
+
 int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gpr_par *pars,
                         int nmat, int32_t *flag, int nvar, void *stream) {
   if (!u || !pars || !flag || ncell < 1 || nmat < 1 || nmat > 2)

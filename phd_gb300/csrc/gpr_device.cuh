@@ -592,7 +592,48 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
       rs += fabs(X[i][j]);
     R = fmax(R, rs);
   }
-  double x = R * (1.0 + 1e-12) + 1e-300;
+  const double Rs = R * (1.0 + 1e-12) + 1e-300;
+  // Starting point in FP32: Laguerre on the scaled polynomial p(Rs y) / Rs^m
+  // (O(1) coefficients, every root |y| <= 1) from y = 1 down to ~1e-4.  On
+  // this GPU FP32 runs at full rate beside the FP64 pipe, so the FP64
+  // iteration below, started just above that estimate, needs one or two
+  // steps instead of ~5 from the bound.  A failed FP32 run (non-finite or out
+  // of (0, 1]) leaves the start at the bound.
+  double x = Rs;
+  {
+    const double iR = 1.0 / Rs;
+    double sc = iR;
+    float cs[4];
+    cs[0] = (float)(-c1 * sc);
+    sc *= iR;
+    cs[1] = (float)(c2 * sc);
+    sc *= iR;
+    cs[2] = (float)(-c3 * sc);
+    sc *= iR;
+    cs[3] = (float)(c4 * sc);
+    float y = 1.0f;
+    for (int it = 0; it < 24; it++) {
+      float p = 1.0f, dp = 0.0f, d2p = 0.0f;
+#pragma unroll
+      for (int k = 0; k < m; k++) {
+        d2p = d2p * y + 2.0f * dp;
+        dp = dp * y + p;
+        p = p * y + cs[k];
+      }
+      if (p == 0.0f)
+        break;
+      float ip = 1.0f / p;
+      float G = dp * ip;
+      float H = G * G - d2p * ip;
+      float disc = fmaxf((m - 1) * (m * H - G * G), 0.0f);
+      float a = m / (G + copysignf(sqrtf(disc), G));
+      y -= a;
+      if (!(fabsf(a) > 1e-4f * fabsf(y)))
+        break;
+    }
+    if (y > 0.0f && y <= 1.0f)
+      x = fmin((double)y * (1.0 + 4e-6), 1.0) * Rs;
+  }
   for (int it = 0; it < 16; it++) {
     double p = 1.0, dp = 0.0, d2p = 0.0;
     const double cf[4] = {-c1, c2, -c3, c4};

@@ -30,6 +30,7 @@ def test_reset_against_golden(G):
     MP = Par.from_array(g["mp"])
     for tol, hit in zip(g["contorted_tol"], g["contorted"]):
         q = T(g["Q"])
+        assert G.solvers.contorted(q, float(tol)) == bool(hit)
         flag = G.solvers.reset_contorted(q, float(tol), [MP])
         assert int(flag.item()) == int(hit)
         ref = g["reset"] if hit else g["Q"]
