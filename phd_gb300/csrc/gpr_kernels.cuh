@@ -167,14 +167,25 @@ GPR_D void weno_point(const double *__restrict__ d0, long sd, double *__restrict
   tR *= tR;
   tR *= tR;
   tR *= tR;
+  const bool useL = ind >= gap, useR = ind <= nx - gap - 1;
+  if (useL && useR) {
+    // weights LAMS / tL, LAMS / tR normalised, i.e. tR / (tL + tR) and
+    // tL / (tL + tR): one division where the reference takes three (equal
+    // side weights; the result moves by an ulp at most)
+    static_assert(LAMS == 1.0, "equal side weights");
+    const double iden = 1.0 / (tL + tR);
+    out[0] = (wL0 * tR + wR0 * tL) * iden;
+    out[so] = (wL1 * tR + wR1 * tL) * iden;
+    return;
+  }
   double oL = LAMS / tL, oR = LAMS / tR;
   double n0 = 0.0, n1 = 0.0, den = 0.0;
-  if (ind >= gap) {
+  if (useL) {
     n0 += wL0 * oL;
     n1 += wL1 * oL;
     den += oL;
   }
-  if (ind <= nx - gap - 1) {
+  if (useR) {
     n0 += wR0 * oR;
     n1 += wR1 * oR;
     den += oR;
@@ -230,6 +241,56 @@ __global__ void k_weno2d_y(double *__restrict__ wh, const double *__restrict__ u
   int gap = (i == 0 || i == nxp - 1) ? 1 : 0;
   weno_point(ux + (((long)i * nyb + j) * NN + ii) * V + k, (long)NN * V,
              wh + (((long)i * nyp + j) * NN * NN + ii * NN) * V + k, V, j, nyp, gap, C);
+}
+
+// Sum an n-vector v over the G lanes of each aligned lane group (xor
+// butterfly) and scatter the sum: afterwards lane r = lane % G holds
+// elements r n/G .. (r + 1) n/G - 1 of the sum in v[0 .. n/G - 1].  At each
+// level a lane keeps one half, chosen by its lane bit (a select: integer
+// work), and adds the partner's copy of it, so a lane issues n/2 + n/4 + ...
+// + n/G FP64 adds where a full butterfly issues n log2 G; on this GPU the
+// FP64 cost is per warp instruction, whatever the active lanes.
+template <int n, int G> struct GroupReduceScatter {
+  static_assert(n % G == 0, "n a multiple of G");
+  static GPR_D void run(double *v, int r) {
+    if constexpr (G > 1) {
+      constexpr int h = n / 2;
+      const bool up = r & (G / 2);
+#pragma unroll
+      for (int j = 0; j < h; j++) {
+        const double keep = up ? v[h + j] : v[j];
+        const double send = up ? v[j] : v[h + j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, G / 2);
+      }
+      GroupReduceScatter<h, G / 2>::run(v, r);
+    }
+  }
+};
+
+// The face contributions kk (b + f) (left cell) and kk (b - f) (right cell)
+// summed over the G quadrature lanes of a face (r = lane within the face)
+// and written to out[0..V-1] / out[V..2V-1] by the lanes that hold them.
+template <int V, int G>
+GPR_D void face_reduce_store(const double *b, const double *f, double kk, bool active,
+                             bool valid, int r, double *out) {
+  constexpr int NPR = (V + G - 1) / G;  // (b, f) pairs per lane after the scatter
+  double v[2 * NPR * G];
+#pragma unroll
+  for (int k = 0; k < NPR * G; k++) {
+    v[2 * k] = (active && k < V) ? kk * b[k] : 0.0;
+    v[2 * k + 1] = (active && k < V) ? kk * f[k] : 0.0;
+  }
+  GroupReduceScatter<2 * NPR * G, G>::run(v, r);
+  if (!valid)
+    return;
+#pragma unroll
+  for (int p = 0; p < NPR; p++) {
+    const int k = r * NPR + p;
+    if (k < V) {
+      out[k] = v[2 * p] + v[2 * p + 1];
+      out[V + k] = v[2 * p] - v[2 * p + 1];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -907,18 +968,7 @@ __global__ void __launch_bounds__(128) k_faces1d(
     for (int k = 0; k < V; k++)
       f[k] = b[k] = 0.0;
   }
-  double *out = fb + fo * 2 * V;
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    double lft = active ? kk * (b[k] + f[k]) : 0.0;
-    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
-    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
-    if (valid && t == 0) {
-      out[k] = lft;
-      out[V + k] = rgt;
-    }
-  }
+  face_reduce_store<V, NN>(b, f, kk, active, valid, t, fb + fo * 2 * V);
 }
 
 // 2D faces: direction dir, faces (i, j) of the (nx+1) x (ny+1) face grid,
@@ -968,20 +1018,7 @@ __global__ void __launch_bounds__(128) k_faces2d(
     for (int k = 0; k < V; k++)
       f[k] = b[k] = 0.0;
   }
-  double *out = fb + fi * 2 * V;
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    double lft = active ? kk * (b[k] + f[k]) : 0.0;
-    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
-    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
-    lft += __shfl_xor_sync(0xffffffffu, lft, 2);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 2);
-    if (valid && lq == 0) {
-      out[k] = lft;
-      out[V + k] = rgt;
-    }
-  }
+  face_reduce_store<V, NQ>(b, f, kk, active, valid, lq, fb + fi * 2 * V);
 }
 
 // Parts of the FV update k_cells applies: the volume term (centers1 /
@@ -1077,15 +1114,24 @@ __global__ void __launch_bounds__(128) k_cells(
     double wt = time_dg ? dt * C.w[t] : dt;
     double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
 #pragma unroll
-    for (int k = 0; k < V; k++) {
-      double x = live ? wn * acc[k] : 0.0;
-#pragma unroll
-      for (int o = 1; o < NP; o <<= 1)
-        x += __shfl_xor_sync(0xffffffffu, x, o);
-      acc[k] = x;
-    }
+    for (int k = 0; k < V; k++)
+      acc[k] = live ? wn * acc[k] : 0.0;
   }
-  if (!valid || g != 0 || !active)
+  // the cell's sum over its NP lanes, scattered: lane g holds variables
+  // g CK .. g CK + CK - 1
+  constexpr int CK = (V + NP - 1) / NP;
+  double red[CK * NP];
+#pragma unroll
+  for (int k = 0; k < CK * NP; k++)
+    red[k] = k < V ? acc[k] : 0.0;
+  if (parts & FV_CENTERS)
+    GroupReduceScatter<CK * NP, NP>::run(red, g);
+  else {
+#pragma unroll
+    for (int k = 0; k < CK; k++)
+      red[k] = 0.0;
+  }
+  if (!valid || !active)
     return;
   const bool faces = parts & FV_INTERFS;
   double *uc = u + cc * V;
@@ -1096,8 +1142,11 @@ __global__ void __launch_bounds__(128) k_cells(
     bool okl = mask == nullptr || (mask[cb - 1] && mask[cb]);
     bool okr = mask == nullptr || (mask[cb] && mask[cb + 1]);
 #pragma unroll
-    for (int k = 0; k < V; k++) {
-      double x = uc[k] + acc[k];
+    for (int p = 0; p < CK; p++) {
+      const int k = g * CK + p;
+      if (k >= V)
+        break;
+      double x = uc[k] + red[p];
       if (faces && okr)
         x -= fr[k];
       if (faces && okl)
@@ -1112,8 +1161,11 @@ __global__ void __launch_bounds__(128) k_cells(
     long fyl = (long)(ci + 1) * (ny + 1) + (cj + 1);
     long fyr = (long)(ci + 1) * (ny + 1) + cj;
 #pragma unroll
-    for (int k = 0; k < V; k++) {
-      double x = uc[k] + acc[k];
+    for (int p = 0; p < CK; p++) {
+      const int k = g * CK + p;
+      if (k >= V)
+        break;
+      double x = uc[k] + red[p];
       if (faces) {
         x -= fbx[fxl * 2 * V + k];
         x -= fbx[fxr * 2 * V + V + k];
