@@ -48,10 +48,10 @@ UNIT = "Mcell-updates/s"
 CONTORTED_TOL = 1.0
 
 OPS = {
-    "predictor_per_cell_iter": 6040.0,    # per predictor cell and Picard iteration
-    "face_quadrature_point": 1655.0,      # D_RUS + Bint + extrapolation, per point
-    "cells_per_cell": 3557.0,             # volume term (both time nodes), per cell
-    "weno_point": 49.0,                   # per (cell, variable, sweep)
+    "predictor_per_cell_iter": 4904.0,    # per predictor cell and Picard iteration
+    "face_quadrature_point": 1559.0,      # D_RUS + Bint + extrapolation, per point
+    "cells_per_cell": 2293.0,             # volume term (both time nodes), per cell
+    "weno_point": 48.0,                   # per (cell, variable, sweep)
     "cfl_per_cell": 980.0,                # per cell (two max_abs_eigs)
 }
 

@@ -181,26 +181,30 @@ int main(int argc, char **argv) {
   }
   auto per = [&](Tally t) { return (double)t.flops() / nst; };
   double Fp = per(tp), Ff = per(tf), Fs = per(ts), Fb = per(tb), Fm = per(tm);
-  // Bint path node: rho, 1/rho, 3 v (3 fma + 3 mul), bdot, accumulate 17 fma
-  double Fbint_node = 1 + 1 + 3 * 2 + 3 + Fb + 17 * 2;
+  // Bint path node: rho, 1/rho, 3 v (3 fma + 3 mul), bdot, accumulate over
+  // the 9 rows where B x can be nonzero (9 fma)
+  double Fbint_node = 1 + 1 + 3 * 2 + 3 + Fb + 9 * 2;
   // face quadrature point (k_faces2d): 2 extrapolations (17 x 3 each), 2 prim,
   // 2 max_abs_eigs, dissipation 17 x (sub, mul), 2 fluxes, dq (17 sub),
-  // 2 Bint nodes, weighting + 2-level lane reduction 17 x (2 fma + 2 x 2 add)
-  double Fface = 2 * 17 * 3 + 2 * Fp + 2 * Fm + 17 * 2 + 2 * Ff + 17 + 2 * Fbint_node +
-                 17 * (4 + 4) + 2;
+  // 2 Bint nodes, weighting (kk b, kk f: 34 mul), reduce-scatter over the 4
+  // lanes (20 + 10 add per lane) and the 5 kept pairs' sums and differences
+  double Fface = 2 * 17 * 3 + 2 * Fp + 2 * Fm + 17 * 2 + 2 * Ff + 17 + 2 * Fbint_node + 34 +
+                 30 + 10;
   // predictor node and Picard iteration (dg_rhs_node + dg_solve_node +
-  // stopping rule): prim, source, 2 x (derivative 17 x 3, bdot, 17 sub),
-  // node weight 17 mul, 2 fluxes, 2 x DG_DER term 17 x 4, r dt + Ww 17 x 2,
-  // DG_MAT^-1 17 x 3, |qn - q| > tol (1 + |q|) 17 x 3
-  double Fpred_node = Fp + Fs + 2 * (17 * 3 + Fb + 17) + 17 + 2 * Ff + 2 * 17 * 4 + 17 * 2 +
-                      17 * 3 + 17 * 3;
-  // volume node (k_cells): prim, source, 2 x (derivative 17 x 3, bdot,
-  // 17 fma), weight 17 mul, lane reduction 3 x 17 add; cell adds 17 x 5
-  double Fcell_node = Fp + Fs + 2 * (17 * 3 + Fb + 17 * 2) + 17 + 3 * 17;
+  // stopping rule): prim, source (node weight in its factors), 2 x
+  // (derivative of the 6 entries bdot reads 6 x 3, bdot, 9 sub), 2 fluxes,
+  // 2 x DG_DER term on the 11 entries of the flux's support (2 fma each),
+  // r dt + Ww 17 x 2, DG_MAT^-1 17 x 3, |qn - q| > tol (1 + |q|) 17 x 3
+  double Fpred_node = Fp + Fs + 2 * (6 * 3 + Fb + 9) + 2 * Ff + 2 * 11 * 4 + 17 * 2 + 17 * 3 +
+                      17 * 3;
+  // volume node (k_cells): prim, source (weight in its factors), 2 x
+  // (derivative 6 x 3, bdot, 9 sub), reduce-scatter over the 8 lanes
+  // (12 + 6 + 3 add per lane); cell adds 17 x 5
+  double Fcell_node = Fp + Fs + 2 * (6 * 3 + Fb + 9) + 21;
   double Fcell = 8 * Fcell_node + 17 * 5;
   // WENO point (weno_point): 4 coefficients 4 x 3, 2 indicators 2 x 9 + eps,
-  // 2 x 3 squarings, 2 weights (div), blend 6, reciprocal + 2 mul
-  double Fweno = 12 + 2 * 10 + 6 + 2 + 6 + 1 + 2;
+  // 2 x 3 squarings, tL + tR and its reciprocal, 2 blends (2 mul, add, mul)
+  double Fweno = 12 + 2 * 10 + 6 + 2 + 8;
   double Fweno_cell = 2 * Fweno * V * 2;  // x sweep (per ub column cell) + y sweep, ~2 per node
   double Fcfl = Fp + 2 * Fm + 3;
   printf("# FP64 operation counts of the device formulation (gpr_device.cuh compiled\n");

@@ -252,6 +252,41 @@ GPR_D void flux_add(const double *q, const Prim<TH> &s, int d, const DevPar &P, 
   }
 }
 
+// Entries of F_d(Q) that can be nonzero (flux_add / flux_set write only
+// these; the rest are exact zeros).
+template <bool TH> __host__ __device__ constexpr bool flux_support(int k, int d) {
+  return k < 5 || (k >= 5 && k < 14 && (k - 5) % 3 == d) || (TH && k >= 14 && k < 17);
+}
+
+// F = F_d(Q): flux_add into a zeroed array without the additions to zero
+// (which the compiler must keep: 0.0 + x is not x for x = -0.0).
+template <bool TH, int V>
+GPR_D void flux_set(const double *q, const Prim<TH> &s, int d, const DevPar &P, double *F) {
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    F[k] = 0.0;
+  double vd = s.v[d];
+  double sg[3];
+  sigma_col(q, s, d, sg);
+  F[0] = q[2 + d];
+  F[1] = vd * (q[1] + s.p) - (sg[0] * s.v[0] + sg[1] * s.v[1] + sg[2] * s.v[2]);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    F[2 + i] = vd * q[2 + i] - sg[i];
+  F[2 + d] += s.p;
+  const double *A = q + 5;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    F[5 + 3 * i + d] = A[3 * i] * s.v[0] + A[3 * i + 1] * s.v[1] + A[3 * i + 2] * s.v[2];
+  if (TH) {
+    F[1] += P.calpha2 * s.T * s.J[d];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      F[14 + i] = vd * q[14 + i];
+    F[14 + d] += s.T;
+  }
+}
+
 GPR_D double det3(const double *A) {
   return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
          A[2] * (A[3] * A[7] - A[4] * A[6]);
@@ -301,20 +336,22 @@ GPR_D double theta1inv(const double *q, const Prim<TH> &s, const DevPar &P) {
 
 // S(Q)   (equations.cpp:50-67)
 template <bool TH, int V>
-GPR_D void source(const double *q, const Prim<TH> &s, const DevPar &P, double *S) {
+GPR_D void source(const double *q, const Prim<TH> &s, const DevPar &P, double *S,
+                  double scale = 1.0) {
+  // scale multiplies the result (through its scalar factors)
 #pragma unroll
   for (int k = 0; k < V; k++)
     S[k] = 0.0;
-  S[2] = P.dp0;
-  S[3] = P.dp1;
-  S[4] = P.dp2;
-  double f = -s.cs2 * theta1inv(q, s, P);
+  S[2] = P.dp0 * scale;
+  S[3] = P.dp1 * scale;
+  S[4] = P.dp2 * scale;
+  double f = -s.cs2 * theta1inv(q, s, P) * scale;
 #pragma unroll
   for (int i = 0; i < 9; i++)
     S[5 + i] = s.AdG[i] * f;
   if (TH) {
     // -rho (calpha2 J) T / (kappa rho)
-    double g = -P.calpha2 * s.T * P.ikappa;
+    double g = -P.calpha2 * s.T * P.ikappa * scale;
 #pragma unroll
     for (int i = 0; i < 3; i++)
       S[14 + i] = g * s.J[i];

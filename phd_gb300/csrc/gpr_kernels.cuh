@@ -303,6 +303,13 @@ GPR_D void face_reduce_store(const double *b, const double *f, double kk, bool a
 // is the reference's Picard update q <- DG_U^-1 (Ww + dt R(q)) with its
 // per-cell stopping rule |q1 - q0| <= dg_tol (1 + |q0|) (dg1.cpp:108-127).
 
+// |x| as the bit pattern of a non-negative double; patterns above
+// FP_INF_BITS are NaNs.
+constexpr unsigned long long FP_INF_BITS = 0x7ff0000000000000ULL;
+GPR_D unsigned long long fp_abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+
 template <int V>
 GPR_D void shfl_vec(const double *src, double *dst, int lanemask) {
 #pragma unroll
@@ -321,11 +328,14 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
   double tmp[V], other[V];
   Prim<L::THERMAL> s;
   prim<L::THERMAL>(q, P, s);
-  source<L::THERMAL, V>(q, s, P, r);
+  // W (S - B dq/dx [- B dq/dy]): the node weight wn folded into the
+  // source's scalar factors and the derivative coefficients (B is linear)
+  const double wn = ND == 1 ? C.w[t] * C.w[i] : C.w[t] * C.w[i] * C.w[j];
+  source<L::THERMAL, V>(q, s, P, r, wn);
   // x derivative: DERVALS[i][m] q(t, m, j) / dx
   shfl_vec<V>(q, other, XB);
   {
-    double a = C.derv[i][i] * idx, b = C.derv[i][1 - i] * idx;
+    double a = C.derv[i][i] * idx * wn, b = C.derv[i][1 - i] * idx * wn;
 #pragma unroll
     for (int k = 0; k < V; k++)
       tmp[k] = a * q[k] + b * other[k];
@@ -337,7 +347,7 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
   }
   if (ND == 2) {
     shfl_vec<V>(q, other, YB);
-    double a = C.derv[j][j] * idy, b = C.derv[j][1 - j] * idy;
+    double a = C.derv[j][j] * idy * wn, b = C.derv[j][1 - j] * idy * wn;
 #pragma unroll
     for (int k = 0; k < V; k++)
       tmp[k] = a * q[k] + b * other[k];
@@ -347,34 +357,26 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
     for (int k = 0; k < V; k++)
       r[k] -= bd[k];
   }
-  double wn = ND == 1 ? C.w[t] * C.w[i] : C.w[t] * C.w[i] * C.w[j];
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    r[k] *= wn;
-  // - W_t [W_j] DG_DER(i, m) F(t, m, j) / dx
-#pragma unroll
-  for (int k = 0; k < V; k++)
-    tmp[k] = 0.0;
-  flux_add<L::THERMAL, V>(q, s, 0, P, tmp);
+  // - W_t [W_j] DG_DER(i, m) F(t, m, j) / dx, as two fused multiply-adds
+  flux_set<L::THERMAL, V>(q, s, 0, P, tmp);
   shfl_vec<V>(tmp, other, XB);
   {
     double wx = (ND == 1 ? C.w[t] : C.w[t] * C.w[j]) * idx;
     double a = wx * C.dgder[i][i], b = wx * C.dgder[i][1 - i];
 #pragma unroll
     for (int k = 0; k < V; k++)
-      r[k] -= a * tmp[k] + b * other[k];
+      if (flux_support<L::THERMAL>(k, 0))
+        r[k] = fma(-b, other[k], fma(-a, tmp[k], r[k]));
   }
   if (ND == 2) {
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      tmp[k] = 0.0;
-    flux_add<L::THERMAL, V>(q, s, 1, P, tmp);
+    flux_set<L::THERMAL, V>(q, s, 1, P, tmp);
     shfl_vec<V>(tmp, other, YB);
     double wy = C.w[t] * C.w[i] * idy;
     double a = wy * C.dgder[j][j], b = wy * C.dgder[j][1 - j];
 #pragma unroll
     for (int k = 0; k < V; k++)
-      r[k] -= a * tmp[k] + b * other[k];
+      if (flux_support<L::THERMAL>(k, 1))
+        r[k] = fma(-b, other[k], fma(-a, tmp[k], r[k]));
   }
 #pragma unroll
   for (int k = 0; k < V; k++)
@@ -452,20 +454,30 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
       break;
     dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
     dg_solve_node<V, ND>(r, qn, t, i, j, C);
+    // the reference's test |q1 - q0| > dg_tol (1 + |q0|) per entry, the
+    // comparisons and maxima on the IEEE bit patterns of the non-negative
+    // operands (integer order equals numeric order there; NaN patterns sort
+    // above infinity and are excluded as the floating-point forms exclude
+    // them), so that only the subtraction and the threshold use the FP64 pipe
     bool big = false, hasnan = false;
-    double dmax = 0.0;
+    unsigned long long dmaxb = 0;
 #pragma unroll
     for (int k = 0; k < V; k++) {
-      double dd = fabs(qn[k] - q[k]);
-      if (dd > C.dg_tol * (1.0 + fabs(q[k])))
+      const unsigned long long ddb = fp_abs_bits(qn[k] - q[k]);
+      const unsigned long long thb = fp_abs_bits(C.dg_tol * (1.0 + fabs(q[k])));
+      if (ddb > thb && ddb <= FP_INF_BITS && thb <= FP_INF_BITS)
         big = true;
-      if (qn[k] != qn[k])
+      if (fp_abs_bits(qn[k]) > FP_INF_BITS)
         hasnan = true;
-      dmax = fmax(dmax, dd);
+      if (ddb <= FP_INF_BITS && ddb > dmaxb)
+        dmaxb = ddb;
     }
 #pragma unroll
-    for (int o = 1; o < NP; o <<= 1)
-      dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    for (int o = 1; o < NP; o <<= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, dmaxb, o);
+      dmaxb = x > dmaxb ? x : dmaxb;
+    }
+    const double dmax = __longlong_as_double((long long)dmaxb);
     unsigned bigm = __ballot_sync(0xffffffffu, big) & gmask;
     unsigned nanm = __ballot_sync(0xffffffffu, hasnan) & gmask;
     if (!done && bigm && it >= 3 && dmax > 1e8 * dmin) {
@@ -473,7 +485,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
       done = true;
       iters = it + 1;
     }
-    dmin = fmin(dmin, dmax);
+    dmin = dmax < dmin ? dmax : dmin;
     if (!done) {
       iters = it + 1;
       if (bigm) {
@@ -920,8 +932,9 @@ GPR_D void interface_point(const double *ql, const double *qr, int d, const DevP
     double bd[V];
     bdot<V, L::LSET>(v, dq, d, bd);
 #pragma unroll
-    for (int k = 0; k < V; k++)
-      b[k] += C.w[n] * bd[k];
+    for (int k = 5; k < V; k++)  // B x is zero outside the distortion and level-set rows
+      if (k < 14 || k >= V - L::LSET)
+        b[k] += C.w[n] * bd[k];
   }
 }
 
@@ -1080,16 +1093,15 @@ __global__ void __launch_bounds__(128) k_cells(
       q[k] = qc[k];
     Prim<L::THERMAL> s;
     prim<L::THERMAL>(q, P, s);
+    // wn (S - B dq/dx [- B dq/dy]), wn folded into the source's scalar
+    // factors and the derivative coefficients (B is linear)
+    const double wt = time_dg ? dt * C.w[t] : dt;
+    const double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
     if (sources)
-      source<L::THERMAL, V>(q, s, P, acc);
-    else {
-#pragma unroll
-      for (int k = 0; k < V; k++)
-        acc[k] = 0.0;
-    }
+      source<L::THERMAL, V>(q, s, P, acc, wn);
     shfl_vec<V>(q, other, XB);
     {
-      double a = C.derv[i][i], b = C.derv[i][1 - i];
+      double a = C.derv[i][i] * idx * wn, b = C.derv[i][1 - i] * idx * wn;
 #pragma unroll
       for (int k = 0; k < V; k++)
         dq[k] = a * q[k] + b * other[k];
@@ -1097,11 +1109,11 @@ __global__ void __launch_bounds__(128) k_cells(
       bdot<V, L::LSET>(s.v, dq, 0, bd);
 #pragma unroll
       for (int k = 0; k < V; k++)
-        acc[k] -= bd[k] * idx;
+        acc[k] -= bd[k];
     }
     if (ND == 2) {
       shfl_vec<V>(q, other, YB);
-      double a = C.derv[j][j], b = C.derv[j][1 - j];
+      double a = C.derv[j][j] * idy * wn, b = C.derv[j][1 - j] * idy * wn;
 #pragma unroll
       for (int k = 0; k < V; k++)
         dq[k] = a * q[k] + b * other[k];
@@ -1109,13 +1121,11 @@ __global__ void __launch_bounds__(128) k_cells(
       bdot<V, L::LSET>(s.v, dq, 1, bd);
 #pragma unroll
       for (int k = 0; k < V; k++)
-        acc[k] -= bd[k] * idy;
+        acc[k] -= bd[k];
     }
-    double wt = time_dg ? dt * C.w[t] : dt;
-    double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
 #pragma unroll
     for (int k = 0; k < V; k++)
-      acc[k] = live ? wn * acc[k] : 0.0;
+      acc[k] = live ? acc[k] : 0.0;
   }
   // the cell's sum over its NP lanes, scattered: lane g holds variables
   // g CK .. g CK + CK - 1
