@@ -49,10 +49,10 @@ CONTORTED_TOL = 1.0
 
 OPS = {
     "predictor_per_cell_iter": 4904.0,    # per predictor cell and Picard iteration
-    "face_quadrature_point": 1559.0,      # D_RUS + Bint + extrapolation, per point
+    "face_quadrature_point": 1459.0,      # D_RUS + Bint + extrapolation, per point
     "cells_per_cell": 2293.0,             # volume term (both time nodes), per cell
     "weno_point": 48.0,                   # per (cell, variable, sweep)
-    "cfl_per_cell": 980.0,                # per cell (two max_abs_eigs)
+    "cfl_per_cell": 880.0,                # per cell (two max_abs_eigs)
 }
 
 

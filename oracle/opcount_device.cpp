@@ -60,6 +60,10 @@ static inline cdouble hypot(cdouble a, cdouble b) {
   T.mul += 2; T.add++; T.sqrt_++;
   return cdouble(::hypot(a.v, b.v));
 }
+static inline cdouble fma(cdouble a, cdouble b, cdouble c) {
+  T.mul++; T.add++;
+  return cdouble(::fma(a.v, b.v, c.v));
+}
 static inline cdouble fmax(cdouble a, cdouble b) { return cdouble(::fmax(a.v, b.v)); }
 static inline cdouble fmin(cdouble a, cdouble b) { return cdouble(::fmin(a.v, b.v)); }
 static inline cdouble copysign(cdouble a, cdouble b) { return cdouble(::copysign(a.v, b.v)); }

@@ -598,26 +598,41 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
 #pragma unroll
   for (int i = 0; i < m; i++)
     c1 += X[i][i];
-#pragma unroll
-  for (int i = 0; i < m; i++)
-#pragma unroll
-    for (int j = i + 1; j < m; j++)
-      c2 += X[i][i] * X[j][j] - X[i][j] * X[j][i];
-  auto det3 = [&](int a, int b, int c) {
-    return X[a][a] * (X[b][b] * X[c][c] - X[b][c] * X[c][b]) -
-           X[a][b] * (X[b][a] * X[c][c] - X[b][c] * X[c][a]) +
-           X[a][c] * (X[b][a] * X[c][b] - X[b][b] * X[c][a]);
-  };
   if (m == 3) {
-    c3 = det3(0, 1, 2);
+#pragma unroll
+    for (int i = 0; i < m; i++)
+#pragma unroll
+      for (int j = i + 1; j < m; j++)
+        c2 += X[i][i] * X[j][j] - X[i][j] * X[j][i];
+    c3 = X[0][0] * (X[1][1] * X[2][2] - X[1][2] * X[2][1]) -
+         X[0][1] * (X[1][0] * X[2][2] - X[1][2] * X[2][0]) +
+         X[0][2] * (X[1][0] * X[2][1] - X[1][1] * X[2][0]);
   } else {
-    c3 = det3(0, 1, 2) + det3(0, 1, 3) + det3(0, 2, 3) + det3(1, 2, 3);
-    // det of the 4x4 by complementary 2x2 minors of rows (0,1) and (2,3)
+    // the 2x2 minors of rows (0, 1) and of rows (2, 3) give c2 (the two
+    // principal ones), the four principal 3x3 minors (expanded along the
+    // third row) and det X (Laplace along rows (0, 1))
+    // (explicit fused multiply-adds: the same rounding in every kernel that
+    // inlines this, whatever contraction the compiler would choose there)
     const int r2 = m == 4 ? 2 : 0, r3 = m == 4 ? 3 : 0;
-    auto s = [&](int a, int b) { return X[0][a] * X[1][b] - X[0][b] * X[1][a]; };
-    auto t = [&](int a, int b) { return X[r2][a] * X[r3][b] - X[r2][b] * X[r3][a]; };
-    c4 = s(0, 1) * t(2, 3) - s(0, 2) * t(1, 3) + s(0, 3) * t(1, 2) + s(1, 2) * t(0, 3) -
-         s(1, 3) * t(0, 2) + s(2, 3) * t(0, 1);
+    auto mn = [](double a, double b, double c, double d) { return fma(a, b, -(c * d)); };
+    auto s = [&](int a, int b) { return mn(X[0][a], X[1][b], X[0][b], X[1][a]); };
+    auto t = [&](int a, int b) { return mn(X[r2][a], X[r3][b], X[r2][b], X[r3][a]); };
+    const double s01 = s(0, 1), s02 = s(0, 2), s03 = s(0, 3), s12 = s(1, 2), s13 = s(1, 3),
+                 s23 = s(2, 3);
+    const double t01 = t(0, 1), t02 = t(0, 2), t03 = t(0, 3), t12 = t(1, 2), t13 = t(1, 3),
+                 t23 = t(2, 3);
+    c2 = ((s01 + t23) + (mn(X[0][0], X[r2][r2], X[0][r2], X[r2][0]) +
+                         mn(X[0][0], X[r3][r3], X[0][r3], X[r3][0]))) +
+         (mn(X[1][1], X[r2][r2], X[1][r2], X[r2][1]) +
+          mn(X[1][1], X[r3][r3], X[1][r3], X[r3][1]));
+    auto e3 = [](double a, double sa, double b, double sb, double c, double sc) {
+      return fma(c, sc, fma(a, sa, -(b * sb)));
+    };
+    c3 = (e3(X[r2][r2], s01, X[r2][1], s02, X[r2][0], s12) +
+          e3(X[r3][r3], s01, X[r3][1], s03, X[r3][0], s13)) +
+         (e3(X[0][0], t23, X[0][r2], t03, X[0][r3], t02) +
+          e3(X[1][1], t23, X[1][r2], t13, X[1][r3], t12));
+    c4 = (mn(s01, t23, s02, t13) + fma(s03, t12, s12 * t03)) - fma(s13, t02, -(s23 * t01));
   }
   // p(x) = x^m - c1 x^(m-1) + c2 x^(m-2) - c3 x^(m-3) [+ c4]
   double R = 0.0;
@@ -638,31 +653,29 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
   // of (0, 1]) leaves the start at the bound.
   double x = Rs;
   {
-    const double iR = 1.0 / Rs;
-    double sc = iR;
+    // scaled coefficients in FP32 (a coefficient beyond the FP32 range makes
+    // the start fail, and the FP64 iteration then starts at the bound)
+    const float iR = 1.0f / (float)Rs;
     float cs[4];
-    cs[0] = (float)(-c1 * sc);
-    sc *= iR;
-    cs[1] = (float)(c2 * sc);
-    sc *= iR;
-    cs[2] = (float)(-c3 * sc);
-    sc *= iR;
-    cs[3] = (float)(c4 * sc);
+    cs[0] = -(float)c1 * iR;
+    cs[1] = ((float)c2 * iR) * iR;
+    cs[2] = -(((float)c3 * iR) * iR) * iR;
+    cs[3] = ((((float)c4 * iR) * iR) * iR) * iR;
     float y = 1.0f;
     for (int it = 0; it < 24; it++) {
       float p = 1.0f, dp = 0.0f, d2p = 0.0f;
 #pragma unroll
       for (int k = 0; k < m; k++) {
-        d2p = d2p * y + 2.0f * dp;
-        dp = dp * y + p;
-        p = p * y + cs[k];
+        d2p = fmaf(d2p, y, 2.0f * dp);
+        dp = fmaf(dp, y, p);
+        p = fmaf(p, y, cs[k]);
       }
       if (p == 0.0f)
         break;
       float ip = 1.0f / p;
       float G = dp * ip;
-      float H = G * G - d2p * ip;
-      float disc = fmaxf((m - 1) * (m * H - G * G), 0.0f);
+      float H = fmaf(G, G, -(d2p * ip));
+      float disc = fmaxf((m - 1) * fmaf((float)m, H, -(G * G)), 0.0f);
       float a = m / (G + copysignf(sqrtf(disc), G));
       y -= a;
       if (!(fabsf(a) > 1e-4f * fabsf(y)))
@@ -676,16 +689,16 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
     const double cf[4] = {-c1, c2, -c3, c4};
 #pragma unroll
     for (int k = 0; k < m; k++) {
-      d2p = d2p * x + 2.0 * dp;
-      dp = dp * x + p;
-      p = p * x + cf[k];
+      d2p = fma(d2p, x, 2.0 * dp);
+      dp = fma(dp, x, p);
+      p = fma(p, x, cf[k]);
     }
     if (p == 0.0)
       break;
     double ip = 1.0 / p;
     double G = dp * ip;
-    double H = G * G - d2p * ip;
-    double disc = fmax((m - 1) * (m * H - G * G), 0.0);
+    double H = fma(G, G, -(d2p * ip));
+    double disc = fmax((m - 1) * fma((double)m, H, -(G * G)), 0.0);
     double a = m / (G + copysign(sqrt(disc), G));
     x -= a;
     if (!(fabs(a) > 1e-5 * fabs(x)))  // cubic convergence: the error is now ~|a|^3
@@ -696,13 +709,15 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
     return false;
   // deflate and certify: all other roots strictly inside |z| < (1-1e-9) lam
   double l = x * (1.0 - 1e-9);
-  double q2 = -c1 + x, q1 = c2 + x * q2;
+  double q2 = -c1 + x, q1 = fma(x, q2, c2);
   if (m == 3) {
-    double a1 = q2 / l, a0 = q1 / (l * l);
+    const double il = 1.0 / l;
+    double a1 = q2 * il, a0 = q1 * il * il;
     return fabs(a0) < 1.0 && fabs(a1) < 1.0 + a0;
   }
-  double q0 = -c3 + x * q1;
-  double a2 = q2 / l, a1 = q1 / (l * l), a0 = q0 / (l * l * l);
+  double q0 = fma(x, q1, -c3);
+  const double il = 1.0 / l;
+  double a2 = q2 * il, a1 = q1 * il * il, a0 = q0 * il * il * il;
   return (1.0 + a2 + a1 + a0 > 0.0) && (1.0 - a2 + a1 - a0 > 0.0) && fabs(a0) < 1.0 &&
          fabs(a0 * a0 - 1.0) > fabs(a0 * a2 - a1);
 }
