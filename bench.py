@@ -921,8 +921,10 @@ def roofline(stage_ms, ncell, n, mean_iters, peak):
     # kernel: (time per launch ms, algorithmic flops per launch)
     kern = {
         "k_faces2d": (stage_ms["faces"] / 2, OPS["face_quadrature_point"] * 4 * nf),
+        # the first iteration runs at one thread per spatial node
+        # (k_predictor_first): half the per-iteration work
         "k_predictor_picard": (stage_ms["predictor"],
-                               OPS["predictor_per_cell_iter"] * ncb * mean_iters),
+                               OPS["predictor_per_cell_iter"] * ncb * (mean_iters - 0.5)),
         "k_cells": (max(stage_ms["fv"] - stage_ms["faces"], 1e-9),
                     OPS["cells_per_cell"] * ncell),
         "k_cfl_max": (stage_ms["cfl"], OPS["cfl_per_cell"] * ncell),

@@ -102,8 +102,11 @@ template <class L> struct Adj {
                                                              amax);
     k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
     k_b_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wh, ub, b.nb, C, B);
+    // every iteration in the Picard kernel (no k_predictor_first): the
+    // tightly converged forward the gradients and their finite-difference
+    // checks difference keeps one arithmetic path
     k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, 128), 128, 0, st>>>(
-        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B);
+        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 0);
     int rc = launch_stiff<L, 1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
                                       C, st, B);
     if (rc)

@@ -317,10 +317,12 @@ GPR_D void shfl_vec(const double *src, double *dst, int lanemask) {
     dst[k] = __shfl_xor_sync(0xffffffffu, src[k], lanemask);
 }
 
-// rhs at this thread's node; returns R in r (Ww added), q unchanged.
-template <class L, int ND>
-GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int i, int j,
-                       double dt, double idx, double idy, const DevPar &P, const Consts &C) {
+// rhs at this thread's node with time weight wt (W_t): r = dt R + Ww
+// (AFFINE) or r = R; q unchanged.  The spatial partners are the lanes
+// g ^ XB (x) and g ^ YB (y), as in both lane layouts that call it.
+template <class L, int ND, bool AFFINE = true>
+GPR_D void dg_rhs_node_w(const double *q, const double *Ww, double *r, double wt, int i, int j,
+                         double dt, double idx, double idy, const DevPar &P, const Consts &C) {
   constexpr int V = L::V;
   // lane bit layout: 1D g = 2t + i ; 2D g = 4t + 2i + j
   constexpr int XB = ND == 1 ? 1 : 2;  // flips i
@@ -330,7 +332,7 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
   prim<L::THERMAL>(q, P, s);
   // W (S - B dq/dx [- B dq/dy]): the node weight wn folded into the
   // source's scalar factors and the derivative coefficients (B is linear)
-  const double wn = ND == 1 ? C.w[t] * C.w[i] : C.w[t] * C.w[i] * C.w[j];
+  const double wn = ND == 1 ? wt * C.w[i] : wt * C.w[i] * C.w[j];
   source<L::THERMAL, V>(q, s, P, r, wn);
   // x derivative: DERVALS[i][m] q(t, m, j) / dx
   shfl_vec<V>(q, other, XB);
@@ -361,7 +363,7 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
   flux_set<L::THERMAL, V>(q, s, 0, P, tmp);
   shfl_vec<V>(tmp, other, XB);
   {
-    double wx = (ND == 1 ? C.w[t] : C.w[t] * C.w[j]) * idx;
+    double wx = (ND == 1 ? wt : wt * C.w[j]) * idx;
     double a = wx * C.dgder[i][i], b = wx * C.dgder[i][1 - i];
 #pragma unroll
     for (int k = 0; k < V; k++)
@@ -371,16 +373,24 @@ GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int 
   if (ND == 2) {
     flux_set<L::THERMAL, V>(q, s, 1, P, tmp);
     shfl_vec<V>(tmp, other, YB);
-    double wy = C.w[t] * C.w[i] * idy;
+    double wy = wt * C.w[i] * idy;
     double a = wy * C.dgder[j][j], b = wy * C.dgder[j][1 - j];
 #pragma unroll
     for (int k = 0; k < V; k++)
       if (flux_support<L::THERMAL>(k, 1))
         r[k] = fma(-b, other[k], fma(-a, tmp[k], r[k]));
   }
+  if (AFFINE) {
 #pragma unroll
-  for (int k = 0; k < V; k++)
-    r[k] = r[k] * dt + Ww[k];
+    for (int k = 0; k < V; k++)
+      r[k] = r[k] * dt + Ww[k];
+  }
+}
+
+template <class L, int ND>
+GPR_D void dg_rhs_node(const double *q, const double *Ww, double *r, int t, int i, int j,
+                       double dt, double idx, double idy, const DevPar &P, const Consts &C) {
+  dg_rhs_node_w<L, ND, true>(q, Ww, r, C.w[t], i, j, dt, idx, idy, P, C);
 }
 
 // q_new(t, s) = sum_m DG_MATinv[t][m] r(m, s) / W_s
@@ -397,6 +407,62 @@ GPR_D void dg_solve_node(const double *r, double *qn, int t, int i, int j, const
     qn[k] = a * r[k] + b * other[k];
 }
 
+// First Picard iteration.  From the standard initial guess q(t, s) = w(s)
+// (initial_guess.cpp:4-15) the rhs at the two time nodes differs only by the
+// weight W_t, so one thread per (cell, spatial node) evaluates it once (time
+// weight 1) and writes q1 = DG_U^-1 (W w + dt R(q0)) at both time nodes
+// into qh; k_predictor_picard (first = 1) takes that as its first iterate
+// and applies the reference's stopping test to it as usual.
+template <class L, int ND, bool BATCH = false>
+__global__ void __launch_bounds__(128) k_predictor_first(
+    double *__restrict__ qh, const double *__restrict__ wh, long ncb,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double idx,
+    double idy, DevPar Pv, Consts C, Batch B) {
+  constexpr int V = L::V;
+  constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
+  constexpr int NP = NN * NS;
+  static_assert(NN == 2, "two time nodes");
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int g = threadIdx.x % NS;
+  long c = gt / NS;
+  bool valid = c < ncb;
+  const long cc = valid ? c : 0;
+  const int inst = BATCH ? B.inst_b[cc] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    dt = B.clk[5 * inst + 1];
+    idx = B.idx[inst];
+  }
+  // the cells k_predictor_picard iterates (finished instances of a batch too)
+  const bool active = valid && (mask == nullptr || mask[c]);
+  const int i = ND == 1 ? g : g / NN, j = ND == 1 ? 0 : g % NN;
+  double q[V], r[V];
+  const double *wc = wh + (cc * NS + g) * V;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = valid ? wc[k] : 1.0;
+  dg_rhs_node_w<L, ND, false>(q, nullptr, r, 1.0, i, j, dt, idx, idy, P, C);
+  if (!active)
+    return;
+  // r_t = dt W_t R + ENDVALS[0][t] W_s w ; q1_t = sum_m DG_MATinv[t][m] r_m / W_s
+  const double Ws = ND == 1 ? C.w[i] : C.w[i] * C.w[j];
+  const double iws = ND == 1 ? 1.0 / C.w[i] : 1.0 / (C.w[i] * C.w[j]);
+  const double d0 = dt * C.w[0], d1 = dt * C.w[1];
+  const double f0 = C.endv[0][0] * Ws, f1 = C.endv[0][1] * Ws;
+  const double a00 = C.dgmatinv[0][0] * iws, a01 = C.dgmatinv[0][1] * iws;
+  const double a10 = C.dgmatinv[1][0] * iws, a11 = C.dgmatinv[1][1] * iws;
+  double *o0 = qh + (c * NP + g) * V, *o1 = qh + (c * NP + NS + g) * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    const double r0 = r[k] * d0 + f0 * q[k];
+    const double r1 = r[k] * d1 + f1 * q[k];
+    o0[k] = a00 * r0 + a01 * r1;
+    o1[k] = a10 * r0 + a11 * r1;
+  }
+}
+
 // Picard predictor.  ncb predictor cells; each warp holds 32/NP cells.
 // status[c] (optional): GPR_PRED_PICARD | iterations << 8 when converged,
 // GPR_PRED_FAILED when Picard did not converge (row left for the Newton pass,
@@ -406,7 +472,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
     const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar Pv, Consts C,
-    Batch B) {
+    Batch B, int first) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
   constexpr int NP = NN * NS;                 // space-time nodes
@@ -452,8 +518,16 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   for (int it = 0; it < maxit; it++) {
     if (__all_sync(0xffffffffu, done))
       break;
-    dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
-    dg_solve_node<V, ND>(r, qn, t, i, j, C);
+    if (it == 0 && first) {
+      // the first iterate, from k_predictor_first
+      const double *src = qh + (cc * NP + g) * V;
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        qn[k] = active ? src[k] : q[k];
+    } else {
+      dg_rhs_node<L, ND>(q, Ww, r, t, i, j, dt, idx, idy, P, C);
+      dg_solve_node<V, ND>(r, qn, t, i, j, C);
+    }
     // the reference's test |q1 - q0| > dg_tol (1 + |q0|) per entry, the
     // comparisons and maxima on the IEEE bit patterns of the non-negative
     // operands (integer order equals numeric order there; NaN patterns sort

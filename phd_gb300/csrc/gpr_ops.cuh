@@ -196,15 +196,23 @@ template <class L> struct Ops {
     const Consts &C = consts();
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
+    // the first Picard iterate at one thread per spatial node (k_predictor_first)
+    const int first = stiff ? 0 : 1;
     if (nd == 1) {
+      if (first)
+        k_predictor_first<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(
+            qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
       long nt = ncb * NN * NN;
       k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first);
       return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
     }
+    if (first)
+      k_predictor_first<L, 2><<<blocks(ncb * NN * NN, 128), 128, 0, st>>>(
+          qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
     long nt = ncb * NN * NN * NN;
     k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
-        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{});
+        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first);
     return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
   }
 
@@ -501,8 +509,10 @@ template <class L> struct Ops {
       k_b_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B);
       k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
       k_b_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wh, ub, b.nb, C, B);
+      k_predictor_first<L, 1, true><<<blocks(b.nb * NN, 128), 128, 0, st>>>(
+          qh, wh, b.nb, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C, B);
       k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, 128), 128, 0, st>>>(
-          qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B);
+          qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1);
       int rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
                                    C, st, B);
       if (rc)
