@@ -47,12 +47,20 @@ UNIT = "Mcell-updates/s"
 # 1 + CONTORTED_TOL.
 CONTORTED_TOL = 1.0
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# the TGV 512^2 kernels from one ncu capture each (profiles/k_faces2d_tgv512.md,
+# profiles/k_predictor_picard_tgv512.md).
+TRAFFIC = {
+    "k_faces2d": 287.910912e6 + 289.751808e6,
+    "k_predictor_picard": 143.945728e6 + 229.694720e6,
+}
+
 OPS = {
     "predictor_per_cell_iter": 4904.0,    # per predictor cell and Picard iteration
-    "face_quadrature_point": 1459.0,      # D_RUS + Bint + extrapolation, per point
+    "face_quadrature_point": 1427.0,      # D_RUS + Bint + extrapolation, per point
     "cells_per_cell": 2293.0,             # volume term (both time nodes), per cell
     "weno_point": 48.0,                   # per (cell, variable, sweep)
-    "cfl_per_cell": 880.0,                # per cell (two max_abs_eigs)
+    "cfl_per_cell": 848.0,                # per cell (two max_abs_eigs)
 }
 
 
@@ -943,6 +951,11 @@ def roofline(stage_ms, ncell, n, mean_iters, peak):
     d = out["per_kernel"][dom]
     out.update(achieved=d["achieved"], frac=d["frac"],
                algorithmic_flops_per_launch=d["algorithmic_flops_per_launch"])
+    if dom in TRAFFIC:
+        out["traffic"] = TRAFFIC[dom]
+        out["traffic_unit"] = "bytes per launch"
+        out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture "
+                                 "(profiles/%s_tgv512.md)" % dom)
     return out
 
 

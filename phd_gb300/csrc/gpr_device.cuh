@@ -592,7 +592,10 @@ template <int n> GPR_D double max_abs_eig(double (&H)[n][n]) {
 // quotient).  Returns false when the certificate fails (complex roots of
 // larger modulus, a multiple largest root, no convergence); the caller then
 // runs the QR iteration, so the result is max |eig| either way.
-template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &lam) {
+// Z: X[1][m-1] and X[2][m-1] are known zeros (the heat-conduction column of
+// the acoustic tensor), left out of the characteristic polynomial.
+template <int m, bool Z = false>
+GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &lam) {
   static_assert(m == 3 || m == 4, "3x3 or 4x4");
   double c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0;
 #pragma unroll
@@ -617,21 +620,27 @@ template <int m> GPR_D bool max_eig_laguerre(const double (&X)[m][m], double &la
     auto mn = [](double a, double b, double c, double d) { return fma(a, b, -(c * d)); };
     auto s = [&](int a, int b) { return mn(X[0][a], X[1][b], X[0][b], X[1][a]); };
     auto t = [&](int a, int b) { return mn(X[r2][a], X[r3][b], X[r2][b], X[r3][a]); };
-    const double s01 = s(0, 1), s02 = s(0, 2), s03 = s(0, 3), s12 = s(1, 2), s13 = s(1, 3),
-                 s23 = s(2, 3);
-    const double t01 = t(0, 1), t02 = t(0, 2), t03 = t(0, 3), t12 = t(1, 2), t13 = t(1, 3),
-                 t23 = t(2, 3);
+    // with Z, X[1][3] = X[2][3] = 0 drop out of the minors that contain them
+    const double s01 = s(0, 1), s02 = s(0, 2), s12 = s(1, 2);
+    const double s03 = Z ? -(X[0][r3] * X[1][0]) : s(0, 3);
+    const double s13 = Z ? -(X[0][r3] * X[1][1]) : s(1, 3);
+    const double s23 = Z ? -(X[0][r3] * X[1][r2]) : s(2, 3);
+    const double t01 = t(0, 1), t02 = t(0, 2), t12 = t(1, 2);
+    const double t03 = Z ? X[r2][0] * X[r3][r3] : t(0, 3);
+    const double t13 = Z ? X[r2][1] * X[r3][r3] : t(1, 3);
+    const double t23 = Z ? X[r2][r2] * X[r3][r3] : t(2, 3);
     c2 = ((s01 + t23) + (mn(X[0][0], X[r2][r2], X[0][r2], X[r2][0]) +
                          mn(X[0][0], X[r3][r3], X[0][r3], X[r3][0]))) +
          (mn(X[1][1], X[r2][r2], X[1][r2], X[r2][1]) +
-          mn(X[1][1], X[r3][r3], X[1][r3], X[r3][1]));
+          (Z ? X[1][1] * X[r3][r3] : mn(X[1][1], X[r3][r3], X[1][r3], X[r3][1])));
     auto e3 = [](double a, double sa, double b, double sb, double c, double sc) {
       return fma(c, sc, fma(a, sa, -(b * sb)));
     };
     c3 = (e3(X[r2][r2], s01, X[r2][1], s02, X[r2][0], s12) +
           e3(X[r3][r3], s01, X[r3][1], s03, X[r3][0], s13)) +
          (e3(X[0][0], t23, X[0][r2], t03, X[0][r3], t02) +
-          e3(X[1][1], t23, X[1][r2], t13, X[1][r3], t12));
+          (Z ? fma(X[1][1], t23, -(X[1][r2] * t13))
+             : e3(X[1][1], t23, X[1][r2], t13, X[1][r3], t12)));
     c4 = (mn(s01, t23, s02, t13) + fma(s03, t12, s12 * t03)) - fma(s13, t02, -(s23 * t01));
   }
   // p(x) = x^m - c1 x^(m-1) + c2 x^(m-2) - c3 x^(m-3) [+ c4]
@@ -801,7 +810,7 @@ GPR_D double max_abs_eigs(const double *q, const Prim<TH> &s, int d, const DevPa
         Xo[i * m + c] = X[i][c];
   }
   double l2;
-  if (!max_eig_laguerre<m>(X, l2))
+  if (!max_eig_laguerre<m, TH>(X, l2))
     l2 = max_abs_eig<m>(X);  // QR fallback: complex or multiple dominant roots
   if (l2o)
     *l2o = l2;
