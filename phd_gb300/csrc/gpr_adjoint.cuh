@@ -21,13 +21,16 @@
 // weights, the Rusanov flux with its max-wave-speed switch, the path integral
 // of B, the renormalisation and the CFL time step are differentiated exactly.
 //
-// Per-node Jacobians of F, S and lambda with respect to the state and six
-// material fields come from forward-mode dual numbers: one thread per
-// (evaluation point, tangent), over a restatement of the device physics for
-// the differentiable model (stiffened-gas EOS, Newtonian viscosity, beta = 0,
-// Tref = 0, direction x).  The eigenvalue derivative of the acoustic tensor
-// uses d lambda = tr(adj(lambda I - X) dX) / tr(adj(lambda I - X)) for the
-// simple dominant eigenvalue.
+// The point functions (F, S and lambda along x, for the differentiable
+// model: stiffened-gas EOS, Newtonian viscosity, beta = 0, Tref = 0) enter
+// only through products with one cotangent, so the backward step applies
+// hand-written reverse sweeps of them (point_vjp; pcache_vjp over a cached
+// primal inside the transposed predictor iteration).  Forward-mode dual
+// numbers over the same restatement give full Jacobians where they are
+// needed: the dense fallback solve, the CFL argmax cell, and as the test
+// reference of the reverse sweeps.  The eigenvalue derivative of the
+// acoustic tensor uses d lambda = tr(adj(lambda I - X) dX) /
+// tr(adj(lambda I - X)) for the simple dominant eigenvalue.
 #pragma once
 
 #include "gpr_kernels.cuh"
