@@ -69,6 +69,9 @@ def _load():
             "or_fv_launcher": (ctypes.c_int, [_dp, _dp, _ip, ctypes.c_double, _dp,
                                               ctypes.c_int, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, P, _u8p]),
+            "or_fv_parts": (ctypes.c_int, [_dp, _dp, _ip, ctypes.c_double, _dp, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, P, _u8p,
+                                           ctypes.c_int]),
             "or_timestep": (ctypes.c_double, [_dp, ctypes.c_long, _dp, ctypes.c_int,
                                               ctypes.c_double, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_int, P]),
@@ -312,6 +315,22 @@ class Oracle:
                            _d(np.asarray(dX, dtype=np.float64)), nd, int(sources),
                            int(time), int(flux), p,
                            _u8(np.ascontiguousarray(mask, dtype=np.uint8)))
+        return u
+
+    def fv_parts(self, u, qh, nX, dt, dX, MP, parts, mask=None, sources=True, time=True,
+                 flux=0):
+        """One or both passes of fv_launcher: parts 1 = centers1/2 (volume
+        term), 2 = interfs1/2 (interface terms), 3 = both."""
+        lib = self._cfg()
+        nX = np.asarray(nX, dtype=np.int32)
+        nd = len(nX)
+        if mask is None:
+            mask = np.ones(int(np.prod(nX + 2)), dtype=np.uint8)
+        c, p = self._par(MP)
+        lib.or_fv_parts(_d(u), _d(np.ascontiguousarray(qh)), _i(nX), dt,
+                        _d(np.asarray(dX, dtype=np.float64)), nd, int(sources), int(time),
+                        int(flux), p, _u8(np.ascontiguousarray(mask, dtype=np.uint8)),
+                        int(parts))
         return u
 
     def timestep(self, u, dX, cfl, t, tf, count, MP):

@@ -2341,9 +2341,11 @@ static void centers_cell(double *ucell, const double *qh_t, int ndim, double dx,
   }
 }
 
-int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
-                   const double *dX, int ndim, int SOURCES, int TIME, int FLUX,
-                   const gpr_par *P, const uint8_t *mask) {
+/* fv_launcher's two passes (fv.cpp:11-279): parts bit 0 the volume term
+ * (centers1 / centers2), bit 1 the interface terms (interfs1 / interfs2). */
+int or_fv_parts(double *u, const double *qh, const int *nX, double dt, const double *dX,
+                int ndim, int SOURCES, int TIME, int FLUX, const gpr_par *P,
+                const uint8_t *mask, int parts) {
   int nt = TIME ? N : 1;
   int nx = nX[0], ny = ndim == 2 ? nX[1] : 1;
   int ns = ndim == 1 ? N : N * N;
@@ -2351,7 +2353,7 @@ int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
   long ncellb = ndim == 1 ? nx + 2 : (long)(nx + 2) * (ny + 2);
   (void)ncellb;
   /* centers (fv.cpp:11-109) */
-  for (int t = 0; t < nt; t++) {
+  for (int t = 0; t < nt && (parts & 1); t++) {
     double wt = TIME ? dt * WGHTS[t] : dt;
 #pragma omp parallel for schedule(static)
     for (long c = 0; c < (long)nx * ny; c++) {
@@ -2363,6 +2365,8 @@ int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
       centers_cell(u + c * V, qt, ndim, dx, dy, wt, SOURCES, P);
     }
   }
+  if (!(parts & 2))
+    return 0;
   /* interfaces (fv.cpp:111-279): fluxes per face computed in parallel,
    * then applied in the reference's order. */
   double ENDL[MAXN], ENDR[MAXN];
@@ -2503,6 +2507,12 @@ int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
   }
   free(fx);
   return 0;
+}
+
+int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
+                   const double *dX, int ndim, int SOURCES, int TIME, int FLUX,
+                   const gpr_par *P, const uint8_t *mask) {
+  return or_fv_parts(u, qh, nX, dt, dX, ndim, SOURCES, TIME, FLUX, P, mask, 3);
 }
 
 /* ------------------------------------------------------------------------ */

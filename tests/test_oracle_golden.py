@@ -94,6 +94,11 @@ def test_stages(name, N):
     O.fv_launcher(ufv, g["qh"], nX, float(g["dt"]), dX, MP, flux=int(g["flux"]))
     tol = 1e-12 if int(g["flux"]) == 2 else 1e-14
     assert rel_err(ufv, g["u_fv"]) < tol
+    if "u_centers" in g.files:  # the two passes alone (centers1/2, interfs1/2)
+        for parts, key in ((1, "u_centers"), (2, "u_interfs")):
+            up = u.copy()
+            O.fv_parts(up, g["qh"], nX, float(g["dt"]), dX, MP, parts, flux=int(g["flux"]))
+            assert rel_err(up, g[key]) < tol, key
     ustep = u.copy()
     O.ader_stepper(ustep, g["ub"], nX, float(g["dt"]), dX, MP, flux=int(g["flux"]))
     O.renorm_distortion(ustep, MP)
