@@ -159,7 +159,7 @@ int gpr_fv_face_fluxes(const double *qh, const int32_t *nX, double dt,
                        const gpr_par *par, const uint8_t *mask, double *fb,
                        int nvar, void *stream);
 
-/* Replaces solvers.timestep (solvers/iterator.cpp:148-177) for one material:
+/* Replaces solvers.timestep (solvers/iterator.cpp:54-83) for one material:
  * dt = CFL / max_cells sum_d max_abs_eigs/dx_d, x0.2 while count <= 5,
  * clipped to tf - t.  The result is written to dt_out (device double).
  * `scratch` must hold gpr_timestep_scratch_doubles(ncell) doubles. */

@@ -305,7 +305,7 @@ def _guess_nvar(u):
 
 
 def timestep(grids, masks, dX, CFL, t, tf, count, MPs, nmat=1):
-    """solvers.timestep (solvers/iterator.cpp:148-177) for the first
+    """solvers.timestep (solvers/iterator.cpp:54-83) for the first
     material's grid; returns a host float."""
     u = grids[0] if isinstance(grids, (list, tuple)) else grids
     MP = MPs[0] if isinstance(MPs, (list, tuple)) else MPs

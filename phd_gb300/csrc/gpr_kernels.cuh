@@ -1262,7 +1262,7 @@ __global__ void __launch_bounds__(128) k_cells(
 }
 
 // ---------------------------------------------------------------------------
-// CFL time step (solvers/iterator.cpp:148-177): per-cell sum_d mae/dx_d,
+// CFL time step (solvers/iterator.cpp:54-83): per-cell sum_d mae/dx_d,
 // block max, atomicMax on the bit pattern (non-negative doubles order as
 // unsigned integers); NaN cells are skipped as std::max skips them.
 template <class L>
@@ -1431,7 +1431,7 @@ __global__ void __launch_bounds__(256) k_b_cfl_max(const double *__restrict__ u,
     atomicMax(mx + inst, (unsigned long long)__double_as_longlong(m));
 }
 
-// per-instance dt (iterator.cpp:148-177 per instance) and the step counter
+// per-instance dt (iterator.cpp:54-83 per instance) and the step counter
 static __global__ void k_b_clock_finalize(unsigned long long *__restrict__ mx, Batch B) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= B.ninst)
