@@ -106,7 +106,7 @@ long gpr_weno_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX,
                       int ndim, double *scratch, int nvar, void *stream);
 
-/* Replaces solvers.dg.predictor (solvers/dg/dg.h:7, dg1.cpp:75-131,
+/* Replaces solvers.dg.predictor (solvers/dg/dg.h:7, dg1.cpp:58-114,
  * dg2.cpp:102-171): local space-time Galerkin predictor of every masked cell.
  * Picard iteration with the reference's initial guess, update and per-cell
  * stopping rule (|dq| <= 6e-6 (1 + |q|), at most 50 iterations).  Cells where
@@ -192,7 +192,7 @@ int gpr_ader_stepper(double *u, const double *ub, const int32_t *nX, int ndim,
                      const gpr_par *par, const uint8_t *mask, double *scratch,
                      int32_t *status, int nvar, void *stream);
 
-/* Replaces solvers.iterator (solvers/iterator.cpp:179-264) for one
+/* Replaces solvers.iterator (solvers/iterator.cpp:85-170) for one
  * material, device resident: runs `nsteps` steps of
  *   CFL time step -> boundaries -> WENO -> predictor -> FV -> renorm
  * with the clock in device memory, clock[5] = {t, dt, tf, cfl, count}
@@ -209,7 +209,7 @@ int gpr_iterate(double *u, const int32_t *nX, int ndim, const double *dX,
 
 /* After each step of gpr_iterate, gpr_iterate_split and gpr_iterate_multi:
  * contorted + reset_distortion (solvers/utils.cpp:44-85, called by
- * iterator.cpp:149-150 with the driver's contorted_tol, 1.0 in
+ * iterator.cpp:150-151 with the driver's contorted_tol, 1.0 in
  * code/python/main.py:21): if any cell's normalised distortion has
  * m0 - 1 > contorted_tol, m0 = |A|_F^2 / (3 |det A|^(2/3)), every cell of a
  * non-vacuum material gets A = (rho / rho0)^(1/3) I and loses its distortion
@@ -251,7 +251,7 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
  *                     the node values without sources or time integration,
  *                     ODE half step on u.  scratch: gpr_split_scratch_doubles.
  * gpr_iterate_split   gpr_iterate with the split scheme in place of the ADER
- *                     step (iterator.cpp:204-245); scratch: gpr_iterate_scratch_doubles. */
+ *                     step (iterator.cpp:109-151); scratch: gpr_iterate_scratch_doubles. */
 int gpr_midstepper(double *wh, double dt, const double *dX, int ndim, const int32_t *nX,
                    const gpr_par *par, const uint8_t *mask, int nvar, void *stream);
 long gpr_split_scratch_doubles(const int32_t *nX, int ndim, int nvar);
@@ -267,7 +267,7 @@ int gpr_iterate_split(double *u, const int32_t *nX, int ndim, const double *dX,
 /* Batched form: many independent 1D grids (instances) of uneven sizes, each
  * with its own material, boundary codes and CFL clock, advanced together by
  * one launch per stage (no counterpart in the reference, which runs one grid
- * per `iterator` call; each instance follows solvers/iterator.cpp:204-245).
+ * per `iterator` call; each instance follows solvers/iterator.cpp:109-151).
  *
  * Instances are packed one after another in u: instance k owns
  * u[off_k .. off_k + nx[k]) cells, off_k = nx[0] + ... + nx[k-1].  The
@@ -437,7 +437,7 @@ int gpr_Bdot(const double *Q, const double *x, double *out, int64_t count,
 int gpr_max_abs_eigs(const double *Q, double *out, int64_t count, int d,
                      const gpr_par *par, int nvar, void *stream);
 /* out[count][V][V] (row = equation) = the system matrix dF_d/dQ + B_d of
- * the quasi-linear form along d (system/equations.cpp:169-177). */
+ * the quasi-linear form along d (system/equations.cpp:169-176). */
 int gpr_system_matrix(const double *Q, double *out, int64_t count, int d,
                       const gpr_par *par, int nvar, void *stream);
 /* out[count][m][m] = Xi1 Xi2 along d (eig.cpp:55-64), m = 4 with heat

@@ -570,7 +570,7 @@ class Oracle:
     # -- a full run ------------------------------------------------------------
     def run(self, u0, MP, tf, dX, bcs, cfl=0.8, flux=0, max_steps=None,
             split=False, half_step=True, contorted_tol=None):
-        """Time loop of solvers/iterator.cpp:179-264 for one material
+        """Time loop of solvers/iterator.cpp:85-170 for one material
         (boundaries -> timestep -> stepper -> renorm [-> contortion reset if
         contorted_tol is given]), returning the final state and the number
         of steps."""

@@ -698,7 +698,7 @@ void or_source(const double *Q, const gpr_par *P, double *ret) {
   }
 }
 
-/* ret = B_d(Q) x   (equations.cpp:189-267) */
+/* ret = B_d(Q) x   (equations.cpp:89-167) */
 void or_Bdot(const double *Q, const double *x, int d, double *ret) {
   double r = Q[0];
   double v0 = Q[2] / r, v1 = Q[3] / r, v2 = Q[4] / r;
@@ -1096,7 +1096,7 @@ double or_max_abs_eigs(const double *Q, int d, const gpr_par *P) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* System Jacobian (system/jacobians.cpp:10-152, equations.cpp:169-187).   */
+/* System Jacobian (system/jacobians.cpp:10-152, equations.cpp:69-87, 169-176). */
 
 static double dEdrho_Q(const double *Q, const gpr_par *P) {
   double r = Q[0];
@@ -1250,7 +1250,7 @@ static void dPdQ(const double *Q, const gpr_par *P, double *ret) {
 #undef R_
 }
 
-/* system_matrix = dFdP dPdQ + B   (equations.cpp:269-276) */
+/* system_matrix = dFdP dPdQ + B   (equations.cpp:169-176) */
 void or_system_matrix(const double *Q, int d, const gpr_par *P, double *M) {
   int n = V;
   double *F = malloc(sizeof(double) * n * n * 2);
@@ -1265,7 +1265,7 @@ void or_system_matrix(const double *Q, int d, const gpr_par *P, double *M) {
       M[i * n + j] = s;
     }
   free(F);
-  /* block (equations.cpp:169-187) */
+  /* block (equations.cpp:69-87) */
   double r = Q[0];
   double vd = Q[2 + d] / r;
   for (int i = 5; i < 14; i++)
@@ -2221,7 +2221,7 @@ static int dg_stiff(int ndim, double *q, const double *Ww, double dt, const doub
 
 int or_stiff_iterations_hist[64];
 
-/* predictor1 / predictor2 (dg1.cpp:75-131, dg2.cpp:102-171).  status[cell]
+/* predictor1 / predictor2 (dg1.cpp:58-114, dg2.cpp:102-171).  status[cell]
  * receives: Picard iteration count (>0) when the reference's Picard
  * converged; -(Newton iterations) - 1000 when Picard failed and the oracle's
  * Newton solve converged; -1 when neither converged (row left unwritten, as
@@ -2516,7 +2516,7 @@ int or_fv_launcher(double *u, const double *qh, const int *nX, double dt,
 }
 
 /* ------------------------------------------------------------------------ */
-/* CFL time step, distortion housekeeping (solvers/iterator.cpp:148-177,    */
+/* CFL time step, distortion housekeeping (solvers/iterator.cpp:54-83,    */
 /* solvers/utils.cpp:6-23).                                                  */
 
 double or_timestep(const double *u, long ncell, const double *dX, int ndim,
@@ -3530,7 +3530,7 @@ static int ls_converged(const double *QL, const double *QR, const gpr_par *PL,
   return mx / (PL->b02 * PL->rho0) < STAR_TOL;
 }
 
-/* star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:57-90). */
+/* star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:31-64). */
 static int ls_star_step(double *QL, double *QR, const gpr_par *PL, const gpr_par *PR) {
   double RL[MAXV * 3], RR[MAXV * 3], xL[3], xR[3], cL[3], cR[3], Pv[MAXV];
   if (ls_constraints(QL, 1, PL, RL))

@@ -2,7 +2,7 @@
 GPR runs with respect to their initial states and material parameters.
 
 The forward pass is the batched time loop (phd_gb300.batch; the reference's
-solvers.iterator, code/cpp/src/solvers/iterator.cpp:179-264, per instance)
+solvers.iterator, code/cpp/src/solvers/iterator.cpp:85-170, per instance)
 with the predictor converged to a tight tolerance, so that its result is the
 fixed point the adjoint differentiates.  It keeps a checkpoint of the states
 and clocks every `checkpoint_every` steps.  The backward pass walks the

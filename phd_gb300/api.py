@@ -412,7 +412,7 @@ def max_abs_eigs(Q, d, MP):
 
 
 def system_matrix(Q, d, MP):
-    """GPRpy.system.system_matrix (system/equations.cpp:169-177): dF_d/dQ +
+    """GPRpy.system.system_matrix (system/equations.cpp:169-176): dF_d/dQ +
     B_d, [..., V, V] with rows the equations."""
     lib, Q, V, count, pp = _pointwise(None, Q, MP)
     out = torch.empty(Q.shape[:-1] + (V, V), dtype=torch.float64, device=Q.device)

@@ -2,7 +2,7 @@
 
 Each instance has its own cell count, material, boundary codes and CFL
 clock (the reference runs one grid per `solvers.iterator` call,
-code/cpp/src/solvers/iterator.cpp:179-264).  All instances are packed into
+code/cpp/src/solvers/iterator.cpp:85-170).  All instances are packed into
 one device buffer and every stage of the step is one kernel launch for all of
 them; the step loop needs no host synchronisation and can be captured in a
 CUDA graph (`capture`).

@@ -1,13 +1,13 @@
 // gpr_adjoint.cuh - hand-written adjoint (reverse mode) of the 1D ADER-WENO
 // step of gpr_kernels.cuh, for the batched packing of many instances.
 //
-// Forward step n (per instance, solvers/iterator.cpp:204-245 with
+// Forward step n (per instance, solvers/iterator.cpp:109-151 with
 // solvers/steppers.cpp:10-48):
 //   dt   = CFL dx / max_c lambda(u_c)        (x 0.2 for the first steps,
 //                                             clipped to tf - t)
 //   ub   = boundaries(u)                     (etc/grid.cpp:12-125)
 //   wh   = WENO(ub)                          (weno/weno.cpp:4-157)
-//   qh   = fixed point of q = DG_U^-1 (W w + dt R(q))   (dg/dg1.cpp:8-131)
+//   qh   = fixed point of q = DG_U^-1 (W w + dt R(q))   (dg/dg1.cpp:8-114)
 //   u'   = u + FV(qh, dt)                    (fv/fv.cpp:11-160)
 //   u+   = renorm(u')                        (solvers/utils.cpp:6-23)
 // Backward step n: given the cotangent of u+, produce the cotangent of u, add

@@ -358,7 +358,7 @@ GPR_D void source(const double *q, const Prim<TH> &s, const DevPar &P, double *S
   }
 }
 
-// B_d(Q) x   (equations.cpp:189-267); v = rho v / rho.
+// B_d(Q) x   (equations.cpp:89-167); v = rho v / rho.
 template <int V, int LSET>
 GPR_D void bdot(const double *v, const double *x, int d, double *out) {
 #pragma unroll

@@ -294,14 +294,14 @@ GPR_D void face_reduce_store(const double *b, const double *f, double kk, bool a
 }
 
 // ---------------------------------------------------------------------------
-// Space-time DG predictor (solvers/dg/dg1.cpp:8-131, dg2.cpp:8-171).
+// Space-time DG predictor (solvers/dg/dg1.cpp:8-114, dg2.cpp:8-171).
 //
 // One thread per space-time node: NP = N^(d+1) consecutive lanes hold one
 // cell (lane g = t N^d + s).  Spatial derivatives, the DG_DER flux term and
 // the DG_U^-1 time coupling need the partner nodes' values, exchanged with
 // warp shuffles (partners differ in one index: lane ^ bit).  Each iteration
 // is the reference's Picard update q <- DG_U^-1 (Ww + dt R(q)) with its
-// per-cell stopping rule |q1 - q0| <= dg_tol (1 + |q0|) (dg1.cpp:108-127).
+// per-cell stopping rule |q1 - q0| <= dg_tol (1 + |q0|) (dg1.cpp:91-110).
 
 // |x| as the bit pattern of a non-negative double; patterns above
 // FP_INF_BITS are NaNs.
@@ -676,8 +676,8 @@ __global__ void __launch_bounds__(128) k_midstep(double *__restrict__ wh, long n
 
 // ---------------------------------------------------------------------------
 // Stiff-source Newton pass for the cells whose Picard iteration failed (the
-// reference leaves their rows unwritten, dg1.cpp:108-127, or falls back to a
-// Jacobian-free Newton-Krylov solve on NaN, dg1.cpp:117-121).
+// reference leaves their rows unwritten, dg1.cpp:91-110, or falls back to a
+// Jacobian-free Newton-Krylov solve on NaN, dg1.cpp:100-105).
 //
 // Iteration on the predictor fixed point Fp(q) = DG_U q - Ww - dt R(q) = 0:
 //   delta = (DG_U - dt W dS/dq)^-1 (Ww + dt R(q) - DG_U q),   q += delta,

@@ -967,7 +967,7 @@ GPR_D bool star_converged(const double *QL, const double *QR, const DevPar &PL,
   return mx / (PL.b02 * PL.rho0) < STAR_TOL;
 }
 
-// star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:57-90).
+// star_stepper (riemann.cpp:156-201) with slip_bcs (conditions.cpp:31-64).
 GPR_D bool star_step(double *QL, double *QR, const DevPar &PL, const DevPar &PR) {
   double RLx[15], RLy[9], cL[3];
   if (!constraints(QL, 1.0, PL, RLx, RLy))

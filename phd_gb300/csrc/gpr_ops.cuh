@@ -340,7 +340,7 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
-  // contorted + reset_distortion after a step (iterator.cpp:147-150); flag
+  // contorted + reset_distortion after a step (iterator.cpp:150-151); flag
   // is device scratch for one int.
   static void contortion(double *u, long ncell, double tol, const DevPar &P0, const DevPar &P1,
                          int *flag, const double *dt_dev, cudaStream_t st) {
@@ -356,7 +356,7 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
-  // One device-resident iterator step (iterator.cpp:204-240 for one
+  // One device-resident iterator step (iterator.cpp:119-151 for one
   // material): CFL -> boundaries -> WENO -> predictor -> FV -> renorm ->
   // clock advance, with dt living in clk[1].
   static int iterate(double *u, const int32_t *nX, int nd, const double *dX,
@@ -447,7 +447,7 @@ template <class L> struct Ops {
     return ncb * ns * V + (w > f ? w : f);
   }
 
-  // Device-resident iterator with the split scheme (iterator.cpp:204-245,
+  // Device-resident iterator with the split scheme (iterator.cpp:109-151,
   // SPLIT = true); scratch as iterate().
   static int iterate_split(double *u, const int32_t *nX, int nd, const double *dX,
                            const int32_t *bcs, const DevPar &P, const uint8_t *mask,

@@ -2,7 +2,7 @@
 // (solvers/fv/fluxes.cpp:22-64): D = sum_i w_i |M(q_i)| (qL - qR) over the
 // Gauss nodes of the straight path q_i = qR + x_i (qL - qR) (Osher), or
 // |sum_i w_i M(q_i)| (qL - qR) (Roe), with M = dF/dQ + B the system matrix
-// (system/equations.cpp:269-276) and |M| = R |Lambda| R^-1 from its real
+// (system/equations.cpp:169-176) and |M| = R |Lambda| R^-1 from its real
 // nonsymmetric eigen-decomposition.
 //
 // The eigen-decomposition (Householder Hessenberg reduction, Francis
@@ -22,7 +22,7 @@ namespace gpr {
 
 constexpr double OSH_MULT_TOL = 1e-12;
 
-// System matrix M = dF_x/dP dP/dQ + B_x (equations.cpp:68-187, 269-276):
+// System matrix M = dF_x/dP dP/dQ + B_x (system/jacobians.cpp:10-152, equations.cpp:69-87, 169-176):
 // row-major V x V into M (ld = V).
 // dF_x/dP into F and dP/dQ into D (V x V row-major, zeroed by the caller).
 template <bool TH, int V>
@@ -180,7 +180,7 @@ GPR_D void system_fd(const double *Q, const Prim<TH> &s, const DevPar &P, double
 #undef RD
 }
 
-// M += the non-conservative block B_x (equations.cpp:169-187)
+// M += the non-conservative block B_x (equations.cpp:69-87)
 template <int V> GPR_D void system_block(const double *v, double *M) {
   constexpr int d = 0;
 #pragma unroll

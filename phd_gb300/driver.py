@@ -1,5 +1,5 @@
 """Time loop of the reference's `solvers.iterator` (code/cpp/src/solvers/
-iterator.cpp:179-264) for one material, on the GPU: CFL time step ->
+iterator.cpp:85-170) for one material, on the GPU: CFL time step ->
 boundaries -> ADER step (or the split scheme, SPLIT = True) -> distortion
 renormalisation -> contortion reset (solvers/utils.cpp:44-85), with the
 reference's 100-snapshot return convention and NaN early exit."""

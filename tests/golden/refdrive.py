@@ -62,7 +62,7 @@ def random_state(rng, MP, V=17, vscale=1.0, jscale=1.0, lset=0):
 
 def run_ref(R, u0, MP, tf, dX, bcs, cfl=0.8, flux=0, max_steps=None,
             split=False, half_step=True, stiff=False):
-    """Reference time loop for one material: solvers/iterator.cpp:204-260
+    """Reference time loop for one material: solvers/iterator.cpp:109-167
     restricted to boundaries -> timestep -> stepper -> renorm (no level set,
     no contortion reset)."""
     P = to_ref_par(R, MP)

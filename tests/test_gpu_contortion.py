@@ -1,5 +1,5 @@
 """The contortion check and reset (solvers/utils.cpp:44-85, applied by the
-reference's time loop after every step, iterator.cpp:149-150) on the GPU:
+reference's time loop after every step, iterator.cpp:150-151) on the GPU:
 gpr_reset_contorted against the oracle and the reference's golden vectors,
 and the time loops with a tolerance that triggers a reset against the
 reference's own loop."""
