@@ -52,6 +52,26 @@ def test_pointwise_physics(G):
                            g["system_matrix"][m, :, d]) < 1e-13
 
 
+def test_source_over_a_wide_range_of_det_A(G):
+    """The distortion source (det(A)^(5/3) by CUDA's cbrt) against the
+    oracle's C library cbrt on states with A scaled so that det A spans
+    1e-9 .. 1e9 and beyond."""
+    O = Oracle()
+    g = golden("pointwise_v17.npz")
+    MP = Par.from_array(g["mp_arrays"][0])
+    rng = np.random.default_rng(3)
+    Q = []
+    for f in np.concatenate([10.0 ** rng.uniform(-3, 3, 60), [1e11, 1e-11, 1.0]]):
+        q = g["Q"][0, rng.integers(g["Q"].shape[1])].copy()
+        q[5:14] *= f
+        Q.append(q)
+    Q = np.array(Q)
+    got = H(G.system.source(T(Q), MP))
+    ref = np.array([O.source(q, MP) for q in Q])
+    scale = np.abs(ref).max(axis=1, keepdims=True) + 1e-300
+    assert (np.abs(got - ref) / scale).max() < 1e-14
+
+
 def test_ode_step(G):
     g = golden("pointwise_v17.npz")
     for m in range(g["Q"].shape[0]):
