@@ -1058,6 +1058,68 @@ __global__ void __launch_bounds__(128) k_faces1d(
   face_reduce_store<V, NN>(b, f, kk, active, valid, t, fb + fo * 2 * V);
 }
 
+// 1D faces for small grids, where a kernel's time is the length of one
+// lane's FP64 instruction chain: one lane per (face, time node, side).  The
+// lane of side 0 (1) evaluates the primitives, wave speed and flux of qL
+// (qR) and the path integral's node 0 (1); the wave speeds are exchanged,
+// the side-0 lane adds the dissipation, and the four lanes' contributions
+// are summed by the reduce-scatter (the same terms as interface_point).
+template <class L>
+__global__ void __launch_bounds__(128) k_faces1d_split(
+    double *__restrict__ fb, const double *__restrict__ qh, long nface,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int time_dg, DevPar P, Consts C) {
+  constexpr int V = L::V;
+  static_assert(NN == 2, "two time nodes and two path nodes");
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int lq = threadIdx.x % 4, t = lq >> 1, side = lq & 1;
+  long face = gt / 4;
+  bool valid = face < nface;
+  long fi = valid ? face : 0;
+  bool active = valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
+  int nt = time_dg ? NN : 1;
+  double ql[V], qr[V], f[V], b[V], dq[V];
+  const double *ql_ = qh + (fi * nt + (time_dg ? t : 0)) * NN * V;
+  const double *qr_ = qh + ((fi + 1) * nt + (time_dg ? t : 0)) * NN * V;
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    ql[k] = C.endv[1][0] * ql_[k] + C.endv[1][1] * ql_[V + k];
+    qr[k] = C.endv[0][0] * qr_[k] + C.endv[0][1] * qr_[V + k];
+    dq[k] = qr[k] - ql[k];
+    b[k] = 0.0;
+  }
+  const double kk = (time_dg ? dt * C.w[t] : dt) / (2.0 * dx);
+  const double *qs = side ? qr : ql;
+  Prim<L::THERMAL> ps;
+  prim<L::THERMAL>(qs, P, ps);
+  const double lam = max_abs_eigs<L::THERMAL>(qs, ps, 0, P);
+  const double lo = __shfl_xor_sync(0xffffffffu, lam, 1);
+  const double m1 = side ? lo : lam, m2 = side ? lam : lo;  // lambda(qL), lambda(qR)
+  const double m = m1 > m2 ? m1 : m2;                        // std::max(m1, m2)
+  flux_set<L::THERMAL, V>(qs, ps, 0, P, f);
+  if (side == 0) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      f[k] += m * (ql[k] - qr[k]);
+  }
+  // Bint node `side`: W_n B(qL + x_n dq) dq   (fluxes.cpp:9-20)
+  {
+    const double xn = C.nodes[side], wn = C.w[side];
+    double ir = 1.0 / (ql[0] + xn * dq[0]);
+    double v[3] = {(ql[2] + xn * dq[2]) * ir, (ql[3] + xn * dq[3]) * ir,
+                   (ql[4] + xn * dq[4]) * ir};
+    double bd[V];
+    bdot<V, L::LSET>(v, dq, 0, bd);
+#pragma unroll
+    for (int k = 5; k < V; k++)
+      if (k < 14 || k >= V - L::LSET)
+        b[k] = wn * bd[k];
+  }
+  face_reduce_store<V, 4>(b, f, kk, active, valid, lq, fb + fi * 2 * V);
+}
+
 // 2D faces: direction dir, faces (i, j) of the (nx+1) x (ny+1) face grid,
 // between predictor cells (i, j) and (i+1, j) (dir 0) or (i, j+1) (dir 1);
 // NQ = N*N lanes per face (time node t, transverse node s).

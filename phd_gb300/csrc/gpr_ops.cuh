@@ -245,9 +245,9 @@ template <class L> struct Ops {
       long nf = (long)(nx + 1) * NN;
       if (!faces)
         ;
-      else if (flux == GPR_FLUX_RUSANOV)
-        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(scratch, qh, (long)nx + 1, mask, dt,
-                                                       dt_dev, dX[0], time_dg, P, C, Batch{});
+      else if (flux == GPR_FLUX_RUSANOV)  // one lane per (face, time node, side)
+        k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
+            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, P, C);
       else
         k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
             scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
@@ -289,8 +289,8 @@ template <class L> struct Ops {
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
       if (flux == GPR_FLUX_RUSANOV)
-        k_faces1d<L><<<blocks(nf, 128), 128, 0, st>>>(fb, qh, (long)nx + 1, mask, dt, nullptr,
-                                                       dX[0], time_dg, P, C, Batch{});
+        k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
+            fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, P, C);
       else
         k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
             fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, flux, P, C, Batch{});
