@@ -34,20 +34,16 @@ TapeLayout tape_layout_v(int ninst, const int32_t *nx, int V) {
   return t;
 }
 
-// Backward-step scratch: Jacobian columns at the nodes (F, S; written only
-// for the cells of the dense solve), lambda and eigen data at the ends,
-// cotangents of qh and wh, stencil cotangents, per-cell material-field and
-// dt partial sums.
+// Backward-step scratch: lambda and eigen data at the ends, cotangents of
+// qh and wh, stencil cotangents, per-cell material-field and dt partial sums.
 struct AdjLayout {
-  long o_jn, o_ev, o_eig, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
+  long o_ev, o_eig, o_qb, o_wb, o_g, o_thf, o_thp, o_dtf, o_dtp, o_mu, o_need, total;
 };
 
 AdjLayout adj_layout_v(int ninst, const int32_t *nx, int V) {
   BatchLayout b = batch_layout_v(ninst, nx, V);
-  const long K = V + NPD;
   Carve cv;
   AdjLayout a;
-  a.o_jn = cv.take(b.nb * 4 * K * 2 * V);
   // lambda and eigen data at the cell ends, then at the CFL argmax states
   a.o_ev = cv.take(b.nb * 4 + ninst);
   a.o_eig = cv.take((b.nb * 4 + ninst) * 17);
@@ -134,7 +130,7 @@ template <class L> struct Adj {
                             const_cast<double *>(tape + tl.o_clk));
     const double *un = tape + tl.o_un, *qh = tape + tl.o_qh, *up = tape + tl.o_up,
                  *aux = tape + tl.o_aux;
-    double *JN = ascr + al.o_jn, *EV = ascr + al.o_ev, *EIG = ascr + al.o_eig,
+    double *EV = ascr + al.o_ev, *EIG = ascr + al.o_eig,
            *EVs = EV + b.nb * 4, *EIGs = EIG + b.nb * 4 * Xi<L::THERMAL>::ND,
            *qb = ascr + al.o_qb, *wb = ascr + al.o_wb, *g = ascr + al.o_g,
            *thf = ascr + al.o_thf, *thp = ascr + al.o_thp, *dtf = ascr + al.o_dtf,
@@ -147,8 +143,12 @@ template <class L> struct Adj {
         ubar, qh, EV, EIG, un, up, b.nb, qb, thf, dtf, C, B);
     k_adj_pred_iter<L><<<blocks(b.nb * 4, ADJ_IT_T), ADJ_IT_T, 0, st>>>(qh, qb, b.nb, mu, need,
                                                                          info, C, B);
-    k_adj_jac_nodes<L><<<blocks(b.nb * 4 * K, 128), 128, 0, st>>>(qh, b.nb, need, JN, B);
-    k_adj_pred_dense<L><<<(unsigned)b.nb, 128, 0, st>>>(qh, qb, JN, b.nb, need, mu, info, C, B);
+    // above 48 KB of dynamic shared memory needs the opt-in (per device)
+    constexpr size_t dsmem = dense_smem_bytes<V>();
+    if (cudaFuncSetAttribute(k_adj_pred_dense<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)dsmem) != cudaSuccess)
+      return GPR_E_CUDA;
+    k_adj_pred_dense<L><<<(unsigned)b.nb, 128, dsmem, st>>>(qh, qb, b.nb, need, mu, info, C, B);
     k_adj_pred_post<L><<<blocks(b.nb * 4, 128), 128, 0, st>>>(qh, mu, b.nb, wb, thp, dtp, C, B);
     k_adj_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wb, un, b.nb, g, C, B);
     k_adj_gather<V><<<blocks(b.nu * V, 256), 256, 0, st>>>(ubar, g, b.nu, B);

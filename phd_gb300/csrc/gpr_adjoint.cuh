@@ -1009,37 +1009,6 @@ __global__ void __launch_bounds__(128) k_adj_eig(const double *__restrict__ qh, 
   xi_eigdata_l2<m>(Xv, l2, EIG + gid * ND);
 }
 
-// Jacobian columns at the 4 space-time nodes of the predictor cells the
-// dense solve takes (need[c]): F and S, JN[((c*4 + e)*K + k)*2V + o].
-template <class L>
-__global__ void __launch_bounds__(128) k_adj_jac_nodes(const double *__restrict__ qh, long nb,
-                                                       const int32_t *__restrict__ need,
-                                                       double *__restrict__ JN, Batch B) {
-  constexpr int V = L::V, K = V + NPD;
-  long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (gid >= nb * 4 * K)
-    return;
-  int k = gid % K;
-  long pt = gid / K;  // c*4 + e
-  long c = pt / 4;
-  int inst = B.inst_b[c];
-  if (B.clk[5 * inst + 1] == 0.0 || !need[c])
-    return;
-  double qp[V];
-  const double *src = qh + pt * V;
-#pragma unroll
-  for (int j = 0; j < V; j++)
-    qp[j] = src[j];
-  Dual F[V], S[V];
-  point_tangent<L>(qp, k, B.P[inst], F, S, nullptr);
-  double *o = JN + (pt * K + k) * 2 * V;
-#pragma unroll
-  for (int j = 0; j < V; j++) {
-    o[j] = F[j].d;
-    o[V + j] = S[j].d;
-  }
-}
-
 // One face's contribution to the cotangent of the state on one side.
 // Face flux f = max(lamL, lamR)(qL - qR) + F(qL) + F(qR) (fluxes.cpp:66-75),
 // path integral b = sum_n w_n B(qL + x_n dq) dq (fluxes.cpp:9-20); the left
@@ -1252,8 +1221,8 @@ __global__ void __launch_bounds__(4 * ADJ_FV_PAIRS) k_adj_fv(
 // where the forward Picard iteration does, each lane applying (dR/dq)^T at
 // its node by one reverse-mode product of F and S; cells it leaves
 // unconverged (those the forward hands to its Newton pass) get the exact
-// dense solve of stage 2 (k_adj_pred_dense, one block per cell, over the
-// node Jacobians k_adj_jac_nodes builds for those cells only); stage 3
+// dense solve of stage 2 (k_adj_pred_dense, one block per cell, building
+// that cell's node Jacobians itself); stage 3
 // (k_adj_pred_post) forms the cotangents from mu.
 // Primal values that the reverse sweep of F and S reads at one node, cached
 // once per node for the transposed iteration (structure of arrays with
@@ -1790,15 +1759,23 @@ GPR_D double Bx_mat(int r, int c, const double *v) {
 }
 
 // Exact transposed solve (DG_U - dt dR/dq)^T mu = qbar for the cells the
-// iteration left unconverged: the 4V x 4V system assembled from the node
-// Jacobians in shared memory, Gaussian elimination with partial pivoting.
+// iteration left unconverged: the cell's node Jacobians (state columns, by
+// dual numbers, one thread per node and column) and the 4V x 4V system in
+// dynamic shared memory (dense_smem_bytes), Gaussian elimination with
+// partial pivoting.
+template <int V> constexpr size_t dense_smem_bytes() {
+  return sizeof(double) * ((size_t)4 * V * (4 * V + 1) + (size_t)4 * V * 2 * V);
+}
+
 template <class L>
 __global__ void __launch_bounds__(128) k_adj_pred_dense(
-    const double *__restrict__ qh, const double *__restrict__ qbar, const double *__restrict__ JN,
-    long nb, const int32_t *__restrict__ need, double *__restrict__ mu_buf,
-    int32_t *__restrict__ info, Consts C, Batch B) {
-  constexpr int V = L::V, K = V + NPD, NQ = 4 * V, LD = NQ + 1;
-  __shared__ double A[NQ * LD];
+    const double *__restrict__ qh, const double *__restrict__ qbar, long nb,
+    const int32_t *__restrict__ need, double *__restrict__ mu_buf, int32_t *__restrict__ info,
+    Consts C, Batch B) {
+  constexpr int V = L::V, NQ = 4 * V, LD = NQ + 1;
+  extern __shared__ double dsm[];
+  double *A = dsm;              // [NQ][LD], transposed system
+  double *JS = dsm + NQ * LD;   // [node][j][F_o, S_o] = d(F_o, S_o)/dq_j
   __shared__ double b[NQ], lcol[NQ];
   __shared__ double xs[4][V], vs[4][3], iq0[4];
   __shared__ int piv;
@@ -1823,6 +1800,17 @@ __global__ void __launch_bounds__(128) k_adj_pred_dense(
   }
   if (threadIdx.x == 0)
     bad = 0;
+  for (int e = threadIdx.x; e < 4 * V; e += blockDim.x) {
+    const int g = e / V, j = e % V;
+    Dual F[V], S[V];
+    point_tangent<L>(qc + g * V, j, B.P[inst], F, S, nullptr);
+    double *o = JS + (g * V + j) * 2 * V;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      o[k] = F[k].d;
+      o[V + k] = S[k].d;
+    }
+  }
   __syncthreads();
   for (int e = threadIdx.x; e < NQ * NQ; e += blockDim.x) {
     int row = e / NQ, col = e % NQ;  // entry M[row][col]
@@ -1830,7 +1818,7 @@ __global__ void __launch_bounds__(128) k_adj_pred_dense(
     int t = gr / 2, i = gr % 2, tc = gc / 2, m = gc % 2;
     double val = (i == m && vr == vc) ? C.dgmat[t][tc] * C.w[i] : 0.0;
     if (t == tc) {
-      const double *Jn = JN + (c * 4 + gc) * K * 2 * V;
+      const double *Jn = JS + gc * V * 2 * V;
       double wn = C.w[t] * C.w[i];
       double r = -C.w[t] * idx * C.dgder[i][m] * Jn[vc * 2 * V + vr];
       if (i == m)
