@@ -465,7 +465,12 @@ def run_gb300(args):
             "tgv_roe_osher": flux2d,
             "shock_bubble": bubble,
             "adjoint": adjoint,
-            "gpu_launches": 14 * args.steps,
+            # kernels of one 2D gpr_iterate step: k_cfl_max, k_clock_finalize,
+            # k_fill_interior, k_ghosts x2, k_weno2d_x, k_weno2d_y,
+            # k_predictor_first, k_predictor_picard, k_predictor_stiff,
+            # k_faces2d x2, k_cells, k_renorm, k_contorted, k_reset_distortion,
+            # k_clock_advance (profiles/launches_tgv512.md lists them)
+            "gpu_launches": 17 * args.steps,
             "clocks": cs.summary()}
     if peak_err:
         line["roofline"]["peak_error"] = peak_err
