@@ -29,7 +29,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# BASELINE.json's metric; "value" is its first part (plain path, TGV 512^2
+# The headline metric; "value" is its first part (plain path, TGV 512^2
 # step), the batched form and adjoint / forward ratio are the "batched" and
 # "adjoint" objects of the same line.
 METRIC = "FP64 Mcell-updates/s plain vs batched; adjoint\u00f7forward time at 1e-6 grad err"
