@@ -98,6 +98,20 @@ def dist_info():
     return rank, world, local
 
 
+def replicas_result(ms, ncell, steps, world, device):
+    """N independent replicas (one per rank, no collective in the step): the
+    timed region's duration is the maximum over ranks, and the whole job
+    advanced every rank's ncell cells for `steps` steps.  Returns (ms, value
+    in Mcell-updates/s)."""
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    return ms, ncell * world * steps / (ms * 1e-3) / 1e6
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
 
@@ -357,14 +371,8 @@ def run_gb300(args):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms, value = replicas_result(e0.elapsed_time(e1), ncell, args.steps, world, dev)
     ms_per_step = ms / args.steps
-    value = ncell * world * args.steps / (ms * 1e-3) / 1e6
     st = status.cpu().numpy()
     iters = (st >> 8)
     kind = st & 0xff
