@@ -78,6 +78,14 @@ typedef struct gpr_par {
 
 /* Returns the library version as an integer (major*10000+minor*100+patch). */
 int gpr_version(void);
+/* The scheme's constants on the host (no GPU needed), N = 2 Gauss nodes:
+ * out[] = nodes[N], weights[N] (solvers.common.scaled_nodes /
+ * scaled_weights, poly/basis.cpp), end values [2][N] (end_values: psi_j(0),
+ * psi_j(1)), derivative values [N][N] (derivative_values: psi_j'(x_i)),
+ * WENO oscillation indicator [N][N] (solvers.weno.oscillation_indicator,
+ * weno_matrices.cpp:31-42).  Returns the count written (16), or GPR_E_ARG
+ * when n is smaller. */
+int gpr_scheme_constants(double *out, int n);
 /* Writes the V values compiled in (up to `cap`) and returns how many. */
 int gpr_supported_nvars(int32_t *out, int cap);
 

@@ -70,7 +70,10 @@ def _renorm_distortion(u, MPs):
 
 
 solvers = SimpleNamespace(
-    weno=SimpleNamespace(weno_launcher=api.weno_launcher),
+    weno=SimpleNamespace(weno_launcher=api.weno_launcher,
+                         oscillation_indicator=api.oscillation_indicator),
+    common=SimpleNamespace(scaled_nodes=api.scaled_nodes, scaled_weights=api.scaled_weights,
+                           end_values=api.end_values, derivative_values=api.derivative_values),
     dg=SimpleNamespace(predictor=api.predictor),
     fv=SimpleNamespace(fv_launcher=api.fv_launcher, centers1=api.centers1,
                        centers2=api.centers2, interfs1=api.interfs1, interfs2=api.interfs2,

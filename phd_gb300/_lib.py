@@ -69,6 +69,7 @@ _I64 = ctypes.c_int64
 
 SIGNATURES = {
     "gpr_version": (_I, []),
+    "gpr_scheme_constants": (_I, [_P, _I]),
     "gpr_supported_nvars": (_I, [_P, _I]),
     "gpr_boundaries": (_I, [_P, _P, _P, _I, _P, _I, _P]),
     "gpr_extend_mask": (_I, [_P, _P, _P, _I, _P]),

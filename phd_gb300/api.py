@@ -411,6 +411,44 @@ def max_abs_eigs(Q, d, MP):
     return out
 
 
+def _scheme_constants():
+    lib = _lib.load()
+    out = np.zeros(16, dtype=np.float64)
+    _lib.check(lib.gpr_scheme_constants(out.ctypes.data_as(ctypes.c_void_p), out.size),
+               "scheme_constants")
+    return out
+
+
+def scaled_nodes():
+    """GPRpy.solvers.common.scaled_nodes (poly/basis.cpp): the N Gauss-Legendre
+    nodes on [0, 1] the kernels use."""
+    return _scheme_constants()[0:2].copy()
+
+
+def scaled_weights():
+    """GPRpy.solvers.common.scaled_weights: the Gauss-Legendre weights on [0, 1]."""
+    return _scheme_constants()[2:4].copy()
+
+
+def end_values(basis=None):
+    """GPRpy.solvers.common.end_values: [psi_j(0); psi_j(1)] of the nodal
+    Lagrange basis (2 x N).  The basis argument of the reference is accepted
+    and ignored: the basis is the one on the Gauss nodes."""
+    return _scheme_constants()[4:8].reshape(2, 2).copy()
+
+
+def derivative_values(basis=None, nodes=None):
+    """GPRpy.solvers.common.derivative_values: psi_j'(x_i) (N x N) at the Gauss
+    nodes (arguments accepted and ignored, as in end_values)."""
+    return _scheme_constants()[8:12].reshape(2, 2).copy()
+
+
+def oscillation_indicator(basis=None):
+    """GPRpy.solvers.weno.oscillation_indicator (weno_matrices.cpp:31-42): the
+    WENO smoothness matrix sum_a int psi_i^(a) psi_j^(a) (N x N)."""
+    return _scheme_constants()[12:16].reshape(2, 2).copy()
+
+
 def system_matrix(Q, d, MP):
     """GPRpy.system.system_matrix (system/equations.cpp:169-176): dF_d/dQ +
     B_d, [..., V, V] with rows the equations."""

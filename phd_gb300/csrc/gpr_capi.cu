@@ -93,6 +93,28 @@ extern "C" {
 
 int gpr_version(void) { return 100; }
 
+int gpr_scheme_constants(double *out, int n) {
+  constexpr int COUNT = 4 * NN + 2 * NN * NN;  // nodes, weights, end values; 2 N x N
+  if (!out || n < COUNT)
+    return GPR_E_ARG;
+  const Consts &C = consts();  // host values (make_consts), no device call
+  int k = 0;
+  for (int i = 0; i < NN; i++)
+    out[k++] = C.nodes[i];
+  for (int i = 0; i < NN; i++)
+    out[k++] = C.w[i];
+  for (int e = 0; e < 2; e++)
+    for (int j = 0; j < NN; j++)
+      out[k++] = C.endv[e][j];
+  for (int i = 0; i < NN; i++)
+    for (int j = 0; j < NN; j++)
+      out[k++] = C.derv[i][j];
+  for (int i = 0; i < NN; i++)
+    for (int j = 0; j < NN; j++)
+      out[k++] = C.sig[i][j];
+  return k;
+}
+
 int gpr_supported_nvars(int32_t *out, int cap) {
   static const int32_t vs[] = {17, 14, 15};
   int n = 0;

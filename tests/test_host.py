@@ -134,3 +134,20 @@ def test_adjoint_field_jacobian_matches_finite_differences():
         fd = (np.array(dev_fields(make_par(tp))) - np.array(dev_fields(make_par(tm)))) / (2 * h)
         scale = np.abs(fd) + np.abs(J[:, j]) + 1e-12
         assert (np.abs(J[:, j] - fd) / scale).max() < 1e-7, (j, J[:, j], fd)
+
+
+def test_scheme_constants_without_gpu():
+    """solvers.common.* and solvers.weno.oscillation_indicator: the constants
+    the kernels use, from the library on the host, against the oracle's
+    (pinned by the golden stage tests) and the closed forms."""
+    import phd_gb300 as G
+    from oracle import Oracle
+    c = Oracle().constants()
+    s3 = 1 / np.sqrt(3)
+    nodes = G.solvers.common.scaled_nodes()
+    assert np.allclose(nodes, [(1 - s3) / 2, (1 + s3) / 2], rtol=0, atol=1e-16)
+    assert np.allclose(nodes, c["nodes"], rtol=0, atol=1e-16)
+    assert np.allclose(G.solvers.common.scaled_weights(), c["weights"], rtol=0, atol=1e-15)
+    assert np.allclose(G.solvers.common.end_values(), c["endvals"], rtol=0, atol=1e-15)
+    assert np.allclose(G.solvers.common.derivative_values(), c["dervals"], rtol=0, atol=1e-14)
+    assert np.allclose(G.solvers.weno.oscillation_indicator(), c["sig"], rtol=0, atol=1e-13)
