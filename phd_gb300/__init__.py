@@ -27,7 +27,9 @@ extend_mask = api.extend_mask
 options = SimpleNamespace(N=lambda: 2, NV=lambda: 17, VISCOUS=lambda: True,
                           THERMAL=lambda: True, MULTI=lambda: False, LSET=lambda: 0)
 
-classes = SimpleNamespace(Par=Par)
+# The reference binds both Params and its subclass Par (system/objects.h:22-60);
+# a Par carries every Params field, so one class serves both names.
+classes = SimpleNamespace(Par=Par, Params=Par)
 
 system = SimpleNamespace(flux=api.flux, source=api.source, Bdot=api.Bdot,
                          max_abs_eigs=api.max_abs_eigs, system_matrix=api.system_matrix,

@@ -39,6 +39,53 @@ def test_library_reports_version_without_gpu():
     assert 17 in list(buf)[:n]
 
 
+# The names the reference's GPRpy module binds (bindings/bindings.cpp:69-265),
+# split into those this package mirrors and those it leaves out: the EOS /
+# Jacobian scalars and the inner steps of bound functions (computed inside
+# the kernels), the reactive and multi-phase hooks, the SciPy ports (replaced
+# by the device Newton pass), the polynomial objects and forward stencil
+# matrices, and rotate_distortion (off in options.h:16).
+BOUND = """options.N options.NV options.VISCOUS options.THERMAL options.MULTI options.LSET
+classes.Params classes.Par boundaries extend_mask
+multi.renormalize_levelsets multi.finite_difference multi.find_interface_cells
+multi.fill_boundary_cells multi.fill_neighbor_cells multi.fill_ghost_cells
+multi.material_indicator system.flux system.source system.Bdot system.system_matrix
+system.max_abs_eigs system.thermo_acoustic_tensor system.multi.left_star_state
+system.multi.distance solvers.common.scaled_nodes solvers.common.scaled_weights
+solvers.common.end_values solvers.common.derivative_values solvers.extended_dimensions
+solvers.ader_stepper solvers.ader_stepper_para solvers.split_stepper
+solvers.split_stepper_para solvers.iterator solvers.make_u solvers.contorted
+solvers.timestep solvers.renorm_distortion solvers.weno.oscillation_indicator
+solvers.weno.weno_launcher solvers.split.midstepper solvers.split.ode_launcher
+solvers.fv.Bint solvers.fv.D_RUS solvers.fv.D_ROE solvers.fv.D_OSH solvers.fv.centers1
+solvers.fv.centers2 solvers.fv.interfs1 solvers.fv.interfs2 solvers.fv.fv_launcher""".split()
+NOT_BOUND = """classes.poly scipy.lgmres_wrapper scipy.newton_krylov system.block
+system.reaction_rate system.ode_stepper_numerical system.dFdP system.dPdQ
+system.multi.eigen system.multi.riemann_constraints system.multi.star_stepper
+solvers.common.basis_polys solvers.rotate_distortion solvers.weno.coefficient_matrices
+solvers.split.analyticSolver_distortion solvers.split.analyticSolver_thermal
+solvers.split.stiff_ode_solve solvers.split.runge_kutta_launcher
+solvers.split.ode_stepper_numerical system.variables.pressure
+system.variables.temperature system.variables.dEdρ system.variables.reaction_rate
+system.variables.solve_multi system.variables.temperature_mg""".split()
+
+
+def _lookup(mod, name):
+    for part in name.split("."):
+        mod = getattr(mod, part)
+    return mod
+
+
+def test_python_mirror_binds_the_reference_names():
+    import phd_gb300 as G
+    assert len(BOUND) + len(NOT_BOUND) == 77 and not set(BOUND) & set(NOT_BOUND)
+    missing = [n for n in BOUND if not callable(_lookup(G, n))]
+    assert not missing, missing
+    for n in NOT_BOUND:
+        with pytest.raises(AttributeError):
+            _lookup(G, n)
+
+
 def test_scratch_queries_and_argument_errors_without_gpu():
     from phd_gb300 import _lib
     lib = _lib.load()
