@@ -12,8 +12,8 @@ advanced one time step), whole job.
 
 --impl reference times the CPU oracle (a C restatement of the reference
 solver; the reference's own C++ cannot be built on the GPU host) on the host
-cores, on a 512 x 64 strip of the same problem (same cell size and time
-step), and prints its own JSON line.
+cores, on the same 512 x 512 problem for the requested steps, and prints its
+own JSON line.
 """
 import argparse
 import ctypes
@@ -37,10 +37,10 @@ UNIT = "Mcell-updates/s"
 
 # Algorithmic FP64 operation counts per unit of work of the algorithm the
 # kernels implement (add/sub/mul/div/sqrt = 1 flop, transcendental call = 1;
-# the FP32 start of the wave-speed root iteration is not counted), from
-# oracle/opcount_device.cpp (profiles/opcount_device_tgv512.txt).  The
-# reference's own formulation needs ~2x more (profiles/opcount_tgv512.txt:
-# it recomputes the pressure per call and runs a QR eigen-solve per wave
+# the FP32 start of the wave-speed root iteration is not counted), counted by
+# oracle/opcount_device.cpp on the device physics compiled for the host.  The
+# reference's own formulation needs ~2x more (oracle/opcount.cpp: it
+# recomputes the pressure per call and runs a QR eigen-solve per wave
 # speed); the roofline uses the work this implementation has to do.
 # The reference driver's contortion tolerance (code/python/main.py:21): a
 # step resets every distortion when one cell's normalised distortion exceeds
@@ -48,8 +48,8 @@ UNIT = "Mcell-updates/s"
 CONTORTED_TOL = 1.0
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-# the TGV 512^2 kernels from one ncu capture each (profiles/k_faces2d_tgv512.md,
-# profiles/k_predictor_picard_tgv512.md).
+# the TGV 512^2 kernels, from an earlier ncu capture of each (not measured by
+# this script; the line labels it so).
 TRAFFIC = {
     "k_faces2d": 287.910912e6 + 289.751808e6,
     "k_predictor_picard": 143.945728e6 + 229.694720e6,
@@ -171,54 +171,76 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm
 
-def cpu_baseline(steps, warmup, n=512, strip=64, cfl=0.4, budget_s=20.0, flux=0):
-    """Oracle (C restatement of the reference solver) on all host cores, on
-    an n x strip slice of the TGV (same dx, dy, time step)."""
+def cpu_baseline(steps, warmup, n=512, cfl=0.4, flux=0):
+    """Oracle (C restatement of the reference solver) on all host cores,
+    `steps` timed steps of the full n x n TGV (after `warmup` untimed ones):
+    timestep -> boundaries -> ADER step -> renorm, the reference iterator's
+    loop body (solvers/iterator.cpp:109-151)."""
     from oracle import Oracle
     from phd_gb300 import problems
     O = Oracle()
     threads = O.num_threads()
     u0, MP, tf, dX, bcs = problems.taylor_green(n=n, cs=10.0, mu=1e-2)
-    u = np.ascontiguousarray(u0[:, :strip, :]).copy()
-    nX = np.array([n, strip], np.int32)
-    ncell = n * strip
+    u = np.ascontiguousarray(u0).copy()
+    nX = np.array([n, n], np.int32)
+    ncell = n * n
     count = 0
+
+    def one():
+        nonlocal count
+        dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
+        ub = O.boundaries(u, nX, [1] * 4)
+        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP, flux=flux)
+        O.renorm_distortion(u.reshape(-1), MP)
+        count += 1
     for _ in range(warmup):
-        dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
-        ub = O.boundaries(u, nX, [1] * 4)
-        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP, flux=flux)
-        O.renorm_distortion(u.reshape(-1), MP)
-        count += 1
+        one()
     t0 = time.perf_counter()
-    done = 0
     for _ in range(steps):
-        dt = O.timestep(u, dX, cfl, 0, 1e9, count, MP)
-        ub = O.boundaries(u, nX, [1] * 4)
-        O.ader_stepper(u.reshape(-1), ub, nX, dt, dX, MP, flux=flux)
-        O.renorm_distortion(u.reshape(-1), MP)
-        count += 1
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
+        one()
     el = time.perf_counter() - t0
-    value = ncell * done / el / 1e6
+    value = ncell * steps / el / 1e6
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "TGV %dx%d strip (same dx, dt as %dx%d), %d steps after %d warm-up, "
-                      "oracle/gpr_oracle.c with %d OpenMP threads" % (n, strip, n, n, done,
-                                                                       warmup, threads),
-            "seconds": el}
+            "sample": "TGV %dx%d (the full grid), %d timed steps after %d warm-up, "
+                      "oracle/gpr_oracle.c with %d OpenMP threads" % (n, n, steps, warmup,
+                                                                      threads),
+            "seconds": el, "ms_per_step": el * 1e3 / max(steps, 1)}
+
+
+def step_vs_oracle(torch, u_dev, MP, nX, dX, bcs, cfl, flux=0, count=10, V=17):
+    """One step of the GPU path and one oracle step from the same state
+    (u_dev, left unchanged): CFL time step (taken by the oracle and given to
+    both), boundaries, ADER step, renormalisation.  Returns (max |a-b| /
+    (1 + |b|), oracle seconds for the step)."""
+    import phd_gb300 as G
+    from oracle import Oracle
+    O = Oracle()
+    nX = np.array(nX, np.int32)
+    u_np = u_dev.detach().cpu().numpy().reshape(tuple(int(k) for k in nX) + (V,)).copy()
+    t0 = time.perf_counter()
+    dt = O.timestep(u_np, dX, cfl, 0.0, 1e9, count, MP)
+    ub = O.boundaries(u_np, nX, bcs)
+    ref = u_np.reshape(-1).copy()
+    O.ader_stepper(ref, ub, nX, dt, dX, MP, flux=flux)
+    O.renorm_distortion(ref, MP)
+    cpu_s = time.perf_counter() - t0
+    u = u_dev.detach().clone().reshape(-1)
+    ubt = torch.empty(int(np.prod(nX + 4)) * V, dtype=torch.float64, device=u.device)
+    G.boundaries(u, ubt, nX, bcs)
+    G.solvers.ader_stepper(u, ubt, nX, dt, dX, False, flux, MP, None)
+    G.solvers.renorm_distortion(u, [MP])
+    got = u.cpu().numpy()
+    return float(np.max(np.abs(got - ref) / (1.0 + np.abs(ref)))), cpu_s
 
 
 def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
         return 0
-    cb = cpu_baseline(args.steps, args.warmup, n=args.n, cfl=args.cfl, budget_s=120.0)
-    # one full n x n step at the rate measured on the strip
-    ms_full = args.n * args.n / (cb["value"] * 1e6) * 1e3
+    cb = cpu_baseline(args.steps, args.warmup, n=args.n, cfl=args.cfl)
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_full, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": "tgv2d_512x512_v17_rusanov_cfl%.2g" % args.cfl,
@@ -479,14 +501,18 @@ def run_gb300(args):
             # k_fill_interior, k_ghosts x2, k_weno2d_x, k_weno2d_y,
             # k_predictor_first, k_predictor_picard, k_predictor_stiff,
             # k_faces2d x2, k_cells, k_renorm, k_contorted, k_reset_distortion,
-            # k_clock_advance (profiles/launches_tgv512.md lists them)
+            # k_clock_advance
             "gpu_launches": 17 * args.steps,
             "clocks": cs.summary()}
     if peak_err:
         line["roofline"]["peak_error"] = peak_err
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(3, 1, n=n, cfl=args.cfl, budget_s=20.0)
+        cb = cpu_baseline(3, 1, n=n, cfl=args.cfl)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # one step of the timed workload against one oracle step from the
+        # same state (the state the timed steps left)
+        line["max_rel_diff_vs_oracle"] = step_vs_oracle(torch, u, MP, nX, dX, [1] * 4,
+                                                        args.cfl)[0]
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -562,8 +588,9 @@ def flux2d_bench(torch, n=512, steps=3, warmup=1, cfl=0.4, cpu=True):
     """The 512 x 512 Taylor-Green step with the Roe (FLUX = 1, the reference
     driver's default, code/python/main.py) and Osher (FLUX = 2) dissipation:
     a V x V eigen-decomposition of the system matrix per face point (and
-    path node), through gpr_iterate; the oracle runs a 512 x 16 strip of the
-    same problem on the host cores."""
+    path node), through gpr_iterate; the oracle runs one step of the same
+    grid on the host cores from the state the timed steps left, and the GPU
+    step from that state is compared with it."""
     import phd_gb300 as G
     from phd_gb300 import _lib
     lib = _lib.load()
@@ -601,8 +628,15 @@ def flux2d_bench(torch, n=512, steps=3, warmup=1, cfl=0.4, cpu=True):
              "value": n * n * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
              "finite": bool(torch.isfinite(u).all().item())}
         if cpu:
-            cb = cpu_baseline(1, 0, n=n, strip=16, cfl=cfl, budget_s=30.0, flux=flux)
-            r["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            # one GPU step and one oracle step from the state the timed steps
+            # left: the difference, and the oracle's time for the full grid
+            from oracle import Oracle
+            err, cpu_s = step_vs_oracle(torch, u, MP, nX, dX, [1] * 4, cfl, flux=flux)
+            r["max_rel_diff_vs_oracle"] = err
+            r["cpu_baseline"] = {"value": n * n / cpu_s / 1e6, "unit": UNIT,
+                                 "cores": Oracle().num_threads(), "kind": "port",
+                                 "sample": "one step of the full %dx%d grid, "
+                                           "oracle/gpr_oracle.c" % (n, n)}
         out[name] = r
     return out
 
@@ -673,8 +707,20 @@ def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
            "e2e": {"value": ncell * steps / (e2e_ms * 1e-3) / 1e6, "unit": UNIT,
                    "h2d_bytes_per_step": ncell * 15 * 8, "d2h_bytes_per_step": ncell * 15 * 8},
            "sim_time": float(clk[0]), "sim_steps": int(clk[4]), "fill_status": status}
+    # one step of the device loop and one oracle step (the reference's loop
+    # body with the ghost fill, solvers/iterator.cpp:109-151) from the same
+    # state and clock: the state the steps above left
+    clk = it.clock.cpu().numpy()
+    O = Oracle(N=2, thermal=False, lset=1)
+    uc = ue.cpu().numpy().reshape(nx, ny, 15).copy()
+    O.step_multi(uc, float(clk[1]), float(clk[0]), tf, int(clk[4]), MPs, dX, 0, cfl=0.8,
+                 contorted_tol=CONTORTED_TOL)
+    it.run(ue, 1)
+    got = ue.cpu().numpy().reshape(nx, ny, 15)
+    cell_err = np.max(np.abs(got - uc) / (1.0 + np.abs(uc)), axis=-1)
+    out["max_rel_diff_vs_oracle"] = float(cell_err.max())
+    out["cells_within_1e-10_of_oracle"] = float((cell_err <= 1e-10).mean())
     if cpu_steps:
-        O = Oracle(N=2, thermal=False, lset=1)
         uc = u0.copy()
         t0 = time.perf_counter()
         dt, t = 0.0, 0.0
@@ -706,7 +752,7 @@ def adjoint_bench(torch, fd_check=True):
     [-1, 1], t_end = 1.0, CFL 0.8, checkpoints every 32 steps): misfit of
     v_y against the run at the true parameters (mu, cs, calpha) =
     (1e-2, 1, 1), gradient at (1.2e-2, 0.9, 1.1) with respect to the
-    parameters and the 400 x 17 initial state.  Times the forward pass and
+    parameters (mu, cs, calpha, gamma) and the 400 x 17 initial state.  Times the forward pass and
     the backward pass (segment recompute + backward steps) with CUDA events,
     reports their ratio per step, and the largest relative error of the
     parameter gradient against central differences (h = 1e-6) of the same
@@ -716,22 +762,24 @@ def adjoint_bench(torch, fd_check=True):
     from phd_gb300.adjoint import Problem, solve
     from phd_gb300.params import material_params
 
-    def make_par(th):
-        return material_params("sg", 1.0, cv=1.0, gamma=1.4, b0=th[1], calpha=th[2], mu=th[0],
-                               Pr=0.75)
+    def make_par(th):  # th = (mu, cs, calpha, gamma)
+        return material_params("sg", 1.0, cv=1.0, gamma=th[3], b0=th[1], calpha=th[2],
+                               mu=th[0], Pr=0.75)
 
     nx, tf = 400, 1.0
     u0, _, _, dX, _ = G.problems.stokes(nx=nx, mu=1e-2, cs=1.0, calpha=1.0, tf=tf)
     dx = dX[0]
-    theta = np.array([1.2e-2, 0.9, 1.1])
+    theta = np.array([1.2e-2, 0.9, 1.1, 1.45])
+    npar = theta.size
     out = {}
     for ninst in (1, 64):
         rng = np.random.default_rng(20261203)
-        th = theta[None, :] * (1.0 + (0.1 * rng.uniform(-1, 1, (ninst, 3)) if ninst > 1 else 0.0))
+        th = theta[None, :] * (1.0 + (0.1 * rng.uniform(-1, 1, (ninst, npar)) if ninst > 1
+                                      else 0.0))
         u0p = np.tile(u0, (ninst, 1))
         Pt = Problem([nx] * ninst, [dx] * ninst, "transitive", make_par, cfl=0.8, tf=tf)
         uT = Pt.forward(torch.tensor(u0p, device="cuda"),
-                        [make_par(np.array([1e-2, 1.0, 1.0]))] * ninst)
+                        [make_par(np.array([1e-2, 1.0, 1.0, 1.4]))] * ninst)
         target = (uT[:, 3] / uT[:, 0]).clone()
 
         def loss(uN):
@@ -775,7 +823,7 @@ def adjoint_bench(torch, fd_check=True):
         if fd_check and ninst == 1:
             g = prob.theta_grad(fb, th)[0]
             errs = []
-            for j in range(3):
+            for j in range(npar):
                 h = 1e-6 * theta[j]
                 Ls = []
                 for s in (1, -1):
@@ -786,7 +834,7 @@ def adjoint_bench(torch, fd_check=True):
                                                     [make_par(t2)]))))
                 fd = (Ls[0] - Ls[1]) / (2 * h)
                 errs.append(abs(g[j] - fd) / abs(fd))
-            r["grad_wrt_mu_cs_calpha"] = [float(x) for x in g]
+            r["grad_wrt_mu_cs_calpha_gamma"] = [float(x) for x in g]
             r["grad_rel_err_vs_fd_h1e-6"] = max(errs)
         out["stokes_%d" % ninst] = r
     return out
@@ -969,8 +1017,9 @@ def roofline(stage_ms, ncell, n, mean_iters, peak):
     if dom in TRAFFIC:
         out["traffic"] = TRAFFIC[dom]
         out["traffic_unit"] = "bytes per launch"
-        out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture "
-                                 "(profiles/%s_tgv512.md)" % dom)
+        out["traffic_source"] = ("from an earlier ncu capture of %s on the TGV 512^2 step "
+                                 "(dram__bytes_read.sum + dram__bytes_write.sum), not "
+                                 "measured in this run" % dom)
     return out
 
 

@@ -240,9 +240,12 @@ int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gp
  * variables (about 4.5 MB, held by every GPU that loads the library until the
  * process exits).  Larger grids are rejected with GPR_E_TOO_LARGE.  The
  * array's device address is looked up on the first call made on each device,
- * so that first call must come before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised by
- * the caller.  Otherwise as gpr_ader_stepper with ndim = 1. */
+ * so that first call must come before any stream capture; the address is
+ * kept for the life of the process, so the entry point must not be used
+ * across a cudaDeviceReset.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller.  Otherwise as
+ * gpr_ader_stepper with ndim = 1: nvar 17, 15 or 14, any of the three flux
+ * codes, mask, status and stiff as there. */
 #define GPR_NOALLOC_MAX_CELLS 4096
 int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
                                 double dt, double dx, int stiff, int flux,

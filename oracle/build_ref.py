@@ -1,10 +1,11 @@
 """Recipe: compile the reference GPR solver (haranjackson/phd, code/cpp) into a
 test-only Python module under oracle/_ref/.
 
-This is test infrastructure.  It reads the reference sources from
-/root/reference (read-only), copies them to a scratch directory under /tmp,
-applies the minimum patch needed for them to compile and to select a model
-variant, and links them with oracle/ref_bindings.cpp (own code) into
+This is test infrastructure.  It reads the reference sources from the
+reference checkout (read-only; its root is taken from --ref ROOT, else the
+environment variable GPR_REFERENCE_ROOT, else /root/reference), copies them
+to a scratch directory under /tmp, applies the minimum patch needed for them
+to compile and to select a model variant, and links them with oracle/ref_bindings.cpp (own code) into
 oracle/_ref/GPRref_<variant>.so.  Reference sources are never copied into the
 repository; oracle/_ref/ is git-ignored.
 
@@ -16,11 +17,11 @@ Patches applied to the scratch copy:
     definition is a hard compile error.
 
 The build uses g++ directly (no cmake), the vendored Eigen 3.3.4 and
-skfmm sources, and the pip pybind11 headers.  It only runs where
-/root/reference exists (the x86 development container); a GPU host never
+skfmm sources, and the pip pybind11 headers.  It only runs where the
+reference checkout exists (the x86 development container); a GPU host never
 needs it.
 
-Usage:  python oracle/build_ref.py [variant ...]     (default: v17)
+Usage:  python oracle/build_ref.py [--ref ROOT] [variant ...]     (default: v17)
 """
 import os
 import re
@@ -30,7 +31,12 @@ import sys
 import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
-REF = "/root/reference/code/cpp"
+REF_ROOT = os.environ.get("GPR_REFERENCE_ROOT", "/root/reference")
+if "--ref" in sys.argv:  # python oracle/build_ref.py --ref ROOT [variant ...]
+    _k = sys.argv.index("--ref")
+    REF_ROOT = sys.argv[_k + 1]
+    del sys.argv[_k:_k + 2]
+REF = os.path.join(REF_ROOT, "code", "cpp")
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 

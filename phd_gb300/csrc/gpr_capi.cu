@@ -482,6 +482,10 @@ int gpr_reset_contorted(double *u, int64_t ncell, double contorted_tol, const gp
 // until the process exits.  Its device address is looked up once per device
 // (cudaGetSymbolAddress, with that device current) on the first call made on
 // that device, so that first call must come before any stream capture.
+// The looked-up address is kept for the life of the process: after a
+// cudaDeviceReset (or a release and re-creation of the device's primary
+// context) the module may be loaded elsewhere, so the entry point must not be
+// used across such a reset.
 // Every call shares the array and it keeps the last call's contents; nothing
 // in it has to start at zero (each call overwrites what it reads), but calls
 // that overlap on the GPU (different streams, or different host threads on
@@ -516,6 +520,19 @@ int noalloc_scratch(double **out) {
   return GPR_OK;
 }
 
+template <class O>
+int noalloc_step(double *u, const double *ub, const int32_t *nX, const double *dX, double dt,
+                 int stiff, int flux, const DevPar &P, const uint8_t *mask, int32_t *status,
+                 double *wh, double *qh, double *fb, cudaStream_t st) {
+  int rc;
+  if ((rc = O::weno(wh, ub, nX, 1, nullptr, st)))
+    return rc;
+  if ((rc = O::predictor(qh, wh, dt, nullptr, dX, 1, nX, stiff, P, mask, status, st)))
+    return rc;
+  // the 1D face pass writes (nx + 1) x 2 x V doubles whatever the flux
+  return O::fv(u, qh, nX, dt, nullptr, dX, 1, 1, 1, P, mask, fb, st, flux);
+}
+
 }  // namespace
 
 extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx, double dt,
@@ -526,7 +543,9 @@ extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t 
     return GPR_E_ARG;
   if (nx > GPR_NOALLOC_MAX_CELLS || nvar > 17)
     return GPR_E_TOO_LARGE;
-  if (flux != GPR_FLUX_RUSANOV)
+  if (flux != GPR_FLUX_RUSANOV && flux != GPR_FLUX_ROE && flux != GPR_FLUX_OSHER)
+    return GPR_E_ARG;
+  if (nvar != 17 && nvar != 15 && nvar != 14)
     return GPR_E_UNSUPPORTED;
   double *scr = nullptr;
   int rc = noalloc_scratch(&scr);
@@ -541,24 +560,12 @@ extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t 
   DevPar P = make_devpar(*par);
   cudaStream_t st = S(stream);
   switch (nvar) {
-  case 17: {
-    using O = Ops<L17>;
-    if ((rc = O::weno(wh, ub, nX, 1, nullptr, st)))
-      return rc;
-    if ((rc = O::predictor(qh, wh, dt, nullptr, dX, 1, nX, stiff, P, mask, status, st)))
-      return rc;
-    return O::fv(u, qh, nX, dt, nullptr, dX, 1, 1, 1, P, mask, fb, st);
-  }
-  case 14: {
-    using O = Ops<L14>;
-    if ((rc = O::weno(wh, ub, nX, 1, nullptr, st)))
-      return rc;
-    if ((rc = O::predictor(qh, wh, dt, nullptr, dX, 1, nX, stiff, P, mask, status, st)))
-      return rc;
-    return O::fv(u, qh, nX, dt, nullptr, dX, 1, 1, 1, P, mask, fb, st);
-  }
+  case 17:
+    return noalloc_step<Ops<L17>>(u, ub, nX, dX, dt, stiff, flux, P, mask, status, wh, qh, fb, st);
+  case 15:
+    return noalloc_step<Ops15>(u, ub, nX, dX, dt, stiff, flux, P, mask, status, wh, qh, fb, st);
   default:
-    return GPR_E_UNSUPPORTED;
+    return noalloc_step<Ops<L14>>(u, ub, nX, dX, dt, stiff, flux, P, mask, status, wh, qh, fb, st);
   }
 }
 

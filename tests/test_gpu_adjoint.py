@@ -24,8 +24,11 @@ def _cuda():
 
 
 def make_par(theta, gamma=1.4):
+    """theta = (mu, cs, calpha[, gamma])."""
     from phd_gb300.params import material_params
     mu, cs, calpha = theta[0], theta[1], theta[2]
+    if len(theta) > 3:
+        gamma = theta[3]
     return material_params("sg", 1.0, cv=1.0, gamma=gamma, b0=cs, calpha=calpha, mu=mu,
                            Pr=0.75)
 
@@ -309,6 +312,36 @@ def test_stokes_parameter_gradient_matches_finite_differences():
         Lpm = []
         for s in (1, -1):
             t2 = THETA.copy()
+            t2[j] += s * h
+            P2 = Problem([nx], [dx], "transitive", make_par, cfl=0.8, tf=tf)
+            Lpm.append(float(_loss(P2.forward(torch.tensor(u0p, device="cuda"),
+                                              [make_par(t2)]), target)))
+        fd = (Lpm[0] - Lpm[1]) / (2 * h)
+        assert abs(g[j] - fd) <= 1e-6 * abs(fd), (j, g[j], fd)
+
+
+def test_stokes_gamma_gradient_matches_finite_differences():
+    """The same misfit with the ratio of specific heats among the parameters,
+    theta = (mu, cs, calpha, gamma) at (1.2e-2, 0.9, 1.1, 1.45): gamma enters
+    the device fields gamma, 1/(gamma - 1) and 1/kappa (kappa = mu gamma cv /
+    Pr); every component against central differences (h = 1e-6 theta_j)."""
+    _cuda()
+    from phd_gb300.adjoint import Problem, solve
+    nx, tf = 400, 1.0
+    theta = np.array([1.2e-2, 0.9, 1.1, 1.45])
+    u0p, dx, target = _misfit_setup(nx, tf)
+    prob = Problem([nx], [dx], "transitive", make_par, cfl=0.8, tf=tf, checkpoint_every=32)
+    u0 = torch.tensor(u0p, device="cuda", requires_grad=True)
+    th = torch.tensor(theta[None, :], dtype=torch.float64, requires_grad=True)
+    L = _loss(solve(u0, th, prob), target)
+    L.backward()
+    g = th.grad.numpy()[0]
+    assert g[3] != 0.0
+    for j in range(4):
+        h = 1e-6 * theta[j]
+        Lpm = []
+        for s in (1, -1):
+            t2 = theta.copy()
             t2[j] += s * h
             P2 = Problem([nx], [dx], "transitive", make_par, cfl=0.8, tf=tf)
             Lpm.append(float(_loss(P2.forward(torch.tensor(u0p, device="cuda"),
