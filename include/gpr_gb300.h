@@ -303,6 +303,35 @@ int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx,
                       int nsteps, double *scratch, int32_t *status,
                       unsigned long long *updates, int nvar, void *stream);
 
+/* Autotuner of the batched step's launch shapes (no counterpart in the
+ * reference).  The shapes are GPR_BATCH_NSHAPES int32 values:
+ *   [0] WENO threads per block (one thread per cell and variable),
+ *   [1] first-iterate threads per block (2 lanes per predictor cell),
+ *   [2] Picard threads per block (4 lanes per predictor cell),
+ *   [3] face-pass lane layout: 0 two lanes per face (one per time node),
+ *       1 four lanes per face (per time node and side),
+ *   [4] face-pass threads per block,
+ *   [5] volume-pass threads per block (4 lanes per cell).
+ * gpr_batch_autotune times every candidate of each stage on the batch's
+ * current state with CUDA events on `stream` (WENO 64/128/256/512; first
+ * iterate x Picard 32/64/128 each; faces both layouts x 32/64/128; volume
+ * 32/64/128) and keeps the fastest for this batch (the scratch buffer
+ * names the batch): later gpr_batch_iterate calls on it launch with those
+ * shapes.  u is unchanged; each clock holds the coming step's dt.  It
+ * synchronises the stream (not capturable); `shapes` (optional) receives
+ * the choice, `times` (optional, GPR_BATCH_NCAND floats) the mean ms of
+ * each candidate in the order above.  gpr_batch_init resets a batch to the
+ * default shapes {256, 128, 128, 0, 128, 128}; gpr_batch_get_shapes /
+ * gpr_batch_set_shapes read and restore a choice (block sizes 32, 64 or 128,
+ * WENO a multiple of 32 up to 1024). */
+#define GPR_BATCH_NSHAPES 6
+#define GPR_BATCH_NCAND 22
+int gpr_batch_autotune(double *u, double *clock, int ninst, const int32_t *nx,
+                       double *scratch, int32_t *shapes, float *times, int nvar,
+                       void *stream);
+int gpr_batch_get_shapes(const double *scratch, int32_t *shapes);
+int gpr_batch_set_shapes(const double *scratch, const int32_t *shapes);
+
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the batched 1D step (no counterpart in the reference, which
  * has no derivatives): reverse-mode cotangents of a misfit with respect to

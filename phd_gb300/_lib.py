@@ -100,6 +100,9 @@ SIGNATURES = {
     "gpr_batch_scratch_doubles": (_L, [_I, _P, _I]),
     "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
     "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
+    "gpr_batch_autotune": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _P]),
+    "gpr_batch_get_shapes": (_I, [_P, _P]),
+    "gpr_batch_set_shapes": (_I, [_P, _P]),
     "gpr_adj_num_fields": (_I, []),
     "gpr_adj_supported": (_I, [_I, _P, _P, _I]),
     "gpr_adj_tape_doubles": (_L, [_I, _P, _I]),

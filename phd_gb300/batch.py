@@ -5,7 +5,9 @@ clock (the reference runs one grid per `solvers.iterator` call,
 code/cpp/src/solvers/iterator.cpp:85-170).  All instances are packed into
 one device buffer and every stage of the step is one kernel launch for all of
 them; the step loop needs no host synchronisation and can be captured in a
-CUDA graph (`capture`).
+CUDA graph (`capture`).  The launch shapes of the stages (threads per block,
+the face pass's lane layout) are chosen per batch by the library's autotuner
+(`autotune`, run by the constructor unless autotune=False).
 """
 import ctypes
 
@@ -22,7 +24,10 @@ BC = {"transitive": 0, "transmissive": 0, "periodic": 1, "slip": 2, "stick": 3,
 class Batch:
     """instances: list of (u0 [nx, V] array, Par, dx, bcs) tuples."""
 
-    def __init__(self, instances, cfl=0.8, tf=0.2, device="cuda"):
+    SHAPE_NAMES = ("weno_block", "first_block", "picard_block", "faces_four_lanes",
+                   "faces_block", "cells_block")
+
+    def __init__(self, instances, cfl=0.8, tf=0.2, device="cuda", autotune=True):
         self.lib = _lib.load()
         self.device = torch.device(device)
         self.V = int(instances[0][0].shape[-1])
@@ -56,6 +61,38 @@ class Batch:
                 self._t(self.clock), self.ninst, self._p(self.nx), self._p(self.dx),
                 self._p(self.bcs), ctypes.cast(pars, ctypes.c_void_p), float(cfl), float(tf),
                 self._t(self.scratch), self.V, self._stream()), "batch_init")
+        self.tuning = None
+        if autotune:
+            self.autotune()
+
+    def autotune(self):
+        """Time the candidate launch shapes on the current state and keep the
+        fastest (gpr_batch_autotune); returns {name: value} of the choice
+        and keeps the per-candidate times in self.tuning."""
+        shapes = np.zeros(6, np.int32)
+        times = np.zeros(22, np.float32)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gpr_batch_autotune(
+                self._t(self.u), self._t(self.clock), self.ninst, self._p(self.nx),
+                self._t(self.scratch), self._p(shapes), self._p(times), self.V,
+                self._stream()), "batch_autotune")
+        self.tuning = {"shapes": dict(zip(self.SHAPE_NAMES, shapes.tolist())),
+                       "candidate_ms": times.tolist()}
+        return self.tuning["shapes"]
+
+    def shapes(self):
+        """The launch shapes gpr_batch_iterate uses for this batch."""
+        out = np.zeros(6, np.int32)
+        _lib.check(self.lib.gpr_batch_get_shapes(self._t(self.scratch), self._p(out)),
+                   "batch_get_shapes")
+        return dict(zip(self.SHAPE_NAMES, out.tolist()))
+
+    def set_shapes(self, shapes):
+        """Launch with the given shapes ({name: value} or a sequence of 6)."""
+        vals = [shapes[k] for k in self.SHAPE_NAMES] if isinstance(shapes, dict) else shapes
+        a = np.ascontiguousarray(np.asarray(vals, dtype=np.int32))
+        _lib.check(self.lib.gpr_batch_set_shapes(self._t(self.scratch), self._p(a)),
+                   "batch_set_shapes")
 
     @staticmethod
     def _p(a):

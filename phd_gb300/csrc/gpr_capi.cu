@@ -571,7 +571,46 @@ extern "C" int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t 
 
 // ---------------------------------------------------------------------------
 // Batched form (many independent 1D instances in one launch per stage).
+#include <map>
 #include <vector>
+
+namespace {
+
+// Launch shapes chosen for each batch, keyed by the batch's scratch buffer
+// (the tables of one batch live there): written by gpr_batch_autotune /
+// gpr_batch_set_shapes, reset by gpr_batch_init, read by gpr_batch_iterate
+// on the host when it enqueues the launches.
+std::mutex g_shapes_mutex;
+std::map<const double *, BatchShapes> g_shapes;
+
+BatchShapes shapes_of(const double *scratch) {
+  std::lock_guard<std::mutex> lk(g_shapes_mutex);
+  auto it = g_shapes.find(scratch);
+  return it == g_shapes.end() ? BatchShapes{} : it->second;
+}
+
+void shapes_put(const double *scratch, const BatchShapes &sh) {
+  std::lock_guard<std::mutex> lk(g_shapes_mutex);
+  g_shapes[scratch] = sh;
+}
+
+void shapes_drop(const double *scratch) {
+  std::lock_guard<std::mutex> lk(g_shapes_mutex);
+  g_shapes.erase(scratch);
+}
+
+void shapes_to_array(const BatchShapes &sh, int32_t *out) {
+  out[0] = sh.weno;
+  out[1] = sh.first;
+  out[2] = sh.picard;
+  out[3] = sh.faces_split;
+  out[4] = sh.faces;
+  out[5] = sh.cells;
+}
+
+bool lane_block(int bs) { return bs == 32 || bs == 64 || bs == 128; }
+
+}  // namespace
 
 extern "C" {
 
@@ -676,6 +715,62 @@ int gpr_batch_init(double *clock, int ninst, const int32_t *nx, const double *dx
     fprintf(stderr, "gpr_gb300: batch init: %s\n", cudaGetErrorString(e));
     return GPR_E_CUDA;
   }
+  shapes_drop(scratch);  // new tables: the default shapes until tuned
+  return GPR_OK;
+}
+
+int gpr_batch_autotune(double *u, double *clock, int ninst, const int32_t *nx, double *scratch,
+                       int32_t *shapes, float *times, int nvar, void *stream) {
+  if (!u || !clock || ninst < 1 || !nx || !scratch)
+    return GPR_E_ARG;
+  for (int k = 0; k < ninst; k++)
+    if (nx[k] < 2)
+      return GPR_E_ARG;
+  BatchShapes sh;
+  int rc;
+  switch (nvar) {
+  case 17:
+    rc = Ops<L17>::batch_autotune(u, clock, ninst, nx, scratch, sh, times, 3, S(stream));
+    break;
+  case 14:
+    rc = Ops<L14>::batch_autotune(u, clock, ninst, nx, scratch, sh, times, 3, S(stream));
+    break;
+  case 15:
+    rc = Ops15::batch_autotune(u, clock, ninst, nx, scratch, sh, times, 3, S(stream));
+    break;
+  default:
+    return GPR_E_UNSUPPORTED;
+  }
+  if (rc)
+    return rc;
+  shapes_put(scratch, sh);
+  if (shapes)
+    shapes_to_array(sh, shapes);
+  return GPR_OK;
+}
+
+int gpr_batch_get_shapes(const double *scratch, int32_t *shapes) {
+  if (!scratch || !shapes)
+    return GPR_E_ARG;
+  shapes_to_array(shapes_of(scratch), shapes);
+  return GPR_OK;
+}
+
+int gpr_batch_set_shapes(const double *scratch, const int32_t *shapes) {
+  if (!scratch || !shapes)
+    return GPR_E_ARG;
+  if (shapes[0] < 32 || shapes[0] > 1024 || shapes[0] % 32 || !lane_block(shapes[1]) ||
+      !lane_block(shapes[2]) || (shapes[3] != 0 && shapes[3] != 1) || !lane_block(shapes[4]) ||
+      !lane_block(shapes[5]))
+    return GPR_E_ARG;
+  BatchShapes sh;
+  sh.weno = shapes[0];
+  sh.first = shapes[1];
+  sh.picard = shapes[2];
+  sh.faces_split = shapes[3];
+  sh.faces = shapes[4];
+  sh.cells = shapes[5];
+  shapes_put(scratch, sh);
   return GPR_OK;
 }
 
@@ -687,8 +782,9 @@ int gpr_batch_iterate(double *u, double *clock, int ninst, const int32_t *nx, in
   for (int k = 0; k < ninst; k++)
     if (nx[k] < 2)
       return GPR_E_ARG;
+  const BatchShapes sh = shapes_of(scratch);
   DISPATCH(nvar, O::batch_iterate(u, clock, ninst, nx, nsteps, scratch, status, updates,
-                                  S(stream)))
+                                  S(stream), sh))
 }
 
 }  // extern "C"

@@ -38,6 +38,20 @@ struct Carve {
   }
 };
 
+// Launch shapes of the batched step: threads per block of each stage (so
+// cells per block = threads / lanes per cell) and the lane layout of the
+// face pass.  The defaults are the single-grid kernels' shapes;
+// Ops::batch_autotune measures the candidates on a batch and picks the
+// fastest of each.
+struct BatchShapes {
+  int weno = 256;       // k_b_weno: one thread per (cell, variable)
+  int first = 128;      // k_predictor_first: 2 lanes per predictor cell
+  int picard = 128;     // k_predictor_picard: 4 lanes per predictor cell
+  int faces_split = 0;  // 0: k_faces1d (2 lanes per face), 1: k_faces1d_split (4)
+  int faces = 128;      // threads per block of the face kernel
+  int cells = 128;      // k_cells: 4 lanes per cell
+};
+
 // Packed sizes and scratch offsets (in doubles) of the batched form.
 struct BatchLayout {
   long nu = 0, nub = 0, nb = 0, nf = 0;

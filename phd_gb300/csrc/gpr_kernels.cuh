@@ -1064,11 +1064,11 @@ __global__ void __launch_bounds__(128) k_faces1d(
 // (qR) and the path integral's node 0 (1); the wave speeds are exchanged,
 // the side-0 lane adds the dissipation, and the four lanes' contributions
 // are summed by the reduce-scatter (the same terms as interface_point).
-template <class L>
+template <class L, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_faces1d_split(
     double *__restrict__ fb, const double *__restrict__ qh, long nface,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    int time_dg, DevPar P, Consts C) {
+    int time_dg, DevPar Pv, Consts C, Batch B) {
   constexpr int V = L::V;
   static_assert(NN == 2, "two time nodes and two path nodes");
   if (dt_dev)
@@ -1077,7 +1077,16 @@ __global__ void __launch_bounds__(128) k_faces1d_split(
   const int lq = threadIdx.x % 4, t = lq >> 1, side = lq & 1;
   long face = gt / 4;
   bool valid = face < nface;
-  long fi = valid ? face : 0;
+  const long fo = valid ? face : 0;
+  // predictor cell on the left of the face (packed index in the batched form)
+  long fi = fo;
+  const int inst = BATCH ? B.inst_f[fo] : 0;
+  const DevPar &P = BATCH ? B.P[inst] : Pv;
+  if (BATCH) {
+    fi = B.off_b[inst] + (fo - B.off_f[inst]);
+    dt = B.clk[5 * inst + 1];
+    dx = 1.0 / B.idx[inst];
+  }
   bool active = valid && (mask == nullptr || (mask[fi] && mask[fi + 1])) && (time_dg || t == 0);
   int nt = time_dg ? NN : 1;
   double ql[V], qr[V], f[V], b[V], dq[V];
@@ -1117,7 +1126,7 @@ __global__ void __launch_bounds__(128) k_faces1d_split(
       if (k < 14 || k >= V - L::LSET)
         b[k] = wn * bd[k];
   }
-  face_reduce_store<V, 4>(b, f, kk, active, valid, lq, fb + fi * 2 * V);
+  face_reduce_store<V, 4>(b, f, kk, active, valid, lq, fb + fo * 2 * V);
 }
 
 // 2D faces: direction dir, faces (i, j) of the (nx+1) x (ny+1) face grid,

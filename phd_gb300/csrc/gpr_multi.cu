@@ -127,8 +127,13 @@ BatchLayout Ops15::batch_layout(int ninst, const int32_t *nx) {
 
 int Ops15::batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,
                            double *scr, int32_t *status, unsigned long long *updates,
-                           cudaStream_t st) {
-  return Ops<L15>::batch_iterate(u, clk, ninst, nx, nsteps, scr, status, updates, st);
+                           cudaStream_t st, const BatchShapes &sh) {
+  return Ops<L15>::batch_iterate(u, clk, ninst, nx, nsteps, scr, status, updates, st, sh);
+}
+
+int Ops15::batch_autotune(double *u, double *clk, int ninst, const int32_t *nx, double *scr,
+                            BatchShapes &sh, float *times, int reps, cudaStream_t st) {
+  return Ops<L15>::batch_autotune(u, clk, ninst, nx, scr, sh, times, reps, st);
 }
 
 int Ops15::ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {

@@ -247,7 +247,7 @@ template <class L> struct Ops {
         ;
       else if (flux == GPR_FLUX_RUSANOV)  // one lane per (face, time node, side)
         k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
-            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, P, C);
+            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, P, C, Batch{});
       else
         k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
             scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
@@ -290,7 +290,7 @@ template <class L> struct Ops {
       long nf = (long)(nx + 1) * NN;
       if (flux == GPR_FLUX_RUSANOV)
         k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
-            fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, P, C);
+            fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, P, C, Batch{});
       else
         k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
             fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, flux, P, C, Batch{});
@@ -495,9 +495,48 @@ template <class L> struct Ops {
     return batch_view_of(scr, ninst, b, clk);
   }
 
+  // The stages of one batched step with the launch shapes sh.
+  static void batch_cfl(double *u, unsigned long long *mx, const BatchLayout &b, const Batch &B,
+                        int ninst, cudaStream_t st) {
+    k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B);
+    k_b_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B);
+  }
+  static void batch_weno(double *wh, const double *ub, const BatchLayout &b, const Batch &B,
+                         int bs, cudaStream_t st) {
+    k_b_weno<V><<<blocks(b.nb * V, bs), bs, 0, st>>>(wh, ub, b.nb, consts(), B);
+  }
+  static void batch_picard_pair(double *qh, const double *wh, int32_t *status,
+                                const BatchLayout &b, const Batch &B, int bs_first,
+                                int bs_picard, cudaStream_t st) {
+    const Consts &C = consts();
+    DevPar P0{};
+    k_predictor_first<L, 1, true><<<blocks(b.nb * NN, bs_first), bs_first, 0, st>>>(
+        qh, wh, b.nb, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C, B);
+    k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, bs_picard), bs_picard, 0, st>>>(
+        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1);
+  }
+  static void batch_faces(double *fb, const double *qh, const BatchLayout &b, const Batch &B,
+                          int split, int bs, cudaStream_t st) {
+    const Consts &C = consts();
+    DevPar P0{};
+    if (split)
+      k_faces1d_split<L, true><<<blocks(b.nf * NN * 2, bs), bs, 0, st>>>(
+          fb, qh, b.nf, nullptr, 0.0, nullptr, 1.0, 1, P0, C, B);
+    else
+      k_faces1d<L, true><<<blocks(b.nf * NN, bs), bs, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
+                                                                nullptr, 1.0, 1, P0, C, B);
+  }
+  static void batch_cells(double *u, const double *qh, const double *fb, const BatchLayout &b,
+                          const Batch &B, int bs, cudaStream_t st) {
+    DevPar P0{};
+    k_cells<L, 1, true><<<blocks(b.nu * NN * NN, bs), bs, 0, st>>>(
+        u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, consts(), B,
+        FV_BOTH);
+  }
+
   static int batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,
                            double *scr, int32_t *status, unsigned long long *updates,
-                           cudaStream_t st) {
+                           cudaStream_t st, const BatchShapes &sh = BatchShapes{}) {
     const Consts &C = consts();
     BatchLayout b = batch_layout(ninst, nx);
     Batch B = batch_view(scr, ninst, b, clk);
@@ -505,27 +544,151 @@ template <class L> struct Ops {
     unsigned long long *mx = (unsigned long long *)(scr + b.o_mx);
     DevPar P0{};
     for (int s = 0; s < nsteps; s++) {
-      k_b_cfl_max<L><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, mx, B);
-      k_b_clock_finalize<<<blocks(ninst, 128), 128, 0, st>>>(mx, B);
+      batch_cfl(u, mx, b, B, ninst, st);
       k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
-      k_b_weno<V><<<blocks(b.nb * V, 256), 256, 0, st>>>(wh, ub, b.nb, C, B);
-      k_predictor_first<L, 1, true><<<blocks(b.nb * NN, 128), 128, 0, st>>>(
-          qh, wh, b.nb, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C, B);
-      k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, 128), 128, 0, st>>>(
-          qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1);
+      batch_weno(wh, ub, b, B, sh.weno, st);
+      batch_picard_pair(qh, wh, status, b, B, sh.first, sh.picard, st);
       int rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
                                    C, st, B);
       if (rc)
         return rc;
-      k_faces1d<L, true><<<blocks(b.nf * NN, 128), 128, 0, st>>>(fb, qh, b.nf, nullptr, 0.0,
-                                                                  nullptr, 1.0, 1, P0, C, B);
-      k_cells<L, 1, true><<<blocks(b.nu * NN * NN, 128), 128, 0, st>>>(
-          u, qh, fb, nullptr, b.nu, 1, nullptr, 0.0, nullptr, 1.0, 1.0, 1, 1, P0, C, B,
-          FV_BOTH);
+      batch_faces(fb, qh, b, B, sh.faces_split, sh.faces, st);
+      batch_cells(u, qh, fb, b, B, sh.cells, st);
       k_b_renorm<V><<<blocks(b.nu, 256), 256, 0, st>>>(u, b.nu, B);
       k_b_clock_advance<<<blocks(ninst, 128), 128, 0, st>>>(B, updates);
     }
     return cuda_rc();
+  }
+
+  // Autotuner of the batched step's launch shapes.  On the batch's current
+  // state it times every candidate of each stage with CUDA events on the
+  // stream (one untimed launch, then `reps` timed ones) and keeps the fastest
+  // in sh: WENO at 64 / 128 / 256 / 512 threads per block; the predictor pair
+  // (first iterate + Picard) at 32 / 64 / 128 threads per block each (8 to
+  // 32 predictor cells per Picard block); the face pass in both lane layouts
+  // (2 or 4 lanes per face) at 32 / 64 / 128; the volume pass at 32 / 64 /
+  // 128.  Every timed launch is idempotent on what the step reads (ub -> wh,
+  // wh -> qh, qh -> fb); the volume pass updates u in place, so it is timed
+  // on a copy of u in the ub area.  Afterwards u is unchanged, each clock
+  // holds this step's dt (as after the first kernels of a step) and ub, wh,
+  // qh and fb hold intermediate values that the next step overwrites.
+  // times[NCAND] (optional) receives the mean time in ms of each candidate,
+  // in the order above (4 + 9 + 6 + 3).  Synchronises the stream.
+  static constexpr int NCAND = 4 + 9 + 6 + 3;
+  static int batch_autotune(double *u, double *clk, int ninst, const int32_t *nx, double *scr,
+                            BatchShapes &sh, float *times, int reps, cudaStream_t st) {
+    BatchLayout b = batch_layout(ninst, nx);
+    Batch B = batch_view(scr, ninst, b, clk);
+    double *ub = scr + b.o_ub, *wh = scr + b.o_wh, *qh = scr + b.o_qh, *fb = scr + b.o_fb;
+    unsigned long long *mx = (unsigned long long *)(scr + b.o_mx);
+    const Consts &C = consts();
+    DevPar P0{};
+    if (reps < 1)
+      reps = 1;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess)
+      return GPR_E_CUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return GPR_E_CUDA;
+    }
+    int rc = GPR_OK;
+    int slot = 0;
+    // mean ms of `reps` runs of f after one untimed run; -1 on a CUDA error
+    auto timeit = [&](auto f) -> float {
+      f();
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps; r++)
+        f();
+      cudaEventRecord(e1, st);
+      float ms = -1.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) !=
+                                                         cudaSuccess ||
+          cudaGetLastError() != cudaSuccess) {
+        rc = GPR_E_CUDA;
+        return -1.f;
+      }
+      ms /= reps;
+      if (times)
+        times[slot] = ms;
+      slot++;
+      return ms;
+    };
+    const int bs3[3] = {32, 64, 128};
+    // this step's dt and ghost cells
+    batch_cfl(u, mx, b, B, ninst, st);
+    k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
+    {
+      const int cand[4] = {64, 128, 256, 512};
+      float best = 1e30f;
+      for (int c : cand) {
+        float ms = timeit([&] { batch_weno(wh, ub, b, B, c, st); });
+        if (rc)
+          break;
+        if (ms < best) {
+          best = ms;
+          sh.weno = c;
+        }
+      }
+    }
+    if (!rc) {
+      float best = 1e30f;
+      for (int f : bs3)
+        for (int p : bs3) {
+          float ms = timeit([&] { batch_picard_pair(qh, wh, nullptr, b, B, f, p, st); });
+          if (rc)
+            break;
+          if (ms < best) {
+            best = ms;
+            sh.first = f;
+            sh.picard = p;
+          }
+        }
+    }
+    if (!rc) {
+      // a complete predictor (the Newton pass finishes flagged cells) for the
+      // face and volume timings
+      batch_picard_pair(qh, wh, nullptr, b, B, sh.first, sh.picard, st);
+      rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C,
+                               st, B);
+    }
+    if (!rc) {
+      float best = 1e30f;
+      for (int split = 0; split < 2 && !rc; split++)
+        for (int c : bs3) {
+          float ms = timeit([&] { batch_faces(fb, qh, b, B, split, c, st); });
+          if (rc)
+            break;
+          if (ms < best) {
+            best = ms;
+            sh.faces_split = split;
+            sh.faces = c;
+          }
+        }
+    }
+    if (!rc) {
+      // the volume pass on a copy of u (ub holds nub >= nu cells)
+      if (cudaMemcpyAsync(ub, u, sizeof(double) * b.nu * V, cudaMemcpyDeviceToDevice, st) !=
+          cudaSuccess)
+        rc = GPR_E_CUDA;
+      float best = 1e30f;
+      for (int c : bs3) {
+        if (rc)
+          break;
+        float ms = timeit([&] { batch_cells(ub, qh, fb, b, B, c, st); });
+        if (rc)
+          break;
+        if (ms < best) {
+          best = ms;
+          sh.cells = c;
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc)
+      fprintf(stderr, "gpr_gb300: batch autotune: CUDA error\n");
+    return rc;
   }
 
   static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {

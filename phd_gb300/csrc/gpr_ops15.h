@@ -54,7 +54,9 @@ struct Ops15 {
   static BatchLayout batch_layout(int ninst, const int32_t *nx);
   static int batch_iterate(double *u, double *clk, int ninst, const int32_t *nx, int nsteps,
                            double *scr, int32_t *status, unsigned long long *updates,
-                           cudaStream_t st);
+                           cudaStream_t st, const BatchShapes &sh = BatchShapes{});
+  static int batch_autotune(double *u, double *clk, int ninst, const int32_t *nx, double *scr,
+                            BatchShapes &sh, float *times, int reps, cudaStream_t st);
   static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st);
 };
 

@@ -142,7 +142,8 @@ def test_batch_graph_replay_equals_eager():
     insts = _instances()
     A = Batch(insts)
     A.step(4)
-    Bg = Batch(insts)
+    Bg = Batch(insts, autotune=False)
+    Bg.set_shapes(A.shapes())  # the same launch shapes as A
     g = Bg.capture(1)
     for _ in range(4):
         g.replay()
@@ -166,3 +167,48 @@ def test_batch_finished_instances_stop():
         ref, n, tt = O.run(u0, MP, 0.004, dX, 0, cfl=0.8)
         assert count[k] == n
         assert rel_err(B.state(k).cpu().numpy(), ref) < 1e-8
+
+
+def test_batch_autotuner():
+    """The autotuner times every candidate shape of each stage and keeps the
+    fastest; a batch starts from the default shapes; every candidate gives
+    the same step (the face pass's lane layout changes the order of a short
+    sum: 1e-13), and invalid shapes are rejected."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from phd_gb300.batch import Batch
+    insts = _instances()
+    B = Batch(insts)
+    sh = B.shapes()
+    assert sh == B.tuning["shapes"]
+    t = np.array(B.tuning["candidate_ms"])
+    assert t.size == 22 and (t > 0).all()
+    assert sh["weno_block"] == [64, 128, 256, 512][int(np.argmin(t[0:4]))]
+    k = int(np.argmin(t[4:13]))
+    assert (sh["first_block"], sh["picard_block"]) == ([32, 64, 128][k // 3], [32, 64, 128][k % 3])
+    k = int(np.argmin(t[13:19]))
+    assert (sh["faces_four_lanes"], sh["faces_block"]) == (k // 3, [32, 64, 128][k % 3])
+    assert sh["cells_block"] == [32, 64, 128][int(np.argmin(t[19:22]))]
+    # the clocks and states are untouched by tuning apart from the coming dt
+    u0 = np.concatenate([np.asarray(i[0]).reshape(-1) for i in insts])
+    assert np.array_equal(B.u.cpu().numpy(), u0)
+    ref = Batch(insts, autotune=False)
+    assert ref.shapes() == dict(zip(Batch.SHAPE_NAMES, [256, 128, 128, 0, 128, 128]))
+    ref.step(3)
+    B.step(3)
+    torch.cuda.synchronize()
+    base = ref.u.cpu().numpy()
+    assert rel_err(B.u.cpu().numpy(), base) < 1e-13
+    assert np.array_equal(B.clock.cpu().numpy(), ref.clock.cpu().numpy()) or \
+        rel_err(B.clock.cpu().numpy(), ref.clock.cpu().numpy()) < 1e-13
+    for split in (0, 1):
+        for bs in (32, 64, 128):
+            C = Batch(insts, autotune=False)
+            C.set_shapes([64, bs, bs, split, bs, bs])
+            C.step(3)
+            torch.cuda.synchronize()
+            assert rel_err(C.u.cpu().numpy(), base) < 1e-13, (split, bs)
+    with pytest.raises(RuntimeError):
+        C.set_shapes([64, 48, 128, 0, 128, 128])
+    with pytest.raises(RuntimeError):
+        C.set_shapes([64, 128, 128, 2, 128, 128])
