@@ -62,6 +62,13 @@ OPS = {
     "weno_point": 48.0,                   # per (cell, variable, sweep)
     "cfl_per_cell": 848.0,                # per cell (two max_abs_eigs)
 }
+# the same for the 1D kernels (the batched form)
+OPS_1D = {
+    "predictor_per_cell_iter": 1840.0,    # per predictor cell and Picard iteration
+    "face_point": 1423.0,                 # per (face, time node)
+    "cells_per_cell": 963.0,              # volume term, per cell
+    "weno_per_cell": 816.0,               # per predictor cell (17 points)
+}
 
 
 def parse():
@@ -84,6 +91,11 @@ def parse():
     ap.add_argument("--profile-shock-tube", type=int, default=-1, metavar="FLUX",
                     help="with --profile-steps K: K steps of the 200-cell shock tube with "
                          "flux FLUX (0 Rusanov, 1 Roe, 2 Osher) through gpr_iterate, no JSON")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="with --profile-steps K: K steps of the 512 batched shock tubes with "
+                         "the default launch shapes or --shapes, no JSON")
+    ap.add_argument("--shapes", default="",
+                    help="six comma-separated launch shapes for --profile-batched")
     ap.add_argument("--profile-adjoint", type=int, default=0, metavar="NINST",
                     help="with --profile-steps K: K steps of the Stokes differentiation "
                          "problem for NINST instances, forward then backward (for ncu "
@@ -456,6 +468,12 @@ def run_gb300(args):
             flux2d = flux2d_bench(torch, cpu=not args.no_cpu_baseline)
         except Exception as ex:  # reported, not fatal to the main line
             flux2d = {"error": str(ex)}
+    cfl08 = None
+    if rank == 0 and not args.no_shock_bubble:
+        try:
+            cfl08 = tgv_cfl08_bench(torch, cpu=not args.no_cpu_baseline)
+        except Exception as ex:  # reported, not fatal to the main line
+            cfl08 = {"error": str(ex)}
     bubble = None
     if rank == 0 and not args.no_shock_bubble:
         try:
@@ -495,6 +513,7 @@ def run_gb300(args):
             "batched": batched,
             "shock_tube": shock,
             "tgv_roe_osher": flux2d,
+            "tgv_cfl08": cfl08,
             "shock_bubble": bubble,
             "adjoint": adjoint,
             # kernels of one 2D gpr_iterate step: k_cfl_max, k_clock_finalize,
@@ -639,6 +658,73 @@ def flux2d_bench(torch, n=512, steps=3, warmup=1, cfl=0.4, cpu=True):
                                            "oracle/gpr_oracle.c" % (n, n)}
         out[name] = r
     return out
+
+
+def tgv_cfl08_bench(torch, n=512, steps=10, warmup=8, cfl=0.8, cpu=True):
+    """The 512 x 512 Taylor-Green step at the production CFL 0.8 (Rusanov):
+    dt ~ 3.5e-4 against the distortion relaxation time 6e-4, where the
+    reference's Picard iteration fails in most predictor cells and the device
+    Newton pass finishes them.  Through gpr_iterate after `warmup` steps (past
+    the reduced first five); the predictor status of the last timed step
+    gives the Picard and Newton iteration histograms; one GPU step and one
+    oracle step (Newton fallback) from the state the timed steps left."""
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    u0, MP, tf, dX, bcs = G.problems.taylor_green(n=n, cs=10.0, mu=1e-2)
+    V = 17
+    nX = np.array([n, n], np.int32)
+    pn = nX.ctypes.data_as(ctypes.c_void_p)
+    dXa = np.array(dX, np.float64)
+    bc = np.array([1, 1, 1, 1], np.int32)
+    cp = MP.to_ctypes()
+    scr = torch.empty(lib.gpr_iterate_scratch_doubles(pn, 2, V), dtype=torch.float64,
+                      device="cuda")
+    status = torch.zeros((n + 2) ** 2, dtype=torch.int32, device="cuda")
+    u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+    clk = torch.tensor([0.0, 0.0, 1e9, cfl, 0.0], dtype=torch.float64, device="cuda")
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def run(k):
+        _lib.check(lib.gpr_iterate(
+            ctypes.c_void_p(u.data_ptr()), pn, 2, dXa.ctypes.data_as(ctypes.c_void_p),
+            bc.ctypes.data_as(ctypes.c_void_p), 0,
+            ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+            ctypes.c_void_p(clk.data_ptr()), k, ctypes.c_void_p(scr.data_ptr()),
+            ctypes.c_void_p(status.data_ptr()), CONTORTED_TOL, V, sp), "iterate")
+    run(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = status.cpu().numpy()
+    iters, kind = st >> 8, st & 0xff
+    pic, newt = kind == 0, kind == 1
+    c = clk.cpu().numpy()
+    r = {"workload": "tgv2d_%dx%d_v17_rusanov_cfl%.2g" % (n, n, cfl), "steps": steps,
+         "warmup": warmup, "ms_per_step": ms / steps,
+         "value": n * n * steps / (ms * 1e-3) / 1e6, "unit": UNIT, "dt": float(c[1]),
+         "predictor": {"cells": int(st.size), "picard_cells": int(pic.sum()),
+                       "newton_cells": int(newt.sum()),
+                       "unconverged_cells": int((kind == 2).sum()),
+                       "picard_iteration_histogram": np.bincount(iters[pic]).tolist()
+                       if pic.any() else [],
+                       "newton_iteration_histogram": np.bincount(iters[newt]).tolist()
+                       if newt.any() else [],
+                       "mean_newton_iterations": float(iters[newt].mean()) if newt.any()
+                       else 0.0}}
+    if cpu:
+        from oracle import Oracle
+        err, cpu_s = step_vs_oracle(torch, u, MP, nX, dX, [1] * 4, cfl)
+        r["max_rel_diff_vs_oracle"] = err
+        r["cpu_baseline"] = {"value": n * n / cpu_s / 1e6, "unit": UNIT,
+                             "cores": Oracle().num_threads(), "kind": "port",
+                             "sample": "one step of the full %dx%d grid with the oracle's "
+                                       "Newton fallback, oracle/gpr_oracle.c" % (n, n)}
+    return r
 
 
 def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
@@ -900,6 +986,45 @@ def batched_bench(torch, steps=10, plain_steps=2, count=512):
     cells = int(B.nx.sum())
     vb = upd_b / (ms_b * 1e-3) / 1e6
     vp = cells * plain_steps / (ms_p * 1e-3) / 1e6
+    # per-stage times at the current state: the autotuner's timings of the
+    # shapes it keeps (CUDA events per launch), and the predictor status of
+    # one step from that state for the Picard iteration count
+    shapes = B.autotune()
+    tm = np.array(B.tuning["candidate_ms"])
+    B.step(1)
+    st2 = B.status.cpu().numpy()
+    iters, kind = st2 >> 8, st2 & 0xff
+    mean_it = float(iters[kind == 0].mean())
+    bs3 = [32, 64, 128]
+    nb = int((B.nx + 2).sum())
+    nf = int((B.nx + 1).sum())
+    stage = {
+        "k_b_weno": (tm[[64, 128, 256, 512].index(shapes["weno_block"])],
+                     OPS_1D["weno_per_cell"] * nb),
+        "k_predictor_first+k_predictor_picard": (
+            tm[4 + 3 * bs3.index(shapes["first_block"]) + bs3.index(shapes["picard_block"])],
+            OPS_1D["predictor_per_cell_iter"] * nb * (mean_it - 0.5)),
+        "k_faces1d" + ("_split" if shapes["faces_four_lanes"] else ""): (
+            tm[13 + 3 * shapes["faces_four_lanes"] + bs3.index(shapes["faces_block"])],
+            OPS_1D["face_point"] * nf * 2),
+        "k_cells": (tm[19 + bs3.index(shapes["cells_block"])], OPS_1D["cells_per_cell"] * cells),
+    }
+    peak = None
+    try:
+        peak = fp64_peak_tflops(torch)
+    except Exception:
+        pass
+    per = {}
+    for k, (ms, fl) in stage.items():
+        ach = fl / (ms * 1e-3) / 1e12
+        per[k] = {"ms_per_launch": float(ms), "algorithmic_flops_per_launch": float(fl),
+                  "achieved": ach, "frac": ach / peak if peak else None}
+    dom = max(per, key=lambda k: per[k]["ms_per_launch"])
+    roof = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": peak,
+            "peak_source": "measured: FP64 DFMA microbenchmark in bench.py on this GPU",
+            "achieved": per[dom]["achieved"], "frac": per[dom]["frac"],
+            "algorithmic_flops_per_launch": per[dom]["algorithmic_flops_per_launch"],
+            "mean_picard_iterations": mean_it, "per_kernel": per, "traffic": None}
     return {"workload": "%d 1D shock tubes, nx ~ U{128..2048} (%d cells), random states and "
                         "materials (mu ~ logU[1e-4,1e-1], cs ~ U[0.5,5], gamma ~ U[1.2,1.67]), "
                         "own CFL-0.8 clocks" % (count, cells),
@@ -907,7 +1032,8 @@ def batched_bench(torch, steps=10, plain_steps=2, count=512):
             "speedup": vb / vp, "batched_ms_per_step": ms_b / steps,
             "plain_loop_ms_per_step": ms_p / plain_steps,
             "newton_cells_last_step": int(((st & 0xff) == 1).sum()),
-            "batched_steps": steps, "plain_steps": plain_steps}
+            "batched_steps": steps, "plain_steps": plain_steps,
+            "autotuned_shapes": shapes, "roofline": roof}
 
 
 def stage_times(lib, torch, u, MP, nX, dXa, bc, cfl, V, dev, sp, stream, reps=3):
@@ -1046,6 +1172,21 @@ def profile_adjoint(ninst, steps):
     return 0
 
 
+def profile_batched(steps, shapes):
+    """`steps` steps of the 512 batched shock tubes (for ncu captures), with
+    the given launch shapes (default shapes if empty), no autotuning."""
+    import torch
+    import phd_gb300 as G
+    from phd_gb300.batch import Batch
+    insts = [(u, MP, dX, bcs) for (u, MP, tf, dX, bcs) in G.problems.batched_shock_tubes(512)]
+    B = Batch(insts, cfl=0.8, tf=0.2, autotune=False)
+    if shapes:
+        B.set_shapes([int(x) for x in shapes.split(",")])
+    B.step(steps)
+    torch.cuda.synchronize()
+    return 0
+
+
 def profile_shock_tube(flux, steps):
     """`steps` steps of the 200-cell shock tube through gpr_iterate (for ncu
     captures)."""
@@ -1076,6 +1217,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_batched:
+        return profile_batched(args.profile_steps or 3, args.shapes)
     if args.profile_adjoint:
         return profile_adjoint(args.profile_adjoint, args.profile_steps or 32)
     if args.profile_shock_tube >= 0:

@@ -225,5 +225,21 @@ int main(int argc, char **argv) {
   printf("weno_point                 %8.1f\n", Fweno);
   printf("cfl_per_cell               %8.1f\n", Fcfl);
   printf("mean_picard_iterations     %8.3f\n", (double)iters / ncb);
+  // 1D kernels (the batched form and 1D grids), same per-state costs:
+  // face point per (face, time node) of k_faces1d: as the 2D point with a
+  // 2-lane reduce-scatter of the 17 (b, f) pairs (18 adds) and the 9 kept
+  // pairs' sums and differences (18); predictor node: one derivative, one
+  // flux and one DG_DER term; volume node: one derivative, a 4-lane
+  // reduce-scatter (10 + 5 adds), cell adds 17 x 3; WENO: 17 points per
+  // predictor cell; CFL: one wave speed.
+  double Fface1 = 2 * 17 * 3 + 2 * Fp + 2 * Fm + 17 * 2 + 2 * Ff + 17 + 2 * Fbint_node + 34 +
+                  18 + 18;
+  double Fpred_node1 = Fp + Fs + (6 * 3 + Fb + 9) + Ff + 11 * 4 + 17 * 2 + 17 * 3 + 17 * 3;
+  double Fcell1 = 4 * (Fp + Fs + (6 * 3 + Fb + 9) + 15) + 17 * 3;
+  printf("face_point_1d              %8.1f\n", Fface1);
+  printf("predictor_cell_iteration_1d %7.1f\n", 4 * Fpred_node1);
+  printf("cells_per_cell_1d          %8.1f\n", Fcell1);
+  printf("weno_per_cell_1d           %8.1f\n", Fweno * V);
+  printf("cfl_per_cell_1d            %8.1f\n", Fp + Fm + 2);
   return 0;
 }
