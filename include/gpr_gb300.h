@@ -253,6 +253,50 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
                                 int32_t *status, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* The 1D step at another number of Gauss nodes.  The reference fixes N (its
+ * basis functions / Gauss nodes per dimension) at compile time
+ * (code/cpp/src/options.h:15); N = 3 is its third-order scheme: degree-2
+ * polynomials in space and time and a WENO reconstruction that adds the
+ * central stencil with weight LAMC = 1e5 (solvers/weno/weno.cpp:17-73).
+ * These entry points take N as `order`: 3 for V = 17 or 14, and 2 for
+ * V = 17 (the same formulation at N = 2, a cross-check of the N = 2 kernels
+ * above).  1D grids only (ndim = 1), Rusanov flux only (Roe and Osher give
+ * GPR_E_UNSUPPORTED).  Layouts as above with N = order:
+ *   ub [nx + 2N][V], wh [nx + 2][N][V], qh [nx + 2][N][N][V].
+ * Each replaces the entry point of the same name without _n; the predictor
+ * runs the reference's Picard iteration (dg/dg1.cpp:58-114) and has no
+ * Newton pass: a cell whose iteration does not converge within 50 steps or
+ * turns NaN gets its last iterate and GPR_PRED_FAILED in `status` (the
+ * reference leaves such rows unwritten or calls Newton-Krylov).
+ * gpr_order_supported returns 1 for the (order, ndim, nvar) compiled in;
+ * gpr_scheme_constants_n writes nodes[N], weights[N], end values [2][N],
+ * derivative values [N][N] and the oscillation indicator [N][N] (returns
+ * the count, 4N + 2N^2). */
+int gpr_order_supported(int order, int ndim, int nvar);
+int gpr_scheme_constants_n(double *out, int n, int order);
+int gpr_boundaries_n(const double *u, double *ub, const int32_t *nX, int ndim,
+                     const int32_t *bcs, int nvar, int order, void *stream);
+int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndim,
+                        int nvar, int order, void *stream);
+int gpr_predictor_n(double *qh, const double *wh, double dt, const double *dX, int ndim,
+                    const int32_t *nX, const gpr_par *par, const uint8_t *mask,
+                    int32_t *status, int nvar, int order, void *stream);
+long gpr_fv_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
+int gpr_fv_launcher_n(double *u, const double *qh, const int32_t *nX, double dt,
+                      const double *dX, int ndim, int flux, const gpr_par *par,
+                      const uint8_t *mask, double *scratch, int nvar, int order,
+                      void *stream);
+long gpr_ader_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
+int gpr_ader_stepper_n(double *u, const double *ub, const int32_t *nX, int ndim, double dt,
+                       const double *dX, int flux, const gpr_par *par, const uint8_t *mask,
+                       double *scratch, int32_t *status, int nvar, int order, void *stream);
+long gpr_iterate_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
+int gpr_iterate_n(double *u, const int32_t *nX, int ndim, const double *dX,
+                  const int32_t *bcs, int flux, const gpr_par *par, const uint8_t *mask,
+                  double *clock, int nsteps, double *scratch, int32_t *status,
+                  double contorted_tol, int nvar, int order, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Split scheme (the reference driver's default, SPLIT = true):
  * gpr_midstepper      GPRpy.solvers.split.midstepper (split/homogeneous.h:7):
  *                     wh -= dt/2 (dF/dx + B dw/dx)/dx [+ y] at the WENO nodes.

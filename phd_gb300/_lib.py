@@ -13,10 +13,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgpr_gb300.so")
-SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu", "gpr_multi.cu"]
+SOURCES = ["gpr_capi.cu", "gpr_adjoint.cu", "gpr_multi.cu", "gpr_order.cu"]
 HEADERS = ["gpr_device.cuh", "gpr_kernels.cuh", "gpr_consts.cuh", "gpr_ode.cuh", "gpr_host.cuh",
            "gpr_osher.cuh", "gpr_ops.cuh", "gpr_ops15.h", "gpr_multi.cuh",
-           "gpr_adjoint.cuh"]
+           "gpr_adjoint.cuh", "gpr_order.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 _lock = threading.Lock()
@@ -101,6 +101,17 @@ SIGNATURES = {
     "gpr_batch_init": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _P, _I, _P]),
     "gpr_batch_iterate": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _I, _P]),
     "gpr_batch_autotune": (_I, [_P, _P, _I, _P, _P, _P, _P, _I, _P]),
+    "gpr_order_supported": (_I, [_I, _I, _I]),
+    "gpr_scheme_constants_n": (_I, [_P, _I, _I]),
+    "gpr_boundaries_n": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
+    "gpr_weno_launcher_n": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "gpr_predictor_n": (_I, [_P, _P, _D, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "gpr_fv_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
+    "gpr_fv_launcher_n": (_I, [_P, _P, _P, _D, _P, _I, _I, _P, _P, _P, _I, _I, _P]),
+    "gpr_ader_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
+    "gpr_ader_stepper_n": (_I, [_P, _P, _P, _I, _D, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "gpr_iterate_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
+    "gpr_iterate_n": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _D, _I, _I, _P]),
     "gpr_batch_get_shapes": (_I, [_P, _P]),
     "gpr_batch_set_shapes": (_I, [_P, _P]),
     "gpr_adj_num_fields": (_I, []),

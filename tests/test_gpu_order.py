@@ -1,0 +1,155 @@
+"""The 1D step at N = 3 Gauss nodes (the reference's third-order scheme)
+through the C ABI, against the reference's golden N = 3 stages and the N = 3
+oracle, and the same kernels at N = 2 against the N = 2 library.
+
+Bars (max |a-b| / (1+|b|)): stages 1e-13, except the WENO reconstruction,
+which at N = 3 adds the central stencil with weight 1e5 and epsilon 1e-14:
+on the nearly constant states of a shock tube the reference itself moves by
+~1e-8 under a one-ulp change of its input, so the reconstruction (and a step
+or run through it) is held at 1e-7."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+from oracle import Oracle
+from phd_gb300.params import Par
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda"
+
+
+@pytest.fixture(scope="module")
+def G3():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from phd_gb300.order import for_order
+    return for_order(3)
+
+
+def T(a, dtype=torch.float64):
+    return torch.tensor(np.ascontiguousarray(a), dtype=dtype, device=DEV)
+
+
+def H(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy()
+
+
+def test_n3_stages_against_golden(G3):
+    g = golden("stages1d_rus_v17n3.npz")
+    MP = Par.from_array(g["mp"])
+    nX, dX = [int(g["nX"][0])], list(g["dX"])
+    nx = nX[0]
+    dt = float(g["dt"])
+    u = T(g["u"])
+    ub = torch.full((g["ub"].size,), np.nan, dtype=torch.float64, device=DEV)
+    G3.boundaries(u, ub, nX, [int(g["bcs"])] * 2)
+    assert rel_err(H(ub), g["ub"]) == 0.0
+    wh = torch.full((g["wh"].size,), np.nan, dtype=torch.float64, device=DEV)
+    G3.solvers.weno.weno_launcher(wh, T(g["ub"]), nX)
+    assert rel_err(H(wh), g["wh"]) < 1e-7
+    qh = torch.full((g["qh"].size,), np.nan, dtype=torch.float64, device=DEV)
+    mask = torch.ones(nx + 2, dtype=torch.bool, device=DEV)
+    status = torch.full((nx + 2,), -1, dtype=torch.int32, device=DEV)
+    G3.solvers.dg.predictor(qh, T(g["wh"]), dt, dX, False, False, MP, mask, status=status)
+    assert ((H(status) & 0xff) == 0).all()
+    assert rel_err(H(qh), g["qh"]) < 1e-13
+    ufv = T(g["u"])
+    G3.solvers.fv.fv_launcher(ufv, T(g["qh"]), nX, dt, dX, True, True, 0, MP, mask)
+    assert rel_err(H(ufv), g["u_fv"]) < 1e-14
+    ust = T(g["u"])
+    G3.solvers.ader_stepper(ust, T(g["ub"]), nX, dt, dX, False, 0, MP, mask)
+    import phd_gb300
+    phd_gb300.solvers.renorm_distortion(ust, [MP])
+    assert rel_err(H(ust), g["u_step"]) < 1e-7
+
+
+def test_n3_stages_against_oracle(G3):
+    """On a state with structure everywhere (a shock tube after 30 oracle
+    steps): WENO to the conditioning bar, predictor, FV update and one full
+    step from the oracle's inputs to 1e-13."""
+    from phd_gb300 import problems
+    O = Oracle(N=3)
+    u0, MP, tf, dX, bcs = problems.shock_tube(nx=128)
+    u_np, _, _ = O.run(u0, MP, 1e9, dX, 0, cfl=0.8, max_steps=30)
+    nX = np.array([128], np.int32)
+    dt = O.timestep(u_np, dX, 0.8, 0.0, 1e9, 30, MP)
+    ub = O.boundaries(u_np, nX, [0, 0])
+    wh = O.weno_launcher(ub, nX)
+    wh_d = torch.empty(wh.size, dtype=torch.float64, device=DEV)
+    G3.solvers.weno.weno_launcher(wh_d, T(ub), nX)
+    assert rel_err(H(wh_d), wh) < 1e-7
+    qh, st = O.predictor(wh, dt, dX, nX, MP, newton_fallback=0)
+    assert (st > 0).all()
+    qh_d = torch.empty(qh.size, dtype=torch.float64, device=DEV)
+    status = torch.full((130,), -1, dtype=torch.int32, device=DEV)
+    G3.solvers.dg.predictor(qh_d, T(wh), dt, dX, False, False, MP, None, status=status, nX=nX)
+    assert rel_err(H(qh_d), qh) < 1e-13
+    assert ((H(status) >> 8) == st).all(), "the same Picard iteration counts"
+    ref = u_np.ravel().copy()
+    O.fv_launcher(ref, qh, nX, dt, dX, MP)
+    u = T(u_np).view(-1)
+    G3.solvers.fv.fv_launcher(u, T(qh), nX, dt, dX, True, True, 0, MP, None)
+    assert rel_err(H(u), ref) < 1e-13
+
+
+def test_n3_shock_tube_run_against_oracle(G3):
+    """60 steps of the 200-cell shock tube at N = 3 through the device loop
+    (CFL time step, boundaries, step, renorm, contortion check on the
+    device clock) against the oracle's loop."""
+    from phd_gb300 import problems
+    O = Oracle(N=3)
+    u0, MP, tf, dX, bcs = problems.shock_tube(nx=200)
+    ref, n, t = O.run(u0, MP, 1e9, dX, 0, cfl=0.8, max_steps=60, contorted_tol=1.0)
+    u = T(u0).view(-1)
+    clock = torch.tensor([0.0, 0.0, 1e9, 0.8, 0.0], dtype=torch.float64, device=DEV)
+    G3.iterate(u, [200], dX, [0, 0], MP, clock, 60, contorted_tol=1.0)
+    c = H(clock)
+    assert int(c[4]) == 60
+    assert abs(c[0] - t) <= 1e-12 * t
+    got = H(u).reshape(ref.shape)
+    assert np.isfinite(got).all()
+    assert rel_err(got, ref) < 1e-7
+
+
+def test_generic_kernels_at_n2_match_the_n2_library():
+    """The node-per-thread kernels at N = 2 against the shuffle-based N = 2
+    kernels: one full step of a 300-cell tube (the two formulations round in
+    different orders)."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import phd_gb300 as G
+    from phd_gb300 import problems
+    from phd_gb300.order import for_order
+    G2 = for_order(2)
+    O = Oracle()
+    u0, MP, tf, dX, bcs = problems.shock_tube(nx=300)
+    u_np, _, _ = O.run(u0, MP, 1e9, dX, 0, cfl=0.8, max_steps=25)
+    nX = np.array([300], np.int32)
+    dt = O.timestep(u_np, dX, 0.8, 0.0, 1e9, 25, MP)
+    ub = T(O.boundaries(u_np, nX, [0, 0]))
+    a = T(u_np).view(-1)
+    b = T(u_np).view(-1)
+    G.solvers.ader_stepper(a, ub, nX, dt, dX, False, 0, MP, None)
+    G2.solvers.ader_stepper(b, ub, nX, dt, dX, False, 0, MP, None)
+    assert rel_err(H(b), H(a)) < 1e-13
+    assert rel_err(H(b), u_np.ravel()) > 1e-6
+
+
+def test_order_arguments_are_checked(G3):
+    from phd_gb300 import _lib, problems
+    lib = _lib.load()
+    assert lib.gpr_order_supported(3, 1, 17) == 1
+    assert lib.gpr_order_supported(3, 2, 17) == 0
+    assert lib.gpr_order_supported(4, 1, 17) == 0
+    u0, MP, tf, dX, bcs = problems.shock_tube(nx=16)
+    u = T(u0).view(-1)
+    ub = torch.zeros((16 + 6) * 17, dtype=torch.float64, device=DEV)
+    with pytest.raises(RuntimeError):  # Osher is not compiled for N = 3
+        G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, False, 2, MP, None)
+    with pytest.raises(RuntimeError):  # no stiff Newton predictor at N = 3
+        G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, True, 0, MP, None)
+    with pytest.raises(RuntimeError):  # unknown boundary code
+        G3.boundaries(u, ub, [16], [0, 9])

@@ -198,3 +198,19 @@ def test_scheme_constants_without_gpu():
     assert np.allclose(G.solvers.common.end_values(), c["endvals"], rtol=0, atol=1e-15)
     assert np.allclose(G.solvers.common.derivative_values(), c["dervals"], rtol=0, atol=1e-14)
     assert np.allclose(G.solvers.weno.oscillation_indicator(), c["sig"], rtol=0, atol=1e-13)
+
+
+def test_scheme_constants_at_three_nodes_without_gpu():
+    """The N = 3 constants the node kernels use, from the library on the host,
+    against the N = 3 oracle's (pinned by the golden N = 3 stages) and the
+    closed forms of three-point Gauss-Legendre on [0, 1]."""
+    from oracle import Oracle
+    from phd_gb300.order import for_order
+    c = Oracle(N=3).constants()
+    k = for_order(3).scheme_constants()
+    s = np.sqrt(0.6)
+    assert np.allclose(k["nodes"], [(1 - s) / 2, 0.5, (1 + s) / 2], rtol=0, atol=1e-16)
+    assert np.allclose(k["weights"], [5 / 18, 8 / 18, 5 / 18], rtol=0, atol=1e-15)
+    for key in ("nodes", "weights", "endvals", "dervals"):
+        assert np.allclose(k[key], c[key], rtol=0, atol=1e-13), key
+    assert np.allclose(k["sig"], c["sig"], rtol=1e-13, atol=1e-12)
