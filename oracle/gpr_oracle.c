@@ -17,6 +17,7 @@
  * compile time.  VISCOUS is always on and MULTI always off.
  */
 #include <math.h>
+#include <float.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -756,6 +757,15 @@ void or_Bdot(const double *Q, const double *x, int d, double *ret) {
 static void hessenberg(int n, double *H, double *Z) {
   /* H is n x n row-major (stride EMAX); Z accumulates (if not NULL). */
   for (int k = 0; k < n - 2; k++) {
+    /* no reflection when the part below the subdiagonal is already zero to
+     * the least normal number, as Eigen's makeHouseholder decides
+     * (eigen3/src/Householder/Householder.h:76-83): reflecting a column of
+     * subnormal entries would divide by an underflowed norm */
+    double tail = 0.0;
+    for (int i = k + 2; i < n; i++)
+      tail += H[i * EMAX + k] * H[i * EMAX + k];
+    if (tail <= DBL_MIN)
+      continue;
     double alpha = 0.0;
     for (int i = k + 1; i < n; i++)
       alpha += H[i * EMAX + k] * H[i * EMAX + k];

@@ -22,6 +22,9 @@
 
 namespace gpr {
 
+// the least positive normal double (DBL_MIN)
+constexpr double DBL_MIN_NORMAL = 2.2250738585072014e-308;
+
 // Material parameters with the per-material constants the kernels need
 // hoisted out of the per-node code (e.g. rho0 / (2 mu^(1/n)), 1/kappa).
 struct DevPar {
@@ -410,13 +413,19 @@ template <int n> GPR_D double max_abs_eig(double (&H)[n][n]) {
 #pragma unroll
   for (int k = 0; k < n - 2; k++) {
     double v[n];
-    double alpha = 0.0;
+    double alpha = 0.0, tail = 0.0;
 #pragma unroll
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < n; i++) {
       if (i > k)
         alpha += H[i][k] * H[i][k];
+      if (i > k + 1)
+        tail += H[i][k] * H[i][k];
+    }
     alpha = sqrt(alpha);
-    if (alpha != 0.0) {
+    // no reflection when the column below the subdiagonal is zero to the
+    // least normal number (Eigen's makeHouseholder rule): a reflector of
+    // subnormal entries would divide by an underflowed norm
+    if (alpha != 0.0 && tail > DBL_MIN_NORMAL) {
       double x0 = H[k + 1][k];
       double beta = x0 > 0 ? -alpha : alpha;
 #pragma unroll

@@ -221,6 +221,16 @@ GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, do
 template <int n> GPR_D void hess_reduce(double *H, double *Z) {
 #pragma unroll 1
   for (int k = 0; k < n - 2; k++) {
+    // no reflection when the column below the subdiagonal is zero to the
+    // least normal number (Eigen's makeHouseholder rule, which the
+    // reference's EigenSolver follows): a reflector built from subnormal
+    // entries would divide by an underflowed norm
+    double tail = 0.0;
+#pragma unroll 1
+    for (int i = k + 2; i < n; i++)
+      tail += H[i * n + k] * H[i * n + k];
+    if (tail <= DBL_MIN_NORMAL)
+      continue;
     double alpha = 0.0;
 #pragma unroll 1
     for (int i = k + 1; i < n; i++)
@@ -838,6 +848,11 @@ GPR_D double warp_sum(double x) {
 template <int n> GPR_D void w_hess(double *H, double *Z, double *v, int lane) {
 #pragma unroll 1
   for (int k = 0; k < n - 2; k++) {
+    double tl = 0.0;  // the column below the subdiagonal (as hess_reduce)
+    for (int i = k + 2 + lane; i < n; i += 32)
+      tl += H[i * n + k] * H[i * n + k];
+    if (warp_sum(tl) <= DBL_MIN_NORMAL)
+      continue;
     double a2 = 0.0;
     for (int i = k + 1 + lane; i < n; i += 32)
       a2 += H[i * n + k] * H[i * n + k];
