@@ -309,3 +309,63 @@ def test_device_loop_per_step_against_oracle(G, O, shear, bar):
         prev, dt_prev, t = got, dt, t1
     assert worst < bar, worst
     assert (it.status.cpu().numpy() == 0).all()
+
+
+def test_config3_loop_per_step_against_oracle(G, O):
+    """The shock-bubble workload's own data: isotropic distortions, mu = 1e-4
+    (the configuration's), a 200 x 100 grid of [0, 2] x [0, 1] with the shock
+    meeting the bubble; every step of the device loop against one oracle
+    step from the GPU's previous state, dt and step count.  Bar per step: the
+    reference scheme's own rounding sensitivity on that state, measured here
+    as the oracle's response to 1e-15 relative noise on its input (1e-13
+    before the shock reaches the bubble, up to ~2e-6 once interface cells
+    carry isotropic star states): the device step within 4x that (and 1e-10
+    at least), at most 1e-5 overall, and at least 99% of the cells within
+    1e-10 at every step."""
+    from phd_gb300 import problems
+    from phd_gb300.ghost import MultiIterator
+    u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=200, ny=100, mu=1e-4, x_shock=0.36)
+    nX = np.array(u0.shape[:2], np.int32)
+    it = MultiIterator(nX, dX, 0, MPs, 0.8, 1e9, device=DEV)
+    ut = T(u0.ravel())
+    prev = u0.copy()
+    dt_prev, t = 0.0, 0.0
+    rng = np.random.default_rng(3)
+    worst, worst_frac = 0.0, 1.0
+    for s in range(12):
+        it.run(ut, 1)
+        t1, dt, _, _, cnt = it.clock.tolist()
+        ref = prev.copy()
+        O.step_multi(ref, dt_prev, t, 1e9, s, MPs, dX, 0, dt=dt, contorted_tol=1.0)
+        resp = 0.0
+        for _ in range(2):
+            noisy = prev * (1 + 1e-15 * rng.standard_normal(prev.shape))
+            O.step_multi(noisy, dt_prev, t, 1e9, s, MPs, dX, 0, dt=dt, contorted_tol=1.0)
+            resp = max(resp, rel_err(noisy, ref))
+        got = ut.cpu().numpy().reshape(u0.shape)
+        assert np.isfinite(got).all() and np.isfinite(ref).all()
+        cell = np.max(np.abs(got - ref) / (1 + np.abs(ref)), axis=-1)
+        assert cell.max() <= max(1e-10, 4 * resp), (s, cell.max(), resp)
+        worst = max(worst, float(cell.max()))
+        worst_frac = min(worst_frac, float((cell <= 1e-10).mean()))
+        prev, dt_prev, t = got, dt, t1
+    assert worst <= 1e-5, worst
+    assert worst_frac >= 0.99, worst_frac
+    assert (it.status.cpu().numpy() == 0).all()
+
+
+def test_config3_fill_against_oracle(G, O):
+    """The ghost fill on the workload's data (isotropic, mu = 1e-4, 240 x 120,
+    the shock through the bubble's left half): masks exact, copied cells
+    exact, filled cells within 1e-6 and at least 90% within 1e-10."""
+    from phd_gb300 import problems
+    u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=240, ny=120, mu=1e-4, x_shock=0.36)
+    nX = np.array(u0.shape[:2], np.int32)
+    u, steps, t = O.run_multi(u0, MPs, 1e9, dX, 0, max_steps=25)
+    dt = 0.8 * min(dX) / 3.0
+    ug, grids, masks, st = _fill_gpu(G, u, nX, dX, dt, MPs)
+    uo, go, mo, im, bad = O.fill_ghost_cells(u.ravel(), nX, dX, dt, MPs)
+    assert bad == 0 and (st == 0).all()
+    assert np.max(np.abs(ug - uo)) < 1e-12
+    assert np.array_equal(masks, mo)
+    _check_fill(grids, go, im, filled_tol=1e-6, frac=0.9)

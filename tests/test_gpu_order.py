@@ -98,20 +98,32 @@ def test_n3_stages_against_oracle(G3):
 def test_n3_shock_tube_run_against_oracle(G3):
     """60 steps of the 200-cell shock tube at N = 3 through the device loop
     (CFL time step, boundaries, step, renorm, contortion check on the
-    device clock) against the oracle's loop."""
+    device clock) against the oracle's loop.  The bar is the reference
+    scheme's own rounding sensitivity on this run, measured here: the oracle
+    rerun from the initial state times (1 + 1e-16 xi) moves by ~5e-7 after
+    60 steps (the central WENO stencil on the tube's nearly constant states);
+    the device run must stay within 10x that."""
     from phd_gb300 import problems
     O = Oracle(N=3)
     u0, MP, tf, dX, bcs = problems.shock_tube(nx=200)
     ref, n, t = O.run(u0, MP, 1e9, dX, 0, cfl=0.8, max_steps=60, contorted_tol=1.0)
+    rng = np.random.default_rng(1)
+    resp = 0.0
+    for _ in range(2):
+        up = u0 * (1 + 1e-16 * rng.standard_normal(u0.shape))
+        r2, _, _ = O.run(up, MP, 1e9, dX, 0, cfl=0.8, max_steps=60, contorted_tol=1.0)
+        resp = max(resp, rel_err(r2, ref))
+    assert 1e-9 < resp < 1e-5, resp
     u = T(u0).view(-1)
     clock = torch.tensor([0.0, 0.0, 1e9, 0.8, 0.0], dtype=torch.float64, device=DEV)
     G3.iterate(u, [200], dX, [0, 0], MP, clock, 60, contorted_tol=1.0)
     c = H(clock)
     assert int(c[4]) == 60
-    assert abs(c[0] - t) <= 1e-12 * t
+    # the clock sums the CFL steps of states held to the WENO bar
+    assert abs(c[0] - t) <= 1e-7 * t
     got = H(u).reshape(ref.shape)
     assert np.isfinite(got).all()
-    assert rel_err(got, ref) < 1e-7
+    assert rel_err(got, ref) < 10 * resp, (rel_err(got, ref), resp)
 
 
 def test_generic_kernels_at_n2_match_the_n2_library():
