@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--profile-shock-tube", type=int, default=-1, metavar="FLUX",
                     help="with --profile-steps K: K steps of the 200-cell shock tube with "
                          "flux FLUX (0 Rusanov, 1 Roe, 2 Osher) through gpr_iterate, no JSON")
+    ap.add_argument("--split", action="store_true",
+                    help="with --profile-shock-tube: the split scheme (gpr_iterate_split)")
     ap.add_argument("--profile-batched", action="store_true",
                     help="with --profile-steps K: K steps of the 512 batched shock tubes with "
                          "the default launch shapes or --shapes, no JSON")
@@ -544,8 +546,10 @@ def shock_tube_bench(torch):
     t_end = 0.2 (248 steps), Rusanov (FLUX 0) and Osher (FLUX 2) ADER steps,
     and the reference driver's default split scheme (SPLIT, HALF_STEP).  The whole
     run is one gpr_iterate call (dt on the device, no host synchronisation),
-    timed with CUDA events; the oracle (C restatement of the reference) runs
-    the same problem on the host cores."""
+    captured once in a CUDA graph and timed as one replay with CUDA events
+    (`gpu_ms_stream_launches`: the same call's launches on the stream); the
+    oracle (C restatement of the reference) runs the same problem on the host
+    cores."""
     import phd_gb300 as G
     from phd_gb300 import _lib
     from oracle import Oracle
@@ -560,10 +564,16 @@ def shock_tube_bench(torch):
                       dtype=torch.float64, device="cuda")
     O = Oracle()
     out = {"workload": "shock tube 200 cells, V=17, CFL 0.8, t_end 0.2"}
+    ut = torch.empty(200 * V, dtype=torch.float64, device="cuda")
+    clk = torch.empty(5, dtype=torch.float64, device="cuda")
+    u0d = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+    clk0 = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
     for flux, split, name in ((0, 0, "rusanov"), (2, 0, "osher"), (0, 1, "split_rusanov")):
         def run():
-            ut = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
-            clk = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
+            # the whole run (260 >= 248 steps; steps past tf change nothing)
+            # on the current stream, inputs already on the device
+            ut.copy_(u0d)
+            clk.copy_(clk0)
             sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
             if split:  # the reference driver's default (SPLIT, HALF_STEP)
                 rc = lib.gpr_iterate_split(
@@ -580,12 +590,28 @@ def shock_tube_bench(torch):
                     ctypes.c_void_p(clk.data_ptr()), 260, ctypes.c_void_p(scr.data_ptr()), None,
                     CONTORTED_TOL, V, sp)
             _lib.check(rc, "iterate")
-            return ut, clk
         run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        ut, clk = run()
+        run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms_stream = e0.elapsed_time(e1)
+        # the same run captured once in a CUDA graph and replayed (the loop
+        # needs no host synchronisation); the run's own launches are
+        # latency-bound at this size, so the replay removes launch gaps
+        g = torch.cuda.CUDAGraph()
+        cs = torch.cuda.Stream()
+        cs.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cs):
+            with torch.cuda.graph(g, stream=cs):
+                run()
+        torch.cuda.current_stream().wait_stream(cs)
+        g.replay()
+        torch.cuda.synchronize()
+        e0.record()
+        g.replay()
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -595,7 +621,7 @@ def shock_tube_bench(torch):
                           half_step=True)
         cpu_s = time.perf_counter() - t0
         got = ut.cpu().numpy().reshape(ref.shape)
-        out[name] = {"steps": steps, "gpu_ms": ms,
+        out[name] = {"steps": steps, "gpu_ms": ms, "gpu_ms_stream_launches": ms_stream,
                      "gpu_value": 200 * steps / (ms * 1e-3) / 1e6,
                      "cpu_value": 200 * n / cpu_s / 1e6, "cpu_cores": O.num_threads(),
                      "unit": UNIT, "max_rel_diff_vs_oracle":
@@ -899,11 +925,37 @@ def adjoint_bench(torch, fd_check=True):
         e[1].record()
         torch.cuda.synchronize()
         fwd_plain = e[0].elapsed_time(e[1])
+        # the same gradient with the forward keeping its segments' tapes (the
+        # whole run fits in device memory): the backward recomputes nothing
+        tp = Problem([nx] * ninst, [dx] * ninst, "transitive", make_par, cfl=0.8, tf=tf,
+                     tape_budget_bytes=32 << 30)
+        uN = tp.forward(torch.tensor(u0p, device="cuda"), pars).clone().requires_grad_(True)
+        loss(uN).backward()
+        tp.backward(uN.grad)
+        torch.cuda.synchronize()
+        e[0].record()
+        uN = tp.forward(torch.tensor(u0p, device="cuda"), pars)
+        e[1].record()
+        uN = uN.clone().requires_grad_(True)
+        loss(uN).backward()
+        ub1, fb1 = tp.backward(uN.grad)
+        e[2].record()
+        torch.cuda.synchronize()
+        fwd_t, bwd_t = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        same = float(torch.max(torch.abs(fb1 - fb) / (1 + torch.abs(fb))).item())
         r = {"instances": ninst, "cells": nx * ninst, "steps": nsteps,
              "forward_ms_per_step": fwd / nsteps, "backward_ms_per_step": bwd / nsteps,
              "adjoint_over_forward": bwd / fwd,
              "plain_forward_ms_per_step": fwd_plain / plain.nsteps,
              "adjoint_over_plain_forward": (bwd / nsteps) / (fwd_plain / plain.nsteps),
+             "checkpoint_every": prob.K,
+             "taped_forward": {"forward_ms_per_step": fwd_t / tp.nsteps,
+                               "backward_ms_per_step": bwd_t / tp.nsteps,
+                               "recomputed_steps": tp.recomputed_steps,
+                               "tape_gb": len(tp.seg_tapes) * tp.K * tp.tape_len * 8 / 1e9,
+                               "adjoint_over_plain_forward": (bwd_t / tp.nsteps) /
+                                                             (fwd_plain / plain.nsteps),
+                               "field_gradient_rel_diff_vs_checkpointed": same},
              "cell_updates_per_s_forward": nx * ninst * nsteps / (fwd * 1e-3),
              "transposed_iterations_mean": prob.adj_iterations}
         if fd_check and ninst == 1:
@@ -1187,9 +1239,9 @@ def profile_batched(steps, shapes):
     return 0
 
 
-def profile_shock_tube(flux, steps):
-    """`steps` steps of the 200-cell shock tube through gpr_iterate (for ncu
-    captures)."""
+def profile_shock_tube(flux, steps, split=False):
+    """`steps` steps of the 200-cell shock tube through gpr_iterate, or
+    gpr_iterate_split with the half step (for ncu captures)."""
     import torch
     import phd_gb300 as G
     from phd_gb300 import _lib
@@ -1203,12 +1255,21 @@ def profile_shock_tube(flux, steps):
                       dtype=torch.float64, device="cuda")
     ut = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
     clk = torch.tensor([0.0, 0.0, tf, 0.8, 0.0], dtype=torch.float64, device="cuda")
-    _lib.check(lib.gpr_iterate(
-        ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
-        dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
-        ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None, ctypes.c_void_p(clk.data_ptr()),
-        steps, ctypes.c_void_p(scr.data_ptr()), None, CONTORTED_TOL, 17,
-        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "iterate")
+    if split:
+        rc = lib.gpr_iterate_split(
+            ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+            dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux, 1,
+            ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+            ctypes.c_void_p(clk.data_ptr()), steps, ctypes.c_void_p(scr.data_ptr()),
+            CONTORTED_TOL, 17, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    else:
+        rc = lib.gpr_iterate(
+            ctypes.c_void_p(ut.data_ptr()), nx.ctypes.data_as(ctypes.c_void_p), 1,
+            dxa.ctypes.data_as(ctypes.c_void_p), bca.ctypes.data_as(ctypes.c_void_p), flux,
+            ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+            ctypes.c_void_p(clk.data_ptr()), steps, ctypes.c_void_p(scr.data_ptr()), None,
+            CONTORTED_TOL, 17, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "iterate")
     torch.cuda.synchronize()
     return 0
 
@@ -1222,7 +1283,7 @@ def main():
     if args.profile_adjoint:
         return profile_adjoint(args.profile_adjoint, args.profile_steps or 32)
     if args.profile_shock_tube >= 0:
-        return profile_shock_tube(args.profile_shock_tube, args.profile_steps or 10)
+        return profile_shock_tube(args.profile_shock_tube, args.profile_steps or 10, args.split)
     if args.profile_shock_bubble:
         return profile_shock_bubble(args.profile_shock_bubble, args.profile_steps or 4)
     return run_gb300(args)

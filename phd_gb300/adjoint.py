@@ -57,10 +57,17 @@ class Problem:
     instance; cfl, tf: as the reference's iterator; make_par(theta) -> Par.
     frozen_dt: differentiate with each step's dt held fixed (False: through
     the CFL rule).  dg_tol / dg_it: predictor stopping rule of the forward.
+    checkpoint_every: steps per segment; the backward pass restores each
+    segment's checkpoint and recomputes its steps with a tape.
+    tape_budget_bytes: device memory the forward pass may spend on keeping
+    the tapes of whole segments as it runs (0: none, the classic
+    checkpointing); a segment taped in the forward needs no recompute in the
+    backward.  The first segments that fit are kept.
     """
 
     def __init__(self, nx, dx, bcs, make_par, cfl=0.8, tf=1.0, nvar=17, frozen_dt=False,
-                 dg_tol=1e-13, dg_it=300, checkpoint_every=32, device="cuda"):
+                 dg_tol=1e-13, dg_it=300, checkpoint_every=32, tape_budget_bytes=0,
+                 device="cuda"):
         self.lib = _lib.load()
         self.nx = np.ascontiguousarray(np.asarray(nx, dtype=np.int32))
         self.ninst = self.nx.size
@@ -88,6 +95,8 @@ class Problem:
         self.ascratch = torch.empty(_lib.check(n, "adj_scratch_doubles"), dtype=torch.float64,
                                     device=self.device)
         self.tapes = None
+        self.tape_budget = int(tape_budget_bytes)
+        self.seg_tapes = {}  # segment start step -> [K, tape_len] tapes kept by the forward
         self.clock = torch.zeros(5 * self.ninst, dtype=torch.float64, device=self.device)
         self.status = torch.zeros(self.nb, dtype=torch.int32, device=self.device)
         self.info = torch.zeros(self.nb, dtype=torch.int32, device=self.device)
@@ -157,6 +166,10 @@ class Problem:
             self.schedule = []
         replay = schedule is not None
         self.checkpoints = []
+        self.seg_tapes = {}
+        seg_bytes = self.K * self.tape_len * 8
+        kept = 0
+        tape = None
         step = 0
         # the clocks are checked once per segment; steps taken after an
         # instance reached tf have dt = 0 and change nothing
@@ -169,7 +182,13 @@ class Problem:
                 if not replay and self._done():
                     break
                 self.checkpoints.append((step, u.clone(), self.clock.clone()))
-            self._step(u, None, step, replay)
+                tape = None
+                if kept + seg_bytes <= self.tape_budget:
+                    tape = torch.empty(self.K, self.tape_len, dtype=torch.float64,
+                                       device=self.device)
+                    self.seg_tapes[step] = tape
+                    kept += seg_bytes
+            self._step(u, tape[step % self.K] if tape is not None else None, step, replay)
             step += 1
         self.nsteps = step
         self.replayed = replay
@@ -185,16 +204,23 @@ class Problem:
         thbar = torch.zeros(self.ninst * 6, dtype=torch.float64, device=self.device)
         tbar = torch.zeros(self.ninst, dtype=torch.float64, device=self.device)
         self.info.zero_()
+        self.recomputed_steps = 0
         for (s0, u_ck, clk_ck) in reversed(self.checkpoints):
             n = min(self.K, self.nsteps - s0)
-            u = u_ck.clone()
-            self.clock.copy_(clk_ck)
-            for j in range(n):
-                self._step(u, self.tapes[j], s0 + j, self.replayed)
+            tapes = self.seg_tapes.get(s0)
+            if tapes is None:  # recompute the segment from its checkpoint
+                tapes = self.tapes
+                u = u_ck.clone()
+                self.clock.copy_(clk_ck)
+                for j in range(n):
+                    self._step(u, tapes[j], s0 + j, self.replayed)
+                self.recomputed_steps += n
+            else:  # the forward's own tape; the backward step needs the clock
+                self.clock.copy_(clk_ck)
             for j in reversed(range(n)):
                 _lib.check(self.lib.gpr_adj_backward_step(
                     self._t(ubar), self._t(thbar), self._t(tbar), int(self.frozen_dt),
-                    self.ninst, self._p(self.nx), self._t(self.scratch), self._t(self.tapes[j]),
+                    self.ninst, self._p(self.nx), self._t(self.scratch), self._t(tapes[j]),
                     self._t(self.ascratch), self._t(self.info), self.V, self._stream()),
                     "adj_backward_step")
         bad = (self.info & 0xff) != 0

@@ -486,3 +486,30 @@ def test_batched_gradients_equal_single_instance():
         assert np.allclose(t1.grad.numpy()[0], G[k], rtol=1e-12, atol=0), k
         assert np.allclose(u1.grad.cpu().numpy(), G0[k * nx:(k + 1) * nx], rtol=1e-12,
                            atol=1e-300), k
+
+
+def test_taped_forward_gives_the_checkpointed_gradient():
+    """A forward pass that keeps its segments' tapes (tape_budget_bytes) lets
+    the backward pass skip the recompute; the tapes are the ones the
+    recompute would write, so the gradients are identical, also when only
+    the first segments fit the budget."""
+    _cuda()
+    from phd_gb300.adjoint import Problem
+    nx, tf = 400, 1.0
+    u0p, dx, target = _misfit_setup(nx, tf)
+    pars = [make_par(THETA)]
+    out = []
+    for budget in (0, 1 << 34, None):
+        prob = Problem([nx], [dx], "transitive", make_par, cfl=0.8, tf=tf, checkpoint_every=32)
+        if budget is None:  # two segments' worth: the rest is recomputed
+            budget = 2 * 32 * prob.tape_len * 8
+        prob.tape_budget = budget
+        uN = prob.forward(torch.tensor(u0p, device="cuda"), pars, max_steps=100)
+        uN = uN.clone().requires_grad_(True)
+        _loss(uN, target).backward()
+        ub0, fb = prob.backward(uN.grad)
+        out.append((ub0.cpu().numpy(), fb.cpu().numpy(), prob.recomputed_steps))
+    assert out[0][2] == 100 and out[1][2] == 0 and out[2][2] == 100 - 64
+    for k in (1, 2):
+        assert np.array_equal(out[k][0], out[0][0])
+        assert np.array_equal(out[k][1], out[0][1])
