@@ -906,34 +906,79 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
       if (!done) {
         Prim<L::THERMAL> st;
         prim<L::THERMAL>(q, P, st);
+        // this time node's diagonal block A_t = M_tt I - a_t dS/dA of the
+        // 18 x 18 Newton matrix (the off-diagonal blocks are M_t,1-t I) and
+        // its right-hand side
         stiff_jacobian_rows<L::THERMAL>(q, st, P, a_t, M0, Am + t * 9 * NA + t * 9, NA,
                                         Jm + t * 3 * NJ + t * 3, NJ);
-#pragma unroll
-        for (int a = 0; a < 9; a++)
-#pragma unroll
-          for (int b = 0; b < 9; b++)
-            Am[(t * 9 + a) * NA + (1 - t) * 9 + b] = a == b ? (float)M1 : 0.0f;
 #pragma unroll
         for (int a = 0; a < 9; a++)
           Ab[t * 9 + a] = (float)(r[5 + a] * iws);
         if (L::THERMAL) {
 #pragma unroll
           for (int a = 0; a < 3; a++)
-#pragma unroll
-            for (int b = 0; b < 3; b++)
-              Jm[(t * 3 + a) * NJ + (1 - t) * 3 + b] = a == b ? (float)M1 : 0.0f;
-#pragma unroll
-          for (int a = 0; a < 3; a++)
             Jb[t * 3 + a] = (float)(r[14 + a] * iws);
+        }
+      }
+      __syncwarp();
+      // Block elimination of [[A0, m01 I], [m10 I, A1]] [x0; x1] = [b0; b1]:
+      // (A0 A1 - m01 m10 I) x1 = A0 b1 - m10 b0 and x0 = (b1 - A1 x1) / m10,
+      // a 9 x 9 solve (3 x 3 for the heat flux) in place of 18 x 18 (6 x 6).
+      // The two time-node lanes form the reduced matrix's rows (into block
+      // (0, 1) of Am), lane t = 0 its right-hand side (block (1, 0)'s first
+      // row) and lane t = 1 the heat-flux system.
+      const float m01 = (float)C.dgmat[0][1], m10 = (float)C.dgmat[1][0];
+      const float *A0 = Am, *A1 = Am + 9 * NA + 9;
+      float *Rm = Am + 9, *Rb = Am + 9 * NA;
+      const float *J0 = Jm, *J1 = Jm + 3 * NJ + 3;
+      float *RJm = Jm + 3, *RJb = Jm + 3 * NJ;
+      if (!done) {
+        const int r0 = t == 0 ? 0 : 5, r1 = t == 0 ? 5 : 9;
+        for (int rr = r0; rr < r1; rr++) {
+#pragma unroll
+          for (int c = 0; c < 9; c++) {
+            float acc = rr == c ? -m01 * m10 : 0.0f;
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+              acc = fmaf(A0[rr * NA + k], A1[k * NA + c], acc);
+            Rm[rr * NA + c] = acc;
+          }
+        }
+        if (t == 0) {
+#pragma unroll
+          for (int rr = 0; rr < 9; rr++) {
+            float acc = -m10 * Ab[rr];
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+              acc = fmaf(A0[rr * NA + k], Ab[9 + k], acc);
+            Rb[rr] = acc;
+          }
+        } else if (L::THERMAL) {
+#pragma unroll
+          for (int rr = 0; rr < 3; rr++) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              float acc = rr == c ? -m01 * m10 : 0.0f;
+#pragma unroll
+              for (int k = 0; k < 3; k++)
+                acc = fmaf(J0[rr * NJ + k], J1[k * NJ + c], acc);
+              RJm[rr * NJ + c] = acc;
+            }
+            float acc = -m10 * Jb[rr];
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+              acc = fmaf(J0[rr * NJ + k], Jb[3 + k], acc);
+            RJb[rr] = acc;
+          }
         }
       }
       __syncwarp();
       bool solved = true;
       if (!done) {
         if (t == 0)
-          solved = smem_solve<NA>(Am, NA, Ab);
+          solved = smem_solve<9>(Rm, NA, Rb);
         else if (L::THERMAL)
-          solved = smem_solve<NJ>(Jm, NJ, Jb);
+          solved = smem_solve<3>(RJm, NJ, RJb);
       }
       __syncwarp();
       // non-stiff variables: DG_MAT^-1 g / W_s (partner time node's residual)
@@ -943,13 +988,33 @@ __global__ void __launch_bounds__(64) k_predictor_stiff(
 #pragma unroll
       for (int k = 0; k < V; k++)
         delta[k] = ia * r[k] + ib * other[k];
+      // stiff variables: x1 from the reduced solve, x0 = (b1 - A1 x1) / m10
+      const float im10 = 1.0f / m10;
 #pragma unroll
-      for (int a = 0; a < 9; a++)
-        delta[5 + a] = (double)Ab[t * 9 + a];
+      for (int a = 0; a < 9; a++) {
+        float x = Rb[a];
+        if (t == 0) {
+          float acc = Ab[9 + a];
+#pragma unroll
+          for (int k = 0; k < 9; k++)
+            acc = fmaf(-A1[a * NA + k], Rb[k], acc);
+          x = acc * im10;
+        }
+        delta[5 + a] = (double)x;
+      }
       if (L::THERMAL) {
 #pragma unroll
-        for (int a = 0; a < 3; a++)
-          delta[14 + a] = (double)Jb[t * 3 + a];
+        for (int a = 0; a < 3; a++) {
+          float x = RJb[a];
+          if (t == 0) {
+            float acc = Jb[3 + a];
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+              acc = fmaf(-J1[a * NJ + k], RJb[k], acc);
+            x = acc * im10;
+          }
+          delta[14 + a] = (double)x;
+        }
       }
       __syncwarp();
       bool big = false, bad = !solved;
