@@ -88,6 +88,8 @@ def parse():
                          "(for ncu captures)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only this many steps (for ncu captures), no JSON")
+    ap.add_argument("--profile-flux", type=int, default=0,
+                    help="with --profile-steps: the TGV steps' flux (0 Rusanov, 1 Roe, 2 Osher)")
     ap.add_argument("--profile-shock-tube", type=int, default=-1, metavar="FLUX",
                     help="with --profile-steps K: K steps of the 200-cell shock tube with "
                          "flux FLUX (0 Rusanov, 1 Roe, 2 Osher) through gpr_iterate, no JSON")
@@ -301,6 +303,77 @@ extern "C" int dfma_peak_launch(double *out, int iters, int grid, int block, voi
 """
 
 
+# FP64 tensor-core throughput (DMMA: mma.sync m8n8k4 f64, 512 flops per warp
+# instruction) measured the same way, to decide DMMA against DFMA for the
+# small FP64 contractions of the path: 8 independent accumulator chains per
+# warp, operands in registers, one guarded store so nothing is dead code.
+DMMA_PEAK_SRC = r"""
+#include <cuda_runtime.h>
+__global__ void dmma_peak(double *out, int iters) {
+  double a = 1.0 + threadIdx.x * 1e-9, b = 0.999999999;
+  double c[8][2];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    c[k][0] = k * 1e-3;
+    c[k][1] = k * 2e-3;
+  }
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, "
+                   "{%0, %1};"
+                   : "+d"(c[k][0]), "+d"(c[k][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    s += c[k][0] + c[k][1];
+  if (s == 12345.678) out[0] = s;
+}
+extern "C" int dmma_peak_launch(double *out, int iters, int grid, int block, void *stream) {
+  dmma_peak<<<grid, block, 0, (cudaStream_t)stream>>>(out, iters);
+  return (int)cudaGetLastError();
+}
+"""
+
+
+def dmma_peak_tflops(torch):
+    """Measured FP64 tensor-core (DMMA) throughput of this GPU in TFLOP/s."""
+    from phd_gb300 import _lib
+    bdir = os.path.join(ROOT, "phd_gb300", "_build")
+    so = os.path.join(bdir, "dmmapeak.so")
+    src = os.path.join(bdir, "dmmapeak.cu")
+    os.makedirs(bdir, exist_ok=True)
+    if not os.path.exists(so) or not os.path.exists(src) or open(src).read() != DMMA_PEAK_SRC:
+        open(src, "w").write(DMMA_PEAK_SRC)
+        subprocess.run(["nvcc"] + _lib.ARCH + ["-O3", "-shared", "-Xcompiler", "-fPIC", "-o",
+                                               so, src], check=True)
+    lib = ctypes.CDLL(so)
+    lib.dmma_peak_launch.restype = ctypes.c_int
+    lib.dmma_peak_launch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_void_p]
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    iters = 1024
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    grid, block = sms * 4, 256
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    po = ctypes.c_void_p(out.data_ptr())
+    assert lib.dmma_peak_launch(po, iters, grid, block, stream) == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        lib.dmma_peak_launch(po, iters, grid, block, stream)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        flops = 512.0 * 8 * iters * grid * (block // 32)
+        best = max(best, flops / (ms * 1e-3) / 1e12)
+    return best
+
+
 def fp64_peak_tflops(torch):
     """Measured FP64 FMA throughput of this GPU (TFLOP/s, 2 flops per DFMA),
     from an own kernel of independent DFMA chains."""
@@ -376,9 +449,11 @@ def run_gb300(args):
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
 
+    flux = args.profile_flux if args.profile_steps else 0
+
     def step(k=1, uu=None):
         uu = u if uu is None else uu
-        _lib.check(lib.gpr_iterate(ctypes.c_void_p(uu.data_ptr()), pn, 2, pd, pb, 0, pp, None,
+        _lib.check(lib.gpr_iterate(ctypes.c_void_p(uu.data_ptr()), pn, 2, pd, pb, flux, pp, None,
                                    ctypes.c_void_p(clock.data_ptr()), k,
                                    ctypes.c_void_p(scratch.data_ptr()),
                                    ctypes.c_void_p(status.data_ptr()), CONTORTED_TOL, V, sp),
@@ -452,6 +527,13 @@ def run_gb300(args):
         peak_err = None
 
     roof = roofline(stage_ms, ncell, n, mean_iters, peak)
+    try:
+        roof["dmma_peak_tflops"] = dmma_peak_tflops(torch)
+        roof["dmma_note"] = ("FP64 tensor-core (mma.sync m8n8k4 f64) throughput measured "
+                             "beside the DFMA peak; the path's contractions stay on DFMA "
+                             "unless this is higher")
+    except Exception as ex:  # reported, not fatal to the line
+        roof["dmma_error"] = str(ex)
     batched = None
     if rank == 0 and not args.no_batched:
         try:
