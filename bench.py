@@ -1125,8 +1125,29 @@ def batched_bench(torch, steps=10, plain_steps=2, count=512):
     # one step from that state for the Picard iteration count
     shapes = B.autotune()
     tm = np.array(B.tuning["candidate_ms"])
+    u_before = B.u.cpu().numpy().copy()
     B.step(1)
     st2 = B.status.cpu().numpy()
+    # that step of every running instance against one oracle step from the
+    # same state and with the same dt (the Newton fallback where Picard fails)
+    from oracle import Oracle
+    O = Oracle()
+    clk = B.clock.view(-1, 5).cpu().numpy()
+    u_after = B.u.cpu().numpy()
+    worst, ninst_checked = 0.0, 0
+    for k, (u_, MP, dX, bc) in enumerate(insts):
+        dtk = float(clk[k, 1])
+        if dtk == 0.0:
+            continue
+        a, b = int(B.off[k]) * V, int(B.off[k + 1]) * V
+        st_k = u_before[a:b].reshape(-1, V)
+        nxk = np.array([st_k.shape[0]], np.int32)
+        code = 1 if bc == "periodic" else 0
+        ref = st_k.ravel().copy()
+        O.ader_stepper(ref, O.boundaries(st_k, nxk, [code, code]), nxk, dtk, dX, MP)
+        O.renorm_distortion(ref, MP)
+        worst = max(worst, float(np.max(np.abs(u_after[a:b] - ref) / (1.0 + np.abs(ref)))))
+        ninst_checked += 1
     iters, kind = st2 >> 8, st2 & 0xff
     mean_it = float(iters[kind == 0].mean())
     bs3 = [32, 64, 128]
@@ -1167,7 +1188,8 @@ def batched_bench(torch, steps=10, plain_steps=2, count=512):
             "plain_loop_ms_per_step": ms_p / plain_steps,
             "newton_cells_last_step": int(((st & 0xff) == 1).sum()),
             "batched_steps": steps, "plain_steps": plain_steps,
-            "autotuned_shapes": shapes, "roofline": roof}
+            "autotuned_shapes": shapes, "roofline": roof,
+            "max_rel_diff_vs_oracle": worst, "instances_checked_against_oracle": ninst_checked}
 
 
 def stage_times(lib, torch, u, MP, nX, dXa, bc, cfl, V, dev, sp, stream, reps=3):
