@@ -1,6 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the compiled
 reference solver (oracle/_ref, built by `python oracle/build_ref.py v17
-v17n3 v15`), one reference variant per process.
+v17n3 v15`), one reference variant per process (`make_golden.py v17n3`
+writes the N = 3 fixtures alone).
 
 Every array in the fixtures is an output of the reference's own C++ code
 (haranjackson/phd, code/cpp/src) on seeded inputs; inputs are stored beside
@@ -283,6 +284,18 @@ def main():
         import subprocess
         for v in ("v15", "v17"):
             subprocess.run([sys.executable, os.path.abspath(__file__), v], check=True)
+        return 0
+    if variant == "v17n3":  # the N = 3 fixtures alone (this variant only)
+        R3 = rd.load("v17n3")
+        if R3 is None:
+            print("oracle/_ref/GPRref_v17n3 not built; run oracle/build_ref.py v17n3")
+            return 1
+        u0, MP, tf, dX, bcs = problems.shock_tube(nx=64)
+        np.savez_compressed(os.path.join(HERE, "stages1d_rus_v17n3.npz"),
+                            **stages(R3, u0, MP, dX, 0, 0.8, 10, flux=0))
+        u0, MP, tf, dX, bcs = problems.taylor_green(n=12, ny=10, cs=10.0, mu=0.1)
+        np.savez_compressed(os.path.join(HERE, "stages2d_rus_v17n3.npz"),
+                            **stages(R3, u0, MP, dX, 1, 0.4, 2, flux=0))
         return 0
     if variant == "v15":
         R15 = rd.load("v15")

@@ -68,7 +68,8 @@ def test_pointwise_physics(O):
                                     ("stages1d_osh_v17.npz", 2),
                                     ("stages2d_rus_v17.npz", 2),
                                     ("stages2d_osh_v17.npz", 2),
-                                    ("stages1d_rus_v17n3.npz", 3)])
+                                    ("stages1d_rus_v17n3.npz", 3),
+                                    ("stages2d_rus_v17n3.npz", 3)])
 def test_stages(name, N):
     g = golden(name)
     O = Oracle(N=N)
