@@ -253,21 +253,25 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
                                 int32_t *status, int nvar, void *stream);
 
 /* ------------------------------------------------------------------------ */
-/* The 1D step at another number of Gauss nodes.  The reference fixes N (its
+/* The step at another number of Gauss nodes.  The reference fixes N (its
  * basis functions / Gauss nodes per dimension) at compile time
  * (code/cpp/src/options.h:15); N = 3 is its third-order scheme: degree-2
  * polynomials in space and time and a WENO reconstruction that adds the
  * central stencil with weight LAMC = 1e5 (solvers/weno/weno.cpp:17-73).
  * These entry points take N as `order`: 3 for V = 17 or 14, and 2 for
  * V = 17 (the same formulation at N = 2, a cross-check of the N = 2 kernels
- * above).  1D grids only (ndim = 1), Rusanov flux only (Roe and Osher give
- * GPR_E_UNSUPPORTED).  Layouts as above with N = order:
- *   ub [nx + 2N][V], wh [nx + 2][N][V], qh [nx + 2][N][N][V].
+ * above).  1D and 2D grids (ndim = 1 or 2; every extent at least N), the
+ * Rusanov flux only (Roe and Osher give GPR_E_UNSUPPORTED).  Layouts as
+ * above with N = order, n_s = N^ndim space nodes per cell:
+ *   ub [nx + 2N] ([ny + 2N]) [V], wh [nx + 2] ([ny + 2]) [n_s][V],
+ *   qh [nx + 2] ([ny + 2]) [N][n_s][V], space nodes x-major.
  * Each replaces the entry point of the same name without _n; the predictor
- * runs the reference's Picard iteration (dg/dg1.cpp:58-114) and has no
- * Newton pass: a cell whose iteration does not converge within 50 steps or
- * turns NaN gets its last iterate and GPR_PRED_FAILED in `status` (the
- * reference leaves such rows unwritten or calls Newton-Krylov).
+ * runs the reference's Picard iteration (dg/dg1.cpp:58-114, dg2.cpp:
+ * 102-171) and has no Newton pass: a cell whose iteration does not converge
+ * within 50 steps or turns NaN gets its last iterate and GPR_PRED_FAILED in
+ * `status` (the reference leaves such rows unwritten or calls Newton-Krylov).
+ * The 2D WENO needs device scratch of gpr_weno_scratch_doubles_n doubles for
+ * its x sweep (0 in 1D, where scratch may be NULL).
  * gpr_order_supported returns 1 for the (order, ndim, nvar) compiled in;
  * gpr_scheme_constants_n writes nodes[N], weights[N], end values [2][N],
  * derivative values [N][N] and the oscillation indicator [N][N] (returns
@@ -276,8 +280,9 @@ int gpr_order_supported(int order, int ndim, int nvar);
 int gpr_scheme_constants_n(double *out, int n, int order);
 int gpr_boundaries_n(const double *u, double *ub, const int32_t *nX, int ndim,
                      const int32_t *bcs, int nvar, int order, void *stream);
+long gpr_weno_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
 int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndim,
-                        int nvar, int order, void *stream);
+                        double *scratch, int nvar, int order, void *stream);
 int gpr_predictor_n(double *qh, const double *wh, double dt, const double *dX, int ndim,
                     const int32_t *nX, const gpr_par *par, const uint8_t *mask,
                     int32_t *status, int nvar, int order, void *stream);

@@ -104,7 +104,8 @@ SIGNATURES = {
     "gpr_order_supported": (_I, [_I, _I, _I]),
     "gpr_scheme_constants_n": (_I, [_P, _I, _I]),
     "gpr_boundaries_n": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
-    "gpr_weno_launcher_n": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "gpr_weno_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
+    "gpr_weno_launcher_n": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
     "gpr_predictor_n": (_I, [_P, _P, _D, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
     "gpr_fv_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
     "gpr_fv_launcher_n": (_I, [_P, _P, _P, _D, _P, _I, _I, _P, _P, _P, _I, _I, _P]),

@@ -1,4 +1,4 @@
-// gpr_order.cu - C ABI of the 1D step at a chosen number of Gauss nodes
+// gpr_order.cu - C ABI of the 1D and 2D step at a chosen number of Gauss nodes
 // (`order`, the reference's compile-time N): the kernels of gpr_order.cuh for
 // N = 3, and the same kernels at N = 2 (a second formulation of the N = 2
 // step, which the tests hold against the shuffle-based N = 2 kernels).
@@ -22,76 +22,126 @@ template <int NO> const ConstsN<NO> &consts_n() {
   return c;
 }
 
-// The 1D step's stages at NO nodes for the layout L.
+// The step's stages at NO nodes for the layout L on a 1D or 2D grid
+// (nX[0] [x nX[1]] interior cells).
 template <class L, int NO> struct OpsN {
   static constexpr int V = L::V;
-  using NB = NodeBlock<NO>;
 
-  static long ub_doubles(int nx) { return (long)(nx + 2 * NO) * V; }
-  static long wh_doubles(int nx) { return (long)(nx + 2) * NO * V; }
-  static long qh_doubles(int nx) { return (long)(nx + 2) * NO * NO * V; }
-  static long fb_doubles(int nx) { return (long)(nx + 1) * NO * 2 * V; }
+  struct Grid {
+    int nd, nx, ny;
+    Grid(const int32_t *nX, int nd_) : nd(nd_), nx(nX[0]), ny(nd_ == 2 ? nX[1] : 1) {}
+    long ncell() const { return (long)nx * ny; }
+    long ncb() const { return nd == 1 ? nx + 2 : (long)(nx + 2) * (ny + 2); }
+    long nub() const { return nd == 1 ? nx + 2 * NO : (long)(nx + 2 * NO) * (ny + 2 * NO); }
+    int ns() const { return nd == 1 ? NO : NO * NO; }
+    // face grid of one direction: 1D nx + 1 faces; 2D (nx + 1) x (ny + 1)
+    long nface() const { return nd == 1 ? nx + 1 : (long)(nx + 1) * (ny + 1); }
+  };
 
-  static int boundaries(const double *u, double *ub, int nx, const int32_t *bcs,
+  static long ub_doubles(const Grid &g) { return g.nub() * V; }
+  static long wh_doubles(const Grid &g) { return g.ncb() * g.ns() * V; }
+  static long qh_doubles(const Grid &g) { return g.ncb() * NO * g.ns() * V; }
+  // the face terms of every direction (the x sweep's node values of the 2D
+  // WENO use the same scratch before them)
+  static long fb_doubles(const Grid &g) {
+    const long faces = g.nface() * g.ns() * 2 * V * g.nd;
+    const long ux = g.nd == 1 ? 0 : (long)(g.nx + 2) * (g.ny + 2 * NO) * NO * V;
+    return faces > ux ? faces : ux;
+  }
+
+  static int boundaries(const double *u, double *ub, const Grid &g, const int32_t *bcs,
                         cudaStream_t st) {
-    long n = ub_doubles(nx);
-    k_boundaries1d_n<V, NO><<<blocks(n, 256), 256, 0, st>>>(u, ub, nx, bcs[0], bcs[1]);
+    k_boundaries_n<V, NO><<<blocks(g.nub(), 128), 128, 0, st>>>(
+        u, ub, g.nx, g.ny, g.nd, bcs[0], bcs[1], g.nd == 2 ? bcs[2] : 0,
+        g.nd == 2 ? bcs[3] : 0);
     return cuda_rc();
   }
-  static int weno(double *wh, const double *ub, int nx, cudaStream_t st) {
-    const int ncb = nx + 2;
-    k_weno1d_n<V, NO><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, consts_n<NO>());
+  static int weno(double *wh, const double *ub, const Grid &g, double *tmp, cudaStream_t st) {
+    const ConstsN<NO> &C = consts_n<NO>();
+    if (g.nd == 1) {
+      const int ncb = g.nx + 2;
+      k_weno1d_n<V, NO><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, C);
+      return cuda_rc();
+    }
+    const int nxp = g.nx + 2, nyp = g.ny + 2, nyb = g.ny + 2 * NO;
+    k_weno2d_x_n<V, NO><<<blocks((long)nxp * nyb * V, 256), 256, 0, st>>>(tmp, ub, nxp, nyb, C);
+    k_weno2d_y_n<V, NO><<<blocks((long)nxp * nyp * NO * V, 256), 256, 0, st>>>(wh, tmp, nxp, nyp,
+                                                                              C);
     return cuda_rc();
   }
-  static int predictor(double *qh, const double *wh, double dt, const double *dt_dev, double dx,
-                       int nx, const DevPar &P, const uint8_t *mask, int32_t *status,
-                       cudaStream_t st) {
-    const long ncb = nx + 2;
-    k_predictor1d_n<L, NO><<<(unsigned)((ncb + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
-        qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dx, P, consts_n<NO>());
+  static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
+                       const double *dX, const Grid &g, const DevPar &P, const uint8_t *mask,
+                       int32_t *status, cudaStream_t st) {
+    const long ncb = g.ncb();
+    const double idy = g.nd == 2 ? 1.0 / dX[1] : 1.0;
+    if (g.nd == 1) {
+      using NB = NodeBlock<NO, 1>;
+      k_predictor_n<L, NO, 1><<<(unsigned)((ncb + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
+          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], idy, P, consts_n<NO>());
+    } else {
+      using NB = NodeBlock<NO, 2>;
+      k_predictor_n<L, NO, 2><<<(unsigned)((ncb + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
+          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], idy, P, consts_n<NO>());
+    }
     return cuda_rc();
   }
-  static int fv(double *u, const double *qh, int nx, double dt, const double *dt_dev, double dx,
-                const DevPar &P, const uint8_t *mask, double *fb, cudaStream_t st) {
-    const long nf = (long)nx + 1;
-    k_faces1d_n<L, NO><<<blocks(nf * NO, 128), 128, 0, st>>>(fb, qh, nf, mask, dt, dt_dev, dx,
-                                                             P, consts_n<NO>());
-    k_cells1d_n<L, NO><<<(unsigned)((nx + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
-        u, qh, fb, nx, mask, dt, dt_dev, dx, P, consts_n<NO>());
+  static int fv(double *u, const double *qh, const Grid &g, double dt, const double *dt_dev,
+                const double *dX, const DevPar &P, const uint8_t *mask, double *fb,
+                cudaStream_t st) {
+    const ConstsN<NO> &C = consts_n<NO>();
+    const long nf = g.nface();
+    const double dy = g.nd == 2 ? dX[1] : 1.0;
+    if (g.nd == 1) {
+      using NB = NodeBlock<NO, 1>;
+      k_faces_n<L, NO, 1><<<blocks(nf * NO, 128), 128, 0, st>>>(fb, qh, g.nx, 1, 0, mask, dt,
+                                                                dt_dev, dX[0], dy, P, C);
+      k_cells_n<L, NO, 1><<<(unsigned)((g.nx + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
+          u, qh, fb, nullptr, g.nx, 1, mask, dt, dt_dev, dX[0], dy, P, C);
+      return cuda_rc();
+    }
+    using NB = NodeBlock<NO, 2>;
+    double *fby = fb + nf * NO * NO * 2 * V;
+    for (int d = 0; d < 2; d++)
+      k_faces_n<L, NO, 2><<<blocks(nf * NO * NO, 128), 128, 0, st>>>(
+          d ? fby : fb, qh, g.nx, g.ny, d, mask, dt, dt_dev, dX[0], dy, P, C);
+    k_cells_n<L, NO, 2><<<(unsigned)((g.ncell() + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
+        u, qh, fb, fby, g.nx, g.ny, mask, dt, dt_dev, dX[0], dy, P, C);
     return cuda_rc();
   }
   // scratch: wh, qh, face terms
-  static long step_scratch(int nx) { return wh_doubles(nx) + qh_doubles(nx) + fb_doubles(nx); }
-  static int step(double *u, const double *ub, int nx, double dt, const double *dt_dev,
-                  double dx, const DevPar &P, const uint8_t *mask, double *scr,
+  static long step_scratch(const Grid &g) { return wh_doubles(g) + qh_doubles(g) + fb_doubles(g); }
+  static int step(double *u, const double *ub, const Grid &g, double dt, const double *dt_dev,
+                  const double *dX, const DevPar &P, const uint8_t *mask, double *scr,
                   int32_t *status, cudaStream_t st) {
-    double *wh = scr, *qh = wh + wh_doubles(nx), *fb = qh + qh_doubles(nx);
+    double *wh = scr, *qh = wh + wh_doubles(g), *fb = qh + qh_doubles(g);
     int rc;
-    if ((rc = weno(wh, ub, nx, st)))
+    if ((rc = weno(wh, ub, g, fb, st)))
       return rc;
-    if ((rc = predictor(qh, wh, dt, dt_dev, dx, nx, P, mask, status, st)))
+    if ((rc = predictor(qh, wh, dt, dt_dev, dX, g, P, mask, status, st)))
       return rc;
-    return fv(u, qh, nx, dt, dt_dev, dx, P, mask, fb, st);
+    return fv(u, qh, g, dt, dt_dev, dX, P, mask, fb, st);
   }
   // scratch: ub, the step's scratch, the CFL maximum and the contortion flag
-  static long iterate_scratch(int nx) { return ub_doubles(nx) + step_scratch(nx) + 2; }
-  static int iterate(double *u, int nx, double dx, const int32_t *bcs, const DevPar &P,
-                     const uint8_t *mask, double *clk, int nsteps, double *scr,
+  static long iterate_scratch(const Grid &g) { return ub_doubles(g) + step_scratch(g) + 2; }
+  static int iterate(double *u, const Grid &g, const double *dX, const int32_t *bcs,
+                     const DevPar &P, const uint8_t *mask, double *clk, int nsteps, double *scr,
                      int32_t *status, double contorted_tol, cudaStream_t st) {
-    double *ub = scr, *sscr = ub + ub_doubles(nx);
-    unsigned long long *mx = (unsigned long long *)(sscr + step_scratch(nx));
+    double *ub = scr, *sscr = ub + ub_doubles(g);
+    unsigned long long *mx = (unsigned long long *)(sscr + step_scratch(g));
     const double *dt_dev = clk + 1;
+    const long ncell = g.ncell();
     for (int s = 0; s < nsteps; s++) {
       cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-      k_cfl_max<L><<<blocks(nx, 256), 256, 0, st>>>(u, nx, 1, dx, 1.0, mx, P);
+      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, g.nd, dX[0],
+                                                        g.nd == 2 ? dX[1] : 1.0, mx, P);
       k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
-      int rc = boundaries(u, ub, nx, bcs, st);
+      int rc = boundaries(u, ub, g, bcs, st);
       if (!rc)
-        rc = step(u, ub, nx, 0.0, dt_dev, dx, P, mask, sscr, status, st);
+        rc = step(u, ub, g, 0.0, dt_dev, dX, P, mask, sscr, status, st);
       if (rc)
         return rc;
-      k_renorm<V><<<blocks(nx, 256), 256, 0, st>>>(u, nx, P.rho0, dt_dev);
-      Ops<L>::contortion(u, nx, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
+      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
+      Ops<L>::contortion(u, ncell, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
       k_clock_advance<<<1, 1, 0, st>>>(clk);
     }
     return cuda_rc();
@@ -117,7 +167,21 @@ template <class L, int NO> struct OpsN {
   } while (0)
 
 bool bad_grid(const int32_t *nX, int ndim, int order) {
-  return !nX || ndim != 1 || nX[0] < order || order < 2;
+  return !nX || (ndim != 1 && ndim != 2) || order < 2 || nX[0] < order ||
+         (ndim == 2 && nX[1] < order);
+}
+
+bool bad_bcs(const int32_t *bcs, int ndim) {
+  if (!bcs)
+    return true;
+  for (int s = 0; s < 2 * ndim; s++)
+    if (bcs[s] < 0 || bcs[s] > 5)
+      return true;
+  return false;
+}
+
+bool bad_dX(const double *dX, int ndim) {
+  return !dX || !(dX[0] > 0) || (ndim == 2 && !(dX[1] > 0));
 }
 
 }  // namespace
@@ -125,7 +189,7 @@ bool bad_grid(const int32_t *nX, int ndim, int order) {
 extern "C" {
 
 int gpr_order_supported(int order, int ndim, int nvar) {
-  if (ndim != 1)
+  if (ndim != 1 && ndim != 2)
     return 0;
   return (order == 3 && (nvar == 17 || nvar == 14)) || (order == 2 && nvar == 17);
 }
@@ -162,88 +226,88 @@ int gpr_scheme_constants_n(double *out, int n, int order) {
 
 int gpr_boundaries_n(const double *u, double *ub, const int32_t *nX, int ndim,
                      const int32_t *bcs, int nvar, int order, void *stream) {
-  if (!u || !ub || !bcs || bad_grid(nX, ndim, order))
+  if (!u || !ub || bad_grid(nX, ndim, order) || bad_bcs(bcs, ndim))
     return GPR_E_ARG;
-  for (int s = 0; s < 2; s++)
-    if (bcs[s] < 0 || bcs[s] > 5)
-      return GPR_E_ARG;
-  DISPATCH_N(nvar, order, O::boundaries(u, ub, nX[0], bcs, S(stream)));
+  DISPATCH_N(nvar, order, O::boundaries(u, ub, typename O::Grid(nX, ndim), bcs, S(stream)));
 }
 
-int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndim, int nvar,
-                        int order, void *stream) {
-  if (!wh || !ub || bad_grid(nX, ndim, order))
+long gpr_weno_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
+  if (bad_grid(nX, ndim, order))
     return GPR_E_ARG;
-  DISPATCH_N(nvar, order, O::weno(wh, ub, nX[0], S(stream)));
+  DISPATCH_N(nvar, order, ndim == 1 ? 0L : O::fb_doubles(typename O::Grid(nX, ndim)));
+}
+
+int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndim,
+                        double *scratch, int nvar, int order, void *stream) {
+  if (!wh || !ub || bad_grid(nX, ndim, order) || (ndim == 2 && !scratch))
+    return GPR_E_ARG;
+  DISPATCH_N(nvar, order, O::weno(wh, ub, typename O::Grid(nX, ndim), scratch, S(stream)));
 }
 
 int gpr_predictor_n(double *qh, const double *wh, double dt, const double *dX, int ndim,
                     const int32_t *nX, const gpr_par *par, const uint8_t *mask, int32_t *status,
                     int nvar, int order, void *stream) {
-  if (!qh || !wh || !dX || !par || bad_grid(nX, ndim, order) || !(dX[0] > 0))
+  if (!qh || !wh || !par || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order,
-             O::predictor(qh, wh, dt, nullptr, dX[0], nX[0], P, mask, status, S(stream)));
+  DISPATCH_N(nvar, order, O::predictor(qh, wh, dt, nullptr, dX, typename O::Grid(nX, ndim), P,
+                                       mask, status, S(stream)));
 }
 
 long gpr_fv_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
   if (bad_grid(nX, ndim, order))
     return GPR_E_ARG;
-  DISPATCH_N(nvar, order, O::fb_doubles(nX[0]));
+  DISPATCH_N(nvar, order, O::fb_doubles(typename O::Grid(nX, ndim)));
 }
 
 int gpr_fv_launcher_n(double *u, const double *qh, const int32_t *nX, double dt,
                       const double *dX, int ndim, int flux, const gpr_par *par,
                       const uint8_t *mask, double *scratch, int nvar, int order, void *stream) {
-  if (!u || !qh || !dX || !par || !scratch || bad_grid(nX, ndim, order) || !(dX[0] > 0))
+  if (!u || !qh || !par || !scratch || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
   if (flux != GPR_FLUX_RUSANOV)
     return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order,
-             O::fv(u, qh, nX[0], dt, nullptr, dX[0], P, mask, scratch, S(stream)));
+  DISPATCH_N(nvar, order, O::fv(u, qh, typename O::Grid(nX, ndim), dt, nullptr, dX, P, mask,
+                                scratch, S(stream)));
 }
 
 long gpr_ader_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
   if (bad_grid(nX, ndim, order))
     return GPR_E_ARG;
-  DISPATCH_N(nvar, order, O::step_scratch(nX[0]));
+  DISPATCH_N(nvar, order, O::step_scratch(typename O::Grid(nX, ndim)));
 }
 
 int gpr_ader_stepper_n(double *u, const double *ub, const int32_t *nX, int ndim, double dt,
                        const double *dX, int flux, const gpr_par *par, const uint8_t *mask,
                        double *scratch, int32_t *status, int nvar, int order, void *stream) {
-  if (!u || !ub || !dX || !par || !scratch || bad_grid(nX, ndim, order) || !(dX[0] > 0))
+  if (!u || !ub || !par || !scratch || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
   if (flux != GPR_FLUX_RUSANOV)
     return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order,
-             O::step(u, ub, nX[0], dt, nullptr, dX[0], P, mask, scratch, status, S(stream)));
+  DISPATCH_N(nvar, order, O::step(u, ub, typename O::Grid(nX, ndim), dt, nullptr, dX, P, mask,
+                                  scratch, status, S(stream)));
 }
 
 long gpr_iterate_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
   if (bad_grid(nX, ndim, order))
     return GPR_E_ARG;
-  DISPATCH_N(nvar, order, O::iterate_scratch(nX[0]));
+  DISPATCH_N(nvar, order, O::iterate_scratch(typename O::Grid(nX, ndim)));
 }
 
 int gpr_iterate_n(double *u, const int32_t *nX, int ndim, const double *dX, const int32_t *bcs,
                   int flux, const gpr_par *par, const uint8_t *mask, double *clock, int nsteps,
                   double *scratch, int32_t *status, double contorted_tol, int nvar, int order,
                   void *stream) {
-  if (!u || !dX || !bcs || !par || !clock || !scratch || nsteps < 0 ||
-      bad_grid(nX, ndim, order) || !(dX[0] > 0))
+  if (!u || !par || !clock || !scratch || nsteps < 0 || bad_grid(nX, ndim, order) ||
+      bad_dX(dX, ndim) || bad_bcs(bcs, ndim))
     return GPR_E_ARG;
-  for (int s = 0; s < 2; s++)
-    if (bcs[s] < 0 || bcs[s] > 5)
-      return GPR_E_ARG;
   if (flux != GPR_FLUX_RUSANOV)
     return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::iterate(u, nX[0], dX[0], bcs, P, mask, clock, nsteps, scratch,
-                                     status, contorted_tol, S(stream)));
+  DISPATCH_N(nvar, order, O::iterate(u, typename O::Grid(nX, ndim), dX, bcs, P, mask, clock,
+                                     nsteps, scratch, status, contorted_tol, S(stream)));
 }
 
 }  // extern "C"

@@ -1,15 +1,17 @@
-// gpr_order.cuh - the 1D ADER-WENO step for a general number of Gauss nodes
-// NO (the reference's compile-time N, options.h:15), used for NO = 3 (third
-// order: degree-2 polynomials in space and time).  The N = 2 kernels in
-// gpr_kernels.cuh map a cell's N^(d+1) = 4 / 8 space-time nodes onto aligned
-// lane groups and exchange values with warp shuffles; 9 nodes per cell do not
-// align with a warp, so these kernels keep one thread per space-time node and
-// exchange a cell's node values through shared memory.
+// gpr_order.cuh - the 1D and 2D ADER-WENO step for a general number of
+// Gauss nodes NO (the reference's compile-time N, options.h:15), used for
+// NO = 3 (third order: degree-2 polynomials in space and time).  The N = 2
+// kernels in gpr_kernels.cuh map a cell's N^(d+1) = 4 / 8 space-time nodes
+// onto aligned lane groups and exchange values with warp shuffles; 9 or 27
+// nodes per cell do not align with a warp, so these kernels keep one thread
+// per space-time node and exchange a cell's node values through shared
+// memory.
 //
-// Restates for general N: etc/grid.cpp:12-146 (ghost cells), weno/weno.cpp:
-// 4-81 (WENO with the central stencil of odd N, LAMC = 1e5), dg/dg1.cpp:
-// 8-114 (Picard predictor), fv/fv.cpp:11-160 and fv/fluxes.cpp:9-75 (volume
-// term and Rusanov interface terms of the 1D FV update).
+// Restates for general N: etc/grid.cpp:12-170 (ghost cells), weno/weno.cpp:
+// 4-124 (WENO with the central stencil of odd N, LAMC = 1e5), dg/dg1.cpp:
+// 8-114 and dg/dg2.cpp:8-171 (Picard predictor), fv/fv.cpp:11-279 and
+// fv/fluxes.cpp:9-75 (volume term and Rusanov interface terms of the FV
+// update).
 #pragma once
 
 #include <math.h>
@@ -216,37 +218,69 @@ template <int NO> inline ConstsN<NO> make_consts_n() {
 
 // ---- kernels ---------------------------------------------------------------
 
-// ub from u with NO ghost cells per side (grid.cpp:12-146 for 1D): one
-// thread per (ub cell, variable).
-template <int V, int NO>
-__global__ void k_boundaries1d_n(const double *__restrict__ u, double *__restrict__ ub, int nx,
-                                 int bcl, int bcr) {
-  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (idx >= (long)(nx + 2 * NO) * V)
-    return;
-  const int k = idx % V;
-  const int c = idx / V;
-  if (c >= NO && c < nx + NO) {
-    ub[idx] = u[(long)(c - NO) * V + k];
-    return;
-  }
-  const int side = c >= nx + NO;
-  const int i = side ? c - nx - NO : c;  // ghost 0..NO-1 of that side
-  int code = side ? bcr : bcl;
-  int si;
+// Ghost-cell index along one axis (etc/grid.cpp:12-146): ghost i (0..NO-1)
+// of side `side` reads interior line index bc_src; periodic reads wrap.
+template <int NO> GPR_D int bc_src_n(int code, int side, int i, int n) {
   if (code == GPR_BC_TRANSMISSIVE)
-    si = side == 0 ? 0 : nx - 1;
-  else if (code == GPR_BC_PERIODIC)
-    si = side == 0 ? nx - NO + i : i;
-  else
-    si = side == 0 ? NO - 1 - i : nx - 1 - i;  // reflecting types
+    return side == 0 ? 0 : n - 1;
   if (code == GPR_BC_PERIODIC)
-    code = GPR_BC_TRANSMISSIVE;  // plain copy
-  ub[idx] = bc_value<V>(code, 0, k, u + (long)si * V);
+    return side == 0 ? n - NO + i : i;
+  return side == 0 ? NO - 1 - i : n - 1 - i;  // reflecting types
 }
 
-// 1D WENO (weno.cpp:17-81): one thread per (predictor cell, variable);
-// predictor cell i reads ub rows i .. i + 2N - 2.
+// ub from u with NO ghost cells per side (grid.cpp:12-170): one thread per
+// ub cell.  In 2D the x ghosts of the interior rows come first and the y
+// ghosts of every row (corners included) are taken from them, as the
+// reference's two passes do: a corner is the y boundary transform of the x
+// boundary transform of its interior source.
+template <int V, int NO>
+__global__ void k_boundaries_n(const double *__restrict__ u, double *__restrict__ ub, int nx,
+                               int ny, int nd, int bx0, int bx1, int by0, int by1) {
+  const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int nyb = nd == 1 ? 1 : ny + 2 * NO;
+  if (c >= (long)(nx + 2 * NO) * nyb)
+    return;
+  const int a = nd == 1 ? (int)c : (int)(c / nyb), b = nd == 1 ? 0 : (int)(c % nyb);
+  int ai = a - NO, bj = nd == 1 ? 0 : b - NO;
+  int cx = -1, cy = -1;  // boundary codes applied (-1: interior along that axis)
+  if (ai < 0 || ai >= nx) {
+    const int side = ai >= nx;
+    cx = side ? bx1 : bx0;
+    ai = bc_src_n<NO>(cx, side, side ? ai - nx : a, nx);
+  }
+  if (nd == 2 && (bj < 0 || bj >= ny)) {
+    const int side = bj >= ny;
+    cy = side ? by1 : by0;
+    bj = bc_src_n<NO>(cy, side, side ? bj - ny : b, ny);
+  }
+  double q[V], w[V];
+  const double *src = u + ((long)ai * (nd == 1 ? 1 : ny) + bj) * V;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    q[k] = src[k];
+  if (cx >= 0 && cx != GPR_BC_PERIODIC) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      w[k] = bc_value<V>(cx, 0, k, q);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      q[k] = w[k];
+  }
+  if (cy >= 0 && cy != GPR_BC_PERIODIC) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      w[k] = bc_value<V>(cy, 1, k, q);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      q[k] = w[k];
+  }
+  double *dst = ub + c * V;
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    dst[k] = q[k];
+}
+
+// WENO (weno.cpp:4-124) at general N.
 template <int NO> GPR_D double weno_weight_n(const double *wv, const ConstsN<NO> &C, double lam) {
   double t = 0.0;
 #pragma unroll
@@ -264,20 +298,17 @@ template <int NO> GPR_D double weno_weight_n(const double *wv, const ConstsN<NO>
   return lam / t;
 }
 
-template <int V, int NO>
-__global__ void k_weno1d_n(double *__restrict__ wh, const double *__restrict__ ub, int ncb,
-                           ConstsN<NO> C) {
+// coeffs (weno.cpp:17-73) for one variable: data rows d[r * sd] (r = 0 ..
+// 2N-2), node values out[a * so]; the side stencils are left out near the
+// ends (`gap`, the reference's NO_CORNERS handling) as the reference does.
+template <int NO>
+GPR_D void weno_point_n(const double *__restrict__ d, long sd, double *__restrict__ out, long so,
+                        int ind, int n, int gap, const ConstsN<NO> &C) {
   static_assert(NO % 2 == 1 || NO == 2, "odd N (central stencil) or N = 2");
-  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (idx >= (long)ncb * V)
-    return;
-  const int k = idx % V;
-  const int i = idx / V;
-  const double *d = ub + (long)i * V + k;
   double row[2 * NO - 1];
 #pragma unroll
   for (int r = 0; r < 2 * NO - 1; r++)
-    row[r] = d[(long)r * V];
+    row[r] = d[(long)r * sd];
   constexpr int FN2 = (NO - 1) / 2;  // floor((N - 1) / 2)
   double wL[NO], wR[NO], wC[NO];
 #pragma unroll
@@ -293,43 +324,103 @@ __global__ void k_weno1d_n(double *__restrict__ wh, const double *__restrict__ u
     wR[a] = sR;
     wC[a] = sC;
   }
+  const bool useL = ind >= gap, useR = ind <= n - gap - 1, useC = NO > 2 && ind + FN2 >= gap;
   const double oL = weno_weight_n<NO>(wL, C, LAMS), oR = weno_weight_n<NO>(wR, C, LAMS);
   const double oC = NO > 2 ? weno_weight_n<NO>(wC, C, LAMC) : 0.0;
-  const double den = NO > 2 ? oL + oR + oC : oL + oR;
-  double *out = wh + (long)i * NO * V + k;
+  double den = 0.0;
+  if (useL)
+    den += oL;
+  if (useR)
+    den += oR;
+  if (useC)
+    den += oC;
 #pragma unroll
   for (int a = 0; a < NO; a++) {
-    double num = wL[a] * oL + wR[a] * oR;
-    if (NO > 2)
+    double num = 0.0;
+    if (useL)
+      num += wL[a] * oL;
+    if (useR)
+      num += wR[a] * oR;
+    if (useC)
       num += wC[a] * oC;
-    out[(long)a * V] = num / den;
+    out[(long)a * so] = num / den;
   }
 }
 
-// Cells per block of the node kernels: NP = N^2 threads per cell.
-template <int NO> struct NodeBlock {
-  static constexpr int NP = NO * NO;
+// 1D: wh[i][a][k] for predictor cell i from ub rows i .. i + 2N - 2.
+template <int V, int NO>
+__global__ void k_weno1d_n(double *__restrict__ wh, const double *__restrict__ ub, int ncb,
+                           ConstsN<NO> C) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)ncb * V)
+    return;
+  const int k = idx % V;
+  const int i = idx / V;
+  weno_point_n<NO>(ub + (long)i * V + k, V, wh + (long)i * NO * V + k, V, i, ncb, 0, C);
+}
+
+// 2D x sweep (weno.cpp:93-104): ux[i][j][a][k] for i < nx + 2 over every
+// ub column j < ny + 2N; the columns within N of the edges leave out their
+// side stencils beyond the first N rows.
+template <int V, int NO>
+__global__ void k_weno2d_x_n(double *__restrict__ ux, const double *__restrict__ ub, int nxp,
+                             int nyb, ConstsN<NO> C) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)nxp * nyb * V)
+    return;
+  const int k = idx % V;
+  const long rest = idx / V;
+  const int j = rest % nyb, i = rest / nyb;
+  const int gap = (j < NO || j >= nyb - NO) ? NO : 0;
+  weno_point_n<NO>(ub + ((long)i * nyb + j) * V + k, (long)nyb * V,
+                   ux + ((long)i * nyb + j) * NO * V + k, V, i, nxp, gap, C);
+}
+
+// 2D y sweep (weno.cpp:106-121): wh[i][j][ii][jj][k] from ux rows j .. j + 2N - 2.
+template <int V, int NO>
+__global__ void k_weno2d_y_n(double *__restrict__ wh, const double *__restrict__ ux, int nxp,
+                             int nyp, ConstsN<NO> C) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)nxp * nyp * NO * V)
+    return;
+  const int k = idx % V;
+  long rest = idx / V;
+  const int ii = rest % NO;
+  rest /= NO;
+  const int j = rest % nyp, i = rest / nyp;
+  const int nyb = nyp + 2 * (NO - 1);
+  const int gap = (i == 0 || i == nxp - 1) ? 1 : 0;
+  weno_point_n<NO>(ux + (((long)i * nyb + j) * NO + ii) * V + k, (long)NO * V,
+                   wh + (((long)i * nyp + j) * NO * NO + ii * NO) * V + k, V, j, nyp, gap, C);
+}
+
+// Node kernels: one thread per space-time node, NP = N^(d+1) per cell,
+// g = t NS + s with s = i (1D) or i N + j (2D, x-node major), NS = N^d.
+template <int NO, int ND> struct NodeBlock {
+  static constexpr int NS = ND == 1 ? NO : NO * NO;
+  static constexpr int NP = NO * NS;
   static constexpr int CPB = 128 / NP;
   static constexpr int THREADS = CPB * NP;
 };
 
-// Picard predictor (dg1.cpp:58-114): q <- DG_U^-1 (W w + dt R(q)) with the
-// reference's initial guess q(t, s) = w(s), per-cell stopping rule |q1 - q0|
-// <= dg_tol (1 + |q0|) and iteration cap.  One thread per space-time node
-// g = t N + i of a cell; the cell's node values pass through shared memory.
-// status[c]: GPR_PRED_PICARD | iterations << 8 when converged; cells that do
-// not converge within the cap, or whose iterate turns NaN, get their last
+// Picard predictor (dg1.cpp:58-114, dg2.cpp:102-171): q <- DG_U^-1 (W w +
+// dt R(q)) with the reference's initial guess q(t, s) = w(s), per-cell
+// stopping rule |q1 - q0| <= dg_tol (1 + |q0|) and iteration cap; R = W (S -
+// B dq/dx [- B dq/dy]) - W_t [W_j] DG_DER F_x / dx [- W_t W_i DG_DER F_y / dy].
+// The cell's node values pass through shared memory.  status[c]:
+// GPR_PRED_PICARD | iterations << 8 when converged; cells that do not
+// converge within the cap, or whose iterate turns NaN, get their last
 // iterate and GPR_PRED_FAILED | iterations << 8 (there is no Newton pass for
 // N != 2; the reference leaves such rows unwritten or calls its
 // Newton-Krylov solver).
-template <class L, int NO>
-__global__ void __launch_bounds__(128) k_predictor1d_n(
+template <class L, int NO, int ND>
+__global__ void __launch_bounds__(128) k_predictor_n(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
-    const double *__restrict__ dt_dev, double idx, DevPar P, ConstsN<NO> C) {
+    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, ConstsN<NO> C) {
   constexpr int V = L::V;
-  using NB = NodeBlock<NO>;
-  constexpr int NP = NB::NP, CPB = NB::CPB;
+  using NB = NodeBlock<NO, ND>;
+  constexpr int NS = NB::NS, NP = NB::NP, CPB = NB::CPB;
   __shared__ double sq[CPB][NP][V];
   __shared__ int cflag[CPB];
   if (dt_dev)
@@ -340,11 +431,13 @@ __global__ void __launch_bounds__(128) k_predictor1d_n(
   const long c = (long)blockIdx.x * CPB + lc;
   const bool valid = in_block && c < ncb;
   const bool active = valid && (mask == nullptr || mask[c]);
-  const int t = g / NO, i = g % NO;
+  const int t = g / NS, sidx = g % NS;
+  const int i = ND == 1 ? sidx : sidx / NO, j = ND == 1 ? 0 : sidx % NO;
   const long cc = valid ? c : 0;  // lanes without a cell read cell 0's data
   double w[V], Ww[V], q[V], r[V], qn[V];
-  const double *wc = wh + (cc * NO + i) * V;
-  const double f = C.endv[0][t] * C.w[i];
+  const double *wc = wh + (cc * NS + (in_block ? sidx : 0)) * V;
+  const double ws = ND == 1 ? C.w[i] : C.w[i] * C.w[j];
+  const double f = C.endv[0][t] * ws;
 #pragma unroll
   for (int k = 0; k < V; k++) {
     w[k] = wc[k];
@@ -353,13 +446,16 @@ __global__ void __launch_bounds__(128) k_predictor1d_n(
   }
   bool done = !active, nan_seen = false;
   int iters = 0;
-  const double wn = C.w[t] * C.w[i];
+  const double wn = C.w[t] * ws;
+  // the partner node of this one with the x (y) index replaced by m
+  auto nx_of = [&](int m) { return ND == 1 ? t * NS + m : t * NS + m * NO + j; };
+  auto ny_of = [&](int m) { return t * NS + i * NO + m; };
   for (int it = 0; it < C.dg_it; it++) {
     if (!__syncthreads_or(!done))
       break;
     Prim<L::THERMAL> s;
     prim<L::THERMAL>(q, P, s);
-    // W (S - B dq/dx) with the node weight in the source's factors
+    // W (S - B dq/dx [- B dq/dy]) with the node weight in the source's factors
     source<L::THERMAL, V>(q, s, P, r, wn);
     if (in_block) {
 #pragma unroll
@@ -367,42 +463,50 @@ __global__ void __launch_bounds__(128) k_predictor1d_n(
         sq[lc][g][k] = q[k];
     }
     __syncthreads();
-    {
+#pragma unroll
+    for (int dir = 0; dir < ND; dir++) {
+      const int e = dir == 0 ? i : j;
+      const double h = dir == 0 ? idx : idy;
       double dq[V];
 #pragma unroll
       for (int k = 0; k < V; k++) {
         double a = 0.0;
 #pragma unroll
         for (int m = 0; m < NO; m++)
-          a += C.derv[i][m] * (in_block ? sq[lc][t * NO + m][k] : 0.0);
-        dq[k] = a * idx * wn;
+          a += C.derv[e][m] * (in_block ? sq[lc][dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
+        dq[k] = a * h * wn;
       }
       double bd[V];
-      bdot<V, L::LSET>(s.v, dq, 0, bd);
+      bdot<V, L::LSET>(s.v, dq, dir, bd);
 #pragma unroll
       for (int k = 0; k < V; k++)
         r[k] -= bd[k];
     }
-    __syncthreads();
-    // - W_t DG_DER(i, m) F(t, m) / dx
-    double F[V];
-    flux_set<L::THERMAL, V>(q, s, 0, P, F);
-    if (in_block) {
+    // - W_t [W_j] DG_DER(i, m) F_x(t, m, j) / dx [- W_t W_i DG_DER(j, m) F_y(t, i, m) / dy]
 #pragma unroll
-      for (int k = 0; k < V; k++)
-        sq[lc][g][k] = F[k];
-    }
-    __syncthreads();
-    const double wx = C.w[t] * idx;
+    for (int dir = 0; dir < ND; dir++) {
+      double F[V];
+      flux_set<L::THERMAL, V>(q, s, dir, P, F);
+      __syncthreads();
+      if (in_block) {
 #pragma unroll
-    for (int k = 0; k < V; k++) {
-      if (!flux_support<L::THERMAL>(k, 0))
-        continue;
-      double a = 0.0;
+        for (int k = 0; k < V; k++)
+          sq[lc][g][k] = F[k];
+      }
+      __syncthreads();
+      const int e = dir == 0 ? i : j;
+      const double wx = dir == 0 ? C.w[t] * (ND == 1 ? 1.0 : C.w[j]) * idx
+                                 : C.w[t] * C.w[i] * idy;
 #pragma unroll
-      for (int m = 0; m < NO; m++)
-        a += C.dgder[i][m] * (in_block ? sq[lc][t * NO + m][k] : 0.0);
-      r[k] -= wx * a;
+      for (int k = 0; k < V; k++) {
+        if (!flux_support<L::THERMAL>(k, dir))
+          continue;
+        double a = 0.0;
+#pragma unroll
+        for (int m = 0; m < NO; m++)
+          a += C.dgder[e][m] * (in_block ? sq[lc][dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
+        r[k] -= wx * a;
+      }
     }
 #pragma unroll
     for (int k = 0; k < V; k++)
@@ -416,14 +520,14 @@ __global__ void __launch_bounds__(128) k_predictor1d_n(
     if (in_block && g == 0)
       cflag[lc] = 0;
     __syncthreads();
-    // q_new(t, i) = sum_m DG_MATinv[t][m] r(m, i) / W_i
-    const double iw = 1.0 / C.w[i];
+    // q_new(t, s) = sum_m DG_MATinv[t][m] r(m, s) / W_s
+    const double iw = 1.0 / ws;
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double a = 0.0;
 #pragma unroll
       for (int m = 0; m < NO; m++)
-        a += C.dgmatinv[t][m] * (in_block ? sq[lc][m * NO + i][k] : 0.0);
+        a += C.dgmatinv[t][m] * (in_block ? sq[lc][m * NS + sidx][k] : 0.0);
       qn[k] = a * iw;
     }
     bool big = false, hasnan = false;
@@ -471,73 +575,104 @@ __global__ void __launch_bounds__(128) k_predictor1d_n(
     status[c] = GPR_PRED_PICARD;
 }
 
-// 1D face terms (interfs1, fv.cpp:111-160; D_RUS and Bint, fluxes.cpp:9-75):
-// one thread per (face, time node t); face f lies between predictor cells f
-// and f + 1.  fb[f][t][0][V] = k (b + f) is subtracted from the left cell,
-// fb[f][t][1][V] = k (b - f) from the right one, k = W_t dt / (2 dx).
+// Interface terms of one face point (D_RUS and Bint, fluxes.cpp:9-75,
+// with NO path nodes): f = max(lambda_L, lambda_R) (qL - qR) + F(qL) + F(qR),
+// b = sum_n W_n B(qL + x_n dq) dq.
 template <class L, int NO>
-__global__ void __launch_bounds__(128) k_faces1d_n(
-    double *__restrict__ fb, const double *__restrict__ qh, long nface,
-    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    DevPar P, ConstsN<NO> C) {
+GPR_D void interface_point_n(const double *ql, const double *qr, int d, const DevPar &P,
+                             const ConstsN<NO> &C, double *f, double *b) {
   constexpr int V = L::V;
-  if (dt_dev)
-    dt = *dt_dev;
-  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long face = gt / NO;
-  const int t = gt % NO;
-  if (face >= nface)
-    return;
-  double *o = fb + ((face * NO + t) * 2) * V;
-  const bool active = mask == nullptr || (mask[face] && mask[face + 1]);
-  if (!active) {
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      o[k] = o[V + k] = 0.0;
-    return;
-  }
-  const double *ql_ = qh + (face * NO + t) * NO * V;
-  const double *qr_ = qh + ((face + 1) * NO + t) * NO * V;
-  double ql[V], qr[V], f[V], b[V], dq[V];
-#pragma unroll
-  for (int k = 0; k < V; k++) {
-    double a = 0.0, e = 0.0;
-#pragma unroll
-    for (int j = 0; j < NO; j++) {
-      a += C.endv[1][j] * ql_[j * V + k];
-      e += C.endv[0][j] * qr_[j * V + k];
-    }
-    ql[k] = a;
-    qr[k] = e;
-  }
   Prim<L::THERMAL> sl, sr;
   prim<L::THERMAL>(ql, P, sl);
   prim<L::THERMAL>(qr, P, sr);
-  const double m1 = max_abs_eigs<L::THERMAL>(ql, sl, 0, P);
-  const double m2 = max_abs_eigs<L::THERMAL>(qr, sr, 0, P);
+  const double m1 = max_abs_eigs<L::THERMAL>(ql, sl, d, P);
+  const double m2 = max_abs_eigs<L::THERMAL>(qr, sr, d, P);
   const double m = m1 > m2 ? m1 : m2;
+  double dq[V];
 #pragma unroll
   for (int k = 0; k < V; k++) {
     f[k] = m * (ql[k] - qr[k]);
     dq[k] = qr[k] - ql[k];
     b[k] = 0.0;
   }
-  flux_add<L::THERMAL, V>(ql, sl, 0, P, f);
-  flux_add<L::THERMAL, V>(qr, sr, 0, P, f);
-  // Bint: sum_n W_n B(qL + x_n dq) dq over the NO path nodes
+  flux_add<L::THERMAL, V>(ql, sl, d, P, f);
+  flux_add<L::THERMAL, V>(qr, sr, d, P, f);
 #pragma unroll
   for (int n = 0; n < NO; n++) {
     const double ir = 1.0 / (ql[0] + C.nodes[n] * dq[0]);
     double v[3] = {(ql[2] + C.nodes[n] * dq[2]) * ir, (ql[3] + C.nodes[n] * dq[3]) * ir,
                    (ql[4] + C.nodes[n] * dq[4]) * ir};
     double bd[V];
-    bdot<V, L::LSET>(v, dq, 0, bd);
+    bdot<V, L::LSET>(v, dq, d, bd);
 #pragma unroll
     for (int k = 5; k < V; k++)
       if (k < 14 || k >= V - L::LSET)
         b[k] += C.w[n] * bd[k];
   }
-  const double kk = dt * C.w[t] / (2.0 * dx);
+}
+
+// Face terms (interfs1 / interfs2, fv.cpp:111-279): one thread per (face,
+// face point p) of direction dir; 1D: face f between predictor cells f and
+// f + 1, p = t; 2D: faces (i, j) of the (nx + 1) x (ny + 1) face grid between
+// predictor cells (i, j) and (i + 1, j) (dir 0) or (i, j + 1) (dir 1), p = t
+// N + s over time node t and transverse node s.  fb[face][p][0][V] = k (b +
+// f) is subtracted from the left cell, fb[face][p][1][V] = k (b - f) from the
+// right one, k = W_t [W_s] dt / (2 dx_dir).
+template <class L, int NO, int ND>
+__global__ void __launch_bounds__(128) k_faces_n(
+    double *__restrict__ fb, const double *__restrict__ qh, int nx, int ny, int dir,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    double dy, DevPar P, ConstsN<NO> C) {
+  constexpr int V = L::V;
+  constexpr int NQ = ND == 1 ? NO : NO * NO;  // points per face
+  constexpr int NS = ND == 1 ? NO : NO * NO;
+  if (dt_dev)
+    dt = *dt_dev;
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long face = gt / NQ;
+  const int p = gt % NQ;
+  const long nf = ND == 1 ? (long)nx + 1 : (long)(nx + 1) * (ny + 1);
+  if (face >= nf)
+    return;
+  const int t = ND == 1 ? p : p / NO, sq = ND == 1 ? 0 : p % NO;
+  long cb, cn;
+  bool geo = true;
+  if (ND == 1) {
+    cb = face;
+    cn = face + 1;
+  } else {
+    const int i = face / (ny + 1), j = face % (ny + 1);
+    cb = (long)i * (ny + 2) + j;
+    cn = dir == 0 ? cb + (ny + 2) : cb + 1;
+    geo = dir == 0 ? (j > 0) : (i > 0);
+  }
+  double *o = fb + ((face * NQ + p) * 2) * V;
+  const bool active = geo && (mask == nullptr || (mask[cb] && mask[cn]));
+  if (!active) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      o[k] = o[V + k] = 0.0;
+    return;
+  }
+  // endpoint extrapolation (evaluations.cpp:20-35): 1D nodes m; 2D dir 0
+  // nodes (m, s), dir 1 nodes (s, m)
+  const double *ql_ = qh + (cb * NO + t) * NS * V;
+  const double *qr_ = qh + (cn * NO + t) * NS * V;
+  double ql[V], qr[V], f[V], b[V];
+#pragma unroll
+  for (int k = 0; k < V; k++) {
+    double a = 0.0, e = 0.0;
+#pragma unroll
+    for (int m = 0; m < NO; m++) {
+      const int node = ND == 1 ? m : (dir == 0 ? m * NO + sq : sq * NO + m);
+      a += C.endv[1][m] * ql_[node * V + k];
+      e += C.endv[0][m] * qr_[node * V + k];
+    }
+    ql[k] = a;
+    qr[k] = e;
+  }
+  interface_point_n<L, NO>(ql, qr, dir, P, C, f, b);
+  const double kk = dt * C.w[t] * (ND == 1 ? 1.0 : C.w[sq]) / (2.0 * (dir == 0 ? dx : dy));
 #pragma unroll
   for (int k = 0; k < V; k++) {
     o[k] = kk * (b[k] + f[k]);
@@ -545,30 +680,38 @@ __global__ void __launch_bounds__(128) k_faces1d_n(
   }
 }
 
-// The 1D FV update of interior cell c (predictor cell c + 1): the volume
-// term (centers1, fv.cpp:11-58) over its NO x NO space-time nodes, one
-// thread per node, summed through shared memory, then the face terms of its
-// left face c (right part) and right face c + 1 (left part).
-template <class L, int NO>
-__global__ void __launch_bounds__(128) k_cells1d_n(
-    double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fb, int nx,
-    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    DevPar P, ConstsN<NO> C) {
+// The FV update of each interior cell (centers1/2 and the interface sums,
+// fv.cpp:11-109, 143-146, 253-276): the volume term over its space-time
+// nodes, one thread per node, summed through shared memory in node order,
+// then the face terms of its faces (1D: left face c (right part), right
+// face c + 1 (left part); 2D: the x faces (ci + 1, cj + 1) and (ci, cj + 1),
+// the y faces (ci + 1, cj + 1) and (ci + 1, cj)), each summed over its points.
+template <class L, int NO, int ND>
+__global__ void __launch_bounds__(128) k_cells_n(
+    double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
+    const double *__restrict__ fby, int nx, int ny, const uint8_t *__restrict__ mask, double dt,
+    const double *__restrict__ dt_dev, double dx, double dy, DevPar P, ConstsN<NO> C) {
   constexpr int V = L::V;
-  using NB = NodeBlock<NO>;
-  constexpr int NP = NB::NP, CPB = NB::CPB;
+  using NB = NodeBlock<NO, ND>;
+  constexpr int NS = NB::NS, NP = NB::NP, CPB = NB::CPB;
+  constexpr int NQ = NS;  // points per face
   __shared__ double sq[CPB][NP][V];
   if (dt_dev)
     dt = *dt_dev;
   const int lc = threadIdx.x / NP;
   const int g = threadIdx.x % NP;
   const bool in_block = threadIdx.x < NB::THREADS;
+  const long ncell = ND == 1 ? nx : (long)nx * ny;
   const long c = (long)blockIdx.x * CPB + lc;
-  const bool valid = in_block && c < nx;
-  const long cb = (valid ? c : 0) + 1;  // lanes without a cell read cell 0's nodes
+  const bool valid = in_block && c < ncell;
+  const long cc = valid ? c : 0;  // lanes without a cell read cell 0's nodes
+  const long ci = ND == 1 ? cc : cc / ny;
+  const int cj = ND == 1 ? 0 : (int)(cc % ny);
+  const long cb = ND == 1 ? ci + 1 : (ci + 1) * (ny + 2) + (cj + 1);
   const bool active = valid && (mask == nullptr || mask[cb]);
-  const int t = g / NO, i = g % NO;
-  const double idx = 1.0 / dx;
+  const int t = g / NS, sidx = g % NS;
+  const int i = ND == 1 ? sidx : sidx / NO, j = ND == 1 ? 0 : sidx % NO;
+  const double idx = 1.0 / dx, idy = 1.0 / dy;
   double q[V], acc[V];
   const double *qc = qh + (cb * NP + (in_block ? g : 0)) * V;
 #pragma unroll
@@ -582,20 +725,26 @@ __global__ void __launch_bounds__(128) k_cells1d_n(
   __syncthreads();
   Prim<L::THERMAL> s;
   prim<L::THERMAL>(q, P, s);
-  const double wn = dt * C.w[t] * C.w[i];
+  const double wn = dt * C.w[t] * C.w[i] * (ND == 1 ? 1.0 : C.w[j]);
   source<L::THERMAL, V>(q, s, P, acc, wn);
-  {
+#pragma unroll
+  for (int dir = 0; dir < ND; dir++) {
+    const int e = dir == 0 ? i : j;
+    const double h = dir == 0 ? idx : idy;
     double dq[V];
 #pragma unroll
     for (int k = 0; k < V; k++) {
       double a = 0.0;
 #pragma unroll
-      for (int m = 0; m < NO; m++)
-        a += C.derv[i][m] * (in_block ? sq[lc][t * NO + m][k] : 0.0);
-      dq[k] = a * idx * wn;
+      for (int m = 0; m < NO; m++) {
+        const int node = ND == 1 ? t * NS + m
+                                 : (dir == 0 ? t * NS + m * NO + j : t * NS + i * NO + m);
+        a += C.derv[e][m] * (in_block ? sq[lc][node][k] : 0.0);
+      }
+      dq[k] = a * h * wn;
     }
     double bd[V];
-    bdot<V, L::LSET>(s.v, dq, 0, bd);
+    bdot<V, L::LSET>(s.v, dq, dir, bd);
 #pragma unroll
     for (int k = 0; k < V; k++)
       acc[k] -= bd[k];
@@ -609,26 +758,45 @@ __global__ void __launch_bounds__(128) k_cells1d_n(
   __syncthreads();
   if (!active)
     return;
-  // lane g sums variables g, g + NP, ... over the cell's nodes in node order
-  const double *fl = fb + (long)c * NO * 2 * V;        // left face c: right part
-  const double *fr = fb + (long)(c + 1) * NO * 2 * V;  // right face c + 1: left part
-  const bool okl = mask == nullptr || (mask[cb - 1] && mask[cb]);
-  const bool okr = mask == nullptr || (mask[cb] && mask[cb + 1]);
   double *uc = u + c * V;
-  for (int k = g; k < V; k += NP) {
-    double x = 0.0;
+  if (ND == 1) {
+    const double *fl = fbx + (long)c * NQ * 2 * V;        // left face c: right part
+    const double *fr = fbx + (long)(c + 1) * NQ * 2 * V;  // right face c + 1: left part
+    const bool okl = mask == nullptr || (mask[cb - 1] && mask[cb]);
+    const bool okr = mask == nullptr || (mask[cb] && mask[cb + 1]);
+    for (int k = g; k < V; k += NP) {
+      double x = 0.0;
 #pragma unroll
-    for (int n = 0; n < NP; n++)
-      x += sq[lc][n][k];
-    x += uc[k];
+      for (int n = 0; n < NP; n++)
+        x += sq[lc][n][k];
+      x += uc[k];
 #pragma unroll
-    for (int tt = 0; tt < NO; tt++) {
-      if (okr)
-        x -= fr[tt * 2 * V + k];
-      if (okl)
-        x -= fl[tt * 2 * V + V + k];
+      for (int p = 0; p < NQ; p++) {
+        if (okr)
+          x -= fr[p * 2 * V + k];
+        if (okl)
+          x -= fl[p * 2 * V + V + k];
+      }
+      uc[k] = x;
     }
-    uc[k] = x;
+  } else {
+    const long fxl = (ci + 1) * (ny + 1) + (cj + 1), fxr = ci * (ny + 1) + (cj + 1);
+    const long fyl = (ci + 1) * (ny + 1) + (cj + 1), fyr = (ci + 1) * (ny + 1) + cj;
+    for (int k = g; k < V; k += NP) {
+      double x = 0.0;
+#pragma unroll
+      for (int n = 0; n < NP; n++)
+        x += sq[lc][n][k];
+      x += uc[k];
+#pragma unroll
+      for (int p = 0; p < NQ; p++) {
+        x -= fbx[(fxl * NQ + p) * 2 * V + k];
+        x -= fbx[(fxr * NQ + p) * 2 * V + V + k];
+        x -= fby[(fyl * NQ + p) * 2 * V + k];
+        x -= fby[(fyr * NQ + p) * 2 * V + V + k];
+      }
+      uc[k] = x;
+    }
   }
 }
 
