@@ -974,6 +974,20 @@ def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
     f1.record(stream)
     torch.cuda.synchronize()
     fill_ms = f0.elapsed_time(f1) / 3
+    # the re-distancing alone (FP64 sweeps), on the current level set, and
+    # its largest difference from the oracle's marcher there
+    col = u.view(-1, 15)[:, 14].contiguous()
+    dd = ghost.distance(col, dX, nX)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    for _ in range(3):
+        dd = ghost.distance(col, dX, nX)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    redist_ms = f0.elapsed_time(f1) / 3
+    redist_diff = float(np.max(np.abs(
+        dd.cpu().numpy() - Oracle(N=2, thermal=False, lset=1).distance(
+            col.cpu().numpy(), dX, np.asarray(nX, np.int32)))))
     # end to end with host buffers: H2D of the state, one step, D2H, per step
     host = torch.empty(ncell * 15, dtype=torch.float64, pin_memory=True)
     host.copy_(u.cpu())
@@ -992,6 +1006,8 @@ def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
            "steps": steps, "ms_per_step": ms / steps,
            "value": ncell * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
            "fill_ms": fill_ms, "fill_share": fill_ms / (ms / steps),
+           "redistance_ms": redist_ms, "redistance_share": redist_ms / (ms / steps),
+           "redistance_max_abs_diff_vs_oracle": redist_diff,
            "e2e": {"value": ncell * steps / (e2e_ms * 1e-3) / 1e6, "unit": UNIT,
                    "h2d_bytes_per_step": ncell * 15 * 8, "d2h_bytes_per_step": ncell * 15 * 8},
            "sim_time": float(clk[0]), "sim_steps": int(clk[4]), "fill_status": status}

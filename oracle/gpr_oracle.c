@@ -2984,7 +2984,12 @@ static int fmm_pop(fmm_t *m) {
 /* updatePointOrderOne + solveQuadratic (distance_marcher.cpp:5-28,72-88):
  * per axis the frozen neighbour of least |distance|, then the upwind
  * quadratic; the root is chosen by the sign of phi; 0 when it has no real
- * root. */
+ * root.  The reference builds with -O3 -march=native (CMakeLists.txt:14),
+ * where gcc fuses b -= idx2 2 value, c += idx2 value^2 and b^2 - 4ac into
+ * fused multiply-adds; the explicit fma() calls below are that build's
+ * roundings (its distances reproduced bit for bit on every test level set),
+ * on any host and under any contraction setting.  The quadratic loses ~17
+ * bits to cancellation, so these roundings show at ~1e-12. */
 static double fmm_point(const fmm_t *m, int i) {
   double a = 0, b = 0, c = 0;
   for (int dim = 0; dim < m->ndim; dim++) {
@@ -2996,12 +3001,12 @@ static double fmm_point(const fmm_t *m, int i) {
     }
     if (value < DBL_MAX) {
       a += m->idx2[dim];
-      b -= m->idx2[dim] * 2 * value;
-      c += m->idx2[dim] * (value * value);
+      b = fma(-(m->idx2[dim] * 2), value, b);
+      c = fma(m->idx2[dim], value * value, c);
     }
   }
   c -= 1;
-  double det = b * b - 4 * a * c;
+  double det = fma(b, b, -(4 * a * c));
   if (!(det > 0))
     return 0;
   double r0 = (-b + sqrt(det)) / 2.0 / a;

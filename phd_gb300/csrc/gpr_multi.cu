@@ -173,6 +173,9 @@ bool grid_ok(const int32_t *nX, int nd) {
 // shock-bubble step), 1024 no faster.
 constexpr int kFmmSweeps = 256;
 
+// Width of the band of FP32 estimates one sweep updates, in grid spacings.
+constexpr double kFmmDelta = 1.0;
+
 // Round budget: information crosses at least one tile per round, and the
 // global Jacobi needs about as many sweeps as the longest marching path in
 // cells (678 at 800 x 400); twice the larger of the two, the second half
@@ -187,7 +190,7 @@ int fmm_rounds(const Grid &g) {
 // Scratch of one fill (offsets in doubles, 256-byte aligned pieces).
 struct FillLayout {
   long o_d, o_phim, o_dphi, o_star, o_plan, o_fz, o_im0, o_im1, o_lastw, o_pidx, o_dep,
-      o_level, o_cnt, o_flags, o_tflag, o_lastg, o_dff, total;
+      o_level, o_cnt, o_flags, o_tflag, o_lastg, total;
 };
 
 int fmm_tiles(const Grid &g) {
@@ -217,7 +220,6 @@ FillLayout fill_layout(const Grid &g) {
   L.o_flags = cv.take(dbl(fmm_rounds(g) * 4L));
   L.o_tflag = cv.take(dbl((long)fmm_rounds(g) * fmm_tiles(g) * 4L));
   L.o_lastg = cv.take(dbl(n * 4));
-  L.o_dff = cv.take(dbl(n * (long)sizeof(Ff)));
   L.total = cv.o;
   return L;
 }
@@ -238,22 +240,22 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
   cudaMemsetAsync(flags, 0, R * sizeof(int), st);
   cudaMemsetAsync(tflag, 0, (size_t)R * fmm_tiles(g) * sizeof(int), st);
   cudaMemsetAsync(lastg, 0xff, g.ncell * sizeof(int), st);
-  Ff *dff = at<Ff>(scr, L.o_dff);
-  k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, dff, fz, g, cnt, clk);
-  FmmConst K = fmm_const(g.dx, g.dy);
+  k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, fz, g, cnt, clk);
+  const double hmin = g.nd == 2 && g.dy < g.dx ? g.dy : g.dx;
+  FmmConst K = fmm_const(g.dx, g.nd == 2 ? g.dy : g.dx, kFmmDelta * hmin);
   if (g.nd == 2) {
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)
-      k_fmm_round<2><<<nb, FMM_THREADS, 0, st>>>(dff, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<2><<<nb, FMM_THREADS, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)
-      k_fmm_round<1><<<nb, FMM_THREADS, 0, st>>>(dff, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<1><<<nb, FMM_THREADS, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   }
-  k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, dff, fz, u, g.ncell, cnt, flags,
-                                                          R - 1, err, clk);
+  k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, u, g.ncell, cnt, flags, R - 1, err,
+                                                          clk);
   return cuda_rc();
 }
 

@@ -16,14 +16,13 @@
 //
 // The reference runs every piece as a sequential sweep over the grid.  Here
 // each is a data-parallel kernel whose result equals the sequential sweep:
-//   * the fast marching order is replaced by tiled Jacobi iterations of the
-//     same causal upwind update, whose fixed point is what the marcher
-//     computes (band neighbours always enter a point's quadratic, the others
-//     only while their distance is below the point's estimate, as the
-//     marcher's heap order makes it); the band is computed in FP64 with the
-//     marcher's roundings, the rest in double-float arithmetic with the
-//     quadratic's root written without cancellation (the marcher's own
-//     formula carries ~3e-13 relative noise per update);
+//   * the fast marching order is replaced by tiled sweeps of the same
+//     causal upwind update, whose fixed point is what the marcher computes
+//     (band neighbours always enter a point's quadratic, the others only
+//     while their distance is below the point's estimate, as the marcher's
+//     heap order makes it), in FP64 with the marcher's quadratic and
+//     roundings; FP32 estimates order the sweeps' work (Dial's buckets
+//     within a tile) and never enter a result;
 //   * a boundary cell reads the right-hand state of the interface from a
 //     cell that an earlier cell of the (i, j) sweep may have filled; those
 //     reads are resolved to the last earlier writer and solved level by
@@ -65,15 +64,11 @@ GPR_D double dvd(double a, double b) { return __ddiv_rn(a, b); }
 // is zero or changes sign across a face, in FP64 with the marcher's
 // roundings.  Others start unknown (+inf).  phi[c * ps] is the level set of
 // cell c.  fz: bit 0 frozen (band), bit 1 the marcher would take the
-// positive root for this cell (phi > DBL_EPSILON).  dff is the double-float
-// working copy of d.
-struct Ff {
-  float h, l;  // value h + l, |l| <= ulp(h) / 2
-};
-
+// positive root for this cell (phi > DBL_EPSILON), bit 2 the point waits
+// for an update (set by the sweeps).
 __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__restrict__ d,
-                           Ff *__restrict__ dff, uint8_t *__restrict__ fz, Grid g,
-                           int *__restrict__ anyfrozen, const double *__restrict__ clk) {
+                           uint8_t *__restrict__ fz, Grid g, int *__restrict__ anyfrozen,
+                           const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
   long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -117,97 +112,85 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
     }
   }
   d[c] = x;
-  float xh = (float)x;
-  dff[c] = Ff{xh, frozen ? (float)(x - (double)xh) : 0.0f};
   fz[c] = (frozen ? 1 : 0) | pos;
   if (frozen)
     atomicOr(anyfrozen, 1);
 }
 
-// ---- double-float arithmetic (Dekker, "A floating-point technique for
-// extending the available precision", Numer. Math. 18, 1971; Knuth TAOCP
-// vol. 2, 4.2.2): a value is an unevaluated sum of two floats, about 48
-// significant bits, on the FP32 pipe.  The _rn intrinsics keep the compiler
-// from contracting the error-free transformations.
-GPR_D Ff ff_two_sum(float a, float b) {
-  float s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return Ff{s, e};
-}
-GPR_D Ff ff_fast_two_sum(float a, float b) {  // |a| >= |b|
-  float s = __fadd_rn(a, b);
-  return Ff{s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-GPR_D Ff ff_add(Ff a, Ff b) {
-  Ff s = ff_two_sum(a.h, b.h), t = ff_two_sum(a.l, b.l);
-  s = ff_fast_two_sum(s.h, __fadd_rn(s.l, t.h));
-  return ff_fast_two_sum(s.h, __fadd_rn(s.l, t.l));
-}
-GPR_D Ff ff_neg(Ff a) { return Ff{-a.h, -a.l}; }
-GPR_D Ff ff_sub(Ff a, Ff b) { return ff_add(a, ff_neg(b)); }
-GPR_D Ff ff_mul(Ff a, Ff b) {
-  float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  return ff_fast_two_sum(p, e);
-}
-GPR_D Ff ff_sqrt(Ff a) {  // a > 0
-  float s = __fsqrt_rn(a.h);
-  float p = __fmul_rn(s, s);
-  float pe = __fmaf_rn(s, s, -p);
-  float r = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(a.h, p), pe), a.l), __fmul_rn(2.0f, s));
-  return ff_fast_two_sum(s, r);
-}
-GPR_D bool ff_lt(Ff a, Ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
-GPR_D Ff ff_abs(Ff a) { return (a.h < 0.0f || (a.h == 0.0f && a.l < 0.0f)) ? ff_neg(a) : a; }
-GPR_D bool ff_eq(Ff a, Ff b) { return a.h == b.h && a.l == b.l; }
-GPR_D bool ff_inf(Ff a) { return isinf(a.h); }
-
-inline Ff ff_of(double x) {
-  float h = (float)x;
-  return Ff{h, (float)(x - (double)h)};
-}
-
-// Grid constants of the update: spacings, and for the two-axis root
-// x = al u + be w +- sqrt(ga - ab (u - w)^2) with ix = 1/dx^2, iy = 1/dy^2,
-// al = ix / (ix + iy), be = iy / (ix + iy), ga = 1 / (ix + iy), ab = al be.
-// That is the root of the marcher's quadratic (distance_marcher.cpp:5-28)
-// written without its cancellation (b^2 - 4ac loses ~17 bits there).
+// Grid constants of the update: 1 / dx^2, 1 / dy^2 for the marcher's FP64
+// quadratic; for the FP32 estimate the root of the same quadratic written
+// without cancellation, x = al u + be w +- sqrt(ga - ab (u - w)^2) with
+// ix = 1/dx^2, iy = 1/dy^2, al = ix / (ix + iy), be = iy / (ix + iy),
+// ga = 1 / (ix + iy), ab = al be; delta is the width of the band of
+// estimates a sweep updates (below).
 struct FmmConst {
-  Ff h[2], al, be, ga, ab;
+  double idx2[2];
+  float h[2], al, be, ga, ab, delta;
 };
 
-inline FmmConst fmm_const(double dx, double dy) {
+inline FmmConst fmm_const(double dx, double dy, double delta) {
   FmmConst K;
-  double ix = 1.0 / dx / dx, iy = 1.0 / dy / dy, S = ix + iy;
-  K.h[0] = ff_of(dx);
-  K.h[1] = ff_of(dy);
-  K.al = ff_of(ix / S);
-  K.be = ff_of(iy / S);
-  K.ga = ff_of(1.0 / S);
-  K.ab = ff_of(ix / S * (iy / S));
+  K.idx2[0] = 1.0 / dx / dx;  // the marcher's idx2 (distance_marcher.cpp)
+  K.idx2[1] = 1.0 / dy / dy;
+  double ix = K.idx2[0], iy = K.idx2[1], S = ix + iy;
+  K.h[0] = (float)dx;
+  K.h[1] = (float)dy;
+  K.al = (float)(ix / S);
+  K.be = (float)(iy / S);
+  K.ga = (float)(1.0 / S);
+  K.ab = (float)(ix / S * (iy / S));
+  K.delta = (float)delta;
   return K;
 }
 
-// Root of the marcher's quadratic for the entered axes (use), positive
-// root where pos; false without a real root.
-GPR_D bool fmm_root(const Ff v[2], const bool use[2], const FmmConst &K, bool pos, Ff &x) {
-  if (use[0] && use[1]) {
-    Ff df = ff_sub(v[0], v[1]);
-    Ff D = ff_sub(K.ga, ff_mul(K.ab, ff_mul(df, df)));
-    if (!(D.h > 0.0f))
+// updatePointOrderOne + solveQuadratic (distance_marcher.cpp:5-28, 72-88)
+// for the entered axes (use): a = sum idx2, b = -sum 2 idx2 v, c = sum idx2
+// v^2 - 1, root (-b +- sqrt(b^2 - 4ac)) / 2 / a by the sign of phi, in FP64
+// with the marcher's operation order and the fused multiply-adds of the
+// reference's -O3 -march=native build (CMakeLists.txt:14): b and c
+// accumulate by fma, det = fma(b, b, -(4 a c)); every other operation is
+// rounded on its own.  The marcher leaves a point unchanged when the
+// quadratic has no real root (its 0 return); so does a false return here.
+struct Root64 {
+  const FmmConst &K;
+  int nd;
+  GPR_D bool operator()(const double v[2], const bool use[2], bool pos, double &x) const {
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int dim = 0; dim < nd; dim++)
+      if (use[dim]) {
+        a = add(a, K.idx2[dim]);
+        b = __fma_rn(-mul(K.idx2[dim], 2.0), v[dim], b);
+        c = __fma_rn(K.idx2[dim], mul(v[dim], v[dim]), c);
+      }
+    c = sub(c, 1.0);
+    const double det = __fma_rn(b, b, -mul(mul(4.0, a), c));
+    if (!(det > 0.0))
       return false;
-    Ff sq = ff_sqrt(D);
-    Ff m = ff_add(ff_mul(K.al, v[0]), ff_mul(K.be, v[1]));
-    x = pos ? ff_add(m, sq) : ff_sub(m, sq);
+    const double sq = __dsqrt_rn(det);
+    x = dvd(dvd(pos ? add(-b, sq) : sub(-b, sq), 2.0), a);
+    return x != 0.0;
+  }
+};
+
+// The FP32 estimate of the same update (cancellation-free root), used only
+// to order the sweeps' work.
+struct Root32 {
+  const FmmConst &K;
+  GPR_D bool operator()(const float v[2], const bool use[2], bool pos, float &x) const {
+    if (use[0] && use[1]) {
+      const float df = v[0] - v[1];
+      const float D = K.ga - K.ab * df * df;
+      if (!(D > 0.0f))
+        return false;
+      const float sq = sqrtf(D), m = K.al * v[0] + K.be * v[1];
+      x = pos ? m + sq : m - sq;
+      return true;
+    }
+    const int k = use[0] ? 0 : 1;
+    x = pos ? v[k] + K.h[k] : v[k] - K.h[k];
     return true;
   }
-  int k = use[0] ? 0 : 1;
-  x = pos ? ff_add(v[k], K.h[k]) : ff_sub(v[k], K.h[k]);
-  return true;
-}
+};
 
 // Update of one unfrozen point from its neighbours' current values
 // (signed; +inf unknown), reproducing what the marcher's heap order makes
@@ -221,51 +204,52 @@ GPR_D bool fmm_root(const Ff v[2], const bool use[2], const FmmConst &K, bool po
 // root exceeds its |d| in exact arithmetic); where rounding says otherwise
 // (a noise-level tie) it is left out, so that no two points feed each other
 // and the iteration cannot cycle.  Returns `old` when nothing is known.
-GPR_D Ff fmm_update(const Ff nb[2][2], const bool band[2][2], bool pos, const FmmConst &K,
-                    int nd, Ff old) {
-  const Ff INF = Ff{INFINITY, 0.0f};
-  Ff v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
+template <class T, class RootF>
+GPR_D T fmm_update(const T nb[2][2], const bool band[2][2], bool pos, int nd, T old,
+                   const RootF &root) {
+  const T INF = (T)INFINITY;
+  T v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
   bool use[2] = {false, false};
   for (int dim = 0; dim < nd; dim++)
     for (int s = 0; s < 2; s++) {
-      Ff x = nb[dim][s], ax = ff_abs(x);
+      const T x = nb[dim][s], ax = fabs(x);
       if (band[dim][s]) {
-        if (!use[dim] || ff_lt(ax, ff_abs(v[dim]))) {
+        if (!use[dim] || ax < fabs(v[dim])) {
           v[dim] = x;
           use[dim] = true;
         }
-      } else if (ff_lt(ax, ck[dim])) {
+      } else if (ax < ck[dim]) {
         ck[dim] = ax;
         cv[dim] = x;
       }
     }
-  Ff t = INF;
+  T t = INF;
   if (use[0] || use[1]) {
-    Ff r;
-    if (fmm_root(v, use, K, pos, r))
+    T r;
+    if (root(v, use, pos, r))
       t = r;
   }
-  bool done[2] = {ff_inf(ck[0]), nd < 2 || ff_inf(ck[1])};
+  bool done[2] = {isinf(ck[0]), nd < 2 || isinf(ck[1])};
   while (!done[0] || !done[1]) {
-    int a = done[0] ? 1 : (done[1] ? 0 : (ff_lt(ck[1], ck[0]) ? 1 : 0));
-    Ff key = ck[a];
-    if (!ff_lt(key, ff_abs(t)))
+    const int a = done[0] ? 1 : (done[1] ? 0 : (ck[1] < ck[0] ? 1 : 0));
+    const T key = ck[a];
+    if (!(key < fabs(t)))
       break;
-    bool both = !done[1 - a] && ff_eq(ck[1 - a], key);
-    Ff sv0 = v[0], sv1 = v[1];
-    bool su0 = use[0], su1 = use[1];
+    const bool both = !done[1 - a] && ck[1 - a] == key;
+    const T sv0 = v[0], sv1 = v[1];
+    const bool su0 = use[0], su1 = use[1];
     for (int q = 0; q < 2; q++) {
-      int dim = q == 0 ? a : 1 - a;
+      const int dim = q == 0 ? a : 1 - a;
       if (q == 1 && !both)
         break;
-      if (!use[dim] || ff_lt(ff_abs(cv[dim]), ff_abs(v[dim]))) {
+      if (!use[dim] || fabs(cv[dim]) < fabs(v[dim])) {
         v[dim] = cv[dim];
         use[dim] = true;
       }
       done[dim] = true;
     }
-    Ff t2;
-    if (!fmm_root(v, use, K, pos, t2) || !ff_lt(key, ff_abs(t2))) {
+    T t2;
+    if (!root(v, use, pos, t2) || !(key < fabs(t2))) {
       v[0] = sv0;
       v[1] = sv1;
       use[0] = su0;
@@ -274,31 +258,58 @@ GPR_D Ff fmm_update(const Ff nb[2][2], const bool band[2][2], bool pos, const Fm
     }
     t = t2;
   }
-  return ff_inf(t) ? old : t;
+  return isinf(t) ? old : t;
 }
 
-// One round of tiled Jacobi sweeps.  Each block loads its tile and a
-// one-cell halo into shared memory and runs up to FMM_K sweeps of the causal
-// update against that halo, then writes back.  Sweeps are numbered globally
-// (round * FMM_K + local sweep); lastg[c] holds the sweep of cell c's last
-// change.  Only a point next to a point that changed in the previous sweep
-// can change (or, in a round's first sweep, next to a halo point that
-// changed at all in the previous round), and each sweep gathers those into
-// a list first, so that whole warps run the updates.  A tile runs only if
-// it or a neighbouring tile changed in the previous round
-// (tflag[round][tile]); flags[round] records whether anything changed, and a
-// round after a round without change returns at once.  The sweeps run in
-// double-float arithmetic: GB300's FP64 pipe issues one warp instruction
-// per 64 cycles per SM partition, the FP32 pipe one per cycle, and the
-// sweeps make ~30 updates per cell.  2D tiles are 32 x 32 cells, 1D tiles
-// 1024; FMM_THREADS threads own 1024 / FMM_THREADS cells each.
+// The four neighbours of shared-memory point m (x neighbours m -+ o0, y
+// neighbours m -+ 1) and whether each is in the frozen band.
+template <class T, int ND>
+GPR_D void fmm_load_nb(const T *src, const uint8_t *sf, int m, int o0, T nb[2][2],
+                       bool bd[2][2]) {
+  nb[0][0] = src[m - o0];
+  nb[0][1] = src[m + o0];
+  bd[0][0] = sf[m - o0] & 1;
+  bd[0][1] = sf[m + o0] & 1;
+  if (ND == 2) {
+    nb[1][0] = src[m - 1];
+    nb[1][1] = src[m + 1];
+    bd[1][0] = sf[m - 1] & 1;
+    bd[1][1] = sf[m + 1] & 1;
+  } else {
+    nb[1][0] = nb[1][1] = (T)INFINITY;
+    bd[1][0] = bd[1][1] = false;
+  }
+}
+
+// One round of tiled sweeps of the causal update, in FP64.  Each block
+// loads its tile and a one-cell halo into shared memory and runs up to
+// `nsweeps` sweeps against that halo, then writes back.  A point waits for
+// an update (dirty) when a neighbour changed after its last update.  Each
+// sweep estimates the new value of every waiting point in FP32, takes the
+// least estimate m of the tile, and updates in FP64 (Jacobi: all reads
+// before all writes) only the waiting points whose estimate is within
+// delta of m; the others wait.  That is Dial's bucketed order of the
+// marcher (Tsitsiklis, "Efficient algorithms for globally optimal
+// trajectories", IEEE TAC 40, 1995) within a tile: a point is mostly
+// updated once its upwind neighbours have settled, instead of once per
+// improvement of each of them, which keeps the FP64 updates per point to a
+// few (GB300's FP64 pipe issues one warp instruction per 64 cycles per SM
+// partition).  The order changes only the work: the sweeps end when no
+// point waits, at the fixed point of the update, whatever the order.
+// lastg[c] is the round of cell c's last change; fz bit 2 carries a
+// waiting point into the next round.  A tile runs if it has waiting points
+// or a neighbouring tile changed in the previous round (tflag bit 1 / bit 0
+// of round - 1); flags[round] records whether anything changed or waits,
+// and a round after a round without either returns at once.  2D tiles are
+// 32 x 32 cells, 1D tiles 1024; FMM_THREADS threads own 1024 / FMM_THREADS
+// cells each.
 constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
 
 template <int ND>
-__global__ void __launch_bounds__(FMM_THREADS, 4)
-    k_fmm_round(Ff *__restrict__ dff, const uint8_t *__restrict__ fz, int *__restrict__ lastg,
+__global__ void __launch_bounds__(FMM_THREADS, 2)
+    k_fmm_round(double *__restrict__ d, uint8_t *__restrict__ fz, int *__restrict__ lastg,
                 Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
-                int FMM_K, int mono, const double *__restrict__ clk) {
+                int nsweeps, int mono, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
   if (round > 0 && flags[round - 1] == 0)
@@ -312,37 +323,41 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
   if (round > 0) {
     const int *prev = tflag + (long)(round - 1) * ntiles;
     int ti = ND == 2 ? t % ntx0 : t, tj = ND == 2 ? t / ntx0 : 0;
-    bool run = prev[t] || (ti > 0 && prev[t - 1]) || (ti < ntx0 - 1 && prev[t + 1]) ||
-               (ND == 2 && ((tj > 0 && prev[t - ntx0]) || (tj < nty0 - 1 && prev[t + ntx0])));
+    bool run = prev[t] != 0 || (ti > 0 && (prev[t - 1] & 1)) ||
+               (ti < ntx0 - 1 && (prev[t + 1] & 1)) ||
+               (ND == 2 && ((tj > 0 && (prev[t - ntx0] & 1)) ||
+                            (tj < nty0 - 1 && (prev[t + ntx0] & 1))));
     if (!run)
       return;
   }
-  __shared__ Ff sd[SX * SY];
-  __shared__ Ff nvs[NT];
+  __shared__ double sd[SX * SY];
+  __shared__ double nvs[NT];
+  __shared__ float s32[SX * SY];
   __shared__ uint8_t sf[SX * SY];
-  __shared__ int last[SX * SY];  // global sweep of the last change
+  __shared__ uint8_t hchg[SX * SY];  // halo point changed in the previous round
+  __shared__ uint8_t dirty[NT];
+  __shared__ uint8_t chg[NT];  // bit 0 changed this sweep, bit 1 this round
   __shared__ int16_t list[NT];
-  __shared__ int wcnt[NW], any[2], total;
+  __shared__ float wmin[NW];
+  __shared__ int wcnt[NW], total;
   const int bi = ND == 2 ? t % ntx0 : t, bj = ND == 2 ? t / ntx0 : 0;
   const int i0 = bi * TX, j0 = bj * TY;
   for (int e = threadIdx.x; e < SX * SY; e += FMM_THREADS) {
     int a = ND == 2 ? e / SY : e, b = ND == 2 ? e % SY : 0;
     int ii = i0 + a - 1, jj = ND == 2 ? j0 + b - 1 : 0;
-    Ff x = Ff{INFINITY, 0.0f};
-    uint8_t f = 0;
-    int lg = -2;
+    double x = INFINITY;
+    uint8_t f = 0, hc = 0;
     if (ii >= 0 && ii < g.nx && jj >= 0 && jj < g.ny) {
       long c = (long)ii * g.ny + jj;
-      x = dff[c];
+      x = d[c];
       f = fz[c];
-      lg = lastg[c];
+      hc = lastg[c] == round - 1;
     }
     sd[e] = x;
+    s32[e] = (float)x;
     sf[e] = f;
-    last[e] = lg;
+    hchg[e] = hc;
   }
-  if (threadIdx.x < 2)
-    any[threadIdx.x] = 0;
   auto smem_of = [&](int l) {
     return ND == 2 ? (l / TY + 1) * SY + (l % TY + 1) : l + 1;
   };
@@ -358,34 +373,71 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
     int a = ND == 2 ? m / SY : m, b = ND == 2 ? m % SY : 1;
     return a == 0 || a == SX - 1 || (ND == 2 && (b == 0 || b == SY - 1));
   };
+  const int o0 = ND == 2 ? SY : 1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __syncthreads();
   bool act[PER];
   for (int k = 0; k < PER; k++) {
-    int l = threadIdx.x + k * FMM_THREADS;
-    act[k] = inside_of(l) && !(sf[smem_of(l)] & 1);
+    const int l = threadIdx.x + k * FMM_THREADS, m = smem_of(l);
+    act[k] = inside_of(l) && !(sf[m] & 1);
+    bool dd = act[k] && (round == 0 || (sf[m] & 4));
+    if (act[k] && !dd) {
+      const int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
+      for (int q = 0; q < (ND == 2 ? 4 : 2); q++)
+        dd = dd || (is_halo(nbm[q]) && hchg[nbm[q]]);
+    }
+    dirty[l] = dd;
+    chg[l] = 0;
   }
-  const int o0 = ND == 2 ? SY : 1;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gs0 = round * FMM_K;
-  for (int it = 0; it < FMM_K; it++) {
-    const int gs = gs0 + it;
-    // 1. gather the points that can move this sweep
-    int mine = 0;
-    bool dirty[PER];
+  __syncthreads();
+  const Root32 r32{K};
+  const Root64 r64{K, ND};
+  for (int it = 0; it < nsweeps; it++) {
+    // 1. FP32 estimates of the waiting points and the tile's least estimate
+    float est[PER];  // |estimate|; -1 nothing known (drops out), -2 FP64 decides
+    float mymin = INFINITY;
+    bool anyd = false;
     for (int k = 0; k < PER; k++) {
-      int m = smem_of(threadIdx.x + k * FMM_THREADS);
-      bool dd = act[k] && gs == 0;
-      if (act[k] && gs > 0) {
-        int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
-        for (int q = 0; q < (ND == 2 ? 4 : 2); q++) {
-          int lq = last[nbm[q]];
-          // a halo point is stale for the whole round: any change of it in
-          // the previous round counts in the first sweep
-          dd = dd || lq == gs - 1 || (it == 0 && is_halo(nbm[q]) && lq >= gs0 - FMM_K);
-        }
+      const int l = threadIdx.x + k * FMM_THREADS;
+      est[k] = INFINITY;
+      if (!dirty[l])
+        continue;
+      anyd = true;
+      const int m = smem_of(l);
+      float nb[2][2];
+      bool bd[2][2];
+      fmm_load_nb<float, ND>(s32, sf, m, o0, nb, bd);
+      if (isinf(nb[0][0]) && isinf(nb[0][1]) && isinf(nb[1][0]) && isinf(nb[1][1])) {
+        est[k] = -1.0f;
+        continue;
       }
-      dirty[k] = dd;
-      mine += dd;
+      const float e = fmm_update<float>(nb, bd, (sf[m] & 2) != 0, ND, (float)INFINITY, r32);
+      if (isinf(e)) {
+        est[k] = -2.0f;
+      } else {
+        est[k] = fabsf(e);
+        mymin = fminf(mymin, est[k]);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      mymin = fminf(mymin, __shfl_xor_sync(0xffffffffu, mymin, o));
+    if (lane == 0)
+      wmin[wid] = mymin;
+    if (!__syncthreads_or(anyd))
+      break;
+    float mn = wmin[0];
+    for (int w = 1; w < NW; w++)
+      mn = fminf(mn, wmin[w]);
+    const float lim = mn + K.delta;
+    // 2. gather the points this sweep updates
+    bool sel[PER];
+    int mine = 0;
+    for (int k = 0; k < PER; k++) {
+      const int l = threadIdx.x + k * FMM_THREADS;
+      sel[k] = est[k] == -2.0f || (est[k] >= 0.0f && est[k] <= lim);
+      if (est[k] == -1.0f)
+        dirty[l] = 0;
+      mine += sel[k];
     }
     int incl = mine;  // inclusive warp scan
     for (int o = 1; o < 32; o <<= 1) {
@@ -401,76 +453,81 @@ __global__ void __launch_bounds__(FMM_THREADS, 4)
       base += wcnt[w];
     int pos = base + incl - mine;
     for (int k = 0; k < PER; k++)
-      if (dirty[k])
+      if (sel[k])
         list[pos++] = (int16_t)(threadIdx.x + k * FMM_THREADS);
     if (threadIdx.x == FMM_THREADS - 1)
       total = pos;
-    if (threadIdx.x == 0)
-      any[(it + 1) & 1] = 0;
     __syncthreads();
-    // 2. update them (Jacobi: read the neighbours, write after a barrier)
+    // 3. FP64 updates (Jacobi: read the neighbours, write after a barrier)
     const int n = total;
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
-      int m = smem_of(list[q]);
-      Ff nb[2][2];
+      const int m = smem_of(list[q]);
+      double nb[2][2];
       bool bd[2][2];
-      nb[0][0] = sd[m - o0];
-      nb[0][1] = sd[m + o0];
-      bd[0][0] = sf[m - o0] & 1;
-      bd[0][1] = sf[m + o0] & 1;
-      if (ND == 2) {
-        nb[1][0] = sd[m - 1];
-        nb[1][1] = sd[m + 1];
-        bd[1][0] = sf[m - 1] & 1;
-        bd[1][1] = sf[m + 1] & 1;
-      } else {
-        nb[1][0] = nb[1][1] = Ff{INFINITY, 0.0f};
-        bd[1][0] = bd[1][1] = false;
-      }
-      nvs[q] = fmm_update(nb, bd, (sf[m] & 2) != 0, K, ND, sd[m]);
+      fmm_load_nb<double, ND>(sd, sf, m, o0, nb, bd);
+      nvs[q] = fmm_update<double>(nb, bd, (sf[m] & 2) != 0, ND, sd[m], r64);
     }
     __syncthreads();
+    // 4. take the new values; from the second half of the round budget on,
+    // only a smaller |d| is taken, which guarantees termination
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
-      int m = smem_of(list[q]);
-      Ff old = sd[m], nv = nvs[q];
-      // from the second half of the round budget on, only a smaller |d| is
-      // taken, which guarantees termination
-      if (mono ? ff_lt(ff_abs(nv), ff_abs(old)) : !ff_eq(nv, old)) {
+      const int l = list[q], m = smem_of(l);
+      const double old = sd[m], nv = nvs[q];
+      dirty[l] = 0;
+      if (mono ? fabs(nv) < fabs(old) : nv != old) {
         sd[m] = nv;
-        last[m] = gs;
-        any[it & 1] = 1;
+        s32[m] = (float)nv;
+        chg[l] = 3;
       }
     }
     __syncthreads();
-    if (!any[it & 1])
-      break;
+    // 5. the unfrozen tile neighbours of a changed point wait for an update
+    for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
+      const int l = list[q];
+      if (!(chg[l] & 1))
+        continue;
+      chg[l] = 2;
+      const int m = smem_of(l);
+      const int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
+      const int nbl[4] = {ND == 2 ? l - TY : l - 1, ND == 2 ? l + TY : l + 1, l - 1, l + 1};
+      for (int k = 0; k < (ND == 2 ? 4 : 2); k++)
+        if (!is_halo(nbm[k]) && !(sf[nbm[k]] & 1) && inside_of(nbl[k]))
+          dirty[nbl[k]] = 1;
+    }
+    __syncthreads();
   }
-  bool wrote = false;
+  bool wrote = false, waits = false;
   for (int k = 0; k < PER; k++) {
-    int l = threadIdx.x + k * FMM_THREADS;
-    int m = smem_of(l);
-    if (act[k] && last[m] >= gs0) {
-      long c = cell_of(l);
-      dff[c] = sd[m];
-      lastg[c] = last[m];
+    const int l = threadIdx.x + k * FMM_THREADS;
+    if (!act[k])
+      continue;
+    const int m = smem_of(l);
+    const long c = cell_of(l);
+    if (chg[l] & 2) {
+      d[c] = sd[m];
+      lastg[c] = round;
       wrote = true;
     }
+    const uint8_t f = (sf[m] & 3) | (dirty[l] ? 4 : 0);
+    if (f != sf[m])
+      fz[c] = f;
+    waits = waits || dirty[l];
   }
-  bool any_wrote = __syncthreads_or(wrote);
+  const bool any_wrote = __syncthreads_or(wrote);
+  const bool any_waits = __syncthreads_or(waits);
   if (threadIdx.x == 0) {
-    tflag[(long)round * ntiles + t] = any_wrote ? 1 : 0;
-    if (any_wrote)
+    const int fl = (any_wrote ? 1 : 0) | (any_waits ? 2 : 0);
+    tflag[(long)round * ntiles + t] = fl;
+    if (fl)
       atomicOr(&flags[round], 1);
   }
 }
 
 // Final values (base_marcher.cpp:103-106, 190-196): zeros when nothing
-// froze, DBL_MAX where the march never arrived; band points keep their FP64
-// values; the distance also replaces the level set in u
-// (renormalize_levelsets, multi/functions.cpp:56-64).
+// froze, DBL_MAX where the march never arrived; the distance also replaces
+// the level set in u (renormalize_levelsets, multi/functions.cpp:56-64).
 template <int V>
-__global__ void k_fmm_finish(double *__restrict__ d, const Ff *__restrict__ dff,
-                             const uint8_t *__restrict__ fz, double *__restrict__ u, long ncell,
+__global__ void k_fmm_finish(double *__restrict__ d, double *__restrict__ u, long ncell,
                              const int *__restrict__ anyfrozen, const int *__restrict__ flags,
                              int last, int *__restrict__ err, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
@@ -481,10 +538,8 @@ __global__ void k_fmm_finish(double *__restrict__ d, const Ff *__restrict__ dff,
   if (c >= ncell)
     return;
   double x = d[c];
-  if (!(fz[c] & 1)) {
-    Ff f = dff[c];
-    x = isinf(f.h) ? DBL_MAX : (double)f.h + (double)f.l;
-  }
+  if (isinf(x))
+    x = DBL_MAX;
   if (!*anyfrozen)
     x = 0.0;
   d[c] = x;

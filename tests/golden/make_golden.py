@@ -1,7 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the compiled
 reference solver (oracle/_ref, built by `python oracle/build_ref.py v17
 v17n3 v15`), one reference variant per process (`make_golden.py v17n3`
-writes the N = 3 fixtures alone).
+writes the N = 3 fixtures alone, `make_golden.py distance` the
+re-distancing fixture alone).
 
 Every array in the fixtures is an output of the reference's own C++ code
 (haranjackson/phd, code/cpp/src) on seeded inputs; inputs are stored beside
@@ -276,6 +277,49 @@ def contortion_multi(R15, name):
     print("wrote", name)
 
 
+def distance_cases():
+    """Level sets for the re-distancing fixture: circles with unequal
+    spacings, a field with many exact zeros, a noisy field with isolated
+    cells, two bubbles, 1D slabs (one with exact zeros)."""
+    out = []
+    nx, ny = 61, 37
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny * 2.0
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    phi = np.sqrt((X - 0.4) ** 2 + (Y - 1.1) ** 2) - 0.3
+    out.append((phi.ravel(), [1.0 / nx, 2.0 / ny], [nx, ny]))
+    out.append((np.round(phi * 8).ravel() / 8, [1.0 / nx, 2.0 / ny], [nx, ny]))
+    rng = np.random.default_rng(SEED)
+    out.append(((rng.uniform(-1, 1, (40, 30)) + 0.6).ravel(), [0.05, 0.05], [40, 30]))
+    nx, ny = 160, 80
+    x = (np.arange(nx) + 0.5) * 2.0 / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    phi = np.minimum(np.hypot(X - 0.5, Y - 0.5) - 0.2, np.hypot(X - 1.3, Y - 0.45) - 0.15)
+    out.append((phi.ravel(), [2.0 / nx, 1.0 / ny], [nx, ny]))
+    out.append((np.where((np.arange(200) >= 80) & (np.arange(200) < 120), 1.0, -1.0),
+                [0.005], [200]))
+    out.append((np.sin(np.arange(3000) * 0.01) + 0.2, [0.001], [3000]))
+    out.append((np.round(np.sin(np.arange(500) * 0.03) * 4) / 4, [0.01], [500]))
+    return out
+
+
+def distances(R, name):
+    """distance (multi/pfmm.cpp:4-26, the vendored scikit-fmm marcher) of
+    the reference build on distance_cases()."""
+    arrs = {}
+    cases = distance_cases()
+    for k, (phi, dX, nX) in enumerate(cases):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        nXa = np.array(nX, np.int32)
+        arrs["phi%d" % k] = phi
+        arrs["dX%d" % k] = np.array(dX, np.float64)
+        arrs["nX%d" % k] = nXa
+        arrs["dist%d" % k] = np.asarray(R.distance(phi, np.array(dX, np.float64), nXa))
+    arrs["count"] = np.array(len(cases))
+    np.savez_compressed(os.path.join(HERE, name), **arrs)
+
+
 def main():
     # one reference variant per process: the variants' Par types collide in
     # pybind11's registry
@@ -297,6 +341,13 @@ def main():
         np.savez_compressed(os.path.join(HERE, "stages2d_rus_v17n3.npz"),
                             **stages(R3, u0, MP, dX, 1, 0.4, 2, flux=0))
         return 0
+    if variant == "distance":  # the re-distancing fixture alone
+        R = rd.load("v17")
+        if R is None:
+            print("oracle/_ref/GPRref_v17 not built; run oracle/build_ref.py v17")
+            return 1
+        distances(R, "distance_v17.npz")
+        return 0
     if variant == "v15":
         R15 = rd.load("v15")
         multi(R15, "multi_v15.npz")
@@ -308,6 +359,7 @@ def main():
         return 1
     contortion(R, "contortion_v17.npz")
     pointwise(R, "pointwise_v17.npz")
+    distances(R, "distance_v17.npz")
 
     # 1D shock tube (200 cells): stages after 20 steps, Rusanov and Osher
     u0, MP, tf, dX, bcs = problems.shock_tube()

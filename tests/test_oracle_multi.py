@@ -31,14 +31,25 @@ def MPs(g):
 def test_distance_normals_interface(O, g):
     nX, dX = g["ls_nX"], list(g["ls_dX"])
     d = O.distance(g["ls_phi"], dX, nX)
-    # the marcher's quadratic updates in a different association order
-    assert np.max(np.abs(d - g["ls_dist"])) < 1e-13
+    # the marcher's quadratic with the reference build's fused multiply-adds
+    assert np.array_equal(d, g["ls_dist"])
     fd = O.finite_difference(g["ls_dist"], dX, nX)
     assert np.array_equal(fd, g["ls_fd"])
     im = O.find_interface_cells(g["ls_dist"], nX)
     assert np.array_equal(im, g["ls_intmask"])
     assert set(np.unique(im)) <= {-2, -1, 0, 1}
     assert (im == 1).sum() > 20 and (im == -1).sum() > 20
+
+
+def test_distance_bit_equal_to_the_reference():
+    """The oracle's marcher against the reference build's on every level
+    set of the re-distancing fixture: bit for bit."""
+    from conftest import golden
+    g = golden("distance_v17.npz")
+    O = Oracle(N=2, thermal=False, lset=1)
+    for k in range(int(g["count"])):
+        d = O.distance(g["phi%d" % k], list(g["dX%d" % k]), g["nX%d" % k])
+        assert np.array_equal(d, g["dist%d" % k]), k
 
 
 def test_distance_no_crossing_is_zero(O):
