@@ -173,8 +173,6 @@ bool grid_ok(const int32_t *nX, int nd) {
 // shock-bubble step), 1024 no faster.
 constexpr int kFmmSweeps = 256;
 
-// Width of the band of FP32 estimates one sweep updates, in grid spacings.
-constexpr double kFmmDelta = 1.0;
 
 // Round budget: information crosses at least one tile per round, and the
 // global Jacobi needs about as many sweeps as the longest marching path in
@@ -241,8 +239,7 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
   cudaMemsetAsync(tflag, 0, (size_t)R * fmm_tiles(g) * sizeof(int), st);
   cudaMemsetAsync(lastg, 0xff, g.ncell * sizeof(int), st);
   k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, fz, g, cnt, clk);
-  const double hmin = g.nd == 2 && g.dy < g.dx ? g.dy : g.dx;
-  FmmConst K = fmm_const(g.dx, g.nd == 2 ? g.dy : g.dx, kFmmDelta * hmin);
+  FmmConst K = fmm_const(g.dx, g.nd == 2 ? g.dy : g.dx);
   if (g.nd == 2) {
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)

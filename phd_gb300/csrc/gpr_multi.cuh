@@ -21,8 +21,7 @@
 //     (band neighbours always enter a point's quadratic, the others only
 //     while their distance is below the point's estimate, as the marcher's
 //     heap order makes it), in FP64 with the marcher's quadratic and
-//     roundings; FP32 estimates order the sweeps' work (Dial's buckets
-//     within a tile) and never enter a result;
+//     roundings;
 //   * a boundary cell reads the right-hand state of the interface from a
 //     cell that an earlier cell of the (i, j) sweep may have filled; those
 //     reads are resolved to the last earlier writer and solved level by
@@ -117,29 +116,26 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
     atomicOr(anyfrozen, 1);
 }
 
-// Grid constants of the update: 1 / dx^2, 1 / dy^2 for the marcher's FP64
-// quadratic; for the FP32 estimate the root of the same quadratic written
-// without cancellation, x = al u + be w +- sqrt(ga - ab (u - w)^2) with
-// ix = 1/dx^2, iy = 1/dy^2, al = ix / (ix + iy), be = iy / (ix + iy),
-// ga = 1 / (ix + iy), ab = al be; delta is the width of the band of
-// estimates a sweep updates (below).
+// Grid constants of the update: the marcher's idx2 = 1 / dx^2, 1 / dy^2
+// (distance_marcher.cpp), its quadratic's leading coefficient for each set
+// of entered axes (idx2[0], idx2[1], idx2[0] + idx2[1], as the marcher sums
+// it) and that coefficient's reciprocal rounded to nearest, and the
+// spacings.
 struct FmmConst {
-  double idx2[2];
-  float h[2], al, be, ga, ab, delta;
+  double idx2[2], a[3], ra[3], h[2];
 };
 
-inline FmmConst fmm_const(double dx, double dy, double delta) {
+inline FmmConst fmm_const(double dx, double dy) {
   FmmConst K;
-  K.idx2[0] = 1.0 / dx / dx;  // the marcher's idx2 (distance_marcher.cpp)
+  K.idx2[0] = 1.0 / dx / dx;
   K.idx2[1] = 1.0 / dy / dy;
-  double ix = K.idx2[0], iy = K.idx2[1], S = ix + iy;
-  K.h[0] = (float)dx;
-  K.h[1] = (float)dy;
-  K.al = (float)(ix / S);
-  K.be = (float)(iy / S);
-  K.ga = (float)(1.0 / S);
-  K.ab = (float)(ix / S * (iy / S));
-  K.delta = (float)delta;
+  K.a[0] = K.idx2[0];
+  K.a[1] = K.idx2[1];
+  K.a[2] = K.idx2[0] + K.idx2[1];
+  for (int k = 0; k < 3; k++)
+    K.ra[k] = 1.0 / K.a[k];
+  K.h[0] = dx;
+  K.h[1] = dy;
   return K;
 }
 
@@ -149,48 +145,33 @@ inline FmmConst fmm_const(double dx, double dy, double delta) {
 // with the marcher's operation order and the fused multiply-adds of the
 // reference's -O3 -march=native build (CMakeLists.txt:14): b and c
 // accumulate by fma, det = fma(b, b, -(4 a c)); every other operation is
-// rounded on its own.  The marcher leaves a point unchanged when the
-// quadratic has no real root (its 0 return); so does a false return here.
-struct Root64 {
-  const FmmConst &K;
-  int nd;
-  GPR_D bool operator()(const double v[2], const bool use[2], bool pos, double &x) const {
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int dim = 0; dim < nd; dim++)
-      if (use[dim]) {
-        a = add(a, K.idx2[dim]);
-        b = __fma_rn(-mul(K.idx2[dim], 2.0), v[dim], b);
-        c = __fma_rn(K.idx2[dim], mul(v[dim], v[dim]), c);
-      }
-    c = sub(c, 1.0);
-    const double det = __fma_rn(b, b, -mul(mul(4.0, a), c));
-    if (!(det > 0.0))
-      return false;
-    const double sq = __dsqrt_rn(det);
-    x = dvd(dvd(pos ? add(-b, sq) : sub(-b, sq), 2.0), a);
-    return x != 0.0;
-  }
-};
-
-// The FP32 estimate of the same update (cancellation-free root), used only
-// to order the sweeps' work.
-struct Root32 {
-  const FmmConst &K;
-  GPR_D bool operator()(const float v[2], const bool use[2], bool pos, float &x) const {
-    if (use[0] && use[1]) {
-      const float df = v[0] - v[1];
-      const float D = K.ga - K.ab * df * df;
-      if (!(D > 0.0f))
-        return false;
-      const float sq = sqrtf(D), m = K.al * v[0] + K.be * v[1];
-      x = pos ? m + sq : m - sq;
-      return true;
+// rounded on its own.  The halving is a multiply by 0.5 (exact, the same
+// value) and the division by a is Markstein's correction of a product with
+// the rounded reciprocal, q = RN(q0 + RN(x - a q0) ra) with q0 = RN(x ra)
+// (P. Markstein, IBM J. Res. Dev. 34, 1990; the correctly rounded quotient
+// when ra = RN(1/a), as __ddiv_rn gives it).  The marcher leaves a point
+// unchanged when the quadratic has no real root (its 0 return); so does a
+// false return here.
+GPR_D bool fmm_root(const double v[2], const bool use[2], const FmmConst &K, int nd, bool pos,
+                    double &x) {
+  double a = 0.0, b = 0.0, c = 0.0;
+  for (int dim = 0; dim < nd; dim++)
+    if (use[dim]) {
+      a = add(a, K.idx2[dim]);
+      b = __fma_rn(-mul(K.idx2[dim], 2.0), v[dim], b);
+      c = __fma_rn(K.idx2[dim], mul(v[dim], v[dim]), c);
     }
-    const int k = use[0] ? 0 : 1;
-    x = pos ? v[k] + K.h[k] : v[k] - K.h[k];
-    return true;
-  }
-};
+  const int ka = use[0] && use[1] ? 2 : (use[0] ? 0 : 1);
+  c = sub(c, 1.0);
+  const double det = __fma_rn(b, b, -mul(mul(4.0, a), c));
+  if (!(det > 0.0))
+    return false;
+  const double sq = __dsqrt_rn(det);
+  const double num = mul(pos ? add(-b, sq) : sub(-b, sq), 0.5);
+  const double q0 = mul(num, K.ra[ka]);
+  x = __fma_rn(__fma_rn(-q0, K.a[ka], num), K.ra[ka], q0);
+  return x != 0.0;
+}
 
 // Update of one unfrozen point from its neighbours' current values
 // (signed; +inf unknown), reproducing what the marcher's heap order makes
@@ -204,15 +185,20 @@ struct Root32 {
 // root exceeds its |d| in exact arithmetic); where rounding says otherwise
 // (a noise-level tie) it is left out, so that no two points feed each other
 // and the iteration cannot cycle.  Returns `old` when nothing is known.
-template <class T, class RootF>
-GPR_D T fmm_update(const T nb[2][2], const bool band[2][2], bool pos, int nd, T old,
-                   const RootF &root) {
-  const T INF = (T)INFINITY;
-  T v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
+//
+// A one-axis root is v +- h up to the quadratic's cancellation (at most
+// ~eps (v^2 / h + |v| + h)); it is taken in that form where it only decides
+// whether the next neighbour enters and the decision is clear by 256 times
+// that bound, and evaluated exactly where it is the result or the decision
+// is close.  The result is the same as evaluating every root exactly.
+GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, int nd,
+                        double old, const FmmConst &K) {
+  const double INF = INFINITY;
+  double v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
   bool use[2] = {false, false};
   for (int dim = 0; dim < nd; dim++)
     for (int s = 0; s < 2; s++) {
-      const T x = nb[dim][s], ax = fabs(x);
+      const double x = nb[dim][s], ax = fabs(x);
       if (band[dim][s]) {
         if (!use[dim] || ax < fabs(v[dim])) {
           v[dim] = x;
@@ -223,20 +209,32 @@ GPR_D T fmm_update(const T nb[2][2], const bool band[2][2], bool pos, int nd, T 
         cv[dim] = x;
       }
     }
-  T t = INF;
+  double t = INF, tm = 0.0;  // tm > 0: t is v +- h, within tm of the exact root
   if (use[0] || use[1]) {
-    T r;
-    if (root(v, use, pos, r))
+    double r;
+    if (fmm_root(v, use, K, nd, pos, r))
       t = r;
   }
+  auto one_axis = [&](double &x, double &m) {  // v +- h of the one entered axis
+    const int k = use[0] ? 0 : 1;
+    const double w = fabs(v[k]), h = K.h[k];
+    x = pos ? v[k] + h : v[k] - h;
+    m = 256.0 * DBL_EPSILON * (w * w / h + w + h);
+    return fabs(x) > m;  // far enough from the marcher's 0 return
+  };
   bool done[2] = {isinf(ck[0]), nd < 2 || isinf(ck[1])};
   while (!done[0] || !done[1]) {
     const int a = done[0] ? 1 : (done[1] ? 0 : (ck[1] < ck[0] ? 1 : 0));
-    const T key = ck[a];
+    const double key = ck[a];
+    if (tm > 0.0 && fabs(key - fabs(t)) <= tm) {
+      double r;
+      t = fmm_root(v, use, K, nd, pos, r) ? r : INF;
+      tm = 0.0;
+    }
     if (!(key < fabs(t)))
       break;
     const bool both = !done[1 - a] && ck[1 - a] == key;
-    const T sv0 = v[0], sv1 = v[1];
+    const double sv0 = v[0], sv1 = v[1];
     const bool su0 = use[0], su1 = use[1];
     for (int q = 0; q < 2; q++) {
       const int dim = q == 0 ? a : 1 - a;
@@ -248,8 +246,17 @@ GPR_D T fmm_update(const T nb[2][2], const bool band[2][2], bool pos, int nd, T 
       }
       done[dim] = true;
     }
-    T t2;
-    if (!root(v, use, pos, t2) || !(key < fabs(t2))) {
+    double t2, m2 = 0.0;
+    bool ok;
+    if (use[0] && use[1]) {
+      ok = fmm_root(v, use, K, nd, pos, t2);
+    } else if (!one_axis(t2, m2) || fabs(key - fabs(t2)) <= m2) {
+      ok = fmm_root(v, use, K, nd, pos, t2);
+      m2 = 0.0;
+    } else {
+      ok = true;
+    }
+    if (!ok || !(key < fabs(t2))) {
       v[0] = sv0;
       v[1] = sv1;
       use[0] = su0;
@@ -257,14 +264,19 @@ GPR_D T fmm_update(const T nb[2][2], const bool band[2][2], bool pos, int nd, T 
       break;
     }
     t = t2;
+    tm = m2;
+  }
+  if (tm > 0.0) {
+    double r;
+    t = fmm_root(v, use, K, nd, pos, r) ? r : INF;
   }
   return isinf(t) ? old : t;
 }
 
 // The four neighbours of shared-memory point m (x neighbours m -+ o0, y
 // neighbours m -+ 1) and whether each is in the frozen band.
-template <class T, int ND>
-GPR_D void fmm_load_nb(const T *src, const uint8_t *sf, int m, int o0, T nb[2][2],
+template <int ND>
+GPR_D void fmm_load_nb(const double *src, const uint8_t *sf, int m, int o0, double nb[2][2],
                        bool bd[2][2]) {
   nb[0][0] = src[m - o0];
   nb[0][1] = src[m + o0];
@@ -276,33 +288,29 @@ GPR_D void fmm_load_nb(const T *src, const uint8_t *sf, int m, int o0, T nb[2][2
     bd[1][0] = sf[m - 1] & 1;
     bd[1][1] = sf[m + 1] & 1;
   } else {
-    nb[1][0] = nb[1][1] = (T)INFINITY;
+    nb[1][0] = nb[1][1] = INFINITY;
     bd[1][0] = bd[1][1] = false;
   }
 }
 
-// One round of tiled sweeps of the causal update, in FP64.  Each block
-// loads its tile and a one-cell halo into shared memory and runs up to
-// `nsweeps` sweeps against that halo, then writes back.  A point waits for
-// an update (dirty) when a neighbour changed after its last update.  Each
-// sweep estimates the new value of every waiting point in FP32, takes the
-// least estimate m of the tile, and updates in FP64 (Jacobi: all reads
-// before all writes) only the waiting points whose estimate is within
-// delta of m; the others wait.  That is Dial's bucketed order of the
-// marcher (Tsitsiklis, "Efficient algorithms for globally optimal
-// trajectories", IEEE TAC 40, 1995) within a tile: a point is mostly
-// updated once its upwind neighbours have settled, instead of once per
-// improvement of each of them, which keeps the FP64 updates per point to a
-// few (GB300's FP64 pipe issues one warp instruction per 64 cycles per SM
-// partition).  The order changes only the work: the sweeps end when no
-// point waits, at the fixed point of the update, whatever the order.
-// lastg[c] is the round of cell c's last change; fz bit 2 carries a
-// waiting point into the next round.  A tile runs if it has waiting points
-// or a neighbouring tile changed in the previous round (tflag bit 1 / bit 0
-// of round - 1); flags[round] records whether anything changed or waits,
-// and a round after a round without either returns at once.  2D tiles are
-// 32 x 32 cells, 1D tiles 1024; FMM_THREADS threads own 1024 / FMM_THREADS
-// cells each.
+// One round of tiled Jacobi sweeps of the causal update, in FP64.  Each
+// block loads its tile and a one-cell halo into shared memory and runs up
+// to `nsweeps` sweeps against that halo, then writes back.  A point waits
+// for an update (dirty) when a neighbour changed after its last update;
+// each sweep gathers the waiting points into a list first, so that whole
+// warps run the updates, and a changed point makes its unfrozen tile
+// neighbours wait.  GB300's FP64 pipe issues one warp instruction per 64
+// cycles per SM partition, so the sweeps' cost is the longest chain of
+// dependent updates (~1400 sweeps at 800 x 400, a tile crossed per round)
+// times the update's FP64 instruction count, which the update above keeps
+// to about one root.  The sweeps end when no point waits, at the fixed
+// point of the update, whatever the order of the work.  lastg[c] is the
+// round of cell c's last change; fz bit 2 carries a waiting point into the
+// next round.  A tile runs if it has waiting points or a neighbouring tile
+// changed in the previous round (tflag bit 1 / bit 0 of round - 1);
+// flags[round] records whether anything changed or waits, and a round after
+// a round without either returns at once.  2D tiles are 32 x 32 cells, 1D
+// tiles 1024; FMM_THREADS threads own 1024 / FMM_THREADS cells each.
 constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
 
 template <int ND>
@@ -332,13 +340,11 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
   }
   __shared__ double sd[SX * SY];
   __shared__ double nvs[NT];
-  __shared__ float s32[SX * SY];
   __shared__ uint8_t sf[SX * SY];
   __shared__ uint8_t hchg[SX * SY];  // halo point changed in the previous round
   __shared__ uint8_t dirty[NT];
-  __shared__ uint8_t chg[NT];  // bit 0 changed this sweep, bit 1 this round
+  __shared__ uint8_t chg[NT];  // changed in this round
   __shared__ int16_t list[NT];
-  __shared__ float wmin[NW];
   __shared__ int wcnt[NW], total;
   const int bi = ND == 2 ? t % ntx0 : t, bj = ND == 2 ? t / ntx0 : 0;
   const int i0 = bi * TX, j0 = bj * TY;
@@ -354,7 +360,6 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
       hc = lastg[c] == round - 1;
     }
     sd[e] = x;
-    s32[e] = (float)x;
     sf[e] = f;
     hchg[e] = hc;
   }
@@ -390,53 +395,14 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
     chg[l] = 0;
   }
   __syncthreads();
-  const Root32 r32{K};
-  const Root64 r64{K, ND};
   for (int it = 0; it < nsweeps; it++) {
-    // 1. FP32 estimates of the waiting points and the tile's least estimate
-    float est[PER];  // |estimate|; -1 nothing known (drops out), -2 FP64 decides
-    float mymin = INFINITY;
-    bool anyd = false;
-    for (int k = 0; k < PER; k++) {
-      const int l = threadIdx.x + k * FMM_THREADS;
-      est[k] = INFINITY;
-      if (!dirty[l])
-        continue;
-      anyd = true;
-      const int m = smem_of(l);
-      float nb[2][2];
-      bool bd[2][2];
-      fmm_load_nb<float, ND>(s32, sf, m, o0, nb, bd);
-      if (isinf(nb[0][0]) && isinf(nb[0][1]) && isinf(nb[1][0]) && isinf(nb[1][1])) {
-        est[k] = -1.0f;
-        continue;
-      }
-      const float e = fmm_update<float>(nb, bd, (sf[m] & 2) != 0, ND, (float)INFINITY, r32);
-      if (isinf(e)) {
-        est[k] = -2.0f;
-      } else {
-        est[k] = fabsf(e);
-        mymin = fminf(mymin, est[k]);
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1)
-      mymin = fminf(mymin, __shfl_xor_sync(0xffffffffu, mymin, o));
-    if (lane == 0)
-      wmin[wid] = mymin;
-    if (!__syncthreads_or(anyd))
-      break;
-    float mn = wmin[0];
-    for (int w = 1; w < NW; w++)
-      mn = fminf(mn, wmin[w]);
-    const float lim = mn + K.delta;
-    // 2. gather the points this sweep updates
-    bool sel[PER];
+    // 1. gather the waiting points (each thread clears its own flags)
     int mine = 0;
+    bool sel[PER];
     for (int k = 0; k < PER; k++) {
       const int l = threadIdx.x + k * FMM_THREADS;
-      sel[k] = est[k] == -2.0f || (est[k] >= 0.0f && est[k] <= lim);
-      if (est[k] == -1.0f)
-        dirty[l] = 0;
+      sel[k] = dirty[l] != 0;
+      dirty[l] = 0;
       mine += sel[k];
     }
     int incl = mine;  // inclusive warp scan
@@ -458,41 +424,33 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
     if (threadIdx.x == FMM_THREADS - 1)
       total = pos;
     __syncthreads();
-    // 3. FP64 updates (Jacobi: read the neighbours, write after a barrier)
     const int n = total;
+    if (n == 0)
+      break;
+    // 2. updates (Jacobi: read the neighbours, write after a barrier)
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
       const int m = smem_of(list[q]);
       double nb[2][2];
       bool bd[2][2];
-      fmm_load_nb<double, ND>(sd, sf, m, o0, nb, bd);
-      nvs[q] = fmm_update<double>(nb, bd, (sf[m] & 2) != 0, ND, sd[m], r64);
+      fmm_load_nb<ND>(sd, sf, m, o0, nb, bd);
+      nvs[q] = fmm_update(nb, bd, (sf[m] & 2) != 0, ND, sd[m], K);
     }
     __syncthreads();
-    // 4. take the new values; from the second half of the round budget on,
-    // only a smaller |d| is taken, which guarantees termination
+    // 3. take the new values (from the second half of the round budget on,
+    // only a smaller |d|, which guarantees termination); the unfrozen tile
+    // neighbours of a changed point wait for the next sweep
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
       const int l = list[q], m = smem_of(l);
       const double old = sd[m], nv = nvs[q];
-      dirty[l] = 0;
       if (mono ? fabs(nv) < fabs(old) : nv != old) {
         sd[m] = nv;
-        s32[m] = (float)nv;
-        chg[l] = 3;
+        chg[l] = 1;
+        const int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
+        const int nbl[4] = {ND == 2 ? l - TY : l - 1, ND == 2 ? l + TY : l + 1, l - 1, l + 1};
+        for (int k = 0; k < (ND == 2 ? 4 : 2); k++)
+          if (!is_halo(nbm[k]) && !(sf[nbm[k]] & 1) && inside_of(nbl[k]))
+            dirty[nbl[k]] = 1;
       }
-    }
-    __syncthreads();
-    // 5. the unfrozen tile neighbours of a changed point wait for an update
-    for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
-      const int l = list[q];
-      if (!(chg[l] & 1))
-        continue;
-      chg[l] = 2;
-      const int m = smem_of(l);
-      const int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
-      const int nbl[4] = {ND == 2 ? l - TY : l - 1, ND == 2 ? l + TY : l + 1, l - 1, l + 1};
-      for (int k = 0; k < (ND == 2 ? 4 : 2); k++)
-        if (!is_halo(nbm[k]) && !(sf[nbm[k]] & 1) && inside_of(nbl[k]))
-          dirty[nbl[k]] = 1;
     }
     __syncthreads();
   }
@@ -503,7 +461,7 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
       continue;
     const int m = smem_of(l);
     const long c = cell_of(l);
-    if (chg[l] & 2) {
+    if (chg[l]) {
       d[c] = sd[m];
       lastg[c] = round;
       wrote = true;
