@@ -169,10 +169,9 @@ bool grid_ok(const int32_t *nX, int nd) {
 }
 
 // Sweeps per re-distancing round (a tile's sweeps between halo exchanges):
-// eight tile widths; 32 was slower (25.7 against 23.4 ms per 800 x 400
-// shock-bubble step), 1024 no faster.
+// a tile converges on a fixed halo within its Manhattan diameter (~2 tile
+// widths); the budget only bounds a round.
 constexpr int kFmmSweeps = 256;
-
 
 // Round budget: information crosses at least one tile per round, and the
 // global Jacobi needs about as many sweeps as the longest marching path in
@@ -243,12 +242,12 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
   if (g.nd == 2) {
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)
-      k_fmm_round<2><<<nb, FMM_THREADS, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<2><<<nb, FmmThreads<2>::value, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)
-      k_fmm_round<1><<<nb, FMM_THREADS, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<1><<<nb, FmmThreads<1>::value, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   }
   k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, u, g.ncell, cnt, flags, R - 1, err,

@@ -191,21 +191,30 @@ GPR_D bool fmm_root(const double v[2], const bool use[2], const FmmConst &K, int
 // whether the next neighbour enters and the decision is clear by 256 times
 // that bound, and evaluated exactly where it is the result or the decision
 // is close.  The result is the same as evaluating every root exactly.
+// |x| as an integer: the order of |x| for finite values and infinity, on
+// the integer pipe (the decisions below then take no FP64 issue slots).
+GPR_D unsigned long long fmm_key(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
 GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, int nd,
                         double old, const FmmConst &K) {
   const double INF = INFINITY;
-  double v[2] = {INF, INF}, cv[2] = {INF, INF}, ck[2] = {INF, INF};
+  const unsigned long long KINF = 0x7ff0000000000000ull;
+  double v[2] = {INF, INF}, cv[2] = {INF, INF};
+  unsigned long long ck[2] = {KINF, KINF};
   bool use[2] = {false, false};
   for (int dim = 0; dim < nd; dim++)
     for (int s = 0; s < 2; s++) {
-      const double x = nb[dim][s], ax = fabs(x);
+      const double x = nb[dim][s];
+      const unsigned long long kx = fmm_key(x);
       if (band[dim][s]) {
-        if (!use[dim] || ax < fabs(v[dim])) {
+        if (!use[dim] || kx < fmm_key(v[dim])) {
           v[dim] = x;
           use[dim] = true;
         }
-      } else if (ax < ck[dim]) {
-        ck[dim] = ax;
+      } else if (kx < ck[dim]) {
+        ck[dim] = kx;
         cv[dim] = x;
       }
     }
@@ -215,23 +224,16 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, 
     if (fmm_root(v, use, K, nd, pos, r))
       t = r;
   }
-  auto one_axis = [&](double &x, double &m) {  // v +- h of the one entered axis
-    const int k = use[0] ? 0 : 1;
-    const double w = fabs(v[k]), h = K.h[k];
-    x = pos ? v[k] + h : v[k] - h;
-    m = 256.0 * DBL_EPSILON * (w * w / h + w + h);
-    return fabs(x) > m;  // far enough from the marcher's 0 return
-  };
-  bool done[2] = {isinf(ck[0]), nd < 2 || isinf(ck[1])};
+  bool done[2] = {ck[0] == KINF, nd < 2 || ck[1] == KINF};
   while (!done[0] || !done[1]) {
     const int a = done[0] ? 1 : (done[1] ? 0 : (ck[1] < ck[0] ? 1 : 0));
-    const double key = ck[a];
-    if (tm > 0.0 && fabs(key - fabs(t)) <= tm) {
+    const unsigned long long key = ck[a];
+    if (tm > 0.0 && fabs(fabs(cv[a]) - fabs(t)) <= tm) {
       double r;
       t = fmm_root(v, use, K, nd, pos, r) ? r : INF;
       tm = 0.0;
     }
-    if (!(key < fabs(t)))
+    if (!(key < fmm_key(t)))
       break;
     const bool both = !done[1 - a] && ck[1 - a] == key;
     const double sv0 = v[0], sv1 = v[1];
@@ -240,23 +242,29 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, 
       const int dim = q == 0 ? a : 1 - a;
       if (q == 1 && !both)
         break;
-      if (!use[dim] || fabs(cv[dim]) < fabs(v[dim])) {
+      if (!use[dim] || fmm_key(cv[dim]) < fmm_key(v[dim])) {
         v[dim] = cv[dim];
         use[dim] = true;
       }
       done[dim] = true;
     }
     double t2, m2 = 0.0;
-    bool ok;
+    bool ok = true;
     if (use[0] && use[1]) {
       ok = fmm_root(v, use, K, nd, pos, t2);
-    } else if (!one_axis(t2, m2) || fabs(key - fabs(t2)) <= m2) {
-      ok = fmm_root(v, use, K, nd, pos, t2);
-      m2 = 0.0;
     } else {
-      ok = true;
+      // v +- h of the one entered axis, and the bound of its distance from
+      // the marcher's root
+      const int k = use[0] ? 0 : 1;
+      const double w = fabs(v[k]), h = K.h[k];
+      t2 = pos ? v[k] + h : v[k] - h;
+      m2 = 256.0 * DBL_EPSILON * (w * w / h + w + h);
+      if (!(fabs(t2) > m2) || fabs(fabs(cv[a]) - fabs(t2)) <= m2) {
+        ok = fmm_root(v, use, K, nd, pos, t2);
+        m2 = 0.0;
+      }
     }
-    if (!ok || !(key < fabs(t2))) {
+    if (!ok || !(key < fmm_key(t2))) {
       v[0] = sv0;
       v[1] = sv1;
       use[0] = su0;
@@ -310,11 +318,16 @@ GPR_D void fmm_load_nb(const double *src, const uint8_t *sf, int m, int o0, doub
 // changed in the previous round (tflag bit 1 / bit 0 of round - 1);
 // flags[round] records whether anything changed or waits, and a round after
 // a round without either returns at once.  2D tiles are 32 x 32 cells, 1D
-// tiles 1024; FMM_THREADS threads own 1024 / FMM_THREADS cells each.
-constexpr int FMM_T2 = 32, FMM_T1 = 1024, FMM_THREADS = 512;
+// tiles 1024 (16 x 16 tiles cross the 800 x 400 grid in 1344 sweeps with
+// 34 updates per cell, 32 x 32 ones in 1392 with 49, and spread the front
+// over more SMs); each thread owns one 2D cell or two 1D cells.
+constexpr int FMM_T2 = 16, FMM_T1 = 1024;
+template <int ND> struct FmmThreads {
+  static constexpr int value = ND == 2 ? 256 : 512;
+};
 
 template <int ND>
-__global__ void __launch_bounds__(FMM_THREADS, 2)
+__global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
     k_fmm_round(double *__restrict__ d, uint8_t *__restrict__ fz, int *__restrict__ lastg,
                 Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
                 int nsweeps, int mono, const double *__restrict__ clk) {
@@ -324,6 +337,7 @@ __global__ void __launch_bounds__(FMM_THREADS, 2)
     return;
   constexpr int TX = ND == 2 ? FMM_T2 : FMM_T1, TY = ND == 2 ? FMM_T2 : 1;
   constexpr int SX = TX + 2, SY = ND == 2 ? TY + 2 : 1;
+  constexpr int FMM_THREADS = FmmThreads<ND>::value;
   constexpr int NT = TX * TY, PER = NT / FMM_THREADS, NW = FMM_THREADS / 32;
   const int ntx0 = (g.nx + TX - 1) / TX, nty0 = ND == 2 ? (g.ny + TY - 1) / TY : 1;
   const int ntiles = ntx0 * nty0;

@@ -366,8 +366,14 @@ def test_config3_loop_per_step_against_oracle(G, O):
 
 def test_config3_fill_against_oracle(G, O):
     """The ghost fill on the workload's data (isotropic, mu = 1e-4, 240 x 120,
-    the shock through the bubble's left half): masks exact, copied cells
-    exact, filled cells within 1e-6 and at least 90% within 1e-10."""
+    the shock through the bubble's left half): the re-distanced level set
+    bit-equal, masks exact, copied cells exact, filled cells within 1e-6.
+    Per filled cell the bar is the reference scheme's own rounding
+    sensitivity there, measured as the oracle's response to 1e-15 relative
+    noise on its input: it exceeds 1e-10 in ~10% of the filled cells (the
+    interface Riemann solve at isotropic distortions), so the device fill
+    must be within max(1e-10, 10x that response) in at least 99% of them,
+    and within 1e-10 in as many cells as the oracle's response allows."""
     from phd_gb300 import problems
     u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=240, ny=120, mu=1e-4, x_shock=0.36)
     nX = np.array(u0.shape[:2], np.int32)
@@ -376,6 +382,19 @@ def test_config3_fill_against_oracle(G, O):
     ug, grids, masks, st = _fill_gpu(G, u, nX, dX, dt, MPs)
     uo, go, mo, im, bad = O.fill_ghost_cells(u.ravel(), nX, dX, dt, MPs)
     assert bad == 0 and (st == 0).all()
-    assert np.max(np.abs(ug - uo)) < 1e-12
+    assert np.array_equal(ug, uo)
     assert np.array_equal(masks, mo)
-    _check_fill(grids, go, im, filled_tol=1e-6, frac=0.9)
+    _check_fill(grids, go, im, filled_tol=1e-6, frac=0.0)
+    filled = (im == 1) | (im > 1)
+    rng = np.random.default_rng(5)
+    resp = np.zeros(go.shape[:2])
+    for _ in range(2):
+        un = u.ravel() * (1 + 1e-15 * rng.standard_normal(u.size))
+        _, g2, m2, im2, _ = O.fill_ghost_cells(un, nX, dX, dt, MPs)
+        assert np.array_equal(im2, im)
+        resp = np.maximum(resp, np.max(np.abs(g2 - go) / (1 + np.abs(go)), axis=2))
+    cell = np.max(np.abs(grids - go) / (1 + np.abs(go)), axis=2)[filled]
+    r = resp[filled]
+    assert np.mean(cell <= np.maximum(1e-10, 10 * r)) >= 0.99
+    assert np.mean(cell <= 1e-10) >= np.mean(r <= 1e-10) - 0.02, (
+        np.mean(cell <= 1e-10), np.mean(r <= 1e-10))
