@@ -187,7 +187,7 @@ int fmm_rounds(const Grid &g) {
 // Scratch of one fill (offsets in doubles, 256-byte aligned pieces).
 struct FillLayout {
   long o_d, o_phim, o_dphi, o_star, o_plan, o_fz, o_im0, o_im1, o_lastw, o_pidx, o_dep,
-      o_level, o_cnt, o_flags, o_tflag, o_lastg, total;
+      o_level, o_cnt, o_flags, o_tflag, o_lastg, o_par, total;
 };
 
 int fmm_tiles(const Grid &g) {
@@ -217,6 +217,7 @@ FillLayout fill_layout(const Grid &g) {
   L.o_flags = cv.take(dbl(fmm_rounds(g) * 4L));
   L.o_tflag = cv.take(dbl((long)fmm_rounds(g) * fmm_tiles(g) * 4L));
   L.o_lastg = cv.take(dbl(n * 4));
+  L.o_par = cv.take(dbl(n));
   L.total = cv.o;
   return L;
 }
@@ -237,17 +238,18 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
   cudaMemsetAsync(flags, 0, R * sizeof(int), st);
   cudaMemsetAsync(tflag, 0, (size_t)R * fmm_tiles(g) * sizeof(int), st);
   cudaMemsetAsync(lastg, 0xff, g.ncell * sizeof(int), st);
-  k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, fz, g, cnt, clk);
+  uint8_t *par = at<uint8_t>(scr, L.o_par);
+  k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, fz, par, g, cnt, clk);
   FmmConst K = fmm_const(g.dx, g.nd == 2 ? g.dy : g.dx);
   if (g.nd == 2) {
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)
-      k_fmm_round<2><<<nb, FmmThreads<2>::value, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<2><<<nb, FmmThreads<2>::value, 0, st>>>(d, fz, par, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)
-      k_fmm_round<1><<<nb, FmmThreads<1>::value, 0, st>>>(d, fz, lastg, g, K, flags, tflag, r,
+      k_fmm_round<1><<<nb, FmmThreads<1>::value, 0, st>>>(d, fz, par, lastg, g, K, flags, tflag, r,
                                                  kFmmSweeps, r >= R / 2, clk);
   }
   k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, u, g.ncell, cnt, flags, R - 1, err,

@@ -64,10 +64,11 @@ GPR_D double dvd(double a, double b) { return __ddiv_rn(a, b); }
 // roundings.  Others start unknown (+inf).  phi[c * ps] is the level set of
 // cell c.  fz: bit 0 frozen (band), bit 1 the marcher would take the
 // positive root for this cell (phi > DBL_EPSILON), bit 2 the point waits
-// for an update (set by the sweeps).
+// for an update (set by the sweeps); par: the neighbours that entered the
+// point's update (set by the sweeps).
 __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__restrict__ d,
-                           uint8_t *__restrict__ fz, Grid g, int *__restrict__ anyfrozen,
-                           const double *__restrict__ clk) {
+                           uint8_t *__restrict__ fz, uint8_t *__restrict__ par, Grid g,
+                           int *__restrict__ anyfrozen, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
   long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -112,6 +113,7 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
   }
   d[c] = x;
   fz[c] = (frozen ? 1 : 0) | pos;
+  par[c] = 0;
   if (frozen)
     atomicOr(anyfrozen, 1);
 }
@@ -175,34 +177,40 @@ GPR_D bool fmm_root(const double v[2], const bool use[2], const FmmConst &K, int
 
 // Update of one unfrozen point from its neighbours' current values
 // (signed; +inf unknown), reproducing what the marcher's heap order makes
-// of it.  Band neighbours (frozen at initialisation) always enter.  The
-// other neighbours enter in increasing |d| (equal keys together, as the
-// marcher freezes them in one batch) while their |d| is below the point's
-// current estimate: exactly those frozen before the point.  Per axis the
-// entered neighbour of least |d| is used (the lower one on ties, as the
-// marcher scans -1 then +1), so per axis only the non-band neighbour of
-// least |d| can matter.  A neighbour that enters lies strictly upwind (the
-// root exceeds its |d| in exact arithmetic); where rounding says otherwise
-// (a noise-level tie) it is left out, so that no two points feed each other
-// and the iteration cannot cycle.  Returns `old` when nothing is known.
+// of it (base_marcher.cpp:98-188): band neighbours (frozen at
+// initialisation) always enter; the other neighbours enter in increasing
+// |d| (equal keys together, as the marcher freezes them in one batch) while
+// their |d| is below the point's current estimate, i.e. they were frozen
+// before the point; after each entry the quadratic of the entered set is
+// the new estimate, or, without a real root, the estimate stays (the
+// marcher's 0 return).  Per axis the entered neighbour of least |d| is used
+// (the lower one on ties, as the marcher scans -1 then +1).  Where
+// rounding makes the new estimate fall below the neighbour that entered (a
+// noise-level tie), the marcher keeps it and freezes the point next, so
+// the point cannot enter that neighbour: each point records the
+// non-band neighbours that entered it (mask bits 2 dim + side), and a
+// neighbour that recorded this point is not a candidate here.  Returns
+// `old` when nothing is known.
 //
 // A one-axis root is v +- h up to the quadratic's cancellation (at most
-// ~eps (v^2 / h + |v| + h)); it is taken in that form where it only decides
+// ~eps (v^2 / h + |v| + h)); it is kept in that form while it only decides
 // whether the next neighbour enters and the decision is clear by 256 times
 // that bound, and evaluated exactly where it is the result or the decision
 // is close.  The result is the same as evaluating every root exactly.
-// |x| as an integer: the order of |x| for finite values and infinity, on
-// the integer pipe (the decisions below then take no FP64 issue slots).
+//
+// |x| compares as the integer of its bits (the order of |x| for finite
+// values and infinity), on the integer pipe.
 GPR_D unsigned long long fmm_key(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
-GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, int nd,
-                        double old, const FmmConst &K) {
+GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], const bool excl[2][2],
+                        bool pos, int nd, double old, const FmmConst &K, int &mask) {
   const double INF = INFINITY;
   const unsigned long long KINF = 0x7ff0000000000000ull;
   double v[2] = {INF, INF}, cv[2] = {INF, INF};
   unsigned long long ck[2] = {KINF, KINF};
+  int cs[2] = {0, 0};
   bool use[2] = {false, false};
   for (int dim = 0; dim < nd; dim++)
     for (int s = 0; s < 2; s++) {
@@ -213,11 +221,13 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, 
           v[dim] = x;
           use[dim] = true;
         }
-      } else if (kx < ck[dim]) {
+      } else if (!excl[dim][s] && kx < ck[dim]) {
         ck[dim] = kx;
         cv[dim] = x;
+        cs[dim] = s;
       }
     }
+  mask = 0;
   double t = INF, tm = 0.0;  // tm > 0: t is v +- h, within tm of the exact root
   if (use[0] || use[1]) {
     double r;
@@ -230,14 +240,13 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, 
     const unsigned long long key = ck[a];
     if (tm > 0.0 && fabs(fabs(cv[a]) - fabs(t)) <= tm) {
       double r;
-      t = fmm_root(v, use, K, nd, pos, r) ? r : INF;
+      if (fmm_root(v, use, K, nd, pos, r))
+        t = r;
       tm = 0.0;
     }
     if (!(key < fmm_key(t)))
       break;
     const bool both = !done[1 - a] && ck[1 - a] == key;
-    const double sv0 = v[0], sv1 = v[1];
-    const bool su0 = use[0], su1 = use[1];
     for (int q = 0; q < 2; q++) {
       const int dim = q == 0 ? a : 1 - a;
       if (q == 1 && !both)
@@ -246,37 +255,38 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], bool pos, 
         v[dim] = cv[dim];
         use[dim] = true;
       }
+      mask |= 1 << (2 * dim + cs[dim]);
       done[dim] = true;
     }
-    double t2, m2 = 0.0;
-    bool ok = true;
     if (use[0] && use[1]) {
-      ok = fmm_root(v, use, K, nd, pos, t2);
+      double r;
+      if (fmm_root(v, use, K, nd, pos, r)) {
+        t = r;
+        tm = 0.0;
+      }
     } else {
       // v +- h of the one entered axis, and the bound of its distance from
       // the marcher's root
       const int k = use[0] ? 0 : 1;
       const double w = fabs(v[k]), h = K.h[k];
-      t2 = pos ? v[k] + h : v[k] - h;
-      m2 = 256.0 * DBL_EPSILON * (w * w / h + w + h);
-      if (!(fabs(t2) > m2) || fabs(fabs(cv[a]) - fabs(t2)) <= m2) {
-        ok = fmm_root(v, use, K, nd, pos, t2);
-        m2 = 0.0;
+      const double t2 = pos ? v[k] + h : v[k] - h;
+      const double m2 = 256.0 * DBL_EPSILON * (w * w / h + w + h);
+      if (fabs(t2) > m2) {
+        t = t2;
+        tm = m2;
+      } else {
+        double r;
+        if (fmm_root(v, use, K, nd, pos, r)) {
+          t = r;
+          tm = 0.0;
+        }
       }
     }
-    if (!ok || !(key < fmm_key(t2))) {
-      v[0] = sv0;
-      v[1] = sv1;
-      use[0] = su0;
-      use[1] = su1;
-      break;
-    }
-    t = t2;
-    tm = m2;
   }
   if (tm > 0.0) {
     double r;
-    t = fmm_root(v, use, K, nd, pos, r) ? r : INF;
+    if (fmm_root(v, use, K, nd, pos, r))
+      t = r;
   }
   return isinf(t) ? old : t;
 }
@@ -328,8 +338,8 @@ template <int ND> struct FmmThreads {
 
 template <int ND>
 __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
-    k_fmm_round(double *__restrict__ d, uint8_t *__restrict__ fz, int *__restrict__ lastg,
-                Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
+    k_fmm_round(double *__restrict__ d, uint8_t *__restrict__ fz, uint8_t *__restrict__ par,
+                int *__restrict__ lastg, Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
                 int nsweeps, int mono, const double *__restrict__ clk) {
   if (clk && clk[0] >= clk[2])
     return;
@@ -355,6 +365,8 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
   __shared__ double sd[SX * SY];
   __shared__ double nvs[NT];
   __shared__ uint8_t sf[SX * SY];
+  __shared__ uint8_t sp[SX * SY];    // the neighbours that entered each point
+  __shared__ uint8_t nms[NT];        // new masks of a sweep's updates
   __shared__ uint8_t hchg[SX * SY];  // halo point changed in the previous round
   __shared__ uint8_t dirty[NT];
   __shared__ uint8_t chg[NT];  // changed in this round
@@ -366,15 +378,17 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
     int a = ND == 2 ? e / SY : e, b = ND == 2 ? e % SY : 0;
     int ii = i0 + a - 1, jj = ND == 2 ? j0 + b - 1 : 0;
     double x = INFINITY;
-    uint8_t f = 0, hc = 0;
+    uint8_t f = 0, hc = 0, pm = 0;
     if (ii >= 0 && ii < g.nx && jj >= 0 && jj < g.ny) {
       long c = (long)ii * g.ny + jj;
       x = d[c];
       f = fz[c];
+      pm = par[c];
       hc = lastg[c] == round - 1;
     }
     sd[e] = x;
     sf[e] = f;
+    sp[e] = pm;
     hchg[e] = hc;
   }
   auto smem_of = [&](int l) {
@@ -447,7 +461,16 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
       double nb[2][2];
       bool bd[2][2];
       fmm_load_nb<ND>(sd, sf, m, o0, nb, bd);
-      nvs[q] = fmm_update(nb, bd, (sf[m] & 2) != 0, ND, sd[m], K);
+      // a neighbour that recorded this point as entered (its bit for the
+      // opposite side) is not a candidate
+      bool ex[2][2];
+      ex[0][0] = (sp[m - o0] >> 1) & 1;
+      ex[0][1] = sp[m + o0] & 1;
+      ex[1][0] = ND == 2 && ((sp[m - 1] >> 3) & 1);
+      ex[1][1] = ND == 2 && ((sp[m + 1] >> 2) & 1);
+      int msk;
+      nvs[q] = fmm_update(nb, bd, ex, (sf[m] & 2) != 0, ND, sd[m], K, msk);
+      nms[q] = (uint8_t)msk;
     }
     __syncthreads();
     // 3. take the new values (from the second half of the round budget on,
@@ -456,8 +479,9 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
     for (int q = threadIdx.x; q < n; q += FMM_THREADS) {
       const int l = list[q], m = smem_of(l);
       const double old = sd[m], nv = nvs[q];
-      if (mono ? fabs(nv) < fabs(old) : nv != old) {
+      if (mono ? fabs(nv) < fabs(old) : (nv != old || nms[q] != sp[m])) {
         sd[m] = nv;
+        sp[m] = nms[q];
         chg[l] = 1;
         const int nbm[4] = {m - o0, m + o0, m - 1, m + 1};
         const int nbl[4] = {ND == 2 ? l - TY : l - 1, ND == 2 ? l + TY : l + 1, l - 1, l + 1};
@@ -477,6 +501,7 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
     const long c = cell_of(l);
     if (chg[l]) {
       d[c] = sd[m];
+      par[c] = sp[m];
       lastg[c] = round;
       wrote = true;
     }

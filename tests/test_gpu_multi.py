@@ -90,6 +90,23 @@ def test_distance_matches_the_marcher(G, O):
         assert np.array_equal(d, ref), (nX, np.max(np.abs(d - ref)), np.mean(d == ref))
 
 
+def test_distance_on_evolved_level_sets(G, O):
+    """Level sets the two-material loop has advected (noise-level ties
+    between neighbours, where the marcher's freezing order decides which
+    enters which): bit-equal to the marcher."""
+    from phd_gb300 import problems
+    for nx, ny, steps in ((200, 100, 40), (400, 200, 30)):
+        u0, MPs, tf, dX, bcs = problems.shock_bubble(nx=nx, ny=ny, mu=1e-4, x_shock=0.36)
+        nX = np.array([nx, ny], np.int32)
+        u, _, _ = O.run_multi(u0, MPs, 1e9, dX, 0, max_steps=steps)
+        phi = np.ascontiguousarray(u[..., -1].ravel())
+        st = torch.zeros(4, dtype=torch.int32, device=DEV)
+        d = G.system.multi.distance(T(phi), dX, nX, status=st).cpu().numpy()
+        assert st.cpu().numpy()[0] == 0
+        ref = O.distance(phi, dX, nX)
+        assert np.array_equal(d, ref), (nx, np.max(np.abs(d - ref)), np.mean(d == ref))
+
+
 def test_distance_against_the_reference_build(G):
     from conftest import golden
     f = golden("distance_v17.npz")
