@@ -124,7 +124,7 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
 // it) and that coefficient's reciprocal rounded to nearest, and the
 // spacings.
 struct FmmConst {
-  double idx2[2], a[3], ra[3], h[2];
+  double idx2[2], a[3], ra[3], h[2], ih[2];
 };
 
 inline FmmConst fmm_const(double dx, double dy) {
@@ -138,6 +138,8 @@ inline FmmConst fmm_const(double dx, double dy) {
     K.ra[k] = 1.0 / K.a[k];
   K.h[0] = dx;
   K.h[1] = dy;
+  K.ih[0] = 1.0 / dx;
+  K.ih[1] = 1.0 / dy;
   return K;
 }
 
@@ -270,7 +272,7 @@ GPR_D double fmm_update(const double nb[2][2], const bool band[2][2], const bool
       const int k = use[0] ? 0 : 1;
       const double w = fabs(v[k]), h = K.h[k];
       const double t2 = pos ? v[k] + h : v[k] - h;
-      const double m2 = 256.0 * DBL_EPSILON * (w * w / h + w + h);
+      const double m2 = 256.0 * DBL_EPSILON * (w * w * K.ih[k] + w + h);
       if (fabs(t2) > m2) {
         t = t2;
         tm = m2;
