@@ -173,16 +173,19 @@ bool grid_ok(const int32_t *nX, int nd) {
 // widths); the budget only bounds a round.
 constexpr int kFmmSweeps = 256;
 
-// Round budget: information crosses at least one tile per round, and the
-// global Jacobi needs about as many sweeps as the longest marching path in
-// cells (678 at 800 x 400); twice the larger of the two, the second half
-// with monotone updates.
-int fmm_rounds(const Grid &g) {
+// Round budget: information crosses at least one tile per round; the
+// 800 x 400 shock bubble needs 43 (static circle) to 54 (advected) of its
+// 75 tile rows plus columns.  Rounds past convergence return at once but
+// still cost a launch, so the budget is that sum plus 16, the last quarter
+// of the sum with monotone updates (which guarantees termination).
+int fmm_tiles_across(const Grid &g) {
   int tiles = g.nd == 1 ? (g.nx + FMM_T1 - 1) / FMM_T1
                         : (g.nx + FMM_T2 - 1) / FMM_T2 + (g.ny + FMM_T2 - 1) / FMM_T2;
   int sweeps = (g.nx + (g.nd == 2 ? g.ny : 0) + kFmmSweeps - 1) / kFmmSweeps;
-  return 2 * (tiles > sweeps ? tiles : sweeps) + 8;
+  return tiles > sweeps ? tiles : sweeps;
 }
+int fmm_rounds(const Grid &g) { return fmm_tiles_across(g) + 16; }
+int fmm_mono_from(const Grid &g) { return fmm_rounds(g) - fmm_tiles_across(g) / 4 - 4; }
 
 // Scratch of one fill (offsets in doubles, 256-byte aligned pieces).
 struct FillLayout {
@@ -245,12 +248,12 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
     int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
     for (int r = 0; r < R; r++)
       k_fmm_round<2><<<nb, FmmThreads<2>::value, 0, st>>>(d, fz, par, lastg, g, K, flags, tflag, r,
-                                                 kFmmSweeps, r >= R / 2, clk);
+                                                 kFmmSweeps, r >= fmm_mono_from(g), clk);
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)
       k_fmm_round<1><<<nb, FmmThreads<1>::value, 0, st>>>(d, fz, par, lastg, g, K, flags, tflag, r,
-                                                 kFmmSweeps, r >= R / 2, clk);
+                                                 kFmmSweeps, r >= fmm_mono_from(g), clk);
   }
   k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, u, g.ncell, cnt, flags, R - 1, err,
                                                           clk);
