@@ -124,7 +124,7 @@ __global__ void k_fmm_init(const double *__restrict__ phi, long ps, double *__re
 // it) and that coefficient's reciprocal rounded to nearest, and the
 // spacings.
 struct FmmConst {
-  double idx2[2], a[3], ra[3], h[2], ih[2];
+  double idx2[2], a[3], a4[3], ra[3], h[2], ih[2];
 };
 
 inline FmmConst fmm_const(double dx, double dy) {
@@ -134,8 +134,10 @@ inline FmmConst fmm_const(double dx, double dy) {
   K.a[0] = K.idx2[0];
   K.a[1] = K.idx2[1];
   K.a[2] = K.idx2[0] + K.idx2[1];
-  for (int k = 0; k < 3; k++)
+  for (int k = 0; k < 3; k++) {
+    K.a4[k] = 4.0 * K.a[k];
     K.ra[k] = 1.0 / K.a[k];
+  }
   K.h[0] = dx;
   K.h[1] = dy;
   K.ih[0] = 1.0 / dx;
@@ -158,16 +160,17 @@ inline FmmConst fmm_const(double dx, double dy) {
 // false return here.
 GPR_D bool fmm_root(const double v[2], const bool use[2], const FmmConst &K, int nd, bool pos,
                     double &x) {
-  double a = 0.0, b = 0.0, c = 0.0;
+  // a (the sum of the entered idx2, in the marcher's order) and 4a are
+  // tabulated per set of entered axes
+  double b = 0.0, c = 0.0;
   for (int dim = 0; dim < nd; dim++)
     if (use[dim]) {
-      a = add(a, K.idx2[dim]);
       b = __fma_rn(-mul(K.idx2[dim], 2.0), v[dim], b);
       c = __fma_rn(K.idx2[dim], mul(v[dim], v[dim]), c);
     }
   const int ka = use[0] && use[1] ? 2 : (use[0] ? 0 : 1);
   c = sub(c, 1.0);
-  const double det = __fma_rn(b, b, -mul(mul(4.0, a), c));
+  const double det = __fma_rn(b, b, -mul(K.a4[ka], c));
   if (!(det > 0.0))
     return false;
   const double sq = __dsqrt_rn(det);
