@@ -333,16 +333,19 @@ GPR_D void fmm_load_nb(const double *src, const uint8_t *sf, int m, int o0, doub
 // changed in the previous round (tflag bit 1 / bit 0 of round - 1);
 // flags[round] records whether anything changed or waits, and a round after
 // a round without either returns at once.  2D tiles are 32 x 32 cells, 1D
-// tiles 1024 (16 x 16 tiles cross the 800 x 400 grid in 1344 sweeps with
-// 34 updates per cell, 32 x 32 ones in 1392 with 49, and spread the front
-// over more SMs); each thread owns one 2D cell or two 1D cells.
-constexpr int FMM_T2 = 16, FMM_T1 = 1024;
+// tiles 1024.  On the 800 x 400 shock bubble 8 x 8 tiles take the step
+// from 23.8 to 22.5 ms against 16 x 16 ones: the front's tiles spread over
+// more SMs, though the sweeps make more updates (33 per cell on the static
+// circle, 91 after 13 steps of advection, against 34 and 60) along about
+// the same chain of 1350-1650 dependent sweeps.  Each thread owns one 2D
+// cell or two 1D cells.
+constexpr int FMM_T2 = 8, FMM_T1 = 1024;
 template <int ND> struct FmmThreads {
-  static constexpr int value = ND == 2 ? 256 : 512;
+  static constexpr int value = ND == 2 ? 64 : 512;
 };
 
 template <int ND>
-__global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 4 : 2)
+__global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 16 : 2)
     k_fmm_round(double *__restrict__ d, uint8_t *__restrict__ fz, uint8_t *__restrict__ par,
                 int *__restrict__ lastg, Grid g, FmmConst K, int *__restrict__ flags, int *__restrict__ tflag, int round,
                 int nsweeps, int mono, const double *__restrict__ clk) {
