@@ -8,25 +8,35 @@
 namespace gpr {
 
 // Symmetric 3x3 eigen-decomposition S = W diag(d) W^T by cyclic Jacobi
-// rotations (fixed sweep budget, register resident).
+// rotations (register resident).  The ODE step is one lane's serial FP64
+// chain per cell, so each rotation takes its tangent in one division,
+// t = sgn(d) e / (|d| + sqrt(d^2 + e^2)) with d = S_qq - S_pp, e = 2 S_pq
+// (the same t as sgn(theta) / (|theta| + sqrt(theta^2 + 1)), theta = d / e),
+// and c = rsqrt(t^2 + 1); the sweeps stop once the off-diagonal sum is
+// below 2^-60 of the trace (S = A^T A is positive semidefinite), where a
+// further rotation moves the eigenvalues by less than a rounding and the
+// eigenvectors only within a subspace of equal eigenvalues, which the
+// distortion update A' = U diag(s') V^T does not see.
 GPR_D void jacobi3(double S[3][3], double W[3][3], double d[3]) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       W[i][j] = i == j ? 1.0 : 0.0;
+  const double stop = 0x1p-60 * (S[0][0] + S[1][1] + S[2][2]);
   for (int sweep = 0; sweep < 12; sweep++) {
     double off = fabs(S[0][1]) + fabs(S[0][2]) + fabs(S[1][2]);
-    if (off == 0.0)
+    if (off <= stop)
       break;
 #pragma unroll
     for (int pq = 0; pq < 3; pq++) {
       const int p = pq == 2 ? 1 : 0;
       const int q = pq == 0 ? 1 : 2;
       if (S[p][q] != 0.0) {
-        double theta = (S[q][q] - S[p][p]) / (2.0 * S[p][q]);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        const double dd = S[q][q] - S[p][p], e = 2.0 * S[p][q];
+        const double rr = sqrt(dd * dd + e * e);
+        double t = (dd >= 0 ? e : -e) / (fabs(dd) + rr);
+        double c = rsqrt(t * t + 1.0), s = t * c;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
           double a = S[k][p], b = S[k][q];
@@ -154,27 +164,31 @@ GPR_D void ode_distortion(double *q, double dt, const DevPar &P) {
   double d13 = cbrt(detA);
   double id23 = 1.0 / (d13 * d13);
   double s0 = s[0] * s[0] * id23, s1 = s[1] * s[1] * id23, s2 = s[2] * s[2] * id23;
-  double m0 = (s0 + s1 + s2) / 3.;
-  double u0 = ((s0 - s1) * (s0 - s1) + (s1 - s2) * (s1 - s2) + (s2 - s0) * (s2 - s0)) / 3.;
+  // divisions by constants as products with the rounded reciprocal (one
+  // rounding apart; each IEEE division is a long FP64 sequence on this
+  // one-lane chain)
+  const double third = 1.0 / 3.0;
+  double m0 = (s0 + s1 + s2) * third;
+  double u0 = ((s0 - s1) * (s0 - s1) + (s1 - s2) * (s1 - s2) + (s2 - s0) * (s2 - s0)) * third;
   if (u0 < 1e-12)
     return;
   double tau = nondim_time(r, d13, m0, u0, dt, P);
   double e6 = exp(-6. * tau), e9 = exp(-9. * tau);
-  double a = 3. * m0 - u0 / 3. - 3.;
-  double b = 2. * m0 - u0 / 3. - 2.;
+  double a = 3. * m0 - u0 * third - 3.;
+  double b = 2. * m0 - u0 * third - 2.;
   double m = 1. + a * e6 - b * e9;
   double u = posd(6. * a * e6 - 9. * b * e9);
   double Dl = -2. * m * m * m + m * u + 2.;
   double arg1 = posd(6. * u * u * u - 81. * Dl * Dl);
   double x1;
   if (fabs(Dl) < 1e-12)
-    x1 = sqrt(6. * u) / 3. * 0.86602540378443864676 + m;  // cos(pi/6)
+    x1 = sqrt(6. * u) * third * 0.86602540378443864676 + m;  // cos(pi/6)
   else if (arg1 == 0.) {
     double tmp = cbrt(54. * Dl);
-    x1 = tmp / 6. + u / tmp + m;
+    x1 = tmp * (1.0 / 6.0) + u / tmp + m;
   } else {
     double th = atan(sqrt(arg1) / (9. * Dl));
-    x1 = sqrt(6. * u) / 3. * cos(th / 3.) + m;
+    x1 = sqrt(6. * u) * third * cos(th * third) + m;
   }
   double tmp2 = 3. * m - x1;
   double arg2 = posd(x1 * tmp2 * tmp2 - 4.);
