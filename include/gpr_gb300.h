@@ -469,10 +469,22 @@ int gpr_adj_point_vjp(const double *Q, int64_t count, const gpr_par *par, const 
  * gpr_timestep_multi       solvers/iterator.cpp:54-83 over the masked cells of
  *                          both grids; dt_out is a device double; scratch: 1 double.
  * gpr_iterate_multi        GPRpy.solvers.iterator (solvers/iterator.cpp:85-170)
- *                          with the ghost fill, ADER scheme, Rusanov flux,
- *                          device resident as gpr_iterate; clock[5] as there
- *                          (set dt = 0 before the first step); scratch:
- *                          gpr_iterate_multi_scratch_doubles. */
+ *                          with the ghost fill, ADER scheme, flux
+ *                          GPR_FLUX_* (Rusanov, Roe or Osher), device
+ *                          resident as gpr_iterate; clock[5] as there (set
+ *                          dt = 0 before the first step); scratch:
+ *                          gpr_iterate_multi_scratch_doubles.
+ * gpr_iterate_multi_scheme the same loop with the reference iterator's
+ *                          SPLIT, HALF_STEP and STIFF arguments
+ *                          (iterator.cpp:85-88, 123-129): split != 0 steps
+ *                          each material with the split scheme (ODE half
+ *                          steps around the homogeneous WENO [-> midstepper
+ *                          when half_step] -> FV step, as
+ *                          gpr_split_stepper); otherwise the ADER step, its
+ *                          predictor straight to the Newton iteration when
+ *                          stiff != 0 (as gpr_predictor).  The reference's
+ *                          Python driver runs this loop with SPLIT = True,
+ *                          FLUX = 1 (code/python/main.py:19-22, 43-45). */
 long gpr_distance_scratch_doubles(const int32_t *nX, int ndim);
 int gpr_distance(const double *phi, double *dist, const int32_t *nX, int ndim,
                  const double *dX, double *scratch, int32_t *status, void *stream);
@@ -507,6 +519,11 @@ int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
                       const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
                       double *clock, int nsteps, double *scratch, int32_t *status,
                       double contorted_tol, int nvar, void *stream);
+int gpr_iterate_multi_scheme(double *u, const int32_t *nX, int ndim, const double *dX,
+                             const int32_t *bcs, int split, int half_step, int stiff, int flux,
+                             const gpr_par *pars, int nmat, double *clock, int nsteps,
+                             double *scratch, int32_t *status, double contorted_tol, int nvar,
+                             void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Pointwise physics (GPRpy.system.*, code/cpp/src/system/equations.cpp,

@@ -507,12 +507,13 @@ class Oracle:
         return u
 
     def step_multi(self, u, dt_prev, t, tf, count, MPs, dX, bcs, cfl=0.8, dt=None,
-                   contorted_tol=None):
+                   contorted_tol=None, split=False, half_step=True, stiff=False, flux=0):
         """One step of the time loop of solvers/iterator.cpp:85-151 with the
         ghost-fluid fill (LSET = 1): fill (with the previous step's dt) ->
-        timestep -> per material boundaries + ADER step on its masked cells
-        -> make_u -> renorm.  u (flat or shaped, cell-major) is updated in
-        place; `dt` overrides the CFL step.  Returns dt."""
+        timestep -> per material boundaries + the ADER step (or the split
+        step, iterator.cpp:123-129) on its masked cells -> make_u -> renorm.
+        u (flat or shaped, cell-major) is updated in place; `dt` overrides
+        the CFL step.  Returns dt."""
         nd = len(dX)
         ncell = u.size // self.V
         nX = np.asarray(u.shape[:-1] if u.ndim > 1 else [ncell], dtype=np.int32)
@@ -531,7 +532,12 @@ class Oracle:
             g = np.ascontiguousarray(grids[mat]).ravel()
             ub = self.boundaries(g, nX, bc)
             maskb = self.extend_mask(masks[mat].astype(np.uint8), nX)
-            self.ader_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb)
+            if split:
+                self.split_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb, flux=flux,
+                                   half_step=half_step)
+            else:
+                self.ader_stepper(g, ub, nX, dt, dX, MPs[mat], mask=maskb, flux=flux,
+                                  stiff=stiff)
             grids[mat] = g.reshape(ncell, self.V)
         self.make_u(uf, grids, masks, MPs)
         self.renorm_multi(uf, MPs)
@@ -539,14 +545,16 @@ class Oracle:
             self.reset_contorted(uf, contorted_tol, MPs)
         return dt
 
-    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None, contorted_tol=None):
+    def run_multi(self, u0, MPs, tf, dX, bcs, cfl=0.8, max_steps=None, contorted_tol=None,
+                  split=False, half_step=True, stiff=False, flux=0):
         """The two-material time loop (step_multi until tf).  Returns
         (u, steps, t)."""
         u = np.ascontiguousarray(u0, dtype=np.float64).copy()
         t, count, dt = 0.0, 0, 0.0
         while t < tf:
             dt = self.step_multi(u, dt, t, tf, count, MPs, dX, bcs, cfl,
-                                 contorted_tol=contorted_tol)
+                                 contorted_tol=contorted_tol, split=split,
+                                 half_step=half_step, stiff=stiff, flux=flux)
             t += dt
             count += 1
             if max_steps is not None and count >= max_steps:

@@ -54,12 +54,12 @@ def _two_materials(u, MPs):
 def _iterator(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
               contorted_tol=1.0, max_steps=None):
     """solvers.iterator: the two-material ghost-fluid loop for V = 15 and two
-    materials (ADER, Rusanov), else the one-material loop."""
+    materials, else the one-material loop; both take the reference's SPLIT,
+    HALF_STEP, STIFF and FLUX."""
     if _two_materials(u, MPs):
-        if SPLIT or FLUX != 0 or STIFF:
-            raise RuntimeError("the ghost-fluid loop runs the ADER scheme with Rusanov flux")
         return _multi.iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=max_steps,
-                              contorted_tol=contorted_tol)
+                              contorted_tol=contorted_tol, SPLIT=SPLIT, HALF_STEP=HALF_STEP,
+                              STIFF=STIFF, FLUX=FLUX)
     from .driver import iterate
     return iterate(u, tf, nX, dX, CFL, boundaryTypes, SPLIT, HALF_STEP, STIFF, FLUX, MPs,
                    max_steps=max_steps, contorted_tol=contorted_tol)

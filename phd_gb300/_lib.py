@@ -138,6 +138,8 @@ SIGNATURES = {
     "gpr_timestep_multi": (_I, [_P, _P, _I64, _P, _I, _D, _D, _D, _I, _P, _I, _P, _P, _I, _P]),
     "gpr_iterate_multi_scratch_doubles": (_L, [_P, _I, _I]),
     "gpr_iterate_multi": (_I, [_P, _P, _I, _P, _P, _I, _P, _I, _P, _I, _P, _P, _D, _I, _P]),
+    "gpr_iterate_multi_scheme": (_I, [_P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _I, _P, _I, _P,
+                                      _P, _D, _I, _P]),
     "gpr_flux": (_I, [_P, _P, _I64, _I, _P, _I, _P]),
     "gpr_source": (_I, [_P, _P, _I64, _P, _I, _P]),
     "gpr_Bdot": (_I, [_P, _P, _P, _I64, _I, _P, _I, _P]),

@@ -545,23 +545,25 @@ long gpr_iterate_multi_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
   return multi_layout(nX, ndim, make_grid(nX, ndim, dX)).total;
 }
 
-// The two-material loop of solvers/iterator.cpp:85-170 (LSET > 0, ADER
-// scheme): fill -> CFL over the masked cells of both grids -> per material
-// boundaries, extended mask and the masked ADER step -> make_u -> renorm
-// -> contortion check and reset (solvers/utils.cpp:44-85) -> clock.  The
-// clock {t, dt, tf, cfl, count} lives on the device; the fill of a step uses
-// the previous step's dt, as the reference does.
-int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
-                      const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
-                      double *clock, int nsteps, double *scratch, int32_t *status,
-                      double contorted_tol, int nvar, void *stream) {
+// The two-material loop of solvers/iterator.cpp:85-170 (LSET > 0): fill ->
+// CFL over the masked cells of both grids -> per material boundaries,
+// extended mask and the masked step (the ADER scheme, or the split scheme
+// when split != 0, iterator.cpp:123-129) -> make_u -> renorm -> contortion
+// check and reset (solvers/utils.cpp:44-85) -> clock.  The clock
+// {t, dt, tf, cfl, count} lives on the device; the fill of a step uses the
+// previous step's dt, as the reference does.
+static int iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
+                         const int32_t *bcs, int split, int half_step, int stiff, int flux,
+                         const gpr_par *pars, int nmat, double *clock, int nsteps,
+                         double *scratch, int32_t *status, double contorted_tol, int nvar,
+                         void *stream) {
   if (!u || !dX || !bcs || !clock || !scratch || !status || nsteps < 0 || !grid_ok(nX, ndim))
     return GPR_E_ARG;
   for (int i = 0; i < 2 * ndim; i++)
     if (bcs[i] < 0 || bcs[i] > 5)
       return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return GPR_E_UNSUPPORTED;
+  if (flux != GPR_FLUX_RUSANOV && flux != GPR_FLUX_ROE && flux != GPR_FLUX_OSHER)
+    return GPR_E_ARG;
   if (nvar != V15)
     return GPR_E_UNSUPPORTED;
   DevPar P[2];
@@ -596,9 +598,17 @@ int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
         return rc;
       if ((rc = gpr_extend_mask(masks + (long)m * g.ncell, maskb, nX, ndim, st)))
         return rc;
+      if (split) {
+        // split_stepper's scratch (wh, then the WENO / FV temporary) spans
+        // the wh, qh and tmp regions, which lie back to back
+        if ((rc = Ops<L15>::split_stepper(grid, ub, nX, ndim, 0.0, dt_dev, dX, half_step, flux,
+                                          P[m], maskb, wh, st)))
+          return rc;
+        continue;
+      }
       if ((rc = Ops<L15>::weno(wh, ub, nX, ndim, tmp, st)))
         return rc;
-      if ((rc = Ops<L15>::predictor(qh, wh, 0.0, dt_dev, dX, ndim, nX, 0, P[m], maskb, pst,
+      if ((rc = Ops<L15>::predictor(qh, wh, 0.0, dt_dev, dX, ndim, nX, stiff, P[m], maskb, pst,
                                     st)))
         return rc;
       if ((rc = Ops<L15>::fv(grid, qh, nX, 0.0, dt_dev, dX, ndim, 1, 1, P[m], maskb, tmp, st,
@@ -614,6 +624,23 @@ int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
     k_clock_advance<<<1, 1, 0, st>>>(clock);
   }
   return cuda_rc();
+}
+
+int gpr_iterate_multi(double *u, const int32_t *nX, int ndim, const double *dX,
+                      const int32_t *bcs, int flux, const gpr_par *pars, int nmat,
+                      double *clock, int nsteps, double *scratch, int32_t *status,
+                      double contorted_tol, int nvar, void *stream) {
+  return iterate_multi(u, nX, ndim, dX, bcs, 0, 0, 0, flux, pars, nmat, clock, nsteps,
+                       scratch, status, contorted_tol, nvar, stream);
+}
+
+int gpr_iterate_multi_scheme(double *u, const int32_t *nX, int ndim, const double *dX,
+                             const int32_t *bcs, int split, int half_step, int stiff, int flux,
+                             const gpr_par *pars, int nmat, double *clock, int nsteps,
+                             double *scratch, int32_t *status, double contorted_tol, int nvar,
+                             void *stream) {
+  return iterate_multi(u, nX, ndim, dX, bcs, split, half_step, stiff, flux, pars, nmat, clock,
+                       nsteps, scratch, status, contorted_tol, nvar, stream);
 }
 
 }  // extern "C"

@@ -249,8 +249,11 @@ def timestep_device(grids, masks, dX, CFL, t, tf, count, MPs, out=None):
 class MultiIterator:
     """Device buffers of the two-material time loop (gpr_iterate_multi)."""
 
-    def __init__(self, nX, dX, bcs, MPs, cfl, tf, device="cuda", contorted_tol=1.0):
+    def __init__(self, nX, dX, bcs, MPs, cfl, tf, device="cuda", contorted_tol=1.0,
+                 split=False, half_step=True, stiff=False, flux=0):
         self.lib = _lib.load()
+        self.split, self.half_step = int(bool(split)), int(bool(half_step))
+        self.stiff, self.flux = int(bool(stiff)), int(flux)
         self.nX, self.pn = _i32(nX)
         self.dX, self.pd = _f64(dX)
         self.nd = self.nX.size
@@ -265,20 +268,24 @@ class MultiIterator:
 
     def run(self, u, nsteps):
         """Enqueue nsteps steps on u (in place); no host synchronisation."""
-        _lib.check(self.lib.gpr_iterate_multi(
-            _dev(u, "u"), self.pn, self.nd, self.pd, self.pb, 0, self.pp, 2,
-            _dev(self.clock, "clock"), int(nsteps), _dev(self.scr, "s"),
-            _dev(self.status, "status", torch.int32), self.contorted_tol, V, _stream()),
-            "iterate_multi")
+        _lib.check(self.lib.gpr_iterate_multi_scheme(
+            _dev(u, "u"), self.pn, self.nd, self.pd, self.pb, self.split, self.half_step,
+            self.stiff, self.flux, self.pp, 2, _dev(self.clock, "clock"), int(nsteps),
+            _dev(self.scr, "s"), _dev(self.status, "status", torch.int32), self.contorted_tol,
+            V, _stream()), "iterate_multi")
         return u
 
 
-def iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=None, contorted_tol=1.0):
+def iterate(u, tf, nX, dX, CFL, boundaryTypes, MPs, max_steps=None, contorted_tol=1.0,
+            SPLIT=False, HALF_STEP=True, STIFF=False, FLUX=0):
     """GPRpy.solvers.iterator (solvers/iterator.cpp:85-170) with the ghost
-    fill (ADER scheme, Rusanov flux): the reference's 100-snapshot list, with
-    the NaN early exit and the contortion reset."""
+    fill: the ADER scheme (STIFF: predictor straight to the Newton pass) or
+    the split scheme (SPLIT, HALF_STEP), flux FLUX (0 Rusanov, 1 Roe,
+    2 Osher); the reference's 100-snapshot list, with the NaN early exit and
+    the contortion reset."""
     it = MultiIterator(nX, dX, boundaryTypes, MPs, CFL, tf, device=u.device,
-                       contorted_tol=contorted_tol)
+                       contorted_tol=contorted_tol, split=SPLIT, half_step=HALF_STEP,
+                       stiff=STIFF, flux=FLUX)
     uf = u.view(-1)
     ret = [None] * 100
     push, count = 0, 0

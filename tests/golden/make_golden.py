@@ -224,6 +224,56 @@ def multi(R, name):
     print("wrote", name)
 
 
+def multi_schemes(R, name):
+    """The two-material loop (solvers/iterator.cpp:85-170, LSET = 1) with
+    the reference driver's own scheme, SPLIT = True and FLUX = 1 (Roe,
+    code/python/main.py:19-22), and with the other schemes and fluxes, on
+    the 1D helium bubble (200 cells) and a 40 x 20 shock bubble, both with
+    sheared distortions.  For the longer 1D split run (52 steps) the
+    reference's own response to 1e-15 relative noise on u0 is stored beside
+    it: the split scheme's analytic distortion step is ill-conditioned at
+    near-isotropic distortions, so rounding grows along that run."""
+    out = {}
+    rng = np.random.default_rng(SEED + 11)
+    cases = [  # (label, problem, tf, SPLIT, HALF_STEP, FLUX)
+        ("h_split_roe", "1d", 0.01, True, True, 1),
+        ("h_split_rus_nohalf", "1d", 0.01, True, False, 0),
+        ("h_ader_osh", "1d", 0.01, False, True, 2),
+        ("h_ader_roe_long", "1d", 0.05, False, True, 1),
+        ("h_split_roe_long", "1d", 0.05, True, True, 1),
+        ("b_split_roe", "2d", 0.004, True, True, 1),
+        ("b_ader_osh", "2d", 0.004, False, True, 2),
+    ]
+    for label, kind, tf, split, half, flux in cases:
+        if kind == "1d":
+            u, MPs, _, dX, _ = problems.helium_bubble_1d(nx=200, shear=0.3)
+        else:
+            u, MPs, _, dX, _ = problems.shock_bubble(nx=40, ny=20, mu=1e-2, shear=0.3)
+        nX = np.array(u.shape[:-1], np.int32)
+        RM = [rd.to_ref_par(R, m) for m in MPs]
+        bc = np.zeros(2 * nX.size, np.int32)
+
+        def run(u0):
+            ret = R.iterator_multi(u0.ravel().copy(), tf, nX, np.array(dX), 0.8, bc, split,
+                                   half, False, flux, RM, 1e9)
+            return np.asarray(ret[99]).reshape(u.shape)
+
+        end = run(u)
+        sens = np.zeros(u.shape[:-1])
+        if label.endswith("_long"):
+            for _ in range(3):
+                un = u * (1 + 1e-15 * rng.standard_normal(u.shape))
+                e = np.max(np.abs(run(un) - end) / (1 + np.abs(end)), axis=-1)
+                sens = np.maximum(sens, e)
+        out.update({label + "_u0": u, label + "_u_end": end, label + "_dX": np.array(dX),
+                    label + "_opts": np.array([tf, split, half, flux], np.float64),
+                    label + "_sens": sens,
+                    label + "_mp": np.stack([MP.to_array() for MP in MPs])})
+    out["labels"] = np.array([c[0] for c in cases])
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print("wrote", name)
+
+
 def contortion(R, name):
     """contorted + reset_distortion (solvers/utils.cpp:44-85): random
     distorted states, and the reference's own time loop (iterator.cpp:85-170
@@ -352,6 +402,14 @@ def main():
         R15 = rd.load("v15")
         multi(R15, "multi_v15.npz")
         contortion_multi(R15, "contortion_v15.npz")
+        multi_schemes(R15, "multi_schemes_v15.npz")
+        return 0
+    if variant == "v15schemes":  # the two-material scheme fixtures alone
+        R15 = rd.load("v15")
+        if R15 is None:
+            print("oracle/_ref/GPRref_v15 not built; run oracle/build_ref.py v15")
+            return 1
+        multi_schemes(R15, "multi_schemes_v15.npz")
         return 0
     R = rd.load("v17")
     if R is None:

@@ -6,6 +6,14 @@ import importlib
 import os
 import sys
 
+# One OpenMP thread, set before the reference module (and its OpenMP
+# runtime) loads: the reference's 2D boundary fill is an OpenMP loop whose
+# iterations read cells that other iterations write (multi/fill.cpp:220-233),
+# so with several threads its result depends on the schedule (8e-4 on a
+# 40 x 20 shock bubble after 4 steps).  One thread gives the loop's
+# sequential (i, j) order, the order the oracle and the device fill follow.
+os.environ["OMP_NUM_THREADS"] = "1"
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))

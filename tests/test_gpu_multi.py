@@ -415,3 +415,65 @@ def test_config3_fill_against_oracle(G, O):
     assert np.mean(cell <= np.maximum(1e-10, 10 * r)) >= 0.99
     assert np.mean(cell <= 1e-10) >= np.mean(r <= 1e-10) - 0.02, (
         np.mean(cell <= 1e-10), np.mean(r <= 1e-10))
+
+
+def test_loop_schemes_against_reference(G, O):
+    """gpr_iterate_multi_scheme through phd_gb300.solvers.iterator (the
+    reference's entry point, with its driver's SPLIT = True, FLUX = 1) and
+    MultiIterator: the split scheme with and without the midstepper and the
+    ADER scheme with Roe and Osher fluxes, 1D helium bubble and 2D shock
+    bubble, sheared distortions, against the reference's own loop
+    (multi_schemes_v15.npz).  Bars as the oracle's against the same
+    fixtures: 1e-10, and for the 52-step 1D split run each cell within
+    1e-10 plus 10x the reference's own response to 1e-15 noise on u0."""
+    from phd_gb300.ghost import MultiIterator
+    gs = golden("multi_schemes_v15.npz")
+    for lab in map(str, gs["labels"]):
+        tf, split, half, flux = gs[lab + "_opts"]
+        MPs = [Par.from_array(a) for a in gs[lab + "_mp"]]
+        u0, dX = gs[lab + "_u0"], list(gs[lab + "_dX"])
+        nX = np.array(u0.shape[:-1], np.int32)
+        ref = gs[lab + "_u_end"]
+        bar = 1e-10 + 10 * gs[lab + "_sens"]
+        if lab == "h_split_roe":
+            ret = G.solvers.iterator(T(u0), float(tf), nX, dX, 0.8,
+                                     np.zeros(2 * nX.size, np.int32), True, True, False, 1,
+                                     MPs, contorted_tol=1e9)
+            got = ret[99].cpu().numpy().reshape(u0.shape)
+        else:
+            it = MultiIterator(nX, dX, 0, MPs, 0.8, float(tf), device=DEV, contorted_tol=1e9,
+                               split=bool(split), half_step=bool(half), flux=int(flux))
+            ut = T(u0.ravel())
+            it.run(ut, 80)  # steps past tf change nothing
+            assert it.clock.tolist()[0] >= tf
+            got = ut.cpu().numpy().reshape(u0.shape)
+            assert (it.status.cpu().numpy() == 0).all()
+        err = np.max(np.abs(got - ref) / (1 + np.abs(ref)), axis=-1)
+        assert (err <= bar).all(), (lab, float(err.max()))
+
+
+def test_loop_stiff_against_oracle(G, O):
+    """STIFF = True with two materials: the ADER predictor of both material
+    grids goes straight to the Newton pass (gpr_predictor's stiff), each
+    step of the device loop against one oracle step (its Newton predictor,
+    to the same 1e-11 tolerance) from the device's previous state and dt,
+    1D helium bubble, Rusanov and Osher.  Bar 1e-9 per step (the two Newton
+    iterations stop at 1e-11 on differently rounded iterates)."""
+    from phd_gb300 import problems
+    from phd_gb300.ghost import MultiIterator
+    u0, MPs, tf, dX, bcs = problems.helium_bubble_1d(nx=200, shear=0.3)
+    nX = np.array([200], np.int32)
+    for flux in (0, 2):
+        it = MultiIterator(nX, dX, 0, MPs, 0.8, 1e9, device=DEV, stiff=True, flux=flux)
+        ut = T(u0.ravel())
+        prev = u0.copy()
+        dt_prev, t = 0.0, 0.0
+        for s in range(6):
+            it.run(ut, 1)
+            t1, dt, _, _, cnt = it.clock.tolist()
+            ref = prev.copy()
+            O.step_multi(ref, dt_prev, t, 1e9, s, MPs, dX, 0, dt=dt, contorted_tol=1.0,
+                         stiff=True, flux=flux)
+            got = ut.cpu().numpy().reshape(u0.shape)
+            assert rel_err(got, ref) < 1e-9, (flux, s, rel_err(got, ref))
+            prev, dt_prev, t = got, dt, t1
