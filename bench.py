@@ -611,11 +611,10 @@ def run_gb300(args):
             "shock_bubble": bubble,
             "adjoint": adjoint,
             # kernels of one 2D gpr_iterate step: k_cfl_max, k_clock_finalize,
-            # k_fill_interior, k_ghosts x2, k_weno2d_x, k_weno2d_y,
-            # k_predictor_first, k_predictor_picard, k_predictor_stiff,
-            # k_faces2d x2, k_cells, k_renorm, k_contorted, k_reset_distortion,
-            # k_clock_advance
-            "gpu_launches": 17 * args.steps,
+            # k_fill_interior, k_ghosts x2, k_weno2d, k_predictor_first,
+            # k_predictor_picard, k_predictor_stiff, k_cells, k_faces2d x4,
+            # k_renorm, k_contorted, k_reset_distortion, k_clock_advance
+            "gpu_launches": 18 * args.steps,
             "clocks": cs.summary()}
     if peak_err:
         line["roofline"]["peak_error"] = peak_err
@@ -1382,14 +1381,22 @@ def stage_times(lib, torch, u, MP, nX, dXa, bc, cfl, V, dev, sp, stream, reps=3)
     e1.record(stream)
     torch.cuda.synchronize()
     acc["cfl"] = e0.elapsed_time(e1) / reps
-    # the FV face pass alone (the two k_faces2d launches of the fv stage)
+    # the two parts of the fv stage alone: the face terms (four in-place
+    # k_faces2d passes) and the volume term (k_cells)
     fe0.record(stream)
     for _ in range(reps):
-        _lib.check(lib.gpr_fv_face_fluxes(P(qh), pn, dt, pd, 2, 1, 0, pp, None, P(ws), V, sp),
-                   "faces")
+        _lib.check(lib.gpr_fv_interfs(P(uu), P(qh), pn, dt, pd, 2, 1, 0, pp, None, P(ws), V,
+                                      sp), "faces")
     fe1.record(stream)
     torch.cuda.synchronize()
     acc["faces"] = fe0.elapsed_time(fe1) / reps
+    fe0.record(stream)
+    for _ in range(reps):
+        _lib.check(lib.gpr_fv_centers(P(uu), P(qh), pn, dt, pd, 2, 1, 1, pp, None, V, sp),
+                   "centers")
+    fe1.record(stream)
+    torch.cuda.synchronize()
+    acc["centers"] = fe0.elapsed_time(fe1) / reps
     acc["_mean_picard_iterations_stage_run"] = float((st.cpu().numpy() >> 8).mean())
     return acc
 
@@ -1401,16 +1408,16 @@ def roofline(stage_ms, ncell, n, mean_iters, peak):
     nf = (n + 1) ** 2  # faces per direction
     # kernel: (time per launch ms, algorithmic flops per launch)
     kern = {
-        "k_faces2d": (stage_ms["faces"] / 2, OPS["face_quadrature_point"] * 4 * nf),
+        # four in-place passes (x / y faces, even / odd), half the faces each
+        "k_faces2d": (stage_ms["faces"] / 4, OPS["face_quadrature_point"] * 4 * nf / 2),
         # the first iteration runs at one thread per spatial node
         # (k_predictor_first): half the per-iteration work
         "k_predictor_picard": (stage_ms["predictor"],
                                OPS["predictor_per_cell_iter"] * ncb * (mean_iters - 0.5)),
-        "k_cells": (max(stage_ms["fv"] - stage_ms["faces"], 1e-9),
-                    OPS["cells_per_cell"] * ncell),
+        "k_cells": (stage_ms["centers"], OPS["cells_per_cell"] * ncell),
         "k_cfl_max": (stage_ms["cfl"], OPS["cfl_per_cell"] * ncell),
     }
-    per_step = {"k_faces2d": 2 * kern["k_faces2d"][0], "k_predictor_picard": kern["k_predictor_picard"][0],
+    per_step = {"k_faces2d": 4 * kern["k_faces2d"][0], "k_predictor_picard": kern["k_predictor_picard"][0],
                 "k_cells": kern["k_cells"][0], "k_cfl_max": kern["k_cfl_max"][0]}
     dom = max(per_step, key=per_step.get)
     out = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": peak,

@@ -107,9 +107,10 @@ int gpr_extend_mask(const uint8_t *mask, uint8_t *maskb, const int32_t *nX,
 
 /* Replaces GPRpy.solvers.weno.weno_launcher (solvers/weno/weno.h:6,
  * weno.cpp:126-157): WENO reconstruction of ub into wh over the nx+2 (x ny+2)
- * predictor cells.  2D needs caller scratch of
- * gpr_weno_scratch_doubles(nX, 2, nvar) doubles (the x-sweep result);
- * 1D needs none (scratch may be NULL). */
+ * predictor cells.  In 2D both sweeps run in one launch, the x sweep's
+ * result kept in shared memory; the scratch argument and its size query
+ * gpr_weno_scratch_doubles(nX, 2, nvar) (the x-sweep result of a two-pass
+ * form) are kept for callers that pass them, and scratch may be NULL. */
 long gpr_weno_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX,
                       int ndim, double *scratch, int nvar, void *stream);
@@ -133,9 +134,14 @@ int gpr_predictor(double *qh, const double *wh, double dt, const double *dX,
 
 /* Replaces solvers.fv.fv_launcher (solvers/fv/fv.h:17, fv.cpp:281-297):
  * u += space-time quadrature of the non-conservative/source terms
- * (SOURCES, TIME) and the path-conservative interface fluxes.  Caller
- * scratch of gpr_fv_scratch_doubles(nX, ndim, nvar) doubles holds the face
- * fluxes. */
+ * (SOURCES, TIME) and the path-conservative interface fluxes.  With the
+ * Rusanov flux the face terms are applied to u inside the face kernels, as
+ * the reference's interfs1/2 update u inside their face loops: in 2D by
+ * four passes (x / y faces of even / odd index, which never share a cell),
+ * in 1D in one launch with the volume term.  With the Osher and Roe fluxes
+ * the face sums go through caller scratch of
+ * gpr_fv_scratch_doubles(nX, ndim, nvar) doubles, which a Rusanov call
+ * does not touch (it may be NULL there). */
 long gpr_fv_scratch_doubles(const int32_t *nX, int ndim, int nvar);
 int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     const double *dX, int ndim, int sources, int time_dg,
@@ -147,8 +153,9 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
  * fv.cpp:11-109: the space-time volume term of the sources and
  * non-conservative products; no scratch), gpr_fv_interfs replaces
  * solvers.fv.interfs1 / interfs2 (fv.h:12-15, fv.cpp:111-279: the interface
- * fluxes and path integrals; scratch as gpr_fv_launcher).  The reference's
- * separate nx / ny / dx / dy arguments are nX[ndim] and dX[ndim] here. */
+ * fluxes and path integrals, applied in place; scratch as gpr_fv_launcher).
+ * The reference's separate nx / ny / dx / dy arguments are nX[ndim] and
+ * dX[ndim] here. */
 int gpr_fv_centers(double *u, const double *qh, const int32_t *nX, double dt,
                    const double *dX, int ndim, int sources, int time_dg,
                    const gpr_par *par, const uint8_t *mask, int nvar, void *stream);

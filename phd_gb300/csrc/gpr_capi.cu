@@ -224,7 +224,7 @@ long gpr_weno_scratch_doubles(const int32_t *nX, int ndim, int nvar) {
 
 int gpr_weno_launcher(double *wh, const double *ub, const int32_t *nX, int ndim,
                       double *scratch, int nvar, void *stream) {
-  if (!wh || !ub || !check_grid(nX, ndim) || (ndim == 2 && !scratch))
+  if (!wh || !ub || !check_grid(nX, ndim))
     return GPR_E_ARG;
   DISPATCH(nvar, O::weno(wh, ub, nX, ndim, scratch, S(stream)))
 }
@@ -249,7 +249,8 @@ int gpr_fv_launcher(double *u, const double *qh, const int32_t *nX, double dt,
                     const double *dX, int ndim, int sources, int time_dg, int flux,
                     const gpr_par *par, const uint8_t *mask, double *scratch, int nvar,
                     void *stream) {
-  if (!u || !qh || !dX || !par || !scratch || !check_grid(nX, ndim))
+  if (!u || !qh || !dX || !par || !check_grid(nX, ndim) ||
+      (!scratch && flux != GPR_FLUX_RUSANOV))
     return GPR_E_ARG;
   if (int rc = check_flux(flux, ndim))
     return rc;
@@ -271,7 +272,8 @@ int gpr_fv_centers(double *u, const double *qh, const int32_t *nX, double dt,
 int gpr_fv_interfs(double *u, const double *qh, const int32_t *nX, double dt,
                    const double *dX, int ndim, int time_dg, int flux, const gpr_par *par,
                    const uint8_t *mask, double *scratch, int nvar, void *stream) {
-  if (!u || !qh || !dX || !par || !scratch || !check_grid(nX, ndim))
+  if (!u || !qh || !dX || !par || !check_grid(nX, ndim) ||
+      (!scratch && flux != GPR_FLUX_RUSANOV))
     return GPR_E_ARG;
   if (int rc = check_flux(flux, ndim))
     return rc;

@@ -104,6 +104,29 @@ __global__ void k_fill_interior(const double *__restrict__ u, double *__restrict
   }
 }
 
+// 1D boundaries in one launch: ub[p] for p in 0..nx+2N-1, interior cells
+// copied from u, ghost cells by the boundary rule from their source cell of u
+// (the values k_fill_interior + k_ghosts give), one thread per (cell, var).
+template <int V>
+__global__ void k_boundaries1d(const double *__restrict__ u, double *__restrict__ ub, int nx,
+                               int bcl, int bcr) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)(nx + 2 * NN) * V)
+    return;
+  const int k = idx % V, p = idx / V;
+  if (p >= NN && p < nx + NN) {
+    ub[idx] = u[(long)(p - NN) * V + k];
+    return;
+  }
+  const int side = p >= nx + NN;
+  const int i = side ? p - nx - NN : p;
+  int code = side ? bcr : bcl;
+  const int si = bc_src_index(code, side, i, nx);
+  if (code == GPR_BC_PERIODIC)
+    code = GPR_BC_TRANSMISSIVE;  // plain copy
+  ub[idx] = bc_value<V>(code, 0, k, u + (long)si * V);
+}
+
 // Ghost rows along one axis.  For axis 0: lines are columns j (interior rows
 // j+N of ub when nd == 2), for axis 1: lines are all ub rows i.
 template <int V>
@@ -207,40 +230,73 @@ __global__ void k_weno1d(double *__restrict__ wh, const double *__restrict__ ub,
   weno_point(ub + (long)i * V + k, V, wh + (long)i * NN * V + k, V, i, ncb, 0, C);
 }
 
-// 2D x sweep (weno.cpp:93-104): ux[i][j][a][k], i in 0..nx'-1 (nx' = nx+2),
-// j over every ub column (ny+2N).
+// 2D, both sweeps in one launch, staged in shared memory: a block takes
+// predictor row i (one of nx+2) and output columns j0 .. j0+jn-1 (jn <= tj).
+// It loads the jn+2 ub columns of ub rows i, i+1, i+2 that the x sweep
+// reads (each row segment is contiguous in the cell-major layout: 16-byte
+// loads, with single doubles only at an unaligned start or end), runs the x
+// sweep on them into a shared ux tile (node a = 0, 1 of each column), and
+// the y sweep of its jn columns from that tile into wh.  Each point is
+// weno_point with the reference's one-sided edges (weno.cpp:93-121); the
+// x sweep's 2 edge columns of a tile are evaluated again by its neighbour
+// tile.  ux never reaches global memory.
+constexpr int WENO2_COLS = 64, WENO2_THREADS = 256;
 template <int V>
-__global__ void k_weno2d_x(double *__restrict__ ux, const double *__restrict__ ub, int nxp,
-                           int nyb, Consts C) {
-  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (idx >= (long)nxp * nyb * V)
-    return;
-  int k = idx % V;
-  long rest = idx / V;
-  int j = rest % nyb;
-  int i = rest / nyb;
-  int gap = (j < NN || j >= nyb - NN) ? NN : 0;
-  weno_point(ub + ((long)i * nyb + j) * V + k, (long)nyb * V,
-             ux + ((long)i * nyb + j) * NN * V + k, V, i, nxp, gap, C);
+__global__ void __launch_bounds__(WENO2_THREADS) k_weno2d(double *__restrict__ wh,
+                                                         const double *__restrict__ ub,
+                                                         int nxp, int nyp, int tj, Consts C) {
+  constexpr int RS = WENO2_COLS * V;  // shared row stride (doubles)
+  __shared__ double sub[3 * RS];
+  __shared__ double sux[WENO2_COLS * NN * V];
+  const int nyb = nyp + 2 * (NN - 1);
+  const int nbj = (nyp + tj - 1) / tj;
+  const int i = blockIdx.x / nbj, j0 = (blockIdx.x % nbj) * tj;
+  const int jn = min(tj, nyp - j0), nc = jn + 2;
+  const int len = nc * V;
+  // 1. stage ub rows i .. i+2, columns j0 .. j0+nc-1
+  for (int r = 0; r < 3; r++) {
+    const double *src = ub + ((long)(i + r) * nyb + j0) * V;
+    const int off = (int)(((unsigned long long)src >> 3) & 1);  // src not 16-byte aligned
+    const int npair = (off + len + 1) / 2;
+    double *dst = sub + r * RS;
+    for (int p = threadIdx.x; p < npair; p += WENO2_THREADS) {
+      const int lo = 2 * p - off;  // element index of the pair's first double
+      if (lo >= 0 && lo + 1 < len) {
+        const double2 x = *reinterpret_cast<const double2 *>(src + lo);
+        dst[lo] = x.x;
+        dst[lo + 1] = x.y;
+      } else {
+        if (lo >= 0)
+          dst[lo] = src[lo];
+        if (lo + 1 >= 0 && lo + 1 < len)
+          dst[lo + 1] = src[lo + 1];
+      }
+    }
+  }
+  __syncthreads();
+  // 2. x sweep (weno.cpp:93-104) of the nc staged columns
+  for (int e = threadIdx.x; e < len; e += WENO2_THREADS) {
+    const int c = e / V, k = e % V;
+    const int j = j0 + c;
+    const int gap = (j < NN || j >= nyb - NN) ? NN : 0;
+    weno_point(sub + c * V + k, RS, sux + c * NN * V + k, V, i, nxp, gap, C);
+  }
+  __syncthreads();
+  // 3. y sweep (weno.cpp:106-121) of the jn output columns
+  const int gap = (i == 0 || i == nxp - 1) ? 1 : 0;
+  for (int e = threadIdx.x; e < jn * NN * V; e += WENO2_THREADS) {
+    const int k = e % V, a = (e / V) % NN, c = e / (NN * V);
+    const int j = j0 + c;
+    weno_point(sux + (c * NN + a) * V + k, (long)NN * V,
+               wh + (((long)i * nyp + j) * NN * NN + a * NN) * V + k, V, j, nyp, gap, C);
+  }
 }
 
-// 2D y sweep (weno.cpp:106-121): wh[i][j][ii][jj][k]
-template <int V>
-__global__ void k_weno2d_y(double *__restrict__ wh, const double *__restrict__ ux, int nxp,
-                           int nyp, Consts C) {
-  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (idx >= (long)nxp * nyp * NN * V)
-    return;
-  int k = idx % V;
-  long rest = idx / V;
-  int ii = rest % NN;
-  rest /= NN;
-  int j = rest % nyp;
-  int i = rest / nyp;
-  int nyb = nyp + 2 * (NN - 1);
-  int gap = (i == 0 || i == nxp - 1) ? 1 : 0;
-  weno_point(ux + (((long)i * nyb + j) * NN + ii) * V + k, (long)NN * V,
-             wh + (((long)i * nyp + j) * NN * NN + ii * NN) * V + k, V, j, nyp, gap, C);
+// Output columns per k_weno2d block: at most WENO2_COLS - 2, spread evenly
+// over the row's blocks.
+inline int weno2d_tile(int nyp) {
+  const int nbj = (nyp + WENO2_COLS - 3) / (WENO2_COLS - 2);
+  return (nyp + nbj - 1) / nbj;
 }
 
 // Sum an n-vector v over the G lanes of each aligned lane group (xor
@@ -290,6 +346,83 @@ GPR_D void face_reduce_store(const double *b, const double *f, double kk, bool a
       out[k] = v[2 * p] + v[2 * p + 1];
       out[V + k] = v[2 * p] - v[2 * p + 1];
     }
+  }
+}
+
+// The same sums applied to the state in place (interfs1 / interfs2 update u
+// inside the face loop, fv.cpp:143-146, 217-222, 257-262): uL -= out[0..V-1]
+// on the cell to the left of the face, uR -= out[V..2V-1] on the cell to its
+// right (either may be null: no interior cell there).  Only for faces with
+// face_on (the face's own activity: geometry and mask, not the lane's).
+template <int V, int G>
+GPR_D void face_reduce_apply(const double *b, const double *f, double kk, bool active,
+                             bool face_on, int r, double *uL, double *uR) {
+  constexpr int NPR = (V + G - 1) / G;
+  double v[2 * NPR * G];
+#pragma unroll
+  for (int k = 0; k < NPR * G; k++) {
+    v[2 * k] = (active && k < V) ? kk * b[k] : 0.0;
+    v[2 * k + 1] = (active && k < V) ? kk * f[k] : 0.0;
+  }
+  GroupReduceScatter<2 * NPR * G, G>::run(v, r);
+  if (!face_on)
+    return;
+#pragma unroll
+  for (int p = 0; p < NPR; p++) {
+    const int k = r * NPR + p;
+    if (k < V) {
+      if (uL)
+        uL[k] -= v[2 * p] + v[2 * p + 1];
+      if (uR)
+        uR[k] -= v[2 * p] - v[2 * p + 1];
+    }
+  }
+}
+
+// Faces of one 2D face pass.  parity < 0: every face (i, j) of the
+// (nx+1) x (ny+1) face grid of direction dir.  parity 0 / 1: only the faces
+// whose index along dir has that parity; two such faces never share a cell,
+// so a pass can update u in place without races, and the four passes
+// (direction x parity) cover every face once.
+struct Face2 {
+  long fi;    // flat face index (i (ny + 1) + j)
+  int i, j;   // predictor-cell indices of the face's left / lower cell
+  bool valid;
+};
+GPR_HD long face2_count(int nx, int ny, int dir, int parity) {
+  if (parity < 0)
+    return (long)(nx + 1) * (ny + 1);
+  return dir == 0 ? (long)((nx + 2 - parity) / 2) * (ny + 1)
+                  : (long)(nx + 1) * ((ny + 2 - parity) / 2);
+}
+GPR_D Face2 face2_of(long face, int nx, int ny, int dir, int parity) {
+  Face2 F;
+  F.valid = face < face2_count(nx, ny, dir, parity);
+  long e = F.valid ? face : 0;
+  if (parity < 0) {
+    F.i = e / (ny + 1);
+    F.j = e % (ny + 1);
+  } else if (dir == 0) {
+    F.i = 2 * (int)(e / (ny + 1)) + parity;
+    F.j = e % (ny + 1);
+  } else {
+    const int nfj = (ny + 2 - parity) / 2;
+    F.i = e / nfj;
+    F.j = 2 * (int)(e % nfj) + parity;
+  }
+  F.fi = (long)F.i * (ny + 1) + F.j;
+  return F;
+}
+// The interior cells on either side of face (i, j) of direction dir, as
+// pointers into u[nx][ny][V] (null where the side is a ghost cell).
+GPR_D void face2_cells(double *u, int i, int j, int nx, int ny, int dir, int V, double *&uL,
+                       double *&uR) {
+  if (dir == 0) {
+    uL = i >= 1 ? u + ((long)(i - 1) * ny + (j - 1)) * V : nullptr;
+    uR = i <= nx - 1 ? u + ((long)i * ny + (j - 1)) * V : nullptr;
+  } else {
+    uL = j >= 1 ? u + ((long)(i - 1) * ny + (j - 1)) * V : nullptr;
+    uR = j <= ny - 1 ? u + ((long)(i - 1) * ny + j) * V : nullptr;
   }
 }
 
@@ -1150,19 +1283,15 @@ __global__ void __launch_bounds__(128) k_faces1d(
 // (qR) and the path integral's node 0 (1); the wave speeds are exchanged,
 // the side-0 lane adds the dissipation, and the four lanes' contributions
 // are summed by the reduce-scatter (the same terms as interface_point).
-template <class L, bool BATCH = false>
-__global__ void __launch_bounds__(128) k_faces1d_split(
-    double *__restrict__ fb, const double *__restrict__ qh, long nface,
-    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    int time_dg, DevPar Pv, Consts C, Batch B) {
+template <class L, bool BATCH>
+GPR_D void faces1d_split_body(double *__restrict__ fb, const double *__restrict__ qh,
+                              long nface, const uint8_t *__restrict__ mask, double dt,
+                              double dx, int time_dg, const DevPar &Pv, const Consts &C,
+                              const Batch &B, long face, int lq, bool inrange, long fbase) {
   constexpr int V = L::V;
   static_assert(NN == 2, "two time nodes and two path nodes");
-  if (dt_dev)
-    dt = *dt_dev;
-  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int lq = threadIdx.x % 4, t = lq >> 1, side = lq & 1;
-  long face = gt / 4;
-  bool valid = face < nface;
+  const int t = lq >> 1, side = lq & 1;
+  bool valid = inrange && face < nface;
   const long fo = valid ? face : 0;
   // predictor cell on the left of the face (packed index in the batched form)
   long fi = fo;
@@ -1212,17 +1341,32 @@ __global__ void __launch_bounds__(128) k_faces1d_split(
       if (k < 14 || k >= V - L::LSET)
         b[k] = wn * bd[k];
   }
-  face_reduce_store<V, 4>(b, f, kk, active, valid, lq, fb + fo * 2 * V);
+  face_reduce_store<V, 4>(b, f, kk, active, valid, lq, fb + (fo - fbase) * 2 * V);
+}
+
+template <class L, bool BATCH = false>
+__global__ void __launch_bounds__(128) k_faces1d_split(
+    double *__restrict__ fb, const double *__restrict__ qh, long nface,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int time_dg, DevPar Pv, Consts C, Batch B) {
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  faces1d_split_body<L, BATCH>(fb, qh, nface, mask, dt, dx, time_dg, Pv, C, B, gt / 4,
+                               threadIdx.x % 4, true, 0);
 }
 
 // 2D faces: direction dir, faces (i, j) of the (nx+1) x (ny+1) face grid,
 // between predictor cells (i, j) and (i+1, j) (dir 0) or (i, j+1) (dir 1);
-// NQ = N*N lanes per face (time node t, transverse node s).
+// NQ = N*N lanes per face (time node t, transverse node s).  parity < 0:
+// every face, contributions written to fb[face][2][V] (the face-flux
+// entry points); parity 0 / 1: the faces of that parity along dir, applied
+// to u (passed as fb) in place, the conservative update of interfs2.
 template <class L>
 __global__ void __launch_bounds__(128) k_faces2d(
     double *__restrict__ fb, const double *__restrict__ qh, int nx, int ny, int dir,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    double dy, int time_dg, DevPar P, Consts C) {
+    double dy, int time_dg, DevPar P, Consts C, int parity = -1) {
   constexpr int V = L::V;
   constexpr int NQ = NN * NN;
   if (dt_dev)
@@ -1230,16 +1374,15 @@ __global__ void __launch_bounds__(128) k_faces2d(
   long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   int lq = threadIdx.x % NQ;
   int t = lq / NN, s = lq % NN;
-  long face = gt / NQ;
-  long nf = (long)(nx + 1) * (ny + 1);
-  bool valid = face < nf;
-  long fi = valid ? face : 0;
-  int i = fi / (ny + 1), j = fi % (ny + 1);
+  const Face2 F = face2_of(gt / NQ, nx, ny, dir, parity);
+  const bool valid = F.valid;
+  const long fi = F.fi;
+  const int i = F.i, j = F.j;
   long cb = (long)i * (ny + 2) + j;
   long cn = dir == 0 ? cb + (ny + 2) : cb + 1;
   bool geo = dir == 0 ? (j > 0) : (i > 0);
-  bool active = valid && geo && (mask == nullptr || (mask[cb] && mask[cn])) &&
-                (time_dg || t == 0);
+  const bool face_on = valid && geo && (mask == nullptr || (mask[cb] && mask[cn]));
+  bool active = face_on && (time_dg || t == 0);
   int nt = time_dg ? NN : 1;
   int tt = time_dg ? t : 0;
   const double *q0 = qh + (cb * nt + tt) * NN * NN * V;
@@ -1262,7 +1405,13 @@ __global__ void __launch_bounds__(128) k_faces2d(
     for (int k = 0; k < V; k++)
       f[k] = b[k] = 0.0;
   }
-  face_reduce_store<V, NQ>(b, f, kk, active, valid, lq, fb + fi * 2 * V);
+  if (parity < 0) {
+    face_reduce_store<V, NQ>(b, f, kk, active, valid, lq, fb + fi * 2 * V);
+  } else {
+    double *uL, *uR;
+    face2_cells(fb, i, j, nx, ny, dir, V, uL, uR);
+    face_reduce_apply<V, NQ>(b, f, kk, active, face_on, lq, uL, uR);
+  }
 }
 
 // Parts of the FV update k_cells applies: the volume term (centers1 /
@@ -1273,24 +1422,22 @@ constexpr int FV_CENTERS = 1, FV_INTERFS = 2, FV_BOTH = 3;
 // Cell pass: one thread per (cell, space-time node): the volume term
 // w_t w_s (S - B dq/dx [- B dq/dy]) (fv.cpp:11-109), reduced over the cell's
 // NP lanes, then u += volume - face contributions (the parts selected).
-template <class L, int ND, bool BATCH = false>
-__global__ void __launch_bounds__(128) k_cells(
-    double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
-    const double *__restrict__ fby, long nx, int ny, const uint8_t *__restrict__ mask,
-    double dt, const double *__restrict__ dt_dev, double dx, double dy, int sources,
-    int time_dg, DevPar Pv, Consts C, Batch B, int parts) {
+// The body for cell c (u index), lane g of its NP lanes; fbx[(fo - fbase)]
+// holds the 1D face on the cell's left (fbase: the first face of a tile
+// staged in shared memory, else 0).
+template <class L, int ND, bool BATCH>
+GPR_D void cells_body(double *__restrict__ u, const double *__restrict__ qh,
+                      const double *__restrict__ fbx, const double *__restrict__ fby, long nx,
+                      int ny, const uint8_t *__restrict__ mask, double dt, double dx,
+                      double dy, int sources, int time_dg, const DevPar &Pv, const Consts &C,
+                      const Batch &B, int parts, long c, int g, bool inrange, long fbase) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;
   constexpr int NP = NN * NS;
   constexpr int XB = ND == 1 ? 1 : 2;
   constexpr int YB = 1;
-  if (dt_dev)
-    dt = *dt_dev;
-  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  int g = threadIdx.x % NP;
-  long c = gt / NP;  // interior cell (u index)
   long ncell = ND == 1 ? nx : (long)nx * ny;
-  bool valid = c < ncell;
+  bool valid = inrange && c < ncell;
   long cc = valid ? c : 0;
   const int inst = BATCH ? B.inst_u[cc] : 0;
   const DevPar &P = BATCH ? B.P[inst] : Pv;
@@ -1378,8 +1525,8 @@ __global__ void __launch_bounds__(128) k_cells(
   double *uc = u + cc * V;
   if (ND == 1) {
     // face ci: R part, face ci+1: L part (fv.cpp:143-146)
-    const double *fl = fbx + fo * 2 * V;
-    const double *fr = fbx + (fo + 1) * 2 * V;
+    const double *fl = fbx + (fo - fbase) * 2 * V;
+    const double *fr = fbx + (fo - fbase + 1) * 2 * V;
     bool okl = mask == nullptr || (mask[cb - 1] && mask[cb]);
     bool okr = mask == nullptr || (mask[cb] && mask[cb + 1]);
 #pragma unroll
@@ -1416,6 +1563,49 @@ __global__ void __launch_bounds__(128) k_cells(
       uc[k] = x;
     }
   }
+}
+
+template <class L, int ND, bool BATCH = false>
+__global__ void __launch_bounds__(128) k_cells(
+    double *__restrict__ u, const double *__restrict__ qh, const double *__restrict__ fbx,
+    const double *__restrict__ fby, long nx, int ny, const uint8_t *__restrict__ mask,
+    double dt, const double *__restrict__ dt_dev, double dx, double dy, int sources,
+    int time_dg, DevPar Pv, Consts C, Batch B, int parts) {
+  constexpr int NP = NN * (ND == 1 ? NN : NN * NN);
+  if (dt_dev)
+    dt = *dt_dev;
+  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  cells_body<L, ND, BATCH>(u, qh, fbx, fby, nx, ny, mask, dt, dx, dy, sources, time_dg, Pv, C,
+                           B, parts, gt / NP, threadIdx.x % NP, true, 0);
+}
+
+// The whole 1D FV update of fv_launcher (centers1 + interfs1, fv.cpp:11-160)
+// in one launch, Rusanov flux: a block takes a tile of FV1_TILE cells; its
+// 128 threads first evaluate the tile's FV1_TILE + 1 faces (one lane per
+// face, time node and side, as k_faces1d_split) into shared memory, then
+// the cells' volume terms (one lane per space-time node, as k_cells), and
+// each cell's lanes apply u += volume - its two faces' contributions.  A
+// face between two tiles is evaluated by both (one face in 32 twice); the
+// sums and their order are those of the two-launch form.
+constexpr int FV1_TILE = 31;
+template <class L>
+__global__ void __launch_bounds__(128) k_fv1d(
+    double *__restrict__ u, const double *__restrict__ qh, long nx,
+    const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
+    int sources, int time_dg, DevPar P, Consts C, int parts) {
+  constexpr int V = L::V;
+  static_assert(NN == 2 && 4 * (FV1_TILE + 1) == 128, "four lanes per face and per cell");
+  __shared__ double sfb[(FV1_TILE + 1) * 2 * V];
+  if (dt_dev)
+    dt = *dt_dev;
+  const long c0 = (long)blockIdx.x * FV1_TILE;  // first cell, and first face, of the tile
+  const int slot = threadIdx.x >> 2, lq = threadIdx.x & 3;
+  if (parts & FV_INTERFS)
+    faces1d_split_body<L, false>(sfb, qh, nx + 1, mask, dt, dx, time_dg, P, C, Batch{},
+                                 c0 + slot, lq, true, c0);
+  __syncthreads();
+  cells_body<L, 1, false>(u, qh, sfb, nullptr, nx, 1, mask, dt, dx, 1.0, sources, time_dg, P, C,
+                          Batch{}, parts, c0 + slot, lq, slot < FV1_TILE, c0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1472,8 +1662,12 @@ static __global__ void k_cfl_finalize(const unsigned long long *__restrict__ mx,
 // Device clock of the device-resident time loop: [t, dt, tf, cfl, count].
 // The CFL finalize reads t/count and writes dt (0 once t >= tf); the advance
 // kernel adds dt to t and counts the step.
+// flag (optional): the step's contortion flag, cleared here for the
+// contortion check later in the same step.
 static __global__ void k_clock_finalize(const unsigned long long *__restrict__ mx,
-                                 double *__restrict__ clk) {
+                                        double *__restrict__ clk, int *__restrict__ flag = nullptr) {
+  if (flag)
+    *flag = 0;
   double t = clk[0], tf = clk[2], cfl = clk[3];
   long count = (long)clk[4];
   double dt = 0.0;
@@ -1488,11 +1682,15 @@ static __global__ void k_clock_finalize(const unsigned long long *__restrict__ m
   clk[1] = dt;
 }
 
-static __global__ void k_clock_advance(double *__restrict__ clk) {
+// mx (optional): the CFL maximum, cleared here for the next step's k_cfl_max.
+static __global__ void k_clock_advance(double *__restrict__ clk,
+                                       unsigned long long *__restrict__ mx = nullptr) {
   if (clk[1] > 0.0) {
     clk[0] += clk[1];
     clk[4] += 1.0;
   }
+  if (mx)
+    *mx = 0ull;
 }
 
 // renorm_distortion (solvers/utils.cpp:6-23); skipped when the device clock
@@ -1517,6 +1715,39 @@ __global__ void k_renorm(double *__restrict__ u, long ncell, double rho0,
     for (int k = 0; k < 9; k++)
       q[5 + k] = A[k] * f;
   }
+}
+
+// k_renorm followed by the contortion test of the renormalised cell
+// (contorted, solvers/utils.cpp:66-85, as k_contorted): one launch for both.
+template <int V>
+__global__ void k_renorm_contorted(double *__restrict__ u, long ncell, double rho0, double tol,
+                                   int *__restrict__ flag, const double *__restrict__ dt_dev) {
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= ncell)
+    return;
+  if (dt_dev && *dt_dev == 0.0)
+    return;
+  double *q = u + c * V;
+  double A[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    A[k] = q[5 + k];
+  const double r = q[0];
+  if (r > 0) {
+    double f = cbrt(r / (rho0 * det3(A)));
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      A[k] *= f;
+      q[5 + k] = A[k];
+    }
+  }
+  double f2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    f2 += A[k] * A[k];
+  double d13 = cbrt(fabs(det3(A)));
+  if (f2 / (3.0 * d13 * d13) - 1.0 > tol)
+    atomicOr(flag, 1);
 }
 
 // ---------------------------------------------------------------------------

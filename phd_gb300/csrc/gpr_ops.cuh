@@ -157,6 +157,11 @@ template <class L> struct Ops {
   static int boundaries(const double *u, double *ub, const int32_t *nX, int nd,
                         const int32_t *bcs, cudaStream_t st) {
     int nx = nX[0], ny = nd == 2 ? nX[1] : 1;
+    if (nd == 1) {
+      k_boundaries1d<V><<<blocks((long)(nx + 2 * NN) * V, 256), 256, 0, st>>>(u, ub, nx, bcs[0],
+                                                                              bcs[1]);
+      return cuda_rc();
+    }
     long n = (long)nx * ny * V;
     k_fill_interior<V><<<blocks(n, 256), 256, 0, st>>>(u, ub, nx, ny, nd);
     long g0 = (long)(nd == 1 ? 1 : ny) * 2 * NN * V;
@@ -182,10 +187,12 @@ template <class L> struct Ops {
       k_weno1d<V><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, C);
       return cuda_rc();
     }
-    int nxp = nX[0] + 2, nyp = nX[1] + 2, nyb = nX[1] + 2 * NN;
-    k_weno2d_x<V><<<blocks((long)nxp * nyb * V, 256), 256, 0, st>>>(scratch, ub, nxp, nyb, C);
-    k_weno2d_y<V><<<blocks((long)nxp * nyp * NN * V, 256), 256, 0, st>>>(wh, scratch, nxp,
-                                                                         nyp, C);
+    // both sweeps in one launch through shared memory (k_weno2d); the
+    // scratch is not used
+    int nxp = nX[0] + 2, nyp = nX[1] + 2;
+    const int tj = weno2d_tile(nyp);
+    const long nblk = (long)nxp * ((nyp + tj - 1) / tj);
+    k_weno2d<V><<<(unsigned)nblk, WENO2_THREADS, 0, st>>>(wh, ub, nxp, nyp, tj, C);
     return cuda_rc();
   }
 
@@ -242,15 +249,18 @@ template <class L> struct Ops {
     int nx = nX[0];
     const bool faces = parts & FV_INTERFS;
     if (nd == 1) {
-      long nf = (long)(nx + 1) * NN;
-      if (!faces)
-        ;
-      else if (flux == GPR_FLUX_RUSANOV)  // one lane per (face, time node, side)
-        k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
-            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, P, C, Batch{});
-      else
-        k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
-            scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
+      if (flux == GPR_FLUX_RUSANOV || !faces) {
+        // faces, volume term and update in one launch (k_fv1d)
+        k_fv1d<L><<<blocks(nx, FV1_TILE), 128, 0, st>>>(u, qh, nx, mask, dt, dt_dev, dX[0],
+                                                        sources, time_dg, P, C, parts);
+        return cuda_rc();
+      }
+      // Osher / Roe: the faces' eigen-decompositions, one warp each, write
+      // the face sums to scratch (a 1D grid has few faces, so one launch over
+      // all of them keeps the decompositions' latency to one), then the cell
+      // pass applies them
+      k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
+          scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
       long nc = (long)nx * NN * NN;
       k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
                                                       dt_dev, dX[0], 1.0, sources, time_dg, P,
@@ -258,21 +268,33 @@ template <class L> struct Ops {
       return cuda_rc();
     }
     int ny = nX[1];
-    long nf = (long)(nx + 1) * (ny + 1);
-    double *fbx = scratch, *fby = faces ? scratch + nf * 2 * V : nullptr;
-    if (!faces) {
-    } else if (flux == GPR_FLUX_RUSANOV) {
-      k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fbx, qh, nx, ny, 0, mask, dt,
-                                                               dt_dev, dX[0], dX[1], time_dg, P,
-                                                               C);
-      k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fby, qh, nx, ny, 1, mask, dt,
-                                                               dt_dev, dX[0], dX[1], time_dg, P,
-                                                               C);
-    } else {
-      faces2d_eig(fbx, qh, nx, ny, 0, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
-      faces2d_eig(fby, qh, nx, ny, 1, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+    const long nc = (long)nx * ny * NN * NN * NN;
+    if (flux == GPR_FLUX_RUSANOV || !faces) {
+      // Rusanov: the volume term first (centers2), then the face terms
+      // applied to u in place by four passes (x / y faces, even / odd index
+      // along the direction; two faces of one pass never share a cell), as
+      // interfs2 updates u inside its face loop (fv.cpp:162-279).  No face
+      // buffer.
+      if (parts & FV_CENTERS)
+        k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, nullptr, nullptr, nx, ny, mask,
+                                                        dt, dt_dev, dX[0], dX[1], sources,
+                                                        time_dg, P, C, Batch{}, FV_CENTERS);
+      if (faces)
+        for (int dir = 0; dir < 2; dir++)
+          for (int par = 0; par < 2; par++) {
+            long nf = face2_count(nx, ny, dir, par);
+            k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(
+                u, qh, nx, ny, dir, mask, dt, dt_dev, dX[0], dX[1], time_dg, P, C, par);
+          }
+      return cuda_rc();
     }
-    long nc = (long)nx * ny * NN * NN * NN;
+    // Osher / Roe: the per-thread eigen-decompositions write the face sums
+    // of each direction to scratch, then the cell pass applies the volume
+    // and face terms
+    long nf = (long)(nx + 1) * (ny + 1);
+    double *fbx = scratch, *fby = scratch + nf * 2 * V;
+    faces2d_eig(fbx, qh, nx, ny, 0, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+    faces2d_eig(fby, qh, nx, ny, 1, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
     k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
                                                     dX[0], dX[1], sources, time_dg, P, C,
                                                     Batch{}, parts);
@@ -375,11 +397,10 @@ template <class L> struct Ops {
                                                                ? weno_scratch(nX, nd)
                                                                : fv_scratch(nX, nd)));
     double *dt_dev = clk + 1;
+    if (nsteps > 0)
+      cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st);
     for (int s = 0; s < nsteps; s++) {
-      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
-                                                        nd == 2 ? dX[1] : 1.0, mx, P);
-      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
+      step_head(u, ncell, nd, dX, P, mx, clk, st);
       int rc = boundaries(u, ub, nX, nd, bcs, st);
       if (rc)
         return rc;
@@ -392,11 +413,30 @@ template <class L> struct Ops {
       rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st, flux);
       if (rc)
         return rc;
-      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
-      contortion(u, ncell, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
-      k_clock_advance<<<1, 1, 0, st>>>(clk);
+      step_tail(u, ncell, P, contorted_tol, mx, clk, st);
     }
     return cuda_rc();
+  }
+
+  // The clock kernels of a device-resident step around its stages:
+  // head = CFL maximum -> dt (and the contortion flag mx[1] cleared); tail =
+  // renorm + contortion test -> reset -> clock advance (and the CFL maximum
+  // mx[0] cleared for the next step).  mx[0..1] must be zero before the
+  // first step.
+  static void step_head(const double *u, long ncell, int nd, const double *dX, const DevPar &P,
+                        unsigned long long *mx, double *clk, cudaStream_t st) {
+    k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+                                                      nd == 2 ? dX[1] : 1.0, mx, P);
+    k_clock_finalize<<<1, 1, 0, st>>>(mx, clk, (int *)(mx + 1));
+  }
+  static void step_tail(double *u, long ncell, const DevPar &P, double tol,
+                        unsigned long long *mx, double *clk, cudaStream_t st) {
+    const double *dt_dev = clk + 1;
+    int *flag = (int *)(mx + 1);
+    k_renorm_contorted<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, tol, flag,
+                                                               dt_dev);
+    k_reset_distortion<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, flag, P, P, dt_dev);
+    k_clock_advance<<<1, 1, 0, st>>>(clk, mx);
   }
 
   // ---- split scheme (steppers.cpp:50-66, split/homogeneous.cpp) -------------
@@ -460,20 +500,17 @@ template <class L> struct Ops {
     double *rest = ub + nub * V;
     unsigned long long *mx = (unsigned long long *)(scratch + iterate_scratch(nX, nd) - 2);
     double *dt_dev = clk + 1;
+    if (nsteps > 0)
+      cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st);
     for (int s = 0; s < nsteps; s++) {
-      cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-      k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
-                                                        nd == 2 ? dX[1] : 1.0, mx, P);
-      k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
+      step_head(u, ncell, nd, dX, P, mx, clk, st);
       int rc = boundaries(u, ub, nX, nd, bcs, st);
       if (rc)
         return rc;
       rc = split_stepper(u, ub, nX, nd, 0.0, dt_dev, dX, half_step, flux, P, mask, rest, st);
       if (rc)
         return rc;
-      k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
-      contortion(u, ncell, contorted_tol, P, P, (int *)(mx + 1), dt_dev, st);
-      k_clock_advance<<<1, 1, 0, st>>>(clk);
+      step_tail(u, ncell, P, contorted_tol, mx, clk, st);
     }
     return cuda_rc();
   }

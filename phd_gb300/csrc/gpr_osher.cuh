@@ -181,10 +181,14 @@ GPR_D void system_fd(const double *Q, const Prim<TH> &s, const DevPar &P, double
 }
 
 // M += the non-conservative block B_x (equations.cpp:69-87)
-template <int V> GPR_D void system_block(const double *v, double *M) {
+template <int V, int LSET> GPR_D void system_block(const double *v, double *M) {
   constexpr int d = 0;
 #pragma unroll
   for (int i = 5; i < 14; i++)
+    M[i * V + i] += v[d];
+  // the level sets are advected: v_d on their diagonal (equations.cpp:85-86)
+#pragma unroll
+  for (int i = V - LSET; i < V; i++)
     M[i * V + i] += v[d];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -213,7 +217,7 @@ GPR_D void system_matrix(const double *Q, const Prim<TH> &s, const DevPar &P, do
         acc += F[i * V + k] * D[k * V + j];
       M[i * V + j] = acc;
     }
-  system_block<V>(s.v, M);
+  system_block<V, V - 14 - (TH ? 3 : 0)>(s.v, M);
 }
 
 // Householder reduction of H (n x n, ld n) to upper Hessenberg form,
@@ -1388,7 +1392,7 @@ template <class L> GPR_D void w_system_matrix(EigWS<L::V> &ws, const DevPar &P, 
   vloc[2] = ws.v[2];
   __syncwarp();
   if (lane == 0)
-    system_block<V>(vloc, ws.H);
+    system_block<V, L::LSET>(vloc, ws.H);
   __syncwarp();
 }
 
