@@ -190,7 +190,8 @@ int fmm_mono_from(const Grid &g) { return fmm_rounds(g) - fmm_tiles_across(g) / 
 // Scratch of one fill (offsets in doubles, 256-byte aligned pieces).
 struct FillLayout {
   long o_d, o_phim, o_dphi, o_star, o_plan, o_fz, o_im0, o_im1, o_lastw, o_pidx, o_dep,
-      o_level, o_cnt, o_flags, o_tflag, o_lastg, o_par, total;
+      o_level, o_cnt, o_flags, o_tflag, o_lastg, o_par, o_d2, o_par2, o_list, o_qst, o_gs,
+      total;
 };
 
 int fmm_tiles(const Grid &g) {
@@ -221,8 +222,42 @@ FillLayout fill_layout(const Grid &g) {
   L.o_tflag = cv.take(dbl((long)fmm_rounds(g) * fmm_tiles(g) * 4L));
   L.o_lastg = cv.take(dbl(n * 4));
   L.o_par = cv.take(dbl(n));
+  // the 2D global sweeps: second buffers, two work lists, list stamps,
+  // counters and the grid barrier
+  L.o_d2 = cv.take(n);
+  L.o_par2 = cv.take(dbl(n));
+  L.o_list = cv.take(dbl(2 * n * 4));
+  L.o_qst = cv.take(dbl(n * 4));
+  L.o_gs = cv.take(dbl(16 * 4));
   L.total = cv.o;
   return L;
+}
+
+// Sweep budget of the 2D global sweeps: the dependency chain of a point is
+// at most ~1.5 (nx + ny) sweeps long; from 2 (nx + ny) + 64 sweeps on only
+// decreasing updates are taken (termination), and 3 (nx + ny) + 128 ends
+// the loop with an error.
+int fmm_mono_sweeps(const Grid &g) { return 2 * (g.nx + g.ny) + 64; }
+int fmm_max_sweeps(const Grid &g) { return 3 * (g.nx + g.ny) + 128; }
+
+// Blocks of the cooperative k_fmm_global launch: one per SM (the lists
+// rarely hold more points than its threads; fewer blocks make the barrier
+// cheaper).
+int fmm_global_blocks() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && cached[dev] > 0)
+    return cached[dev];
+  int nsm = 0, per = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fmm_global, 256, 0);
+  if (per > 1)
+    per = 1;
+  const int nb = nsm * (per > 0 ? per : 0);
+  if (dev >= 0 && dev < 64)
+    cached[dev] = nb;
+  return nb;
 }
 
 template <class T> T *at(double *scr, long off) { return (T *)(scr + off); }
@@ -239,16 +274,45 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
   int R = fmm_rounds(g);
   cudaMemsetAsync(cnt, 0, 8 * sizeof(int), st);
   cudaMemsetAsync(flags, 0, R * sizeof(int), st);
-  cudaMemsetAsync(tflag, 0, (size_t)R * fmm_tiles(g) * sizeof(int), st);
-  cudaMemsetAsync(lastg, 0xff, g.ncell * sizeof(int), st);
+  if (g.nd == 1) {
+    cudaMemsetAsync(tflag, 0, (size_t)R * fmm_tiles(g) * sizeof(int), st);
+    cudaMemsetAsync(lastg, 0xff, g.ncell * sizeof(int), st);
+  }
   uint8_t *par = at<uint8_t>(scr, L.o_par);
   k_fmm_init<<<blocks(g.ncell, 256), 256, 0, st>>>(phi, ps, d, fz, par, g, cnt, clk);
   FmmConst K = fmm_const(g.dx, g.nd == 2 ? g.dy : g.dx);
   if (g.nd == 2) {
-    int nb = ((g.nx + FMM_T2 - 1) / FMM_T2) * ((g.ny + FMM_T2 - 1) / FMM_T2);
-    for (int r = 0; r < R; r++)
-      k_fmm_round<2><<<nb, FmmThreads<2>::value, 0, st>>>(d, fz, par, lastg, g, K, flags, tflag, r,
-                                                 kFmmSweeps, r >= fmm_mono_from(g), clk);
+    FmmGlobal G;
+    G.d[0] = d;
+    G.d[1] = scr + L.o_d2;
+    G.par[0] = par;
+    G.par[1] = at<uint8_t>(scr, L.o_par2);
+    G.fz = fz;
+    G.list[0] = at<int>(scr, L.o_list);
+    G.list[1] = G.list[0] + g.ncell;
+    G.qst = at<int>(scr, L.o_qst);
+    G.cnt = at<int>(scr, L.o_gs);
+    G.bar = (unsigned *)(G.cnt + 8);
+    G.err = err;
+    G.mono_from = fmm_mono_sweeps(g);
+    G.max_sweeps = fmm_max_sweeps(g);
+    const int nb = fmm_global_blocks();
+    if (nb <= 0)
+      return GPR_E_CUDA;
+    cudaMemsetAsync(G.cnt, 0, 16 * sizeof(int), st);
+    cudaMemsetAsync(G.qst, 0xff, g.ncell * sizeof(int), st);
+    cudaMemcpyAsync(G.d[1], d, g.ncell * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(G.par[1], par, g.ncell, cudaMemcpyDeviceToDevice, st);
+    k_fmm_seed<<<blocks(g.ncell, 256), 256, 0, st>>>(g, G, clk);
+    void *args[] = {(void *)&g, (void *)&K, (void *)&G, (void *)&clk};
+    if (cudaLaunchCooperativeKernel((const void *)k_fmm_global, dim3(nb), dim3(256), args, 0,
+                                    st) != cudaSuccess)
+      return cuda_rc();
+    // the sweeps end with both buffers equal (no point changed in the last
+    // one); d[0] is d.  flags[0] is zero: the kernel reports its own budget.
+    k_fmm_finish<V15><<<blocks(g.ncell, 256), 256, 0, st>>>(d, u, g.ncell, cnt, flags, 0, err,
+                                                            clk);
+    return cuda_rc();
   } else {
     int nb = (g.nx + FMM_T1 - 1) / FMM_T1;
     for (int r = 0; r < R; r++)

@@ -528,6 +528,206 @@ __global__ void __launch_bounds__(FmmThreads<ND>::value, ND == 2 ? 16 : 2)
   }
 }
 
+// ---------------------------------------------------------------------------
+// 2D re-distancing as one persistent grid: global Jacobi sweeps of the same
+// update (fmm_update), one grid barrier per sweep.  The tiled rounds above
+// exchange halos only between launches, so information crosses a tile per
+// round and each tile re-sweeps its points until its halo settles (33-91
+// updates per cell on the 800 x 400 bubble).  Here every sweep sees the
+// previous sweep's values everywhere: a sweep updates only the points whose
+// neighbours changed in the previous sweep (a work list), the front moves a
+// cell per sweep, and the number of sweeps is the depth of the marcher's
+// dependency chain (~1.4 x the largest distance in cells).  Each sweep is
+// one FP64 update per listed point (one lane each) and one barrier, so a
+// sweep costs about one update's FP64 chain (on GB300 a warp's FP64
+// instruction holds its partition's FP64 unit ~64 cycles) plus the barrier.
+//
+// Jacobi with two buffers: sweep s reads d[s % 2] / par[s % 2] and writes
+// d[(s + 1) % 2] / par[(s + 1) % 2] for its listed points; a point that
+// changes lists itself for the next sweep as well as its unfrozen
+// neighbours, which copies its new value into the other buffer, so after
+// sweep s the written buffer holds every point's latest value.  The fixed
+// point, and so the result, is that of the tiled form: the sweeps end when
+// no point changes, whatever the order of the work.  From sweep mono_from
+// on only smaller |d| is taken (termination, as the tiled form's last
+// rounds); a list still non-empty after max_sweeps sets err bit 0.
+//
+// The blocks wait for one another at the barrier, so the kernel is launched
+// cooperatively (all blocks resident); each wait is bounded (~1 s), after
+// which the block sets err bit 2 and leaves.
+struct FmmGlobal {
+  double *d[2];
+  uint8_t *par[2];
+  const uint8_t *fz;
+  int *list[2];
+  int *qst;           // the sweep a point is listed for (dedupes the lists)
+  int *cnt;           // cnt[3]: list lengths, rotating
+  unsigned *bar;      // bar[0] arrivals; bar[2..3] generation and list length
+  int *err;
+  int mono_from, max_sweeps;
+};
+
+// Grid barrier of the sweeps.  bar[0] counts arrivals; the 64-bit word at
+// bar + 2 holds the generation (high half) and, published by the last block
+// to arrive, the length of the next sweep's list (low half), read from
+// *next once every block has finished its appends.  One thread per block
+// fences and waits (after the block barrier, which orders the block's
+// writes before it); the wait gives up after ~1 s (err bit 2).  Returns the
+// next list's length, or -1 after a timeout.
+GPR_D int fmm_grid_sync(unsigned *bar, unsigned nblocks, const int *next, int *err) {
+  __shared__ int shn;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long *word = (unsigned long long *)(bar + 2);
+    volatile unsigned long long *vw = word;
+    const unsigned g = (unsigned)(*vw >> 32);
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      const int n = atomicAdd((int *)next, 0);
+      __threadfence();
+      atomicExch(word, ((unsigned long long)(g + 1u) << 32) | (unsigned)n);
+      shn = n;
+    } else {
+      const long long t0 = clock64();
+      unsigned long long v;
+      shn = -1;
+      while (((v = *vw) >> 32) == g) {
+        if (clock64() - t0 > 2000000000LL) {  // ~1 s at 2 GHz
+          atomicOr(err, 4);
+          break;
+        }
+      }
+      if ((v >> 32) != g)
+        shn = (int)(unsigned)(v & 0xffffffffull);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return shn;
+}
+
+// Lists the candidates cand[k] with want[k] for sweep s, each point once per
+// sweep (stamps in qst): the stamps' atomics are issued back to back, and a
+// warp reserves its list entries with one atomic.
+template <int K>
+GPR_D void fmm_enqueue(const bool (&want)[K], const int (&cand)[K], int s, const FmmGlobal &G) {
+  bool mine[K];
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    mine[k] = want[k] ? atomicMax(G.qst + cand[k], s) < s : false;
+  int nk = 0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    nk += mine[k];
+  const int lane = threadIdx.x & 31;
+  int incl = nk;  // inclusive warp scan
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o)
+      incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0)
+    return;
+  int base = 0;
+  if (lane == 31)
+    base = atomicAdd(G.cnt + s % 3, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  int pos = base + incl - nk;
+  int *lst = G.list[s & 1];
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (mine[k])
+      lst[pos++] = cand[k];
+}
+
+// The first list: unfrozen points next to the frozen band.
+__global__ void k_fmm_seed(Grid g, FmmGlobal G, const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  bool want[1] = {false};
+  if (c < g.ncell && !(G.fz[c] & 1)) {
+    const int i = c / g.ny, j = c % g.ny;
+    want[0] = (i > 0 && (G.fz[c - g.ny] & 1)) || (i < g.nx - 1 && (G.fz[c + g.ny] & 1)) ||
+              (j > 0 && (G.fz[c - 1] & 1)) || (j < g.ny - 1 && (G.fz[c + 1] & 1));
+  }
+  const int cand[1] = {(int)(c < g.ncell ? c : 0)};
+  fmm_enqueue<1>(want, cand, 0, G);
+}
+
+__global__ void __launch_bounds__(256) k_fmm_global(Grid g, FmmConst K, FmmGlobal G,
+                                                     const double *__restrict__ clk) {
+  if (clk && clk[0] >= clk[2])
+    return;
+  const unsigned nb = gridDim.x;
+  const long nthr = (long)gridDim.x * blockDim.x;
+  const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int s = 0;
+  int n = __ldcg(G.cnt);  // the first list (k_fmm_seed)
+  for (; s < G.max_sweeps; s++) {
+    if (n <= 0)
+      break;
+    if (gid == 0)
+      G.cnt[(s + 2) % 3] = 0;  // the list count of sweep s - 1, no longer read
+    const double *src = G.d[s & 1];
+    double *dst = G.d[(s + 1) & 1];
+    const uint8_t *psrc = G.par[s & 1];
+    uint8_t *pdst = G.par[(s + 1) & 1];
+    const int *lst = G.list[s & 1];
+    const bool mono = s >= G.mono_from;
+    // whole warps take list entries, so that the enqueues can aggregate
+    const long nround = (n + 31) / 32 * 32;
+    for (long q = gid; q < nround; q += nthr) {
+      const bool live = q < n;
+      const int c = live ? __ldcg(lst + q) : 0;
+      const int i = c / g.ny, j = c % g.ny;
+      bool chg = false;
+      if (live) {
+        double nb4[2][2];
+        bool bd[2][2], ex[2][2];
+        const long cn[2][2] = {{c - g.ny, c + g.ny}, {c - 1, c + 1}};
+        const bool in[2][2] = {{i > 0, i < g.nx - 1}, {j > 0, j < g.ny - 1}};
+        // a neighbour that recorded this point as entered (its bit for the
+        // opposite side) is not a candidate: bits 2 dim + side
+        const int xb[2][2] = {{1, 0}, {3, 2}};
+        for (int dim = 0; dim < 2; dim++)
+          for (int sd = 0; sd < 2; sd++) {
+            const bool ok = in[dim][sd];
+            const long m = ok ? cn[dim][sd] : c;
+            nb4[dim][sd] = ok ? __ldcg(src + m) : INFINITY;
+            bd[dim][sd] = ok && (G.fz[m] & 1);
+            ex[dim][sd] = ok && ((__ldcg(psrc + m) >> xb[dim][sd]) & 1);
+          }
+        const double old = __ldcg(src + c);
+        const uint8_t pold = __ldcg(psrc + c);
+        int msk;
+        const double nv = fmm_update(nb4, bd, ex, (G.fz[c] & 2) != 0, 2, old, K, msk);
+        chg = mono ? fabs(nv) < fabs(old) : (nv != old || (uint8_t)msk != pold);
+        __stcg(dst + c, chg ? nv : old);
+        __stcg(pdst + c, chg ? (uint8_t)msk : pold);
+      }
+      // list the point itself and its unfrozen neighbours for sweep s + 1
+      const int cand[5] = {c, i > 0 ? c - g.ny : c, i < g.nx - 1 ? c + g.ny : c,
+                           j > 0 ? c - 1 : c, j < g.ny - 1 ? c + 1 : c};
+      bool want[5] = {chg, chg && i > 0, chg && i < g.nx - 1, chg && j > 0, chg && j < g.ny - 1};
+#pragma unroll
+      for (int k = 1; k < 5; k++)
+        want[k] = want[k] && !(G.fz[cand[k]] & 1);
+      fmm_enqueue<5>(want, cand, s + 1, G);
+    }
+    n = fmm_grid_sync(G.bar, nb, G.cnt + (s + 1) % 3, G.err);
+    if (n < 0)
+      return;
+  }
+  if (gid == 0 && s >= G.max_sweeps && n != 0)
+    atomicOr(G.err, 1);  // not converged within the sweep budget
+  if (gid == 0)
+    G.cnt[3] = s;  // the sweeps taken
+}
+
 // Final values (base_marcher.cpp:103-106, 190-196): zeros when nothing
 // froze, DBL_MAX where the march never arrived; the distance also replaces
 // the level set in u (renormalize_levelsets, multi/functions.cpp:56-64).

@@ -236,7 +236,10 @@ template <class L> struct Ops {
   static long fv_scratch(const int32_t *nX, int nd) {
     if (nd == 1)
       return (long)(nX[0] + 1) * 2 * V;
-    return 2L * (nX[0] + 1) * (nX[1] + 1) * 2 * V;
+    // x and y face sums, then the per-point terms of one direction (Osher /
+    // Roe, k_faces2d_eigp)
+    const long nf = (long)(nX[0] + 1) * (nX[1] + 1);
+    return 2L * nf * 2 * V + nf * NN * NN * 2 * V;
   }
 
   // parts: FV_BOTH (fv_launcher), FV_CENTERS (centers1/2: the volume term,
@@ -292,9 +295,9 @@ template <class L> struct Ops {
     // of each direction to scratch, then the cell pass applies the volume
     // and face terms
     long nf = (long)(nx + 1) * (ny + 1);
-    double *fbx = scratch, *fby = scratch + nf * 2 * V;
-    faces2d_eig(fbx, qh, nx, ny, 0, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
-    faces2d_eig(fby, qh, nx, ny, 1, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+    double *fbx = scratch, *fby = scratch + nf * 2 * V, *pp = scratch + 2 * nf * 2 * V;
+    faces2d_eig(fbx, pp, qh, nx, ny, 0, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
+    faces2d_eig(fby, pp, qh, nx, ny, 1, mask, dt, dt_dev, dX, time_dg, flux, P, C, st);
     k_cells<L, 2><<<blocks(nc, 128), 128, 0, st>>>(u, qh, fbx, fby, nx, ny, mask, dt, dt_dev,
                                                     dX[0], dX[1], sources, time_dg, P, C,
                                                     Batch{}, parts);
@@ -321,9 +324,10 @@ template <class L> struct Ops {
     int ny = nX[1];
     long nf = (long)(nx + 1) * (ny + 1);
     if (flux != GPR_FLUX_RUSANOV) {
-      faces2d_eig(fb, qh, nx, ny, 0, mask, dt, nullptr, dX, time_dg, flux, P, C, st);
-      faces2d_eig(fb + nf * 2 * V, qh, nx, ny, 1, mask, dt, nullptr, dX, time_dg, flux, P, C,
-                  st);
+      double *pp = fb + 2 * nf * 2 * V;
+      faces2d_eig(fb, pp, qh, nx, ny, 0, mask, dt, nullptr, dX, time_dg, flux, P, C, st);
+      faces2d_eig(fb + nf * 2 * V, pp, qh, nx, ny, 1, mask, dt, nullptr, dX, time_dg, flux, P,
+                  C, st);
       return cuda_rc();
     }
     k_faces2d<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(fb, qh, nx, ny, 0, mask, dt,
@@ -336,14 +340,16 @@ template <class L> struct Ops {
   }
 
   // Osher / Roe faces of one direction on a 2D grid: one thread per face
-  // quadrature point.
-  static void faces2d_eig(double *fb, const double *qh, int nx, int ny, int dir,
+  // quadrature point into the per-point buffer pp (nf x 4 x 2V doubles),
+  // then the face sums into fb.
+  static void faces2d_eig(double *fb, double *pp, const double *qh, int nx, int ny, int dir,
                           const uint8_t *mask, double dt, const double *dt_dev, const double *dX,
                           int time_dg, int flux, const DevPar &P, const Consts &C,
                           cudaStream_t st) {
     long nf = (long)(nx + 1) * (ny + 1);
-    k_faces2d_eigt<L><<<blocks(nf * NN * NN, 128), 128, 0, st>>>(
-        fb, qh, nx, ny, dir, mask, dt, dt_dev, dX[0], dX[1], time_dg, flux, P, C);
+    k_faces2d_eigp<L><<<blocks(nf * NN * NN, 64), 64, 0, st>>>(
+        pp, qh, nx, ny, dir, mask, dt, dt_dev, dX[0], dX[1], time_dg, flux, P, C);
+    k_faces2d_eigsum<V><<<blocks(nf * 2 * V, 256), 256, 0, st>>>(fb, pp, nf);
   }
 
   static int timestep(const double *u, long ncell, const double *dX, int nd, double cfl,

@@ -1533,70 +1533,80 @@ __global__ void __launch_bounds__(32 * EIG_WARPS) k_faces1d_eigw(
   }
 }
 
-// 2D faces with the Osher or Roe dissipation, one thread per face
-// quadrature point (the layout and summation of k_faces2d), each running its
-// eigen-decompositions alone with the matrices in local memory; y faces go
-// through the x form on axis-exchanged states (eig_dissipation_d).  With
-// millions of independent eigenproblems per step this beats the
-// warp-per-eigenproblem form (k_faces1d_eigw, built for the few faces of a
-// 1D grid) 4x: 694 against 2772 ms per 512 x 512 Roe step.
+// 2D Osher / Roe faces in two launches.  k_faces2d_eigp: one thread per face
+// quadrature point (time node t, transverse node s), as the pointwise
+// interface-terms kernel: it evaluates D_OSH / D_ROE + F(qL) + F(qR) and
+// the path integral of B, and stores kk (b + f) and kk (b - f) to
+// pp[face][lane][2][V].  k_faces2d_eigsum adds each face's four points as
+// a butterfly over the lanes would, (l0 + l1) + (l2 + l3), into
+// fb[face][2][V].  A one-kernel form (the four points of a face in
+// neighbouring lanes, summed by shuffles) gave, on two-material (V = 15)
+// grids, faces that differed from the oracle by up to 4e-2 (Osher only)
+// while the same states through the pointwise kernel matched it to 2e-15,
+// also under 1e-15 noise; this form keeps the per-point evaluation in the
+// pointwise kernel's shape.  With millions of independent eigenproblems in
+// a 512 x 512 step, one thread per eigenproblem beats a warp per
+// eigenproblem (k_faces1d_eigw, built for the few faces of a 1D grid).
 template <class L>
-__global__ void __launch_bounds__(128) k_faces2d_eigt(
-    double *__restrict__ fb, const double *__restrict__ qh, int nx, int ny, int dir,
+__global__ void __launch_bounds__(64) k_faces2d_eigp(
+    double *__restrict__ pp, const double *__restrict__ qh, int nx, int ny, int dir,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
     double dy, int time_dg, int flux, DevPar P, Consts C) {
   constexpr int V = L::V;
   constexpr int NQ = NN * NN;
   if (dt_dev)
     dt = *dt_dev;
-  long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  int lq = threadIdx.x % NQ;
-  int t = lq / NN, s = lq % NN;
-  long face = gt / NQ;
-  long nf = (long)(nx + 1) * (ny + 1);
-  bool valid = face < nf;
-  long fi = valid ? face : 0;
-  int i = fi / (ny + 1), j = fi % (ny + 1);
-  long cb = (long)i * (ny + 2) + j;
-  long cn = dir == 0 ? cb + (ny + 2) : cb + 1;
-  bool geo = dir == 0 ? (j > 0) : (i > 0);
-  bool active = valid && geo && (mask == nullptr || (mask[cb] && mask[cn])) &&
-                (time_dg || t == 0);
-  int nt = time_dg ? NN : 1;
-  int tt = time_dg ? t : 0;
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long nf = (long)(nx + 1) * (ny + 1);
+  if (gt >= nf * NQ)
+    return;
+  const long fi = gt / NQ;
+  const int lq = (int)(gt % NQ), t = lq / NN, s = lq % NN;
+  const int i = fi / (ny + 1), j = fi % (ny + 1);
+  const long cb = (long)i * (ny + 2) + j;
+  const long cn = dir == 0 ? cb + (ny + 2) : cb + 1;
+  const bool geo = dir == 0 ? (j > 0) : (i > 0);
+  const bool active = geo && (mask == nullptr || (mask[cb] && mask[cn])) && (time_dg || t == 0);
+  double *o = pp + gt * 2 * V;
+  if (!active) {
+#pragma unroll
+    for (int k = 0; k < 2 * V; k++)
+      o[k] = 0.0;
+    return;
+  }
+  const int nt = time_dg ? NN : 1, tt = time_dg ? t : 0;
   const double *q0 = qh + (cb * nt + tt) * NN * NN * V;
   const double *q1 = qh + (cn * nt + tt) * NN * NN * V;
   double ql[V], qr[V], f[V], b[V];
-  long o0 = dir == 0 ? (long)s * V : (long)s * NN * V;
-  long st = dir == 0 ? (long)NN * V : (long)V;
+  const long o0 = dir == 0 ? (long)s * V : (long)s * NN * V;
+  const long st = dir == 0 ? (long)NN * V : (long)V;
 #pragma unroll
   for (int k = 0; k < V; k++) {
     ql[k] = C.endv[1][0] * q0[o0 + k] + C.endv[1][1] * q0[o0 + st + k];
     qr[k] = C.endv[0][0] * q1[o0 + k] + C.endv[0][1] * q1[o0 + st + k];
   }
-  double wt = time_dg ? dt * C.w[t] : dt;
-  double kk = wt / (2.0 * (dir == 0 ? dx : dy)) * C.w[s];
-  if (active) {
-    interface_point_eig<L>(ql, qr, flux, P, C, f, b, dir);
-  } else {
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      f[k] = b[k] = 0.0;
-  }
-  double *out = fb + fi * 2 * V;
+  const double wt = time_dg ? dt * C.w[t] : dt;
+  const double kk = wt / (2.0 * (dir == 0 ? dx : dy)) * C.w[s];
+  interface_point_eig<L>(ql, qr, flux, P, C, f, b, dir);
 #pragma unroll
   for (int k = 0; k < V; k++) {
-    double lft = active ? kk * (b[k] + f[k]) : 0.0;
-    double rgt = active ? kk * (b[k] - f[k]) : 0.0;
-    lft += __shfl_xor_sync(0xffffffffu, lft, 1);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 1);
-    lft += __shfl_xor_sync(0xffffffffu, lft, 2);
-    rgt += __shfl_xor_sync(0xffffffffu, rgt, 2);
-    if (valid && lq == 0) {
-      out[k] = lft;
-      out[V + k] = rgt;
-    }
+    o[k] = kk * (b[k] + f[k]);
+    o[V + k] = kk * (b[k] - f[k]);
   }
+}
+
+template <int V>
+__global__ void k_faces2d_eigsum(double *__restrict__ fb, const double *__restrict__ pp,
+                                 long nf) {
+  constexpr int NQ = NN * NN;
+  static_assert(NQ == 4, "four quadrature points per 2D face");
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= nf * 2 * V)
+    return;
+  const long face = idx / (2 * V);
+  const int e = (int)(idx % (2 * V));
+  const double *p = pp + face * NQ * 2 * V + e;
+  fb[idx] = (p[0] + p[2 * V]) + (p[4 * V] + p[6 * V]);
 }
 
 }  // namespace gpr
