@@ -562,46 +562,61 @@ struct FmmGlobal {
   int *list[2];
   int *qst;           // the sweep a point is listed for (dedupes the lists)
   int *cnt;           // cnt[3]: list lengths, rotating
-  unsigned *bar;      // bar[0] arrivals; bar[2..3] generation and list length
+  unsigned *bar;      // bar + 2: the barrier's two 64-bit words
   int *err;
   int mono_from, max_sweeps;
 };
 
-// Grid barrier of the sweeps.  bar[0] counts arrivals; the 64-bit word at
-// bar + 2 holds the generation (high half) and, published by the last block
-// to arrive, the length of the next sweep's list (low half), read from
-// *next once every block has finished its appends.  One thread per block
-// fences and waits (after the block barrier, which orders the block's
-// writes before it); the wait gives up after ~1 s (err bit 2).  Returns the
-// next list's length, or -1 after a timeout.
-GPR_D int fmm_grid_sync(unsigned *bar, unsigned nblocks, const int *next, int *err) {
+// GPU-scope acquire / release accesses (PTX memory model, sm_70 and later).
+GPR_D unsigned long long fmm_add_acq_rel64(unsigned long long *p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;"
+               : "=l"(old)
+               : "l"(p), "l"(v)
+               : "memory");
+  return old;
+}
+GPR_D unsigned long long fmm_ld_acquire(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier at the end of sweep s, which also sums the sweep's list
+// appends: the 64-bit word words[s % 2] counts the blocks' arrivals (bits
+// 40..63) and the entries they appended (bits 0..39) over the sweeps of that
+// parity.  Each block arrives once (one thread, an acquire-release add of
+// 2^40 + its appends, after the block barrier, which orders the block's
+// writes before it) and waits with acquire loads until all blocks have
+// arrived for this sweep: nblocks (s / 2 + 1) arrivals.  Two words, so that
+// a block already at the next sweep's barrier cannot be counted here.  The
+// next list's length is the sum's growth since the previous sweep of the
+// same parity (prev[2], kept by the block).  The wait gives up after ~1 s
+// (err bit 2).  Returns the length, or -1 after a timeout.
+GPR_D int fmm_grid_sync(unsigned long long *words, unsigned nblocks, int s, int appended,
+                        unsigned long long prev[2], int *err) {
   __shared__ int shn;
+  constexpr unsigned long long ARR = 1ull << 40, CNT = ARR - 1;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long *word = (unsigned long long *)(bar + 2);
-    volatile unsigned long long *vw = word;
-    const unsigned g = (unsigned)(*vw >> 32);
-    __threadfence();
-    if (atomicAdd(bar, 1u) == nblocks - 1) {
-      atomicExch(bar, 0u);
-      const int n = atomicAdd((int *)next, 0);
-      __threadfence();
-      atomicExch(word, ((unsigned long long)(g + 1u) << 32) | (unsigned)n);
-      shn = n;
-    } else {
-      const long long t0 = clock64();
-      unsigned long long v;
-      shn = -1;
-      while (((v = *vw) >> 32) == g) {
-        if (clock64() - t0 > 2000000000LL) {  // ~1 s at 2 GHz
-          atomicOr(err, 4);
-          break;
-        }
+    const int k = s & 1;
+    unsigned long long *w = words + k;
+    const unsigned long long target = (unsigned long long)nblocks * (unsigned)(s / 2 + 1);
+    unsigned long long v = fmm_add_acq_rel64(w, ARR + (unsigned)appended) + ARR + (unsigned)appended;
+    const long long t0 = clock64();
+    shn = 0;
+    while ((v >> 40) < target) {
+      if (clock64() - t0 > 2000000000LL) {  // ~1 s at 2 GHz
+        atomicOr(err, 4);
+        shn = -1;
+        break;
       }
-      if ((v >> 32) != g)
-        shn = (int)(unsigned)(v & 0xffffffffull);
+      v = fmm_ld_acquire(w);
     }
-    __threadfence();
+    if (shn == 0) {
+      shn = (int)((v & CNT) - prev[k]);
+      prev[k] = v & CNT;
+    }
   }
   __syncthreads();
   return shn;
@@ -611,7 +626,8 @@ GPR_D int fmm_grid_sync(unsigned *bar, unsigned nblocks, const int *next, int *e
 // sweep (stamps in qst): the stamps' atomics are issued back to back, and a
 // warp reserves its list entries with one atomic.
 template <int K>
-GPR_D void fmm_enqueue(const bool (&want)[K], const int (&cand)[K], int s, const FmmGlobal &G) {
+GPR_D void fmm_enqueue(const bool (&want)[K], const int (&cand)[K], int s, const FmmGlobal &G,
+                       int *appended = nullptr) {
   bool mine[K];
 #pragma unroll
   for (int k = 0; k < K; k++)
@@ -632,8 +648,11 @@ GPR_D void fmm_enqueue(const bool (&want)[K], const int (&cand)[K], int s, const
   if (total == 0)
     return;
   int base = 0;
-  if (lane == 31)
+  if (lane == 31) {
     base = atomicAdd(G.cnt + s % 3, total);
+    if (appended)
+      atomicAdd(appended, total);  // the block's appends (shared memory)
+  }
   base = __shfl_sync(0xffffffffu, base, 31);
   int pos = base + incl - nk;
   int *lst = G.list[s & 1];
@@ -665,6 +684,10 @@ __global__ void __launch_bounds__(256) k_fmm_global(Grid g, FmmConst K, FmmGloba
   const unsigned nb = gridDim.x;
   const long nthr = (long)gridDim.x * blockDim.x;
   const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  __shared__ int appended;
+  if (threadIdx.x == 0)
+    appended = 0;
+  unsigned long long prev[2] = {0ull, 0ull};  // used by thread 0
   int s = 0;
   int n = __ldcg(G.cnt);  // the first list (k_fmm_seed)
   for (; s < G.max_sweeps; s++) {
@@ -716,9 +739,14 @@ __global__ void __launch_bounds__(256) k_fmm_global(Grid g, FmmConst K, FmmGloba
 #pragma unroll
       for (int k = 1; k < 5; k++)
         want[k] = want[k] && !(G.fz[cand[k]] & 1);
-      fmm_enqueue<5>(want, cand, s + 1, G);
+      fmm_enqueue<5>(want, cand, s + 1, G, &appended);
     }
-    n = fmm_grid_sync(G.bar, nb, G.cnt + (s + 1) % 3, G.err);
+    __syncthreads();
+    const int app = appended;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      appended = 0;
+    n = fmm_grid_sync((unsigned long long *)(G.bar + 2), nb, s, app, prev, G.err);
     if (n < 0)
       return;
   }

@@ -710,11 +710,17 @@ GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const D
                            const Consts &C, double *f) {
   constexpr int V = L::V;
   double dq[V], q[V], M[V * V];
+  bool flat = true;
 #pragma unroll
   for (int k = 0; k < V; k++) {
     dq[k] = ql[k] - qr[k];
     f[k] = 0.0;
+    flat = flat && dq[k] == 0.0;
   }
+  // qL = qR (a uniform region): |A| dq is exactly zero, whatever A's
+  // eigen-decomposition
+  if (flat)
+    return;
   bool ok = true;
   if (flux == GPR_FLUX_OSHER) {
 #pragma unroll 1
@@ -1441,8 +1447,15 @@ __global__ void __launch_bounds__(32 * EIG_WARPS) k_faces1d_eigw(
       ws.f[k] = 0.0;
     }
     __syncwarp();
-    bool ok;
-    if (flux == GPR_FLUX_OSHER) {
+    // qL = qR (a uniform region): |A| dq is exactly zero, whatever A's
+    // eigen-decomposition; the dissipation stays zero without it
+    bool flat = true;
+    for (int k = lane; k < V; k += 32)
+      flat = flat && ws.dq[k] == 0.0;
+    flat = __all_sync(0xffffffffu, flat);
+    bool ok = true;
+    if (flat) {
+    } else if (flux == GPR_FLUX_OSHER) {
       for (int k = lane; k < V; k += 32)
         ws.q[k] = ws.qr[k] + C.nodes[ip] * ws.dq[k];
       __syncwarp();
