@@ -51,7 +51,9 @@ CONTORTED_TOL = 1.0
 # the TGV 512^2 kernels, from an earlier ncu capture of each (not measured by
 # this script; the line labels it so).
 TRAFFIC = {
-    "k_faces2d": 287.910912e6 + 289.751808e6,
+    # one in-place face pass (x faces of even index): every predictor
+    # cell's qh read (each cell has a face of each parity) and u updated
+    "k_faces2d": 323.219456e6 + 159.500544e6,
     "k_predictor_picard": 143.945728e6 + 229.694720e6,
 }
 
@@ -976,8 +978,10 @@ def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
     # the re-distancing alone (FP64 sweeps), on the current level set, and
     # its largest difference from the oracle's marcher there
     col = u.view(-1, 15)[:, 14].contiguous()
-    dd = ghost.distance(col, dX, nX)
+    dst = torch.zeros(4, dtype=torch.int32, device=dev)
+    dd = ghost.distance(col, dX, nX, status=dst)
     torch.cuda.synchronize()
+    redist_sweeps = int(dst[3].item())
     f0.record(stream)
     for _ in range(3):
         dd = ghost.distance(col, dX, nX)
@@ -1006,6 +1010,8 @@ def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
            "value": ncell * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
            "fill_ms": fill_ms, "fill_share": fill_ms / (ms / steps),
            "redistance_ms": redist_ms, "redistance_share": redist_ms / (ms / steps),
+           "redistance_sweeps": redist_sweeps,
+           "redistance_us_per_sweep": 1e3 * redist_ms / max(redist_sweeps, 1),
            "redistance_max_abs_diff_vs_oracle": redist_diff,
            "e2e": {"value": ncell * steps / (e2e_ms * 1e-3) / 1e6, "unit": UNIT,
                    "h2d_bytes_per_step": ncell * 15 * 8, "d2h_bytes_per_step": ncell * 15 * 8},

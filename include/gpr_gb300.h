@@ -445,11 +445,13 @@ int gpr_adj_point_vjp(const double *Q, int64_t count, const gpr_par *par, const 
  * no heat conduction) and exactly two materials: material 0 occupies
  * phi < 0, material 1 phi >= 0 (functions/vectors.cpp:24-31); pars[2].
  * nX[d] >= 3.  Every fill call accumulates error counts in the caller's
- * device status[4] (zero it first): [0] the re-distancing did not converge
- * within its round budget, [1] boundary cells whose fill would read outside
- * the grid in the reference (left unfilled), [2] extrapolation cells whose
- * copy source would lie outside the grid (they copy their layer neighbour),
- * [3] reserved.
+ * device status[4] (zero it first): [0] bit 0: the re-distancing did not
+ * converge within its budget, bit 2: its grid barrier gave up waiting
+ * (~1 s), [1] boundary cells whose fill would read outside the grid in the
+ * reference (left unfilled), [2] extrapolation cells whose copy source
+ * would lie outside the grid (they copy their layer neighbour), [3]
+ * gpr_distance on a 2D grid: the global sweeps its re-distancing took
+ * (untouched otherwise).
  *
  * gpr_distance             GPRpy.system.multi.distance (multi/pfmm.cpp:4-26):
  *                          first-order signed distance to the zero level of

@@ -266,7 +266,8 @@ const int kPlanGrid = 152 * 8;  // grid-stride launches over the plan entries
 
 // Re-distance phi (stride ps) into d; also writes u's level set when u != 0.
 int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr,
-               const FillLayout &L, int *err, const double *clk, cudaStream_t st) {
+               const FillLayout &L, int *err, const double *clk, cudaStream_t st,
+               int *sweeps = nullptr) {
   double *d = scr + L.o_d;
   uint8_t *fz = at<uint8_t>(scr, L.o_fz);
   int *cnt = at<int>(scr, L.o_cnt), *flags = at<int>(scr, L.o_flags);
@@ -294,6 +295,7 @@ int redistance(const double *phi, long ps, double *u, const Grid &g, double *scr
     G.cnt = at<int>(scr, L.o_gs);
     G.bar = (unsigned *)(G.cnt + 8);
     G.err = err;
+    G.sweeps = sweeps;
     G.mono_from = fmm_mono_sweeps(g);
     G.max_sweeps = fmm_max_sweeps(g);
     const int nb = fmm_global_blocks();
@@ -453,7 +455,7 @@ int gpr_distance(const double *phi, double *dist, const int32_t *nX, int ndim,
   Grid g = make_grid(nX, ndim, dX);
   FillLayout L = fill_layout(g);
   cudaStream_t st = S(stream);
-  int rc = redistance(phi, 1, nullptr, g, scratch, L, status, nullptr, st);
+  int rc = redistance(phi, 1, nullptr, g, scratch, L, status, nullptr, st, status + 3);
   if (rc)
     return rc;
   cudaMemcpyAsync(dist, scratch + L.o_d, g.ncell * sizeof(double), cudaMemcpyDeviceToDevice,

@@ -564,6 +564,7 @@ struct FmmGlobal {
   int *cnt;           // cnt[3]: list lengths, rotating
   unsigned *bar;      // bar + 2: the barrier's two 64-bit words
   int *err;
+  int *sweeps;        // optional: receives the sweeps taken
   int mono_from, max_sweeps;
 };
 
@@ -752,8 +753,11 @@ __global__ void __launch_bounds__(256) k_fmm_global(Grid g, FmmConst K, FmmGloba
   }
   if (gid == 0 && s >= G.max_sweeps && n != 0)
     atomicOr(G.err, 1);  // not converged within the sweep budget
-  if (gid == 0)
+  if (gid == 0) {
     G.cnt[3] = s;  // the sweeps taken
+    if (G.sweeps)
+      *G.sweeps = s;
+  }
 }
 
 // Final values (base_marcher.cpp:103-106, 190-196): zeros when nothing

@@ -311,3 +311,55 @@ def test_errors_are_raised(G):
         G.solvers.fv.interfs2(u2, torch.zeros(6 * 6 * 8 * 17, dtype=torch.float64, device=DEV),
                               4, 4, 1e-3, 0.1, 0.1, True, -1, MP,
                               torch.ones(36, dtype=torch.bool, device=DEV))
+
+
+@pytest.mark.parametrize("shape", [(13, 7), (31, 1 + 31), (62, 3)])
+def test_odd_grids_step_against_oracle(G, shape):
+    """Grids whose sizes exercise the edges of the launch decompositions: odd
+    face counts along each direction for the four in-place face passes (x
+    and y faces of even and odd index), WENO tiles that end mid-row (58
+    output columns per block), a 1D grid the size of one FV tile (31 cells)
+    and one past it; an ADER step (Rusanov) and the FV stage alone with NULL
+    scratch (the Rusanov passes use none) against the oracle, 1e-10."""
+    import ctypes
+    from oracle import Oracle
+    from phd_gb300 import _lib
+    O = Oracle()
+    nx, ny = shape
+    if ny == 1 + 31:  # the 1D cases: 31 and 32 cells
+        cases = [(np.array([31], np.int32), 0), (np.array([32], np.int32), 0)]
+    else:
+        cases = [(np.array([nx, ny], np.int32), 1)]
+    for nX, bc in cases:
+        if nX.size == 1:
+            u0, MP, tf, dX, bcs = G.problems.shock_tube(nx=int(nX[0]))
+            u0, _, _ = O.run(u0, MP, 1e9, dX, 0, max_steps=8)
+        else:
+            u0, MP, tf, dX, bcs = G.problems.taylor_green(n=int(nX[0]), ny=int(nX[1]), cs=10.0,
+                                                        mu=1.0)
+        bcl = [bc] * (2 * nX.size)
+        dt = O.timestep(u0, dX, 0.4, 0, 1e9, 0, MP)
+        ub = O.boundaries(u0, nX, bcl)
+        ref = u0.ravel().copy()
+        O.ader_stepper(ref, ub, nX, dt, dX, MP)
+        u = T(u0).view(-1)
+        ubt = torch.empty_like(T(ub))
+        G.boundaries(u, ubt, nX, bcl)
+        G.solvers.ader_stepper(u, ubt, nX, dt, dX, False, 0, MP, None)
+        assert rel_err(H(u), ref) < 1e-10, (nX, rel_err(H(u), ref))
+        # the FV stage alone through the C ABI with no scratch (Rusanov)
+        wh = O.weno_launcher(ub, nX)
+        qh, _ = O.predictor(wh, dt, dX, nX, MP)
+        ref2 = u0.ravel().copy()
+        O.fv_launcher(ref2, qh, nX, dt, dX, MP)
+        lib = _lib.load()
+        cp = MP.to_ctypes()
+        u2 = T(u0).view(-1)
+        qt = T(np.asarray(qh).ravel())
+        dXa = np.asarray(dX, np.float64)
+        _lib.check(lib.gpr_fv_launcher(
+            ctypes.c_void_p(u2.data_ptr()), ctypes.c_void_p(qt.data_ptr()),
+            nX.ctypes.data_as(ctypes.c_void_p), dt, dXa.ctypes.data_as(ctypes.c_void_p),
+            int(nX.size), 1, 1, 0, ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None, None,
+            17, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "fv")
+        assert rel_err(H(u2), ref2) < 1e-12, (nX, rel_err(H(u2), ref2))
