@@ -56,7 +56,7 @@ struct BatchShapes {
 struct BatchLayout {
   long nu = 0, nub = 0, nb = 0, nf = 0;
   long o_par, o_iu, o_iub, o_ib, o_if, o_nx, o_ou, o_oub, o_ob, o_of, o_bc, o_idx, o_mx;
-  long o_ub, o_wh, o_qh, o_fb, total;
+  long o_ub, o_wh, o_qh, o_fb, o_rlist, o_rn, o_rit, o_rdmin, total;
 };
 
 inline BatchLayout batch_layout_v(int ninst, const int32_t *nx, int V) {
@@ -86,6 +86,10 @@ inline BatchLayout batch_layout_v(int ninst, const int32_t *nx, int V) {
   b.o_wh = cv.take(b.nb * NN * V);
   b.o_qh = cv.take(b.nb * NN * NN * V);
   b.o_fb = cv.take(b.nf * 2 * V);
+  b.o_rlist = cv.take(dbl(b.nb * 4));
+  b.o_rn = cv.take(1);
+  b.o_rit = cv.take(dbl(b.nb * 4));
+  b.o_rdmin = cv.take(b.nb);
   b.total = cv.o;
   return b;
 }

@@ -603,12 +603,20 @@ __global__ void __launch_bounds__(128) k_predictor_first(
 // status[c] (optional): GPR_PRED_PICARD | iterations << 8 when converged,
 // GPR_PRED_FAILED when Picard did not converge (row left for the Newton pass,
 // with the last Picard iterate written so the row is always defined).
+struct PicardResume {
+  int cap = 0;
+  int *list = nullptr, *n = nullptr;
+  int *it = nullptr;
+  double *dmin = nullptr;
+  const int *in = nullptr, *n_in = nullptr;
+};
+
 template <class L, int ND, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_predictor_picard(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
     const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar Pv, Consts C,
-    Batch B, int first) {
+    Batch B, int first, PicardResume R = PicardResume{}) {
   constexpr int V = L::V;
   constexpr int NS = ND == 1 ? NN : NN * NN;  // spatial nodes
   constexpr int NP = NN * NS;                 // space-time nodes
@@ -618,6 +626,11 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   int g = threadIdx.x % NP;
   long c = gt / NP;
   bool valid = c < ncb;
+  if (R.in) {
+    const long qi = gt / NP;
+    valid = qi < *R.n_in;
+    c = valid ? R.in[qi] : 0;
+  }
   const int inst = BATCH ? B.inst_b[valid ? c : 0] : 0;
   const DevPar &P = BATCH ? B.P[inst] : Pv;
   if (BATCH) {
@@ -635,7 +648,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   for (int k = 0; k < V; k++) {
     w[k] = valid ? wc[k] : 1.0;
     Ww[k] = f * w[k];
-    q[k] = w[k];  // standard initial guess (initial_guess.cpp:4-15)
+    q[k] = (R.in && valid) ? qh[(cc * NP + g) * V + k] : w[k];
   }
   // groups are aligned to NP lanes; the group shares the convergence decision
   unsigned lane = threadIdx.x & 31u;
@@ -654,11 +667,34 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
   // 4 .. 25 iterations and saturate near O(1) updates (without this test
   // they run the whole cap of 50).  So every cell the reference's Picard
   // iteration converges still converges by Picard.
-  double dmin = 1e300;
-  for (int it = 0; it < maxit; it++) {
+  const bool resume = R.in != nullptr && valid;
+  const int it0 = resume ? R.it[c] : 0;
+  double dmin = resume ? R.dmin[c] : 1e300;
+  bool failed = false, deferred = false;
+  for (int kq = 0;; kq++) {
+    const int it = it0 + kq;
+    if (!done && it >= maxit) {
+      failed = true;
+      done = true;
+    }
+    if (!done && R.cap > 0 && kq == R.cap) {
+      double *outd = qh + (c * NP + g) * V;
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        outd[k] = q[k];
+      if (g == 0) {
+        R.it[c] = it;
+        R.dmin[c] = dmin;
+        R.list[atomicAdd(R.n, 1)] = (int)c;
+      }
+      deferred = true;
+      done = true;
+    }
     if (__all_sync(0xffffffffu, done))
       break;
-    if (it == 0 && first) {
+    // (a continuation never takes this branch, not even on its unused lanes,
+    // whose it0 is 0: the other branch's shuffles need the whole warp)
+    if (it == 0 && first && R.in == nullptr) {
       // the first iterate, from k_predictor_first
       const double *src = qh + (cc * NP + g) * V;
 #pragma unroll
@@ -699,7 +735,8 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
       done = true;
       iters = it + 1;
     }
-    dmin = dmax < dmin ? dmax : dmin;
+    if (!done)
+      dmin = dmax < dmin ? dmax : dmin;
     if (!done) {
       iters = it + 1;
       if (bigm) {
@@ -725,7 +762,7 @@ __global__ void __launch_bounds__(128) k_predictor_picard(
       }
     }
   }
-  if (active && (!done || nan_seen)) {
+  if (active && !deferred && (failed || nan_seen)) {
     // Picard failed: write the initial guess and flag the cell for the
     // stiff-source Newton pass with a NaN in its first entry
     double *out = qh + (c * NP + g) * V;

@@ -675,7 +675,7 @@ static int iterate_multi(double *u, const int32_t *nX, int ndim, const double *d
       if ((rc = Ops<L15>::weno(wh, ub, nX, ndim, tmp, st)))
         return rc;
       if ((rc = Ops<L15>::predictor(qh, wh, 0.0, dt_dev, dX, ndim, nX, stiff, P[m], maskb, pst,
-                                    st)))
+                                    st, tmp)))
         return rc;
       if ((rc = Ops<L15>::fv(grid, qh, nX, 0.0, dt_dev, dX, ndim, 1, 1, P[m], maskb, tmp, st,
                              flux)))

@@ -196,22 +196,51 @@ template <class L> struct Ops {
     return cuda_rc();
   }
 
+  // Deferred Picard cells (PicardResume) in a caller's scratch of at least
+  // predictor_resume_doubles(ncb) doubles: the list, its length, the next
+  // iteration indices and the smallest updates.
+  static long predictor_resume_doubles(long ncb) { return 2 * ncb + 8; }
+  static PicardResume resume_view(double *scr, long ncb) {
+    PicardResume R;
+    R.cap = 3;
+    R.dmin = scr;
+    R.it = (int *)(scr + ncb);
+    R.list = R.it + ncb;
+    R.n = R.list + ncb;
+    return R;
+  }
+
+  // resume: optional scratch (predictor_resume_doubles) with which cells
+  // still iterating after three Picard iterations continue in a second
+  // launch over a compacted list of them (k_predictor_picard, PicardResume).
   static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
                        const double *dX, int nd, const int32_t *nX, int stiff,
                        const DevPar &P, const uint8_t *mask, int32_t *status,
-                       cudaStream_t st) {
+                       cudaStream_t st, double *resume = nullptr) {
     const Consts &C = consts();
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
     // the first Picard iterate at one thread per spatial node (k_predictor_first)
     const int first = stiff ? 0 : 1;
+    PicardResume R, R2;
+    if (resume && !stiff) {
+      R = resume_view(resume, ncb);
+      cudaMemsetAsync(R.n, 0, sizeof(int), st);
+      R2.it = R.it;
+      R2.dmin = R.dmin;
+      R2.in = R.list;
+      R2.n_in = R.n;
+    }
     if (nd == 1) {
       if (first)
         k_predictor_first<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(
             qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
       long nt = ncb * NN * NN;
       k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first);
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R);
+      if (R.cap)
+        k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
+            qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R2);
       return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
     }
     if (first)
@@ -219,7 +248,10 @@ template <class L> struct Ops {
           qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
     long nt = ncb * NN * NN * NN;
     k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
-        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first);
+        qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R);
+    if (R.cap)
+      k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R2);
     return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
   }
 
@@ -413,7 +445,9 @@ template <class L> struct Ops {
       rc = weno(wh, ub, nX, nd, tmp, st);
       if (rc)
         return rc;
-      rc = predictor(qh, wh, 0.0, dt_dev, dX, nd, nX, 0, P, mask, status, st);
+      // tmp (the FV face buffers, used after the predictor) holds the
+      // predictor's deferred cells meanwhile
+      rc = predictor(qh, wh, 0.0, dt_dev, dX, nd, nX, 0, P, mask, status, st, tmp);
       if (rc)
         return rc;
       rc = fv(u, qh, nX, 0.0, dt_dev, dX, nd, 1, 1, P, mask, tmp, st, flux);
@@ -551,13 +585,27 @@ template <class L> struct Ops {
   }
   static void batch_picard_pair(double *qh, const double *wh, int32_t *status,
                                 const BatchLayout &b, const Batch &B, int bs_first,
-                                int bs_picard, cudaStream_t st) {
+                                int bs_picard, double *scr, cudaStream_t st) {
     const Consts &C = consts();
     DevPar P0{};
+    PicardResume R;
+    R.cap = 3;
+    R.list = (int *)(scr + b.o_rlist);
+    R.n = (int *)(scr + b.o_rn);
+    R.it = (int *)(scr + b.o_rit);
+    R.dmin = scr + b.o_rdmin;
+    cudaMemsetAsync(R.n, 0, sizeof(int), st);
     k_predictor_first<L, 1, true><<<blocks(b.nb * NN, bs_first), bs_first, 0, st>>>(
         qh, wh, b.nb, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C, B);
     k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, bs_picard), bs_picard, 0, st>>>(
-        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1);
+        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1, R);
+    PicardResume R2;
+    R2.it = R.it;
+    R2.dmin = R.dmin;
+    R2.in = R.list;
+    R2.n_in = R.n;
+    k_predictor_picard<L, 1, true><<<blocks(b.nb * NN * NN, bs_picard), bs_picard, 0, st>>>(
+        qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, 0, P0, C, B, 1, R2);
   }
   static void batch_faces(double *fb, const double *qh, const BatchLayout &b, const Batch &B,
                           int split, int bs, cudaStream_t st) {
@@ -591,7 +639,7 @@ template <class L> struct Ops {
       batch_cfl(u, mx, b, B, ninst, st);
       k_b_boundaries<V><<<blocks(b.nub * V, 256), 256, 0, st>>>(u, ub, b.nub, B);
       batch_weno(wh, ub, b, B, sh.weno, st);
-      batch_picard_pair(qh, wh, status, b, B, sh.first, sh.picard, st);
+      batch_picard_pair(qh, wh, status, b, B, sh.first, sh.picard, scr, st);
       int rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, status, 0.0, nullptr, 1.0, 1.0, P0,
                                    C, st, B);
       if (rc)
@@ -679,7 +727,7 @@ template <class L> struct Ops {
       float best = 1e30f;
       for (int f : bs3)
         for (int p : bs3) {
-          float ms = timeit([&] { batch_picard_pair(qh, wh, nullptr, b, B, f, p, st); });
+          float ms = timeit([&] { batch_picard_pair(qh, wh, nullptr, b, B, f, p, scr, st); });
           if (rc)
             break;
           if (ms < best) {
@@ -692,7 +740,7 @@ template <class L> struct Ops {
     if (!rc) {
       // a complete predictor (the Newton pass finishes flagged cells) for the
       // face and volume timings
-      batch_picard_pair(qh, wh, nullptr, b, B, sh.first, sh.picard, st);
+      batch_picard_pair(qh, wh, nullptr, b, B, sh.first, sh.picard, scr, st);
       rc = stiff_pass<1, true>(qh, wh, b.nb, nullptr, nullptr, 0.0, nullptr, 1.0, 1.0, P0, C,
                                st, B);
     }
