@@ -19,6 +19,39 @@ inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
 inline int blocks(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// SMs of the current device, read once per device.
+inline int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64)
+    return 152;
+  if (!cache[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = n > 0 ? n : 152;
+  }
+  return cache[dev];
+}
+
+// Threads per block for n threads of a kernel written for bs (a power of
+// two): halved, down to one warp, while the grid would hold fewer than two
+// blocks per SM.  On GB300 a warp issues one FP64 instruction per ~63
+// cycles whatever its active lanes, and an SM one per ~19 cycles over all
+// its warps, so the few warps of a small grid (the 200-cell tube) finish
+// their FP64 chains sooner on separate SMs than four or eight to an SM.
+// For kernels whose threads are independent, or whose block reduction is a
+// max, the result is the same at any block size.
+inline int spread(long n, int bs) {
+  const long want = 2L * sm_count();
+  while (bs > 32 && (n + bs - 1) / bs < want)
+    bs >>= 1;
+  return bs;
+}
+
+// grid and block of a launch of n threads shaped by spread()
+#define GPR_SPREAD(n, bs) blocks((n), spread((n), (bs))), spread((n), (bs))
+
 inline int cuda_rc() {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -1617,32 +1617,36 @@ __global__ void __launch_bounds__(128) k_cells(
 }
 
 // The whole 1D FV update of fv_launcher (centers1 + interfs1, fv.cpp:11-160)
-// in one launch, Rusanov flux: a block takes a tile of FV1_TILE cells; its
-// 128 threads first evaluate the tile's FV1_TILE + 1 faces (one lane per
+// in one launch, Rusanov flux: a block takes a tile of TILE cells; its
+// 4 (TILE + 1) threads first evaluate the tile's TILE + 1 faces (one lane per
 // face, time node and side, as k_faces1d_split) into shared memory, then
 // the cells' volume terms (one lane per space-time node, as k_cells), and
 // each cell's lanes apply u += volume - its two faces' contributions.  A
-// face between two tiles is evaluated by both (one face in 32 twice); the
-// sums and their order are those of the two-launch form.
+// face between two tiles is evaluated by both (one face in TILE + 1 twice);
+// the sums and their order are those of the two-launch form.
+// A small grid takes tiles of FV1_TILE_SMALL cells (one warp per block), so
+// that its few warps run on separate SMs.
 constexpr int FV1_TILE = 31;
-template <class L>
+constexpr int FV1_TILE_SMALL = 7;
+template <class L, int TILE = FV1_TILE>
 __global__ void __launch_bounds__(128) k_fv1d(
     double *__restrict__ u, const double *__restrict__ qh, long nx,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
     int sources, int time_dg, DevPar P, Consts C, int parts) {
   constexpr int V = L::V;
-  static_assert(NN == 2 && 4 * (FV1_TILE + 1) == 128, "four lanes per face and per cell");
-  __shared__ double sfb[(FV1_TILE + 1) * 2 * V];
+  static_assert(NN == 2 && 4 * (TILE + 1) <= 128 && (TILE + 1) % 8 == 0,
+                "four lanes per face and per cell, whole warps");
+  __shared__ double sfb[(TILE + 1) * 2 * V];
   if (dt_dev)
     dt = *dt_dev;
-  const long c0 = (long)blockIdx.x * FV1_TILE;  // first cell, and first face, of the tile
+  const long c0 = (long)blockIdx.x * TILE;  // first cell, and first face, of the tile
   const int slot = threadIdx.x >> 2, lq = threadIdx.x & 3;
   if (parts & FV_INTERFS)
     faces1d_split_body<L, false>(sfb, qh, nx + 1, mask, dt, dx, time_dg, P, C, Batch{},
                                  c0 + slot, lq, true, c0);
   __syncthreads();
   cells_body<L, 1, false>(u, qh, sfb, nullptr, nx, 1, mask, dt, dx, 1.0, sources, time_dg, P, C,
-                          Batch{}, parts, c0 + slot, lq, slot < FV1_TILE, c0);
+                          Batch{}, parts, c0 + slot, lq, slot < TILE, c0);
 }
 
 // ---------------------------------------------------------------------------

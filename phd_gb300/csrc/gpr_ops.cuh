@@ -184,7 +184,7 @@ template <class L> struct Ops {
     const Consts &C = consts();
     if (nd == 1) {
       int ncb = nX[0] + 2;
-      k_weno1d<V><<<blocks((long)ncb * V, 256), 256, 0, st>>>(wh, ub, ncb, C);
+      k_weno1d<V><<<GPR_SPREAD((long)ncb * V, 256), 0, st>>>(wh, ub, ncb, C);
       return cuda_rc();
     }
     // both sweeps in one launch through shared memory (k_weno2d); the
@@ -210,9 +210,10 @@ template <class L> struct Ops {
     return R;
   }
 
-  // resume: optional scratch (predictor_resume_doubles) with which cells
-  // still iterating after three Picard iterations continue in a second
-  // launch over a compacted list of them (k_predictor_picard, PicardResume).
+  // resume: optional scratch (predictor_resume_doubles) with which, on grids
+  // of 8192 cells or more, cells still iterating after three Picard
+  // iterations continue in a second launch over a compacted list of them
+  // (k_predictor_picard, PicardResume).
   static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
                        const double *dX, int nd, const int32_t *nX, int stiff,
                        const DevPar &P, const uint8_t *mask, int32_t *status,
@@ -223,7 +224,10 @@ template <class L> struct Ops {
     // the first Picard iterate at one thread per spatial node (k_predictor_first)
     const int first = stiff ? 0 : 1;
     PicardResume R, R2;
-    if (resume && !stiff) {
+    // Below ~8k cells the Picard launch fits in one wave of resident warps,
+    // so there are no later warps to free and the continuation would only
+    // add its launch (the 200-cell tube: ~8 us per step).
+    if (resume && !stiff && ncb >= 8192) {
       R = resume_view(resume, ncb);
       cudaMemsetAsync(R.n, 0, sizeof(int), st);
       R2.it = R.it;
@@ -233,24 +237,24 @@ template <class L> struct Ops {
     }
     if (nd == 1) {
       if (first)
-        k_predictor_first<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(
+        k_predictor_first<L, 1><<<GPR_SPREAD(ncb * NN, 128), 0, st>>>(
             qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
       long nt = ncb * NN * NN;
-      k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
+      k_predictor_picard<L, 1><<<GPR_SPREAD(nt, 128), 0, st>>>(
           qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R);
       if (R.cap)
-        k_predictor_picard<L, 1><<<blocks(nt, 128), 128, 0, st>>>(
+        k_predictor_picard<L, 1><<<GPR_SPREAD(nt, 128), 0, st>>>(
             qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R2);
       return stiff_pass<1>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
     }
     if (first)
-      k_predictor_first<L, 2><<<blocks(ncb * NN * NN, 128), 128, 0, st>>>(
+      k_predictor_first<L, 2><<<GPR_SPREAD(ncb * NN * NN, 128), 0, st>>>(
           qh, wh, ncb, mask, dt, dt_dev, idx, idy, P, C, Batch{});
     long nt = ncb * NN * NN * NN;
-    k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
+    k_predictor_picard<L, 2><<<GPR_SPREAD(nt, 128), 0, st>>>(
         qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R);
     if (R.cap)
-      k_predictor_picard<L, 2><<<blocks(nt, 128), 128, 0, st>>>(
+      k_predictor_picard<L, 2><<<GPR_SPREAD(nt, 128), 0, st>>>(
           qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C, Batch{}, first, R2);
     return stiff_pass<2>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P, C, st);
   }
@@ -286,8 +290,13 @@ template <class L> struct Ops {
     if (nd == 1) {
       if (flux == GPR_FLUX_RUSANOV || !faces) {
         // faces, volume term and update in one launch (k_fv1d)
-        k_fv1d<L><<<blocks(nx, FV1_TILE), 128, 0, st>>>(u, qh, nx, mask, dt, dt_dev, dX[0],
-                                                        sources, time_dg, P, C, parts);
+        if (blocks(nx, FV1_TILE) < 2 * sm_count())
+          k_fv1d<L, FV1_TILE_SMALL><<<blocks(nx, FV1_TILE_SMALL), 4 * (FV1_TILE_SMALL + 1), 0,
+                                      st>>>(u, qh, nx, mask, dt, dt_dev, dX[0], sources,
+                                            time_dg, P, C, parts);
+        else
+          k_fv1d<L><<<blocks(nx, FV1_TILE), 128, 0, st>>>(u, qh, nx, mask, dt, dt_dev, dX[0],
+                                                          sources, time_dg, P, C, parts);
         return cuda_rc();
       }
       // Osher / Roe: the faces' eigen-decompositions, one warp each, write
@@ -297,9 +306,9 @@ template <class L> struct Ops {
       k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
           scratch, qh, (long)nx + 1, mask, dt, dt_dev, dX[0], time_dg, flux, P, C, Batch{});
       long nc = (long)nx * NN * NN;
-      k_cells<L, 1><<<blocks(nc, 128), 128, 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
-                                                      dt_dev, dX[0], 1.0, sources, time_dg, P,
-                                                      C, Batch{}, parts);
+      k_cells<L, 1><<<GPR_SPREAD(nc, 128), 0, st>>>(u, qh, scratch, nullptr, nx, 1, mask, dt,
+                                                     dt_dev, dX[0], 1.0, sources, time_dg, P,
+                                                     C, Batch{}, parts);
       return cuda_rc();
     }
     int ny = nX[1];
@@ -346,7 +355,7 @@ template <class L> struct Ops {
     if (nd == 1) {
       long nf = (long)(nx + 1) * NN;
       if (flux == GPR_FLUX_RUSANOV)
-        k_faces1d_split<L><<<blocks(nf * 2, 128), 128, 0, st>>>(
+        k_faces1d_split<L><<<GPR_SPREAD(nf * 2, 128), 0, st>>>(
             fb, qh, (long)nx + 1, mask, dt, nullptr, dX[0], time_dg, P, C, Batch{});
       else
         k_faces1d_eigw<L><<<(unsigned)(nx + 1), 32 * EIG_WARPS, 0, st>>>(
@@ -389,14 +398,14 @@ template <class L> struct Ops {
                       double *scratch, cudaStream_t st) {
     unsigned long long *mx = (unsigned long long *)scratch;
     cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st);
-    k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+    k_cfl_max<L><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, nd, dX[0],
                                                       nd == 2 ? dX[1] : 1.0, mx, P);
     k_cfl_finalize<<<1, 1, 0, st>>>(mx, cfl, t, tf, count, dt_out);
     return cuda_rc();
   }
 
   static int renorm(double *u, long ncell, const DevPar &P, cudaStream_t st) {
-    k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, nullptr);
+    k_renorm<V><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, P.rho0, nullptr);
     return cuda_rc();
   }
 
@@ -405,8 +414,8 @@ template <class L> struct Ops {
   static void contortion(double *u, long ncell, double tol, const DevPar &P0, const DevPar &P1,
                          int *flag, const double *dt_dev, cudaStream_t st) {
     cudaMemsetAsync(flag, 0, sizeof(int), st);
-    k_contorted<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, tol, flag, dt_dev);
-    k_reset_distortion<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, flag, P0, P1, dt_dev);
+    k_contorted<V><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, tol, flag, dt_dev);
+    k_reset_distortion<L><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, flag, P0, P1, dt_dev);
   }
 
   static int pointwise(int what, const double *Q, const double *X, double *out, double *out2,
@@ -465,7 +474,7 @@ template <class L> struct Ops {
   // first step.
   static void step_head(const double *u, long ncell, int nd, const double *dX, const DevPar &P,
                         unsigned long long *mx, double *clk, cudaStream_t st) {
-    k_cfl_max<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, nd, dX[0],
+    k_cfl_max<L><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, nd, dX[0],
                                                       nd == 2 ? dX[1] : 1.0, mx, P);
     k_clock_finalize<<<1, 1, 0, st>>>(mx, clk, (int *)(mx + 1));
   }
@@ -473,9 +482,9 @@ template <class L> struct Ops {
                         unsigned long long *mx, double *clk, cudaStream_t st) {
     const double *dt_dev = clk + 1;
     int *flag = (int *)(mx + 1);
-    k_renorm_contorted<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, tol, flag,
+    k_renorm_contorted<V><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, P.rho0, tol, flag,
                                                                dt_dev);
-    k_reset_distortion<L><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, flag, P, P, dt_dev);
+    k_reset_distortion<L><<<GPR_SPREAD(ncell, 256), 0, st>>>(u, ncell, flag, P, P, dt_dev);
     k_clock_advance<<<1, 1, 0, st>>>(clk, mx);
   }
 
@@ -486,10 +495,10 @@ template <class L> struct Ops {
     long ncb = nd == 1 ? nX[0] + 2 : (long)(nX[0] + 2) * (nX[1] + 2);
     double idx = 1.0 / dX[0], idy = nd == 2 ? 1.0 / dX[1] : 1.0;
     if (nd == 1)
-      k_midstep<L, 1><<<blocks(ncb * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev, idx,
+      k_midstep<L, 1><<<GPR_SPREAD(ncb * NN, 128), 0, st>>>(wh, ncb, mask, dt, dt_dev, idx,
                                                               idy, P, C);
     else
-      k_midstep<L, 2><<<blocks(ncb * NN * NN, 128), 128, 0, st>>>(wh, ncb, mask, dt, dt_dev,
+      k_midstep<L, 2><<<GPR_SPREAD(ncb * NN * NN, 128), 0, st>>>(wh, ncb, mask, dt, dt_dev,
                                                                    idx, idy, P, C);
     return cuda_rc();
   }
@@ -507,7 +516,7 @@ template <class L> struct Ops {
     long ns = nd == 1 ? NN : NN * NN;
     double *wh = scratch, *tmp = wh + ncb * ns * V;
     // the half steps on u and ub in one launch
-    k_ode<L><<<blocks(ncell + nub, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P, ub,
+    k_ode<L><<<GPR_SPREAD(ncell + nub, 128), 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P, ub,
                                                        nub);
     int rc = weno(wh, ub, nX, nd, tmp, st);
     if (rc)
@@ -517,7 +526,7 @@ template <class L> struct Ops {
     rc = fv(u, wh, nX, dt, dt_dev, dX, nd, 0, 0, P, mask, tmp, st, flux);
     if (rc)
       return rc;
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
+    k_ode<L><<<GPR_SPREAD(ncell, 128), 0, st>>>(u, ncell, dt / 2, dt_dev, 0.5, P);
     return cuda_rc();
   }
 
@@ -784,7 +793,7 @@ template <class L> struct Ops {
   }
 
   static int ode(double *u, long ncell, double dt, const DevPar &P, cudaStream_t st) {
-    k_ode<L><<<blocks(ncell, 128), 128, 0, st>>>(u, ncell, dt, nullptr, 1.0, P);
+    k_ode<L><<<GPR_SPREAD(ncell, 128), 0, st>>>(u, ncell, dt, nullptr, 1.0, P);
     return cuda_rc();
   }
 };

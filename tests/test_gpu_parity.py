@@ -318,16 +318,19 @@ def test_odd_grids_step_against_oracle(G, shape):
     """Grids whose sizes exercise the edges of the launch decompositions: odd
     face counts along each direction for the four in-place face passes (x
     and y faces of even and odd index), WENO tiles that end mid-row (58
-    output columns per block), a 1D grid the size of one FV tile (31 cells)
-    and one past it; an ADER step (Rusanov) and the FV stage alone with NULL
-    scratch (the Rusanov passes use none) against the oracle, 1e-10."""
+    output columns per block), 1D grids the size of one one-launch FV tile
+    and one past it (7 and 8 cells, 31 and 32), and a 1D grid of 9500 cells,
+    large enough (more than two tiles of 31 cells per SM of a 152-SM GPU)
+    for the 31-cell tiles and the full-size blocks of the other 1D kernels;
+    an ADER step (Rusanov) and the FV stage alone with NULL scratch (the
+    Rusanov passes use none) against the oracle, 1e-10."""
     import ctypes
     from oracle import Oracle
     from phd_gb300 import _lib
     O = Oracle()
     nx, ny = shape
     if ny == 1 + 31:  # the 1D cases: 31 and 32 cells
-        cases = [(np.array([31], np.int32), 0), (np.array([32], np.int32), 0)]
+        cases = [(np.array([n], np.int32), 0) for n in (7, 8, 31, 32, 9500)]
     else:
         cases = [(np.array([nx, ny], np.int32), 1)]
     for nX, bc in cases:
