@@ -82,6 +82,8 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--cfl", type=float, default=0.4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-issue", action="store_true",
+                    help="print the FP64 issue-rate probe (cycles per warp instruction) and exit")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-shock-bubble", action="store_true")
@@ -341,6 +343,84 @@ extern "C" int dmma_peak_launch(double *out, int iters, int grid, int block, voi
   return (int)cudaGetLastError();
 }
 """
+
+
+# FP64 issue rate of one warp and of one SM (own kernel): each thread of one
+# block runs `iters` dependent DFMAs (or four independent chains) if its lane
+# is below `active`; clock64 around the loop.  Cycles per warp instruction
+# against active lanes and warps per block show what bounds a kernel whose
+# few warps each run a long FP64 chain (the small 1D grids).
+FP64_ISSUE_SRC = r"""
+#include <cuda_runtime.h>
+__global__ void fp64_issue(double *out, long long *cyc, int active, int iters, int ilp) {
+  const int lane = threadIdx.x & 31;
+  double a = 1.0 + threadIdx.x * 1e-9, a2 = a + 1e-3, a3 = a + 2e-3, a4 = a + 3e-3;
+  const double b = 0.999999, c = 1e-7;
+  __syncwarp();
+  const long long t0 = clock64();
+  if (lane < active) {
+    if (ilp == 1) {
+      for (int i = 0; i < iters; i++)
+        a = fma(a, b, c);
+    } else {
+      for (int i = 0; i < iters; i++) {
+        a = fma(a, b, c);
+        a2 = fma(a2, b, c);
+        a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c);
+      }
+    }
+  }
+  __syncwarp();
+  const long long t1 = clock64();
+  out[threadIdx.x] = a + a2 + a3 + a4;
+  if (threadIdx.x == 0)
+    cyc[0] = t1 - t0;
+}
+extern "C" int fp64_issue_launch(double *out, long long *cyc, int active, int iters, int ilp,
+                                 int block, void *stream) {
+  fp64_issue<<<1, block, 0, (cudaStream_t)stream>>>(out, cyc, active, iters, ilp);
+  return (int)cudaGetLastError();
+}
+"""
+
+
+def fp64_issue_probe(torch):
+    """Cycles per FP64 warp instruction of one block on one SM, for 1 / 4 / 8
+    warps, 1 and 32 active lanes, dependent and four-way independent chains:
+    one JSON line."""
+    from phd_gb300 import _lib
+    bdir = os.path.join(ROOT, "phd_gb300", "_build")
+    so = os.path.join(bdir, "fp64issue.so")
+    src = os.path.join(bdir, "fp64issue.cu")
+    os.makedirs(bdir, exist_ok=True)
+    if not os.path.exists(so) or not os.path.exists(src) or open(src).read() != FP64_ISSUE_SRC:
+        open(src, "w").write(FP64_ISSUE_SRC)
+        subprocess.run(["nvcc"] + _lib.ARCH + ["-O3", "-shared", "-Xcompiler", "-fPIC", "-o",
+                                               so, src], check=True)
+    lib = ctypes.CDLL(so)
+    lib.fp64_issue_launch.restype = ctypes.c_int
+    lib.fp64_issue_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 4 + [
+        ctypes.c_void_p]
+    out = torch.zeros(256, dtype=torch.float64, device="cuda")
+    cyc = torch.zeros(1, dtype=torch.int64, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    iters = 4096
+    rows = []
+    for ilp in (1, 4):
+        for block in (32, 128, 256):
+            for active in (1, 32):
+                for _ in range(2):  # the second launch is the one kept
+                    assert lib.fp64_issue_launch(ctypes.c_void_p(out.data_ptr()),
+                                                 ctypes.c_void_p(cyc.data_ptr()), active, iters,
+                                                 ilp, block, stream) == 0
+                torch.cuda.synchronize()
+                per = float(cyc.item()) / (iters * ilp)
+                rows.append({"independent_chains": ilp, "warps_per_sm": block // 32,
+                             "active_lanes": active,
+                             "cycles_per_warp_fp64_instruction": round(per, 1)})
+    print(json.dumps({"fp64_issue": rows, "iters": iters}), flush=True)
+    return 0
 
 
 def dmma_peak_tflops(torch):
@@ -1523,6 +1603,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.fp64_issue:
+        import torch
+        return fp64_issue_probe(torch)
     if args.profile_batched:
         return profile_batched(args.profile_steps or 3, args.shapes)
     if args.profile_n3:
