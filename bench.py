@@ -976,13 +976,14 @@ def tgv_n3_bench(torch, n=512, steps=10, warmup=8, cfl=0.4, cpu=True, profile_st
          "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
          "value": n * n * steps / (ms * 1e-3) / 1e6, "unit": UNIT, "dt": float(c[1]),
          "predictor": {"cells": int(st.size), "picard_cells": int(pic.sum()),
+                       "newton_cells": int((kind == 1).sum()),
                        "unconverged_cells": int((kind == 2).sum()),
                        "picard_iteration_histogram": np.bincount(iters[pic]).tolist()
                        if pic.any() else []},
          # per step: k_cfl_max, k_clock_finalize, k_boundaries_n, k_weno2d_x_n,
-         # k_weno2d_y_n, k_predictor_n, k_faces_n x2, k_cells_n, k_renorm,
-         # k_contorted, k_reset_distortion, k_clock_advance
-         "gpu_launches": 13 * steps}
+         # k_weno2d_y_n, k_predictor_n, k_predictor_stiff_n, k_faces_n x2,
+         # k_cells_n, k_renorm, k_contorted, k_reset_distortion, k_clock_advance
+         "gpu_launches": 14 * steps}
     if cpu:
         from oracle import Oracle
         O = Oracle(N=N)

@@ -274,9 +274,10 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
  *   qh [nx + 2] ([ny + 2]) [N][n_s][V], space nodes x-major.
  * Each replaces the entry point of the same name without _n; the predictor
  * runs the reference's Picard iteration (dg/dg1.cpp:58-114, dg2.cpp:
- * 102-171) and has no Newton pass: a cell whose iteration does not converge
- * within 50 steps or turns NaN gets its last iterate and GPR_PRED_FAILED in
- * `status` (the reference leaves such rows unwritten or calls Newton-Krylov).
+ * 102-171), and the stiff-source Newton pass of gpr_predictor finishes the
+ * cells whose iteration does not converge within 50 steps or turns NaN
+ * (every cell with stiff != 0), its correction systems (9N) x (9N) for the
+ * distortion and (3N) x (3N) for the heat flux; `status` as there.
  * The 2D WENO needs device scratch of gpr_weno_scratch_doubles_n doubles for
  * its x sweep (0 in 1D, where scratch may be NULL).
  * gpr_order_supported returns 1 for the (order, ndim, nvar) compiled in;
@@ -291,7 +292,7 @@ long gpr_weno_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order
 int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndim,
                         double *scratch, int nvar, int order, void *stream);
 int gpr_predictor_n(double *qh, const double *wh, double dt, const double *dX, int ndim,
-                    const int32_t *nX, const gpr_par *par, const uint8_t *mask,
+                    const int32_t *nX, int stiff, const gpr_par *par, const uint8_t *mask,
                     int32_t *status, int nvar, int order, void *stream);
 long gpr_fv_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
 int gpr_fv_launcher_n(double *u, const double *qh, const int32_t *nX, double dt,
@@ -300,8 +301,9 @@ int gpr_fv_launcher_n(double *u, const double *qh, const int32_t *nX, double dt,
                       void *stream);
 long gpr_ader_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
 int gpr_ader_stepper_n(double *u, const double *ub, const int32_t *nX, int ndim, double dt,
-                       const double *dX, int flux, const gpr_par *par, const uint8_t *mask,
-                       double *scratch, int32_t *status, int nvar, int order, void *stream);
+                       const double *dX, int stiff, int flux, const gpr_par *par,
+                       const uint8_t *mask, double *scratch, int32_t *status, int nvar,
+                       int order, void *stream);
 long gpr_iterate_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order);
 int gpr_iterate_n(double *u, const int32_t *nX, int ndim, const double *dX,
                   const int32_t *bcs, int flux, const gpr_par *par, const uint8_t *mask,

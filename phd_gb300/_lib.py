@@ -106,11 +106,11 @@ SIGNATURES = {
     "gpr_boundaries_n": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
     "gpr_weno_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
     "gpr_weno_launcher_n": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
-    "gpr_predictor_n": (_I, [_P, _P, _D, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "gpr_predictor_n": (_I, [_P, _P, _D, _P, _I, _P, _I, _P, _P, _P, _I, _I, _P]),
     "gpr_fv_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
     "gpr_fv_launcher_n": (_I, [_P, _P, _P, _D, _P, _I, _I, _P, _P, _P, _I, _I, _P]),
     "gpr_ader_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
-    "gpr_ader_stepper_n": (_I, [_P, _P, _P, _I, _D, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "gpr_ader_stepper_n": (_I, [_P, _P, _P, _I, _D, _P, _I, _I, _P, _P, _P, _P, _I, _I, _P]),
     "gpr_iterate_scratch_doubles_n": (_L, [_P, _I, _I, _I]),
     "gpr_iterate_n": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I, _P, _P, _D, _I, _I, _P]),
     "gpr_batch_get_shapes": (_I, [_P, _P]),

@@ -69,21 +69,38 @@ template <class L, int NO> struct OpsN {
                                                                               C);
     return cuda_rc();
   }
+  // Picard pass, then the stiff Newton pass over the cells it marked (all
+  // cells with stiff): a persistent grid of one-warp blocks, each taking
+  // windows of 32 cells.
   static int predictor(double *qh, const double *wh, double dt, const double *dt_dev,
-                       const double *dX, const Grid &g, const DevPar &P, const uint8_t *mask,
-                       int32_t *status, cudaStream_t st) {
+                       const double *dX, const Grid &g, int stiff, const DevPar &P,
+                       const uint8_t *mask, int32_t *status, cudaStream_t st) {
     const long ncb = g.ncb();
-    const double idy = g.nd == 2 ? 1.0 / dX[1] : 1.0;
+    const double idx = 1.0 / dX[0], idy = g.nd == 2 ? 1.0 / dX[1] : 1.0;
+    const ConstsN<NO> &C = consts_n<NO>();
     if (g.nd == 1) {
       using NB = NodeBlock<NO, 1>;
       k_predictor_n<L, NO, 1><<<(unsigned)((ncb + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], idy, P, consts_n<NO>());
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+      k_predictor_stiff_n<L, NO, 1><<<stiff_grid(k_predictor_stiff_n<L, NO, 1>, ncb), 32, 0,
+                                      st>>>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P,
+                                            C);
     } else {
       using NB = NodeBlock<NO, 2>;
       k_predictor_n<L, NO, 2><<<(unsigned)((ncb + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
-          qh, wh, ncb, mask, status, dt, dt_dev, 1.0 / dX[0], idy, P, consts_n<NO>());
+          qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, stiff, P, C);
+      k_predictor_stiff_n<L, NO, 2><<<stiff_grid(k_predictor_stiff_n<L, NO, 2>, ncb), 32, 0,
+                                      st>>>(qh, wh, ncb, mask, status, dt, dt_dev, idx, idy, P,
+                                            C);
     }
     return cuda_rc();
+  }
+  template <class K> static unsigned stiff_grid(K kernel, long ncb) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32, 0);
+    long grid = (long)sm_count() * (per_sm > 0 ? per_sm : 1);
+    const long windows = (ncb + 31) / 32;
+    return (unsigned)(grid < windows ? grid : windows);
   }
   static int fv(double *u, const double *qh, const Grid &g, double dt, const double *dt_dev,
                 const double *dX, const DevPar &P, const uint8_t *mask, double *fb,
@@ -111,13 +128,13 @@ template <class L, int NO> struct OpsN {
   // scratch: wh, qh, face terms
   static long step_scratch(const Grid &g) { return wh_doubles(g) + qh_doubles(g) + fb_doubles(g); }
   static int step(double *u, const double *ub, const Grid &g, double dt, const double *dt_dev,
-                  const double *dX, const DevPar &P, const uint8_t *mask, double *scr,
-                  int32_t *status, cudaStream_t st) {
+                  const double *dX, int stiff, const DevPar &P, const uint8_t *mask,
+                  double *scr, int32_t *status, cudaStream_t st) {
     double *wh = scr, *qh = wh + wh_doubles(g), *fb = qh + qh_doubles(g);
     int rc;
     if ((rc = weno(wh, ub, g, fb, st)))
       return rc;
-    if ((rc = predictor(qh, wh, dt, dt_dev, dX, g, P, mask, status, st)))
+    if ((rc = predictor(qh, wh, dt, dt_dev, dX, g, stiff, P, mask, status, st)))
       return rc;
     return fv(u, qh, g, dt, dt_dev, dX, P, mask, fb, st);
   }
@@ -137,7 +154,7 @@ template <class L, int NO> struct OpsN {
       k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
       int rc = boundaries(u, ub, g, bcs, st);
       if (!rc)
-        rc = step(u, ub, g, 0.0, dt_dev, dX, P, mask, sscr, status, st);
+        rc = step(u, ub, g, 0.0, dt_dev, dX, 0, P, mask, sscr, status, st);
       if (rc)
         return rc;
       k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
@@ -245,13 +262,13 @@ int gpr_weno_launcher_n(double *wh, const double *ub, const int32_t *nX, int ndi
 }
 
 int gpr_predictor_n(double *qh, const double *wh, double dt, const double *dX, int ndim,
-                    const int32_t *nX, const gpr_par *par, const uint8_t *mask, int32_t *status,
-                    int nvar, int order, void *stream) {
+                    const int32_t *nX, int stiff, const gpr_par *par, const uint8_t *mask,
+                    int32_t *status, int nvar, int order, void *stream) {
   if (!qh || !wh || !par || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::predictor(qh, wh, dt, nullptr, dX, typename O::Grid(nX, ndim), P,
-                                       mask, status, S(stream)));
+  DISPATCH_N(nvar, order, O::predictor(qh, wh, dt, nullptr, dX, typename O::Grid(nX, ndim),
+                                       stiff, P, mask, status, S(stream)));
 }
 
 long gpr_fv_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
@@ -279,15 +296,16 @@ long gpr_ader_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order
 }
 
 int gpr_ader_stepper_n(double *u, const double *ub, const int32_t *nX, int ndim, double dt,
-                       const double *dX, int flux, const gpr_par *par, const uint8_t *mask,
-                       double *scratch, int32_t *status, int nvar, int order, void *stream) {
+                       const double *dX, int stiff, int flux, const gpr_par *par,
+                       const uint8_t *mask, double *scratch, int32_t *status, int nvar,
+                       int order, void *stream) {
   if (!u || !ub || !par || !scratch || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
   if (flux != GPR_FLUX_RUSANOV)
     return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::step(u, ub, typename O::Grid(nX, ndim), dt, nullptr, dX, P, mask,
-                                  scratch, status, S(stream)));
+  DISPATCH_N(nvar, order, O::step(u, ub, typename O::Grid(nX, ndim), dt, nullptr, dX, stiff, P,
+                                  mask, scratch, status, S(stream)));
 }
 
 long gpr_iterate_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {

@@ -33,9 +33,10 @@ template <int NO> struct ConstsN {
   double mCinv[NO][NO];                // central stencil of odd N
   double sig[NO][NO];                  // oscillation indicator
   double dgder[NO][NO];                // DG_DER
-  double dgmatinv[NO][NO];             // (DG_END - DG_DER^T)^-1
-  double dg_tol;
-  int dg_it;
+  double dgmat[NO][NO];                // DG_END - DG_DER^T
+  double dgmatinv[NO][NO];             // its inverse
+  double dg_tol, stiff_tol;
+  int dg_it, stiff_it;
 };
 
 // ---- host construction (polynomials in the monomial basis) ----------------
@@ -197,7 +198,6 @@ template <int NO> inline ConstsN<NO> make_consts_n() {
       C.sig[i][j] = s;
     }
   // DG matrices (dg/dg_matrices.cpp:29-53)
-  double dgmat[NO][NO];
   for (int i = 0; i < NO; i++)
     for (int j = 0; j < NO; j++) {
       if (i == j) {
@@ -209,10 +209,12 @@ template <int NO> inline ConstsN<NO> make_consts_n() {
     }
   for (int i = 0; i < NO; i++)
     for (int j = 0; j < NO; j++)
-      dgmat[i][j] = psi[i].eval(1.0) * psi[j].eval(1.0) - C.dgder[j][i];
-  invert_small<NO>(dgmat, C.dgmatinv);
+      C.dgmat[i][j] = psi[i].eval(1.0) * psi[j].eval(1.0) - C.dgder[j][i];
+  invert_small<NO>(C.dgmat, C.dgmatinv);
   C.dg_tol = 6e-6;
   C.dg_it = 50;
+  C.stiff_tol = 1e-11;  // the stiff Newton pass: as the N = 2 library's
+  C.stiff_it = 60;
   return C;
 }
 
@@ -403,21 +405,97 @@ template <int NO, int ND> struct NodeBlock {
   static constexpr int THREADS = CPB * NP;
 };
 
+// r = W w + dt R(q) at one space-time node (the Picard right-hand side,
+// dg1.cpp:75-89, dg2.cpp:115-150): R = W (S - B dq/dx [- B dq/dy]) - W_t
+// [W_j] DG_DER F_x / dx [- W_t W_i DG_DER F_y / dy].  The cell's node values
+// pass through sq (NP x V doubles); every thread of the block calls it (it
+// synchronises the block) and threads without a node (in_block false) read
+// zeros.
+template <class L, int NO, int ND>
+GPR_D void picard_rhs_n(const double *q, const double *Ww, double *r, double (*sq)[L::V],
+                        bool in_block, int g, int t, int i, int j, double wn, double dt,
+                        double idx, double idy, const DevPar &P, const ConstsN<NO> &C) {
+  constexpr int V = L::V;
+  constexpr int NS = NodeBlock<NO, ND>::NS;
+  // the partner node of this one with the x (y) index replaced by m
+  auto nx_of = [&](int m) { return ND == 1 ? t * NS + m : t * NS + m * NO + j; };
+  auto ny_of = [&](int m) { return t * NS + i * NO + m; };
+  Prim<L::THERMAL> s;
+  prim<L::THERMAL>(q, P, s);
+  // W (S - B dq/dx [- B dq/dy]) with the node weight in the source's factors
+  source<L::THERMAL, V>(q, s, P, r, wn);
+  if (in_block) {
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      sq[g][k] = q[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int dir = 0; dir < ND; dir++) {
+    const int e = dir == 0 ? i : j;
+    const double h = dir == 0 ? idx : idy;
+    double dq[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      double a = 0.0;
+#pragma unroll
+      for (int m = 0; m < NO; m++)
+        a += C.derv[e][m] * (in_block ? sq[dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
+      dq[k] = a * h * wn;
+    }
+    double bd[V];
+    bdot<V, L::LSET>(s.v, dq, dir, bd);
+#pragma unroll
+    for (int k = 0; k < V; k++)
+      r[k] -= bd[k];
+  }
+  // - W_t [W_j] DG_DER(i, m) F_x(t, m, j) / dx [- W_t W_i DG_DER(j, m) F_y(t, i, m) / dy]
+#pragma unroll
+  for (int dir = 0; dir < ND; dir++) {
+    double F[V];
+    flux_set<L::THERMAL, V>(q, s, dir, P, F);
+    __syncthreads();
+    if (in_block) {
+#pragma unroll
+      for (int k = 0; k < V; k++)
+        sq[g][k] = F[k];
+    }
+    __syncthreads();
+    const int e = dir == 0 ? i : j;
+    const double wx = dir == 0 ? C.w[t] * (ND == 1 ? 1.0 : C.w[j]) * idx
+                               : C.w[t] * C.w[i] * idy;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      if (!flux_support<L::THERMAL>(k, dir))
+        continue;
+      double a = 0.0;
+#pragma unroll
+      for (int m = 0; m < NO; m++)
+        a += C.dgder[e][m] * (in_block ? sq[dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
+      r[k] -= wx * a;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < V; k++)
+    r[k] = r[k] * dt + Ww[k];
+}
+
 // Picard predictor (dg1.cpp:58-114, dg2.cpp:102-171): q <- DG_U^-1 (W w +
 // dt R(q)) with the reference's initial guess q(t, s) = w(s), per-cell
-// stopping rule |q1 - q0| <= dg_tol (1 + |q0|) and iteration cap; R = W (S -
-// B dq/dx [- B dq/dy]) - W_t [W_j] DG_DER F_x / dx [- W_t W_i DG_DER F_y / dy].
-// The cell's node values pass through shared memory.  status[c]:
-// GPR_PRED_PICARD | iterations << 8 when converged; cells that do not
-// converge within the cap, or whose iterate turns NaN, get their last
-// iterate and GPR_PRED_FAILED | iterations << 8 (there is no Newton pass for
-// N != 2; the reference leaves such rows unwritten or calls its
-// Newton-Krylov solver).
+// stopping rule |q1 - q0| <= dg_tol (1 + |q0|) and iteration cap (none with
+// STIFF: every cell goes to the Newton pass).  The cell's node values pass
+// through shared memory.  status[c]: GPR_PRED_PICARD | iterations << 8 when
+// converged; a cell that does not converge within the cap, or whose
+// iterate turns NaN, gets the initial guess with a NaN marker in its first
+// entry (0x7ff8000000000bad) and GPR_PRED_FAILED | iterations << 8, and
+// k_predictor_stiff_n finishes it (the reference leaves such rows unwritten
+// or calls its Newton-Krylov solver).
 template <class L, int NO, int ND>
 __global__ void __launch_bounds__(128) k_predictor_n(
     double *__restrict__ qh, const double *__restrict__ wh, long ncb,
     const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
-    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, ConstsN<NO> C) {
+    const double *__restrict__ dt_dev, double idx, double idy, int stiff, DevPar P,
+    ConstsN<NO> C) {
   constexpr int V = L::V;
   using NB = NodeBlock<NO, ND>;
   constexpr int NS = NB::NS, NP = NB::NP, CPB = NB::CPB;
@@ -447,70 +525,12 @@ __global__ void __launch_bounds__(128) k_predictor_n(
   bool done = !active, nan_seen = false;
   int iters = 0;
   const double wn = C.w[t] * ws;
-  // the partner node of this one with the x (y) index replaced by m
-  auto nx_of = [&](int m) { return ND == 1 ? t * NS + m : t * NS + m * NO + j; };
-  auto ny_of = [&](int m) { return t * NS + i * NO + m; };
-  for (int it = 0; it < C.dg_it; it++) {
+  double(*sqc)[V] = sq[in_block ? lc : 0];
+  const int maxit = stiff ? 0 : C.dg_it;
+  for (int it = 0; it < maxit; it++) {
     if (!__syncthreads_or(!done))
       break;
-    Prim<L::THERMAL> s;
-    prim<L::THERMAL>(q, P, s);
-    // W (S - B dq/dx [- B dq/dy]) with the node weight in the source's factors
-    source<L::THERMAL, V>(q, s, P, r, wn);
-    if (in_block) {
-#pragma unroll
-      for (int k = 0; k < V; k++)
-        sq[lc][g][k] = q[k];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int dir = 0; dir < ND; dir++) {
-      const int e = dir == 0 ? i : j;
-      const double h = dir == 0 ? idx : idy;
-      double dq[V];
-#pragma unroll
-      for (int k = 0; k < V; k++) {
-        double a = 0.0;
-#pragma unroll
-        for (int m = 0; m < NO; m++)
-          a += C.derv[e][m] * (in_block ? sq[lc][dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
-        dq[k] = a * h * wn;
-      }
-      double bd[V];
-      bdot<V, L::LSET>(s.v, dq, dir, bd);
-#pragma unroll
-      for (int k = 0; k < V; k++)
-        r[k] -= bd[k];
-    }
-    // - W_t [W_j] DG_DER(i, m) F_x(t, m, j) / dx [- W_t W_i DG_DER(j, m) F_y(t, i, m) / dy]
-#pragma unroll
-    for (int dir = 0; dir < ND; dir++) {
-      double F[V];
-      flux_set<L::THERMAL, V>(q, s, dir, P, F);
-      __syncthreads();
-      if (in_block) {
-#pragma unroll
-        for (int k = 0; k < V; k++)
-          sq[lc][g][k] = F[k];
-      }
-      __syncthreads();
-      const int e = dir == 0 ? i : j;
-      const double wx = dir == 0 ? C.w[t] * (ND == 1 ? 1.0 : C.w[j]) * idx
-                                 : C.w[t] * C.w[i] * idy;
-#pragma unroll
-      for (int k = 0; k < V; k++) {
-        if (!flux_support<L::THERMAL>(k, dir))
-          continue;
-        double a = 0.0;
-#pragma unroll
-        for (int m = 0; m < NO; m++)
-          a += C.dgder[e][m] * (in_block ? sq[lc][dir == 0 ? nx_of(m) : ny_of(m)][k] : 0.0);
-        r[k] -= wx * a;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < V; k++)
-      r[k] = r[k] * dt + Ww[k];
+    picard_rhs_n<L, NO, ND>(q, Ww, r, sqc, in_block, g, t, i, j, wn, dt, idx, idy, P, C);
     __syncthreads();
     if (in_block) {
 #pragma unroll
@@ -567,12 +587,195 @@ __global__ void __launch_bounds__(128) k_predictor_n(
     double *out = qh + (c * NP + g) * V;
 #pragma unroll
     for (int k = 0; k < V; k++)
-      out[k] = q[k];
+      out[k] = w[k];
+    if (g == 0)
+      out[0] = __longlong_as_double(0x7ff8000000000badll);
     if (status && g == 0)
       status[c] = GPR_PRED_FAILED | (iters << 8);
   }
   if (valid && !active && status && g == 0)
     status[c] = GPR_PRED_PICARD;
+}
+
+// Stiff-source Newton pass at NO nodes for the cells the Picard pass marked
+// (first entry 0x7ff8000000000bad): the N = 2 pass's iteration (the exact
+// local Jacobian of the relaxation sources, stiff_jacobian_rows, with the
+// correction systems in FP32 and the residual in FP64, so the converged
+// point is the FP64 fixed point), from the initial guess, with the NO time
+// nodes of a spatial node coupled through DG_MAT in one (9 NO) x (9 NO)
+// system for A and one (3 NO) x (3 NO) system for rho J, as the oracle's
+// dg_stiff:
+//   (DG_MAT (x) I - dt W_t dS/dq) delta = (W w + dt R(q) - W_s DG_MAT q) / W_s,
+// the other variables by DG_MAT^-1.  One cell at a time per one-warp block
+// (NP <= 27 node lanes); the lanes first test 32 cells' markers at once and
+// the block then takes the marked ones in turn.
+template <class L, int NO, int ND> struct StiffN {
+  static constexpr int NS = NodeBlock<NO, ND>::NS;
+  static constexpr int NP = NodeBlock<NO, ND>::NP;
+  static constexpr int NA = 9 * NO, NJ = 3 * NO;
+  // odd: the solver lanes of neighbouring spatial nodes start on different banks
+  static constexpr int per_node = (NA * NA + NA + (L::THERMAL ? NJ * NJ + NJ : 0)) | 1;
+};
+
+template <class L, int NO, int ND>
+__global__ void __launch_bounds__(32) k_predictor_stiff_n(
+    double *__restrict__ qh, const double *__restrict__ wh, long ncb,
+    const uint8_t *__restrict__ mask, int32_t *__restrict__ status, double dt,
+    const double *__restrict__ dt_dev, double idx, double idy, DevPar P, ConstsN<NO> C) {
+  constexpr int V = L::V;
+  using SN = StiffN<L, NO, ND>;
+  constexpr int NS = SN::NS, NP = SN::NP, NA = SN::NA, NJ = SN::NJ;
+  static_assert(NP <= 32, "one cell per warp");
+  __shared__ double sq[NP][V];
+  __shared__ float sm[NS * SN::per_node];
+  if (dt_dev)
+    dt = *dt_dev;
+  const int lane = threadIdx.x;
+  const bool in_block = lane < NP;
+  const int g = in_block ? lane : 0;
+  const int t = g / NS, sidx = g % NS;
+  const int i = ND == 1 ? sidx : sidx / NO, j = ND == 1 ? 0 : sidx % NO;
+  const double ws = ND == 1 ? C.w[i] : C.w[i] * C.w[j];
+  const double f = C.endv[0][t] * ws;
+  const double wn = C.w[t] * ws;
+  const double a_t = dt * C.w[t];
+  float *Am = sm + sidx * SN::per_node;  // (9 NO) x (9 NO)
+  float *Ab = Am + NA * NA;              // 9 NO
+  float *Jm = Ab + NA;                   // (3 NO) x (3 NO)
+  float *Jb = Jm + NJ * NJ;              // 3 NO
+  for (long base = (long)blockIdx.x * 32; base < ncb; base += (long)gridDim.x * 32) {
+    const long cl = base + lane;
+    bool marked = false;
+    if (cl < ncb && (mask == nullptr || mask[cl])) {
+      const double flag = qh[cl * NP * V];
+      marked = flag != flag;
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, marked);
+    while (todo) {  // uniform over the block (one warp)
+      const long c = base + __ffs(todo) - 1;
+      todo &= todo - 1;
+      double Ww[V], q[V], r[V], delta[V];
+      const double *wc = wh + (c * NS + sidx) * V;
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        const double w = wc[k];
+        Ww[k] = f * w;
+        q[k] = w;
+      }
+      bool ok = false;
+      int iters = 0;
+      for (int it = 0; it < C.stiff_it; it++) {
+        __syncthreads();  // the previous iteration's reads of sq and sm are done
+        picard_rhs_n<L, NO, ND>(q, Ww, r, sq, in_block, g, t, i, j, wn, dt, idx, idy, P, C);
+        // residual r - W_s sum_m DG_MAT[t][m] q(m, s)
+        __syncthreads();
+        if (in_block) {
+#pragma unroll
+          for (int k = 0; k < V; k++)
+            sq[g][k] = q[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+          double uq = 0.0;
+#pragma unroll
+          for (int m = 0; m < NO; m++)
+            uq += C.dgmat[t][m] * sq[m * NS + sidx][k];
+          r[k] -= ws * uq;
+        }
+        if (in_block) {
+          // this time node's rows of the two systems: the diagonal block
+          // DG_MAT[t][t] I - dt W_t dS/dq, the others DG_MAT[t][t2] I
+          Prim<L::THERMAL> st;
+          prim<L::THERMAL>(q, P, st);
+          stiff_jacobian_rows<L::THERMAL>(q, st, P, a_t, C.dgmat[t][t], Am + t * 9 * NA + t * 9,
+                                          NA, Jm + t * 3 * NJ + t * 3, NJ);
+#pragma unroll
+          for (int t2 = 0; t2 < NO; t2++) {
+            if (t2 == t)
+              continue;
+            const float m = (float)C.dgmat[t][t2];
+#pragma unroll
+            for (int a = 0; a < 9; a++)
+#pragma unroll
+              for (int b = 0; b < 9; b++)
+                Am[(t * 9 + a) * NA + t2 * 9 + b] = a == b ? m : 0.0f;
+            if (L::THERMAL) {
+#pragma unroll
+              for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++)
+                  Jm[(t * 3 + a) * NJ + t2 * 3 + b] = a == b ? m : 0.0f;
+            }
+          }
+#pragma unroll
+          for (int a = 0; a < 9; a++)
+            Ab[t * 9 + a] = (float)(r[5 + a] / ws);
+          if (L::THERMAL) {
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+              Jb[t * 3 + a] = (float)(r[14 + a] / ws);
+          }
+        }
+        __syncthreads();
+        bool solved = true;
+        if (in_block && t == 0)
+          solved = smem_solve<NA>(Am, NA, Ab);
+        else if (L::THERMAL && in_block && t == 1)
+          solved = smem_solve<NJ>(Jm, NJ, Jb);
+        // the other variables: DG_MAT^-1 of the residual, / W_s
+        if (in_block) {
+#pragma unroll
+          for (int k = 0; k < V; k++)
+            sq[g][k] = r[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+          double acc = 0.0;
+#pragma unroll
+          for (int m = 0; m < NO; m++)
+            acc += C.dgmatinv[t][m] * sq[m * NS + sidx][k];
+          delta[k] = acc / ws;
+        }
+#pragma unroll
+        for (int a = 0; a < 9; a++)
+          delta[5 + a] = (double)Ab[t * 9 + a];
+        if (L::THERMAL) {
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+            delta[14 + a] = (double)Jb[t * 3 + a];
+        }
+        bool big = false, bad = !solved;
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+          const double qn = q[k] + delta[k];
+          if (fabs(delta[k]) > C.stiff_tol * (1.0 + fabs(qn)))
+            big = true;
+          if (qn != qn)
+            bad = true;
+          q[k] = qn;
+        }
+        const int anybad = __syncthreads_or(in_block && bad);
+        const int anybig = __syncthreads_or(in_block && big);
+        iters = it + 1;
+        if (anybad)
+          break;
+        if (!anybig) {
+          ok = true;
+          break;
+        }
+      }
+      if (in_block) {
+        double *out = qh + (c * NP + g) * V;
+#pragma unroll
+        for (int k = 0; k < V; k++)
+          out[k] = q[k];
+        if (status && g == 0)
+          status[c] = (ok ? GPR_PRED_NEWTON : GPR_PRED_FAILED) | (iters << 8);
+      }
+    }
+  }
 }
 
 // Interface terms of one face point (D_RUS and Bint, fluxes.cpp:9-75,

@@ -79,9 +79,10 @@ def for_order(N):
     def predictor(qh, wh, dt, dX, STIFF, STIFF_IG, MP, mask, status=None, nX=None):
         """As the reference, the call takes no grid size: in 1D it comes
         from the mask (nx + 2 predictor cells); in 2D from nX, else from the
-        last grid given to a call of this namespace that takes nX."""
-        if STIFF:
-            raise RuntimeError("N = %d has no stiff Newton predictor" % N)
+        last grid given to a call of this namespace that takes nX.  STIFF
+        sends every cell to the stiff-source Newton pass (STIFF_IG, the
+        reference's option of a stiff initial guess, is not used: the Newton
+        pass starts from the standard initial guess)."""
         dXa, pd = _f64(dX)
         nd = dXa.size
         if nX is not None:
@@ -101,8 +102,9 @@ def for_order(N):
         pm, _ = _mask_ptr(mask, ncb)
         c, pp = _par(MP)
         ps = _dev(status, "status", torch.int32) if status is not None else None
-        _lib.check(lib.gpr_predictor_n(_dev(qh, "qh"), _dev(wh, "wh"), float(dt), pd, nd, pn, pp,
-                                       pm, ps, V, N, _stream()), "predictor")
+        _lib.check(lib.gpr_predictor_n(_dev(qh, "qh"), _dev(wh, "wh"), float(dt), pd, nd, pn,
+                                       int(bool(STIFF)), pp, pm, ps, V, N, _stream()),
+                   "predictor")
         return qh
 
     def fv_launcher(u, qh, nX, dt, dX, SOURCES, TIME, FLUX, MP, mask):
@@ -124,8 +126,6 @@ def for_order(N):
         return u
 
     def ader_stepper(u, ub, nX, dt, dX, STIFF, FLUX, MP, mask, status=None):
-        if STIFF:
-            raise RuntimeError("N = %d has no stiff Newton predictor" % N)
         nXa, pn = _i32(nX)
         dXa, pd = _f64(dX)
         nd = nXa.size
@@ -138,8 +138,8 @@ def for_order(N):
                           device=u.device)
         ps = _dev(status, "status", torch.int32) if status is not None else None
         _lib.check(lib.gpr_ader_stepper_n(_dev(u, "u"), _dev(ub, "ub"), pn, nd, float(dt), pd,
-                                          int(FLUX), pp, pm, _dev(scr, "s"), ps, V, N,
-                                          _stream()), "ader_stepper")
+                                          int(bool(STIFF)), int(FLUX), pp, pm, _dev(scr, "s"),
+                                          ps, V, N, _stream()), "ader_stepper")
         return u
 
     def iterate(u, nX, dX, bcs, MP, clock, nsteps, FLUX=0, mask=None, status=None,

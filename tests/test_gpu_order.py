@@ -162,10 +162,64 @@ def test_order_arguments_are_checked(G3):
     ub = torch.zeros((16 + 6) * 17, dtype=torch.float64, device=DEV)
     with pytest.raises(RuntimeError):  # Osher is not compiled for N = 3
         G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, False, 2, MP, None)
-    with pytest.raises(RuntimeError):  # no stiff Newton predictor at N = 3
-        G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, True, 0, MP, None)
     with pytest.raises(RuntimeError):  # unknown boundary code
         G3.boundaries(u, ub, [16], [0, 9])
+
+
+@pytest.mark.parametrize("case", ["tgv16_cfl08", "tube_stiff", "forced_stiff"])
+def test_n3_stiff_predictor_against_oracle(G3, case):
+    """The stiff-source Newton pass at N = 3: cells where the reference's
+    Picard iteration does not converge (all of them on the 16 x 16 vortex at
+    CFL 0.8, 6 of 66 on the stiff tube), or every cell with STIFF, are
+    finished by the Newton iteration on the (27 x 27 and 9 x 9 per spatial
+    node) correction systems; the same cells as the oracle's, whose Newton
+    solve (dg_stiff at N = 3) converges to 1e-11 and agrees with its dense
+    finite-difference Newton solve of the same fixed point; then one ADER
+    step with that predictor against the oracle's."""
+    from phd_gb300 import problems
+    O = Oracle(N=3)
+    stiff = False
+    if case == "tgv16_cfl08":
+        u0, MP, tf, dX, bcs = problems.taylor_green(n=16, cs=10.0, mu=1e-2)
+        nX, bc, cfl = np.array([16, 16], np.int32), [1] * 4, 0.8
+    elif case == "tube_stiff":
+        u0, MP, tf, dX, bcs = problems.shock_tube(nx=64, mu=1e-4, cs=5.0)
+        nX, bc, cfl = np.array([64], np.int32), [0, 0], 0.8
+    else:  # STIFF = True on a non-stiff tube: Newton from the start
+        u0, MP, tf, dX, bcs = problems.shock_tube(nx=48)
+        nX, bc, cfl, stiff = np.array([48], np.int32), [0, 0], 0.8, True
+    u, _, _ = O.run(u0, MP, 1e9, dX, bc[0], cfl=0.4, max_steps=3)
+    dt = O.timestep(u, dX, cfl, 0.0, 1e9, 10, MP)
+    ub = O.boundaries(u, nX, bc)
+    wh = O.weno_launcher(ub, nX)
+    ref, st_ref = O.predictor(wh, dt, dX, nX, MP, stiff=stiff, newton_fallback=1)
+    fd, st_fd = O.predictor(wh, dt, dX, nX, MP, stiff=stiff, newton_fallback=2)
+    assert (st_ref < -1000).sum() > 0, "case must exercise the stiff path"
+    assert not ((st_ref == -1) | (st_ref == -2)).any()
+    ncb = int(np.prod(nX + 2))
+    qh = torch.full((ref.size,), np.nan, dtype=torch.float64, device=DEV)
+    status = torch.full((ncb,), -1, dtype=torch.int32, device=DEV)
+    G3.solvers.dg.predictor(qh, T(wh), dt, dX, stiff, False, MP, None, status=status, nX=nX)
+    got, st = H(qh), H(status)
+    assert np.isfinite(got).all()
+    newton = (st & 0xff) == 1
+    assert (newton == (st_ref < -1000)).all(), "same cells take the stiff path"
+    assert ((st & 0xff) != 2).all(), "no cell may be left unconverged"
+    pic = st_ref > 0
+    assert ((st[pic] >> 8) == st_ref[pic]).all(), "the same Picard iteration counts"
+    assert rel_err(got, ref) < 1e-10, rel_err(got, ref)
+    assert rel_err(got, fd) < 1e-9, rel_err(got, fd)
+    # one ADER step with the stiff predictor.  Both Newton passes stop at
+    # relative updates of 1e-11, so their predictors differ at that level,
+    # and the step's stiff volume source multiplies a difference in the
+    # distortion by about dt / tau (the stiffness that makes Picard fail
+    # here): 1e-9 for the step (1.3e-10 measured on the vortex, where every
+    # cell takes the Newton pass)
+    ref_u = u.ravel().copy()
+    O.ader_stepper(ref_u, ub, nX, dt, dX, MP, stiff=stiff, newton_fallback=1)
+    ud = T(u).view(-1)
+    G3.solvers.ader_stepper(ud, T(ub), nX, dt, dX, stiff, 0, MP, None)
+    assert rel_err(H(ud), ref_u) < 1e-9, rel_err(H(ud), ref_u)
 
 
 def test_n3_2d_stages_against_golden(G3):
