@@ -267,8 +267,9 @@ int gpr_ader_stepper_1d_noalloc(double *u, const double *ub, int32_t nx,
  * central stencil with weight LAMC = 1e5 (solvers/weno/weno.cpp:17-73).
  * These entry points take N as `order`: 3 for V = 17 or 14, and 2 for
  * V = 17 (the same formulation at N = 2, a cross-check of the N = 2 kernels
- * above).  1D and 2D grids (ndim = 1 or 2; every extent at least N), the
- * Rusanov flux only (Roe and Osher give GPR_E_UNSUPPORTED).  Layouts as
+ * above).  1D and 2D grids (ndim = 1 or 2; every extent at least N); the
+ * Rusanov, Roe and Osher fluxes (the eigen dissipation with N path nodes,
+ * one thread per face point).  Layouts as
  * above with N = order, n_s = N^ndim space nodes per cell:
  *   ub [nx + 2N] ([ny + 2N]) [V], wh [nx + 2] ([ny + 2]) [n_s][V],
  *   qh [nx + 2] ([ny + 2]) [N][n_s][V], space nodes x-major.

@@ -102,16 +102,32 @@ template <class L, int NO> struct OpsN {
     const long windows = (ncb + 31) / 32;
     return (unsigned)(grid < windows ? grid : windows);
   }
+  // Face terms of direction dir: Rusanov, or the Roe / Osher eigen
+  // dissipation at one thread per face point in 64-thread blocks (its 17 x 17
+  // matrices live in local memory, as in the N = 2 per-point kernel).
+  template <int ND>
+  static void faces(double *fb, const double *qh, const Grid &g, int dir, double dt,
+                    const double *dt_dev, const double *dX, int flux, const DevPar &P,
+                    const uint8_t *mask, cudaStream_t st) {
+    const ConstsN<NO> &C = consts_n<NO>();
+    const long n = g.nface() * (ND == 1 ? NO : NO * NO);
+    const double dy = g.nd == 2 ? dX[1] : 1.0;
+    if (flux == GPR_FLUX_RUSANOV)
+      k_faces_n<L, NO, ND><<<blocks(n, 128), 128, 0, st>>>(fb, qh, g.nx, g.ny, dir, mask, dt,
+                                                           dt_dev, dX[0], dy, P, C);
+    else
+      k_faces_n<L, NO, ND, true><<<blocks(n, 64), 64, 0, st>>>(
+          fb, qh, g.nx, g.ny, dir, mask, dt, dt_dev, dX[0], dy, P, C, flux);
+  }
   static int fv(double *u, const double *qh, const Grid &g, double dt, const double *dt_dev,
-                const double *dX, const DevPar &P, const uint8_t *mask, double *fb,
+                const double *dX, int flux, const DevPar &P, const uint8_t *mask, double *fb,
                 cudaStream_t st) {
     const ConstsN<NO> &C = consts_n<NO>();
     const long nf = g.nface();
     const double dy = g.nd == 2 ? dX[1] : 1.0;
     if (g.nd == 1) {
       using NB = NodeBlock<NO, 1>;
-      k_faces_n<L, NO, 1><<<blocks(nf * NO, 128), 128, 0, st>>>(fb, qh, g.nx, 1, 0, mask, dt,
-                                                                dt_dev, dX[0], dy, P, C);
+      faces<1>(fb, qh, g, 0, dt, dt_dev, dX, flux, P, mask, st);
       k_cells_n<L, NO, 1><<<(unsigned)((g.nx + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
           u, qh, fb, nullptr, g.nx, 1, mask, dt, dt_dev, dX[0], dy, P, C);
       return cuda_rc();
@@ -119,8 +135,7 @@ template <class L, int NO> struct OpsN {
     using NB = NodeBlock<NO, 2>;
     double *fby = fb + nf * NO * NO * 2 * V;
     for (int d = 0; d < 2; d++)
-      k_faces_n<L, NO, 2><<<blocks(nf * NO * NO, 128), 128, 0, st>>>(
-          d ? fby : fb, qh, g.nx, g.ny, d, mask, dt, dt_dev, dX[0], dy, P, C);
+      faces<2>(d ? fby : fb, qh, g, d, dt, dt_dev, dX, flux, P, mask, st);
     k_cells_n<L, NO, 2><<<(unsigned)((g.ncell() + NB::CPB - 1) / NB::CPB), 128, 0, st>>>(
         u, qh, fb, fby, g.nx, g.ny, mask, dt, dt_dev, dX[0], dy, P, C);
     return cuda_rc();
@@ -128,7 +143,7 @@ template <class L, int NO> struct OpsN {
   // scratch: wh, qh, face terms
   static long step_scratch(const Grid &g) { return wh_doubles(g) + qh_doubles(g) + fb_doubles(g); }
   static int step(double *u, const double *ub, const Grid &g, double dt, const double *dt_dev,
-                  const double *dX, int stiff, const DevPar &P, const uint8_t *mask,
+                  const double *dX, int stiff, int flux, const DevPar &P, const uint8_t *mask,
                   double *scr, int32_t *status, cudaStream_t st) {
     double *wh = scr, *qh = wh + wh_doubles(g), *fb = qh + qh_doubles(g);
     int rc;
@@ -136,11 +151,11 @@ template <class L, int NO> struct OpsN {
       return rc;
     if ((rc = predictor(qh, wh, dt, dt_dev, dX, g, stiff, P, mask, status, st)))
       return rc;
-    return fv(u, qh, g, dt, dt_dev, dX, P, mask, fb, st);
+    return fv(u, qh, g, dt, dt_dev, dX, flux, P, mask, fb, st);
   }
   // scratch: ub, the step's scratch, the CFL maximum and the contortion flag
   static long iterate_scratch(const Grid &g) { return ub_doubles(g) + step_scratch(g) + 2; }
-  static int iterate(double *u, const Grid &g, const double *dX, const int32_t *bcs,
+  static int iterate(double *u, const Grid &g, const double *dX, const int32_t *bcs, int flux,
                      const DevPar &P, const uint8_t *mask, double *clk, int nsteps, double *scr,
                      int32_t *status, double contorted_tol, cudaStream_t st) {
     double *ub = scr, *sscr = ub + ub_doubles(g);
@@ -154,7 +169,7 @@ template <class L, int NO> struct OpsN {
       k_clock_finalize<<<1, 1, 0, st>>>(mx, clk);
       int rc = boundaries(u, ub, g, bcs, st);
       if (!rc)
-        rc = step(u, ub, g, 0.0, dt_dev, dX, 0, P, mask, sscr, status, st);
+        rc = step(u, ub, g, 0.0, dt_dev, dX, 0, flux, P, mask, sscr, status, st);
       if (rc)
         return rc;
       k_renorm<V><<<blocks(ncell, 256), 256, 0, st>>>(u, ncell, P.rho0, dt_dev);
@@ -199,6 +214,10 @@ bool bad_bcs(const int32_t *bcs, int ndim) {
 
 bool bad_dX(const double *dX, int ndim) {
   return !dX || !(dX[0] > 0) || (ndim == 2 && !(dX[1] > 0));
+}
+
+bool bad_flux(int flux) {
+  return flux != GPR_FLUX_RUSANOV && flux != GPR_FLUX_ROE && flux != GPR_FLUX_OSHER;
 }
 
 }  // namespace
@@ -282,11 +301,11 @@ int gpr_fv_launcher_n(double *u, const double *qh, const int32_t *nX, double dt,
                       const uint8_t *mask, double *scratch, int nvar, int order, void *stream) {
   if (!u || !qh || !par || !scratch || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
+  if (bad_flux(flux))
+    return GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::fv(u, qh, typename O::Grid(nX, ndim), dt, nullptr, dX, P, mask,
-                                scratch, S(stream)));
+  DISPATCH_N(nvar, order, O::fv(u, qh, typename O::Grid(nX, ndim), dt, nullptr, dX, flux, P,
+                                mask, scratch, S(stream)));
 }
 
 long gpr_ader_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
@@ -301,11 +320,11 @@ int gpr_ader_stepper_n(double *u, const double *ub, const int32_t *nX, int ndim,
                        int order, void *stream) {
   if (!u || !ub || !par || !scratch || bad_grid(nX, ndim, order) || bad_dX(dX, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
+  if (bad_flux(flux))
+    return GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::step(u, ub, typename O::Grid(nX, ndim), dt, nullptr, dX, stiff, P,
-                                  mask, scratch, status, S(stream)));
+  DISPATCH_N(nvar, order, O::step(u, ub, typename O::Grid(nX, ndim), dt, nullptr, dX, stiff,
+                                  flux, P, mask, scratch, status, S(stream)));
 }
 
 long gpr_iterate_scratch_doubles_n(const int32_t *nX, int ndim, int nvar, int order) {
@@ -321,11 +340,12 @@ int gpr_iterate_n(double *u, const int32_t *nX, int ndim, const double *dX, cons
   if (!u || !par || !clock || !scratch || nsteps < 0 || bad_grid(nX, ndim, order) ||
       bad_dX(dX, ndim) || bad_bcs(bcs, ndim))
     return GPR_E_ARG;
-  if (flux != GPR_FLUX_RUSANOV)
-    return flux == GPR_FLUX_ROE || flux == GPR_FLUX_OSHER ? GPR_E_UNSUPPORTED : GPR_E_ARG;
+  if (bad_flux(flux))
+    return GPR_E_ARG;
   DevPar P = make_devpar(*par);
-  DISPATCH_N(nvar, order, O::iterate(u, typename O::Grid(nX, ndim), dX, bcs, P, mask, clock,
-                                     nsteps, scratch, status, contorted_tol, S(stream)));
+  DISPATCH_N(nvar, order, O::iterate(u, typename O::Grid(nX, ndim), dX, bcs, flux, P, mask,
+                                     clock, nsteps, scratch, status, contorted_tol,
+                                     S(stream)));
 }
 
 }  // extern "C"

@@ -17,6 +17,7 @@
 #include <math.h>
 
 #include "gpr_kernels.cuh"
+#include "gpr_osher.cuh"
 
 namespace gpr {
 namespace order {
@@ -778,25 +779,37 @@ __global__ void __launch_bounds__(32) k_predictor_stiff_n(
   }
 }
 
-// Interface terms of one face point (D_RUS and Bint, fluxes.cpp:9-75,
-// with NO path nodes): f = max(lambda_L, lambda_R) (qL - qR) + F(qL) + F(qR),
-// b = sum_n W_n B(qL + x_n dq) dq.
-template <class L, int NO>
+// Interface terms of one face point (D_RUS / D_ROE / D_OSH and Bint,
+// fluxes.cpp:9-75, with NO path nodes): f = D + F(qL) + F(qR), D =
+// max(lambda_L, lambda_R) (qL - qR) for Rusanov (EIG false) or the eigen
+// part of D_ROE / D_OSH (EIG true, flux GPR_FLUX_ROE or GPR_FLUX_OSHER, one
+// 17 x 17 eigen-decomposition per path node for Osher, one of the
+// path-averaged matrix for Roe); b = sum_n W_n B(qL + x_n dq) dq.
+template <class L, int NO, bool EIG = false>
 GPR_D void interface_point_n(const double *ql, const double *qr, int d, const DevPar &P,
-                             const ConstsN<NO> &C, double *f, double *b) {
+                             const ConstsN<NO> &C, double *f, double *b, int flux = 0) {
   constexpr int V = L::V;
   Prim<L::THERMAL> sl, sr;
   prim<L::THERMAL>(ql, P, sl);
   prim<L::THERMAL>(qr, P, sr);
-  const double m1 = max_abs_eigs<L::THERMAL>(ql, sl, d, P);
-  const double m2 = max_abs_eigs<L::THERMAL>(qr, sr, d, P);
-  const double m = m1 > m2 ? m1 : m2;
   double dq[V];
+  if (EIG) {
+    eig_dissipation_qd<L, NO>(ql, qr, d, flux, P, C.nodes, C.w, f);
 #pragma unroll
-  for (int k = 0; k < V; k++) {
-    f[k] = m * (ql[k] - qr[k]);
-    dq[k] = qr[k] - ql[k];
-    b[k] = 0.0;
+    for (int k = 0; k < V; k++) {
+      dq[k] = qr[k] - ql[k];
+      b[k] = 0.0;
+    }
+  } else {
+    const double m1 = max_abs_eigs<L::THERMAL>(ql, sl, d, P);
+    const double m2 = max_abs_eigs<L::THERMAL>(qr, sr, d, P);
+    const double m = m1 > m2 ? m1 : m2;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      f[k] = m * (ql[k] - qr[k]);
+      dq[k] = qr[k] - ql[k];
+      b[k] = 0.0;
+    }
   }
   flux_add<L::THERMAL, V>(ql, sl, d, P, f);
   flux_add<L::THERMAL, V>(qr, sr, d, P, f);
@@ -820,12 +833,13 @@ GPR_D void interface_point_n(const double *ql, const double *qr, int d, const De
 // predictor cells (i, j) and (i + 1, j) (dir 0) or (i, j + 1) (dir 1), p = t
 // N + s over time node t and transverse node s.  fb[face][p][0][V] = k (b +
 // f) is subtracted from the left cell, fb[face][p][1][V] = k (b - f) from the
-// right one, k = W_t [W_s] dt / (2 dx_dir).
-template <class L, int NO, int ND>
+// right one, k = W_t [W_s] dt / (2 dx_dir).  EIG: the Roe or Osher
+// dissipation (flux), one thread per face point as for Rusanov.
+template <class L, int NO, int ND, bool EIG = false>
 __global__ void __launch_bounds__(128) k_faces_n(
     double *__restrict__ fb, const double *__restrict__ qh, int nx, int ny, int dir,
     const uint8_t *__restrict__ mask, double dt, const double *__restrict__ dt_dev, double dx,
-    double dy, DevPar P, ConstsN<NO> C) {
+    double dy, DevPar P, ConstsN<NO> C, int flux = 0) {
   constexpr int V = L::V;
   constexpr int NQ = ND == 1 ? NO : NO * NO;  // points per face
   constexpr int NS = ND == 1 ? NO : NO * NO;
@@ -874,7 +888,7 @@ __global__ void __launch_bounds__(128) k_faces_n(
     ql[k] = a;
     qr[k] = e;
   }
-  interface_point_n<L, NO>(ql, qr, dir, P, C, f, b);
+  interface_point_n<L, NO, EIG>(ql, qr, dir, P, C, f, b, flux);
   const double kk = dt * C.w[t] * (ND == 1 ? 1.0 : C.w[sq]) / (2.0 * (dir == 0 ? dx : dy));
 #pragma unroll
   for (int k = 0; k < V; k++) {

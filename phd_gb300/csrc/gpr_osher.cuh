@@ -705,9 +705,10 @@ template <int n> GPR_D bool abs_apply(double *M, const double *dq, double w, dou
 
 // Eigen part of D_OSH (flux 2) / D_ROE (flux 1) at one interface into f
 // (overwritten); NaN if the eigen-decomposition fails (fluxes.cpp:22-64).
-template <class L>
-GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const DevPar &P,
-                           const Consts &C, double *f) {
+// The path qR -> qL takes the scheme's NQ Gauss nodes (nodes, wts on [0, 1]).
+template <class L, int NQ>
+GPR_D void eig_dissipation_q(const double *ql, const double *qr, int flux, const DevPar &P,
+                             const double *nodes, const double *wts, double *f) {
   constexpr int V = L::V;
   double dq[V], q[V], M[V * V];
   bool flat = true;
@@ -724,14 +725,14 @@ GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const D
   bool ok = true;
   if (flux == GPR_FLUX_OSHER) {
 #pragma unroll 1
-    for (int i = 0; i < NN; i++) {
+    for (int i = 0; i < NQ; i++) {
 #pragma unroll
       for (int k = 0; k < V; k++)
-        q[k] = qr[k] + C.nodes[i] * dq[k];
+        q[k] = qr[k] + nodes[i] * dq[k];
       Prim<L::THERMAL> s;
       prim<L::THERMAL>(q, P, s);
       system_matrix<L::THERMAL, V>(q, s, P, M);
-      ok = ok && abs_apply<V>(M, dq, C.w[i], f);
+      ok = ok && abs_apply<V>(M, dq, wts[i], f);
     }
   } else {
     double Mi[V * V];
@@ -739,16 +740,16 @@ GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const D
     for (int i = 0; i < V * V; i++)
       M[i] = 0.0;
 #pragma unroll 1
-    for (int i = 0; i < NN; i++) {
+    for (int i = 0; i < NQ; i++) {
 #pragma unroll
       for (int k = 0; k < V; k++)
-        q[k] = qr[k] + C.nodes[i] * dq[k];
+        q[k] = qr[k] + nodes[i] * dq[k];
       Prim<L::THERMAL> s;
       prim<L::THERMAL>(q, P, s);
       system_matrix<L::THERMAL, V>(q, s, P, Mi);
 #pragma unroll 1
       for (int k = 0; k < V * V; k++)
-        M[k] += C.w[i] * Mi[k];
+        M[k] += wts[i] * Mi[k];
     }
     ok = abs_apply<V>(M, dq, 1.0, f);
   }
@@ -757,6 +758,12 @@ GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const D
     for (int k = 0; k < V; k++)
       f[k] = __longlong_as_double(0x7ff8000000000000ll);
   }
+}
+
+template <class L>
+GPR_D void eig_dissipation(const double *ql, const double *qr, int flux, const DevPar &P,
+                           const Consts &C, double *f) {
+  eig_dissipation_q<L, NN>(ql, qr, flux, P, C.nodes, C.w, f);
 }
 
 // Index of state entry k with spatial axes 0 and d exchanged: velocity and
@@ -778,12 +785,13 @@ template <class L> GPR_D int axis_swap(int k, int d) {
 }
 
 // D_OSH / D_ROE along direction d (fluxes.cpp:22-64) through the x form.
-template <class L>
-GPR_D void eig_dissipation_d(const double *ql, const double *qr, int d, int flux,
-                             const DevPar &P, const Consts &C, double *f) {
+template <class L, int NQ>
+GPR_D void eig_dissipation_qd(const double *ql, const double *qr, int d, int flux,
+                              const DevPar &P, const double *nodes, const double *wts,
+                              double *f) {
   constexpr int V = L::V;
   if (d == 0) {
-    eig_dissipation<L>(ql, qr, flux, P, C, f);
+    eig_dissipation_q<L, NQ>(ql, qr, flux, P, nodes, wts, f);
     return;
   }
   double pl[V], pr[V], pf[V];
@@ -792,10 +800,15 @@ GPR_D void eig_dissipation_d(const double *ql, const double *qr, int d, int flux
     pl[k] = ql[axis_swap<L>(k, d)];
     pr[k] = qr[axis_swap<L>(k, d)];
   }
-  eig_dissipation<L>(pl, pr, flux, P, C, pf);
+  eig_dissipation_q<L, NQ>(pl, pr, flux, P, nodes, wts, pf);
 #pragma unroll
   for (int k = 0; k < V; k++)
     f[k] = pf[axis_swap<L>(k, d)];
+}
+template <class L>
+GPR_D void eig_dissipation_d(const double *ql, const double *qr, int d, int flux,
+                             const DevPar &P, const Consts &C, double *f) {
+  eig_dissipation_qd<L, NN>(ql, qr, d, flux, P, C.nodes, C.w, f);
 }
 
 // Interface terms for flux 1 / 2 along d: f = D + F(qL) + F(qR) and the path

@@ -3,7 +3,8 @@ N, code/cpp/src/options.h:15): N = 3 is its third-order scheme.
 
 The reference builds one N per compiled module; here the N = 2 entry points
 live in the package root (`phd_gb300.solvers` ...), and `for_order(N)`
-returns the same GPRpy names for N (1D and 2D grids, Rusanov flux):
+returns the same GPRpy names for N (1D and 2D grids; Rusanov, Roe and Osher
+fluxes; the stiff Newton pass):
 
     G3 = phd_gb300.order.for_order(3)
     G3.boundaries(u, ub, nX, bcs)

@@ -160,8 +160,8 @@ def test_order_arguments_are_checked(G3):
     u0, MP, tf, dX, bcs = problems.shock_tube(nx=16)
     u = T(u0).view(-1)
     ub = torch.zeros((16 + 6) * 17, dtype=torch.float64, device=DEV)
-    with pytest.raises(RuntimeError):  # Osher is not compiled for N = 3
-        G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, False, 2, MP, None)
+    with pytest.raises(RuntimeError):  # unknown flux code
+        G3.solvers.ader_stepper(u, ub, [16], 1e-3, dX, False, 5, MP, None)
     with pytest.raises(RuntimeError):  # unknown boundary code
         G3.boundaries(u, ub, [16], [0, 9])
 
@@ -220,6 +220,58 @@ def test_n3_stiff_predictor_against_oracle(G3, case):
     ud = T(u).view(-1)
     G3.solvers.ader_stepper(ud, T(ub), nX, dt, dX, stiff, 0, MP, None)
     assert rel_err(H(ud), ref_u) < 1e-9, rel_err(H(ud), ref_u)
+
+
+@pytest.mark.parametrize("flux", [1, 2])
+@pytest.mark.parametrize("dim", [1, 2])
+def test_n3_roe_osher_against_oracle(G3, dim, flux):
+    """Roe (1) and Osher (2) at N = 3: the eigen dissipation at every face
+    point with the scheme's three path nodes (Osher: three 17 x 17
+    eigen-decompositions per point, Roe: one of the path-averaged matrix),
+    x and y faces in 2D; the FV update from the oracle's predictor within
+    1e-12 of the oracle's; one ADER step within 1e-10 in 1D and, in 2D,
+    within 10x the oracle's own response to 1e-16 relative noise on its input
+    (the central WENO stencil's conditioning on the vortex's near-constant
+    fields, as for the Rusanov step)."""
+    from phd_gb300 import problems
+    O = Oracle(N=3)
+    if dim == 1:
+        u0, MP, tf, dX, bcs = problems.shock_tube(nx=64)
+        nX, bc = np.array([64], np.int32), [0, 0]
+        u, _, _ = O.run(u0, MP, 1e9, dX, 0, cfl=0.8, max_steps=20)
+    else:
+        # mu = 1: Picard converges in every cell (the stiff pass is tested
+        # above)
+        u0, MP, tf, dX, bcs = problems.taylor_green(n=12, ny=10, cs=10.0, mu=1.0)
+        nX, bc = np.array([12, 10], np.int32), [1] * 4
+        u, _, _ = O.run(u0, MP, 1e9, dX, 1, cfl=0.4, max_steps=2)
+    dt = O.timestep(u, dX, 0.4, 0.0, 1e9, 10, MP)
+    ub = O.boundaries(u, nX, bc)
+    wh = O.weno_launcher(ub, nX)
+    qh, st = O.predictor(wh, dt, dX, nX, MP)
+    assert (st > 0).all()
+    ref = u.ravel().copy()
+    O.fv_launcher(ref, qh, nX, dt, dX, MP, flux=flux)
+    assert np.isfinite(ref).all()
+    ud = T(u).view(-1)
+    G3.solvers.fv.fv_launcher(ud, T(qh), nX, dt, dX, True, True, flux, MP, None)
+    assert rel_err(H(ud), ref) < 1e-12, rel_err(H(ud), ref)
+    ref_u = u.ravel().copy()
+    O.ader_stepper(ref_u, ub, nX, dt, dX, MP, flux=flux)
+    bar = 1e-10
+    if dim == 2:
+        rng = np.random.default_rng(3)
+        resp = 0.0
+        for _ in range(2):
+            up = u * (1 + 1e-16 * rng.standard_normal(u.shape))
+            r2 = up.ravel().copy()
+            O.ader_stepper(r2, O.boundaries(up, nX, bc), nX, dt, dX, MP, flux=flux)
+            resp = max(resp, rel_err(r2, ref_u))
+        assert resp < 1e-6, resp
+        bar = max(bar, 10 * resp)
+    ud = T(u).view(-1)
+    G3.solvers.ader_stepper(ud, T(ub), nX, dt, dX, False, flux, MP, None)
+    assert rel_err(H(ud), ref_u) < bar, (rel_err(H(ud), ref_u), bar)
 
 
 def test_n3_2d_stages_against_golden(G3):
