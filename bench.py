@@ -649,6 +649,10 @@ def run_gb300(args):
             third = tgv_n3_bench(torch, cpu=not args.no_cpu_baseline)
         except Exception as ex:  # reported, not fatal to the main line
             third = {"error": str(ex)}
+        try:
+            third["roe_osher"] = tgv_n3_flux_bench(torch, cpu=not args.no_cpu_baseline)
+        except Exception as ex:
+            third["roe_osher"] = {"error": str(ex)}
     bubble = None
     if rank == 0 and not args.no_shock_bubble:
         try:
@@ -1009,6 +1013,79 @@ def tgv_n3_bench(torch, n=512, steps=10, warmup=8, cfl=0.4, cpu=True, profile_st
                              "sample": "one step of the full %dx%d grid at N = 3, "
                                        "oracle/gpr_oracle.c" % (n, n)}
     return r
+
+
+def tgv_n3_flux_bench(torch, n=256, steps=2, warmup=1, cfl=0.4, cpu=True):
+    """The Taylor-Green step at N = 3 with the Roe (1) and Osher (2)
+    dissipation through gpr_iterate_n (the eigen dissipation at each of the
+    9 points of a face with three path nodes), 256 x 256 (a 512 x 512 step
+    takes seconds); one GPU step and one N = 3 oracle step from the state the
+    timed steps left."""
+    import phd_gb300 as G
+    from phd_gb300 import _lib
+    lib = _lib.load()
+    u0, MP, tf, dX, bcs = G.problems.taylor_green(n=n, cs=10.0, mu=1e-2)
+    V, N = 17, 3
+    nX = np.array([n, n], np.int32)
+    pn = nX.ctypes.data_as(ctypes.c_void_p)
+    dXa = np.array(dX, np.float64)
+    bc = np.array([1, 1, 1, 1], np.int32)
+    cp = MP.to_ctypes()
+    scr = torch.empty(lib.gpr_iterate_scratch_doubles_n(pn, 2, V, N), dtype=torch.float64,
+                      device="cuda")
+    status = torch.zeros((n + 2) ** 2, dtype=torch.int32, device="cuda")
+    out = {"workload": "tgv2d_%dx%d_v17_cfl%.2g_N3" % (n, n, cfl)}
+    for flux, name in ((1, "roe"), (2, "osher")):
+        u = torch.tensor(u0.reshape(-1), dtype=torch.float64, device="cuda")
+        clk = torch.tensor([0.0, 0.0, 1e9, cfl, 0.0], dtype=torch.float64, device="cuda")
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def run(k):
+            _lib.check(lib.gpr_iterate_n(
+                ctypes.c_void_p(u.data_ptr()), pn, 2, dXa.ctypes.data_as(ctypes.c_void_p),
+                bc.ctypes.data_as(ctypes.c_void_p), flux,
+                ctypes.cast(ctypes.pointer(cp), ctypes.c_void_p), None,
+                ctypes.c_void_p(clk.data_ptr()), k, ctypes.c_void_p(scr.data_ptr()),
+                ctypes.c_void_p(status.data_ptr()), CONTORTED_TOL, V, N, sp), "iterate_n")
+        run(warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        kind = status.cpu().numpy() & 0xff
+        r = {"steps": steps, "ms_per_step": ms / steps,
+             "value": n * n * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
+             "finite": bool(torch.isfinite(u).all().item()),
+             "newton_cells": int((kind == 1).sum())}
+        if cpu:
+            from oracle import Oracle
+            from phd_gb300.order import for_order
+            O = Oracle(N=N)
+            G3 = for_order(N)
+            u_np = u.detach().cpu().numpy().reshape(n, n, V).copy()
+            t0 = time.perf_counter()
+            dt = O.timestep(u_np, dX, cfl, 0.0, 1e9, 10, MP)
+            ub = O.boundaries(u_np, nX, [1] * 4)
+            ref = u_np.reshape(-1).copy()
+            O.ader_stepper(ref, ub, nX, dt, dX, MP, flux=flux)
+            O.renorm_distortion(ref, MP)
+            cpu_s = time.perf_counter() - t0
+            ud = u.detach().clone()
+            ubt = torch.empty(ub.size, dtype=torch.float64, device="cuda")
+            G3.boundaries(ud, ubt, nX, [1] * 4)
+            G3.solvers.ader_stepper(ud, ubt, nX, dt, dX, False, flux, MP, None)
+            G.solvers.renorm_distortion(ud, [MP])
+            got = ud.cpu().numpy()
+            r["max_rel_diff_vs_oracle"] = float(np.max(np.abs(got - ref) / (1.0 + np.abs(ref))))
+            r["cpu_baseline"] = {"value": n * n / cpu_s / 1e6, "unit": UNIT,
+                                 "cores": O.num_threads(), "kind": "port",
+                                 "sample": "one step of the full %dx%d grid at N = 3, "
+                                           "oracle/gpr_oracle.c" % (n, n)}
+        out[name] = r
+    return out
 
 
 def shock_bubble_bench(torch, steps=10, warmup=3, nx=800, cpu_steps=2):
